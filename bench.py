@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Benchmark: design iterations/s of the voxel-SIMP inner loop on one GB300.
+
+Workload (the large single-GPU configuration): a 256x128x128 hex8 cantilever
+(4,194,304 elements, 12,830,211 DOFs), E0 = 1, nu = 0.3, p = 3, rho_min = 1e-3
+(the reference's material law), filter radius 1.5, volume fraction 0.3, move 0.2,
+MG-PCG to a relative residual of 1e-8 on the FP64 residual.  The x = 0 face is
+clamped; a unit -z load sits at a seeded uniform point (numpy default_rng(0)) of
+the x = nx end face, spread bilinearly to its four nodes.  Synthetic, seeded.
+
+A step is one design iteration on a resident job (filter, penalised solve,
+sensitivities, OC update with its bisection), timed with CUDA events on the job's
+stream; `value` is the mixed-precision form (FP32 V-cycle inside FP64 iterative
+refinement), the plain FP64 form is reported beside it.  `e2e` runs the public
+host API (tg_simp_optimize with host buffers: problem upload, the optimisation,
+the design read-back) for K iterations.  Inputs are larger than L2 (the fine
+vectors alone are 100 MB each), so no L2 flush is needed.
+
+--impl reference times the CPU implementation of the same step on the host
+cores: the oracle's C restatement of the reference (the reference tree itself is
+not present on the GPU host), measured on a bounded sample and scaled.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(nx=256, ny=128, nz=128)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cantilever_random_load(nx, ny, nz, seed=0):
+    """Clamped x = 0 face; unit -z load at a seeded point of the x = nx face."""
+    rng = np.random.default_rng(seed)
+    yy, zz = rng.uniform(0.0, ny), rng.uniform(0.0, nz)
+    b0, c0 = min(int(yy), ny - 1), min(int(zz), nz - 1)
+    ty, tz = yy - b0, zz - c0
+
+    def node(a, b, c):
+        return (c * (ny + 1) + b) * (nx + 1) + a
+
+    bcs = [(node(0, b, c), k, 0.0) for c in range(nz + 1) for b in range(ny + 1) for k in range(3)]
+    loads = []
+    for db, wb in ((0, 1.0 - ty), (1, ty)):
+        for dc, wc in ((0, 1.0 - tz), (1, tz)):
+            if wb * wc > 0.0:
+                loads.append((node(nx, b0 + db, c0 + dc), 2, -1.0 * wb * wc))
+    return bcs, loads
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_sample(nx, ny, nz, applies_per_iter, budget_s=25.0):
+    """Time the oracle's C restatement on a bounded sample of one design
+    iteration: one fine-operator apply, the sensitivity sweep and one OC update
+    (filter + bisection) on the full grid; scale the apply by the number of fine
+    applies one iteration needs (as counted by the FP64 GPU run).  Coarse-level
+    multigrid work is not charged to the CPU (in its favour)."""
+    from oracle.oracle import OracleLib, Problem
+    port = OracleLib("port")
+    bcs, loads = cantilever_random_load(nx, ny, nz)
+    pb = Problem(nx, ny, nz, 1.0, None, bcs, loads)
+    rng = np.random.default_rng(1)
+    rho = rng.random(pb.nv) * 0.9 + 0.05
+    E = rho ** 3
+    u = rng.standard_normal(pb.ndof)
+    t0 = time.perf_counter()
+    port.apply(pb, u, E)
+    t_apply = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    port.sensitivity(pb, rho, u)
+    t_sens = time.perf_counter() - t0
+    t_oc = 0.0
+    if t_apply + t_sens < budget_s:
+        dc = -rng.random(pb.nv)
+        t0 = time.perf_counter()
+        port.oc_update(pb, rho, dc, 0.3)
+        t_oc = time.perf_counter() - t0
+    t_iter = applies_per_iter * t_apply + t_sens + t_oc
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return dict(value=1.0 / t_iter, unit="design_iters/s", cores=port_threads(),
+                kind="port",
+                sample=(f"oracle C restatement on {nx}x{ny}x{nz}: 1 fine apply "
+                        f"({t_apply:.2f}s) x {applies_per_iter:.0f} applies/iteration + "
+                        f"sensitivities ({t_sens:.2f}s) + 1 OC update ({t_oc:.2f}s); "
+                        f"{threads} host threads available"),
+                t_apply_s=t_apply, t_sens_s=t_sens, t_oc_s=t_oc)
+
+
+def port_threads():
+    from oracle.oracle import OracleLib
+    try:
+        return int(OracleLib("port").threads())
+    except Exception:
+        return 1
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return
+    nx, ny, nz = args.nx, args.ny, args.nz
+    applies = args.ref_applies
+    vals = []
+    for _ in range(max(1, args.steps if args.steps <= 3 else 1)):
+        s = cpu_sample(nx, ny, nz, applies)
+        vals.append(s["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "design_iters_per_s", "value": v,
+            "unit": "design_iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(args),
+            "cpu_baseline": {"value": v, "unit": "design_iters/s", "cores": s["cores"],
+                             "kind": s["kind"], "sample": s["sample"]},
+            "e2e": {"value": v, "unit": "design_iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": f"cantilever {args.nx}x{args.ny}x{args.nz} hex8 SIMP, seeded end-face load",
+            "elements": args.nx * args.ny * args.nz,
+            "dofs": 3 * (args.nx + 1) * (args.ny + 1) * (args.nz + 1),
+            "volfrac": 0.3, "rmin": 1.5, "move": 0.2, "penal": 3, "cg_tol": 1e-8,
+            "solver": "MG-PCG (Galerkin, damped Jacobi 1+1, dense Cholesky coarsest)",
+            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+# ----------------------------------------------------------------- our arm
+def run_ours(args, world, rank, local, pg):
+    import topopt_gb300 as tg
+    from topopt_gb300.build import build
+    build()
+    tg.lib().tg_set_device(local)
+    nx, ny, nz = args.nx, args.ny, args.nz
+    bcs, loads = cantilever_random_load(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, bcs, loads)
+    params = tg.SimpParams()
+
+    def opts(prec, K):
+        return tg.SimpOptions(volume_fraction=0.3, filter_radius=1.5, move=0.2, change_tol=0.0,
+                              cg_tolerance=1e-8, max_iterations=K,
+                              solve=tg.SolveOptions(precision=prec, mg_levels=args.mg_levels))
+
+    fp64_peak, fp32_peak = tg.device_fma_peaks()
+    forms = {}
+    order = ["mixed", "fp64"] if not args.skip_fp64 else ["mixed"]
+    for form in order:
+        prec = tg.PREC_MIXED if form == "mixed" else tg.PREC_FP64
+        job = tg.SimpJob(pb, params, opts(prec, args.warmup + args.steps + 1))
+        for _ in range(args.warmup):
+            job.step()
+        barrier(pg)
+        launches0 = tg.kernel_launches()
+        rows = []
+        with ClockSampler(local) as cs:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                rows.append(job.step())
+            wall = time.perf_counter() - t0
+        launches = tg.kernel_launches() - launches0
+        dev_s = sum(r["t_device_ms"] for r in rows) / 1e3
+        dev_s = max_over_ranks(pg, dev_s)
+        forms[form] = dict(
+            design_iters_per_s=sum_over_ranks(pg, args.steps) / dev_s,
+            ms_per_step=1e3 * dev_s / args.steps, wall_s=wall, launches=launches,
+            clocks=cs.summary(),
+            solve_ms=statistics.median(r["t_solve_ms"] for r in rows),
+            cg_iterations=[r["cg_iterations"] for r in rows],
+            fine_matvecs_fp64=statistics.median(r["fine_matvecs"] for r in rows),
+            fine_matvecs_fp32=statistics.median(r["fine_matvecs_lowp"] for r in rows),
+            oc_volume_evals=statistics.median(r["oc_volume_evals"] for r in rows),
+            compliance=[r["compliance"] for r in rows],
+            device_gb=job.device_bytes / 1e9)
+        # Dominant-kernel timing (CUDA events, job stream).
+        forms[form]["op_fp64_ms"] = job.time_operator(tg.PREC_FP64, 5)
+        if form == "mixed":
+            forms[form]["op_fp32_ms"] = job.time_operator(tg.PREC_MIXED, 20)
+            design, _ = job.read()
+        job.close()
+    # Mixed vs FP64 accuracy on the same design (compliance and displacement).
+    acc = {}
+    if not args.skip_fp64:
+        r64 = tg.simp_compliance(pb, params, _phys_of(tg, pb, design), tolerance=1e-8,
+                                 options=tg.SolveOptions(precision=tg.PREC_FP64))
+        r32 = tg.simp_compliance(pb, params, _phys_of(tg, pb, design), tolerance=1e-8,
+                                 options=tg.SolveOptions(precision=tg.PREC_MIXED))
+        acc = {"compliance_rel_err": abs(r32["compliance"] - r64["compliance"]) / abs(r64["compliance"]),
+               "u_rel_maxnorm_err": float(np.abs(r32["u"] - r64["u"]).max() / np.abs(r64["u"]).max()),
+               "solve_ms_fp64": r64["cg"].t_solve_ms, "solve_ms_mixed": r32["cg"].t_solve_ms,
+               "cg_iters_fp64": r64["cg"].iterations, "cg_iters_mixed_inner": r32["cg"].iterations,
+               "refinements_mixed": r32["cg"].refinements}
+    # End to end through the public host API.
+    K = args.steps
+    o = opts(tg.PREC_MIXED, K)
+    barrier(pg)
+    t0 = time.perf_counter()
+    res = tg.simp_optimize(pb, params, o)
+    e2e_wall = max_over_ranks(pg, time.perf_counter() - t0)
+    nv, ndof = pb.nv, pb.ndof
+    h2d = (len(bcs) + len(loads)) * 16 + 64
+    d2h = 2 * nv * 8
+    hbm, src = peaks()
+    m = forms["mixed"]
+    op_bytes32 = 2 * ndof * 4 + nv * 4
+    achieved = op_bytes32 / (m["op_fp32_ms"] * 1e-3) / 1e9
+    fp64_alg_flops = 1152 * nv
+    line = {
+        "metric": "design_iters_per_s", "value": m["design_iters_per_s"], "unit": "design_iters/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded cantilever)", "config": workload_config(args),
+        "clocks": m["clocks"], "gpu_launches": int(m["launches"]),
+        "e2e": {"value": sum_over_ranks(pg, K) / e2e_wall, "unit": "design_iters/s",
+                "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+                "includes": "problem upload + job setup + K iterations + certification solve + read-back"},
+        "roofline": {"bound": "hbm", "kernel": "fine operator apply, FP32 (mixed V-cycle)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "bytes_per_launch": op_bytes32, "traffic": None,
+                     "ms_per_launch": m["op_fp32_ms"]},
+        "fp64_operator": {"ms_per_launch": m["op_fp64_ms"],
+                          "reference_flops_per_launch": fp64_alg_flops,
+                          "reference_equiv_tflops": fp64_alg_flops / (m["op_fp64_ms"] * 1e-3) / 1e12,
+                          "executed_fp64_ops_per_element": 212,
+                          "executed_tflops": 212 * nv / (m["op_fp64_ms"] * 1e-3) / 1e12,
+                          "fp64_fma_peak_tflops": fp64_peak, "fp32_fma_peak_tflops": fp32_peak},
+        "forms": forms, "mixed_vs_fp64": acc,
+    }
+    if rank == 0 and not args.no_cpu:
+        applies = forms.get("fp64", m)["fine_matvecs_fp64"] or 60
+        cb = cpu_sample(nx, ny, nz, applies)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def _phys_of(tg, pb, design):
+    return tg.make_density_filter(pb, 1.5).filter_density(design)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=WORKLOAD["nx"])
+    ap.add_argument("--ny", type=int, default=WORKLOAD["ny"])
+    ap.add_argument("--nz", type=int, default=WORKLOAD["nz"])
+    ap.add_argument("--mg-levels", type=int, default=7)
+    ap.add_argument("--ref-applies", type=float, default=60.0)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

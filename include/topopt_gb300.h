@@ -1,0 +1,237 @@
+/*
+ * topopt_gb300.h -- C ABI of the GB300-native voxel-SIMP inner loop.
+ *
+ * A drop-in for the reference's optimizer/solver entry points (Anarkissed/TopOpt,
+ * core/).  Every entry point takes caller-owned HOST buffers and sizes, copies
+ * them to the device, runs hand-written sm_103a kernels and copies results back;
+ * nothing throws across the ABI.  The resident-job API (tg_job_*) keeps a design's
+ * density, displacement and multigrid hierarchy on the device across design
+ * iterations.
+ *
+ * Conventions are the reference's (core/include/topopt/fea.hpp:18-29, :140-171):
+ *   voxel (i,j,k) -> (k*ny + j)*nx + i; node (a,b,c) -> (c*(ny+1) + b)*(nx+1) + a;
+ *   DOF = 3*node + component; Hex8 nodes bottom face CCW then top face CCW.
+ *
+ * Errors: every function returns a tg_status; tg_last_error() returns the
+ * calling thread's message for the last failure.  The codes map the reference's
+ * exception classes (fea.hpp:418-469, matfree.cpp:782-814):
+ *   TG_EINVAL      std::invalid_argument   (sizes, indices, E <= 0, nu range)
+ *   TG_ESINGULAR   std::runtime_error      (void-only system, load on a void DOF)
+ *   TG_ENONCONV    SolverNonConvergence    (tg_cg_info carries iterations/residual)
+ *   TG_EDEADLINE   SolverDeadlineExceeded
+ *   TG_EDEVICE     a CUDA error (the message names the call)
+ *   TG_ECANCELLED  the caller's cancel flag was observed
+ *
+ * Threading: every entry point is re-entrant; a tg_job is driven by one thread
+ * at a time and owns one CUDA stream.
+ */
+#ifndef TOPOPT_GB300_H
+#define TOPOPT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TG_OK = 0,
+  TG_EINVAL = 1,
+  TG_ESINGULAR = 2,
+  TG_ENONCONV = 3,
+  TG_EDEADLINE = 4,
+  TG_EDEVICE = 5,
+  TG_ENOMEM = 6,
+  TG_ECANCELLED = 7
+} tg_status;
+
+/* VoxelGrid (core/include/topopt/voxel.hpp:56-92).  `tags` holds one VoxelTag
+ * byte per voxel (0 = Empty, anything else solid); NULL means every voxel is
+ * Interior. */
+typedef struct {
+  int32_t nx, ny, nz;
+  double spacing;
+  const uint8_t* tags;
+} tg_grid;
+
+/* DirichletBC / NodalLoad (core/include/topopt/fea.hpp:173-187). */
+typedef struct {
+  int32_t node, component;
+  double value;
+} tg_dirichlet_bc;
+typedef struct {
+  int32_t node, component;
+  double value;
+} tg_nodal_load;
+
+/* SimpParams (core/include/topopt/simp.hpp:36-40).  material_law 0 is the
+ * reference law E = clamp(rho, rho_min, 1)^p * E0 (simp.cpp:44-47, :656);
+ * 1 is the modified law E = Emin + rho^p (E0 - Emin) with Emin = e_min. */
+typedef struct {
+  double youngs_modulus, poisson, penalty, density_min;
+  int32_t material_law;
+  double e_min;
+} tg_simp_params;
+
+typedef enum { TG_SOLVER_MGCG = 0, TG_SOLVER_JACOBI_CG = 1 } tg_solver_kind;
+typedef enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 } tg_precision;
+
+/* Solver knobs.  Zero-initialised means: MG-PCG, FP64, the deepest hierarchy the
+ * grid allows, the reference's iteration budget of 300 MG cycles before the
+ * Jacobi-PCG fallback (multigrid.cpp:122), damped Jacobi w = 0.6 with 1+1 sweeps
+ * (multigrid.cpp:72-76). */
+typedef struct {
+  int32_t solver;          /* tg_solver_kind */
+  int32_t precision;       /* tg_precision */
+  int32_t mg_levels;       /* 0 = deepest (coarsest axis >= 2 elements) */
+  int32_t mg_iter_budget;  /* 0 = 300 */
+  double omega;            /* 0 = 0.6 */
+  double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve, 0 = 1e-3 */
+  int32_t max_refinements; /* mixed: outer FP64 refinement steps, 0 = 20 */
+  int32_t reserved;
+} tg_solve_options;
+
+/* CgInfo subset (core/include/topopt/fea.hpp:272-382). */
+typedef struct {
+  int32_t converged, iterations;
+  double residual;
+  int32_t used_multigrid, mg_levels, hier_built, mg_cycles_attempted;
+  int64_t matvecs;        /* fine FP64 operator applies */
+  int64_t matvecs_lowp;   /* fine reduced-precision operator applies */
+  int32_t refinements;    /* mixed: outer FP64 refinement steps */
+  int32_t ng;             /* surviving (kept) DOFs */
+  double t_build_ms, t_mg_build_ms, t_solve_ms, t_total_ms;
+} tg_cg_info;
+
+/* The OC subset of SimpOptions (core/include/topopt/simp.hpp:1028-1138). */
+typedef struct {
+  double volume_fraction, filter_radius, move, change_tol, cg_tolerance;
+  int32_t max_iterations, cg_max_iterations;
+  tg_solve_options solve;
+} tg_simp_options;
+
+/* One row of the per-iteration record (SimpIteration + the observation fields
+ * of simp.hpp:913-960 that the iterations.csv schema carries). */
+typedef struct {
+  int32_t iteration;
+  double compliance, change, volume_fraction;
+  int32_t cg_iterations, mg_levels, used_multigrid, oc_volume_evals;
+  double t_filter_ms, t_solve_ms, t_sensitivity_ms, t_update_ms, t_total_ms;
+  double t_device_ms; /* CUDA-event time of the iteration on the job's stream */
+  int64_t fine_matvecs, fine_matvecs_lowp;
+} tg_simp_iteration;
+
+typedef struct {
+  int32_t iterations, converged, cancelled, infeasible, non_convergent;
+  double compliance, initial_compliance, volume_fraction;
+} tg_simp_result;
+
+/* Progress hook (TopOptBridge.hpp:262-263): called on the optimizing thread
+ * after every design iteration. */
+typedef void (*tg_progress_fn)(void* ctx, int32_t iteration, double compliance, double change);
+
+const char* tg_last_error(void);
+/* Device ordinal the library uses (set before the first call; default 0). */
+int tg_set_device(int32_t device);
+/* Library and kernel build identification. */
+const char* tg_version(void);
+
+/* hex8_stiffness (core/src/fea/hex_element.cpp:93-115): 24x24 row-major Ke. */
+int tg_hex8_stiffness(double youngs_modulus, double poisson, double element_size,
+                      double* ke576);
+
+/* fea_matfree_apply (core/include/topopt/fea.hpp:760-766; matfree.cpp:1079-1098):
+ * y = K u over the full grid.  youngs_per_voxel NULL -> uniform youngs_modulus.
+ * precision TG_PREC_MIXED runs the FP32 operator (inputs rounded to float). */
+int tg_matfree_apply(const tg_grid* grid, double youngs_modulus, double poisson,
+                     const double* youngs_per_voxel, int32_t precision, const double* u,
+                     double* y);
+
+/* mf_build_reduced's void-DOF gate (core/src/fea/matfree.cpp:670-834): kept[d] = 1
+ * for surviving DOFs, rhs = f - K u_p on them, invdiag the Jacobi inverse
+ * diagonal; all ndof long.  Returns TG_ESINGULAR on the reference's rejections. */
+int tg_build_reduced(const tg_grid* grid, const double* youngs_per_voxel, double poisson,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, uint8_t* kept, double* rhs, double* invdiag,
+                     int32_t* ng_out);
+
+/* fea_solve_mgcg_matfree (graded overload, core/include/topopt/fea.hpp:707-715;
+ * core/src/fea/multigrid.cpp:2098-2320): solves the reduced, void-gated system
+ * to ||b - A x|| <= tolerance ||b||, MG-PCG with a Jacobi-PCG fallback.
+ * active_mask (one byte per voxel, 0 removes the element) and initial_guess
+ * (ndof) may be NULL.  u_out receives the full ndof field. */
+int tg_solve(const tg_grid* grid, const double* youngs_per_voxel, double poisson,
+             const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+             int32_t nloads, double tolerance, int32_t max_iterations,
+             const tg_solve_options* options, const uint8_t* active_mask,
+             const double* initial_guess, double* u_out, tg_cg_info* info);
+
+/* simp_compliance (core/include/topopt/simp.hpp:247-255; simp.cpp:567-828):
+ * the penalised solve, c = sum E(rho_e) q_e and dc/drho.  u_out (ndof) and
+ * dc_out (voxels) may be NULL. */
+int tg_simp_compliance(const tg_grid* grid, const tg_simp_params* params,
+                       const double* density, const tg_dirichlet_bc* bcs, int32_t nbc,
+                       const tg_nodal_load* loads, int32_t nloads, double tolerance,
+                       int32_t max_iterations, const tg_solve_options* options,
+                       double* u_out, double* dc_out, double* compliance_out,
+                       tg_cg_info* info);
+
+/* DensityFilter::filter_density / filter_sensitivity over the solid voxels
+ * (core/src/simp/simp.cpp:834-942); radius in voxel units.  adjoint 0 = forward. */
+int tg_filter(const tg_grid* grid, double radius, int32_t adjoint, const double* x,
+              double* out);
+
+/* oc_update (core/include/topopt/simp.hpp:481-485; simp.cpp:948-1025): the OC
+ * step with the lambda bisection on the filtered volume.  Bit-identical to the
+ * reference for the same inputs. */
+int tg_oc_update(const tg_grid* grid, double radius, const double* density,
+                 const double* dcompliance, double volume_fraction, double move,
+                 double density_min, double* x_new);
+
+/* simp_optimize (core/include/topopt/simp.hpp:1783-1786; simp.cpp:2018-2592):
+ * the OC loop with no projection.  history (max_iterations rows), design_out and
+ * phys_out (voxels) may be NULL; cancel (may be NULL) is polled once per
+ * iteration, before the solve (simp.cpp:2161). */
+int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, const tg_simp_options* options, tg_progress_fn progress,
+                     void* progress_ctx, const volatile int32_t* cancel,
+                     tg_simp_iteration* history, double* design_out, double* phys_out,
+                     tg_simp_result* result);
+
+/* ---- resident jobs: state stays on the device between design iterations ---- */
+typedef struct tg_job tg_job;
+
+/* Set up a job (grid, filter, BC mask, hierarchy structure) and its uniform start
+ * design; no design iteration runs. */
+int tg_job_create(const tg_grid* grid, const tg_simp_params* params,
+                  const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                  int32_t nloads, const tg_simp_options* options, tg_job** job_out);
+/* One design iteration on the device: filter, solve, sensitivities, OC update. */
+int tg_job_step(tg_job* job, tg_simp_iteration* row);
+/* Copy the current design x and physical density filter(x) to the host. */
+int tg_job_read(tg_job* job, double* design_out, double* phys_out);
+/* Replace the design with a host field (voxels). */
+int tg_job_write_design(tg_job* job, const double* design);
+/* Bytes of device memory the job holds. */
+int64_t tg_job_device_bytes(const tg_job* job);
+/* Estimate, before creating it, the device bytes a job on this grid needs. */
+int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* options);
+void tg_job_destroy(tg_job* job);
+
+/* ---- measurement (no reference counterpart) ---- */
+/* Average device time of one fine-operator launch (y = A x on the job's current
+ * element factors), precision TG_PREC_FP64 or TG_PREC_MIXED (FP32), over `reps`
+ * back-to-back launches timed with CUDA events on the job's stream. */
+int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* avg_ms);
+/* Kernels this library has launched in the process so far. */
+int64_t tg_kernel_launches(void);
+/* FMA microbenchmark: sustained FP64 and FP32 FMA throughput of the device in
+ * TFLOP/s (2 flops per FMA), all SMs, register-resident operands. */
+int tg_device_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,335 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Two CPU implementations of the reference voxel-SIMP inner loop share one Python
+face here:
+
+* ``OracleLib("port")``  -- oracle/topopt_oracle.c, the C restatement, built by
+  ``build_port()`` into oracle/_build/ on any machine;
+* ``OracleLib("reference")`` -- the reference's own compiled C++ (built from the
+  reference tree by oracle/build_ref.sh into oracle/_ref/), present only where the
+  reference tree was available at build time.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module.  The product library never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libtopopt_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libtopopt_ref.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_bp = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+
+def build_port(force: bool = False) -> str:
+    """Compile the C restatement (gcc, -ffp-contract=off, no -march; OpenMP when
+    the compiler has it -- threading never changes a result)."""
+    src = os.path.join(HERE, "topopt_oracle.c")
+    hdr = os.path.join(HERE, "topopt_oracle.h")
+    os.makedirs(os.path.dirname(PORT_SO), exist_ok=True)
+    newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+    if force or not os.path.exists(PORT_SO) or newest > os.path.getmtime(PORT_SO):
+        base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-o",
+                PORT_SO + ".tmp", src, "-lm"]
+        try:
+            subprocess.check_call(base[:2] + ["-fopenmp"] + base[2:], stderr=subprocess.DEVNULL)
+        except subprocess.CalledProcessError:
+            subprocess.check_call(base)
+        os.replace(PORT_SO + ".tmp", PORT_SO)
+    return PORT_SO
+
+
+def build_reference() -> str | None:
+    """Compile the reference's own code (needs the reference tree); None if absent."""
+    script = os.path.join(HERE, "build_ref.sh")
+    subprocess.check_call(["bash", script])
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class Problem:
+    """A voxel problem in the reference's conventions (see topopt_oracle.h)."""
+
+    def __init__(self, nx, ny, nz, spacing=1.0, solid=None, bcs=(), loads=()):
+        self.nx, self.ny, self.nz, self.h = int(nx), int(ny), int(nz), float(spacing)
+        self.nv = self.nx * self.ny * self.nz
+        self.nnodes = (self.nx + 1) * (self.ny + 1) * (self.nz + 1)
+        self.ndof = 3 * self.nnodes
+        self.solid = None if solid is None else np.ascontiguousarray(solid, dtype=np.uint8).ravel()
+        bcs = list(bcs)
+        loads = list(loads)
+        self.bc_node = np.array([b[0] for b in bcs], dtype=np.int32)
+        self.bc_comp = np.array([b[1] for b in bcs], dtype=np.int32)
+        self.bc_val = np.array([b[2] for b in bcs], dtype=np.float64)
+        self.ld_node = np.array([l[0] for l in loads], dtype=np.int32)
+        self.ld_comp = np.array([l[1] for l in loads], dtype=np.int32)
+        self.ld_val = np.array([l[2] for l in loads], dtype=np.float64)
+
+    def node(self, a, b, c):
+        return (c * (self.ny + 1) + b) * (self.nx + 1) + a
+
+    def bc_args(self):
+        return (len(self.bc_node), self.bc_node, self.bc_comp, self.bc_val,
+                len(self.ld_node), self.ld_node, self.ld_comp, self.ld_val)
+
+
+class OracleLib:
+    def __init__(self, kind: str = "port"):
+        self.kind = kind
+        if kind == "port":
+            path = build_port()
+            self.lib = C.CDLL(path)
+            self._p = "or_"
+        elif kind == "reference":
+            if not os.path.exists(REF_SO):
+                raise FileNotFoundError(REF_SO)
+            self.lib = C.CDLL(REF_SO)
+            self._p = "ref_"
+        else:
+            raise ValueError(kind)
+        L, p = self.lib, self._p
+        getattr(L, p + "last_error").restype = C.c_char_p
+        L.__getattr__  # noqa: B018
+        self._fn = {}
+        sig = {
+            "hex8_stiffness": [C.c_double, C.c_double, C.c_double, _dp],
+            "apply": [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                      _dp, _dp],
+            "build_reduced": [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p, C.c_double,
+                                              C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip,
+                                              _ip, _dp, _bp, _dp, _dp, _dp, C.POINTER(C.c_int)],
+            "simp_compliance": [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double, C.c_double,
+                                                C.c_double, C.c_double, _dp, C.c_int, _ip, _ip,
+                                                _dp, C.c_int, _ip, _ip, _dp, C.c_double, C.c_int,
+                                                _dp, _dp, C.POINTER(C.c_double),
+                                                C.POINTER(C.c_int), C.POINTER(C.c_double)],
+        }
+        for name, args in sig.items():
+            f = getattr(L, p + name)
+            f.argtypes = args
+            f.restype = C.c_int
+            self._fn[name] = f
+        solve = getattr(L, p + ("solve_cg"))
+        solve.argtypes = [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p, C.c_double,
+                                          C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip,
+                                          _dp, C.c_double, C.c_int, C.c_void_p, _dp,
+                                          C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        solve.restype = C.c_int
+        self._fn["solve_cg"] = solve
+        if kind == "port":
+            L.or_filter_make.restype = C.c_void_p
+            L.or_filter_make.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_void_p, C.c_double]
+            L.or_filter_free.argtypes = [C.c_void_p]
+            L.or_filter_nnz.argtypes = [C.c_void_p]
+            L.or_filter_nnz.restype = C.c_size_t
+            for n in ("or_filter_weight_sum",):
+                getattr(L, n).argtypes = [C.c_void_p, _dp]
+            for n in ("or_filter_density", "or_filter_sensitivity"):
+                getattr(L, n).argtypes = [C.c_void_p, _dp, _dp]
+            L.or_oc_update.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_void_p, _dp, _dp,
+                                                       C.c_double, C.c_double, C.c_double, _dp,
+                                                       C.POINTER(C.c_double), C.POINTER(C.c_int)]
+            L.or_simp_optimize.argtypes = (
+                [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                 C.c_void_p, _dp, _dp, _dp, _ip, _dp, _dp, C.c_void_p])
+            L.or_sensitivity.argtypes = [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double,
+                                                         C.c_double, C.c_double, C.c_double, _dp,
+                                                         _dp, _dp, C.POINTER(C.c_double)]
+        else:
+            L.ref_filter.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_double, C.c_int, _dp, _dp,
+                                                     C.c_void_p]
+            L.ref_oc_update.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_double, _dp, _dp,
+                                                        C.c_double, C.c_double, C.c_double, _dp]
+            L.ref_set_threads.argtypes = [C.c_int]
+            L.ref_simp_optimize.argtypes = (
+                [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                 C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                 C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip])
+
+    # ---------------------------------------------------------------- helpers
+    def _check(self, st):
+        if st != 0:
+            msg = getattr(self.lib, self._p + "last_error")().decode()
+            raise OracleError(st, msg)
+
+    @staticmethod
+    def _ptr(a):
+        return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+    def threads(self):
+        if self.kind == "port":
+            self.lib.or_threads.restype = C.c_int
+            return self.lib.or_threads()
+        return 1
+
+    def set_threads(self, n):
+        if self.kind == "reference":
+            self.lib.ref_set_threads(int(n))
+
+    # ------------------------------------------------------------------- API
+    def hex8_stiffness(self, E=1.0, nu=0.3, h=1.0):
+        ke = np.zeros(576)
+        self._check(self._fn["hex8_stiffness"](E, nu, h, ke))
+        return ke.reshape(24, 24)
+
+    def apply(self, pb: Problem, u, factor=None, E=1.0, nu=0.3):
+        y = np.zeros(pb.ndof)
+        f = None if factor is None else np.ascontiguousarray(factor, dtype=np.float64)
+        self._check(self._fn["apply"](pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(f),
+                                      E, nu, np.ascontiguousarray(u, dtype=np.float64), y))
+        return y
+
+    def build_reduced(self, pb: Problem, factor=None, E=1.0, nu=0.3):
+        kept = np.zeros(pb.ndof, np.uint8)
+        rhs, invd, up = np.zeros(pb.ndof), np.zeros(pb.ndof), np.zeros(pb.ndof)
+        ng = C.c_int(0)
+        f = None if factor is None else np.ascontiguousarray(factor, dtype=np.float64)
+        self._check(self._fn["build_reduced"](pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid),
+                                              self._ptr(f), E, nu, *pb.bc_args(), kept, rhs, invd,
+                                              up, C.byref(ng)))
+        return dict(kept=kept, rhs=rhs, invdiag=invd, up=up, ng=ng.value)
+
+    def solve_cg(self, pb: Problem, factor=None, E=1.0, nu=0.3, tol=1e-8, max_it=0, guess=None):
+        u = np.zeros(pb.ndof)
+        it, res = C.c_int(0), C.c_double(0)
+        f = None if factor is None else np.ascontiguousarray(factor, dtype=np.float64)
+        g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float64)
+        self._check(self._fn["solve_cg"](pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(f),
+                                         E, nu, *pb.bc_args(), tol, max_it, self._ptr(g), u,
+                                         C.byref(it), C.byref(res)))
+        return u, it.value, res.value
+
+    def simp_compliance(self, pb: Problem, density, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3,
+                        tol=1e-8, max_it=0):
+        u, dc = np.zeros(pb.ndof), np.zeros(pb.nv)
+        c, it, res = C.c_double(0), C.c_int(0), C.c_double(0)
+        self._check(self._fn["simp_compliance"](
+            pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+            np.ascontiguousarray(density, dtype=np.float64), *pb.bc_args(), tol, max_it, u, dc,
+            C.byref(c), C.byref(it), C.byref(res)))
+        return dict(u=u, dc=dc, compliance=c.value, iterations=it.value, residual=res.value)
+
+    def sensitivity(self, pb: Problem, density, u, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3):
+        assert self.kind == "port"
+        dc = np.zeros(pb.nv)
+        c = C.c_double(0)
+        self._check(self.lib.or_sensitivity(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu,
+                                            penal, rho_min,
+                                            np.ascontiguousarray(density, dtype=np.float64),
+                                            np.ascontiguousarray(u, dtype=np.float64), dc,
+                                            C.byref(c)))
+        return c.value, dc
+
+    def filter(self, pb: Problem, x, radius=1.5, adjoint=False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(pb.nv)
+        if self.kind == "port":
+            f = self.lib.or_filter_make(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), None, radius)
+            if not f:
+                self._check(1)
+            try:
+                (self.lib.or_filter_sensitivity if adjoint else self.lib.or_filter_density)(f, x, out)
+            finally:
+                self.lib.or_filter_free(f)
+        else:
+            self._check(self.lib.ref_filter(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), radius,
+                                            int(adjoint), x, out, None))
+        return out
+
+    def weight_sum(self, pb: Problem, radius=1.5):
+        hs = np.zeros(pb.nv)
+        if self.kind == "port":
+            f = self.lib.or_filter_make(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), None, radius)
+            self.lib.or_filter_weight_sum(f, hs)
+            self.lib.or_filter_free(f)
+        else:
+            tmp = np.zeros(pb.nv)
+            self._check(self.lib.ref_filter(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), radius, 0,
+                                            np.zeros(pb.nv), tmp, hs.ctypes.data_as(C.c_void_p)))
+        return hs
+
+    def oc_update(self, pb: Problem, density, dc, volfrac, radius=1.5, move=0.2, rho_min=1e-3):
+        xn = np.zeros(pb.nv)
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        g = np.ascontiguousarray(dc, dtype=np.float64)
+        if self.kind == "port":
+            f = self.lib.or_filter_make(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), None, radius)
+            lam, nvol = C.c_double(0), C.c_int(0)
+            try:
+                self._check(self.lib.or_oc_update(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), f, d, g,
+                                                  volfrac, move, rho_min, xn, C.byref(lam),
+                                                  C.byref(nvol)))
+            finally:
+                self.lib.or_filter_free(f)
+        else:
+            self._check(self.lib.ref_oc_update(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), radius, d,
+                                               g, volfrac, move, rho_min, xn))
+        return xn
+
+    def simp_optimize(self, pb: Problem, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3, volfrac=0.3,
+                      radius=1.5, move=0.2, max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0):
+        hc, hch, hvf = np.zeros(max_it), np.zeros(max_it), np.zeros(max_it)
+        design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+        if self.kind == "reference":
+            sc, ints = np.zeros(3), np.zeros(4, np.int32)
+            self._check(self.lib.ref_simp_optimize(
+                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                *pb.bc_args(), volfrac, radius, move, max_it, change_tol, cg_tol, cg_max_it, hc,
+                hch, hvf, design, phys, sc, ints))
+            n = int(ints[0])
+            return dict(compliance=sc[0], volume_fraction=sc[1], initial_compliance=sc[2],
+                        iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
+                        infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
+                        hist_vf=hvf[:n], design=design, phys=phys)
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it)
+        res = _OrSimpResult()
+        hcg = np.zeros(max_it, np.int32)
+        self._check(self.lib.or_simp_optimize(
+            pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min, *pb.bc_args(),
+            C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        n = res.iterations
+        return dict(compliance=res.compliance, volume_fraction=res.volume_fraction,
+                    initial_compliance=res.initial_compliance, iterations=n,
+                    converged=bool(res.converged), non_convergent=bool(res.non_convergent),
+                    infeasible=bool(res.infeasible), hist_c=hc[:n], hist_change=hch[:n],
+                    hist_vf=hvf[:n], hist_cg=hcg[:n], design=design, phys=phys)
+
+
+class _OrSimpOptions(C.Structure):
+    _fields_ = [("volume_fraction", C.c_double), ("filter_radius", C.c_double),
+                ("move", C.c_double), ("change_tol", C.c_double), ("cg_tolerance", C.c_double),
+                ("max_iterations", C.c_int), ("cg_max_iterations", C.c_int)]
+
+
+class _OrSimpResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("non_convergent", C.c_int),
+                ("infeasible", C.c_int), ("compliance", C.c_double),
+                ("volume_fraction", C.c_double), ("initial_compliance", C.c_double)]
+
+
+def cantilever(nx, ny, nz, total_load=-1.0, spacing=1.0, solid=None):
+    """Cantilever of the benchmark configs: every DOF of the x=0 face clamped, a
+    total z-load spread equally over the nodes of the x=nx edge at mid-height
+    (c = nz//2), all b."""
+    pb = Problem(nx, ny, nz, spacing, solid)
+    bcs = [(pb.node(0, b, c), comp, 0.0) for c in range(nz + 1) for b in range(ny + 1)
+           for comp in range(3)]
+    cmid = nz // 2
+    nodes = [pb.node(nx, b, cmid) for b in range(ny + 1)]
+    loads = [(n, 2, total_load / len(nodes)) for n in nodes]
+    return Problem(nx, ny, nz, spacing, solid, bcs, loads)

@@ -1,0 +1,259 @@
+// ref_capi.cpp -- flat extern "C" face over the reference's OWN compiled hot-path
+// code (core/src/fea/hex_element.cpp, matfree.cpp, core/src/simp/simp.cpp), so the
+// tests and the CPU baseline can call it through ctypes with the same argument
+// layout as oracle/topopt_oracle.h.
+//
+// TEST INFRASTRUCTURE ONLY: the reference build is a checker and the timed CPU
+// baseline; the product never links it.  Every entry point returns 0 on success,
+// 1 for std::invalid_argument, 2 for std::runtime_error (void-gate rejections),
+// 3 for SolverNonConvergence, 4 for anything else; ref_last_error() holds the
+// exception text.
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fea/fea_matfree.hpp"
+#include "topopt/fea.hpp"
+#include "topopt/simp.hpp"
+
+using namespace topopt;
+
+namespace {
+thread_local std::string g_err;
+
+VoxelGrid make_grid(int nx, int ny, int nz, double h, const uint8_t* solid) {
+  VoxelGrid g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.spacing = h;
+  const std::size_t nv = static_cast<std::size_t>(nx) * ny * nz;
+  g.tags.assign(nv, VoxelTag::Interior);
+  if (solid)
+    for (std::size_t e = 0; e < nv; ++e)
+      if (!solid[e]) g.tags[e] = VoxelTag::Empty;
+  return g;
+}
+
+std::vector<DirichletBC> make_bcs(int n, const int* node, const int* comp, const double* val) {
+  std::vector<DirichletBC> v(static_cast<std::size_t>(n));
+  for (int i = 0; i < n; ++i) v[i] = DirichletBC{node[i], comp[i], val[i]};
+  return v;
+}
+
+std::vector<NodalLoad> make_loads(int n, const int* node, const int* comp, const double* val) {
+  std::vector<NodalLoad> v(static_cast<std::size_t>(n));
+  for (int i = 0; i < n; ++i) v[i] = NodalLoad{node[i], comp[i], val[i]};
+  return v;
+}
+
+template <class F>
+int guarded(F&& fn) {
+  try {
+    fn();
+    g_err.clear();
+    return 0;
+  } catch (const SolverNonConvergence& e) {
+    g_err = e.what();
+    return 3;
+  } catch (const std::invalid_argument& e) {
+    g_err = e.what();
+    return 1;
+  } catch (const std::runtime_error& e) {
+    g_err = e.what();
+    return 2;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return 4;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error(void) { return g_err.c_str(); }
+
+int ref_set_threads(int n) { return fea_set_matfree_threads(n); }
+
+int ref_hex8_stiffness(double E, double nu, double h, double* ke) {
+  return guarded([&] {
+    const Hex8Stiffness K = hex8_stiffness(E, nu, h);
+    std::memcpy(ke, K.k.data(), sizeof(double) * 576);
+  });
+}
+
+int ref_apply(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
+              double E, double nu, const double* u, double* y) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, h, solid);
+    const std::size_t ndof = 3 * static_cast<std::size_t>(fea_node_count(g));
+    std::vector<double> uv(u, u + ndof), yv;
+    if (factor) {
+      std::vector<double> fv(factor, factor + g.voxel_count());
+      yv = fea_matfree_apply(g, fv, nu, uv);
+    } else {
+      yv = fea_matfree_apply(g, E, nu, uv);
+    }
+    std::memcpy(y, yv.data(), ndof * sizeof(double));
+  });
+}
+
+// Reduced-system build: kept mask, reduced rhs and Jacobi inverse diagonal
+// scattered to full-length arrays, prescribed field (matfree.cpp:670-834).
+int ref_build_reduced(int nx, int ny, int nz, double h, const uint8_t* solid,
+                      const double* factor, double E, double nu, int nbc, const int* bc_node,
+                      const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+                      const int* ld_comp, const double* ld_val, uint8_t* kept, double* rhs,
+                      double* invdiag, double* up, int* ng_out) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, h, solid);
+    std::vector<double> fv;
+    if (factor) fv.assign(factor, factor + g.voxel_count());
+    CgInfo info;
+    const fea_detail::MatfreeReduced m = fea_detail::mf_build_reduced(
+        g, E, nu, make_bcs(nbc, bc_node, bc_comp, bc_val),
+        make_loads(nload, ld_node, ld_comp, ld_val), factor ? &fv : nullptr, "ref_build_reduced",
+        &info);
+    const std::size_t ndof = static_cast<std::size_t>(m.ndof);
+    std::memset(kept, 0, ndof);
+    std::memset(rhs, 0, ndof * sizeof(double));
+    std::memset(invdiag, 0, ndof * sizeof(double));
+    for (int k = 0; k < m.ng; ++k) {
+      const int d = m.kept_global[static_cast<std::size_t>(k)];
+      kept[d] = 1;
+      rhs[d] = m.rg[static_cast<std::size_t>(k)];
+      invdiag[d] = m.invdiag[static_cast<std::size_t>(k)];
+    }
+    std::memcpy(up, m.up.data(), ndof * sizeof(double));
+    *ng_out = m.ng;
+  });
+}
+
+// The reference's exact matrix-free Jacobi-PCG (fea_solve_cg_matfree).
+int ref_solve_cg(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
+                 double E, double nu, int nbc, const int* bc_node, const int* bc_comp,
+                 const double* bc_val, int nload, const int* ld_node, const int* ld_comp,
+                 const double* ld_val, double tol, int max_it, const double* initial_guess,
+                 double* u, int* iters, double* resid) {
+  CgInfo info;
+  const int st = guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, h, solid);
+    const auto bcs = make_bcs(nbc, bc_node, bc_comp, bc_val);
+    const auto loads = make_loads(nload, ld_node, ld_comp, ld_val);
+    FeaSolution sol;
+    if (factor) {
+      std::vector<double> fv(factor, factor + g.voxel_count());
+      FeaSolution guess;
+      if (initial_guess)
+        guess.u.assign(initial_guess, initial_guess + 3 * static_cast<std::size_t>(fea_node_count(g)));
+      sol = fea_solve_cg_matfree(g, fv, nu, bcs, loads, tol, max_it, &info,
+                                 initial_guess ? &guess : nullptr, nullptr);
+    } else {
+      sol = fea_solve_cg_matfree(g, E, nu, bcs, loads, tol, max_it, &info);
+    }
+    std::memcpy(u, sol.u.data(), sol.u.size() * sizeof(double));
+  });
+  *iters = info.iterations;
+  *resid = info.residual;
+  return st;
+}
+
+// simp_compliance on the production solver kind; the oracle build routes its
+// multigrid solve to the exact Jacobi-PCG (ref_shim.cpp).
+int ref_simp_compliance(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                        double nu, double penal, double rho_min, const double* density, int nbc,
+                        const int* bc_node, const int* bc_comp, const double* bc_val, int nload,
+                        const int* ld_node, const int* ld_comp, const double* ld_val, double tol,
+                        int max_it, double* u, double* dc, double* compliance, int* iters,
+                        double* resid) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, h, solid);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    std::vector<double> rho(density, density + g.voxel_count());
+    const SimpCompliance c =
+        simp_compliance(g, p, rho, make_bcs(nbc, bc_node, bc_comp, bc_val),
+                        make_loads(nload, ld_node, ld_comp, ld_val), tol, max_it, nullptr,
+                        nullptr, SolverKind::MultigridCG_Matfree);
+    std::memcpy(u, c.solution.u.data(), c.solution.u.size() * sizeof(double));
+    std::memcpy(dc, c.dcompliance.data(), c.dcompliance.size() * sizeof(double));
+    *compliance = c.compliance;
+    *iters = c.cg.iterations;
+    *resid = c.cg.residual;
+  });
+}
+
+int ref_filter(int nx, int ny, int nz, const uint8_t* solid, double radius, int adjoint,
+               const double* x, double* out, double* weight_sum) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, 1.0, solid);
+    const DensityFilter f = make_density_filter(g, radius);
+    std::vector<double> xv(x, x + g.voxel_count());
+    const std::vector<double> o = adjoint ? f.filter_sensitivity(xv) : f.filter_density(xv);
+    std::memcpy(out, o.data(), o.size() * sizeof(double));
+    if (weight_sum) std::memcpy(weight_sum, f.weight_sum.data(), o.size() * sizeof(double));
+  });
+}
+
+int ref_oc_update(int nx, int ny, int nz, const uint8_t* solid, double radius,
+                  const double* density, const double* dc, double volfrac, double move,
+                  double rho_min, double* x_new) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, 1.0, solid);
+    const DensityFilter f = make_density_filter(g, radius);
+    std::vector<double> xv(density, density + g.voxel_count());
+    std::vector<double> dv(dc, dc + g.voxel_count());
+    const std::vector<double> o = oc_update(g, f, xv, dv, volfrac, move, rho_min);
+    std::memcpy(x_new, o.data(), o.size() * sizeof(double));
+  });
+}
+
+// simp_optimize with OC, no projection, SolverKind::MultigridCG_Matfree.
+int ref_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                      double nu, double penal, double rho_min, int nbc, const int* bc_node,
+                      const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+                      const int* ld_comp, const double* ld_val, double volfrac, double radius,
+                      double move, int max_it, double change_tol, double cg_tol, int cg_max_it,
+                      double* hist_c, double* hist_change, double* hist_vf, double* design,
+                      double* phys, double* out_scalars /* compliance, vf, init_c */,
+                      int* out_ints /* iterations, converged, non_convergent, infeasible */) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, h, solid);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    SimpOptions o;
+    o.volume_fraction = volfrac;
+    o.filter_radius = radius;
+    o.move = move;
+    o.max_iterations = max_it;
+    o.change_tol = change_tol;
+    o.cg_tolerance = cg_tol;
+    o.cg_max_iterations = cg_max_it;
+    o.solver = SolverKind::MultigridCG_Matfree;
+    const SimpOptimizeResult r = simp_optimize(g, p, make_bcs(nbc, bc_node, bc_comp, bc_val),
+                                               make_loads(nload, ld_node, ld_comp, ld_val), o);
+    for (std::size_t i = 0; i < r.history.size(); ++i) {
+      hist_c[i] = r.history[i].compliance;
+      hist_change[i] = r.history[i].change;
+      hist_vf[i] = r.history[i].volume_fraction;
+    }
+    std::memcpy(design, r.design.data(), r.design.size() * sizeof(double));
+    std::memcpy(phys, r.physical_density.data(), r.physical_density.size() * sizeof(double));
+    out_scalars[0] = r.compliance;
+    out_scalars[1] = r.volume_fraction;
+    out_scalars[2] = r.initial_compliance;
+    out_ints[0] = r.iterations;
+    out_ints[1] = r.converged ? 1 : 0;
+    out_ints[2] = r.non_convergent ? 1 : 0;
+    out_ints[3] = r.infeasible ? 1 : 0;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,796 @@
+/*
+ * topopt_oracle.c -- CPU restatement of the reference voxel-SIMP inner loop.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product).  See
+ * topopt_oracle.h for the conventions and the parity pin.  Build with
+ * -ffp-contract=off: every multiply/add below must stay a separate multiply and a
+ * separate add so the sums round exactly like the reference's
+ * (core/src/fea/matfree.cpp:66-73 uses explicit mul+add for this reason).
+ */
+#include "topopt_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static __thread char g_err[512];
+const char* or_last_error(void) { return g_err; }
+
+/* Host threads the OpenMP loops below use (1 without OpenMP).  Threading never
+ * changes a result: the element apply runs one colour at a time (no two
+ * elements of a colour share a node, fea_matfree_hpp:41-49) and the filter and
+ * OC candidate loops write one output each. */
+int or_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+static int fail(int code, const char* msg) {
+  snprintf(g_err, sizeof g_err, "%s", msg);
+  return code;
+}
+
+#define IDX(i, j, k) (((size_t)(k) * (size_t)ny + (size_t)(j)) * (size_t)nx + (size_t)(i))
+
+/* Hex8 corner natural coordinates, bottom face CCW then top face CCW
+ * (core/include/topopt/fea.hpp:18-21; hex_element.cpp:14-16). */
+static const double kXi[8] = {-1, +1, +1, -1, -1, +1, +1, -1};
+static const double kEta[8] = {-1, -1, +1, +1, -1, -1, +1, +1};
+static const double kZeta[8] = {-1, -1, -1, -1, +1, +1, +1, +1};
+/* Unit offsets (a,b,c) of the 8 corners: n0(0,0,0) n1(1,0,0) n2(1,1,0) n3(0,1,0)
+ * n4(0,0,1) n5(1,0,1) n6(1,1,1) n7(0,1,1). */
+static const int kCx[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+static const int kCy[8] = {0, 0, 1, 1, 0, 0, 1, 1};
+static const int kCz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+
+/* ---------------------------------------------------------------- element */
+/* Ke = sum over the 2x2x2 Gauss points of B^T D B detJ, unit weights; the
+ * isotropic D in Voigt [xx,yy,zz,gxy,gyz,gzx] with engineering shear
+ * (hex_element.cpp:23-89 integrator, :93-115 isotropic D). */
+int or_hex8_stiffness(double E, double nu, double h, double* ke) {
+  if (!(E > 0.0)) return fail(OR_EINVAL, "hex8_stiffness: youngs_modulus must be > 0");
+  if (!(h > 0.0)) return fail(OR_EINVAL, "hex8_stiffness: element_size must be > 0");
+  if (!(nu > -1.0 && nu < 0.5))
+    return fail(OR_EINVAL, "hex8_stiffness: poisson must be in (-1, 0.5)");
+  double D[6][6];
+  memset(D, 0, sizeof D);
+  const double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  D[0][0] = D[1][1] = D[2][2] = c * (1.0 - nu);
+  D[0][1] = D[0][2] = D[1][0] = D[1][2] = D[2][0] = D[2][1] = c * nu;
+  const double G = c * (1.0 - 2.0 * nu) / 2.0;
+  D[3][3] = D[4][4] = D[5][5] = G;
+
+  const double g = 1.0 / sqrt(3.0);
+  const double pts[2] = {-g, +g};
+  const double half = h / 2.0;
+  const double detJ = half * half * half;
+  const double s = 2.0 / h;
+  memset(ke, 0, sizeof(double) * 576);
+  for (int ig = 0; ig < 2; ++ig)
+    for (int jg = 0; jg < 2; ++jg)
+      for (int kg = 0; kg < 2; ++kg) {
+        const double xi = pts[ig], eta = pts[jg], zeta = pts[kg];
+        double dx[8], dy[8], dz[8];
+        for (int a = 0; a < 8; ++a) {
+          const double xa = kXi[a], ea = kEta[a], za = kZeta[a];
+          dx[a] = s * (0.125 * xa * (1.0 + eta * ea) * (1.0 + zeta * za));
+          dy[a] = s * (0.125 * ea * (1.0 + xi * xa) * (1.0 + zeta * za));
+          dz[a] = s * (0.125 * za * (1.0 + xi * xa) * (1.0 + eta * ea));
+        }
+        double B[6][24];
+        memset(B, 0, sizeof B);
+        for (int a = 0; a < 8; ++a) {
+          B[0][3 * a] = dx[a];
+          B[1][3 * a + 1] = dy[a];
+          B[2][3 * a + 2] = dz[a];
+          B[3][3 * a] = dy[a];
+          B[3][3 * a + 1] = dx[a];
+          B[4][3 * a + 1] = dz[a];
+          B[4][3 * a + 2] = dy[a];
+          B[5][3 * a] = dz[a];
+          B[5][3 * a + 2] = dx[a];
+        }
+        double DB[6][24];
+        for (int r = 0; r < 6; ++r)
+          for (int col = 0; col < 24; ++col) {
+            double acc = 0.0;
+            for (int m = 0; m < 6; ++m) acc += D[r][m] * B[m][col];
+            DB[r][col] = acc;
+          }
+        for (int r = 0; r < 24; ++r)
+          for (int col = 0; col < 24; ++col) {
+            double acc = 0.0;
+            for (int m = 0; m < 6; ++m) acc += B[m][r] * DB[m][col];
+            ke[r * 24 + col] += acc * detJ;
+          }
+      }
+  return OR_OK;
+}
+
+/* ----------------------------------------------------------------- apply */
+static void elem_dofs(int nx, int ny, int i, int j, int k, int* edof) {
+  const int nnx = nx + 1, nny = ny + 1;
+  for (int a = 0; a < 8; ++a) {
+    const int n = ((k + kCz[a]) * nny + (j + kCy[a])) * nnx + (i + kCx[a]);
+    for (int c = 0; c < 3; ++c) edof[3 * a + c] = 3 * n + c;
+  }
+}
+
+static int is_solid(const uint8_t* solid, size_t e) { return solid == NULL || solid[e] != 0; }
+
+/* Full-grid y = sum_e factor_e Ke u_e, element colours 0..7 in order (colour =
+ * (i&1)|(j&1)<<1|(k&1)<<2, matfree.cpp:465, fea_matfree.hpp:41-49), each
+ * element's 24 outputs accumulated column by column with mul+add
+ * (matfree.cpp:75-123), then scaled by the factor and added to y. */
+static void apply_full(int nx, int ny, int nz, const uint8_t* solid, const double* factor,
+                       const double* ke, const double* u, double* y) {
+  const size_t ndof = 3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  memset(y, 0, sizeof(double) * ndof);
+  double kcm[576];
+  for (int r = 0; r < 24; ++r)
+    for (int c = 0; c < 24; ++c) kcm[c * 24 + r] = ke[r * 24 + c];
+  for (int color = 0; color < 8; ++color) {
+    const int pi = color & 1, pj = (color >> 1) & 1, pk = (color >> 2) & 1;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = pk; k < nz; k += 2)
+      for (int j = pj; j < ny; j += 2)
+        for (int i = pi; i < nx; i += 2) {
+          const size_t e = IDX(i, j, k);
+          if (!is_solid(solid, e)) continue;
+          int edof[24];
+          elem_dofs(nx, ny, i, j, k, edof);
+          double ul[24], res[24];
+          for (int r = 0; r < 24; ++r) {
+            ul[r] = u[edof[r]];
+            res[r] = 0.0;
+          }
+          for (int c = 0; c < 24; ++c) {
+            const double w = ul[c];
+            const double* col = &kcm[c * 24];
+            for (int r = 0; r < 24; ++r) {
+              const double t = w * col[r];
+              res[r] = res[r] + t;
+            }
+          }
+          const double f = factor ? factor[e] : 1.0;
+          for (int r = 0; r < 24; ++r) {
+            const double t = f * res[r];
+            y[edof[r]] = y[edof[r]] + t;
+          }
+        }
+  }
+}
+
+static int check_factor(int nx, int ny, int nz, const uint8_t* solid, const double* factor) {
+  if (!factor) return OR_OK;
+  const size_t nv = (size_t)nx * ny * nz;
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(solid, e) && !(factor[e] > 0.0))
+      return fail(OR_EINVAL, "per-voxel Young's modulus must be > 0 on a solid voxel");
+  return OR_OK;
+}
+
+int or_apply(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
+             double E, double nu, const double* u, double* y) {
+  double ke[576];
+  int st = or_hex8_stiffness(factor ? 1.0 : E, nu, h, ke);
+  if (st) return st;
+  if ((st = check_factor(nx, ny, nz, solid, factor))) return st;
+  apply_full(nx, ny, nz, solid, factor, ke, u, y);
+  return OR_OK;
+}
+
+/* -------------------------------------------------------- reduced system */
+typedef struct {
+  int nx, ny, nz;
+  const uint8_t* solid;
+  const double* factor;
+  double ke[576];
+  size_t ndof;
+  int ng;
+  uint8_t* kept;
+  double *rhs, *invdiag, *up;
+  double *xfull, *yfull;
+} red_sys;
+
+/* matfree.cpp:670-834: BC mask + prescribed field, load vector, rhs = f - K up,
+ * free-DOF touch test by solid elements (the void-DOF gate), the Jacobi diagonal
+ * accumulated in colour order, the void-only and void-load rejections. */
+static int build_reduced(red_sys* m, int nbc, const int* bc_node, const int* bc_comp,
+                         const double* bc_val, int nload, const int* ld_node,
+                         const int* ld_comp, const double* ld_val) {
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  const int nnodes = (nx + 1) * (ny + 1) * (nz + 1);
+  const size_t ndof = m->ndof;
+  uint8_t* fixed = calloc(ndof, 1);
+  double* f = calloc(ndof, sizeof(double));
+  double* diag = calloc(ndof, sizeof(double));
+  uint8_t* touched = calloc(ndof, 1);
+  int nonzero_bc = 0, st = OR_OK;
+  for (int b = 0; b < nbc; ++b) {
+    if (bc_node[b] < 0 || bc_node[b] >= nnodes || bc_comp[b] < 0 || bc_comp[b] > 2) {
+      st = fail(OR_EINVAL, "BC index out of range");
+      goto out;
+    }
+    const int d = 3 * bc_node[b] + bc_comp[b];
+    fixed[d] = 1;
+    m->up[d] = bc_val[b];
+    if (bc_val[b] != 0.0) nonzero_bc = 1;
+  }
+  for (int l = 0; l < nload; ++l) {
+    if (ld_node[l] < 0 || ld_node[l] >= nnodes || ld_comp[l] < 0 || ld_comp[l] > 2) {
+      st = fail(OR_EINVAL, "load index out of range");
+      goto out;
+    }
+    f[3 * ld_node[l] + ld_comp[l]] += ld_val[l];
+  }
+  if (nonzero_bc) {
+    apply_full(nx, ny, nz, m->solid, m->factor, m->ke, m->up, m->yfull);
+    for (size_t d = 0; d < ndof; ++d) f[d] -= m->yfull[d];
+  }
+  /* touch + diagonal, colour order (the reference sweeps its colour-sorted table). */
+  for (int color = 0; color < 8; ++color) {
+    const int pi = color & 1, pj = (color >> 1) & 1, pk = (color >> 2) & 1;
+    for (int k = pk; k < nz; k += 2)
+      for (int j = pj; j < ny; j += 2)
+        for (int i = pi; i < nx; i += 2) {
+          const size_t e = IDX(i, j, k);
+          if (!is_solid(m->solid, e)) continue;
+          int edof[24];
+          elem_dofs(nx, ny, i, j, k, edof);
+          const double fac = m->factor ? m->factor[e] : 1.0;
+          for (int r = 0; r < 24; ++r) {
+            if (!fixed[edof[r]]) touched[edof[r]] = 1;
+            const double t = fac * m->ke[r * 24 + r];
+            diag[edof[r]] = diag[edof[r]] + t;
+          }
+        }
+  }
+  {
+    size_t nf = 0, ntouched = 0;
+    double rmax = 0.0;
+    for (size_t d = 0; d < ndof; ++d)
+      if (!fixed[d]) {
+        ++nf;
+        if (touched[d]) ++ntouched;
+        rmax = fmax(rmax, fabs(f[d]));
+      }
+    if (nf > 0 && ntouched == 0) {
+      st = fail(OR_ESINGULAR, "singular system (no stiffness - every free DOF is void)");
+      goto out;
+    }
+    const double load_tol = 1e-9 * rmax;
+    for (size_t d = 0; d < ndof; ++d)
+      if (!fixed[d] && !touched[d] && fabs(f[d]) > load_tol) {
+        st = fail(OR_ESINGULAR,
+                  "under-constrained system (load applied to a void DOF with no stiffness)");
+        goto out;
+      }
+  }
+  m->ng = 0;
+  for (size_t d = 0; d < ndof; ++d) {
+    const int k = !fixed[d] && touched[d];
+    m->kept[d] = (uint8_t)k;
+    m->rhs[d] = k ? f[d] : 0.0;
+    m->invdiag[d] = k ? 1.0 / diag[d] : 0.0;
+    m->ng += k;
+  }
+out:
+  free(fixed);
+  free(f);
+  free(diag);
+  free(touched);
+  return st;
+}
+
+static int red_init(red_sys* m, int nx, int ny, int nz, double h, const uint8_t* solid,
+                    const double* factor, double E, double nu) {
+  memset(m, 0, sizeof *m);
+  m->nx = nx; m->ny = ny; m->nz = nz;
+  m->solid = solid;
+  m->factor = factor;
+  int st = or_hex8_stiffness(factor ? 1.0 : E, nu, h, m->ke);
+  if (st) return st;
+  if ((st = check_factor(nx, ny, nz, solid, factor))) return st;
+  m->ndof = 3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  m->kept = calloc(m->ndof, 1);
+  m->rhs = calloc(m->ndof, sizeof(double));
+  m->invdiag = calloc(m->ndof, sizeof(double));
+  m->up = calloc(m->ndof, sizeof(double));
+  m->xfull = calloc(m->ndof, sizeof(double));
+  m->yfull = calloc(m->ndof, sizeof(double));
+  return OR_OK;
+}
+
+static void red_free(red_sys* m) {
+  free(m->kept); free(m->rhs); free(m->invdiag); free(m->up); free(m->xfull); free(m->yfull);
+}
+
+int or_build_reduced(int nx, int ny, int nz, double h, const uint8_t* solid,
+                     const double* factor, double E, double nu, int nbc, const int* bc_node,
+                     const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+                     const int* ld_comp, const double* ld_val, uint8_t* kept, double* rhs,
+                     double* invdiag, double* up, int* ng_out) {
+  red_sys m;
+  int st = red_init(&m, nx, ny, nz, h, solid, factor, E, nu);
+  if (!st) st = build_reduced(&m, nbc, bc_node, bc_comp, bc_val, nload, ld_node, ld_comp, ld_val);
+  if (!st) {
+    memcpy(kept, m.kept, m.ndof);
+    memcpy(rhs, m.rhs, m.ndof * sizeof(double));
+    memcpy(invdiag, m.invdiag, m.ndof * sizeof(double));
+    memcpy(up, m.up, m.ndof * sizeof(double));
+    *ng_out = m.ng;
+  }
+  red_free(&m);
+  return st;
+}
+
+/* ------------------------------------------------------------ Jacobi-PCG */
+/* y_kept = K_gg x_kept: scatter (x is already zero off the kept set), full
+ * apply, gather (matfree.cpp:595-608). */
+static void apply_kgg(red_sys* m, const double* x, double* y) {
+  apply_full(m->nx, m->ny, m->nz, m->solid, m->factor, m->ke, x, m->yfull);
+  for (size_t d = 0; d < m->ndof; ++d) y[d] = m->kept[d] ? m->yfull[d] : 0.0;
+}
+
+static double kdot(const red_sys* m, const double* a, const double* b) {
+  double s = 0.0;
+  for (size_t d = 0; d < m->ndof; ++d)
+    if (m->kept[d]) s += a[d] * b[d];
+  return s;
+}
+
+/* Eigen-style Jacobi-PCG (matfree.cpp:841-1076): threshold tol^2*|b|^2 clamped
+ * to DBL_MIN, the iteration that reaches it is not counted, error =
+ * sqrt(|r|^2/|b|^2), converged iff error <= tol and the iterate is finite. */
+static int cg_solve(red_sys* m, double tol, int max_it, double* x, int* iters_out,
+                    double* err_out) {
+  const size_t n = m->ndof;
+  const int maxIters = max_it > 0 ? max_it : 2 * m->ng;
+  double* r = calloc(n, sizeof(double));
+  double* p = calloc(n, sizeof(double));
+  double* z = calloc(n, sizeof(double));
+  double* t = calloc(n, sizeof(double));
+  int converged = 0, it = 0;
+  double err = 0.0;
+  const double rhs2 = kdot(m, m->rhs, m->rhs);
+  if (rhs2 == 0.0) {
+    for (size_t d = 0; d < n; ++d) x[d] = 0.0;
+    converged = 1;
+    goto done;
+  }
+  double threshold = tol * tol * rhs2;
+  if (threshold < DBL_MIN) threshold = DBL_MIN;
+  apply_kgg(m, x, t);
+  for (size_t d = 0; d < n; ++d) r[d] = m->kept[d] ? m->rhs[d] - t[d] : 0.0;
+  double rn2 = kdot(m, r, r);
+  if (rn2 < threshold) {
+    err = sqrt(rn2 / rhs2);
+    converged = err <= tol;
+    goto done;
+  }
+  for (size_t d = 0; d < n; ++d) p[d] = m->invdiag[d] * r[d];
+  double absNew = kdot(m, r, p);
+  while (it < maxIters) {
+    apply_kgg(m, p, t);
+    const double alpha = absNew / kdot(m, p, t);
+    for (size_t d = 0; d < n; ++d)
+      if (m->kept[d]) {
+        x[d] += alpha * p[d];
+        r[d] -= alpha * t[d];
+      }
+    rn2 = kdot(m, r, r);
+    if (rn2 < threshold) break;
+    for (size_t d = 0; d < n; ++d) z[d] = m->invdiag[d] * r[d];
+    const double absOld = absNew;
+    absNew = kdot(m, r, z);
+    const double beta = absNew / absOld;
+    for (size_t d = 0; d < n; ++d)
+      if (m->kept[d]) p[d] = z[d] + beta * p[d];
+    ++it;
+  }
+  err = sqrt(rn2 / rhs2);
+  {
+    int finite = 1;
+    for (size_t d = 0; d < n; ++d)
+      if (m->kept[d] && !isfinite(x[d])) finite = 0;
+    converged = (err <= tol) && finite;
+  }
+done:
+  *iters_out = it;
+  *err_out = err;
+  free(r); free(p); free(z); free(t);
+  return converged ? OR_OK : fail(OR_ENONCONV, "CG did not reach the requested tolerance");
+}
+
+int or_solve_cg(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
+                double E, double nu, int nbc, const int* bc_node, const int* bc_comp,
+                const double* bc_val, int nload, const int* ld_node, const int* ld_comp,
+                const double* ld_val, double tol, int max_it, const double* initial_guess,
+                double* u, int* iters, double* resid) {
+  red_sys m;
+  int st = red_init(&m, nx, ny, nz, h, solid, factor, E, nu);
+  if (!st) st = build_reduced(&m, nbc, bc_node, bc_comp, bc_val, nload, ld_node, ld_comp, ld_val);
+  *iters = 0;
+  *resid = 0.0;
+  if (!st) {
+    double* x = calloc(m.ndof, sizeof(double));
+    if (initial_guess)
+      for (size_t d = 0; d < m.ndof; ++d) x[d] = m.kept[d] ? initial_guess[d] : 0.0;
+    if (m.ng > 0) st = cg_solve(&m, tol, max_it, x, iters, resid);
+    for (size_t d = 0; d < m.ndof; ++d) u[d] = m.kept[d] ? x[d] : m.up[d];
+    free(x);
+  }
+  red_free(&m);
+  return st;
+}
+
+/* ---------------------------------------------------------- compliance */
+static double clamp_density(double rho, double rho_min) {
+  /* std::min(1.0, std::max(rho_min, rho)) (simp.cpp:44-47). */
+  const double lo = (rho_min < rho) ? rho : rho_min;
+  return (lo < 1.0) ? lo : 1.0;
+}
+
+int or_sensitivity(int nx, int ny, int nz, double h, const uint8_t* solid, double E0, double nu,
+                   double penal, double rho_min, const double* density, const double* u,
+                   double* dc, double* compliance) {
+  double ke[576];
+  int st = or_hex8_stiffness(1.0, nu, h, ke);
+  if (st) return st;
+  const size_t nv = (size_t)nx * ny * nz;
+  memset(dc, 0, nv * sizeof(double));
+  double c = 0.0;
+  /* simp.cpp:747-824: grid order, q = u_e^T Kunit u_e row by row. */
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t e = IDX(i, j, k);
+        if (!is_solid(solid, e)) continue;
+        int edof[24];
+        elem_dofs(nx, ny, i, j, k, edof);
+        double ue[24];
+        for (int r = 0; r < 24; ++r) ue[r] = u[edof[r]];
+        const double rho = clamp_density(density[e], rho_min);
+        double q = 0.0;
+        for (int r = 0; r < 24; ++r) {
+          double kr = 0.0;
+          for (int cc = 0; cc < 24; ++cc) kr += ke[r * 24 + cc] * ue[cc];
+          q += ue[r] * kr;
+        }
+        c += pow(rho, penal) * E0 * q;
+        dc[e] = -penal * pow(rho, penal - 1.0) * E0 * q;
+      }
+  *compliance = c;
+  return OR_OK;
+}
+
+int or_simp_compliance(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                       double nu, double penal, double rho_min, const double* density,
+                       int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                       int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                       double tol, int max_it, double* u, double* dc, double* compliance,
+                       int* iters, double* resid) {
+  if (!(E0 > 0.0)) return fail(OR_EINVAL, "simp: youngs_modulus (E0) must be > 0");
+  if (!(penal > 0.0)) return fail(OR_EINVAL, "simp: penalty (p) must be > 0");
+  if (!(rho_min > 0.0 && rho_min <= 1.0))
+    return fail(OR_EINVAL, "simp: density_min must be in (0, 1]");
+  const size_t nv = (size_t)nx * ny * nz;
+  double* E = calloc(nv, sizeof(double));
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(solid, e)) E[e] = pow(clamp_density(density[e], rho_min), penal) * E0;
+  int st = or_solve_cg(nx, ny, nz, h, solid, E, 1.0, nu, nbc, bc_node, bc_comp, bc_val, nload,
+                       ld_node, ld_comp, ld_val, tol, max_it, NULL, u, iters, resid);
+  free(E);
+  if (st) return st;
+  return or_sensitivity(nx, ny, nz, h, solid, E0, nu, penal, rho_min, density, u, dc,
+                        compliance);
+}
+
+/* --------------------------------------------------------------- filter */
+struct or_filter {
+  size_t nv;
+  size_t* row;
+  int* nbr;
+  double* w;
+  double* hs;
+};
+
+/* make_density_filter (simp.cpp:834-890): for every active voxel, the active
+ * voxels within ceil(r) in (dk,dj,di) ascending order with weight r - dist > 0. */
+or_filter* or_filter_make(int nx, int ny, int nz, const uint8_t* solid, const uint8_t* active,
+                          double radius) {
+  if (!(radius > 0.0)) {
+    fail(OR_EINVAL, "make_density_filter: radius must be > 0");
+    return NULL;
+  }
+  or_filter* f = calloc(1, sizeof *f);
+  const size_t nv = (size_t)nx * ny * nz;
+  f->nv = nv;
+  f->row = calloc(nv + 1, sizeof(size_t));
+  f->hs = calloc(nv, sizeof(double));
+  const int R = (int)ceil(radius);
+  const size_t cap_per = (size_t)(2 * R + 1) * (2 * R + 1) * (2 * R + 1);
+  size_t cap = nv * cap_per, nnz = 0;
+  if (cap > ((size_t)1 << 31)) cap = (size_t)1 << 31;
+  f->nbr = malloc(cap * sizeof(int));
+  f->w = malloc(cap * sizeof(double));
+#define ACT(i, j, k) (is_solid(solid, IDX(i, j, k)) && (active == NULL || active[IDX(i, j, k)]))
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t e = IDX(i, j, k);
+        f->row[e] = nnz;
+        if (!ACT(i, j, k)) continue;
+        double hs = 0.0;
+        for (int dk = -R; dk <= R; ++dk)
+          for (int dj = -R; dj <= R; ++dj)
+            for (int di = -R; di <= R; ++di) {
+              const int ii = i + di, jj = j + dj, kk = k + dk;
+              if (ii < 0 || ii >= nx || jj < 0 || jj >= ny || kk < 0 || kk >= nz) continue;
+              if (!ACT(ii, jj, kk)) continue;
+              const double dist = sqrt((double)(di * di + dj * dj + dk * dk));
+              const double wgt = radius - dist;
+              if (wgt <= 0.0) continue;
+              if (nnz == cap) {
+                cap *= 2;
+                f->nbr = realloc(f->nbr, cap * sizeof(int));
+                f->w = realloc(f->w, cap * sizeof(double));
+              }
+              f->nbr[nnz] = (int)IDX(ii, jj, kk);
+              f->w[nnz] = wgt;
+              ++nnz;
+              hs += wgt;
+            }
+        f->hs[e] = hs;
+      }
+#undef ACT
+  f->row[nv] = nnz;
+  return f;
+}
+
+void or_filter_free(or_filter* f) {
+  if (!f) return;
+  free(f->row); free(f->nbr); free(f->w); free(f->hs); free(f);
+}
+size_t or_filter_nnz(const or_filter* f) { return f->row[f->nv]; }
+void or_filter_weight_sum(const or_filter* f, double* hs) {
+  memcpy(hs, f->hs, f->nv * sizeof(double));
+}
+
+/* filter_density (simp.cpp:913-926). */
+void or_filter_density(const or_filter* f, const double* x, double* out) {
+#pragma omp parallel for schedule(static)
+  for (size_t e = 0; e < f->nv; ++e) {
+    out[e] = 0.0;
+    if (!(f->hs[e] > 0.0)) continue;
+    double acc = 0.0;
+    for (size_t p = f->row[e]; p < f->row[e + 1]; ++p) acc += f->w[p] * x[f->nbr[p]];
+    out[e] = acc / f->hs[e];
+  }
+}
+
+/* filter_sensitivity, the transpose (simp.cpp:928-942). */
+void or_filter_sensitivity(const or_filter* f, const double* s, double* out) {
+  memset(out, 0, f->nv * sizeof(double));
+  for (size_t e = 0; e < f->nv; ++e) {
+    if (!(f->hs[e] > 0.0)) continue;
+    const double se = s[e] / f->hs[e];
+    for (size_t p = f->row[e]; p < f->row[e + 1]; ++p) out[f->nbr[p]] += f->w[p] * se;
+  }
+}
+
+/* ------------------------------------------------------------------- OC */
+typedef struct {
+  int nx, ny, nz;
+  const uint8_t* solid;
+  const or_filter* f;
+  const double *x, *dc, *dv;
+  double move, rho_min;
+  double *xnew, *xp;
+} oc_ctx;
+
+/* candidate(lambda) of simp.cpp:980-1000. */
+static void oc_candidate(oc_ctx* c, double lambda) {
+  const size_t nv = (size_t)c->nx * c->ny * c->nz;
+#pragma omp parallel for schedule(static)
+  for (size_t e = 0; e < nv; ++e) {
+    c->xnew[e] = 0.0;
+    if (!is_solid(c->solid, e)) continue;
+    const double xe = c->x[e];
+    double be = 0.0;
+    if (c->dv[e] > 0.0) be = -c->dc[e] / (lambda * c->dv[e]);
+    if (be < 0.0) be = 0.0;
+    double xt = xe * sqrt(be);
+    const double lo = (c->rho_min < xe - c->move) ? xe - c->move : c->rho_min;
+    const double hi = (xe + c->move < 1.0) ? xe + c->move : 1.0;
+    if (xt < lo) xt = lo;
+    if (xt > hi) xt = hi;
+    c->xnew[e] = xt;
+  }
+}
+
+/* phys_vol of simp.cpp:1003-1011: sequential FP64 sum of the filtered candidate
+ * over solid voxels in grid order. */
+static double oc_phys_vol(oc_ctx* c) {
+  or_filter_density(c->f, c->xnew, c->xp);
+  const size_t nv = (size_t)c->nx * c->ny * c->nz;
+  double v = 0.0;
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(c->solid, e)) v += c->xp[e];
+  return v;
+}
+
+int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* f,
+                 const double* density, const double* dc, double volfrac, double move,
+                 double rho_min, double* x_new, double* lambda_out, int* nvol_out) {
+  if (!(volfrac > 0.0 && volfrac <= 1.0))
+    return fail(OR_EINVAL, "oc_update: volume_fraction must be in (0, 1]");
+  if (!(move > 0.0)) return fail(OR_EINVAL, "oc_update: move must be > 0");
+  if (!(rho_min > 0.0 && rho_min <= 1.0))
+    return fail(OR_EINVAL, "oc_update: density_min must be in (0, 1]");
+  const size_t nv = (size_t)nx * ny * nz;
+  double* dcf = malloc(nv * sizeof(double));
+  double* ones = calloc(nv, sizeof(double));
+  double* dv = malloc(nv * sizeof(double));
+  double* xp = malloc(nv * sizeof(double));
+  size_t n_design = 0;
+  or_filter_sensitivity(f, dc, dcf);
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(solid, e)) {
+      ones[e] = 1.0;
+      ++n_design;
+    }
+  or_filter_sensitivity(f, ones, dv);
+  const double target = volfrac * (double)n_design;
+  oc_ctx c = {nx, ny, nz, solid, f, density, dcf, dv, move, rho_min, x_new, xp};
+  double l1 = 0.0, l2 = 1.0;
+  int nvol = 0;
+  for (;;) {
+    if (!(l2 < 1e30)) break;
+    oc_candidate(&c, l2);
+    ++nvol;
+    if (!(oc_phys_vol(&c) > target)) break;
+    l2 *= 2.0;
+  }
+  for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
+    const double lmid = 0.5 * (l1 + l2);
+    oc_candidate(&c, lmid);
+    ++nvol;
+    if (oc_phys_vol(&c) > target)
+      l1 = lmid;
+    else
+      l2 = lmid;
+  }
+  const double lam = 0.5 * (l1 + l2);
+  oc_candidate(&c, lam);
+  if (lambda_out) *lambda_out = lam;
+  if (nvol_out) *nvol_out = nvol;
+  free(dcf); free(ones); free(dv); free(xp);
+  return OR_OK;
+}
+
+/* ---------------------------------------------------------- simp loop */
+/* rung_infeasible (simp.cpp:1140-1186) with the SimpOptions defaults
+ * (simp.hpp:1299-1302): ratio 100, cg blow-up 4, flat tol 1e-3, window 5. */
+static int rung_infeasible(const double* c, const int* cg, int n) {
+  const int window = 5;
+  const double ratio = 100.0, cg_blowup = 4.0, flat_tol = 1e-3;
+  if (n < window + 1) return 0;
+  if (!(isfinite(c[0]) && c[0] > 0.0)) return 0;
+  int cgmin = cg[0];
+  for (int i = 1; i < n - window; ++i)
+    if (cg[i] < cgmin) cgmin = cg[i];
+  if (cgmin <= 0) return 0;
+  const double cbar = ratio * c[0], cgbar = cg_blowup * (double)cgmin;
+  double lo = c[n - window], hi = c[n - window];
+  for (int i = n - window; i < n; ++i) {
+    if (!isfinite(c[i])) return 0;
+    if (!(c[i] >= cbar)) return 0;
+    if (!((double)cg[i] >= cgbar)) return 0;
+    lo = fmin(lo, c[i]);
+    hi = fmax(hi, c[i]);
+  }
+  if (!(lo > 0.0)) return 0;
+  return (hi - lo) / lo <= flat_tol;
+}
+
+int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                     double nu, double penal, double rho_min, int nbc, const int* bc_node,
+                     const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+                     const int* ld_comp, const double* ld_val, const or_simp_options* o,
+                     double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
+                     double* design, double* phys, or_simp_result* res) {
+  memset(res, 0, sizeof *res);
+  if (!(o->volume_fraction > 0.0 && o->volume_fraction <= 1.0))
+    return fail(OR_EINVAL, "simp_optimize: volume_fraction must be in (0, 1]");
+  if (!(o->move > 0.0)) return fail(OR_EINVAL, "simp_optimize: move must be > 0");
+  if (o->max_iterations < 1)
+    return fail(OR_EINVAL, "simp_optimize: max_iterations must be >= 1");
+  or_filter* f = or_filter_make(nx, ny, nz, solid, NULL, o->filter_radius);
+  if (!f) return OR_EINVAL;
+  const size_t nv = (size_t)nx * ny * nz;
+  const size_t ndof = 3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  double n_design = 0.0;
+  double* x = calloc(nv, sizeof(double));
+  double* xphys = malloc(nv * sizeof(double));
+  double* xnew = malloc(nv * sizeof(double));
+  double* dc = malloc(nv * sizeof(double));
+  double* u = malloc(ndof * sizeof(double));
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(solid, e)) {
+      x[e] = o->volume_fraction; /* simp_uniform_density (simp.cpp:305-312) */
+      n_design += 1.0;
+    }
+  int st = OR_OK;
+  for (int it = 0; it < o->max_iterations; ++it) {
+    or_filter_density(f, x, xphys);
+    double c = 0.0, resid = 0.0;
+    int cgit = 0;
+    st = or_simp_compliance(nx, ny, nz, h, solid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
+                            bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
+                            o->cg_max_iterations, u, dc, &c, &cgit, &resid);
+    if (st == OR_ENONCONV) {
+      res->non_convergent = 1;
+      st = OR_OK;
+      break;
+    }
+    if (st) goto out;
+    st = or_oc_update(nx, ny, nz, solid, f, x, dc, o->volume_fraction, o->move, rho_min, xnew,
+                      NULL, NULL);
+    if (st) goto out;
+    double change = 0.0;
+    for (size_t e = 0; e < nv; ++e) change = fmax(change, fabs(xnew[e] - x[e]));
+    memcpy(x, xnew, nv * sizeof(double));
+    if (res->iterations == 0) res->initial_compliance = c;
+    const int n = res->iterations++;
+    or_filter_density(f, x, xphys);
+    double vol = 0.0;
+    for (size_t e = 0; e < nv; ++e) vol += xphys[e];
+    hist_c[n] = c;
+    hist_change[n] = change;
+    hist_vf[n] = n_design > 0.0 ? vol / n_design : 0.0;
+    hist_cg[n] = cgit;
+    if (rung_infeasible(hist_c, hist_cg, res->iterations)) {
+      res->infeasible = 1;
+      break;
+    }
+    if (change < o->change_tol) {
+      res->converged = 1;
+      break;
+    }
+  }
+  memcpy(design, x, nv * sizeof(double));
+  or_filter_density(f, x, phys);
+  if (res->infeasible || res->non_convergent) {
+    res->compliance = res->iterations ? hist_c[res->iterations - 1] : 0.0;
+  } else {
+    double resid = 0.0;
+    int cgit = 0;
+    st = or_simp_compliance(nx, ny, nz, h, solid, E0, nu, penal, rho_min, phys, nbc, bc_node,
+                            bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
+                            o->cg_max_iterations, u, dc, &res->compliance, &cgit, &resid);
+    if (st == OR_ENONCONV) {
+      res->non_convergent = 1;
+      res->converged = 0;
+      res->compliance = res->iterations ? hist_c[res->iterations - 1] : 0.0;
+      st = OR_OK;
+    }
+  }
+  {
+    double vol = 0.0;
+    for (size_t e = 0; e < nv; ++e) vol += phys[e];
+    res->volume_fraction = n_design > 0.0 ? vol / n_design : 0.0;
+  }
+out:
+  free(x); free(xphys); free(xnew); free(dc); free(u);
+  or_filter_free(f);
+  return st;
+}

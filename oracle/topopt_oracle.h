@@ -1,0 +1,131 @@
+/*
+ * topopt_oracle.h -- CPU restatement of the reference voxel-SIMP inner loop.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: it is linked by the
+ * tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by
+ * the product library (topopt_gb300/csrc).  Every function restates one piece of
+ * the reference algorithm (Anarkissed/TopOpt, core/) in plain C, in the same
+ * arithmetic order where the reference fixes one, and cites the file:line it
+ * follows.  Compile with -ffp-contract=off so no multiply/add pair is fused; the
+ * reference uses explicit mul+add for the same reason (core/src/fea/matfree.cpp:66-73).
+ *
+ * Parity pin: the restatement is checked against (1) the reference's own Ke
+ * fixture core/tests/fixtures/fea/hex_stiffness_reference.json and (2) golden
+ * vectors produced by the reference's own compiled code (oracle/_ref, built by
+ * oracle/build_ref.sh) and committed under tests/golden/.
+ *
+ * Conventions (core/include/topopt/fea.hpp:18-29, :153-171):
+ *   voxel (i,j,k)  -> e = (k*ny + j)*nx + i               (x fastest)
+ *   node  (a,b,c)  -> n = (c*(ny+1) + b)*(nx+1) + a
+ *   DOF            -> 3*n + comp                          (node-major interleaved)
+ *   Hex8 local node order: bottom face CCW then top face CCW.
+ * `solid` is one byte per voxel (non-zero = solid, i.e. VoxelTag != Empty); NULL
+ * means every voxel is solid.
+ */
+#ifndef TOPOPT_ORACLE_H
+#define TOPOPT_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OR_OK = 0, OR_EINVAL = 1, OR_ESINGULAR = 2, OR_ENONCONV = 3 };
+
+/* Host threads the oracle's parallel loops use (1 when built without OpenMP). */
+int or_threads(void);
+
+/* Last error message of the calling thread ("" when none). */
+const char* or_last_error(void);
+
+/* 24x24 row-major element stiffness, 2x2x2 Gauss (hex_element.cpp:23-115). */
+int or_hex8_stiffness(double E, double nu, double h, double* ke576);
+
+/* y = K u over the full grid; factor == NULL -> uniform modulus E baked into Ke,
+ * else Ke(E=1) and factor[e] per solid voxel (matfree.cpp:1079-1098, :535-553).
+ * Colour-ordered element loop with the reference's column-major mul+add. */
+int or_apply(int nx, int ny, int nz, double h, const uint8_t* solid,
+             const double* factor, double E, double nu, const double* u, double* y);
+
+/* Reduced, void-gated system (matfree.cpp:670-834).  Outputs (all ndof long):
+ *   kept[d]   1 if DOF d survives (free and touched by a solid element)
+ *   rhs[d]    f - K u_p on kept DOFs, 0 elsewhere
+ *   invdiag[d] 1/diag on kept DOFs, 0 elsewhere
+ *   up[d]     prescribed displacement field
+ * Returns OR_ESINGULAR for a void-only system or a load on a void DOF. */
+int or_build_reduced(int nx, int ny, int nz, double h, const uint8_t* solid,
+                     const double* factor, double E, double nu,
+                     int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                     int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                     uint8_t* kept, double* rhs, double* invdiag, double* up, int* ng_out);
+
+/* Jacobi-PCG solve of the reduced system, Eigen-criterion (matfree.cpp:841-1076,
+ * 1106-1170).  u (ndof) receives the full field.  initial_guess may be NULL. */
+int or_solve_cg(int nx, int ny, int nz, double h, const uint8_t* solid,
+                const double* factor, double E, double nu,
+                int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                double tol, int max_it, const double* initial_guess,
+                double* u, int* iters, double* resid);
+
+/* SIMP compliance + sensitivities (simp.cpp:567-828): reference law
+ * E = clamp(rho, rho_min, 1)^p * E0.  dc is 0 on non-solid voxels. */
+int or_simp_compliance(int nx, int ny, int nz, double h, const uint8_t* solid,
+                       double E0, double nu, double penal, double rho_min,
+                       const double* density,
+                       int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                       int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                       double tol, int max_it, double* u, double* dc,
+                       double* compliance, int* iters, double* resid);
+
+/* Compliance + sensitivities from a given displacement field (the sweep of
+ * simp.cpp:747-824 without the solve). */
+int or_sensitivity(int nx, int ny, int nz, double h, const uint8_t* solid,
+                   double E0, double nu, double penal, double rho_min,
+                   const double* density, const double* u, double* dc,
+                   double* compliance);
+
+/* Density filter (simp.cpp:834-942): CSR over active design voxels.  `active`
+ * (one byte per voxel, NULL = solid) selects the design voxels. */
+typedef struct or_filter or_filter;
+or_filter* or_filter_make(int nx, int ny, int nz, const uint8_t* solid,
+                          const uint8_t* active, double radius);
+void or_filter_free(or_filter* f);
+size_t or_filter_nnz(const or_filter* f);
+void or_filter_weight_sum(const or_filter* f, double* hs);
+void or_filter_density(const or_filter* f, const double* x, double* out);
+void or_filter_sensitivity(const or_filter* f, const double* s, double* out);
+
+/* OC update with lambda bisection (simp.cpp:948-1025).  Writes x_new; the final
+ * lambda and the number of volume evaluations are returned for diagnostics. */
+int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* f,
+                 const double* density, const double* dc, double volfrac,
+                 double move, double rho_min, double* x_new,
+                 double* lambda_out, int* nvol_out);
+
+/* Plain simp_optimize with the OC updater and no projection (simp.cpp:2018-2592).
+ * The solve is the exact Jacobi-PCG above.  hist_* have room for max_it rows.
+ * Guards: change_tol stop; rung-infeasibility window (simp.cpp:1140-1186) with
+ * the reference defaults; non-convergence ends the run. */
+typedef struct {
+  double volume_fraction, filter_radius, move, change_tol, cg_tolerance;
+  int max_iterations, cg_max_iterations;
+} or_simp_options;
+typedef struct {
+  int iterations, converged, non_convergent, infeasible;
+  double compliance, volume_fraction, initial_compliance;
+} or_simp_result;
+int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid,
+                     double E0, double nu, double penal, double rho_min,
+                     int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                     int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                     const or_simp_options* opt, double* hist_c, double* hist_change,
+                     double* hist_vf, int* hist_cg, double* design, double* phys,
+                     or_simp_result* res);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,97 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's OWN code.
+
+Runs the reference's compiled hot path (oracle/_ref/libtopopt_ref.so, built by
+oracle/build_ref.sh from the reference tree) on small seeded problems and saves
+inputs and outputs as golden.npz.  Only runs where the reference tree is
+available; the committed golden.npz is what the tests read everywhere else.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+from oracle.oracle import OracleLib, Problem, build_reference, cantilever  # noqa: E402
+
+REF_KE_JSON = "/root/reference/core/tests/fixtures/fea/hex_stiffness_reference.json"
+
+
+def main():
+    if build_reference() is None:
+        raise SystemExit("reference tree not available; nothing generated")
+    R = OracleLib("reference")
+    R.set_threads(1)
+    rng = np.random.default_rng(20261203)
+    out = {}
+    # Element stiffness, pinned to the reference's own JSON fixture too.
+    for nu in (0.3, 0.4):
+        ke = R.hex8_stiffness(1.0, nu, 1.0)
+        out[f"ke_nu{int(nu * 100):02d}"] = ke
+    ref = json.load(open(REF_KE_JSON))
+    for key, case in ref["cases"].items():
+        K = np.array(case["K"])
+        nu = case["poisson"]
+        got = out[f"ke_nu{int(round(nu * 100)):02d}"]
+        assert np.abs(got - K).max() <= 1e-10 * np.abs(K).max(), key
+    out["ke_h05_E2"] = R.hex8_stiffness(2.0, 0.3, 0.5)
+
+    # Operator apply on a grid with voids, graded and uniform.
+    nx, ny, nz = 13, 6, 5
+    solid = (rng.random(nx * ny * nz) > 0.15).astype(np.uint8).reshape(nz, ny, nx)
+    solid[nz // 2 - 1:nz // 2 + 1, :, nx - 1] = 1  # keep the loaded edge stiff
+    solid = solid.ravel()
+    pb = cantilever(nx, ny, nz, solid=solid)
+    u = rng.standard_normal(pb.ndof)
+    fac = rng.random(pb.nv) * 0.99 + 0.01
+    out.update(apply_dims=np.array([nx, ny, nz]), apply_solid=solid, apply_u=u, apply_factor=fac,
+               apply_y_graded=R.apply(pb, u, fac), apply_y_uniform=R.apply(pb, u, None, E=2.5))
+
+    # Reduced system, void-DOF gate and the exact Jacobi-PCG solve.
+    red = R.build_reduced(pb, fac)
+    out.update(red_kept=red["kept"], red_rhs=red["rhs"], red_invdiag=red["invdiag"],
+               red_ng=np.array(red["ng"]))
+    ucg, it, res = R.solve_cg(pb, fac, tol=1e-12)
+    out.update(cg_u=ucg, cg_iters=np.array(it), cg_resid=np.array(res))
+
+    # simp_compliance on a graded density (solve at 1e-12).
+    pb2 = cantilever(16, 6, 6)
+    rho = rng.random(pb2.nv) * 0.95 + 0.05
+    c = R.simp_compliance(pb2, rho, tol=1e-12)
+    out.update(comp_dims=np.array([16, 6, 6]), comp_rho=rho, comp_u=c["u"], comp_dc=c["dc"],
+               comp_c=np.array(c["compliance"]))
+
+    # Density filter, forward and adjoint, r = 1.5 and 2.5, with voids.
+    x = rng.random(pb.nv)
+    for r in (1.5, 2.5):
+        tag = str(r).replace(".", "")
+        out[f"filt_x"] = x
+        out[f"filt_fwd_r{tag}"] = R.filter(pb, x, r, False)
+        out[f"filt_adj_r{tag}"] = R.filter(pb, x, r, True)
+
+    # OC update with the reference's own dc.
+    xd = np.where(solid > 0, rng.random(pb.nv) * 0.8 + 0.1, 0.0)
+    dc = -np.where(solid > 0, rng.random(pb.nv) * 10.0, 0.0)
+    out.update(oc_x=xd, oc_dc=dc, oc_xnew=R.oc_update(pb, xd, dc, 0.3, 1.5, 0.2, 1e-3),
+               oc_xnew_r25=R.oc_update(pb, xd, dc, 0.4, 2.5, 0.1, 1e-3))
+
+    # A short simp_optimize run (the reference loop, Jacobi-PCG solves).
+    pb3 = cantilever(12, 4, 4)
+    s = R.simp_optimize(pb3, volfrac=0.3, radius=1.5, move=0.2, max_it=20, change_tol=0.01,
+                        cg_tol=1e-10)
+    out.update(simp_dims=np.array([12, 4, 4]), simp_hist_c=s["hist_c"],
+               simp_hist_change=s["hist_change"], simp_hist_vf=s["hist_vf"],
+               simp_design=s["design"], simp_phys=s["phys"],
+               simp_compliance=np.array(s["compliance"]), simp_iterations=np.array(s["iterations"]))
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
+    print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,112 @@
+"""The CPU oracle (a C restatement of the reference) pinned against the
+reference's own fixtures and against golden vectors produced by the reference's
+own compiled code (tests/golden/make_golden.py).  CPU only."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Problem, cantilever
+
+REF_KE_JSON = "/root/reference/core/tests/fixtures/fea/hex_stiffness_reference.json"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_KE_JSON), reason="reference tree not mounted")
+def test_ke_against_reference_fixture(port):
+    ref = json.load(open(REF_KE_JSON))
+    for key, case in ref["cases"].items():
+        K = np.array(case["K"])
+        got = port.hex8_stiffness(case["youngs_modulus"], case["poisson"], 1.0)
+        # hex_stiffness_reference.json: entrywise <= 1e-10 * max|K|.
+        assert np.abs(got - K).max() <= 1e-10 * np.abs(K).max(), key
+        assert np.abs(got - got.T).max() <= 1e-12 * np.abs(got).max()
+        ev = np.linalg.eigvalsh(got)
+        assert (np.abs(ev) < 1e-10).sum() == 6
+        assert abs(np.trace(got) - case["properties"]["trace"]) < 1e-12
+
+
+def test_ke_golden_bit_exact(port, golden):
+    assert np.array_equal(port.hex8_stiffness(1.0, 0.3, 1.0), golden["ke_nu30"])
+    assert np.array_equal(port.hex8_stiffness(1.0, 0.4, 1.0), golden["ke_nu40"])
+    assert np.array_equal(port.hex8_stiffness(2.0, 0.3, 0.5), golden["ke_h05_E2"])
+
+
+def _apply_problem(golden):
+    nx, ny, nz = (int(v) for v in golden["apply_dims"])
+    return cantilever(nx, ny, nz, solid=golden["apply_solid"])
+
+
+def test_apply_golden_bit_exact(port, golden):
+    pb = _apply_problem(golden)
+    y = port.apply(pb, golden["apply_u"], golden["apply_factor"])
+    assert np.array_equal(y, golden["apply_y_graded"])
+    y = port.apply(pb, golden["apply_u"], None, E=2.5)
+    assert np.array_equal(y, golden["apply_y_uniform"])
+
+
+def test_reduced_and_cg_golden(port, golden):
+    pb = _apply_problem(golden)
+    red = port.build_reduced(pb, golden["apply_factor"])
+    assert red["ng"] == int(golden["red_ng"])
+    for k in ("kept", "rhs", "invdiag"):
+        assert np.array_equal(red[k], golden["red_" + k]), k
+    u, it, res = port.solve_cg(pb, golden["apply_factor"], tol=1e-12)
+    assert it == int(golden["cg_iters"])
+    assert np.array_equal(u, golden["cg_u"])
+
+
+def test_compliance_golden(port, golden):
+    pb = cantilever(*(int(v) for v in golden["comp_dims"]))
+    c = port.simp_compliance(pb, golden["comp_rho"], tol=1e-12)
+    assert c["compliance"] == float(golden["comp_c"])
+    assert np.array_equal(c["dc"], golden["comp_dc"])
+
+
+def test_filter_and_oc_golden(port, golden):
+    pb = _apply_problem(golden)
+    for r, tag in ((1.5, "15"), (2.5, "25")):
+        assert np.array_equal(port.filter(pb, golden["filt_x"], r, False), golden["filt_fwd_r" + tag])
+        assert np.array_equal(port.filter(pb, golden["filt_x"], r, True), golden["filt_adj_r" + tag])
+    assert np.array_equal(port.oc_update(pb, golden["oc_x"], golden["oc_dc"], 0.3, 1.5, 0.2),
+                          golden["oc_xnew"])
+    assert np.array_equal(port.oc_update(pb, golden["oc_x"], golden["oc_dc"], 0.4, 2.5, 0.1),
+                          golden["oc_xnew_r25"])
+
+
+def test_simp_loop_golden(port, golden):
+    pb = cantilever(*(int(v) for v in golden["simp_dims"]))
+    s = port.simp_optimize(pb, volfrac=0.3, radius=1.5, move=0.2, max_it=20, change_tol=0.01,
+                           cg_tol=1e-10)
+    assert s["iterations"] == int(golden["simp_iterations"])
+    assert np.array_equal(s["hist_c"], golden["simp_hist_c"])
+    assert np.array_equal(s["design"], golden["simp_design"])
+    assert s["compliance"] == float(golden["simp_compliance"])
+
+
+def test_filter_properties(port):
+    """Partition of unity and the adjoint identity (test_simp.cpp:312-386)."""
+    rng = np.random.default_rng(3)
+    solid = (rng.random(9 * 7 * 5) > 0.2).astype(np.uint8)
+    pb = Problem(9, 7, 5, solid=solid)
+    ones = solid.astype(float)
+    f1 = port.filter(pb, ones, 1.5)
+    assert np.allclose(f1[solid > 0], 1.0, atol=1e-15)
+    a, b = rng.random(pb.nv) * solid, rng.random(pb.nv) * solid
+    lhs = np.dot(port.filter(pb, a, 1.5), b)
+    rhs = np.dot(a, port.filter(pb, b, 1.5, adjoint=True))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_void_gate_errors(port):
+    from oracle.oracle import OracleError
+    pb = cantilever(6, 3, 3, solid=np.zeros(54, np.uint8))
+    with pytest.raises(OracleError) as e:
+        port.build_reduced(pb)
+    assert e.value.code == 2 and "singular" in str(e.value)
+    solid = np.ones((3, 3, 6), np.uint8)
+    solid[:, :, 5] = 0
+    pb = cantilever(6, 3, 3, solid=solid.ravel())
+    with pytest.raises(OracleError) as e:
+        port.build_reduced(pb)
+    assert e.value.code == 2 and "void DOF" in str(e.value)

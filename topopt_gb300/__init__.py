@@ -1,0 +1,45 @@
+"""GB300-native voxel-SIMP inner loop: Python face of the C-ABI library.
+
+The product is ``libtopopt_gb300.so`` (hand-written sm_103a kernels behind the
+``extern "C"`` boundary declared in include/topopt_gb300.h).  This module binds
+it with ctypes and mirrors the reference's library API (Anarkissed/TopOpt,
+core/include/topopt/fea.hpp and simp.hpp): the same function names, argument
+meaning and error classes, so callers written against the reference read the
+same here.
+
+There is no CPU fallback: importing works anywhere, but every call that needs
+the library raises ``LibraryMissing`` when it has not been built, and every call
+fails with ``DeviceError`` when no CUDA device is usable.
+"""
+from __future__ import annotations
+
+from ._capi import (  # noqa: F401
+    CgInfo,
+    DensityFilter,
+    DeviceError,
+    LibraryMissing,
+    Problem,
+    SimpJob,
+    SimpParams,
+    SimpOptions,
+    SolveOptions,
+    SolverNonConvergence,
+    device_fma_peaks,
+    fea_build_reduced,
+    kernel_launches,
+    fea_matfree_apply,
+    fea_solve_mgcg_matfree,
+    hex8_stiffness,
+    lib,
+    library_path,
+    make_density_filter,
+    oc_update,
+    simp_compliance,
+    simp_optimize,
+    PREC_FP64,
+    PREC_MIXED,
+    SOLVER_MGCG,
+    SOLVER_JACOBI_CG,
+)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

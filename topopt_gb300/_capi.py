@@ -1,0 +1,474 @@
+"""ctypes binding of libtopopt_gb300.so (include/topopt_gb300.h).
+
+Names follow the reference library (core/include/topopt/fea.hpp, simp.hpp):
+``hex8_stiffness``, ``fea_matfree_apply``, ``fea_solve_mgcg_matfree``,
+``simp_compliance``, ``make_density_filter`` (+ ``filter_density`` /
+``filter_sensitivity``), ``oc_update``, ``simp_optimize``.  Errors map the
+reference's exception classes: ``ValueError`` for std::invalid_argument,
+``RuntimeError`` for std::runtime_error (void-gate rejections),
+``SolverNonConvergence`` (iterations, residual) for the solver's own exception.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, "libtopopt_gb300.so")
+
+TG_OK, TG_EINVAL, TG_ESINGULAR, TG_ENONCONV, TG_EDEADLINE, TG_EDEVICE, TG_ENOMEM, TG_ECANCELLED = range(8)
+SOLVER_MGCG, SOLVER_JACOBI_CG = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class LibraryMissing(RuntimeError):
+    """The CUDA library has not been built (run topopt_gb300.build.build())."""
+
+
+class DeviceError(RuntimeError):
+    """A CUDA error inside the library."""
+
+
+class SolverNonConvergence(RuntimeError):
+    """The solve did not reach its tolerance (fea.hpp:418-426)."""
+
+    def __init__(self, msg, iterations=0, residual=0.0):
+        super().__init__(msg)
+        self.iterations = iterations
+        self.residual = residual
+
+
+# ----------------------------------------------------------------- structs
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("spacing", C.c_double), ("tags", C.c_void_p)]
+
+
+class _Bc(C.Structure):
+    _fields_ = [("node", C.c_int32), ("component", C.c_int32), ("value", C.c_double)]
+
+
+class _Params(C.Structure):
+    _fields_ = [("youngs_modulus", C.c_double), ("poisson", C.c_double), ("penalty", C.c_double),
+                ("density_min", C.c_double), ("material_law", C.c_int32), ("e_min", C.c_double)]
+
+
+class _SolveOpt(C.Structure):
+    _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("mg_levels", C.c_int32),
+                ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
+                ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class _CgInfo(C.Structure):
+    _fields_ = [("converged", C.c_int32), ("iterations", C.c_int32), ("residual", C.c_double),
+                ("used_multigrid", C.c_int32), ("mg_levels", C.c_int32),
+                ("hier_built", C.c_int32), ("mg_cycles_attempted", C.c_int32),
+                ("matvecs", C.c_int64), ("matvecs_lowp", C.c_int64),
+                ("refinements", C.c_int32), ("ng", C.c_int32), ("t_build_ms", C.c_double),
+                ("t_mg_build_ms", C.c_double), ("t_solve_ms", C.c_double),
+                ("t_total_ms", C.c_double)]
+
+
+class _SimpOpt(C.Structure):
+    _fields_ = [("volume_fraction", C.c_double), ("filter_radius", C.c_double),
+                ("move", C.c_double), ("change_tol", C.c_double), ("cg_tolerance", C.c_double),
+                ("max_iterations", C.c_int32), ("cg_max_iterations", C.c_int32),
+                ("solve", _SolveOpt)]
+
+
+class _Iter(C.Structure):
+    _fields_ = [("iteration", C.c_int32), ("compliance", C.c_double), ("change", C.c_double),
+                ("volume_fraction", C.c_double), ("cg_iterations", C.c_int32),
+                ("mg_levels", C.c_int32), ("used_multigrid", C.c_int32),
+                ("oc_volume_evals", C.c_int32), ("t_filter_ms", C.c_double),
+                ("t_solve_ms", C.c_double), ("t_sensitivity_ms", C.c_double),
+                ("t_update_ms", C.c_double), ("t_total_ms", C.c_double),
+                ("t_device_ms", C.c_double), ("fine_matvecs", C.c_int64),
+                ("fine_matvecs_lowp", C.c_int64)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("cancelled", C.c_int32),
+                ("infeasible", C.c_int32), ("non_convergent", C.c_int32),
+                ("compliance", C.c_double), ("initial_compliance", C.c_double),
+                ("volume_fraction", C.c_double)]
+
+
+_PROGRESS = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_double, C.c_double)
+
+# ------------------------------------------------------------------ loading
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """Load (once) and return the CUDA library; raises LibraryMissing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise LibraryMissing(f"{_LIB_PATH} is not built; run topopt_gb300.build.build()")
+    L = C.CDLL(_LIB_PATH)
+    vp, i32, dbl = C.c_void_p, C.c_int32, C.c_double
+    sig = {
+        "tg_last_error": ([], C.c_char_p),
+        "tg_set_device": ([i32], C.c_int),
+        "tg_version": ([], C.c_char_p),
+        "tg_hex8_stiffness": ([dbl, dbl, dbl, vp], C.c_int),
+        "tg_matfree_apply": ([vp, dbl, dbl, vp, i32, vp, vp], C.c_int),
+        "tg_build_reduced": ([vp, vp, dbl, vp, i32, vp, i32, vp, vp, vp, vp], C.c_int),
+        "tg_solve": ([vp, vp, dbl, vp, i32, vp, i32, dbl, i32, vp, vp, vp, vp, vp], C.c_int),
+        "tg_simp_compliance": ([vp, vp, vp, vp, i32, vp, i32, dbl, i32, vp, vp, vp, vp, vp],
+                               C.c_int),
+        "tg_filter": ([vp, dbl, i32, vp, vp], C.c_int),
+        "tg_oc_update": ([vp, dbl, vp, vp, dbl, dbl, dbl, vp], C.c_int),
+        "tg_simp_optimize": ([vp, vp, vp, i32, vp, i32, vp, _PROGRESS, vp, vp, vp, vp, vp, vp],
+                             C.c_int),
+        "tg_job_create": ([vp, vp, vp, i32, vp, i32, vp, vp], C.c_int),
+        "tg_job_step": ([vp, vp], C.c_int),
+        "tg_job_read": ([vp, vp, vp], C.c_int),
+        "tg_job_write_design": ([vp, vp], C.c_int),
+        "tg_job_device_bytes": ([vp], C.c_int64),
+        "tg_job_estimate_bytes": ([vp, vp], C.c_int64),
+        "tg_job_destroy": ([vp], None),
+        "tg_job_time_operator": ([vp, i32, i32, vp], C.c_int),
+        "tg_kernel_launches": ([], C.c_int64),
+        "tg_device_fma_peaks": ([vp, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc, info: "_CgInfo | None" = None):
+    if rc == TG_OK:
+        return
+    msg = lib().tg_last_error().decode()
+    if rc == TG_EINVAL:
+        raise ValueError(msg)
+    if rc == TG_ESINGULAR:
+        raise RuntimeError(msg)
+    if rc == TG_ENONCONV:
+        it = info.iterations if info is not None else 0
+        res = info.residual if info is not None else 0.0
+        raise SolverNonConvergence(msg, it, res)
+    if rc == TG_ENOMEM:
+        raise MemoryError(msg)
+    raise DeviceError(f"[{rc}] {msg}")
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    if n is not None and a.size != n:
+        raise ValueError(f"array size {a.size} != expected {n}")
+    return a
+
+
+# ------------------------------------------------------------------- types
+class Problem:
+    """VoxelGrid + Dirichlet BCs + nodal loads, in the reference's indexing
+    (voxel (k*ny+j)*nx+i, node (c*(ny+1)+b)*(nx+1)+a, DOF 3*node+comp)."""
+
+    def __init__(self, nx, ny, nz, spacing=1.0, tags=None, bcs=(), loads=()):
+        self.nx, self.ny, self.nz, self.spacing = int(nx), int(ny), int(nz), float(spacing)
+        self.nv = self.nx * self.ny * self.nz
+        self.nnodes = (self.nx + 1) * (self.ny + 1) * (self.nz + 1)
+        self.ndof = 3 * self.nnodes
+        self.tags = None if tags is None else np.ascontiguousarray(tags, dtype=np.uint8).ravel()
+        if self.tags is not None and self.tags.size != self.nv:
+            raise ValueError("tags size != voxel_count")
+        bcs, loads = list(bcs), list(loads)
+        self._bcs = (_Bc * max(1, len(bcs)))(*[_Bc(int(n), int(c), float(v)) for n, c, v in bcs])
+        self._loads = (_Bc * max(1, len(loads)))(*[_Bc(int(n), int(c), float(v)) for n, c, v in loads])
+        self.nbc, self.nloads = len(bcs), len(loads)
+        self.bcs, self.loads = bcs, loads
+        self._grid = _Grid(self.nx, self.ny, self.nz, self.spacing, _p(self.tags))
+
+    def node(self, a, b, c):
+        return (c * (self.ny + 1) + b) * (self.nx + 1) + a
+
+    def _args(self):
+        return (C.byref(self._grid), C.cast(self._bcs, C.c_void_p), self.nbc,
+                C.cast(self._loads, C.c_void_p), self.nloads)
+
+    @classmethod
+    def cantilever(cls, nx, ny, nz, total_load=-1.0, spacing=1.0, tags=None):
+        """The benchmark cantilever: every DOF of the x = 0 face clamped; a total
+        -z load spread equally over the x = nx edge nodes at mid-height."""
+        pb = cls(nx, ny, nz, spacing, tags)
+        bcs = [(pb.node(0, b, c), k, 0.0) for c in range(nz + 1) for b in range(ny + 1)
+               for k in range(3)]
+        nodes = [pb.node(nx, b, nz // 2) for b in range(ny + 1)]
+        loads = [(n, 2, total_load / len(nodes)) for n in nodes]
+        return cls(nx, ny, nz, spacing, tags, bcs, loads)
+
+
+@dataclass
+class SolveOptions:
+    solver: int = SOLVER_MGCG
+    precision: int = PREC_FP64
+    mg_levels: int = 0
+    mg_iter_budget: int = 0
+    omega: float = 0.0
+    inner_tolerance: float = 0.0
+    max_refinements: int = 0
+
+    def _c(self):
+        return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
+                         self.omega, self.inner_tolerance, self.max_refinements, 0)
+
+
+@dataclass
+class SimpParams:
+    youngs_modulus: float = 1.0
+    poisson: float = 0.3
+    penalty: float = 3.0
+    density_min: float = 1e-3
+    material_law: int = 0
+    e_min: float = 0.0
+
+    def _c(self):
+        return _Params(self.youngs_modulus, self.poisson, self.penalty, self.density_min,
+                       self.material_law, self.e_min)
+
+
+@dataclass
+class SimpOptions:
+    volume_fraction: float = 0.5
+    filter_radius: float = 1.5
+    move: float = 0.2
+    change_tol: float = 0.01
+    cg_tolerance: float = 1e-8
+    max_iterations: int = 200
+    cg_max_iterations: int = 0
+    solve: SolveOptions = field(default_factory=SolveOptions)
+
+    def _c(self):
+        return _SimpOpt(self.volume_fraction, self.filter_radius, self.move, self.change_tol,
+                        self.cg_tolerance, self.max_iterations, self.cg_max_iterations,
+                        self.solve._c())
+
+
+@dataclass
+class CgInfo:
+    converged: bool
+    iterations: int
+    residual: float
+    used_multigrid: bool
+    mg_levels: int
+    hier_built: bool
+    mg_cycles_attempted: int
+    matvecs: int
+    matvecs_lowp: int
+    refinements: int
+    ng: int
+    t_build_ms: float
+    t_mg_build_ms: float
+    t_solve_ms: float
+    t_total_ms: float
+
+    @classmethod
+    def _from(cls, c: _CgInfo):
+        return cls(bool(c.converged), c.iterations, c.residual, bool(c.used_multigrid),
+                   c.mg_levels, bool(c.hier_built), c.mg_cycles_attempted, c.matvecs,
+                   c.matvecs_lowp, c.refinements, c.ng, c.t_build_ms, c.t_mg_build_ms,
+                   c.t_solve_ms, c.t_total_ms)
+
+
+# --------------------------------------------------------------- functions
+def hex8_stiffness(youngs_modulus, poisson, element_size):
+    """hex_element.cpp:93-115: the 24x24 element stiffness (row-major)."""
+    ke = np.zeros(576)
+    _check(lib().tg_hex8_stiffness(youngs_modulus, poisson, element_size, _p(ke)))
+    return ke.reshape(24, 24)
+
+
+def fea_matfree_apply(pb: Problem, u, youngs_modulus=1.0, poisson=0.3, youngs_per_voxel=None,
+                      precision=PREC_FP64):
+    """fea.hpp:760-766: y = K u over the full grid (no BCs)."""
+    u = _f64(u, pb.ndof)
+    yv = None if youngs_per_voxel is None else _f64(youngs_per_voxel, pb.nv)
+    y = np.zeros(pb.ndof)
+    _check(lib().tg_matfree_apply(C.byref(pb._grid), youngs_modulus, poisson, _p(yv), precision,
+                                  _p(u), _p(y)))
+    return y
+
+
+def fea_build_reduced(pb: Problem, youngs_per_voxel=None, poisson=0.3):
+    """The void-DOF gate of mf_build_reduced: kept mask, reduced rhs, Jacobi
+    inverse diagonal (full length)."""
+    yv = None if youngs_per_voxel is None else _f64(youngs_per_voxel, pb.nv)
+    kept = np.zeros(pb.ndof, np.uint8)
+    rhs, inv = np.zeros(pb.ndof), np.zeros(pb.ndof)
+    ng = C.c_int32(0)
+    g, b, nb, l, nl = pb._args()
+    _check(lib().tg_build_reduced(g, _p(yv), poisson, b, nb, l, nl, _p(kept), _p(rhs), _p(inv),
+                                  C.byref(ng)))
+    return dict(kept=kept, rhs=rhs, invdiag=inv, ng=ng.value)
+
+
+def fea_solve_mgcg_matfree(pb: Problem, youngs_per_voxel, poisson=0.3, tolerance=1e-8,
+                           max_iterations=0, options: SolveOptions | None = None,
+                           active_mask=None, initial_guess=None):
+    """fea.hpp:707-715 (graded overload).  Returns (u, CgInfo)."""
+    yv = _f64(youngs_per_voxel, pb.nv)
+    am = None if active_mask is None else np.ascontiguousarray(active_mask, np.uint8).ravel()
+    ig = None if initial_guess is None else _f64(initial_guess, pb.ndof)
+    u = np.zeros(pb.ndof)
+    info = _CgInfo()
+    opt = (options or SolveOptions())._c()
+    g, b, nb, l, nl = pb._args()
+    rc = lib().tg_solve(g, _p(yv), poisson, b, nb, l, nl, tolerance, max_iterations,
+                        C.byref(opt), _p(am), _p(ig), _p(u), C.byref(info))
+    _check(rc, info)
+    return u, CgInfo._from(info)
+
+
+def simp_compliance(pb: Problem, params: SimpParams, density, tolerance=1e-8, max_iterations=0,
+                    options: SolveOptions | None = None):
+    """simp.hpp:247-255.  Returns dict(u, dcompliance, compliance, cg)."""
+    d = _f64(density, pb.nv)
+    u, dc = np.zeros(pb.ndof), np.zeros(pb.nv)
+    c = C.c_double(0.0)
+    info = _CgInfo()
+    prm = params._c()
+    opt = (options or SolveOptions())._c()
+    g, b, nb, l, nl = pb._args()
+    rc = lib().tg_simp_compliance(g, C.byref(prm), _p(d), b, nb, l, nl, tolerance, max_iterations,
+                                  C.byref(opt), _p(u), _p(dc), C.byref(c), C.byref(info))
+    _check(rc, info)
+    return dict(u=u, dcompliance=dc, compliance=c.value, cg=CgInfo._from(info))
+
+
+class DensityFilter:
+    """make_density_filter(grid, radius) (simp.cpp:834-896) over the solid voxels."""
+
+    def __init__(self, pb: Problem, radius: float):
+        self.pb, self.radius = pb, float(radius)
+
+    def filter_density(self, x):
+        x = _f64(x, self.pb.nv)
+        out = np.zeros(self.pb.nv)
+        _check(lib().tg_filter(C.byref(self.pb._grid), self.radius, 0, _p(x), _p(out)))
+        return out
+
+    def filter_sensitivity(self, s):
+        s = _f64(s, self.pb.nv)
+        out = np.zeros(self.pb.nv)
+        _check(lib().tg_filter(C.byref(self.pb._grid), self.radius, 1, _p(s), _p(out)))
+        return out
+
+
+def make_density_filter(pb: Problem, radius: float) -> DensityFilter:
+    if not (radius > 0.0):
+        raise ValueError("make_density_filter: radius must be > 0")
+    return DensityFilter(pb, radius)
+
+
+def oc_update(pb: Problem, filt: DensityFilter, density, dcompliance, volume_fraction, move=0.2,
+              density_min=1e-3):
+    """oc_update (simp.hpp:481-485): bit-identical to the reference."""
+    d, dc = _f64(density, pb.nv), _f64(dcompliance, pb.nv)
+    out = np.zeros(pb.nv)
+    _check(lib().tg_oc_update(C.byref(pb._grid), filt.radius, _p(d), _p(dc), volume_fraction, move,
+                              density_min, _p(out)))
+    return out
+
+
+def kernel_launches() -> int:
+    return int(lib().tg_kernel_launches())
+
+
+def device_fma_peaks():
+    """(fp64, fp32) sustained FMA TFLOP/s from the library's microbenchmark."""
+    a, b = C.c_double(0.0), C.c_double(0.0)
+    _check(lib().tg_device_fma_peaks(C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def _rows(hist, n):
+    keys = [f[0] for f in _Iter._fields_]
+    return [{k: getattr(hist[i], k) for k in keys} for i in range(n)]
+
+
+def simp_optimize(pb: Problem, params: SimpParams, options: SimpOptions, progress=None,
+                  cancel=None):
+    """simp.hpp:1783-1786 (OC, no projection).  ``cancel`` may be a one-element
+    int32 numpy array polled once per iteration."""
+    prm, opt = params._c(), options._c()
+    hist = (_Iter * options.max_iterations)()
+    design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+    res = _Result()
+    cb = _PROGRESS(lambda ctx, it, c, ch: progress(it, c, ch)) if progress else _PROGRESS()
+    cptr = None if cancel is None else cancel.ctypes.data_as(C.c_void_p)
+    g, b, nb, l, nl = pb._args()
+    rc = lib().tg_simp_optimize(g, C.byref(prm), b, nb, l, nl, C.byref(opt), cb, None, cptr,
+                                C.cast(hist, C.c_void_p), _p(design), _p(phys), C.byref(res))
+    _check(rc)
+    return dict(design=design, physical_density=phys, compliance=res.compliance,
+                initial_compliance=res.initial_compliance, volume_fraction=res.volume_fraction,
+                iterations=res.iterations, converged=bool(res.converged),
+                cancelled=bool(res.cancelled), infeasible=bool(res.infeasible),
+                non_convergent=bool(res.non_convergent), history=_rows(hist, res.iterations))
+
+
+class SimpJob:
+    """A resident optimisation job: density, displacement and the multigrid
+    hierarchy stay on the device between ``step()`` calls."""
+
+    def __init__(self, pb: Problem, params: SimpParams, options: SimpOptions):
+        self.pb = pb
+        self._prm, self._opt = params._c(), options._c()
+        self._h = C.c_void_p()
+        g, b, nb, l, nl = pb._args()
+        _check(lib().tg_job_create(g, C.byref(self._prm), b, nb, l, nl, C.byref(self._opt),
+                                   C.byref(self._h)))
+
+    def step(self):
+        row = _Iter()
+        _check(lib().tg_job_step(self._h, C.byref(row)))
+        return {f[0]: getattr(row, f[0]) for f in _Iter._fields_}
+
+    def read(self):
+        x, xp = np.zeros(self.pb.nv), np.zeros(self.pb.nv)
+        _check(lib().tg_job_read(self._h, _p(x), _p(xp)))
+        return x, xp
+
+    def write_design(self, x):
+        x = _f64(x, self.pb.nv)
+        _check(lib().tg_job_write_design(self._h, _p(x)))
+
+    def time_operator(self, precision=PREC_FP64, reps=20):
+        """Average device ms of one fine-operator launch (CUDA events)."""
+        ms = C.c_double(0.0)
+        _check(lib().tg_job_time_operator(self._h, precision, reps, C.byref(ms)))
+        return ms.value
+
+    @property
+    def device_bytes(self):
+        return int(lib().tg_job_device_bytes(self._h))
+
+    def close(self):
+        if self._h:
+            lib().tg_job_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,879 @@
+// api.cu -- the extern "C" boundary (include/topopt_gb300.h) and the resident
+// SIMP job.  Host code above the kernels: argument validation with the
+// reference's messages, the optimizer loop of simp_optimize
+// (core/src/simp/simp.cpp:2018-2592) and the OC bisection of oc_update
+// (simp.cpp:948-1025).
+//
+// OC bisection parity.  The reference compares a SEQUENTIAL FP64 sum of the
+// filtered candidate against the target (simp.cpp:1003-1016).  Here the volume
+// is summed exactly (192-bit fixed point, order independent).  The sequential
+// sum s differs from the exact sum S by at most gamma_{n-1} * S (n terms, all
+// non-negative), so when |S - target| exceeds that bound the branch is the
+// reference's for certain; otherwise the filtered candidate is copied to the
+// host and summed sequentially in grid order, exactly as the reference does.
+// With the candidate and the filter rounding like the reference (k_simp.cu),
+// every bisection branch -- and therefore x_new -- is bit-identical.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tg_solver.h"
+
+namespace tg {
+
+namespace {
+thread_local std::string g_err;
+int g_device = 0;
+std::atomic<int64_t> g_launches{0};
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+}  // namespace
+
+void raise(int code, const std::string& msg) { throw Error(code, msg); }
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "CUDA error %d (%s) in %s at %s:%d", int(e), cudaGetErrorString(e),
+                what, file, line);
+  throw Error(e == cudaErrorMemoryAllocation ? TG_ENOMEM : TG_EDEVICE, buf);
+}
+
+template <class F>
+int guarded(F&& fn) {
+  try {
+    TG_CUDA(cudaSetDevice(g_device));
+    fn();
+    return TG_OK;
+  } catch (const Error& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return TG_ENOMEM;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return TG_EINVAL;
+  }
+}
+
+// A stream that lives for one call.
+struct CallStream {
+  cudaStream_t s = nullptr;
+  CallStream() { TG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+  ~CallStream() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+template <class T>
+void upload(DBuf<T>& d, const T* h, size_t n, cudaStream_t s) {
+  d.alloc(n);
+  TG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+void validate_grid(const tg_grid* g) {
+  if (!g) raise(TG_EINVAL, "grid is null");
+  if (g->nx < 1 || g->ny < 1 || g->nz < 1) raise(TG_EINVAL, "grid dimensions must be >= 1");
+  if (!(g->spacing > 0.0)) raise(TG_EINVAL, "grid spacing must be > 0");
+  if (int64_t(g->nx + 1) * (g->ny + 1) * (g->nz + 1) * 3 > (int64_t(1) << 31) - 1)
+    raise(TG_EINVAL, "grid too large: DOF indices must fit a 32-bit int");
+}
+
+// SimpParams checks (simp.cpp:34-41).
+void validate_params(const tg_simp_params* p) {
+  if (!p) raise(TG_EINVAL, "params is null");
+  if (!(p->youngs_modulus > 0.0)) raise(TG_EINVAL, "simp: youngs_modulus (E0) must be > 0");
+  if (!(p->penalty > 0.0)) raise(TG_EINVAL, "simp: penalty (p) must be > 0");
+  if (!(p->density_min > 0.0 && p->density_min <= 1.0))
+    raise(TG_EINVAL, "simp: density_min must be in (0, 1]");
+  if (p->material_law != 0 && p->material_law != 1)
+    raise(TG_EINVAL, "simp: material_law must be 0 (reference) or 1 (modified)");
+  if (p->material_law == 1 && !(p->e_min > 0.0 && p->e_min < p->youngs_modulus))
+    raise(TG_EINVAL, "simp: e_min must be in (0, E0) for the modified law");
+}
+
+tg_solve_options default_solve(const tg_solve_options* o) {
+  tg_solve_options d;
+  std::memset(&d, 0, sizeof d);
+  if (o) d = *o;
+  if (d.solver != TG_SOLVER_MGCG && d.solver != TG_SOLVER_JACOBI_CG)
+    raise(TG_EINVAL, "solve options: unknown solver kind");
+  if (d.precision != TG_PREC_FP64 && d.precision != TG_PREC_MIXED)
+    raise(TG_EINVAL, "solve options: unknown precision");
+  if (d.precision == TG_PREC_MIXED && d.solver != TG_SOLVER_MGCG)
+    raise(TG_EINVAL, "solve options: mixed precision needs the multigrid solver");
+  return d;
+}
+
+void fill_info(tg_cg_info* info, const SolverStats& st, const FineProblem& fp, double t_build,
+               double t_total) {
+  if (!info) return;
+  std::memset(info, 0, sizeof *info);
+  info->converged = st.converged;
+  info->iterations = st.iterations;
+  info->residual = st.residual;
+  info->used_multigrid = st.used_mg;
+  info->mg_levels = st.mg_levels;
+  info->hier_built = st.hier_built;
+  info->mg_cycles_attempted = st.mg_cycles;
+  info->matvecs = st.matvecs;
+  info->matvecs_lowp = st.matvecs_lowp;
+  info->refinements = st.refinements;
+  info->ng = int32_t(fp.ng);
+  info->t_build_ms = t_build;
+  info->t_mg_build_ms = st.t_mg_build_ms;
+  info->t_solve_ms = st.t_solve_ms;
+  info->t_total_ms = t_total;
+}
+
+// ------------------------------------------------------------ filter state
+struct FilterState {
+  FilterStencil st;
+  DBuf<unsigned char> st_buf;
+  const void* st_dev = nullptr;
+  DBuf<double> hs, tmp;
+  void init(const Grid& g, double radius, const uint8_t* act, cudaStream_t s) {
+    if (!(radius > 0.0)) raise(TG_EINVAL, "make_density_filter: radius must be > 0");
+    st = FilterStencil::make(radius);
+    st_dev = filter_stencil_device(st, st_buf, s);
+    hs.alloc(size_t(g.nv));
+    tmp.alloc(size_t(g.nv));
+    launch_weight_sum(g, st_dev, st.n, act, hs.p, s);
+  }
+  void fwd(const Grid& g, const uint8_t* act, const double* x, double* out, cudaStream_t s) {
+    launch_filter_fwd(g, st_dev, st.n, act, hs.p, x, out, s);
+  }
+  void adj(const Grid& g, const uint8_t* act, const double* x, double* out, cudaStream_t s) {
+    launch_filter_adj(g, st_dev, st.n, act, hs.p, x, tmp.p, out, s);
+  }
+  size_t bytes() const { return st_buf.bytes() + hs.bytes() + tmp.bytes(); }
+};
+
+// ------------------------------------------------------------ OC update
+struct OcState {
+  DBuf<double> dcf, dvf, xp;
+  DBuf<uint64_t> part, total;
+  DBuf<int> inexact;
+  uint64_t* h_total = nullptr;  // pinned: 3 limbs + flag
+  std::vector<double> h_xp;
+  int64_t n_solid = 0;
+  int fallbacks = 0, evals = 0;
+  void init(const Grid& g, cudaStream_t) {
+    dcf.alloc(size_t(g.nv));
+    dvf.alloc(size_t(g.nv));
+    xp.alloc(size_t(g.nv));
+    part.alloc(size_t(3 * exact_sum_blocks()));
+    total.alloc(3);
+    inexact.alloc(1);
+    TG_CUDA(cudaMallocHost(&h_total, 4 * sizeof(uint64_t)));
+  }
+  ~OcState() {
+    if (h_total) cudaFreeHost(h_total);
+  }
+  size_t bytes() const {
+    return dcf.bytes() + dvf.bytes() + xp.bytes() + part.bytes() + total.bytes() + inexact.bytes();
+  }
+};
+
+// Exact sum of v over the active voxels, as a double (3 roundings of the exact
+// 192-bit value); *exact tells whether every term was representable.
+double exact_volume(OcState& oc, const Grid& g, const uint8_t* act, const double* v, bool* exact,
+                    cudaStream_t s) {
+  TG_CUDA(cudaMemsetAsync(oc.inexact.p, 0, sizeof(int), s));
+  launch_exact_sum(v, act, g.nv, oc.part.p, oc.total.p, oc.inexact.p, s);
+  TG_CUDA(cudaMemcpyAsync(oc.h_total, oc.total.p, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  TG_CUDA(cudaMemcpyAsync(oc.h_total + 3, oc.inexact.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+  *exact = (reinterpret_cast<const int*>(oc.h_total + 3)[0] == 0);
+  return double(oc.h_total[2]) + std::ldexp(double(oc.h_total[1]), -64) +
+         std::ldexp(double(oc.h_total[0]), -128);
+}
+
+// phys_vol(candidate) > target, decided exactly as the reference's sequential
+// sum would decide it (see the file comment).
+bool volume_exceeds(OcState& oc, const Grid& g, const uint8_t* act,
+                    const std::vector<uint8_t>& act_h, double target, cudaStream_t s) {
+  ++oc.evals;
+  bool exact = false;
+  const double S = exact_volume(oc, g, act, oc.xp.p, &exact, s);
+  if (exact && std::isfinite(S)) {
+    const double u = std::ldexp(1.0, -53);
+    const double n1 = double(std::max<int64_t>(oc.n_solid - 1, 0));
+    const double gamma = n1 * u / (1.0 - n1 * u);
+    const double bound = gamma * S * 1.0000001 + 8.0 * u * S + 1e-300;
+    if (S - target > bound) return true;
+    if (target - S > bound) return false;
+  }
+  ++oc.fallbacks;
+  oc.h_xp.resize(size_t(g.nv));
+  TG_CUDA(cudaMemcpyAsync(oc.h_xp.data(), oc.xp.p, size_t(g.nv) * sizeof(double),
+                          cudaMemcpyDeviceToHost, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+  double v = 0.0;
+  for (int64_t e = 0; e < g.nv; ++e)
+    if (act_h[size_t(e)]) v += oc.h_xp[size_t(e)];
+  return v > target;
+}
+
+// oc_update (simp.cpp:948-1025) on device-resident fields; dvf must hold the
+// filtered unit volume sensitivity.
+void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t* act,
+                      const std::vector<uint8_t>& act_h, const double* x, const double* dc,
+                      double volfrac, double move, double rho_min, double* xnew, cudaStream_t s) {
+  fs.adj(g, act, dc, oc.dcf.p, s);
+  const double target = volfrac * double(oc.n_solid);
+  auto eval = [&](double lam) {
+    launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, lam, move, rho_min, xnew, s);
+    fs.fwd(g, act, xnew, oc.xp.p, s);
+    return volume_exceeds(oc, g, act, act_h, target, s);
+  };
+  double l1 = 0.0, l2 = 1.0;
+  while (l2 < 1e30 && eval(l2)) l2 *= 2.0;
+  for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
+    const double lmid = 0.5 * (l1 + l2);
+    if (eval(lmid))
+      l1 = lmid;
+    else
+      l2 = lmid;
+  }
+  launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, 0.5 * (l1 + l2), move, rho_min, xnew, s);
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+// ------------------------------------------------------------------ the job
+struct tg_job {
+  cudaStream_t s = nullptr;
+  tg_simp_params params{};
+  tg_simp_options opt{};
+  FineProblem fp;
+  std::unique_ptr<Solver> solver;
+  FilterState filt;
+  OcState oc;
+  DBuf<uint8_t> solid;
+  std::vector<uint8_t> solid_h;
+  DBuf<double> x, xnew, xphys, E, u, dc, part, scal;
+  double* h_scal = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int64_t n_solid = 0;
+  int iteration = 0;
+  bool xphys_valid = false;
+  std::vector<double> hist_c;
+  std::vector<int> hist_cg;
+
+  ~tg_job() {
+    solver.reset();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (h_scal) cudaFreeHost(h_scal);
+    if (s) cudaStreamDestroy(s);
+  }
+  size_t bytes() const {
+    size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes();
+    for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal}) b += d->bytes();
+    return b + (solver ? solver->device_bytes() : 0);
+  }
+};
+
+namespace tg {
+namespace {
+
+void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
+              const tg_dirichlet_bc* bcs, int nbc, const tg_nodal_load* loads, int nloads,
+              const tg_simp_options* options) {
+  validate_grid(grid);
+  validate_params(params);
+  if (!options) raise(TG_EINVAL, "options is null");
+  const tg_simp_options& o = *options;
+  if (!(o.volume_fraction > 0.0 && o.volume_fraction <= 1.0))
+    raise(TG_EINVAL, "simp_optimize: volume_fraction must be in (0, 1]");
+  if (!(o.move > 0.0)) raise(TG_EINVAL, "simp_optimize: move must be > 0");
+  if (o.max_iterations < 1) raise(TG_EINVAL, "simp_optimize: max_iterations must be >= 1");
+  if (o.change_tol < 0.0) raise(TG_EINVAL, "simp_optimize: change_tol must be >= 0");
+  if (!(o.filter_radius > 0.0)) raise(TG_EINVAL, "make_density_filter: radius must be > 0");
+  if (!(o.cg_tolerance > 0.0)) raise(TG_EINVAL, "simp_optimize: cg_tolerance must be > 0");
+  j->params = *params;
+  j->opt = o;
+  j->opt.solve = default_solve(&o.solve);
+  TG_CUDA(cudaStreamCreateWithFlags(&j->s, cudaStreamNonBlocking));
+  TG_CUDA(cudaEventCreate(&j->ev0));
+  TG_CUDA(cudaEventCreate(&j->ev1));
+  cudaStream_t s = j->s;
+  j->fp.build(*grid, params->poisson, bcs, nbc, loads, nloads, nullptr, s);
+  const Grid& g = j->fp.g;
+  j->solver = std::make_unique<Solver>(j->fp, j->opt.solve, s);
+  j->solid_h = j->fp.elem_h;  // no active mask on this path: elem == solid
+  j->n_solid = 0;
+  for (uint8_t v : j->solid_h) j->n_solid += v;
+  upload(j->solid, j->solid_h.data(), j->solid_h.size(), s);
+  for (DBuf<double>* d : {&j->x, &j->xnew, &j->xphys, &j->E, &j->dc}) d->alloc(size_t(g.nv));
+  j->u.alloc(size_t(g.ndof));
+  j->part.alloc(size_t(4 * kRedBlocks + 152 * 32));
+  j->scal.alloc(8);
+  TG_CUDA(cudaMallocHost(&j->h_scal, 8 * sizeof(double)));
+  j->filt.init(g, o.filter_radius, j->solid.p, s);
+  j->oc.init(g, s);
+  j->oc.n_solid = j->n_solid;
+  // dv = filter_sensitivity(ones on solid voxels) (simp.cpp:967-976): fixed.
+  std::vector<double> ones(size_t(g.nv));
+  for (int64_t e = 0; e < g.nv; ++e) ones[size_t(e)] = j->solid_h[size_t(e)] ? 1.0 : 0.0;
+  TG_CUDA(cudaMemcpyAsync(j->xnew.p, ones.data(), j->xnew.bytes(), cudaMemcpyHostToDevice, s));
+  j->filt.adj(g, j->solid.p, j->xnew.p, j->oc.dvf.p, s);
+  // simp_uniform_density (simp.cpp:305-312).
+  for (int64_t e = 0; e < g.nv; ++e) ones[size_t(e)] = j->solid_h[size_t(e)] ? o.volume_fraction : 0.0;
+  TG_CUDA(cudaMemcpyAsync(j->x.p, ones.data(), j->x.bytes(), cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+}
+
+double read1(tg_job* j, const double* dptr) {
+  TG_CUDA(cudaMemcpyAsync(j->h_scal, dptr, sizeof(double), cudaMemcpyDeviceToHost, j->s));
+  TG_CUDA(cudaStreamSynchronize(j->s));
+  return j->h_scal[0];
+}
+
+// Compliance + dc at the current physical density and displacement.
+double job_sensitivity(tg_job* j) {
+  const Grid& g = j->fp.g;
+  const tg_simp_params& p = j->params;
+  int nparts = 0;
+  launch_sensitivity(g, j->fp.mc, j->xphys.p, j->fp.elem.p, j->u.p, p.youngs_modulus, p.penalty,
+                     p.density_min, p.material_law, p.e_min, j->dc.p, j->part.p, &nparts, j->s);
+  launch_sum_partials(j->part.p, nparts, j->scal.p, j->s);
+  return read1(j, j->scal.p);
+}
+
+// Penalised solve at the current physical density.
+SolverStats job_solve(tg_job* j, double tol, int max_it) {
+  const Grid& g = j->fp.g;
+  const tg_simp_params& p = j->params;
+  launch_modulus(j->xphys.p, j->fp.elem.p, g.nv, p.youngs_modulus, p.penalty, p.density_min,
+                 p.material_law, p.e_min, j->E.p, j->s);
+  j->solver->set_modulus(j->E.p);
+  return j->solver->solve(tol, max_it, nullptr, j->u.p);
+}
+
+void job_filter_x(tg_job* j) {
+  j->filt.fwd(j->fp.g, j->solid.p, j->x.p, j->xphys.p, j->s);
+  j->xphys_valid = true;
+}
+
+// One design iteration of simp_optimize's loop body (simp.cpp:2158-2340).
+int job_step(tg_job* j, tg_simp_iteration* row) {
+  const Grid& g = j->fp.g;
+  const tg_simp_options& o = j->opt;
+  tg_simp_iteration r;
+  std::memset(&r, 0, sizeof r);
+  const double t0 = now_ms();
+  TG_CUDA(cudaEventRecord(j->ev0, j->s));
+  if (!j->xphys_valid) job_filter_x(j);
+  TG_CUDA(cudaStreamSynchronize(j->s));
+  const double t1 = now_ms();
+  SolverStats st = job_solve(j, o.cg_tolerance, o.cg_max_iterations);
+  const double t2 = now_ms();
+  if (!st.converged) {
+    Error e(TG_ENONCONV, "simp_optimize: the trajectory solve did not reach the requested tolerance");
+    e.iterations = st.iterations;
+    e.residual = st.residual;
+    throw e;
+  }
+  const double c = job_sensitivity(j);
+  const double t3 = now_ms();
+  const int fb0 = j->oc.evals;
+  oc_update_device(j->oc, j->filt, g, j->solid.p, j->solid_h, j->x.p, j->dc.p, o.volume_fraction,
+                   o.move, j->params.density_min, j->xnew.p, j->s);
+  launch_absdiff_max(j->xnew.p, j->x.p, g.nv, j->part.p, j->scal.p + 1, j->s);
+  const double change = read1(j, j->scal.p + 1);
+  std::swap(j->x.p, j->xnew.p);
+  job_filter_x(j);
+  bool exact = false;
+  const double vol = exact_volume(j->oc, g, j->solid.p, j->xphys.p, &exact, j->s);
+  TG_CUDA(cudaEventRecord(j->ev1, j->s));
+  TG_CUDA(cudaEventSynchronize(j->ev1));
+  float dev_ms = 0.0f;
+  TG_CUDA(cudaEventElapsedTime(&dev_ms, j->ev0, j->ev1));
+  const double t4 = now_ms();
+  j->iteration += 1;
+  r.iteration = j->iteration;
+  r.compliance = c;
+  r.change = change;
+  r.volume_fraction = j->n_solid > 0 ? vol / double(j->n_solid) : 0.0;
+  r.cg_iterations = st.iterations;
+  r.mg_levels = st.mg_levels;
+  r.used_multigrid = st.used_mg;
+  r.oc_volume_evals = j->oc.evals - fb0;
+  r.t_filter_ms = t1 - t0;
+  r.t_solve_ms = t2 - t1;
+  r.t_sensitivity_ms = t3 - t2;
+  r.t_update_ms = t4 - t3;
+  r.t_total_ms = t4 - t0;
+  r.t_device_ms = dev_ms;
+  r.fine_matvecs = st.matvecs;
+  r.fine_matvecs_lowp = st.matvecs_lowp;
+  j->hist_c.push_back(c);
+  j->hist_cg.push_back(st.iterations);
+  if (row) *row = r;
+  return TG_OK;
+}
+
+// rung_infeasible (simp.cpp:1140-1186) at the SimpOptions defaults
+// (simp.hpp:1299-1302): ratio 100, CG blow-up 4, flat 1e-3, window 5.
+bool rung_infeasible(const std::vector<double>& c, const std::vector<int>& cg) {
+  const int window = 5;
+  const int n = int(c.size());
+  if (n < window + 1) return false;
+  if (!(std::isfinite(c[0]) && c[0] > 0.0)) return false;
+  int cgmin = cg[0];
+  for (int i = 1; i < n - window; ++i) cgmin = std::min(cgmin, cg[size_t(i)]);
+  if (cgmin <= 0) return false;
+  const double cbar = 100.0 * c[0], cgbar = 4.0 * double(cgmin);
+  double lo = c[size_t(n - window)], hi = lo;
+  for (int i = n - window; i < n; ++i) {
+    if (!std::isfinite(c[size_t(i)])) return false;
+    if (!(c[size_t(i)] >= cbar)) return false;
+    if (!(double(cg[size_t(i)]) >= cgbar)) return false;
+    lo = std::min(lo, c[size_t(i)]);
+    hi = std::max(hi, c[size_t(i)]);
+  }
+  if (!(lo > 0.0)) return false;
+  return (hi - lo) / lo <= 1e-3;
+}
+
+}  // namespace
+}  // namespace tg
+
+// ================================================================= C ABI
+extern "C" {
+
+const char* tg_last_error(void) { return tg::g_err.c_str(); }
+
+int tg_set_device(int32_t device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    tg::g_err = "tg_set_device: no such CUDA device";
+    return TG_EINVAL;
+  }
+  tg::g_device = device;
+  return TG_OK;
+}
+
+const char* tg_version(void) { return "topopt_gb300 0.1 (sm_103a)"; }
+
+int tg_hex8_stiffness(double E, double nu, double h, double* ke) {
+  try {
+    if (!ke) raise(TG_EINVAL, "ke is null");
+    if (!(E > 0.0)) raise(TG_EINVAL, "hex8_stiffness: youngs_modulus must be > 0");
+    if (!(h > 0.0)) raise(TG_EINVAL, "hex8_stiffness: element_size must be > 0");
+    if (!(nu > -1.0 && nu < 0.5)) raise(TG_EINVAL, "hex8_stiffness: poisson must be in (-1, 0.5)");
+    hex8_ke(E, nu, h, ke);
+    return TG_OK;
+  } catch (const Error& e) {
+    tg::g_err = e.what();
+    return e.code;
+  }
+}
+
+int tg_matfree_apply(const tg_grid* grid, double E, double nu, const double* youngs,
+                     int32_t precision, const double* u, double* y) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!u || !y) raise(TG_EINVAL, "u and y must be non-null");
+    if (!youngs && !(E > 0.0)) raise(TG_EINVAL, "hex8_stiffness: youngs_modulus must be > 0");
+    if (!(nu > -1.0 && nu < 0.5)) raise(TG_EINVAL, "hex8_stiffness: poisson must be in (-1, 0.5)");
+    CallStream cs;
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    std::vector<double> f(size_t(g.nv), 0.0);
+    for (int64_t e = 0; e < g.nv; ++e) {
+      const bool sol = grid->tags == nullptr || grid->tags[e] != 0;
+      if (!sol) continue;
+      f[size_t(e)] = youngs ? youngs[e] : E;
+      if (youngs && !(youngs[e] > 0.0))
+        raise(TG_EINVAL,
+              "fea_matfree_apply: per-voxel Young's modulus must be > 0 on a solid voxel");
+    }
+    ModalConsts mc = ModalConsts::make(nu, g.h);
+    DBuf<double> df, du, dy;
+    upload(df, f.data(), f.size(), cs.s);
+    upload(du, u, size_t(g.ndof), cs.s);
+    dy.alloc(size_t(g.ndof));
+    if (precision == TG_PREC_MIXED) {
+      DBuf<float> ff(size_t(g.nv)), fu(size_t(g.ndof)), fy(size_t(g.ndof));
+      launch_copy_d2f(ff.p, df.p, g.nv, cs.s);
+      launch_copy_d2f(fu.p, du.p, g.ndof, cs.s);
+      launch_fine_op<float>(kApply, g, mc, ff.p, nullptr, fu.p, nullptr, nullptr, 0.0f, fy.p,
+                            nullptr, nullptr, cs.s);
+      std::vector<float> hy(size_t(g.ndof));
+      TG_CUDA(cudaMemcpyAsync(hy.data(), fy.p, fy.bytes(), cudaMemcpyDeviceToHost, cs.s));
+      TG_CUDA(cudaStreamSynchronize(cs.s));
+      for (int64_t d = 0; d < g.ndof; ++d) y[d] = double(hy[size_t(d)]);
+      return;
+    }
+    launch_fine_op<double>(kApply, g, mc, df.p, nullptr, du.p, nullptr, nullptr, 0.0, dy.p,
+                           nullptr, nullptr, cs.s);
+    TG_CUDA(cudaMemcpyAsync(y, dy.p, dy.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+}
+
+int tg_build_reduced(const tg_grid* grid, const double* youngs, double nu,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, uint8_t* kept, double* rhs, double* invdiag,
+                     int32_t* ng_out) {
+  return guarded([&] {
+    validate_grid(grid);
+    CallStream cs;
+    FineProblem fp;
+    fp.build(*grid, nu, bcs, nbc, loads, nloads, nullptr, cs.s);
+    const Grid& g = fp.g;
+    std::vector<double> f(size_t(g.nv), 0.0);
+    for (int64_t e = 0; e < g.nv; ++e)
+      if (fp.elem_h[size_t(e)]) {
+        f[size_t(e)] = youngs ? youngs[e] : 1.0;
+        if (!(f[size_t(e)] > 0.0))
+          raise(TG_EINVAL, "per-voxel Young's modulus must be > 0 on a solid voxel");
+      }
+    DBuf<double> dE;
+    upload(dE, f.data(), f.size(), cs.s);
+    tg_solve_options so;
+    std::memset(&so, 0, sizeof so);
+    so.solver = TG_SOLVER_JACOBI_CG;
+    Solver sv(fp, so, cs.s);
+    sv.set_modulus(dE.p);
+    std::vector<double> tmp(size_t(g.ndof));
+    if (rhs) {
+      TG_CUDA(cudaMemcpyAsync(rhs, sv.rhs(), size_t(g.ndof) * sizeof(double),
+                              cudaMemcpyDeviceToHost, cs.s));
+    }
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+    if (kept) std::memcpy(kept, fp.kept_h.data(), size_t(g.ndof));
+    if (invdiag) {
+      DBuf<double> inv(size_t(g.ndof));
+      launch_fine_invdiag(g, fp.mc.kdiag, dE.p, fp.kept.p, inv.p, cs.s);
+      TG_CUDA(cudaMemcpyAsync(invdiag, inv.p, inv.bytes(), cudaMemcpyDeviceToHost, cs.s));
+      TG_CUDA(cudaStreamSynchronize(cs.s));
+    }
+    if (ng_out) *ng_out = int32_t(fp.ng);
+  });
+}
+
+int tg_solve(const tg_grid* grid, const double* youngs, double nu, const tg_dirichlet_bc* bcs,
+             int32_t nbc, const tg_nodal_load* loads, int32_t nloads, double tol, int32_t max_it,
+             const tg_solve_options* options, const uint8_t* active_mask, const double* guess,
+             double* u_out, tg_cg_info* info) {
+  SolverStats st;
+  FineProblem fp;
+  double t_build = 0.0;
+  const double t0 = now_ms();
+  const int rc = guarded([&] {
+    validate_grid(grid);
+    if (!youngs || !u_out) raise(TG_EINVAL, "youngs_per_voxel and u_out must be non-null");
+    const tg_solve_options so = default_solve(options);
+    CallStream cs;
+    fp.build(*grid, nu, bcs, nbc, loads, nloads, active_mask, cs.s);
+    const Grid& g = fp.g;
+    std::vector<double> f(size_t(g.nv), 0.0);
+    for (int64_t e = 0; e < g.nv; ++e)
+      if (fp.elem_h[size_t(e)]) {
+        f[size_t(e)] = youngs[e];
+        if (!(youngs[e] > 0.0))
+          raise(TG_EINVAL,
+                "fea_solve_mgcg_matfree: per-voxel Young's modulus must be > 0 on a solid voxel");
+      }
+    DBuf<double> dE, du, dg;
+    upload(dE, f.data(), f.size(), cs.s);
+    du.alloc(size_t(g.ndof));
+    if (guess) upload(dg, guess, size_t(g.ndof), cs.s);
+    Solver sv(fp, so, cs.s);
+    const double tb = now_ms();
+    sv.set_modulus(dE.p);
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+    st = sv.solve(tol, max_it, guess ? dg.p : nullptr, du.p);
+    st.t_mg_build_ms = now_ms() - tb - st.t_solve_ms;
+    t_build = tb - t0;
+    if (!st.converged) {
+      Error e(TG_ENONCONV,
+              "fea_solve_mgcg_matfree: CG did not reach the requested tolerance within "
+              "max_iterations");
+      throw e;
+    }
+    TG_CUDA(cudaMemcpyAsync(u_out, du.p, du.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+  fill_info(info, st, fp, t_build, now_ms() - t0);
+  return rc;
+}
+
+int tg_simp_compliance(const tg_grid* grid, const tg_simp_params* params, const double* density,
+                       const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                       int32_t nloads, double tol, int32_t max_it,
+                       const tg_solve_options* options, double* u_out, double* dc_out,
+                       double* compliance_out, tg_cg_info* info) {
+  SolverStats st;
+  std::unique_ptr<tg_job> jp;
+  const double t0 = now_ms();
+  const int rc = guarded([&] {
+    validate_grid(grid);
+    validate_params(params);
+    if (!density) raise(TG_EINVAL, "density is null");
+    tg_simp_options o;
+    std::memset(&o, 0, sizeof o);
+    o.volume_fraction = 0.5;
+    o.filter_radius = 1.5;
+    o.move = 0.2;
+    o.max_iterations = 1;
+    o.cg_tolerance = tol > 0.0 ? tol : 1e-8;
+    o.cg_max_iterations = max_it;
+    if (options) o.solve = *options;
+    jp = std::make_unique<tg_job>();
+    job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, &o);
+    tg_job* j = jp.get();
+    const Grid& g = j->fp.g;
+    TG_CUDA(cudaMemcpyAsync(j->xphys.p, density, j->xphys.bytes(), cudaMemcpyHostToDevice, j->s));
+    j->xphys_valid = true;
+    st = job_solve(j, o.cg_tolerance, max_it);
+    if (!st.converged) raise(TG_ENONCONV, "simp_compliance: CG did not reach the requested tolerance");
+    const double c = job_sensitivity(j);
+    if (compliance_out) *compliance_out = c;
+    if (u_out)
+      TG_CUDA(cudaMemcpyAsync(u_out, j->u.p, j->u.bytes(), cudaMemcpyDeviceToHost, j->s));
+    if (dc_out)
+      TG_CUDA(cudaMemcpyAsync(dc_out, j->dc.p, size_t(g.nv) * sizeof(double),
+                              cudaMemcpyDeviceToHost, j->s));
+    TG_CUDA(cudaStreamSynchronize(j->s));
+  });
+  if (jp) fill_info(info, st, jp->fp, 0.0, now_ms() - t0);
+  return rc;
+}
+
+int tg_filter(const tg_grid* grid, double radius, int32_t adjoint, const double* x, double* out) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!x || !out) raise(TG_EINVAL, "x and out must be non-null");
+    CallStream cs;
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    std::vector<uint8_t> act(size_t(g.nv));
+    for (int64_t e = 0; e < g.nv; ++e) act[size_t(e)] = grid->tags == nullptr || grid->tags[e] != 0;
+    DBuf<uint8_t> dact;
+    DBuf<double> dx, dout(size_t(g.nv));
+    upload(dact, act.data(), act.size(), cs.s);
+    upload(dx, x, size_t(g.nv), cs.s);
+    FilterState fs;
+    fs.init(g, radius, dact.p, cs.s);
+    if (adjoint)
+      fs.adj(g, dact.p, dx.p, dout.p, cs.s);
+    else
+      fs.fwd(g, dact.p, dx.p, dout.p, cs.s);
+    TG_CUDA(cudaMemcpyAsync(out, dout.p, dout.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+}
+
+int tg_oc_update(const tg_grid* grid, double radius, const double* density, const double* dc,
+                 double volfrac, double move, double rho_min, double* x_new) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!density || !dc || !x_new) raise(TG_EINVAL, "density, dc and x_new must be non-null");
+    if (!(volfrac > 0.0 && volfrac <= 1.0))
+      raise(TG_EINVAL, "oc_update: volume_fraction must be in (0, 1]");
+    if (!(move > 0.0)) raise(TG_EINVAL, "oc_update: move must be > 0");
+    if (!(rho_min > 0.0 && rho_min <= 1.0))
+      raise(TG_EINVAL, "oc_update: density_min must be in (0, 1]");
+    CallStream cs;
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    std::vector<uint8_t> act(size_t(g.nv));
+    int64_t n_solid = 0;
+    for (int64_t e = 0; e < g.nv; ++e) {
+      act[size_t(e)] = grid->tags == nullptr || grid->tags[e] != 0;
+      n_solid += act[size_t(e)];
+    }
+    DBuf<uint8_t> dact;
+    DBuf<double> dx, ddc, dxn(size_t(g.nv)), ones;
+    upload(dact, act.data(), act.size(), cs.s);
+    upload(dx, density, size_t(g.nv), cs.s);
+    upload(ddc, dc, size_t(g.nv), cs.s);
+    std::vector<double> o1(size_t(g.nv));
+    for (int64_t e = 0; e < g.nv; ++e) o1[size_t(e)] = act[size_t(e)] ? 1.0 : 0.0;
+    upload(ones, o1.data(), o1.size(), cs.s);
+    FilterState fs;
+    fs.init(g, radius, dact.p, cs.s);
+    OcState oc;
+    oc.init(g, cs.s);
+    oc.n_solid = n_solid;
+    fs.adj(g, dact.p, ones.p, oc.dvf.p, cs.s);
+    oc_update_device(oc, fs, g, dact.p, act, dx.p, ddc.p, volfrac, move, rho_min, dxn.p, cs.s);
+    TG_CUDA(cudaMemcpyAsync(x_new, dxn.p, dxn.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+}
+
+int tg_job_create(const tg_grid* grid, const tg_simp_params* params, const tg_dirichlet_bc* bcs,
+                  int32_t nbc, const tg_nodal_load* loads, int32_t nloads,
+                  const tg_simp_options* options, tg_job** job_out) {
+  return guarded([&] {
+    if (!job_out) raise(TG_EINVAL, "job_out is null");
+    auto j = std::make_unique<tg_job>();
+    job_init(j.get(), grid, params, bcs, nbc, loads, nloads, options);
+    *job_out = j.release();
+  });
+}
+
+int tg_job_step(tg_job* job, tg_simp_iteration* row) {
+  tg_simp_iteration r;
+  std::memset(&r, 0, sizeof r);
+  const int rc = guarded([&] {
+    if (!job) raise(TG_EINVAL, "job is null");
+    job_step(job, &r);
+  });
+  if (row) *row = r;
+  return rc;
+}
+
+int tg_job_read(tg_job* job, double* design_out, double* phys_out) {
+  return guarded([&] {
+    if (!job) raise(TG_EINVAL, "job is null");
+    const Grid& g = job->fp.g;
+    if (!job->xphys_valid) job_filter_x(job);
+    if (design_out)
+      TG_CUDA(cudaMemcpyAsync(design_out, job->x.p, size_t(g.nv) * sizeof(double),
+                              cudaMemcpyDeviceToHost, job->s));
+    if (phys_out)
+      TG_CUDA(cudaMemcpyAsync(phys_out, job->xphys.p, size_t(g.nv) * sizeof(double),
+                              cudaMemcpyDeviceToHost, job->s));
+    TG_CUDA(cudaStreamSynchronize(job->s));
+  });
+}
+
+int tg_job_write_design(tg_job* job, const double* design) {
+  return guarded([&] {
+    if (!job || !design) raise(TG_EINVAL, "job and design must be non-null");
+    TG_CUDA(cudaMemcpyAsync(job->x.p, design, job->x.bytes(), cudaMemcpyHostToDevice, job->s));
+    job->xphys_valid = false;
+    TG_CUDA(cudaStreamSynchronize(job->s));
+  });
+}
+
+int64_t tg_job_device_bytes(const tg_job* job) { return job ? int64_t(job->bytes()) : 0; }
+
+int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* options) {
+  if (!grid || grid->nx < 1 || grid->ny < 1 || grid->nz < 1) return -1;
+  const double nv = double(grid->nx) * grid->ny * grid->nz;
+  const double ndof = 3.0 * (grid->nx + 1.0) * (grid->ny + 1.0) * (grid->nz + 1.0);
+  const bool mixed = options && options->solve.precision == TG_PREC_MIXED;
+  // Fine: 9 FP64 DOF vectors + kept/f/up; ~12 voxel arrays.  Hierarchy: the
+  // level-1 element matrices (576 doubles per 8 voxels) and stencils (243
+  // doubles per node / 8), a geometric series over the coarser levels.
+  double b = ndof * (9 * 8 + 1 + 16) + nv * (12 * 8 + 2);
+  b += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 243 * 8 * 8.0 / 7.0;
+  if (mixed) b += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 243 * 4 * 8.0 / 7.0 + nv * 4;
+  return int64_t(b * 1.05) + (64 << 20);
+}
+
+void tg_job_destroy(tg_job* job) { delete job; }
+
+int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* avg_ms) {
+  return guarded([&] {
+    if (!job || !avg_ms || reps < 1) raise(TG_EINVAL, "job, avg_ms and reps >= 1 required");
+    if (!job->xphys_valid) job_filter_x(job);
+    const Grid& g = job->fp.g;
+    const tg_simp_params& p = job->params;
+    launch_modulus(job->xphys.p, job->fp.elem.p, g.nv, p.youngs_modulus, p.penalty,
+                   p.density_min, p.material_law, p.e_min, job->E.p, job->s);
+    job->solver->set_modulus(job->E.p);
+    *avg_ms = job->solver->time_operator(precision == TG_PREC_MIXED, reps);
+  });
+}
+
+int64_t tg_kernel_launches(void) { return tg::g_launches.load(); }
+
+int tg_device_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
+  return guarded([&] {
+    if (fp64_tflops) *fp64_tflops = fma_probe_tflops(true);
+    if (fp32_tflops) *fp32_tflops = fma_probe_tflops(false);
+  });
+}
+
+int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, const tg_simp_options* options, tg_progress_fn progress,
+                     void* progress_ctx, const volatile int32_t* cancel,
+                     tg_simp_iteration* history, double* design_out, double* phys_out,
+                     tg_simp_result* result) {
+  tg_simp_result res;
+  std::memset(&res, 0, sizeof res);
+  const int rc = guarded([&] {
+    auto jp = std::make_unique<tg_job>();
+    job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, options);
+    tg_job* j = jp.get();
+    const tg_simp_options& o = j->opt;
+    for (int it = 0; it < o.max_iterations; ++it) {
+      if (cancel && *cancel) {
+        res.cancelled = 1;
+        break;
+      }
+      tg_simp_iteration row;
+      try {
+        job_step(j, &row);
+      } catch (const Error& e) {
+        if (e.code != TG_ENONCONV) throw;
+        res.non_convergent = 1;  // simp.cpp:2254-2266: ends the run, no throw
+        break;
+      }
+      if (history) history[it] = row;
+      if (it == 0) res.initial_compliance = row.compliance;
+      res.iterations = j->iteration;
+      if (progress) progress(progress_ctx, row.iteration, row.compliance, row.change);
+      if (rung_infeasible(j->hist_c, j->hist_cg)) {
+        res.infeasible = 1;
+        break;
+      }
+      if (row.change < o.change_tol) {
+        res.converged = 1;
+        break;
+      }
+    }
+    const Grid& g = j->fp.g;
+    job_filter_x(j);
+    if (res.infeasible || res.non_convergent || res.cancelled) {
+      res.compliance = j->hist_c.empty() ? 0.0 : j->hist_c.back();
+    } else {
+      // The certification solve at the tight tolerance (simp.cpp:2566-2570).
+      const SolverStats st = job_solve(j, o.cg_tolerance, o.cg_max_iterations);
+      if (!st.converged) {
+        res.non_convergent = 1;
+        res.converged = 0;
+        res.compliance = j->hist_c.empty() ? 0.0 : j->hist_c.back();
+      } else {
+        res.compliance = job_sensitivity(j);
+      }
+    }
+    bool exact = false;
+    const double vol = exact_volume(j->oc, g, j->solid.p, j->xphys.p, &exact, j->s);
+    res.volume_fraction = j->n_solid > 0 ? vol / double(j->n_solid) : 0.0;
+    if (design_out)
+      TG_CUDA(cudaMemcpyAsync(design_out, j->x.p, size_t(g.nv) * sizeof(double),
+                              cudaMemcpyDeviceToHost, j->s));
+    if (phys_out)
+      TG_CUDA(cudaMemcpyAsync(phys_out, j->xphys.p, size_t(g.nv) * sizeof(double),
+                              cudaMemcpyDeviceToHost, j->s));
+    TG_CUDA(cudaStreamSynchronize(j->s));
+  });
+  if (result) *result = res;
+  return rc;
+}
+
+}  // extern "C"

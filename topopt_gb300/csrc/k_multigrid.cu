@@ -1,0 +1,640 @@
+// k_multigrid.cu -- geometric multigrid on the voxel hierarchy.
+//
+// Reference counterparts (core/src/fea/multigrid.cpp):
+//   axis_weights           :494-505   trilinear vertex stencil 1 | 1/2,1/2
+//   coarse active DOFs     :1387-1403 active iff the coincident fine DOF is
+//   P0 and A1 = P0^T A0 P0 :1408-1446, galerkin_a1_from_prolong :1543-1899
+//   levels 2.. (Galerkin)  :557-697 (build_hierarchy)
+//   jacobi_sweep, v_cycle  :780-817, mf_jacobi_sweep / mf_v_cycle :1128-1160
+//   coarsest direct solve  SimplicialLDLT :690-695 -> here a dense Cholesky
+//
+// Coarse operators are Galerkin, formed element by element: a coarse element's
+// 24x24 matrix is the sum over its (up to) eight children of W^T K_child W, with
+// W the trilinear interpolation from the parent's 8 nodes to the child's 8
+// nodes.  Because P restricted to an element is exactly that local W, the
+// assembled sum equals P^T A P -- including the masks: rows and columns of
+// inactive DOFs are zeroed on both sides, as the reference drops them from P.
+// Odd axes are handled by ceil-halving the element extents; a coarse node whose
+// coincident fine node lies beyond the grid is inactive, which reproduces the
+// reference's index-space padding (multigrid.cpp:391-459).
+//
+// Coarse levels are applied as assembled 27-point node stencils stored as
+// structure of arrays A[243][nnodes] (block (d, c1, c2) for neighbour offset d),
+// so a thread per node reads coalesced rows.
+#include <cuda_runtime.h>
+
+#include "tg_internal.h"
+#include "tg_multigrid.h"
+
+namespace tg {
+
+namespace {
+constexpr int kThreads = 256;
+
+int nblk(int64_t n, int t = kThreads) {
+  const int64_t b = (n + t - 1) / t;
+  return int(b < 152 * 64 ? (b > 0 ? b : 1) : 152 * 64);
+}
+
+// 1-D trilinear weight of coarse corner t (0 or 1) at fine offset pos (0,1,2)
+// inside the parent element.
+__device__ __forceinline__ double w1d(int pos, int t) {
+  return pos == 1 ? 0.5 : ((pos == 0) == (t == 0) ? 1.0 : 0.0);
+}
+
+// Local corner index -> offsets; corners in Walsh bit order (x | y<<1 | z<<2).
+__device__ __forceinline__ int cx(int c) { return c & 1; }
+__device__ __forceinline__ int cy(int c) { return (c >> 1) & 1; }
+__device__ __forceinline__ int cz(int c) { return c >> 2; }
+
+// Element matrices are stored in corner-bit order: row = 3*corner + comp.
+// One warp per coarse element; lane l accumulates entries l, l+32, ... (18 each).
+// Children at level 0 carry f*Ke (Ke given in corner-bit order); a child with
+// every DOF active uses the precomputed G_c = W_c^T Ke W_c (8 of them).
+__global__ void k_galerkin_level1(MgDims fd, MgDims cd, const double* __restrict__ ef,
+                                  const uint8_t* __restrict__ fact,
+                                  const uint8_t* __restrict__ cact,
+                                  const double* __restrict__ Ke,  // 576, corner-bit order
+                                  const double* __restrict__ G,   // 8 x 576
+                                  double* __restrict__ Kc) {
+  __shared__ double sKe[576];
+  __shared__ double sX[8][576];  // per-warp scratch for the masked path
+  for (int i = threadIdx.x; i < 576; i += blockDim.x) sKe[i] = Ke[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
+  for (int64_t ce = blockIdx.x * 8 + warp; ce < nce; ce += int64_t(gridDim.x) * 8) {
+    const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
+              K = int(ce / (int64_t(cd.ex) * cd.ey));
+    double acc[18];
+#pragma unroll
+    for (int q = 0; q < 18; ++q) acc[q] = 0.0;
+    for (int ch = 0; ch < 8; ++ch) {
+      const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
+      if (fi >= fd.ex || fj >= fd.ey || fk >= fd.ez) continue;
+      const double f = ef[(int64_t(fk) * fd.ey + fj) * fd.ex + fi];
+      if (f == 0.0) continue;
+      // Masks of the child's 24 DOFs (bit r set when DOF r is active).
+      unsigned int m = 0;
+      for (int r = lane; r < 24; r += 32) {
+        const int c = r / 3, comp = r % 3;
+        const int64_t node =
+            (int64_t(fk + cz(c)) * fd.nny + (fj + cy(c))) * fd.nnx + (fi + cx(c));
+        if (fact[3 * node + comp]) m |= 1u << r;
+      }
+      m = __reduce_or_sync(0xffffffffu, m);
+      if (m == 0xffffffu) {
+#pragma unroll
+        for (int q = 0; q < 18; ++q) acc[q] += f * G[ch * 576 + lane + 32 * q];
+      } else {
+        // X = (M Ke M) W (24 x 24), then acc += f * W^T X.
+        double* X = sX[warp];
+        for (int e = lane; e < 576; e += 32) {
+          const int r = e / 24, col = e % 24;  // col = 3*t + c2
+          const int t = col / 3, c2 = col % 3;
+          double s = 0.0;
+          if (m & (1u << r))
+            for (int sc = 0; sc < 8; ++sc) {
+              const int rr = 3 * sc + c2;
+              if (!(m & (1u << rr))) continue;
+              const double w = w1d(cx(ch) + cx(sc), cx(t)) * w1d(cy(ch) + cy(sc), cy(t)) *
+                               w1d(cz(ch) + cz(sc), cz(t));
+              s += sKe[r * 24 + rr] * w;
+            }
+          X[e] = s;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 18; ++q) {
+          const int e = lane + 32 * q;
+          const int row = e / 24, col = e % 24;
+          const int t1 = row / 3, c1 = row % 3;
+          double s = 0.0;
+          for (int sc = 0; sc < 8; ++sc) {
+            const double w = w1d(cx(ch) + cx(sc), cx(t1)) * w1d(cy(ch) + cy(sc), cy(t1)) *
+                             w1d(cz(ch) + cz(sc), cz(t1));
+            if (w != 0.0) s += w * X[(3 * sc + c1) * 24 + col];
+          }
+          acc[q] += f * s;
+        }
+        __syncwarp();
+      }
+    }
+    // Zero rows/cols of inactive coarse DOFs.
+    unsigned int cm = 0;
+    for (int r = lane; r < 24; r += 32) {
+      const int c = r / 3, comp = r % 3;
+      const int64_t node = (int64_t(K + cz(c)) * cd.nny + (J + cy(c))) * cd.nnx + (I + cx(c));
+      if (cact[3 * node + comp]) cm |= 1u << r;
+    }
+    cm = __reduce_or_sync(0xffffffffu, cm);
+#pragma unroll
+    for (int q = 0; q < 18; ++q) {
+      const int e = lane + 32 * q;
+      const int row = e / 24, col = e % 24;
+      const bool keep = (cm >> row & 1u) && (cm >> col & 1u);
+      Kc[ce * 576 + e] = keep ? acc[q] : 0.0;
+    }
+  }
+}
+
+// Level l -> l+1 from stored (already masked) child element matrices.
+constexpr int kCoarseWarps = 4;  // 2 x 4 x 576 doubles of shared memory per CTA
+__global__ void k_galerkin_coarse(MgDims fd, MgDims cd, const double* __restrict__ Kf,
+                                  const uint8_t* __restrict__ cact, double* __restrict__ Kc) {
+  __shared__ double sK[kCoarseWarps][576];
+  __shared__ double sX[kCoarseWarps][576];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
+  for (int64_t ce = blockIdx.x * int64_t(kCoarseWarps) + warp; ce < nce;
+       ce += int64_t(gridDim.x) * kCoarseWarps) {
+    const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
+              K = int(ce / (int64_t(cd.ex) * cd.ey));
+    double acc[18];
+#pragma unroll
+    for (int q = 0; q < 18; ++q) acc[q] = 0.0;
+    for (int ch = 0; ch < 8; ++ch) {
+      const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
+      if (fi >= fd.ex || fj >= fd.ey || fk >= fd.ez) continue;
+      const int64_t fe = (int64_t(fk) * fd.ey + fj) * fd.ex + fi;
+      double* S = sK[warp];
+      double* X = sX[warp];
+      for (int e = lane; e < 576; e += 32) S[e] = Kf[fe * 576 + e];
+      __syncwarp();
+      for (int e = lane; e < 576; e += 32) {
+        const int r = e / 24, col = e % 24;
+        const int t = col / 3, c2 = col % 3;
+        double s = 0.0;
+        for (int sc = 0; sc < 8; ++sc) {
+          const double w = w1d(cx(ch) + cx(sc), cx(t)) * w1d(cy(ch) + cy(sc), cy(t)) *
+                           w1d(cz(ch) + cz(sc), cz(t));
+          if (w != 0.0) s += S[r * 24 + 3 * sc + c2] * w;
+        }
+        X[e] = s;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 18; ++q) {
+        const int e = lane + 32 * q;
+        const int row = e / 24, col = e % 24;
+        const int t1 = row / 3, c1 = row % 3;
+        double s = 0.0;
+        for (int sc = 0; sc < 8; ++sc) {
+          const double w = w1d(cx(ch) + cx(sc), cx(t1)) * w1d(cy(ch) + cy(sc), cy(t1)) *
+                           w1d(cz(ch) + cz(sc), cz(t1));
+          if (w != 0.0) s += w * X[(3 * sc + c1) * 24 + col];
+        }
+        acc[q] += s;
+      }
+      __syncwarp();
+    }
+    unsigned int cm = 0;
+    for (int r = lane; r < 24; r += 32) {
+      const int c = r / 3, comp = r % 3;
+      const int64_t node = (int64_t(K + cz(c)) * cd.nny + (J + cy(c))) * cd.nnx + (I + cx(c));
+      if (cact[3 * node + comp]) cm |= 1u << r;
+    }
+    cm = __reduce_or_sync(0xffffffffu, cm);
+#pragma unroll
+    for (int q = 0; q < 18; ++q) {
+      const int e = lane + 32 * q;
+      const int row = e / 24, col = e % 24;
+      const bool keep = (cm >> row & 1u) && (cm >> col & 1u);
+      Kc[ce * 576 + e] = keep ? acc[q] : 0.0;
+    }
+  }
+}
+
+// Node stencil from the element matrices around each node.  Entry index
+// q = (d*3 + c1)*3 + c2, d = (dz+1)*9 + (dy+1)*3 + (dx+1).
+__global__ void k_assemble_stencil(MgDims d, const double* __restrict__ Kel,
+                                   const uint8_t* __restrict__ act, double* __restrict__ A,
+                                   double* __restrict__ invdiag) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % d.nnx), b = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
+    bool ra[3];
+    for (int k = 0; k < 3; ++k) ra[k] = act[3 * n + k] != 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
+          double blk[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) blk[k] = 0.0;
+          // Elements containing both n and n+d: offsets ox in {-1,0} with the
+          // node at corner (-ox) and the neighbour at corner (-ox + dx) in [0,1].
+          for (int oz = -1; oz <= 0; ++oz) {
+            const int lz = -oz, mz = lz + dz;
+            if (mz < 0 || mz > 1) continue;
+            for (int oy = -1; oy <= 0; ++oy) {
+              const int ly = -oy, my = ly + dy;
+              if (my < 0 || my > 1) continue;
+              for (int ox = -1; ox <= 0; ++ox) {
+                const int lx = -ox, mx = lx + dx;
+                if (mx < 0 || mx > 1) continue;
+                const int ei = a + ox, ej = b + oy, ek = c + oz;
+                if (ei < 0 || ei >= d.ex || ej < 0 || ej >= d.ey || ek < 0 || ek >= d.ez) continue;
+                const int64_t e = (int64_t(ek) * d.ey + ej) * d.ex + ei;
+                const int ln = lx | (ly << 1) | (lz << 2), lm = mx | (my << 1) | (mz << 2);
+                const double* Ke = Kel + e * 576;
+#pragma unroll
+                for (int c1 = 0; c1 < 3; ++c1)
+#pragma unroll
+                  for (int c2 = 0; c2 < 3; ++c2) blk[c1 * 3 + c2] += Ke[(3 * ln + c1) * 24 + 3 * lm + c2];
+              }
+            }
+          }
+#pragma unroll
+          for (int c1 = 0; c1 < 3; ++c1)
+#pragma unroll
+            for (int c2 = 0; c2 < 3; ++c2)
+              A[int64_t(di * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : 0.0;
+          if (di == 13)
+            for (int k = 0; k < 3; ++k) {
+              const double dg = blk[k * 3 + k];
+              invdiag[3 * n + k] = (ra[k] && dg > 0.0) ? 1.0 / dg : 0.0;
+            }
+        }
+  }
+}
+
+template <class T>
+__global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads)
+    d[i] = T(s[i]);
+}
+
+// Stencil operator: y = A x / b - A x / x + w D^-1 (b - A x), masked by act.
+template <class T, int MODE>
+__global__ void __launch_bounds__(kThreads) k_stencil_op(MgDims d, const T* __restrict__ A,
+                                                         const uint8_t* __restrict__ act,
+                                                         const T* __restrict__ x,
+                                                         const T* __restrict__ b,
+                                                         const T* __restrict__ invdiag, T omega,
+                                                         T* __restrict__ y) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny),
+              c = int(n / (int64_t(d.nnx) * d.nny));
+    T s0 = 0, s1 = 0, s2 = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int k = c + dz;
+      if (k < 0 || k >= d.nnz) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int j = bb + dy;
+        if (j < 0 || j >= d.nny) continue;
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int i = a + dx;
+          if (i < 0 || i >= d.nnx) continue;
+          const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
+          const int64_t m = (int64_t(k) * d.nny + j) * d.nnx + i;
+          const T x0 = x[3 * m], x1 = x[3 * m + 1], x2 = x[3 * m + 2];
+          const T* Ab = A + int64_t(di * 9) * nn + n;
+          s0 += Ab[0] * x0 + Ab[nn] * x1 + Ab[2 * nn] * x2;
+          s1 += Ab[3 * nn] * x0 + Ab[4 * nn] * x1 + Ab[5 * nn] * x2;
+          s2 += Ab[6 * nn] * x0 + Ab[7 * nn] * x1 + Ab[8 * nn] * x2;
+        }
+      }
+    }
+    const T s[3] = {s0, s1, s2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int64_t dof = 3 * n + k;
+      T out;
+      if (!act[dof]) {
+        out = T(0);
+      } else if (MODE == kApply) {
+        out = s[k];
+      } else if (MODE == kResidual) {
+        out = b[dof] - s[k];
+      } else {
+        out = x[dof] + omega * invdiag[dof] * (b[dof] - s[k]);
+      }
+      y[dof] = out;
+    }
+  }
+}
+
+// x = omega * invdiag .* b (the first smoother sweep from a zero iterate).
+template <class T>
+__global__ void k_jacobi_first(const T* __restrict__ b, const T* __restrict__ invdiag, T omega,
+                               int64_t n, T* __restrict__ x) {
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads)
+    x[i] = omega * invdiag[i] * b[i];
+}
+
+// Restriction R = P^T: coarse node N gathers the (up to 27) fine nodes
+// 2N + delta, delta in {-1,0,1}^3, weight prod(1 or 1/2).  Inactive coarse DOFs
+// get 0; fine residuals are already 0 on inactive fine DOFs.
+template <class T>
+__global__ void k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
+                           const uint8_t* __restrict__ cact, T* __restrict__ bc) {
+  const int64_t nn = int64_t(cd.nnx) * cd.nny * cd.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % cd.nnx), b = int((n / cd.nnx) % cd.nny), c = int(n / (int64_t(cd.nnx) * cd.nny));
+    T s0 = 0, s1 = 0, s2 = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int k = 2 * c + dz;
+      if (k < 0 || k >= fd.nnz) continue;
+      const T wz = dz == 0 ? T(1) : T(0.5);
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int j = 2 * b + dy;
+        if (j < 0 || j >= fd.nny) continue;
+        const T wy = dy == 0 ? T(1) : T(0.5);
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int i = 2 * a + dx;
+          if (i < 0 || i >= fd.nnx) continue;
+          const T w = (dx == 0 ? T(1) : T(0.5)) * wy * wz;
+          const int64_t m = (int64_t(k) * fd.nny + j) * fd.nnx + i;
+          s0 += w * rf[3 * m];
+          s1 += w * rf[3 * m + 1];
+          s2 += w * rf[3 * m + 2];
+        }
+      }
+    }
+    bc[3 * n] = cact[3 * n] ? s0 : T(0);
+    bc[3 * n + 1] = cact[3 * n + 1] ? s1 : T(0);
+    bc[3 * n + 2] = cact[3 * n + 2] ? s2 : T(0);
+  }
+}
+
+// Prolongation + correction: x_f += P e_c on active fine DOFs.
+template <class T>
+__global__ void k_prolong_add(MgDims fd, MgDims cd, const T* __restrict__ ec,
+                              const uint8_t* __restrict__ fact, T* __restrict__ xf) {
+  const int64_t nn = int64_t(fd.nnx) * fd.nny * fd.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % fd.nnx), b = int((n / fd.nnx) % fd.nny), c = int(n / (int64_t(fd.nnx) * fd.nny));
+    const int ia0 = a >> 1, ia1 = (a + 1) >> 1, ib0 = b >> 1, ib1 = (b + 1) >> 1;
+    const int ic0 = c >> 1, ic1 = (c + 1) >> 1;
+    const T wa = (a & 1) ? T(0.5) : T(1), wb = (b & 1) ? T(0.5) : T(1), wc = (c & 1) ? T(0.5) : T(1);
+    T s0 = 0, s1 = 0, s2 = 0;
+    for (int zz = 0; zz < ((c & 1) ? 2 : 1); ++zz) {
+      const int k = zz ? ic1 : ic0;
+      for (int yy = 0; yy < ((b & 1) ? 2 : 1); ++yy) {
+        const int j = yy ? ib1 : ib0;
+        for (int xx = 0; xx < ((a & 1) ? 2 : 1); ++xx) {
+          const int i = xx ? ia1 : ia0;
+          if (i >= cd.nnx || j >= cd.nny || k >= cd.nnz) continue;
+          const int64_t m = (int64_t(k) * cd.nny + j) * cd.nnx + i;
+          const T w = wa * wb * wc;
+          s0 += w * ec[3 * m];
+          s1 += w * ec[3 * m + 1];
+          s2 += w * ec[3 * m + 2];
+        }
+      }
+    }
+    if (fact[3 * n]) xf[3 * n] += s0;
+    if (fact[3 * n + 1]) xf[3 * n + 1] += s1;
+    if (fact[3 * n + 2]) xf[3 * n + 2] += s2;
+  }
+}
+
+// ---------------------------------------------------------- coarsest solve
+// Dense lower-triangular A (row-major, nc x nc) from the coarsest stencil over
+// the compact numbering cidx (-1 = inactive).
+__global__ void k_dense_from_stencil(MgDims d, const double* __restrict__ A,
+                                     const int* __restrict__ cidx, int nc,
+                                     double* __restrict__ D) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % d.nnx), b = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
+    for (int c1 = 0; c1 < 3; ++c1) {
+      const int row = cidx[3 * n + c1];
+      if (row < 0) continue;
+      for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int i = a + dx, j = b + dy, k = c + dz;
+            if (i < 0 || i >= d.nnx || j < 0 || j >= d.nny || k < 0 || k >= d.nnz) continue;
+            const int64_t m = (int64_t(k) * d.nny + j) * d.nnx + i;
+            const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
+            for (int c2 = 0; c2 < 3; ++c2) {
+              const int col = cidx[3 * m + c2];
+              if (col < 0) continue;
+              D[int64_t(row) * nc + col] = A[int64_t(di * 9 + c1 * 3 + c2) * nn + n];
+            }
+          }
+    }
+  }
+}
+
+// Blocked right-looking Cholesky, panel width 32.  Step 1: factor the diagonal
+// block in shared memory (one CTA); a non-positive pivot sets *fail.
+__global__ void k_chol_diag(double* __restrict__ D, int nc, int k0, int* __restrict__ fail) {
+  __shared__ double s[32][33];
+  const int nb = min(32, nc - k0);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 32 threads
+  if (tx < nb && ty < nb) s[ty][tx] = D[int64_t(k0 + ty) * nc + k0 + tx];
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (tx == 0 && ty == 0) {
+      const double p = s[j][j];
+      if (!(p > 0.0)) *fail = 1;
+      s[j][j] = p > 0.0 ? sqrt(p) : 1.0;
+    }
+    __syncthreads();
+    if (ty == 0 && tx > j && tx < nb) s[tx][j] /= s[j][j];
+    __syncthreads();
+    if (ty > j && tx > j && ty < nb && tx <= ty) s[ty][tx] -= s[ty][j] * s[tx][j];
+    __syncthreads();
+  }
+  if (tx < nb && ty < nb && tx <= ty) D[int64_t(k0 + ty) * nc + k0 + tx] = s[ty][tx];
+}
+
+// Step 2: rows below the diagonal block: L[i, k0:k0+nb] = A[i, .] L_kk^-T.
+__global__ void k_chol_panel(double* __restrict__ D, int nc, int k0) {
+  __shared__ double L[32][33];
+  const int nb = min(32, nc - k0);
+  for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+    const int r = t / 32, c = t % 32;
+    L[r][c] = (r < nb && c < nb && c <= r) ? D[int64_t(k0 + r) * nc + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  const int i = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  double row[32];
+  for (int c = 0; c < nb; ++c) row[c] = D[int64_t(i) * nc + k0 + c];
+  for (int c = 0; c < nb; ++c) {
+    double v = row[c];
+    for (int t = 0; t < c; ++t) v -= row[t] * L[c][t];
+    row[c] = v / L[c][c];
+  }
+  for (int c = 0; c < nb; ++c) D[int64_t(i) * nc + k0 + c] = row[c];
+}
+
+// Step 3: trailing update of the lower triangle, 32x32 tiles.
+__global__ void k_chol_update(double* __restrict__ D, int nc, int k0) {
+  const int nb = min(32, nc - k0);
+  const int r0 = k0 + nb + blockIdx.y * 32, c0 = k0 + nb + blockIdx.x * 32;
+  if (c0 > r0 + 31) return;
+  __shared__ double Li[32][33], Lj[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int yy = ty; yy < 32; yy += blockDim.x / 32) {
+    Li[yy][tx] = (r0 + yy < nc && tx < nb) ? D[int64_t(r0 + yy) * nc + k0 + tx] : 0.0;
+    Lj[yy][tx] = (c0 + yy < nc && tx < nb) ? D[int64_t(c0 + yy) * nc + k0 + tx] : 0.0;
+  }
+  __syncthreads();
+  for (int yy = ty; yy < 32; yy += blockDim.x / 32) {
+    const int i = r0 + yy, j = c0 + tx;
+    if (i >= nc || j >= nc || j > i) continue;
+    double s = 0.0;
+    for (int t = 0; t < nb; ++t) s += Li[yy][t] * Lj[tx][t];
+    D[int64_t(i) * nc + j] -= s;
+  }
+}
+
+// Forward and backward substitution with the factor, one CTA; the coarsest
+// right-hand side is gathered from / scattered to the stencil-level vector.
+template <class T>
+__global__ void k_chol_solve(const double* __restrict__ L, int nc, const int* __restrict__ cidx,
+                             int64_t ndof, const T* __restrict__ b, T* __restrict__ x,
+                             double* __restrict__ work) {
+  for (int64_t d = threadIdx.x; d < ndof; d += blockDim.x) {
+    const int ci = cidx[d];
+    if (ci >= 0) work[ci] = double(b[d]);
+  }
+  __syncthreads();
+  for (int j = 0; j < nc; ++j) {  // L y = b
+    __shared__ double yj;
+    if (threadIdx.x == 0) {
+      yj = work[j] / L[int64_t(j) * nc + j];
+      work[j] = yj;
+    }
+    __syncthreads();
+    for (int i = j + 1 + threadIdx.x; i < nc; i += blockDim.x) work[i] -= L[int64_t(i) * nc + j] * yj;
+    __syncthreads();
+  }
+  for (int j = nc - 1; j >= 0; --j) {  // L^T x = y
+    __shared__ double xj;
+    if (threadIdx.x == 0) {
+      xj = work[j] / L[int64_t(j) * nc + j];
+      work[j] = xj;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < j; i += blockDim.x) work[i] -= L[int64_t(j) * nc + i] * xj;
+    __syncthreads();
+  }
+  for (int64_t d = threadIdx.x; d < ndof; d += blockDim.x) {
+    const int ci = cidx[d];
+    x[d] = ci >= 0 ? T(work[ci]) : T(0);
+  }
+}
+}  // namespace
+
+void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const double* ef,
+                        const uint8_t* fact, const uint8_t* cact, const double* Ke,
+                        const double* G, double* Kc, cudaStream_t s) {
+  const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
+  k_galerkin_level1<<<nblk(nce, 8), 256, 0, s>>>(fd, cd, ef, fact, cact, Ke, G, Kc);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const double* Kf, const uint8_t* cact,
+                        double* Kc, cudaStream_t s) {
+  const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
+  k_galerkin_coarse<<<nblk(nce, kCoarseWarps), 32 * kCoarseWarps, 0, s>>>(fd, cd, Kf, cact, Kc);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_assemble_stencil(const MgDims& d, const double* Kel, const uint8_t* act, double* A,
+                         double* invdiag, cudaStream_t s) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  k_assemble_stencil<<<nblk(nn), kThreads, 0, s>>>(d, Kel, act, A, invdiag);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s) {
+  k_to_float<float><<<nblk(n), kThreads, 0, s>>>(src, dst, n);
+  TG_LAUNCH_CHECK();
+}
+
+template <class T>
+void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
+                   const T* b, const T* invdiag, T omega, T* y, cudaStream_t s) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  const int nb = nblk(nn);
+  if (mode == kApply)
+    k_stencil_op<T, kApply><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+  else if (mode == kResidual)
+    k_stencil_op<T, kResidual><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+  else
+    k_stencil_op<T, kSmooth><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+  TG_LAUNCH_CHECK();
+}
+
+template <class T>
+void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cudaStream_t s) {
+  k_jacobi_first<T><<<nblk(n), kThreads, 0, s>>>(b, invdiag, omega, n, x);
+  TG_LAUNCH_CHECK();
+}
+
+template <class T>
+void mg_restrict(const MgDims& fd, const MgDims& cd, const T* rf, const uint8_t* cact, T* bc,
+                 cudaStream_t s) {
+  const int64_t nn = int64_t(cd.nnx) * cd.nny * cd.nnz;
+  k_restrict<T><<<nblk(nn), kThreads, 0, s>>>(fd, cd, rf, cact, bc);
+  TG_LAUNCH_CHECK();
+}
+
+template <class T>
+void mg_prolong_add(const MgDims& fd, const MgDims& cd, const T* ec, const uint8_t* fact, T* xf,
+                    cudaStream_t s) {
+  const int64_t nn = int64_t(fd.nnx) * fd.nny * fd.nnz;
+  k_prolong_add<T><<<nblk(nn), kThreads, 0, s>>>(fd, cd, ec, fact, xf);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_dense_from_stencil(const MgDims& d, const double* A, const int* cidx, int nc, double* D,
+                           cudaStream_t s) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  TG_CUDA(cudaMemsetAsync(D, 0, sizeof(double) * size_t(nc) * nc, s));
+  k_dense_from_stencil<<<nblk(nn), kThreads, 0, s>>>(d, A, cidx, nc, D);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_cholesky(double* D, int nc, int* fail, cudaStream_t s) {
+  for (int k0 = 0; k0 < nc; k0 += 32) {
+    k_chol_diag<<<1, 1024, 0, s>>>(D, nc, k0, fail);
+    TG_LAUNCH_CHECK();
+    const int rest = nc - k0 - 32;
+    if (rest <= 0) break;
+    k_chol_panel<<<(rest + 127) / 128, 128, 0, s>>>(D, nc, k0);
+    TG_LAUNCH_CHECK();
+    const int tiles = (rest + 31) / 32;
+    k_chol_update<<<dim3(tiles, tiles), 256, 0, s>>>(D, nc, k0);
+    TG_LAUNCH_CHECK();
+  }
+}
+
+template <class T>
+void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const T* b, T* x,
+                   double* work, cudaStream_t s) {
+  k_chol_solve<T><<<1, 512, 0, s>>>(L, nc, cidx, ndof, b, x, work);
+  TG_LAUNCH_CHECK();
+}
+
+#define TG_INST(T)                                                                            \
+  template void mg_stencil_op<T>(int, const MgDims&, const T*, const uint8_t*, const T*,      \
+                                 const T*, const T*, T, T*, cudaStream_t);                    \
+  template void mg_jacobi_first<T>(const T*, const T*, T, int64_t, T*, cudaStream_t);         \
+  template void mg_restrict<T>(const MgDims&, const MgDims&, const T*, const uint8_t*, T*,    \
+                               cudaStream_t);                                                 \
+  template void mg_prolong_add<T>(const MgDims&, const MgDims&, const T*, const uint8_t*, T*, \
+                                  cudaStream_t);                                              \
+  template void mg_chol_solve<T>(const double*, int, const int*, int64_t, const T*, T*,       \
+                                 double*, cudaStream_t);
+TG_INST(double)
+TG_INST(float)
+#undef TG_INST
+
+}  // namespace tg

@@ -1,0 +1,489 @@
+// k_simp.cu -- SIMP kernels around the solve: material law, compliance and
+// sensitivities, the density filter (forward and adjoint), the OC candidate and
+// an exact, order-independent volume sum.
+//
+// Reference counterparts (core/src/simp/simp.cpp):
+//   modulus fill               :628-657   E = clamp(rho, rho_min, 1)^p * E0
+//   compliance + dc/drho sweep :747-824   q_e = u_e^T K_unit u_e
+//   make_density_filter        :834-890   weights r - |d| over active voxels
+//   filter_density             :913-926
+//   filter_sensitivity         :928-942   (the transpose, here as a gather)
+//   oc_update candidate        :980-1000
+//
+// Bit parity: the filter and the OC candidate round exactly like the reference:
+// each neighbour product and each running sum is a separate IEEE operation
+// (__dmul_rn/__dadd_rn keep the compiler from fusing them), neighbours are
+// visited in ascending voxel index, and the division and square root are the
+// correctly rounded IEEE ones.  The adjoint gathers out[j] = sum_e w(e,j) s_e/Hs_e
+// over neighbours e in ascending index, which is the order the reference's
+// scatter adds them in.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "tg_internal.h"
+
+namespace tg {
+
+namespace {
+constexpr int kThreads = 256;
+
+struct GridDev {
+  int nx, ny, nz, nnx, nny, nnz;
+};
+GridDev dev(const Grid& g) { return GridDev{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz}; }
+
+int grid_blocks(int64_t n) {
+  const int64_t b = (n + kThreads - 1) / kThreads;
+  return int(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double block_sum256(double v) {
+  __shared__ double red[kThreads / 32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (wid == 0) {
+    s = lane < kThreads / 32 ? red[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ double clamp_density(double rho, double rho_min) {
+  const double lo = (rho_min < rho) ? rho : rho_min;  // std::max(rho_min, rho)
+  return (lo < 1.0) ? lo : 1.0;                       // std::min(1.0, lo)
+}
+
+__global__ void k_modulus(const double* __restrict__ rho, const uint8_t* __restrict__ elem,
+                          int64_t n, double E0, double p, double rho_min, int law, double emin,
+                          double* __restrict__ E) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double v = 0.0;
+    if (elem[e]) {
+      if (law == 0)
+        v = pow(clamp_density(rho[e], rho_min), p) * E0;
+      else
+        v = emin + pow(rho[e], p) * (E0 - emin);
+    }
+    E[e] = v;
+  }
+}
+
+// The same Walsh-modal element operator as k_operator.cu, unit modulus, FP64.
+struct Modal64 {
+  double L0, L1, M0, M1, M02, M12, LM2;
+};
+
+__device__ __forceinline__ void walsh_fwd(double (&v)[8]) {
+#pragma unroll
+  for (int b = 1; b < 8; b <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (i & b) continue;
+      const double lo = v[i], hi = v[i | b];
+      v[i] = hi + lo;
+      v[i | b] = hi - lo;
+    }
+}
+
+// Strain energy q = u^T K u of one element from its mode coefficients:
+// q = sum over monomial classes of (unnormalised) modes x stresses, which is
+// u . (K u) evaluated in the modal basis (Parseval of the Walsh transform: the
+// corner-space dot equals 1/8 of the mode-space dot).
+__device__ __forceinline__ double modal_energy(const Modal64& mc, double (&ux)[8],
+                                               double (&uy)[8], double (&uz)[8]) {
+  walsh_fwd(ux);
+  walsh_fwd(uy);
+  walsh_fwd(uz);
+  double gx[8], gy[8], gz[8];
+  {
+    const double Ltr = mc.L0 * (ux[1] + uy[2] + uz[4]);
+    gx[1] = Ltr + mc.M02 * ux[1];
+    gy[2] = Ltr + mc.M02 * uy[2];
+    gz[4] = Ltr + mc.M02 * uz[4];
+    const double txy = mc.M0 * (uy[1] + ux[2]);
+    const double txz = mc.M0 * (uz[1] + ux[4]);
+    const double tyz = mc.M0 * (uz[2] + uy[4]);
+    gy[1] = txy; gz[1] = txz;
+    gx[2] = txy; gz[2] = tyz;
+    gx[4] = txz; gy[4] = tyz;
+  }
+  {
+    const double Ltr = mc.L1 * (uy[3] + uz[5]);
+    const double t = mc.M1 * (uz[3] + uy[5]);
+    gx[3] = mc.M1 * ux[3];
+    gy[3] = Ltr + mc.M12 * uy[3];
+    gz[3] = t;
+    gx[5] = mc.M1 * ux[5];
+    gy[5] = t;
+    gz[5] = Ltr + mc.M12 * uz[5];
+  }
+  {
+    const double Ltr = mc.L1 * (ux[3] + uz[6]);
+    const double t = mc.M1 * (uz[3] + ux[6]);
+    gx[3] += Ltr + mc.M12 * ux[3];
+    gy[3] += mc.M1 * uy[3];
+    gz[3] += t;
+    gx[6] = t;
+    gy[6] = mc.M1 * uy[6];
+    gz[6] = Ltr + mc.M12 * uz[6];
+  }
+  {
+    const double Ltr = mc.L1 * (ux[5] + uy[6]);
+    const double t = mc.M1 * (uy[5] + ux[6]);
+    gx[5] += Ltr + mc.M12 * ux[5];
+    gy[5] += t;
+    gz[5] += mc.M1 * uz[5];
+    gx[6] += t;
+    gy[6] += Ltr + mc.M12 * uy[6];
+    gz[6] += mc.M1 * uz[6];
+  }
+  gx[7] = mc.LM2 * ux[7];
+  gy[7] = mc.LM2 * uy[7];
+  gz[7] = mc.LM2 * uz[7];
+  // K u = H g (corner space), so u.(K u) = (H^T u).g = sum over modes of M.g,
+  // where M = H^T u are exactly the unnormalised mode coefficients above.
+  double q = 0.0;
+#pragma unroll
+  for (int i = 1; i < 8; ++i) q += ux[i] * gx[i] + uy[i] * gy[i] + uz[i] * gz[i];
+  return q;
+}
+
+__global__ void k_sensitivity(GridDev g, Modal64 mc, const double* __restrict__ rho,
+                              const uint8_t* __restrict__ elem, const double* __restrict__ u,
+                              double E0, double p, double rho_min, int law, double emin,
+                              double* __restrict__ dc, double* __restrict__ c_part) {
+  const int64_t n = int64_t(g.nx) * g.ny * g.nz;
+  double csum = 0.0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double d = 0.0;
+    if (elem[e]) {
+      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      double ux[8], uy[8], uz[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int64_t node =
+            (int64_t(k + (c >> 2)) * g.nny + (j + ((c >> 1) & 1))) * g.nnx + i + (c & 1);
+        ux[c] = u[3 * node];
+        uy[c] = u[3 * node + 1];
+        uz[c] = u[3 * node + 2];
+      }
+      const double q = modal_energy(mc, ux, uy, uz);
+      if (law == 0) {
+        const double r = clamp_density(rho[e], rho_min);
+        csum += pow(r, p) * E0 * q;
+        d = -p * pow(r, p - 1.0) * E0 * q;
+      } else {
+        const double r = rho[e];
+        csum += (emin + pow(r, p) * (E0 - emin)) * q;
+        d = -p * pow(r, p - 1.0) * (E0 - emin) * q;
+      }
+    }
+    dc[e] = d;
+  }
+  csum = block_sum256(csum);
+  if (threadIdx.x == 0) c_part[blockIdx.x] = csum;
+}
+
+// ------------------------------------------------------------------ filter
+struct StencilEntry {
+  int di, dj, dk, pad;
+  double w;
+};
+
+__device__ __forceinline__ bool in_grid(const GridDev& g, int i, int j, int k) {
+  return i >= 0 && i < g.nx && j >= 0 && j < g.ny && k >= 0 && k < g.nz;
+}
+
+__global__ void k_weight_sum(GridDev g, const StencilEntry* __restrict__ st, int ns,
+                             const uint8_t* __restrict__ act, double* __restrict__ hs) {
+  const int64_t n = int64_t(g.nx) * g.ny * g.nz;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double s = 0.0;
+    if (act[e]) {
+      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      for (int q = 0; q < ns; ++q) {
+        const int ii = i + st[q].di, jj = j + st[q].dj, kk = k + st[q].dk;
+        if (!in_grid(g, ii, jj, kk)) continue;
+        if (!act[(int64_t(kk) * g.ny + jj) * g.nx + ii]) continue;
+        s = __dadd_rn(s, st[q].w);
+      }
+    }
+    hs[e] = s;
+  }
+}
+
+__global__ void k_filter_fwd(GridDev g, const StencilEntry* __restrict__ st, int ns,
+                             const uint8_t* __restrict__ act, const double* __restrict__ hs,
+                             const double* __restrict__ x, double* __restrict__ out) {
+  const int64_t n = int64_t(g.nx) * g.ny * g.nz;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double v = 0.0;
+    const double h = hs[e];
+    if (h > 0.0) {
+      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      double acc = 0.0;
+      for (int q = 0; q < ns; ++q) {
+        const int ii = i + st[q].di, jj = j + st[q].dj, kk = k + st[q].dk;
+        if (!in_grid(g, ii, jj, kk)) continue;
+        const int64_t nb = (int64_t(kk) * g.ny + jj) * g.nx + ii;
+        if (!act[nb]) continue;
+        acc = __dadd_rn(acc, __dmul_rn(st[q].w, x[nb]));
+      }
+      v = __ddiv_rn(acc, h);
+    }
+    out[e] = v;
+  }
+}
+
+__global__ void k_filter_scale(int64_t n, const double* __restrict__ hs,
+                               const double* __restrict__ s, double* __restrict__ se) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    const double h = hs[e];
+    se[e] = h > 0.0 ? __ddiv_rn(s[e], h) : 0.0;
+  }
+}
+
+__global__ void k_filter_adj(GridDev g, const StencilEntry* __restrict__ st, int ns,
+                             const uint8_t* __restrict__ act, const double* __restrict__ hs,
+                             const double* __restrict__ se, double* __restrict__ out) {
+  const int64_t n = int64_t(g.nx) * g.ny * g.nz;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double acc = 0.0;
+    if (act[e]) {
+      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      for (int q = 0; q < ns; ++q) {
+        const int ii = i + st[q].di, jj = j + st[q].dj, kk = k + st[q].dk;
+        if (!in_grid(g, ii, jj, kk)) continue;
+        const int64_t nb = (int64_t(kk) * g.ny + jj) * g.nx + ii;
+        if (!(hs[nb] > 0.0)) continue;
+        acc = __dadd_rn(acc, __dmul_rn(st[q].w, se[nb]));
+      }
+    }
+    out[e] = acc;
+  }
+}
+
+// --------------------------------------------------------------------- OC
+__global__ void k_oc_candidate(const double* __restrict__ x, const double* __restrict__ dcf,
+                               const double* __restrict__ dvf, const uint8_t* __restrict__ act,
+                               int64_t n, double lambda, double move, double rho_min,
+                               double* __restrict__ xnew) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double xt = 0.0;
+    if (act[e]) {
+      const double xe = x[e];
+      double be = 0.0;
+      if (dvf[e] > 0.0) be = __ddiv_rn(-dcf[e], __dmul_rn(lambda, dvf[e]));
+      if (be < 0.0) be = 0.0;
+      xt = __dmul_rn(xe, __dsqrt_rn(be));
+      const double xm = __dsub_rn(xe, move), xp = __dadd_rn(xe, move);
+      const double lo = (rho_min < xm) ? xm : rho_min;
+      const double hi = (xp < 1.0) ? xp : 1.0;
+      if (xt < lo) xt = lo;
+      if (xt > hi) xt = hi;
+    }
+    xnew[e] = xt;
+  }
+}
+
+// Exact fixed-point accumulation: value = A * 2^-128, A a 192-bit unsigned
+// integer in three 64-bit limbs.  Integer addition is associative, so the total
+// is the same whatever the summation order -- the exact sum, not an
+// approximation of it.  Values below 2^-75 (bits below 2^-128) or above 2^40 set
+// the inexact flag and the caller falls back to the sequential reference sum.
+struct U192 {
+  unsigned long long l0, l1, l2;
+};
+__device__ __forceinline__ void add192(U192& a, const U192& b) {
+  unsigned long long s0 = a.l0 + b.l0;
+  unsigned long long c0 = s0 < a.l0;
+  unsigned long long s1 = a.l1 + b.l1;
+  unsigned long long c1 = s1 < a.l1;
+  s1 += c0;
+  c1 += (s1 < c0);
+  a.l0 = s0;
+  a.l1 = s1;
+  a.l2 = a.l2 + b.l2 + c1;
+}
+__device__ __forceinline__ bool to192(double v, U192& out) {
+  out.l0 = out.l1 = out.l2 = 0;
+  if (v == 0.0) return true;
+  if (!(v > 0.0) || v > 1099511627776.0) return false;  // negative, NaN or > 2^40
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int ex = int((bits >> 52) & 0x7ff);
+  if (ex == 0) return false;  // subnormal
+  const unsigned long long m = (bits & 0xfffffffffffffull) | (1ull << 52);
+  const int shift = ex - 1075 + 128;  // position of m's lowest bit in A
+  if (shift < 0) return false;
+  const int li = shift >> 6, off = shift & 63;
+  unsigned long long lo = m << off;
+  unsigned long long hi = off ? (m >> (64 - off)) : 0ull;
+  if (li == 0) {
+    out.l0 = lo;
+    out.l1 = hi;
+  } else if (li == 1) {
+    out.l1 = lo;
+    out.l2 = hi;
+  } else {
+    out.l2 = lo;
+  }
+  return true;
+}
+
+__global__ void k_exact_sum(const double* __restrict__ v, const uint8_t* __restrict__ act,
+                            int64_t n, unsigned long long* __restrict__ part,
+                            int* __restrict__ inexact) {
+  __shared__ U192 sh[kThreads];
+  U192 acc{0, 0, 0};
+  bool ok = true;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    if (!act[e]) continue;
+    U192 t;
+    ok &= to192(v[e], t);
+    add192(acc, t);
+  }
+  if (!ok) *inexact = 1;
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) add192(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = sh[0].l0;
+    part[3 * blockIdx.x + 1] = sh[0].l1;
+    part[3 * blockIdx.x + 2] = sh[0].l2;
+  }
+}
+
+__global__ void k_exact_total(const unsigned long long* __restrict__ part, int nparts,
+                              unsigned long long* __restrict__ total) {
+  __shared__ U192 sh[kThreads];
+  U192 acc{0, 0, 0};
+  for (int i = threadIdx.x; i < nparts; i += kThreads) {
+    const U192 t{part[3 * i], part[3 * i + 1], part[3 * i + 2]};
+    add192(acc, t);
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) add192(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    total[0] = sh[0].l0;
+    total[1] = sh[0].l1;
+    total[2] = sh[0].l2;
+  }
+}
+}  // namespace
+
+void launch_modulus(const double* rho, const uint8_t* elem, int64_t n, double E0, double p,
+                    double rho_min, int law, double emin, double* E, cudaStream_t s) {
+  k_modulus<<<grid_blocks(n), kThreads, 0, s>>>(rho, elem, n, E0, p, rho_min, law, emin, E);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_sensitivity(const Grid& g, const ModalConsts& c, const double* rho,
+                        const uint8_t* elem, const double* u, double E0, double p,
+                        double rho_min, int law, double emin, double* dc, double* c_part,
+                        int* nparts, cudaStream_t s) {
+  const Modal64 mc{c.L[0], c.L[1], c.M[0], c.M[1], 2 * c.M[0], 2 * c.M[1], c.L[2] + 4 * c.M[2]};
+  const int nb = grid_blocks(g.nv);
+  *nparts = nb;
+  k_sensitivity<<<nb, kThreads, 0, s>>>(dev(g), mc, rho, elem, u, E0, p, rho_min, law, emin, dc,
+                                        c_part);
+  TG_LAUNCH_CHECK();
+}
+
+FilterStencil FilterStencil::make(double radius) {
+  FilterStencil st;
+  st.R = int(std::ceil(radius));
+  for (int dk = -st.R; dk <= st.R; ++dk)
+    for (int dj = -st.R; dj <= st.R; ++dj)
+      for (int di = -st.R; di <= st.R; ++di) {
+        const double dist = std::sqrt(double(di * di + dj * dj + dk * dk));
+        const double w = radius - dist;
+        if (w <= 0.0) continue;
+        st.di.push_back(di);
+        st.dj.push_back(dj);
+        st.dk.push_back(dk);
+        st.w.push_back(w);
+      }
+  st.n = int(st.w.size());
+  return st;
+}
+
+// The stencil lives in a per-job device buffer (jobs may use different radii).
+void* filter_stencil_device(const FilterStencil& st, DBuf<unsigned char>& buf, cudaStream_t s) {
+  std::vector<StencilEntry> h(st.n);
+  for (int q = 0; q < st.n; ++q) h[q] = StencilEntry{st.di[q], st.dj[q], st.dk[q], 0, st.w[q]};
+  buf.alloc(sizeof(StencilEntry) * std::max(1, st.n));
+  TG_CUDA(cudaMemcpyAsync(buf.p, h.data(), sizeof(StencilEntry) * st.n, cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+  return buf.p;
+}
+
+void launch_weight_sum(const Grid& g, const void* st, int ns, const uint8_t* act, double* hs,
+                       cudaStream_t s) {
+  k_weight_sum<<<grid_blocks(g.nv), kThreads, 0, s>>>(
+      dev(g), static_cast<const StencilEntry*>(st), ns, act, hs);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_filter_fwd(const Grid& g, const void* st, int ns, const uint8_t* act,
+                       const double* hs, const double* x, double* out, cudaStream_t s) {
+  k_filter_fwd<<<grid_blocks(g.nv), kThreads, 0, s>>>(
+      dev(g), static_cast<const StencilEntry*>(st), ns, act, hs, x, out);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_filter_adj(const Grid& g, const void* st, int ns, const uint8_t* act,
+                       const double* hs, const double* s_in, double* tmp, double* out,
+                       cudaStream_t s) {
+  k_filter_scale<<<grid_blocks(g.nv), kThreads, 0, s>>>(g.nv, hs, s_in, tmp);
+  TG_LAUNCH_CHECK();
+  k_filter_adj<<<grid_blocks(g.nv), kThreads, 0, s>>>(
+      dev(g), static_cast<const StencilEntry*>(st), ns, act, hs, tmp, out);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
+                         const uint8_t* act, int64_t n, double lambda, double move,
+                         double rho_min, double* xnew, cudaStream_t s) {
+  k_oc_candidate<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, lambda, move, rho_min,
+                                                     xnew);
+  TG_LAUNCH_CHECK();
+}
+
+int exact_sum_blocks() { return kRedBlocks; }
+
+void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,
+                      uint64_t* total, int* inexact, cudaStream_t s) {
+  k_exact_sum<<<kRedBlocks, kThreads, 0, s>>>(v, act, n,
+                                              reinterpret_cast<unsigned long long*>(part), inexact);
+  TG_LAUNCH_CHECK();
+  k_exact_total<<<1, kThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(part),
+                                       kRedBlocks, reinterpret_cast<unsigned long long*>(total));
+  TG_LAUNCH_CHECK();
+}
+
+}  // namespace tg

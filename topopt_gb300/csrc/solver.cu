@@ -1,0 +1,777 @@
+// solver.cu -- host orchestration of the reduced system and its solvers.
+//
+// Reference counterparts:
+//   mf_build_reduced (void-DOF gate)   core/src/fea/matfree.cpp:670-834
+//   mf_cg_solve (Eigen-style Jacobi-PCG, the exact fallback) matfree.cpp:841-1076
+//   build_mf_hierarchy / v_cycle / mf_mgpcg   core/src/fea/multigrid.cpp:1344-1515,
+//                                             :780-817, :1143-1160, :1211-1313
+//   solve_mgcg_matfree (budget, fallback)      multigrid.cpp:2098-2320
+//   mixed-precision V-cycle (FP32 fine level)  multigrid.cpp:1179-1204
+//
+// Everything numeric runs on the device; the host only sequences launches and
+// reads two or three FP64 scalars per Krylov iteration (the convergence test).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "tg_solver.h"
+
+namespace tg {
+
+namespace {
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+// Hex8 local node order -> corner bit index (x | y<<1 | z<<2).
+const int kLocToBit[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+const double kXi[8] = {-1, +1, +1, -1, -1, +1, +1, -1};
+const double kEta[8] = {-1, -1, +1, +1, -1, -1, +1, +1};
+const double kZeta[8] = {-1, -1, -1, -1, +1, +1, +1, +1};
+constexpr int kMaxCoarseDof = 8192;  // dense coarsest factor <= 512 MB
+
+MgDims dims_of(int ex, int ey, int ez) { return MgDims{ex, ey, ez, ex + 1, ey + 1, ez + 1}; }
+}  // namespace
+
+// 2x2x2 Gauss integration of B^T D B (the reference's quadrature,
+// hex_element.cpp:23-89), isotropic D (:93-115).
+void hex8_ke(double E, double nu, double h, double* ke) {
+  double D[6][6] = {};
+  const double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  D[0][0] = D[1][1] = D[2][2] = c * (1.0 - nu);
+  D[0][1] = D[0][2] = D[1][0] = D[1][2] = D[2][0] = D[2][1] = c * nu;
+  D[3][3] = D[4][4] = D[5][5] = c * (1.0 - 2.0 * nu) / 2.0;
+  const double g = 1.0 / std::sqrt(3.0);
+  const double pts[2] = {-g, +g};
+  const double half = h / 2.0, detJ = half * half * half, s = 2.0 / h;
+  std::memset(ke, 0, sizeof(double) * 576);
+  for (int ig = 0; ig < 2; ++ig)
+    for (int jg = 0; jg < 2; ++jg)
+      for (int kg = 0; kg < 2; ++kg) {
+        const double xi = pts[ig], eta = pts[jg], zeta = pts[kg];
+        double dx[8], dy[8], dz[8];
+        for (int a = 0; a < 8; ++a) {
+          dx[a] = s * (0.125 * kXi[a] * (1.0 + eta * kEta[a]) * (1.0 + zeta * kZeta[a]));
+          dy[a] = s * (0.125 * kEta[a] * (1.0 + xi * kXi[a]) * (1.0 + zeta * kZeta[a]));
+          dz[a] = s * (0.125 * kZeta[a] * (1.0 + xi * kXi[a]) * (1.0 + eta * kEta[a]));
+        }
+        double B[6][24] = {};
+        for (int a = 0; a < 8; ++a) {
+          B[0][3 * a] = dx[a];
+          B[1][3 * a + 1] = dy[a];
+          B[2][3 * a + 2] = dz[a];
+          B[3][3 * a] = dy[a];
+          B[3][3 * a + 1] = dx[a];
+          B[4][3 * a + 1] = dz[a];
+          B[4][3 * a + 2] = dy[a];
+          B[5][3 * a] = dz[a];
+          B[5][3 * a + 2] = dx[a];
+        }
+        double DB[6][24];
+        for (int r = 0; r < 6; ++r)
+          for (int col = 0; col < 24; ++col) {
+            double acc = 0.0;
+            for (int m = 0; m < 6; ++m) acc += D[r][m] * B[m][col];
+            DB[r][col] = acc;
+          }
+        for (int r = 0; r < 24; ++r)
+          for (int col = 0; col < 24; ++col) {
+            double acc = 0.0;
+            for (int m = 0; m < 6; ++m) acc += B[m][r] * DB[m][col];
+            ke[r * 24 + col] += acc * detJ;
+          }
+      }
+}
+
+// ------------------------------------------------------------- FineProblem
+void FineProblem::build(const tg_grid& grid, double poisson, const tg_dirichlet_bc* bcs, int nbc,
+                        const tg_nodal_load* loads, int nloads, const uint8_t* active_mask,
+                        cudaStream_t s) {
+  if (grid.nx < 1 || grid.ny < 1 || grid.nz < 1) raise(TG_EINVAL, "grid dimensions must be >= 1");
+  if (!(grid.spacing > 0.0)) raise(TG_EINVAL, "hex8_stiffness: element_size must be > 0");
+  if (!(poisson > -1.0 && poisson < 0.5))
+    raise(TG_EINVAL, "hex8_stiffness: poisson must be in (-1, 0.5)");
+  if (nbc < 0 || nloads < 0 || (nbc > 0 && !bcs) || (nloads > 0 && !loads))
+    raise(TG_EINVAL, "bcs/loads arrays do not match their counts");
+  g = Grid::make(grid.nx, grid.ny, grid.nz, grid.spacing);
+  nu = poisson;
+  mc = ModalConsts::make(nu, g.h);
+  ke.assign(576, 0.0);
+  hex8_ke(1.0, nu, g.h, ke.data());
+  mc.kdiag = ke[0];
+  elem_h.assign(size_t(g.nv), 0);
+  for (int64_t e = 0; e < g.nv; ++e)
+    elem_h[size_t(e)] = uint8_t((grid.tags == nullptr || grid.tags[e] != 0) &&
+                                (active_mask == nullptr || active_mask[e] != 0));
+  std::vector<uint8_t>& fixed = fixed_h;
+  fixed.assign(size_t(g.ndof), 0);
+  std::vector<uint8_t> touched(size_t(g.nnodes), 0);
+  up_h.assign(size_t(g.ndof), 0.0);
+  f_h.assign(size_t(g.ndof), 0.0);
+  nonzero_bc = false;
+  for (int b = 0; b < nbc; ++b) {
+    if (bcs[b].node < 0 || bcs[b].node >= g.nnodes || bcs[b].component < 0 || bcs[b].component > 2)
+      raise(TG_EINVAL, "BC index out of range");
+    const int64_t d = 3 * int64_t(bcs[b].node) + bcs[b].component;
+    fixed[size_t(d)] = 1;
+    up_h[size_t(d)] = bcs[b].value;
+    if (bcs[b].value != 0.0) nonzero_bc = true;
+  }
+  for (int l = 0; l < nloads; ++l) {
+    if (loads[l].node < 0 || loads[l].node >= g.nnodes || loads[l].component < 0 ||
+        loads[l].component > 2)
+      raise(TG_EINVAL, "load index out of range");
+    f_h[size_t(3 * int64_t(loads[l].node) + loads[l].component)] += loads[l].value;
+  }
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) {
+        if (!elem_h[size_t((int64_t(k) * g.ny + j) * g.nx + i)]) continue;
+        for (int c = 0; c < 8; ++c) {
+          const int64_t n = (int64_t(k + (c >> 2)) * g.nny + (j + ((c >> 1) & 1))) * g.nnx + i + (c & 1);
+          touched[size_t(n)] = 1;
+        }
+      }
+  kept_h.assign(size_t(g.ndof), 0);
+  ng = 0;
+  n_free = 0;
+  int64_t n_touched_free = 0;
+  double rmax = 0.0;
+  for (int64_t d = 0; d < g.ndof; ++d) {
+    if (fixed[size_t(d)]) continue;
+    ++n_free;
+    rmax = std::max(rmax, std::fabs(f_h[size_t(d)]));
+    if (touched[size_t(d / 3)]) {
+      ++n_touched_free;
+      kept_h[size_t(d)] = 1;
+      ++ng;
+    }
+  }
+  if (n_free > 0 && n_touched_free == 0)
+    raise(TG_ESINGULAR, "singular system (no stiffness - every free DOF is void)");
+  const double load_tol = 1e-9 * rmax;
+  if (!nonzero_bc)
+    for (int64_t d = 0; d < g.ndof; ++d)
+      if (!fixed[size_t(d)] && !touched[size_t(d / 3)] && std::fabs(f_h[size_t(d)]) > load_tol)
+        raise(TG_ESINGULAR,
+              "under-constrained system (load applied to a void DOF with no stiffness - no "
+              "equilibrium possible)");
+  elem.alloc(size_t(g.nv));
+  kept.alloc(size_t(g.ndof));
+  f.alloc(size_t(g.ndof));
+  up.alloc(size_t(g.ndof));
+  TG_CUDA(cudaMemcpyAsync(elem.p, elem_h.data(), elem.bytes(), cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaMemcpyAsync(kept.p, kept_h.data(), kept.bytes(), cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaMemcpyAsync(f.p, f_h.data(), f.bytes(), cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaMemcpyAsync(up.p, up_h.data(), up.bytes(), cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+}
+
+size_t FineProblem::device_bytes() const {
+  return elem.bytes() + kept.bytes() + f.bytes() + up.bytes();
+}
+
+// ------------------------------------------------------------------ levels
+struct Solver::Level {
+  MgDims d{};
+  int64_t nn = 0, ndof = 0, nel = 0, nact = 0;
+  std::vector<uint8_t> act_h;
+  DBuf<uint8_t> act;
+  DBuf<double> Kel, A, invd, xa, xb, b;
+  DBuf<float> Af, invdf, fxa, fxb, fb;
+  double *x = nullptr, *r = nullptr;
+  float *xf = nullptr, *rf = nullptr;
+  template <class T>
+  T*& X();
+  template <class T>
+  T*& R();
+  template <class T>
+  T* B();
+  template <class T>
+  const T* Am();
+  template <class T>
+  const T* Dinv();
+};
+template <>
+double*& Solver::Level::X<double>() { return x; }
+template <>
+float*& Solver::Level::X<float>() { return xf; }
+template <>
+double*& Solver::Level::R<double>() { return r; }
+template <>
+float*& Solver::Level::R<float>() { return rf; }
+template <>
+double* Solver::Level::B<double>() { return b.p; }
+template <>
+float* Solver::Level::B<float>() { return fb.p; }
+template <>
+const double* Solver::Level::Am<double>() { return A.p; }
+template <>
+const float* Solver::Level::Am<float>() { return Af.p; }
+template <>
+const double* Solver::Level::Dinv<double>() { return invd.p; }
+template <>
+const float* Solver::Level::Dinv<float>() { return invdf.p; }
+
+// ------------------------------------------------------------------ Solver
+Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t s)
+    : fp_(fp), opt_(opt), s_(s) {
+  omega_ = opt.omega > 0.0 ? opt.omega : 0.6;
+  budget_ = opt.mg_iter_budget > 0 ? opt.mg_iter_budget : 300;
+  mixed_ = opt.precision == TG_PREC_MIXED;
+  const size_t n = size_t(fp.g.ndof);
+  for (DBuf<double>* b : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_}) b->alloc(n);
+  part_n_ = std::max({kRedBlocks, fine_op_blocks(fp.g, true), fine_op_blocks(fp.g, false),
+                      152 * 32});
+  part_.alloc(size_t(part_n_));
+  scal_.alloc(32);
+  TG_CUDA(cudaMallocHost(&h_scal_, 32 * sizeof(double)));
+  if (mixed_) {
+    Ef_.alloc(size_t(fp.g.nv));
+    for (DBuf<float>* b : {&invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_}) b->alloc(n);
+  }
+  if (opt.solver == TG_SOLVER_MGCG) build_structure();
+}
+
+Solver::~Solver() {
+  if (h_scal_) cudaFreeHost(h_scal_);
+}
+
+size_t Solver::device_bytes() const {
+  size_t b = 0;
+  for (const DBuf<double>* d : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_, &part_,
+                                &scal_, &keb_, &G_, &chol_, &chol_work_})
+    b += d->bytes();
+  for (const DBuf<float>* d : {&Ef_, &invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_})
+    b += d->bytes();
+  for (const auto& L : levels_) {
+    b += L->act.bytes() + L->Kel.bytes() + L->A.bytes() + L->invd.bytes() + L->xa.bytes() +
+         L->xb.bytes() + L->b.bytes();
+    b += L->Af.bytes() + L->invdf.bytes() + L->fxa.bytes() + L->fxb.bytes() + L->fb.bytes();
+  }
+  return b + cidx_.bytes();
+}
+
+void Solver::build_structure() {
+  const Grid& g = fp_.g;
+  const int max_levels = opt_.mg_levels > 0 ? opt_.mg_levels : 64;
+  std::vector<MgDims> dims{dims_of(g.nx, g.ny, g.nz)};
+  // Halve (rounding up) while every coarse axis keeps >= 2 elements
+  // (kMgMinCoarseElems, coarsen.hpp:80); a requested depth below what keeps the
+  // coarsest level dense-factorable is deepened.
+  while (true) {
+    const MgDims& d = dims.back();
+    const int cx = (d.ex + 1) / 2, cy = (d.ey + 1) / 2, cz = (d.ez + 1) / 2;
+    if (cx < 2 || cy < 2 || cz < 2) break;
+    const int64_t dof_here = 3 * int64_t(d.nnx) * d.nny * d.nnz;
+    if (int(dims.size()) >= max_levels && dof_here <= kMaxCoarseDof) break;
+    dims.push_back(dims_of(cx, cy, cz));
+  }
+  if (dims.size() < 2) return;
+  std::vector<uint8_t> prev = fp_.kept_h;
+  MgDims pd = dims[0];
+  for (size_t l = 1; l < dims.size(); ++l) {
+    auto L = std::make_unique<Level>();
+    L->d = dims[l];
+    L->nn = int64_t(L->d.nnx) * L->d.nny * L->d.nnz;
+    L->ndof = 3 * L->nn;
+    L->nel = int64_t(L->d.ex) * L->d.ey * L->d.ez;
+    L->act_h.assign(size_t(L->ndof), 0);
+    for (int c = 0; c < L->d.nnz; ++c)
+      for (int b = 0; b < L->d.nny; ++b)
+        for (int a = 0; a < L->d.nnx; ++a) {
+          if (2 * a >= pd.nnx || 2 * b >= pd.nny || 2 * c >= pd.nnz) continue;  // pad node
+          const int64_t fn = (int64_t(2 * c) * pd.nny + 2 * b) * pd.nnx + 2 * a;
+          const int64_t cn = (int64_t(c) * L->d.nny + b) * L->d.nnx + a;
+          for (int k = 0; k < 3; ++k)
+            if (prev[size_t(3 * fn + k)]) {
+              L->act_h[size_t(3 * cn + k)] = 1;
+              ++L->nact;
+            }
+        }
+    if (L->nact == 0) break;  // multigrid.cpp:1404: nothing left to coarsen onto
+    prev = L->act_h;
+    pd = L->d;
+    levels_.push_back(std::move(L));
+  }
+  if (levels_.empty()) return;
+  // Coarsest compact numbering; too large for a dense factor -> no hierarchy.
+  Level& C = *levels_.back();
+  std::vector<int> cidx(size_t(C.ndof), -1);
+  nc_ = 0;
+  for (int64_t d = 0; d < C.ndof; ++d)
+    if (C.act_h[size_t(d)]) cidx[size_t(d)] = nc_++;
+  if (nc_ > kMaxCoarseDof || nc_ == 0) {
+    levels_.clear();
+    return;
+  }
+  for (auto& Lp : levels_) {
+    Level& L = *Lp;
+    L.act.alloc(size_t(L.ndof));
+    TG_CUDA(cudaMemcpyAsync(L.act.p, L.act_h.data(), L.act.bytes(), cudaMemcpyHostToDevice, s_));
+    L.Kel.alloc(size_t(L.nel) * 576);
+    L.A.alloc(size_t(L.nn) * 243);
+    for (DBuf<double>* b : {&L.invd, &L.xa, &L.xb, &L.b}) b->alloc(size_t(L.ndof));
+    L.x = L.xa.p;
+    L.r = L.xb.p;
+    if (mixed_) {
+      L.Af.alloc(size_t(L.nn) * 243);
+      for (DBuf<float>* b : {&L.invdf, &L.fxa, &L.fxb, &L.fb}) b->alloc(size_t(L.ndof));
+      L.xf = L.fxa.p;
+      L.rf = L.fxb.p;
+    }
+  }
+  cidx_.alloc(size_t(C.ndof));
+  TG_CUDA(cudaMemcpyAsync(cidx_.p, cidx.data(), cidx_.bytes(), cudaMemcpyHostToDevice, s_));
+  chol_.alloc(size_t(nc_) * nc_);
+  chol_work_.alloc(size_t(nc_));
+  chol_fail_.alloc(1);
+  // Ke in corner-bit order and the 8 child Galerkin blocks G_c = W_c^T Ke W_c.
+  std::vector<double> kb(576);
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b)
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          kb[size_t((3 * kLocToBit[a] + i) * 24 + 3 * kLocToBit[b] + j)] =
+              fp_.ke[size_t((3 * a + i) * 24 + 3 * b + j)];
+  auto w1 = [](int pos, int t) { return pos == 1 ? 0.5 : ((pos == 0) == (t == 0) ? 1.0 : 0.0); };
+  std::vector<double> G(8 * 576, 0.0);
+  for (int ch = 0; ch < 8; ++ch) {
+    double W[8][8];
+    for (int sc = 0; sc < 8; ++sc)
+      for (int t = 0; t < 8; ++t)
+        W[sc][t] = w1((ch & 1) + (sc & 1), t & 1) * w1(((ch >> 1) & 1) + ((sc >> 1) & 1), (t >> 1) & 1) *
+                   w1((ch >> 2) + (sc >> 2), t >> 2);
+    for (int t1 = 0; t1 < 8; ++t1)
+      for (int c1 = 0; c1 < 3; ++c1)
+        for (int t2 = 0; t2 < 8; ++t2)
+          for (int c2 = 0; c2 < 3; ++c2) {
+            double acc = 0.0;
+            for (int s1 = 0; s1 < 8; ++s1) {
+              if (W[s1][t1] == 0.0) continue;
+              for (int s2 = 0; s2 < 8; ++s2)
+                acc += W[s1][t1] * W[s2][t2] * kb[size_t((3 * s1 + c1) * 24 + 3 * s2 + c2)];
+            }
+            G[size_t(ch * 576 + (3 * t1 + c1) * 24 + 3 * t2 + c2)] = acc;
+          }
+  }
+  keb_.alloc(576);
+  G_.alloc(8 * 576);
+  TG_CUDA(cudaMemcpyAsync(keb_.p, kb.data(), keb_.bytes(), cudaMemcpyHostToDevice, s_));
+  TG_CUDA(cudaMemcpyAsync(G_.p, G.data(), G_.bytes(), cudaMemcpyHostToDevice, s_));
+  TG_CUDA(cudaStreamSynchronize(s_));
+  have_mg_ = true;
+}
+
+double Solver::read_scalar(int idx) {
+  TG_CUDA(cudaMemcpyAsync(h_scal_ + idx, scal_.p + idx, sizeof(double), cudaMemcpyDeviceToHost, s_));
+  TG_CUDA(cudaStreamSynchronize(s_));
+  return h_scal_[idx];
+}
+
+void Solver::read_scalars(int idx0, int n, double* out) {
+  TG_CUDA(cudaMemcpyAsync(h_scal_ + idx0, scal_.p + idx0, sizeof(double) * n,
+                          cudaMemcpyDeviceToHost, s_));
+  TG_CUDA(cudaStreamSynchronize(s_));
+  for (int i = 0; i < n; ++i) out[i] = h_scal_[idx0 + i];
+}
+
+void Solver::apply_unmasked(const double* E, const double* x, double* y) {
+  launch_fine_op<double>(kApply, fp_.g, fp_.mc, E, nullptr, x, nullptr, nullptr, 0.0, y, nullptr,
+                         nullptr, s_);
+}
+
+double Solver::time_operator(bool fp32, int reps) {
+  const Grid& g = fp_.g;
+  if (fp32 && !mixed_) raise(TG_EINVAL, "time_operator: FP32 operator needs a mixed-precision job");
+  launch_fill<double>(p_.p, 1.0, g.ndof, s_);
+  if (fp32) launch_copy_d2f(pf_.p, p_.p, g.ndof, s_);
+  cudaEvent_t a, b;
+  TG_CUDA(cudaEventCreate(&a));
+  TG_CUDA(cudaEventCreate(&b));
+  TG_CUDA(cudaEventRecord(a, s_));
+  for (int i = 0; i < reps; ++i) {
+    if (fp32)
+      launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
+                            apf_.p, nullptr, nullptr, s_);
+    else
+      launch_fine_op<double>(kApply, g, fp_.mc, E_, fp_.kept.p, p_.p, nullptr, nullptr, 0.0,
+                             ap_.p, nullptr, nullptr, s_);
+  }
+  TG_CUDA(cudaEventRecord(b, s_));
+  TG_CUDA(cudaEventSynchronize(b));
+  float ms = 0.0f;
+  TG_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return double(ms) / reps;
+}
+
+void Solver::set_modulus(const double* E) {
+  E_ = E;
+  const Grid& g = fp_.g;
+  launch_fine_invdiag(g, fp_.mc.kdiag, E, fp_.kept.p, invdiag_.p, s_);
+  // rhs = f - K u_p on the kept DOFs (matfree.cpp:740-750).
+  if (fp_.nonzero_bc) {
+    apply_unmasked(E, fp_.up.p, t0_.p);
+  } else {
+    launch_fill<double>(t0_.p, 0.0, g.ndof, s_);
+  }
+  launch_sub_mask(rhs_.p, fp_.f.p, t0_.p, fp_.kept.p, g.ndof, s_);
+  if (fp_.nonzero_bc) {
+    // The void-load check on the full right-hand side f - K u_p, rmax over the
+    // free DOFs (matfree.cpp:796-814).
+    std::vector<double> kup(size_t(g.ndof));
+    TG_CUDA(cudaMemcpyAsync(kup.data(), t0_.p, t0_.bytes(), cudaMemcpyDeviceToHost, s_));
+    TG_CUDA(cudaStreamSynchronize(s_));
+    double rmax = 0.0;
+    for (int64_t d = 0; d < g.ndof; ++d)
+      if (!fp_.fixed_h[size_t(d)])
+        rmax = std::max(rmax, std::fabs(fp_.f_h[size_t(d)] - kup[size_t(d)]));
+    for (int64_t d = 0; d < g.ndof; ++d)
+      if (!fp_.fixed_h[size_t(d)] && !fp_.kept_h[size_t(d)] &&
+          std::fabs(fp_.f_h[size_t(d)] - kup[size_t(d)]) > 1e-9 * rmax)
+        raise(TG_ESINGULAR,
+              "under-constrained system (load applied to a void DOF with no stiffness - no "
+              "equilibrium possible)");
+  }
+  if (mixed_) {
+    launch_copy_d2f(Ef_.p, E, g.nv, s_);
+    launch_copy_d2f(invdiagf_.p, invdiag_.p, g.ndof, s_);
+  }
+  if (have_mg_) build_numeric();
+}
+
+void Solver::build_numeric() {
+  const Grid& g = fp_.g;
+  const MgDims fd = dims_of(g.nx, g.ny, g.nz);
+  MgDims pd = fd;
+  for (size_t l = 0; l < levels_.size(); ++l) {
+    Level& L = *levels_[l];
+    if (l == 0)
+      mg_galerkin_level1(fd, L.d, E_, fp_.kept.p, L.act.p, keb_.p, G_.p, L.Kel.p, s_);
+    else
+      mg_galerkin_coarse(pd, L.d, levels_[l - 1]->Kel.p, L.act.p, L.Kel.p, s_);
+    mg_assemble_stencil(L.d, L.Kel.p, L.act.p, L.A.p, L.invd.p, s_);
+    if (mixed_) {
+      mg_to_float(L.A.p, L.Af.p, L.nn * 243, s_);
+      mg_to_float(L.invd.p, L.invdf.p, L.ndof, s_);
+    }
+    pd = L.d;
+  }
+  Level& C = *levels_.back();
+  mg_dense_from_stencil(C.d, C.A.p, cidx_.p, nc_, chol_.p, s_);
+  TG_CUDA(cudaMemsetAsync(chol_fail_.p, 0, sizeof(int), s_));
+  mg_cholesky(chol_.p, nc_, chol_fail_.p, s_);
+  int fail = 0;
+  TG_CUDA(cudaMemcpyAsync(&fail, chol_fail_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+  TG_CUDA(cudaStreamSynchronize(s_));
+  numeric_ok_ = (fail == 0);
+}
+
+// ------------------------------------------------------------------ V-cycle
+template <class T>
+void Solver::vcycle_level(size_t l) {
+  Level& L = *levels_[l - 1];
+  if (l == levels_.size()) {
+    mg_chol_solve<T>(chol_.p, nc_, cidx_.p, L.ndof, L.B<T>(), L.X<T>(), chol_work_.p, s_);
+    return;
+  }
+  Level& N = *levels_[l];
+  const T w = T(omega_);
+  mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);
+  mg_stencil_op<T>(kResidual, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
+                   L.R<T>(), s_);
+  mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
+  vcycle_level<T>(l + 1);
+  mg_prolong_add<T>(L.d, N.d, N.X<T>(), L.act.p, L.X<T>(), s_);
+  mg_stencil_op<T>(kSmooth, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
+                   L.R<T>(), s_);
+  std::swap(L.X<T>(), L.R<T>());
+}
+
+template <>
+double* Solver::vcycle<double>(const double* b) {
+  const Grid& g = fp_.g;
+  Level& N = *levels_[0];
+  const MgDims fd = dims_of(g.nx, g.ny, g.nz);
+  double* x = t1_.p;
+  double* r = t0_.p;
+  mg_jacobi_first<double>(b, invdiag_.p, omega_, g.ndof, x, s_);
+  launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
+                         nullptr, nullptr, s_);
+  mg_restrict<double>(fd, N.d, r, N.act.p, N.B<double>(), s_);
+  vcycle_level<double>(1);
+  mg_prolong_add<double>(fd, N.d, N.X<double>(), fp_.kept.p, x, s_);
+  launch_fine_op<double>(kSmooth, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
+                         nullptr, nullptr, s_);
+  fine_matvecs_ += 2;
+  return r;
+}
+
+template <>
+float* Solver::vcycle<float>(const float* b) {
+  const Grid& g = fp_.g;
+  Level& N = *levels_[0];
+  const MgDims fd = dims_of(g.nx, g.ny, g.nz);
+  float* x = t1f_.p;
+  float* r = t0f_.p;
+  const float w = float(omega_);
+  mg_jacobi_first<float>(b, invdiagf_.p, w, g.ndof, x, s_);
+  launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
+                        nullptr, s_);
+  mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_);
+  vcycle_level<float>(1);
+  mg_prolong_add<float>(fd, N.d, N.X<float>(), fp_.kept.p, x, s_);
+  launch_fine_op<float>(kSmooth, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
+                        nullptr, s_);
+  lowp_matvecs_ += 2;
+  return r;
+}
+
+// ------------------------------------------------------------------ MG-PCG
+// mf_mgpcg (multigrid.cpp:1211-1313): stop at ||r|| <= tol ||b||, breakdown when
+// pAp <= 0 or non-finite, x finite at exit.
+bool Solver::mgpcg(double tol, int max_it, bool warm, SolverStats& st) {
+  const Grid& g = fp_.g;
+  const int64_t n = g.ndof;
+  launch_dot(rhs_.p, rhs_.p, n, part_.p, scal_.p + 4, s_);
+  const double bnorm2 = read_scalar(4);
+  st.iterations = 0;
+  st.residual = 0.0;
+  if (!(bnorm2 > 0.0)) {
+    launch_fill<double>(x_.p, 0.0, n, s_);
+    return true;
+  }
+  const double bnorm = std::sqrt(bnorm2), threshold = tol * bnorm;
+  if (warm) {
+    launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x_.p, rhs_.p, nullptr, 0.0, r_.p,
+                           nullptr, nullptr, s_);
+    ++fine_matvecs_;
+  } else {
+    launch_fill<double>(x_.p, 0.0, n, s_);
+    TG_CUDA(cudaMemcpyAsync(r_.p, rhs_.p, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, s_));
+  }
+  double* z = vcycle<double>(r_.p);
+  TG_CUDA(cudaMemcpyAsync(p_.p, z, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, s_));
+  launch_dot(r_.p, z, n, part_.p, scal_.p + 0, s_);
+  if (!std::isfinite(read_scalar(0))) return false;
+  int nb = 0;
+  for (int k = 1; k <= max_it; ++k) {
+    launch_fine_op<double>(kApply, g, fp_.mc, E_, fp_.kept.p, p_.p, nullptr, nullptr, 0.0, ap_.p,
+                           part_.p, &nb, s_);
+    ++fine_matvecs_;
+    launch_sum_partials(part_.p, nb, scal_.p + 1, s_);
+    launch_cg_update_xr<double>(x_.p, r_.p, p_.p, ap_.p, scal_.p + 0, scal_.p + 1, n, part_.p, s_);
+    launch_sum_partials(part_.p, kRedBlocks, scal_.p + 2, s_);
+    double sc[2];
+    read_scalars(1, 2, sc);
+    const double pap = sc[0], rr = sc[1];
+    if (!(pap > 0.0) || !std::isfinite(pap)) return false;
+    st.iterations = k;
+    const double rn = std::sqrt(rr);
+    st.residual = rn / bnorm;
+    if (rn <= threshold) {
+      launch_dot(x_.p, x_.p, n, part_.p, scal_.p + 5, s_);
+      return std::isfinite(read_scalar(5));
+    }
+    z = vcycle<double>(r_.p);
+    launch_dot(r_.p, z, n, part_.p, scal_.p + 3, s_);
+    launch_cg_update_p<double>(p_.p, z, scal_.p + 3, scal_.p + 0, n, s_);
+    TG_CUDA(cudaMemcpyAsync(scal_.p + 0, scal_.p + 3, sizeof(double), cudaMemcpyDeviceToDevice, s_));
+  }
+  return false;
+}
+
+// FP32 inner MG-PCG on the unit-norm residual held in zf_; solution in xf_.
+// FP64 dot products; stops at relative residual rel_tol or max_it.
+template <>
+bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* iters) {
+  const Grid& g = fp_.g;
+  const int64_t n = g.ndof;
+  launch_fill<float>(xf_.p, 0.0f, n, s_);
+  TG_CUDA(cudaMemcpyAsync(rf_.p, zf_.p, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, s_));
+  launch_dot_f(rf_.p, rf_.p, n, part_.p, scal_.p + 10, s_);
+  float* z = vcycle<float>(rf_.p);
+  TG_CUDA(cudaMemcpyAsync(pf_.p, z, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, s_));
+  launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 6, s_);
+  const double b2 = read_scalar(10);
+  const double thr = rel_tol * std::sqrt(b2);
+  int nb = 0;
+  *iters = 0;
+  for (int k = 1; k <= max_it; ++k) {
+    launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
+                          apf_.p, part_.p, &nb, s_);
+    ++lowp_matvecs_;
+    launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
+    launch_cg_update_xr<float>(xf_.p, rf_.p, pf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);
+    launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
+    double sc[2];
+    read_scalars(7, 2, sc);
+    if (!(sc[0] > 0.0) || !std::isfinite(sc[0])) return k > 1;
+    *iters = k;
+    if (std::sqrt(sc[1]) <= thr) return true;
+    z = vcycle<float>(rf_.p);
+    launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 9, s_);
+    launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
+    TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice, s_));
+  }
+  (void)st;
+  return true;
+}
+
+// Mixed precision: FP64 iterative refinement around FP32 MG-PCG inner solves.
+// Convergence is judged on the FP64-recomputed residual ||b - A x|| <= tol ||b||.
+bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
+  const Grid& g = fp_.g;
+  const int64_t n = g.ndof;
+  launch_dot(rhs_.p, rhs_.p, n, part_.p, scal_.p + 4, s_);
+  const double bnorm2 = read_scalar(4);
+  st.iterations = 0;
+  st.residual = 0.0;
+  if (!(bnorm2 > 0.0)) {
+    launch_fill<double>(x_.p, 0.0, n, s_);
+    return true;
+  }
+  const double bnorm = std::sqrt(bnorm2), threshold = tol * bnorm;
+  if (warm) {
+    launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x_.p, rhs_.p, nullptr, 0.0, r_.p,
+                           nullptr, nullptr, s_);
+    ++fine_matvecs_;
+  } else {
+    launch_fill<double>(x_.p, 0.0, n, s_);
+    TG_CUDA(cudaMemcpyAsync(r_.p, rhs_.p, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, s_));
+  }
+  const double inner_tol = opt_.inner_tolerance > 0.0 ? opt_.inner_tolerance : 1e-3;
+  const int max_ref = opt_.max_refinements > 0 ? opt_.max_refinements : 20;
+  int total_inner = 0;
+  for (int ref = 0; ref <= max_ref; ++ref) {
+    launch_dot(r_.p, r_.p, n, part_.p, scal_.p + 5, s_);
+    const double rr = read_scalar(5);
+    const double rn = std::sqrt(rr);
+    st.residual = rn / bnorm;
+    if (!std::isfinite(rn)) return false;
+    if (rn <= threshold) {
+      st.iterations = total_inner;
+      return true;
+    }
+    if (ref == max_ref || total_inner >= max_it) break;
+    launch_scale_d2f(zf_.p, r_.p, scal_.p + 5, n, s_);
+    int it = 0;
+    inner_pcg<float>(std::min(budget_, max_it - total_inner), inner_tol, st, &it);
+    total_inner += it;
+    launch_axpy_scaled_f2d(x_.p, xf_.p, scal_.p + 5, n, s_);
+    launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x_.p, rhs_.p, nullptr, 0.0, r_.p,
+                           nullptr, nullptr, s_);
+    ++fine_matvecs_;
+    ++st.refinements;
+  }
+  st.iterations = total_inner;
+  return false;
+}
+
+// ------------------------------------------------------------ Jacobi-PCG
+// The Eigen-style Jacobi-PCG of mf_cg_solve (matfree.cpp:841-1076): squared
+// threshold tol^2 |b|^2 clamped to DBL_MIN, the converging iteration uncounted.
+bool Solver::jacobi_pcg(double tol, int max_it, bool warm, SolverStats& st) {
+  const Grid& g = fp_.g;
+  const int64_t n = g.ndof;
+  const int maxIters = max_it > 0 ? max_it : int(std::min<int64_t>(2 * fp_.ng, 1 << 30));
+  launch_dot(rhs_.p, rhs_.p, n, part_.p, scal_.p + 4, s_);
+  const double rhs2 = read_scalar(4);
+  st.iterations = 0;
+  st.residual = 0.0;
+  if (rhs2 == 0.0) {
+    launch_fill<double>(x_.p, 0.0, n, s_);
+    return true;
+  }
+  double threshold = tol * tol * rhs2;
+  if (threshold < std::numeric_limits<double>::min()) threshold = std::numeric_limits<double>::min();
+  if (!warm) launch_fill<double>(x_.p, 0.0, n, s_);
+  launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x_.p, rhs_.p, nullptr, 0.0, r_.p,
+                         nullptr, nullptr, s_);
+  ++fine_matvecs_;
+  launch_dot(r_.p, r_.p, n, part_.p, scal_.p + 2, s_);
+  double rr = read_scalar(2);
+  if (rr < threshold) {
+    st.residual = std::sqrt(rr / rhs2);
+    return st.residual <= tol;
+  }
+  launch_scale_mask(p_.p, r_.p, invdiag_.p, n, part_.p, s_);
+  launch_sum_partials(part_.p, kRedBlocks, scal_.p + 0, s_);
+  int i = 0, nb = 0;
+  while (i < maxIters) {
+    launch_fine_op<double>(kApply, g, fp_.mc, E_, fp_.kept.p, p_.p, nullptr, nullptr, 0.0, ap_.p,
+                           part_.p, &nb, s_);
+    ++fine_matvecs_;
+    launch_sum_partials(part_.p, nb, scal_.p + 1, s_);
+    launch_cg_update_xr<double>(x_.p, r_.p, p_.p, ap_.p, scal_.p + 0, scal_.p + 1, n, part_.p, s_);
+    launch_sum_partials(part_.p, kRedBlocks, scal_.p + 2, s_);
+    rr = read_scalar(2);
+    if (rr < threshold) break;
+    launch_scale_mask(z_.p, r_.p, invdiag_.p, n, part_.p, s_);
+    launch_sum_partials(part_.p, kRedBlocks, scal_.p + 3, s_);
+    launch_cg_update_p<double>(p_.p, z_.p, scal_.p + 3, scal_.p + 0, n, s_);
+    TG_CUDA(cudaMemcpyAsync(scal_.p + 0, scal_.p + 3, sizeof(double), cudaMemcpyDeviceToDevice, s_));
+    ++i;
+  }
+  st.iterations = i;
+  st.residual = std::sqrt(rr / rhs2);
+  launch_dot(x_.p, x_.p, n, part_.p, scal_.p + 5, s_);
+  const bool finite = std::isfinite(read_scalar(5));
+  return st.residual <= tol && finite;
+}
+
+// ------------------------------------------------------------------ solve
+SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u) {
+  SolverStats st;
+  const double t0 = now_ms();
+  fine_matvecs_ = lowp_matvecs_ = 0;
+  const Grid& g = fp_.g;
+  st.hier_built = have_mg_ && numeric_ok_;
+  if (fp_.ng == 0) {
+    st.converged = true;
+    launch_mask_select(u, nullptr, fp_.up.p, fp_.kept.p, g.ndof, s_);
+    TG_CUDA(cudaStreamSynchronize(s_));
+    return st;
+  }
+  const int cap = max_it > 0 ? max_it : int(std::max<int64_t>(1000, 2 * fp_.ng));
+  const bool warm = guess != nullptr;
+  auto seed = [&]() { launch_mask_select(x_.p, guess, nullptr, fp_.kept.p, g.ndof, s_); };
+  bool solved = false;
+  if (have_mg_ && numeric_ok_) {
+    if (mixed_) {
+      if (warm) seed();
+      solved = mixed_refine(tol, std::min(cap, budget_), warm, st);
+    }
+    if (!solved) {
+      if (warm) seed();
+      solved = mgpcg(tol, std::min(cap, budget_), warm, st);
+    }
+    st.mg_cycles = st.iterations;
+    if (solved) {
+      st.used_mg = true;
+      st.mg_levels = levels();
+    }
+  }
+  if (!solved) {
+    if (warm) seed();
+    solved = jacobi_pcg(tol, cap, warm, st);
+    st.used_mg = false;
+    st.mg_levels = 0;
+  }
+  st.converged = solved;
+  st.matvecs = fine_matvecs_;
+  st.matvecs_lowp = lowp_matvecs_;
+  if (solved) launch_mask_select(u, x_.p, fp_.up.p, fp_.kept.p, g.ndof, s_);
+  TG_CUDA(cudaStreamSynchronize(s_));
+  st.t_solve_ms = now_ms() - t0;
+  return st;
+}
+
+}  // namespace tg

@@ -1,0 +1,190 @@
+// tg_internal.h -- shared declarations of the GB300 voxel-SIMP library.
+//
+// Layout in HBM (all arrays dense, structure-of-arrays where it matters):
+//   element arrays  [nv]          voxel order (k*ny + j)*nx + i
+//   DOF vectors     [ndof]        node-major interleaved, 3*node + comp
+//   kept mask       [ndof] uint8  1 on surviving free DOFs
+// Vectors of the reduced system are kept full length with zeros on non-kept
+// DOFs, so the fine operator never scatters or gathers through an index list.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/topopt_gb300.h"
+
+namespace tg {
+
+struct Error : std::runtime_error {
+  int code;
+  double residual = 0.0;
+  int iterations = 0;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void raise(int code, const std::string& msg);
+void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define TG_CUDA(call)                                                  \
+  do {                                                                 \
+    cudaError_t tg_e_ = (call);                                        \
+    if (tg_e_ != cudaSuccess) ::tg::cuda_fail(tg_e_, #call, __FILE__, __LINE__); \
+  } while (0)
+void note_launch();
+#define TG_LAUNCH_CHECK()          \
+  do {                             \
+    ::tg::note_launch();           \
+    TG_CUDA(cudaGetLastError());   \
+  } while (0)
+
+// Owning device buffer (cudaMallocAsync on the job's stream would tie lifetime to
+// a stream; plain cudaMalloc keeps ownership simple for long-lived job state).
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count) {
+      cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+      if (e != cudaSuccess) {
+        p = nullptr;
+        raise(TG_ENOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
+                             cudaGetErrorString(e));
+      }
+    }
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct Grid {
+  int nx = 0, ny = 0, nz = 0;
+  double h = 1.0;
+  int nnx = 0, nny = 0, nnz = 0;
+  int64_t nv = 0, nnodes = 0, ndof = 0;
+  static Grid make(int nx, int ny, int nz, double h) {
+    Grid g;
+    g.nx = nx; g.ny = ny; g.nz = nz; g.h = h;
+    g.nnx = nx + 1; g.nny = ny + 1; g.nnz = nz + 1;
+    g.nv = int64_t(nx) * ny * nz;
+    g.nnodes = int64_t(g.nnx) * g.nny * g.nnz;
+    g.ndof = 3 * g.nnodes;
+    return g;
+  }
+};
+
+// Per-class constants of the Walsh-modal hex8 operator for unit modulus:
+// L[k] = lambda*h/(16*3^k), M[k] = mu*h/(16*3^k), k = number of axes a mode's
+// gradient coefficient is constant along (see k_operator.cu).
+struct ModalConsts {
+  double L[3], M[3];
+  double kdiag;  // the (common) diagonal entry of the unit-modulus Ke
+  static ModalConsts make(double nu, double h);
+};
+
+// ---------------------------------------------------------------- operator
+enum ApplyMode { kApply = 0, kResidual = 1, kSmooth = 2 };
+
+// Fine operator on the full grid, element factors `ef` (0 = no element):
+//   kApply:    y = M A x                 (M = kept mask; dot = sum x.y if dot_part)
+//   kResidual: y = M (b - A x)
+//   kSmooth:   y = x + omega*invdiag*(b - A x)   (invdiag is 0 off the kept set)
+template <class T>
+void launch_fine_op(int mode, const Grid& g, const ModalConsts& mc, const T* ef,
+                    const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
+                    T* y, double* dot_part, int* nblocks_out, cudaStream_t s);
+int fine_op_blocks(const Grid& g, bool fp64);
+
+// Jacobi diagonal of the fine operator: diag = kdiag * sum of adjacent factors.
+void launch_fine_invdiag(const Grid& g, double kdiag, const double* ef, const uint8_t* kept,
+                         double* invdiag, cudaStream_t s);
+
+// ------------------------------------------------------------------ vectors
+// Deterministic reductions: a fixed grid of kRedBlocks blocks writes partials,
+// one block sums them in order.
+constexpr int kRedBlocks = 608;  // 4 x 152 SMs
+void launch_dot(const double* a, const double* b, int64_t n, double* part, double* out,
+                cudaStream_t s);
+void launch_dot_f(const float* a, const float* b, int64_t n, double* part, double* out,
+                  cudaStream_t s);
+void launch_sum_partials(const double* part, int n, double* out, cudaStream_t s);
+// PCG pieces with scalars living in device memory (no host round trip).
+template <class T>
+void launch_cg_update_xr(T* x, T* r, const T* p, const T* ap, const double* rz,
+                         const double* pap, int64_t n, double* rr_part, cudaStream_t s);
+void launch_scale_mask(double* z, const double* r, const double* invdiag, int64_t n,
+                       double* rz_part, cudaStream_t s);
+template <class T>
+void launch_cg_update_p(T* p, const T* z, const double* rz_new, const double* rz_old, int64_t n,
+                        cudaStream_t s);
+void launch_scale_d2f(float* dst, const double* src, const double* nrm2, int64_t n,
+                      cudaStream_t s);
+void launch_axpy_scaled_f2d(double* y, const float* x, const double* nrm2, int64_t n,
+                            cudaStream_t s);
+template <class T>
+void launch_fill(T* a, T v, int64_t n, cudaStream_t s);
+void launch_copy_d2f(float* dst, const double* src, int64_t n, cudaStream_t s);
+void launch_axpy_f2d(double* y, const float* x, int64_t n, cudaStream_t s);
+void launch_sub_mask(double* r, const double* b, const double* ax, const uint8_t* kept, int64_t n,
+                     cudaStream_t s);
+// u = kept ? x : alt; a null x or alt reads as zeros.
+void launch_mask_select(double* u, const double* x, const double* alt, const uint8_t* kept,
+                        int64_t n, cudaStream_t s);
+
+// ---------------------------------------------------------------- SIMP
+void launch_modulus(const double* rho, const uint8_t* elem, int64_t n, double E0, double p,
+                    double rho_min, int law, double emin, double* E, cudaStream_t s);
+// Compliance + sensitivity sweep: dc[e], and per-block partial compliances.
+void launch_sensitivity(const Grid& g, const ModalConsts& mc, const double* rho,
+                        const uint8_t* elem, const double* u, double E0, double p,
+                        double rho_min, int law, double emin, double* dc, double* c_part,
+                        int* nparts, cudaStream_t s);
+
+struct FilterStencil {
+  int R = 0, n = 0;
+  std::vector<int> di, dj, dk;
+  std::vector<double> w;
+  static FilterStencil make(double radius);
+};
+// Uploads the stencil into `buf`; returns the device pointer kernels take.
+void* filter_stencil_device(const FilterStencil& st, DBuf<unsigned char>& buf, cudaStream_t s);
+void launch_weight_sum(const Grid& g, const void* st, int ns, const uint8_t* act, double* hs,
+                       cudaStream_t s);
+void launch_filter_fwd(const Grid& g, const void* st, int ns, const uint8_t* act,
+                       const double* hs, const double* x, double* out, cudaStream_t s);
+void launch_filter_adj(const Grid& g, const void* st, int ns, const uint8_t* act,
+                       const double* hs, const double* s_in, double* tmp, double* out,
+                       cudaStream_t s);
+void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
+                         const uint8_t* act, int64_t n, double lambda, double move,
+                         double rho_min, double* xnew, cudaStream_t s);
+// Exact (fixed-point, order independent) sum of a non-negative field over the
+// solid voxels; returns per-block 192-bit partials, then the final total.
+int exact_sum_blocks();
+void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,
+                      uint64_t* total, int* inexact, cudaStream_t s);
+double fma_probe_tflops(bool fp64);
+void launch_absdiff_max(const double* a, const double* b, int64_t n, double* part, double* out,
+                        cudaStream_t s);
+
+}  // namespace tg

@@ -1,0 +1,40 @@
+// tg_multigrid.h -- launchers of the multigrid kernels (k_multigrid.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace tg {
+
+// Element and node extents of one hierarchy level.
+struct MgDims {
+  int ex, ey, ez, nnx, nny, nnz;
+};
+
+void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const double* ef,
+                        const uint8_t* fact, const uint8_t* cact, const double* Ke,
+                        const double* G, double* Kc, cudaStream_t s);
+void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const double* Kf, const uint8_t* cact,
+                        double* Kc, cudaStream_t s);
+void mg_assemble_stencil(const MgDims& d, const double* Kel, const uint8_t* act, double* A,
+                         double* invdiag, cudaStream_t s);
+void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s);
+template <class T>
+void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
+                   const T* b, const T* invdiag, T omega, T* y, cudaStream_t s);
+template <class T>
+void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cudaStream_t s);
+template <class T>
+void mg_restrict(const MgDims& fd, const MgDims& cd, const T* rf, const uint8_t* cact, T* bc,
+                 cudaStream_t s);
+template <class T>
+void mg_prolong_add(const MgDims& fd, const MgDims& cd, const T* ec, const uint8_t* fact, T* xf,
+                    cudaStream_t s);
+void mg_dense_from_stencil(const MgDims& d, const double* A, const int* cidx, int nc, double* D,
+                           cudaStream_t s);
+void mg_cholesky(double* D, int nc, int* fail, cudaStream_t s);
+template <class T>
+void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const T* b, T* x,
+                   double* work, cudaStream_t s);
+
+}  // namespace tg

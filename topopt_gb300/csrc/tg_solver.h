@@ -1,0 +1,113 @@
+// tg_solver.h -- the reduced FEA system and its solvers (host orchestration).
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "tg_internal.h"
+#include "tg_multigrid.h"
+
+namespace tg {
+
+// Host Ke of the reference's 2x2x2 Gauss integration (hex_element.cpp:23-115),
+// row-major 24x24 in the reference's local node order.
+void hex8_ke(double E, double nu, double h, double* ke576);
+
+// The design-independent part of the reduced, void-gated system
+// (matfree.cpp:670-834): which elements exist, which DOFs survive, the load
+// vector and the prescribed field.  Built once per grid + BCs + active mask.
+struct FineProblem {
+  Grid g;
+  double nu = 0.3;
+  ModalConsts mc{};
+  std::vector<double> ke;          // unit-modulus Ke, reference order
+  std::vector<uint8_t> elem_h;     // element exists (solid and active) [nv]
+  std::vector<uint8_t> kept_h;     // [ndof]
+  std::vector<double> f_h;         // load vector [ndof]
+  std::vector<double> up_h;        // prescribed field [ndof]
+  std::vector<uint8_t> fixed_h;    // Dirichlet mask [ndof]
+  bool nonzero_bc = false;
+  int64_t ng = 0, n_free = 0;
+  DBuf<uint8_t> elem, kept;
+  DBuf<double> f, up;
+
+  // Throws Error(TG_EINVAL) on bad indices, Error(TG_ESINGULAR) on a void-only
+  // system or a load on a void DOF (the load check uses f; with non-zero
+  // prescribed values the caller re-checks with f - K u_p).
+  void build(const tg_grid& grid, double poisson, const tg_dirichlet_bc* bcs, int nbc,
+             const tg_nodal_load* loads, int nloads, const uint8_t* active_mask,
+             cudaStream_t s);
+  size_t device_bytes() const;
+};
+
+struct SolverStats {
+  int iterations = 0;
+  double residual = 0.0;
+  bool converged = false, used_mg = false, hier_built = false;
+  int mg_levels = 0, mg_cycles = 0, refinements = 0;
+  int64_t matvecs = 0, matvecs_lowp = 0;
+  double t_mg_build_ms = 0.0, t_solve_ms = 0.0;
+};
+
+// The solver holds device state sized for one FineProblem; per solve it takes
+// element factors E (device, [nv], 0 = no element) and returns x on the kept
+// DOFs (full length, 0 elsewhere).
+class Solver {
+ public:
+  Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t s);
+  ~Solver();
+  // Set the element factors for the next solve: rebuilds the Jacobi diagonal,
+  // the reduced right-hand side and (MG) the numeric hierarchy.
+  void set_modulus(const double* E);
+  // Solve A x = rhs to ||r|| <= tol ||rhs||.  guess (device, ndof) may be null.
+  // Writes the full displacement u = x on kept DOFs, u_p elsewhere.
+  SolverStats solve(double tol, int max_it, const double* guess, double* u);
+  // y = A x on the full grid (no mask), for the public apply entry point.
+  void apply_unmasked(const double* E, const double* x, double* y);
+  const double* rhs() const { return rhs_.p; }
+  // Time `reps` fine-operator launches (FP64 or FP32) on the current factors.
+  double time_operator(bool fp32, int reps);
+  size_t device_bytes() const;
+  int levels() const { return int(levels_.size()) + 1; }
+
+ private:
+  struct Level;
+  struct Impl;
+  void build_structure();
+  void build_numeric();
+  bool mgpcg(double tol, int max_it, bool warm, SolverStats& st);
+  bool jacobi_pcg(double tol, int max_it, bool warm, SolverStats& st);
+  bool mixed_refine(double tol, int max_it, bool warm, SolverStats& st);
+  template <class T>
+  T* vcycle(const T* b);
+  template <class T>
+  void vcycle_level(size_t l);
+  template <class T>
+  bool inner_pcg(int max_it, double rel_tol, SolverStats& st, int* iters);
+  double read_scalar(int idx);
+  void read_scalars(int idx0, int n, double* out);
+
+  const FineProblem& fp_;
+  tg_solve_options opt_;
+  cudaStream_t s_;
+  double omega_ = 0.6;
+  int budget_ = 300;
+  bool mixed_ = false;
+  // fine state
+  const double* E_ = nullptr;
+  DBuf<double> invdiag_, rhs_, x_, r_, z_, p_, ap_, t0_, t1_;
+  DBuf<float> Ef_, invdiagf_, xf_, rf_, zf_, pf_, apf_, t0f_, t1f_;
+  DBuf<double> part_, scal_;
+  double* h_scal_ = nullptr;  // pinned
+  int part_n_ = 0;
+  // hierarchy
+  std::vector<std::unique_ptr<Level>> levels_;  // levels 1..L-1
+  DBuf<double> keb_, G_;                         // Ke in corner-bit order, 8 G_c
+  bool have_mg_ = false, numeric_ok_ = false;
+  int64_t fine_matvecs_ = 0, lowp_matvecs_ = 0;
+  int nc_ = 0;
+  DBuf<int> cidx_, chol_fail_;
+  DBuf<double> chol_, chol_work_;
+};
+
+}  // namespace tg
