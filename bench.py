@@ -294,7 +294,7 @@ def run_ours(args, world, rank, local, pg):
         job.close()
     # Mixed vs FP64 accuracy on the same design (compliance and displacement).
     acc = {}
-    if not args.skip_fp64:
+    if not args.skip_fp64 and not args.profile:
         r64 = tg.simp_compliance(pb, params, _phys_of(tg, pb, design), tolerance=1e-8,
                                  options=tg.SolveOptions(precision=tg.PREC_FP64))
         r32 = tg.simp_compliance(pb, params, _phys_of(tg, pb, design), tolerance=1e-8,
@@ -309,7 +309,8 @@ def run_ours(args, world, rank, local, pg):
     o = opts(tg.PREC_MIXED, K)
     barrier(pg)
     t0 = time.perf_counter()
-    res = tg.simp_optimize(pb, params, o)
+    if not args.profile:
+        tg.simp_optimize(pb, params, o)
     e2e_wall = max_over_ranks(pg, time.perf_counter() - t0)
     nv, ndof = pb.nv, pb.ndof
     h2d = (len(bcs) + len(loads)) * 16 + 64
@@ -348,6 +349,21 @@ def run_ours(args, world, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def run_op_only(args):
+    """Three fine-operator applies at the workload size (for ncu captures)."""
+    import topopt_gb300 as tg
+    from topopt_gb300.build import build
+    build()
+    pb = tg.Problem(args.nx, args.ny, args.nz)
+    rng = np.random.default_rng(0)
+    f = rng.random(pb.nv) * 0.999 + 0.001
+    u = rng.standard_normal(pb.ndof)
+    prec = tg.PREC_MIXED if args.op_only == "fp32" else tg.PREC_FP64
+    for _ in range(3):
+        y = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f, precision=prec)
+    print(json.dumps({"op_only": args.op_only, "checksum": float(np.abs(y).sum())}))
+
+
 def _phys_of(tg, pb, design):
     return tg.make_density_filter(pb, 1.5).filter_density(design)
 
@@ -365,9 +381,18 @@ def main():
     ap.add_argument("--ref-applies", type=float, default=60.0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--op-only", choices=["fp32", "fp64"], default=None,
+                    help="profiling aid: run only the fine operator (fea_matfree_apply) 3 times")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling aid: allow warmup < 3, skip e2e and the CPU baseline")
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.op_only:
+        run_op_only(args)
+        return
+    if args.warmup < 3 and not args.profile:
         args.warmup = 3
+    if args.profile:
+        args.no_cpu = True
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank, pg)

@@ -165,7 +165,9 @@ struct FilterState {
 
 // ------------------------------------------------------------ OC update
 struct OcState {
-  DBuf<double> dcf, dvf, xp;
+  DBuf<double> dcf, dvf, xp, sq, lo, hi, vpart, vsum;
+  int fast_evals = 0, exact_evals = 0;
+  double radius = 1.5;
   DBuf<uint64_t> part, total;
   DBuf<int> inexact;
   uint64_t* h_total = nullptr;  // pinned: 3 limbs + flag
@@ -173,9 +175,9 @@ struct OcState {
   int64_t n_solid = 0;
   int fallbacks = 0, evals = 0;
   void init(const Grid& g, cudaStream_t) {
-    dcf.alloc(size_t(g.nv));
-    dvf.alloc(size_t(g.nv));
-    xp.alloc(size_t(g.nv));
+    for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi}) d->alloc(size_t(g.nv));
+    vpart.alloc(size_t(kRedBlocks));
+    vsum.alloc(1);
     part.alloc(size_t(3 * exact_sum_blocks()));
     total.alloc(3);
     inexact.alloc(1);
@@ -185,7 +187,8 @@ struct OcState {
     if (h_total) cudaFreeHost(h_total);
   }
   size_t bytes() const {
-    return dcf.bytes() + dvf.bytes() + xp.bytes() + part.bytes() + total.bytes() + inexact.bytes();
+    return dcf.bytes() + dvf.bytes() + xp.bytes() + sq.bytes() + lo.bytes() + hi.bytes() +
+           vpart.bytes() + vsum.bytes() + part.bytes() + total.bytes() + inexact.bytes();
   }
 };
 
@@ -207,7 +210,6 @@ double exact_volume(OcState& oc, const Grid& g, const uint8_t* act, const double
 // sum would decide it (see the file comment).
 bool volume_exceeds(OcState& oc, const Grid& g, const uint8_t* act,
                     const std::vector<uint8_t>& act_h, double target, cudaStream_t s) {
-  ++oc.evals;
   bool exact = false;
   const double S = exact_volume(oc, g, act, oc.xp.p, &exact, s);
   if (exact && std::isfinite(S)) {
@@ -230,13 +232,48 @@ bool volume_exceeds(OcState& oc, const Grid& g, const uint8_t* act,
 }
 
 // oc_update (simp.cpp:948-1025) on device-resident fields; dvf must hold the
-// filtered unit volume sensitivity.
+// filtered unit volume sensitivity.  Each bisection branch is first decided from
+// the fast linear volume sum_n dv_n x~_n(lambda) (k_oc_volume), whose distance to
+// the reference's sequential sum of filtered candidates is bounded by
+//   (n - 1) u V            (the sequential sum)
+// + (m + 1) u V            (the filter's m products and the division, per voxel)
+// + (m + 1) u V            (the rounding of dv itself)
+// + 12 u V                 (candidate: reference div/mul/sqrt vs sqrt(B)/sqrt(lambda))
+// + (n/(608*256) + 64) u V (this FP64 sum: a per-thread run, then trees),
+// m the stencil size, u = 2^-53.  Only inside that band is the exact path run:
+// the reference's candidate, the filter and the exact sum, then -- if still
+// within the sequential-sum bound -- the host's sequential sum.
 void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t* act,
                       const std::vector<uint8_t>& act_h, const double* x, const double* dc,
                       double volfrac, double move, double rho_min, double* xnew, cudaStream_t s) {
   fs.adj(g, act, dc, oc.dcf.p, s);
   const double target = volfrac * double(oc.n_solid);
+  launch_oc_prepare(x, oc.dcf.p, oc.dvf.p, act, g.nv, move, rho_min, oc.sq.p, oc.lo.p, oc.hi.p, s);
+  const double u = std::ldexp(1.0, -53);
+  const double n = double(std::max<int64_t>(oc.n_solid, 1));
+  const double m = double(fs.st.n);
+  const double eps =
+      (n + 2.0 * (m + 1.0) + 12.0 + n / (double(kRedBlocks) * 256.0) + 64.0) * u * 1.01;
   auto eval = [&](double lam) {
+    ++oc.evals;
+    launch_oc_volume(oc.sq.p, oc.lo.p, oc.hi.p, oc.dvf.p, g.nv, 1.0 / std::sqrt(lam), oc.vpart.p,
+                     oc.vsum.p, s);
+    double V = 0.0;
+    TG_CUDA(cudaMemcpyAsync(oc.h_total, oc.vsum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    std::memcpy(&V, oc.h_total, sizeof(double));
+    const double bound = eps * V / (1.0 - eps) + 1e-300;
+    if (std::isfinite(V)) {
+      if (V - target > bound) {
+        ++oc.fast_evals;
+        return true;
+      }
+      if (target - V > bound) {
+        ++oc.fast_evals;
+        return false;
+      }
+    }
+    ++oc.exact_evals;
     launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, lam, move, rho_min, xnew, s);
     fs.fwd(g, act, xnew, oc.xp.p, s);
     return volume_exceeds(oc, g, act, act_h, target, s);

@@ -36,180 +36,152 @@ int nblk(int64_t n, int t = kThreads) {
   return int(b < 152 * 64 ? (b > 0 ? b : 1) : 152 * 64);
 }
 
-// 1-D trilinear weight of coarse corner t (0 or 1) at fine offset pos (0,1,2)
-// inside the parent element.
-__device__ __forceinline__ double w1d(int pos, int t) {
-  return pos == 1 ? 0.5 : ((pos == 0) == (t == 0) ? 1.0 : 0.0);
-}
-
 // Local corner index -> offsets; corners in Walsh bit order (x | y<<1 | z<<2).
 __device__ __forceinline__ int cx(int c) { return c & 1; }
 __device__ __forceinline__ int cy(int c) { return (c >> 1) & 1; }
 __device__ __forceinline__ int cz(int c) { return c >> 2; }
 
-// Element matrices are stored in corner-bit order: row = 3*corner + comp.
-// One warp per coarse element; lane l accumulates entries l, l+32, ... (18 each).
-// Children at level 0 carry f*Ke (Ke given in corner-bit order); a child with
-// every DOF active uses the precomputed G_c = W_c^T Ke W_c (8 of them).
-__global__ void k_galerkin_level1(MgDims fd, MgDims cd, const double* __restrict__ ef,
-                                  const uint8_t* __restrict__ fact,
-                                  const uint8_t* __restrict__ cact,
-                                  const double* __restrict__ Ke,  // 576, corner-bit order
-                                  const double* __restrict__ G,   // 8 x 576
-                                  double* __restrict__ Kc) {
-  __shared__ double sKe[576];
-  __shared__ double sX[8][576];  // per-warp scratch for the masked path
-  for (int i = threadIdx.x; i < 576; i += blockDim.x) sKe[i] = Ke[i];
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
-  for (int64_t ce = blockIdx.x * 8 + warp; ce < nce; ce += int64_t(gridDim.x) * 8) {
-    const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
-              K = int(ce / (int64_t(cd.ex) * cd.ey));
-    double acc[18];
+// Trilinear weight of coarse corner t for child-corner sc of child ch: the
+// product over axes of 1 (pos 0 with t 0, or pos 2 with t 1), 1/2 (pos 1) or 0,
+// with pos = ch_axis + sc_axis.  Integer logic only: the FP pipes see just the
+// multiply-adds by the nonzero weights.
+__device__ __forceinline__ int wexp(int ch, int sc, int t) {
+  int e = 0;
 #pragma unroll
-    for (int q = 0; q < 18; ++q) acc[q] = 0.0;
-    for (int ch = 0; ch < 8; ++ch) {
-      const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
-      if (fi >= fd.ex || fj >= fd.ey || fk >= fd.ez) continue;
-      const double f = ef[(int64_t(fk) * fd.ey + fj) * fd.ex + fi];
-      if (f == 0.0) continue;
-      // Masks of the child's 24 DOFs (bit r set when DOF r is active).
-      unsigned int m = 0;
-      for (int r = lane; r < 24; r += 32) {
-        const int c = r / 3, comp = r % 3;
-        const int64_t node =
-            (int64_t(fk + cz(c)) * fd.nny + (fj + cy(c))) * fd.nnx + (fi + cx(c));
-        if (fact[3 * node + comp]) m |= 1u << r;
-      }
-      m = __reduce_or_sync(0xffffffffu, m);
-      if (m == 0xffffffu) {
-#pragma unroll
-        for (int q = 0; q < 18; ++q) acc[q] += f * G[ch * 576 + lane + 32 * q];
-      } else {
-        // X = (M Ke M) W (24 x 24), then acc += f * W^T X.
-        double* X = sX[warp];
-        for (int e = lane; e < 576; e += 32) {
-          const int r = e / 24, col = e % 24;  // col = 3*t + c2
-          const int t = col / 3, c2 = col % 3;
-          double s = 0.0;
-          if (m & (1u << r))
-            for (int sc = 0; sc < 8; ++sc) {
-              const int rr = 3 * sc + c2;
-              if (!(m & (1u << rr))) continue;
-              const double w = w1d(cx(ch) + cx(sc), cx(t)) * w1d(cy(ch) + cy(sc), cy(t)) *
-                               w1d(cz(ch) + cz(sc), cz(t));
-              s += sKe[r * 24 + rr] * w;
-            }
-          X[e] = s;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < 18; ++q) {
-          const int e = lane + 32 * q;
-          const int row = e / 24, col = e % 24;
-          const int t1 = row / 3, c1 = row % 3;
-          double s = 0.0;
-          for (int sc = 0; sc < 8; ++sc) {
-            const double w = w1d(cx(ch) + cx(sc), cx(t1)) * w1d(cy(ch) + cy(sc), cy(t1)) *
-                             w1d(cz(ch) + cz(sc), cz(t1));
-            if (w != 0.0) s += w * X[(3 * sc + c1) * 24 + col];
-          }
-          acc[q] += f * s;
-        }
-        __syncwarp();
-      }
-    }
-    // Zero rows/cols of inactive coarse DOFs.
-    unsigned int cm = 0;
-    for (int r = lane; r < 24; r += 32) {
-      const int c = r / 3, comp = r % 3;
-      const int64_t node = (int64_t(K + cz(c)) * cd.nny + (J + cy(c))) * cd.nnx + (I + cx(c));
-      if (cact[3 * node + comp]) cm |= 1u << r;
-    }
-    cm = __reduce_or_sync(0xffffffffu, cm);
-#pragma unroll
-    for (int q = 0; q < 18; ++q) {
-      const int e = lane + 32 * q;
-      const int row = e / 24, col = e % 24;
-      const bool keep = (cm >> row & 1u) && (cm >> col & 1u);
-      Kc[ce * 576 + e] = keep ? acc[q] : 0.0;
+  for (int a = 0; a < 3; ++a) {
+    const int pos = ((ch >> a) & 1) + ((sc >> a) & 1), ta = (t >> a) & 1;
+    if (pos == 1) {
+      ++e;
+    } else if ((pos == 0) != (ta == 0)) {
+      return -1;
     }
   }
+  return e;  // weight = 2^-e, or -1 for zero
+}
+template <class T>
+__device__ __forceinline__ T wval(int e) {
+  return e == 0 ? T(1) : (e == 1 ? T(0.5) : (e == 2 ? T(0.25) : T(0.125)));
 }
 
-// Level l -> l+1 from stored (already masked) child element matrices.
-constexpr int kCoarseWarps = 4;  // 2 x 4 x 576 doubles of shared memory per CTA
-__global__ void k_galerkin_coarse(MgDims fd, MgDims cd, const double* __restrict__ Kf,
-                                  const uint8_t* __restrict__ cact, double* __restrict__ Kc) {
-  __shared__ double sK[kCoarseWarps][576];
-  __shared__ double sX[kCoarseWarps][576];
+// One warp per coarse element; lane c < 24 owns column c of the coarse element
+// matrix (rows in corner-bit order, row = 3*corner + comp).  For every child,
+// X = S W (lane r = row r of S) then Y += W^T X (lane c = column c), with the
+// sparsity pattern of W uniform across the warp.  S is the child's matrix:
+// level 1 -- f * Ke with inactive fine DOFs zeroed (or the precomputed
+// G_c = W_c^T Ke W_c times f when all 24 are active); deeper levels -- the stored,
+// already masked, child element matrix.  Rows/cols of inactive coarse DOFs are
+// zeroed at the end.
+template <class T, bool LEVEL1>
+__global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T* __restrict__ ef,
+                                                  const uint8_t* __restrict__ fact,
+                                                  const uint8_t* __restrict__ cact,
+                                                  const T* __restrict__ Ke,
+                                                  const T* __restrict__ G,
+                                                  const T* __restrict__ Kf,
+                                                  T* __restrict__ Kc) {
+  constexpr int NW = 4;
+  __shared__ T sS[NW][576];
+  __shared__ T sX[NW][576];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* S = sS[warp];
+  T* X = sX[warp];
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
-  for (int64_t ce = blockIdx.x * int64_t(kCoarseWarps) + warp; ce < nce;
-       ce += int64_t(gridDim.x) * kCoarseWarps) {
+  for (int64_t ce = blockIdx.x * int64_t(NW) + warp; ce < nce; ce += int64_t(gridDim.x) * NW) {
     const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
               K = int(ce / (int64_t(cd.ex) * cd.ey));
-    double acc[18];
+    T acc[24];
 #pragma unroll
-    for (int q = 0; q < 18; ++q) acc[q] = 0.0;
+    for (int r = 0; r < 24; ++r) acc[r] = T(0);
     for (int ch = 0; ch < 8; ++ch) {
       const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
       if (fi >= fd.ex || fj >= fd.ey || fk >= fd.ez) continue;
       const int64_t fe = (int64_t(fk) * fd.ey + fj) * fd.ex + fi;
-      double* S = sK[warp];
-      double* X = sX[warp];
-      for (int e = lane; e < 576; e += 32) S[e] = Kf[fe * 576 + e];
-      __syncwarp();
-      for (int e = lane; e < 576; e += 32) {
-        const int r = e / 24, col = e % 24;
-        const int t = col / 3, c2 = col % 3;
-        double s = 0.0;
-        for (int sc = 0; sc < 8; ++sc) {
-          const double w = w1d(cx(ch) + cx(sc), cx(t)) * w1d(cy(ch) + cy(sc), cy(t)) *
-                           w1d(cz(ch) + cz(sc), cz(t));
-          if (w != 0.0) s += S[r * 24 + 3 * sc + c2] * w;
+      T f = T(1);
+      unsigned int m = 0xffffffu;
+      if (LEVEL1) {
+        f = ef[fe];
+        if (f == T(0)) continue;
+        unsigned int mm = 0;
+        if (lane < 24) {
+          const int c = lane / 3, comp = lane % 3;
+          const int64_t node =
+              (int64_t(fk + cz(c)) * fd.nny + (fj + cy(c))) * fd.nnx + (fi + cx(c));
+          if (fact[3 * node + comp]) mm = 1u << lane;
         }
-        X[e] = s;
+        m = __reduce_or_sync(0xffffffffu, mm);
+        if (m == 0xffffffu) {
+          if (lane < 24)
+#pragma unroll
+            for (int r = 0; r < 24; ++r) acc[r] += f * G[ch * 576 + r * 24 + lane];
+          continue;
+        }
+        for (int e = lane; e < 576; e += 32) {
+          const int r = e / 24, c2 = e % 24;
+          S[e] = ((m >> r) & 1u) && ((m >> c2) & 1u) ? f * Ke[e] : T(0);
+        }
+      } else {
+        for (int e = lane; e < 576; e += 32) S[e] = Kf[fe * 576 + e];
       }
       __syncwarp();
+      if (lane < 24) {  // X = S W: lane = row
+        for (int t = 0; t < 8; ++t) {
+          T xa = 0, xb = 0, xc = 0;
 #pragma unroll
-      for (int q = 0; q < 18; ++q) {
-        const int e = lane + 32 * q;
-        const int row = e / 24, col = e % 24;
-        const int t1 = row / 3, c1 = row % 3;
-        double s = 0.0;
-        for (int sc = 0; sc < 8; ++sc) {
-          const double w = w1d(cx(ch) + cx(sc), cx(t1)) * w1d(cy(ch) + cy(sc), cy(t1)) *
-                           w1d(cz(ch) + cz(sc), cz(t1));
-          if (w != 0.0) s += w * X[(3 * sc + c1) * 24 + col];
+          for (int sc = 0; sc < 8; ++sc) {
+            const int e = wexp(ch, sc, t);
+            if (e < 0) continue;
+            const T w = wval<T>(e);
+            xa += S[lane * 24 + 3 * sc] * w;
+            xb += S[lane * 24 + 3 * sc + 1] * w;
+            xc += S[lane * 24 + 3 * sc + 2] * w;
+          }
+          X[lane * 24 + 3 * t] = xa;
+          X[lane * 24 + 3 * t + 1] = xb;
+          X[lane * 24 + 3 * t + 2] = xc;
         }
-        acc[q] += s;
+      }
+      __syncwarp();
+      if (lane < 24) {  // Y += W^T X: lane = column
+#pragma unroll
+        for (int t1 = 0; t1 < 8; ++t1) {
+          T ya = 0, yb = 0, yc = 0;
+#pragma unroll
+          for (int sc = 0; sc < 8; ++sc) {
+            const int e = wexp(ch, sc, t1);
+            if (e < 0) continue;
+            const T w = wval<T>(e);
+            ya += w * X[(3 * sc) * 24 + lane];
+            yb += w * X[(3 * sc + 1) * 24 + lane];
+            yc += w * X[(3 * sc + 2) * 24 + lane];
+          }
+          acc[3 * t1] += ya;
+          acc[3 * t1 + 1] += yb;
+          acc[3 * t1 + 2] += yc;
+        }
       }
       __syncwarp();
     }
     unsigned int cm = 0;
-    for (int r = lane; r < 24; r += 32) {
-      const int c = r / 3, comp = r % 3;
+    if (lane < 24) {
+      const int c = lane / 3, comp = lane % 3;
       const int64_t node = (int64_t(K + cz(c)) * cd.nny + (J + cy(c))) * cd.nnx + (I + cx(c));
-      if (cact[3 * node + comp]) cm |= 1u << r;
+      if (cact[3 * node + comp]) cm = 1u << lane;
     }
     cm = __reduce_or_sync(0xffffffffu, cm);
+    if (lane < 24) {
+      const bool colk = (cm >> lane) & 1u;
 #pragma unroll
-    for (int q = 0; q < 18; ++q) {
-      const int e = lane + 32 * q;
-      const int row = e / 24, col = e % 24;
-      const bool keep = (cm >> row & 1u) && (cm >> col & 1u);
-      Kc[ce * 576 + e] = keep ? acc[q] : 0.0;
+      for (int r = 0; r < 24; ++r) Kc[ce * 576 + r * 24 + lane] = (colk && ((cm >> r) & 1u)) ? acc[r] : T(0);
     }
   }
 }
 
 // Node stencil from the element matrices around each node.  Entry index
 // q = (d*3 + c1)*3 + c2, d = (dz+1)*9 + (dy+1)*3 + (dx+1).
-__global__ void k_assemble_stencil(MgDims d, const double* __restrict__ Kel,
-                                   const uint8_t* __restrict__ act, double* __restrict__ A,
-                                   double* __restrict__ invdiag) {
+template <class T>
+__global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
+                                   const uint8_t* __restrict__ act, T* __restrict__ A,
+                                   T* __restrict__ invdiag) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
        n += int64_t(gridDim.x) * kThreads) {
@@ -220,9 +192,9 @@ __global__ void k_assemble_stencil(MgDims d, const double* __restrict__ Kel,
       for (int dy = -1; dy <= 1; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {
           const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
-          double blk[9];
+          T blk[9];
 #pragma unroll
-          for (int k = 0; k < 9; ++k) blk[k] = 0.0;
+          for (int k = 0; k < 9; ++k) blk[k] = T(0);
           // Elements containing both n and n+d: offsets ox in {-1,0} with the
           // node at corner (-ox) and the neighbour at corner (-ox + dx) in [0,1].
           for (int oz = -1; oz <= 0; ++oz) {
@@ -238,7 +210,7 @@ __global__ void k_assemble_stencil(MgDims d, const double* __restrict__ Kel,
                 if (ei < 0 || ei >= d.ex || ej < 0 || ej >= d.ey || ek < 0 || ek >= d.ez) continue;
                 const int64_t e = (int64_t(ek) * d.ey + ej) * d.ex + ei;
                 const int ln = lx | (ly << 1) | (lz << 2), lm = mx | (my << 1) | (mz << 2);
-                const double* Ke = Kel + e * 576;
+                const T* Ke = Kel + e * 576;
 #pragma unroll
                 for (int c1 = 0; c1 < 3; ++c1)
 #pragma unroll
@@ -250,11 +222,11 @@ __global__ void k_assemble_stencil(MgDims d, const double* __restrict__ Kel,
           for (int c1 = 0; c1 < 3; ++c1)
 #pragma unroll
             for (int c2 = 0; c2 < 3; ++c2)
-              A[int64_t(di * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : 0.0;
+              A[int64_t(di * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : T(0);
           if (di == 13)
             for (int k = 0; k < 3; ++k) {
-              const double dg = blk[k * 3 + k];
-              invdiag[3 * n + k] = (ra[k] && dg > 0.0) ? 1.0 / dg : 0.0;
+              const T dg = blk[k * 3 + k];
+              invdiag[3 * n + k] = (ra[k] && dg > T(0)) ? T(1) / dg : T(0);
             }
         }
   }
@@ -401,7 +373,8 @@ __global__ void k_prolong_add(MgDims fd, MgDims cd, const T* __restrict__ ec,
 // ---------------------------------------------------------- coarsest solve
 // Dense lower-triangular A (row-major, nc x nc) from the coarsest stencil over
 // the compact numbering cidx (-1 = inactive).
-__global__ void k_dense_from_stencil(MgDims d, const double* __restrict__ A,
+template <class T>
+__global__ void k_dense_from_stencil(MgDims d, const T* __restrict__ A,
                                      const int* __restrict__ cidx, int nc,
                                      double* __restrict__ D) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
@@ -421,7 +394,7 @@ __global__ void k_dense_from_stencil(MgDims d, const double* __restrict__ A,
             for (int c2 = 0; c2 < 3; ++c2) {
               const int col = cidx[3 * m + c2];
               if (col < 0) continue;
-              D[int64_t(row) * nc + col] = A[int64_t(di * 9 + c1 * 3 + c2) * nn + n];
+              D[int64_t(row) * nc + col] = double(A[int64_t(di * 9 + c1 * 3 + c2) * nn + n]);
             }
           }
     }
@@ -531,25 +504,28 @@ __global__ void k_chol_solve(const double* __restrict__ L, int nc, const int* __
 }
 }  // namespace
 
-void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const double* ef,
-                        const uint8_t* fact, const uint8_t* cact, const double* Ke,
-                        const double* G, double* Kc, cudaStream_t s) {
+template <class T>
+void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const T* ef, const uint8_t* fact,
+                        const uint8_t* cact, const T* Ke, const T* G, T* Kc, cudaStream_t s) {
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
-  k_galerkin_level1<<<nblk(nce, 8), 256, 0, s>>>(fd, cd, ef, fact, cact, Ke, G, Kc);
+  k_galerkin<T, true><<<nblk(nce, 4), 128, 0, s>>>(fd, cd, ef, fact, cact, Ke, G, nullptr, Kc);
   TG_LAUNCH_CHECK();
 }
 
-void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const double* Kf, const uint8_t* cact,
-                        double* Kc, cudaStream_t s) {
+template <class T>
+void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const T* Kf, const uint8_t* cact,
+                        T* Kc, cudaStream_t s) {
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
-  k_galerkin_coarse<<<nblk(nce, kCoarseWarps), 32 * kCoarseWarps, 0, s>>>(fd, cd, Kf, cact, Kc);
+  k_galerkin<T, false><<<nblk(nce, 4), 128, 0, s>>>(fd, cd, nullptr, nullptr, cact, nullptr,
+                                                    nullptr, Kf, Kc);
   TG_LAUNCH_CHECK();
 }
 
-void mg_assemble_stencil(const MgDims& d, const double* Kel, const uint8_t* act, double* A,
-                         double* invdiag, cudaStream_t s) {
+template <class T>
+void mg_assemble_stencil(const MgDims& d, const T* Kel, const uint8_t* act, T* A, T* invdiag,
+                         cudaStream_t s) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  k_assemble_stencil<<<nblk(nn), kThreads, 0, s>>>(d, Kel, act, A, invdiag);
+  k_assemble_stencil<T><<<nblk(nn), kThreads, 0, s>>>(d, Kel, act, A, invdiag);
   TG_LAUNCH_CHECK();
 }
 
@@ -594,11 +570,12 @@ void mg_prolong_add(const MgDims& fd, const MgDims& cd, const T* ec, const uint8
   TG_LAUNCH_CHECK();
 }
 
-void mg_dense_from_stencil(const MgDims& d, const double* A, const int* cidx, int nc, double* D,
+template <class T>
+void mg_dense_from_stencil(const MgDims& d, const T* A, const int* cidx, int nc, double* D,
                            cudaStream_t s) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   TG_CUDA(cudaMemsetAsync(D, 0, sizeof(double) * size_t(nc) * nc, s));
-  k_dense_from_stencil<<<nblk(nn), kThreads, 0, s>>>(d, A, cidx, nc, D);
+  k_dense_from_stencil<T><<<nblk(nn), kThreads, 0, s>>>(d, A, cidx, nc, D);
   TG_LAUNCH_CHECK();
 }
 
@@ -632,7 +609,15 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
   template void mg_prolong_add<T>(const MgDims&, const MgDims&, const T*, const uint8_t*, T*, \
                                   cudaStream_t);                                              \
   template void mg_chol_solve<T>(const double*, int, const int*, int64_t, const T*, T*,       \
-                                 double*, cudaStream_t);
+                                 double*, cudaStream_t);                                      \
+  template void mg_galerkin_level1<T>(const MgDims&, const MgDims&, const T*, const uint8_t*,  \
+                                      const uint8_t*, const T*, const T*, T*, cudaStream_t);  \
+  template void mg_galerkin_coarse<T>(const MgDims&, const MgDims&, const T*, const uint8_t*,  \
+                                      T*, cudaStream_t);                                      \
+  template void mg_assemble_stencil<T>(const MgDims&, const T*, const uint8_t*, T*, T*,       \
+                                       cudaStream_t);                                         \
+  template void mg_dense_from_stencil<T>(const MgDims&, const T*, const int*, int, double*,   \
+                                         cudaStream_t);
 TG_INST(double)
 TG_INST(float)
 #undef TG_INST

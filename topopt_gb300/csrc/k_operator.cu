@@ -17,13 +17,10 @@
 // FP64 at roughly 1/64 of its FP32 rate.  The result equals Ke u to rounding
 // (checked against the oracle's dense Ke in the tests).
 //
-// Scheduling: one CTA owns a brick of BX x BY x BZ nodes.  It stages the
-// (BX+2)(BY+2)(BZ+2) node values it needs in shared memory, evaluates every
-// element adjacent to an owned node (a one-element halo is recomputed by the
-// neighbouring brick), and accumulates element outputs into shared memory in
-// eight corner sub-steps: in sub-step k every element adds its corner-k output,
-// so no two writers meet and the per-node summation order is fixed -- the apply
-// is deterministic run to run without atomics.
+// Scheduling: x-pencils marching in z (see k_fine_op below): element outputs are
+// combined along x by warp shuffles, along y through shared memory and along z
+// in registers, so each node is finished exactly once without atomics and the
+// per-node summation order is fixed -- the apply is deterministic run to run.
 #include <cuda_runtime.h>
 
 #include "tg_internal.h"
@@ -186,133 +183,175 @@ __device__ __forceinline__ double block_sum(double v) {
   return s;  // valid in thread 0
 }
 
-template <class T, int BX, int BY, int BZ, int NT, int MODE>
-__global__ void __launch_bounds__(NT) k_fine_op(GridDev g, ModalT<T> mc,
-                                                const T* __restrict__ ef,
-                                                const uint8_t* __restrict__ kept,
-                                                const T* __restrict__ x, const T* __restrict__ b,
-                                                const T* __restrict__ invdiag, T omega,
-                                                T* __restrict__ y, double* __restrict__ dot_part) {
-  constexpr int TX = BX + 2, TY = BY + 2, TZ = BZ + 2, TN = TX * TY * TZ;
-  constexpr int EX = BX + 1, EY = BY + 1, EZ = BZ + 1, EN = EX * EY * EZ;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* xs = reinterpret_cast<T*>(smem_raw);
-  T* ys = xs + 3 * TN;
-  const int n0x = blockIdx.x * BX, n0y = blockIdx.y * BY, n0z = blockIdx.z * BZ;
+// Pencil geometry.  A CTA is PY warps.  Lane l of warp w evaluates the elements
+// (ex, ey, ez) with ex = 31*bx - 1 + l and ey = (PY-1)*by - 1 + w for KZ+1
+// consecutive element layers, marching upward in z.  Contributions are combined
+//   along x by a warp shuffle (an element's +x corners belong to the next lane),
+//   along y through shared memory (a warp's +y corners belong to the next warp),
+//   along z in registers (a layer's +z corners wait for the next step),
+// so lane l >= 1 of warp w >= 1 finishes node (ex, ey, ez) once element layers
+// ez-1 and ez are in.  Lane 0, warp 0 and the first element layer are the halo:
+// recomputed, never written.  One __syncthreads per element layer, no atomics,
+// and a fixed summation order per node (x, then y, then z), so the result is
+// deterministic run to run.
+template <class T>
+struct Pencil;
+template <>
+struct Pencil<double> {
+  static constexpr int PY = 8, KZ = 16;
+};
+template <>
+struct Pencil<float> {
+  static constexpr int PY = 16, KZ = 16;
+};
 
-  // Stage the node tile [n0-1, n0+B] (zeros outside the grid) and clear ys.
-  for (int t3 = threadIdx.x; t3 < 3 * TN; t3 += NT) {
-    const int t = t3 / 3, c = t3 - 3 * t;
-    const int lx = t % TX, ly = (t / TX) % TY, lz = t / (TX * TY);
-    const int gx = n0x - 1 + lx, gy = n0y - 1 + ly, gz = n0z - 1 + lz;
-    T v = T(0);
-    if (gx >= 0 && gx < g.nnx && gy >= 0 && gy < g.nny && gz >= 0 && gz < g.nnz)
-      v = x[3 * ((int64_t(gz) * g.nny + gy) * g.nnx + gx) + c];
-    xs[t3] = v;
-    ys[t3] = T(0);
+template <class T>
+__device__ __forceinline__ void load_node(const GridDev& g, const T* __restrict__ x, int a, int b,
+                                          int c, T (&v)[3]) {
+  if (a >= 0 && a < g.nnx && b >= 0 && b < g.nny && c >= 0 && c < g.nnz) {
+    const T* p = x + 3 * ((int64_t(c) * g.nny + b) * g.nnx + a);
+    v[0] = p[0];
+    v[1] = p[1];
+    v[2] = p[2];
+  } else {
+    v[0] = v[1] = v[2] = T(0);
   }
-  __syncthreads();
+}
 
-  for (int base = 0; base < EN; base += NT) {
-    const int le = base + threadIdx.x;
-    bool active = false;
-    int ex = 0, ey = 0, ez = 0;
-    T ux[8], uy[8], uz[8];
-    if (le < EN) {
-      ex = le % EX;
-      ey = (le / EX) % EY;
-      ez = le / (EX * EY);
-      const int gex = n0x - 1 + ex, gey = n0y - 1 + ey, gez = n0z - 1 + ez;
-      if (gex >= 0 && gex < g.nx && gey >= 0 && gey < g.ny && gez >= 0 && gez < g.nz) {
-        const T f = ef[(int64_t(gez) * g.ny + gey) * g.nx + gex];
-        if (f != T(0)) {
-          active = true;
+// Loads layer c of the lane's element corners: v[yb][xb][comp] for nodes
+// (ex + xb, ey + yb, c).  The +x nodes come from the next lane; lane 31 loads its own.
+template <class T>
+__device__ __forceinline__ void load_layer(const GridDev& g, const T* __restrict__ x, int ex,
+                                           int ey, int c, int lane, T (&v)[2][2][3]) {
+  load_node(g, x, ex, ey, c, v[0][0]);
+  load_node(g, x, ex, ey + 1, c, v[1][0]);
 #pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const int tl = ((ez + (k >> 2)) * TY + (ey + ((k >> 1) & 1))) * TX + ex + (k & 1);
-            ux[k] = xs[3 * tl];
-            uy[k] = xs[3 * tl + 1];
-            uz[k] = xs[3 * tl + 2];
-          }
-          modal_apply(mc, f, ux, uy, uz);
-        }
-      }
-    }
+  for (int yb = 0; yb < 2; ++yb)
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (active) {
-        const int tl = ((ez + (k >> 2)) * TY + (ey + ((k >> 1) & 1))) * TX + ex + (k & 1);
-        ys[3 * tl] += ux[k];
-        ys[3 * tl + 1] += uy[k];
-        ys[3 * tl + 2] += uz[k];
-      }
-      __syncthreads();
-    }
+    for (int k = 0; k < 3; ++k) v[yb][1][k] = __shfl_down_sync(0xffffffffu, v[yb][0][k], 1);
+  if (lane == 31) {
+    load_node(g, x, ex + 1, ey, c, v[0][1]);
+    load_node(g, x, ex + 1, ey + 1, c, v[1][1]);
   }
+}
 
+template <class T, int PY, int KZ, int MODE>
+__global__ void __launch_bounds__(32 * PY) k_fine_op(GridDev g, ModalT<T> mc,
+                                                     const T* __restrict__ ef,
+                                                     const uint8_t* __restrict__ kept,
+                                                     const T* __restrict__ x, const T* __restrict__ b,
+                                                     const T* __restrict__ invdiag, T omega,
+                                                     T* __restrict__ y, double* __restrict__ dot_part) {
+  __shared__ T sy[2][PY][6][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ex = blockIdx.x * 31 - 1 + lane;
+  const int ey = blockIdx.y * (PY - 1) - 1 + w;
+  const int k0 = blockIdx.z * KZ;
+  const bool own_xy = lane >= 1 && w >= 1 && ex < g.nnx && ey < g.nny;
+  const bool exy_ok = ex >= 0 && ex < g.nx && ey >= 0 && ey < g.ny;
+  T cur[2][2][3], nxt[2][2][3];
+  load_layer(g, x, ex, ey, k0 - 1, lane, cur);
+  T pend[3] = {T(0), T(0), T(0)};
   double dsum = 0.0;
-  for (int t3 = threadIdx.x; t3 < 3 * BX * BY * BZ; t3 += NT) {
-    const int t = t3 / 3, c = t3 - 3 * t;
-    const int ox = t % BX, oy = (t / BX) % BY, oz = t / (BX * BY);
-    const int gx = n0x + ox, gy = n0y + oy, gz = n0z + oz;
-    if (gx >= g.nnx || gy >= g.nny || gz >= g.nnz) continue;
-    const int tl = ((oz + 1) * TY + (oy + 1)) * TX + ox + 1;
-    const int64_t d = 3 * ((int64_t(gz) * g.nny + gy) * g.nnx + gx) + c;
-    const bool k = kept == nullptr || kept[d] != 0;
-    const T ax = ys[3 * tl + c];
-    T out;
-    if (MODE == kApply) {
-      out = k ? ax : T(0);
-      dsum += double(xs[3 * tl + c]) * double(out);
-    } else if (MODE == kResidual) {
-      out = k ? T(b[d] - ax) : T(0);
-    } else {
-      out = k ? T(xs[3 * tl + c] + omega * invdiag[d] * (b[d] - ax)) : T(0);
+#pragma unroll 1
+  for (int s = 0; s <= KZ; ++s) {
+    const int ez = k0 - 1 + s;
+    load_layer(g, x, ex, ey, ez + 1, lane, nxt);
+    T ux[8], uy[8], uz[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int xb = c & 1, yb = (c >> 1) & 1, zb = c >> 2;
+      ux[c] = zb ? nxt[yb][xb][0] : cur[yb][xb][0];
+      uy[c] = zb ? nxt[yb][xb][1] : cur[yb][xb][1];
+      uz[c] = zb ? nxt[yb][xb][2] : cur[yb][xb][2];
     }
-    y[d] = out;
+    const T f = (exy_ok && ez >= 0 && ez < g.nz) ? ef[(int64_t(ez) * g.ny + ey) * g.nx + ex] : T(0);
+    if (f != T(0)) {
+      modal_apply(mc, f, ux, uy, uz);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) ux[c] = uy[c] = uz[c] = T(0);
+    }
+    // x: add the previous lane's +x corners to this lane's -x corners.
+    T L[2][2][3];  // [yb][zb][comp] at node x = ex
+#pragma unroll
+    for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+      for (int zb = 0; zb < 2; ++zb) {
+        const int c0 = (yb << 1) | (zb << 2);
+        L[yb][zb][0] = ux[c0] + __shfl_up_sync(0xffffffffu, ux[c0 | 1], 1);
+        L[yb][zb][1] = uy[c0] + __shfl_up_sync(0xffffffffu, uy[c0 | 1], 1);
+        L[yb][zb][2] = uz[c0] + __shfl_up_sync(0xffffffffu, uz[c0 | 1], 1);
+      }
+    // y: hand the +y corners to the next warp through shared memory.
+    const int buf = s & 1;
+#pragma unroll
+    for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) sy[buf][w][zb * 3 + k][lane] = L[1][zb][k];
+    __syncthreads();
+    T N[2][3];
+#pragma unroll
+    for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        N[zb][k] = L[0][zb][k] + (w >= 1 ? sy[buf][w - 1][zb * 3 + k][lane] : T(0));
+    // z: node layer ez is complete (element layers ez-1 and ez).
+    if (s >= 1 && own_xy && ez < g.nnz) {
+      const int64_t d0 = 3 * ((int64_t(ez) * g.nny + ey) * g.nnx + ex);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int64_t d = d0 + k;
+        const bool kk = kept == nullptr || kept[d] != 0;
+        const T ax = pend[k] + N[0][k];
+        const T xv = cur[0][0][k];
+        T out;
+        if (MODE == kApply) {
+          out = kk ? ax : T(0);
+          dsum += double(xv) * double(out);
+        } else if (MODE == kResidual) {
+          out = kk ? T(b[d] - ax) : T(0);
+        } else {
+          out = kk ? T(xv + omega * invdiag[d] * (b[d] - ax)) : T(0);
+        }
+        y[d] = out;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pend[k] = N[1][k];
+#pragma unroll
+    for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+      for (int xb = 0; xb < 2; ++xb)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) cur[yb][xb][k] = nxt[yb][xb][k];
   }
   if (MODE == kApply && dot_part != nullptr) {
-    const double s = block_sum(dsum);
+    const double sum = block_sum(dsum);
     if (threadIdx.x == 0)
-      dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
+      dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sum;
   }
 }
 
 template <class T>
-struct Brick;
-template <>
-struct Brick<double> {
-  static constexpr int BX = 8, BY = 8, BZ = 8, NT = 256;
-};
-template <>
-struct Brick<float> {
-  static constexpr int BX = 16, BY = 8, BZ = 8, NT = 512;
-};
+static dim3 pencil_grid(const Grid& g) {
+  using P = Pencil<T>;
+  return dim3((g.nnx + 30) / 31, (g.nny + P::PY - 2) / (P::PY - 1), (g.nnz + P::KZ - 1) / P::KZ);
+}
 
 int fine_op_blocks(const Grid& g, bool fp64) {
-  const int bx = fp64 ? Brick<double>::BX : Brick<float>::BX;
-  const int by = fp64 ? Brick<double>::BY : Brick<float>::BY;
-  const int bz = fp64 ? Brick<double>::BZ : Brick<float>::BZ;
-  return ((g.nnx + bx - 1) / bx) * ((g.nny + by - 1) / by) * ((g.nnz + bz - 1) / bz);
+  const dim3 d = fp64 ? pencil_grid<double>(g) : pencil_grid<float>(g);
+  return int(d.x * d.y * d.z);
 }
 
 template <class T, int MODE>
 static void launch_mode(const Grid& g, const ModalConsts& c, const T* ef, const uint8_t* kept,
                         const T* x, const T* b, const T* invdiag, T omega, T* y,
                         double* dot_part, cudaStream_t s) {
-  using B = Brick<T>;
-  constexpr int TN = (B::BX + 2) * (B::BY + 2) * (B::BZ + 2);
-  constexpr size_t smem = 2 * 3 * TN * sizeof(T);
-  auto kern = k_fine_op<T, B::BX, B::BY, B::BZ, B::NT, MODE>;
-  static bool configured = false;
-  if (!configured) {
-    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    configured = true;
-  }
-  const dim3 grid((g.nnx + B::BX - 1) / B::BX, (g.nny + B::BY - 1) / B::BY,
-                  (g.nnz + B::BZ - 1) / B::BZ);
+  using P = Pencil<T>;
   const GridDev gd{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz};
-  kern<<<grid, B::NT, smem, s>>>(gd, to_modal<T>(c), ef, kept, x, b, invdiag, omega, y, dot_part);
+  k_fine_op<T, P::PY, P::KZ, MODE><<<pencil_grid<T>(g), 32 * P::PY, 0, s>>>(
+      gd, to_modal<T>(c), ef, kept, x, b, invdiag, omega, y, dot_part);
   TG_LAUNCH_CHECK();
 }
 

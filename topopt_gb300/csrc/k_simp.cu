@@ -303,6 +303,51 @@ __global__ void k_oc_candidate(const double* __restrict__ x, const double* __res
   }
 }
 
+// Fast bisection support.  The filtered volume of a candidate is linear in the
+// candidate: sum_e xp_e = sum_n dv_n x_n with dv = filter_sensitivity(1), so one
+// weighted sum replaces a filter pass per bisection step; and the candidate is
+// clamp(x_e sqrt(B_e) / sqrt(lambda)) with B_e = -dc_e / dv_e, so sqrt(B_e) is
+// taken once per OC update.  These only DECIDE bisection branches under a
+// certified error bound (api.cu); x_new itself always comes from k_oc_candidate.
+__global__ void k_oc_prepare(const double* __restrict__ x, const double* __restrict__ dcf,
+                             const double* __restrict__ dvf, const uint8_t* __restrict__ act,
+                             int64_t n, double move, double rho_min, double* __restrict__ sq,
+                             double* __restrict__ lo, double* __restrict__ hi) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double s = 0.0, l = 0.0, h = 0.0;
+    if (act[e]) {
+      const double xe = x[e];
+      double be = 0.0;
+      if (dvf[e] > 0.0) be = -dcf[e] / dvf[e];
+      if (be < 0.0) be = 0.0;
+      s = xe * sqrt(be);
+      const double xm = xe - move, xp = xe + move;
+      l = (rho_min < xm) ? xm : rho_min;
+      h = (xp < 1.0) ? xp : 1.0;
+    }
+    sq[e] = s;
+    lo[e] = l;
+    hi[e] = h;
+  }
+}
+
+__global__ void k_oc_volume(const double* __restrict__ sq, const double* __restrict__ lo,
+                            const double* __restrict__ hi, const double* __restrict__ dvf,
+                            int64_t n, double c, double* __restrict__ part) {
+  double acc = 0.0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double xt = sq[e] * c;
+    const double l = lo[e], h = hi[e];
+    xt = xt < l ? l : xt;
+    xt = xt > h ? h : xt;
+    acc += dvf[e] * xt;
+  }
+  acc = block_sum256(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
 // Exact fixed-point accumulation: value = A * 2^-128, A a 192-bit unsigned
 // integer in three 64-bit limbs.  Integer addition is associative, so the total
 // is the same whatever the summation order -- the exact sum, not an
@@ -475,6 +520,20 @@ void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
 }
 
 int exact_sum_blocks() { return kRedBlocks; }
+
+void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, const uint8_t* act,
+                       int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
+                       cudaStream_t s) {
+  k_oc_prepare<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, move, rho_min, sq, lo, hi);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_oc_volume(const double* sq, const double* lo, const double* hi, const double* dvf,
+                      int64_t n, double c, double* part, double* out, cudaStream_t s) {
+  k_oc_volume<<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, c, part);
+  TG_LAUNCH_CHECK();
+  launch_sum_partials(part, kRedBlocks, out, s);
+}
 
 void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,
                       uint64_t* total, int* inexact, cudaStream_t s) {

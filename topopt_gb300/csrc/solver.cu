@@ -182,10 +182,14 @@ struct Solver::Level {
   int64_t nn = 0, ndof = 0, nel = 0, nact = 0;
   std::vector<uint8_t> act_h;
   DBuf<uint8_t> act;
+  // FP64 operators and vectors (plain form, and the FP64 retry of the mixed form).
   DBuf<double> Kel, A, invd, xa, xb, b;
-  DBuf<float> Af, invdf, fxa, fxb, fb;
+  // FP32 operators and vectors (mixed form).
+  DBuf<float> Kelf, Af, invdf, fxa, fxb, fb;
   double *x = nullptr, *r = nullptr;
   float *xf = nullptr, *rf = nullptr;
+  template <class T>
+  void ensure();
   template <class T>
   T*& X();
   template <class T>
@@ -193,10 +197,35 @@ struct Solver::Level {
   template <class T>
   T* B();
   template <class T>
-  const T* Am();
+  T* Am();
   template <class T>
-  const T* Dinv();
+  T* Dinv();
+  template <class T>
+  T* Ke();
+  size_t bytes() const {
+    return act.bytes() + Kel.bytes() + A.bytes() + invd.bytes() + xa.bytes() + xb.bytes() +
+           b.bytes() + Kelf.bytes() + Af.bytes() + invdf.bytes() + fxa.bytes() + fxb.bytes() +
+           fb.bytes();
+  }
 };
+template <>
+void Solver::Level::ensure<double>() {
+  if (Kel.p) return;
+  Kel.alloc(size_t(nel) * 576);
+  A.alloc(size_t(nn) * 243);
+  for (DBuf<double>* v : {&invd, &xa, &xb, &b}) v->alloc(size_t(ndof));
+  x = xa.p;
+  r = xb.p;
+}
+template <>
+void Solver::Level::ensure<float>() {
+  if (Kelf.p) return;
+  Kelf.alloc(size_t(nel) * 576);
+  Af.alloc(size_t(nn) * 243);
+  for (DBuf<float>* v : {&invdf, &fxa, &fxb, &fb}) v->alloc(size_t(ndof));
+  xf = fxa.p;
+  rf = fxb.p;
+}
 template <>
 double*& Solver::Level::X<double>() { return x; }
 template <>
@@ -210,13 +239,17 @@ double* Solver::Level::B<double>() { return b.p; }
 template <>
 float* Solver::Level::B<float>() { return fb.p; }
 template <>
-const double* Solver::Level::Am<double>() { return A.p; }
+double* Solver::Level::Am<double>() { return A.p; }
 template <>
-const float* Solver::Level::Am<float>() { return Af.p; }
+float* Solver::Level::Am<float>() { return Af.p; }
 template <>
-const double* Solver::Level::Dinv<double>() { return invd.p; }
+double* Solver::Level::Dinv<double>() { return invd.p; }
 template <>
-const float* Solver::Level::Dinv<float>() { return invdf.p; }
+float* Solver::Level::Dinv<float>() { return invdf.p; }
+template <>
+double* Solver::Level::Ke<double>() { return Kel.p; }
+template <>
+float* Solver::Level::Ke<float>() { return Kelf.p; }
 
 // ------------------------------------------------------------------ Solver
 Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t s)
@@ -249,12 +282,8 @@ size_t Solver::device_bytes() const {
     b += d->bytes();
   for (const DBuf<float>* d : {&Ef_, &invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_})
     b += d->bytes();
-  for (const auto& L : levels_) {
-    b += L->act.bytes() + L->Kel.bytes() + L->A.bytes() + L->invd.bytes() + L->xa.bytes() +
-         L->xb.bytes() + L->b.bytes();
-    b += L->Af.bytes() + L->invdf.bytes() + L->fxa.bytes() + L->fxb.bytes() + L->fb.bytes();
-  }
-  return b + cidx_.bytes();
+  for (const auto& L : levels_) b += L->bytes();
+  return b + cidx_.bytes() + kebf_.bytes() + Gf_.bytes();
 }
 
 void Solver::build_structure() {
@@ -314,17 +343,10 @@ void Solver::build_structure() {
     Level& L = *Lp;
     L.act.alloc(size_t(L.ndof));
     TG_CUDA(cudaMemcpyAsync(L.act.p, L.act_h.data(), L.act.bytes(), cudaMemcpyHostToDevice, s_));
-    L.Kel.alloc(size_t(L.nel) * 576);
-    L.A.alloc(size_t(L.nn) * 243);
-    for (DBuf<double>* b : {&L.invd, &L.xa, &L.xb, &L.b}) b->alloc(size_t(L.ndof));
-    L.x = L.xa.p;
-    L.r = L.xb.p;
-    if (mixed_) {
-      L.Af.alloc(size_t(L.nn) * 243);
-      for (DBuf<float>* b : {&L.invdf, &L.fxa, &L.fxb, &L.fb}) b->alloc(size_t(L.ndof));
-      L.xf = L.fxa.p;
-      L.rf = L.fxb.p;
-    }
+    if (mixed_)
+      L.ensure<float>();
+    else
+      L.ensure<double>();
   }
   cidx_.alloc(size_t(C.ndof));
   TG_CUDA(cudaMemcpyAsync(cidx_.p, cidx.data(), cidx_.bytes(), cudaMemcpyHostToDevice, s_));
@@ -364,6 +386,11 @@ void Solver::build_structure() {
   G_.alloc(8 * 576);
   TG_CUDA(cudaMemcpyAsync(keb_.p, kb.data(), keb_.bytes(), cudaMemcpyHostToDevice, s_));
   TG_CUDA(cudaMemcpyAsync(G_.p, G.data(), G_.bytes(), cudaMemcpyHostToDevice, s_));
+  std::vector<float> kbf(kb.begin(), kb.end()), Gf(G.begin(), G.end());
+  kebf_.alloc(576);
+  Gf_.alloc(8 * 576);
+  TG_CUDA(cudaMemcpyAsync(kebf_.p, kbf.data(), kebf_.bytes(), cudaMemcpyHostToDevice, s_));
+  TG_CUDA(cudaMemcpyAsync(Gf_.p, Gf.data(), Gf_.bytes(), cudaMemcpyHostToDevice, s_));
   TG_CUDA(cudaStreamSynchronize(s_));
   have_mg_ = true;
 }
@@ -444,34 +471,55 @@ void Solver::set_modulus(const double* E) {
     launch_copy_d2f(Ef_.p, E, g.nv, s_);
     launch_copy_d2f(invdiagf_.p, invdiag_.p, g.ndof, s_);
   }
-  if (have_mg_) build_numeric();
+  numeric_[0] = numeric_[1] = false;
+  numeric_ok_ = false;
+  if (have_mg_) {
+    const double t0 = now_ms();
+    numeric_ok_ = mixed_ ? build_numeric<float>() : build_numeric<double>();
+    mg_build_ms_ = now_ms() - t0;
+  }
 }
 
-void Solver::build_numeric() {
+template <class T>
+static const T* pick(const DBuf<double>& d, const DBuf<float>& f);
+template <>
+const double* pick<double>(const DBuf<double>& d, const DBuf<float>&) {
+  return d.p;
+}
+template <>
+const float* pick<float>(const DBuf<double>&, const DBuf<float>& f) {
+  return f.p;
+}
+
+// Galerkin hierarchy in precision T from the current element factors, then the
+// FP64 dense Cholesky factor of the coarsest level.  Returns false when the
+// factorisation meets a non-positive pivot (the caller falls back).
+template <class T>
+bool Solver::build_numeric() {
   const Grid& g = fp_.g;
   const MgDims fd = dims_of(g.nx, g.ny, g.nz);
   MgDims pd = fd;
+  const T* ef = sizeof(T) == 8 ? reinterpret_cast<const T*>(E_) : reinterpret_cast<const T*>(Ef_.p);
   for (size_t l = 0; l < levels_.size(); ++l) {
     Level& L = *levels_[l];
+    L.ensure<T>();
     if (l == 0)
-      mg_galerkin_level1(fd, L.d, E_, fp_.kept.p, L.act.p, keb_.p, G_.p, L.Kel.p, s_);
+      mg_galerkin_level1<T>(fd, L.d, ef, fp_.kept.p, L.act.p, pick<T>(keb_, kebf_),
+                            pick<T>(G_, Gf_), L.Ke<T>(), s_);
     else
-      mg_galerkin_coarse(pd, L.d, levels_[l - 1]->Kel.p, L.act.p, L.Kel.p, s_);
-    mg_assemble_stencil(L.d, L.Kel.p, L.act.p, L.A.p, L.invd.p, s_);
-    if (mixed_) {
-      mg_to_float(L.A.p, L.Af.p, L.nn * 243, s_);
-      mg_to_float(L.invd.p, L.invdf.p, L.ndof, s_);
-    }
+      mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
+    mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, L.Am<T>(), L.Dinv<T>(), s_);
     pd = L.d;
   }
   Level& C = *levels_.back();
-  mg_dense_from_stencil(C.d, C.A.p, cidx_.p, nc_, chol_.p, s_);
+  mg_dense_from_stencil<T>(C.d, C.Am<T>(), cidx_.p, nc_, chol_.p, s_);
   TG_CUDA(cudaMemsetAsync(chol_fail_.p, 0, sizeof(int), s_));
   mg_cholesky(chol_.p, nc_, chol_fail_.p, s_);
   int fail = 0;
   TG_CUDA(cudaMemcpyAsync(&fail, chol_fail_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
   TG_CUDA(cudaStreamSynchronize(s_));
-  numeric_ok_ = (fail == 0);
+  numeric_[sizeof(T) == 8 ? 1 : 0] = (fail == 0);
+  return fail == 0;
 }
 
 // ------------------------------------------------------------------ V-cycle
@@ -734,6 +782,7 @@ SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u
   fine_matvecs_ = lowp_matvecs_ = 0;
   const Grid& g = fp_.g;
   st.hier_built = have_mg_ && numeric_ok_;
+  st.t_mg_build_ms = mg_build_ms_;
   if (fp_.ng == 0) {
     st.converged = true;
     launch_mask_select(u, nullptr, fp_.up.p, fp_.kept.p, g.ndof, s_);
@@ -749,7 +798,7 @@ SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u
       if (warm) seed();
       solved = mixed_refine(tol, std::min(cap, budget_), warm, st);
     }
-    if (!solved) {
+    if (!solved && (!mixed_ || build_numeric<double>())) {
       if (warm) seed();
       solved = mgpcg(tol, std::min(cap, budget_), warm, st);
     }

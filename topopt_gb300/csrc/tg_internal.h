@@ -181,6 +181,11 @@ void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
 // Exact (fixed-point, order independent) sum of a non-negative field over the
 // solid voxels; returns per-block 192-bit partials, then the final total.
 int exact_sum_blocks();
+void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, const uint8_t* act,
+                       int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
+                       cudaStream_t s);
+void launch_oc_volume(const double* sq, const double* lo, const double* hi, const double* dvf,
+                      int64_t n, double c, double* part, double* out, cudaStream_t s);
 void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,
                       uint64_t* total, int* inexact, cudaStream_t s);
 double fma_probe_tflops(bool fp64);

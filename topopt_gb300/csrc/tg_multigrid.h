@@ -11,13 +11,15 @@ struct MgDims {
   int ex, ey, ez, nnx, nny, nnz;
 };
 
-void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const double* ef,
-                        const uint8_t* fact, const uint8_t* cact, const double* Ke,
-                        const double* G, double* Kc, cudaStream_t s);
-void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const double* Kf, const uint8_t* cact,
-                        double* Kc, cudaStream_t s);
-void mg_assemble_stencil(const MgDims& d, const double* Kel, const uint8_t* act, double* A,
-                         double* invdiag, cudaStream_t s);
+template <class T>
+void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const T* ef, const uint8_t* fact,
+                        const uint8_t* cact, const T* Ke, const T* G, T* Kc, cudaStream_t s);
+template <class T>
+void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const T* Kf, const uint8_t* cact,
+                        T* Kc, cudaStream_t s);
+template <class T>
+void mg_assemble_stencil(const MgDims& d, const T* Kel, const uint8_t* act, T* A, T* invdiag,
+                         cudaStream_t s);
 void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s);
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
@@ -30,7 +32,8 @@ void mg_restrict(const MgDims& fd, const MgDims& cd, const T* rf, const uint8_t*
 template <class T>
 void mg_prolong_add(const MgDims& fd, const MgDims& cd, const T* ec, const uint8_t* fact, T* xf,
                     cudaStream_t s);
-void mg_dense_from_stencil(const MgDims& d, const double* A, const int* cidx, int nc, double* D,
+template <class T>
+void mg_dense_from_stencil(const MgDims& d, const T* A, const int* cidx, int nc, double* D,
                            cudaStream_t s);
 void mg_cholesky(double* D, int nc, int* fail, cudaStream_t s);
 template <class T>

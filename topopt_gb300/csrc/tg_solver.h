@@ -74,7 +74,9 @@ class Solver {
   struct Level;
   struct Impl;
   void build_structure();
-  void build_numeric();
+  template <class T>
+  bool build_numeric();
+
   bool mgpcg(double tol, int max_it, bool warm, SolverStats& st);
   bool jacobi_pcg(double tol, int max_it, bool warm, SolverStats& st);
   bool mixed_refine(double tol, int max_it, bool warm, SolverStats& st);
@@ -103,7 +105,9 @@ class Solver {
   // hierarchy
   std::vector<std::unique_ptr<Level>> levels_;  // levels 1..L-1
   DBuf<double> keb_, G_;                         // Ke in corner-bit order, 8 G_c
-  bool have_mg_ = false, numeric_ok_ = false;
+  DBuf<float> kebf_, Gf_;
+  bool have_mg_ = false, numeric_ok_ = false, numeric_[2] = {false, false};
+  double mg_build_ms_ = 0.0;
   int64_t fine_matvecs_ = 0, lowp_matvecs_ = 0;
   int nc_ = 0;
   DBuf<int> cidx_, chol_fail_;
