@@ -21,6 +21,7 @@
 // Coarse levels are applied as assembled 27-point node stencils stored as
 // structure of arrays A[243][nnodes] (block (d, c1, c2) for neighbour offset d),
 // so a thread per node reads coalesced rows.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "tg_internal.h"
@@ -292,6 +293,97 @@ __global__ void __launch_bounds__(kThreads) k_stencil_op(MgDims d, const T* __re
   }
 }
 
+// Diagonally scaled FP16 copy of an FP32 stencil: Ah = S A S with
+// S = diag(1/sqrt(diag A)), so every entry lies in [-1, 1] (A is SPD) and the
+// diagonal is 1 -- the range FP16 represents best.  sc receives S.
+__global__ void k_scale_vector(const float* __restrict__ invd, int64_t n, float* __restrict__ sc) {
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads)
+    sc[i] = sqrtf(invd[i]);
+}
+
+__global__ void k_normalize_stencil(MgDims d, const float* __restrict__ A,
+                                    const float* __restrict__ sc, __half* __restrict__ Ah) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
+    for (int di = 0; di < 27; ++di) {
+      const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
+      const int i = a + dx, j = bb + dy, k = c + dz;
+      const bool in = i >= 0 && i < d.nnx && j >= 0 && j < d.nny && k >= 0 && k < d.nnz;
+      const int64_t m = in ? (int64_t(k) * d.nny + j) * d.nnx + i : n;
+#pragma unroll
+      for (int c1 = 0; c1 < 3; ++c1)
+#pragma unroll
+        for (int c2 = 0; c2 < 3; ++c2) {
+          const int64_t q = int64_t(di * 9 + c1 * 3 + c2) * nn + n;
+          const float v = in ? sc[3 * n + c1] * A[q] * sc[3 * m + c2] : 0.0f;
+          Ah[q] = __float2half_rn(v);
+        }
+    }
+  }
+}
+
+// Stencil operator on the scaled FP16 copy: (A x)_n = s_n * sum_m Ah_nm (s_m x_m),
+// FP32 arithmetic; same modes and masking as k_stencil_op.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_stencil_op_h(MgDims d, const __half* __restrict__ A,
+                                                           const float* __restrict__ sc,
+                                                           const uint8_t* __restrict__ act,
+                                                           const float* __restrict__ x,
+                                                           const float* __restrict__ b,
+                                                           const float* __restrict__ invdiag,
+                                                           float omega, float* __restrict__ y) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
+       n += int64_t(gridDim.x) * kThreads) {
+    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny),
+              c = int(n / (int64_t(d.nnx) * d.nny));
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int k = c + dz;
+      if (k < 0 || k >= d.nnz) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int j = bb + dy;
+        if (j < 0 || j >= d.nny) continue;
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int i = a + dx;
+          if (i < 0 || i >= d.nnx) continue;
+          const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
+          const int64_t m = (int64_t(k) * d.nny + j) * d.nnx + i;
+          const float x0 = sc[3 * m] * x[3 * m], x1 = sc[3 * m + 1] * x[3 * m + 1],
+                      x2 = sc[3 * m + 2] * x[3 * m + 2];
+          const __half* Ab = A + int64_t(di * 9) * nn + n;
+          s0 += __half2float(Ab[0]) * x0 + __half2float(Ab[nn]) * x1 + __half2float(Ab[2 * nn]) * x2;
+          s1 += __half2float(Ab[3 * nn]) * x0 + __half2float(Ab[4 * nn]) * x1 +
+                __half2float(Ab[5 * nn]) * x2;
+          s2 += __half2float(Ab[6 * nn]) * x0 + __half2float(Ab[7 * nn]) * x1 +
+                __half2float(Ab[8 * nn]) * x2;
+        }
+      }
+    }
+    const float sv[3] = {s0, s1, s2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int64_t dof = 3 * n + k;
+      const float ax = sc[dof] * sv[k];
+      float out;
+      if (!act[dof]) {
+        out = 0.f;
+      } else if (MODE == kApply) {
+        out = ax;
+      } else if (MODE == kResidual) {
+        out = b[dof] - ax;
+      } else {
+        out = x[dof] + omega * invdiag[dof] * (b[dof] - ax);
+      }
+      y[dof] = out;
+    }
+  }
+}
+
 // x = omega * invdiag .* b (the first smoother sweep from a zero iterate).
 template <class T>
 __global__ void k_jacobi_first(const T* __restrict__ b, const T* __restrict__ invdiag, T omega,
@@ -545,6 +637,30 @@ void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, co
     k_stencil_op<T, kResidual><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else
     k_stencil_op<T, kSmooth><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_normalize_stencil(const MgDims& d, const float* A, const float* invd, float* sc,
+                          void* Ah, cudaStream_t s) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  k_scale_vector<<<nblk(3 * nn), kThreads, 0, s>>>(invd, 3 * nn, sc);
+  TG_LAUNCH_CHECK();
+  k_normalize_stencil<<<nblk(nn), kThreads, 0, s>>>(d, A, sc, static_cast<__half*>(Ah));
+  TG_LAUNCH_CHECK();
+}
+
+void mg_stencil_op_h(int mode, const MgDims& d, const void* Ah, const float* sc,
+                     const uint8_t* act, const float* x, const float* b, const float* invdiag,
+                     float omega, float* y, cudaStream_t s) {
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  const int nb = nblk(nn);
+  const __half* A = static_cast<const __half*>(Ah);
+  if (mode == kApply)
+    k_stencil_op_h<kApply><<<nb, kThreads, 0, s>>>(d, A, sc, act, x, b, invdiag, omega, y);
+  else if (mode == kResidual)
+    k_stencil_op_h<kResidual><<<nb, kThreads, 0, s>>>(d, A, sc, act, x, b, invdiag, omega, y);
+  else
+    k_stencil_op_h<kSmooth><<<nb, kThreads, 0, s>>>(d, A, sc, act, x, b, invdiag, omega, y);
   TG_LAUNCH_CHECK();
 }
 

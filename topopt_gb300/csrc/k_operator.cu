@@ -198,11 +198,11 @@ template <class T>
 struct Pencil;
 template <>
 struct Pencil<double> {
-  static constexpr int PY = 8, KZ = 16;
+  static constexpr int PY = 8, KZ = 16, MINB = 2;
 };
 template <>
 struct Pencil<float> {
-  static constexpr int PY = 16, KZ = 16;
+  static constexpr int PY = 8, KZ = 16, MINB = 3;
 };
 
 template <class T>
@@ -218,25 +218,36 @@ __device__ __forceinline__ void load_node(const GridDev& g, const T* __restrict_
   }
 }
 
-// Loads layer c of the lane's element corners: v[yb][xb][comp] for nodes
-// (ex + xb, ey + yb, c).  The +x nodes come from the next lane; lane 31 loads its own.
+// Raw loads of layer c for the lane's own column: nodes (ex, ey, c), (ex, ey+1, c)
+// and, for lane 31, (ex+1, ey, c), (ex+1, ey+1, c).  Issued one step ahead so
+// their latency overlaps the current layer's arithmetic.
 template <class T>
-__device__ __forceinline__ void load_layer(const GridDev& g, const T* __restrict__ x, int ex,
-                                           int ey, int c, int lane, T (&v)[2][2][3]) {
-  load_node(g, x, ex, ey, c, v[0][0]);
-  load_node(g, x, ex, ey + 1, c, v[1][0]);
-#pragma unroll
-  for (int yb = 0; yb < 2; ++yb)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) v[yb][1][k] = __shfl_down_sync(0xffffffffu, v[yb][0][k], 1);
+__device__ __forceinline__ void load_raw(const GridDev& g, const T* __restrict__ x, int ex, int ey,
+                                         int c, int lane, T (&r)[2][2][3]) {
+  load_node(g, x, ex, ey, c, r[0][0]);
+  load_node(g, x, ex, ey + 1, c, r[1][0]);
   if (lane == 31) {
-    load_node(g, x, ex + 1, ey, c, v[0][1]);
-    load_node(g, x, ex + 1, ey + 1, c, v[1][1]);
+    load_node(g, x, ex + 1, ey, c, r[0][1]);
+    load_node(g, x, ex + 1, ey + 1, c, r[1][1]);
   }
 }
 
-template <class T, int PY, int KZ, int MODE>
-__global__ void __launch_bounds__(32 * PY) k_fine_op(GridDev g, ModalT<T> mc,
+// Completes a layer: v[yb][xb][comp] for nodes (ex + xb, ey + yb); the +x nodes
+// come from the next lane (lane 31 loaded its own).
+template <class T>
+__device__ __forceinline__ void finish_layer(int lane, const T (&r)[2][2][3], T (&v)[2][2][3]) {
+#pragma unroll
+  for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      v[yb][0][k] = r[yb][0][k];
+      const T nb = __shfl_down_sync(0xffffffffu, r[yb][0][k], 1);
+      v[yb][1][k] = lane == 31 ? r[yb][1][k] : nb;
+    }
+}
+
+template <class T, int PY, int KZ, int MINB, int MODE>
+__global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> mc,
                                                      const T* __restrict__ ef,
                                                      const uint8_t* __restrict__ kept,
                                                      const T* __restrict__ x, const T* __restrict__ b,
@@ -249,14 +260,17 @@ __global__ void __launch_bounds__(32 * PY) k_fine_op(GridDev g, ModalT<T> mc,
   const int k0 = blockIdx.z * KZ;
   const bool own_xy = lane >= 1 && w >= 1 && ex < g.nnx && ey < g.nny;
   const bool exy_ok = ex >= 0 && ex < g.nx && ey >= 0 && ey < g.ny;
-  T cur[2][2][3], nxt[2][2][3];
-  load_layer(g, x, ex, ey, k0 - 1, lane, cur);
+  T cur[2][2][3], nxt[2][2][3], raw[2][2][3];
+  load_raw(g, x, ex, ey, k0 - 1, lane, raw);
+  finish_layer(lane, raw, cur);
+  load_raw(g, x, ex, ey, k0, lane, raw);
   T pend[3] = {T(0), T(0), T(0)};
   double dsum = 0.0;
 #pragma unroll 1
   for (int s = 0; s <= KZ; ++s) {
     const int ez = k0 - 1 + s;
-    load_layer(g, x, ex, ey, ez + 1, lane, nxt);
+    finish_layer(lane, raw, nxt);
+    if (s < KZ) load_raw(g, x, ex, ey, ez + 2, lane, raw);
     T ux[8], uy[8], uz[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -350,7 +364,7 @@ static void launch_mode(const Grid& g, const ModalConsts& c, const T* ef, const 
                         double* dot_part, cudaStream_t s) {
   using P = Pencil<T>;
   const GridDev gd{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz};
-  k_fine_op<T, P::PY, P::KZ, MODE><<<pencil_grid<T>(g), 32 * P::PY, 0, s>>>(
+  k_fine_op<T, P::PY, P::KZ, P::MINB, MODE><<<pencil_grid<T>(g), 32 * P::PY, 0, s>>>(
       gd, to_modal<T>(c), ef, kept, x, b, invdiag, omega, y, dot_part);
   TG_LAUNCH_CHECK();
 }

@@ -185,7 +185,8 @@ struct Solver::Level {
   // FP64 operators and vectors (plain form, and the FP64 retry of the mixed form).
   DBuf<double> Kel, A, invd, xa, xb, b;
   // FP32 operators and vectors (mixed form).
-  DBuf<float> Kelf, Af, invdf, fxa, fxb, fb;
+  DBuf<float> Kelf, Af, invdf, fxa, fxb, fb, scf;
+  DBuf<uint16_t> Ah;  // FP16 scaled stencil (mixed form, levels above the coarsest)
   double *x = nullptr, *r = nullptr;
   float *xf = nullptr, *rf = nullptr;
   template <class T>
@@ -205,7 +206,7 @@ struct Solver::Level {
   size_t bytes() const {
     return act.bytes() + Kel.bytes() + A.bytes() + invd.bytes() + xa.bytes() + xb.bytes() +
            b.bytes() + Kelf.bytes() + Af.bytes() + invdf.bytes() + fxa.bytes() + fxb.bytes() +
-           fb.bytes();
+           fb.bytes() + scf.bytes() + Ah.bytes();
   }
 };
 template <>
@@ -509,6 +510,14 @@ bool Solver::build_numeric() {
     else
       mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
     mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, L.Am<T>(), L.Dinv<T>(), s_);
+    if (sizeof(T) == 4 && half_coarse_ && l + 1 < levels_.size()) {
+      if (!L.Ah.p) {
+        L.Ah.alloc(size_t(L.nn) * 243);
+        L.scf.alloc(size_t(L.ndof));
+      }
+      mg_normalize_stencil(L.d, reinterpret_cast<const float*>(L.Am<T>()),
+                           reinterpret_cast<const float*>(L.Dinv<T>()), L.scf.p, L.Ah.p, s_);
+    }
     pd = L.d;
   }
   Level& C = *levels_.back();
@@ -532,14 +541,23 @@ void Solver::vcycle_level(size_t l) {
   }
   Level& N = *levels_[l];
   const T w = T(omega_);
+  const bool half = sizeof(T) == 4 && L.Ah.p != nullptr;
+  auto op = [&](int mode) {
+    if (half)
+      mg_stencil_op_h(mode, L.d, L.Ah.p, L.scf.p, L.act.p, reinterpret_cast<const float*>(L.X<T>()),
+                      reinterpret_cast<const float*>(L.B<T>()),
+                      reinterpret_cast<const float*>(L.Dinv<T>()), float(omega_),
+                      reinterpret_cast<float*>(L.R<T>()), s_);
+    else
+      mg_stencil_op<T>(mode, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
+                       L.R<T>(), s_);
+  };
   mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);
-  mg_stencil_op<T>(kResidual, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
-                   L.R<T>(), s_);
+  op(kResidual);
   mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
   vcycle_level<T>(l + 1);
   mg_prolong_add<T>(L.d, N.d, N.X<T>(), L.act.p, L.X<T>(), s_);
-  mg_stencil_op<T>(kSmooth, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
-                   L.R<T>(), s_);
+  op(kSmooth);
   std::swap(L.X<T>(), L.R<T>());
 }
 
