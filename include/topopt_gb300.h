@@ -89,7 +89,9 @@ typedef struct {
   double omega;            /* 0 = 0.6 */
   double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve, 0 = 1e-3 */
   int32_t max_refinements; /* mixed: outer FP64 refinement steps, 0 = 20 */
-  int32_t reserved;
+  int32_t coarse_fp16;     /* mixed: coarse stencils in diagonally scaled FP16 (1 = on; default 0 =
+                              FP32).  FP16 rounding breaks the stencils' zero row sums (the
+                              rigid-translation null space) and the V-cycle can lose definiteness. */
 } tg_solve_options;
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */
@@ -101,6 +103,8 @@ typedef struct {
   int64_t matvecs_lowp;   /* fine reduced-precision operator applies */
   int32_t refinements;    /* mixed: outer FP64 refinement steps */
   int32_t ng;             /* surviving (kept) DOFs */
+  int32_t mixed_fallback; /* mixed: the FP32 inner solve failed and FP64 MG-PCG took over */
+  int32_t inner_breakdowns;
   double t_build_ms, t_mg_build_ms, t_solve_ms, t_total_ms;
 } tg_cg_info;
 

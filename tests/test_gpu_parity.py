@@ -25,6 +25,17 @@ def _pb(tg, golden, key="apply"):
     return tg.Problem(nx, ny, nz, 1.0, tags, bcs, loads), o
 
 
+def smooth_modulus(pb, seed=2):
+    """A SIMP-like (filtered, hence smooth) density field rho in [1e-3, 1], E = rho^3."""
+    k, j, i = np.meshgrid(np.arange(pb.nz), np.arange(pb.ny), np.arange(pb.nx), indexing="ij")
+    rng = np.random.default_rng(seed)
+    rho = np.full(i.shape, 0.3)
+    for _ in range(4):
+        fx, fy, fz, ph = rng.uniform(0.5, 3.0, 3).tolist() + [rng.uniform(0, 6.3)]
+        rho += 0.15 * np.sin(fx * np.pi * i / pb.nx + fy * np.pi * j / pb.ny + fz * np.pi * k / pb.nz + ph)
+    return np.clip(rho, 1e-3, 1.0).ravel() ** 3
+
+
 def rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
@@ -90,6 +101,21 @@ def test_solve_matches_reference(tg, golden, solver, prec, tol):
     assert rel(u, golden["cg_u"]) < 1e-8
     if solver == 0:
         assert info.used_multigrid and info.mg_levels >= 2
+    if prec == 1:  # the mixed path itself converged: no FP64 MG-PCG takeover
+        assert not info.mixed_fallback and info.matvecs_lowp > 0 and info.refinements >= 1
+
+
+@pytest.mark.parametrize("fp16", [0])
+def test_mixed_solve_large(tg, fp16):
+    """96x48x48 cantilever with a smooth (SIMP-like) modulus field: the mixed form
+    (FP32 V-cycle, FP32 coarse stencils) converges on its own, to the FP64 solution."""
+    pb = tg.Problem.cantilever(96, 48, 48)
+    E = smooth_modulus(pb)
+    u64, i64 = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10)
+    u32, i32 = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        precision=tg.PREC_MIXED, coarse_fp16=fp16))
+    assert not i32.mixed_fallback and i32.inner_breakdowns == 0, i32
+    assert rel(u32, u64) < 1e-8
 
 
 def test_compliance_and_sensitivity(tg, golden):

@@ -60,7 +60,7 @@ class _SolveOpt(C.Structure):
     _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("mg_levels", C.c_int32),
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
                 ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("coarse_fp16", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -68,7 +68,8 @@ class _CgInfo(C.Structure):
                 ("used_multigrid", C.c_int32), ("mg_levels", C.c_int32),
                 ("hier_built", C.c_int32), ("mg_cycles_attempted", C.c_int32),
                 ("matvecs", C.c_int64), ("matvecs_lowp", C.c_int64),
-                ("refinements", C.c_int32), ("ng", C.c_int32), ("t_build_ms", C.c_double),
+                ("refinements", C.c_int32), ("ng", C.c_int32), ("mixed_fallback", C.c_int32),
+                ("inner_breakdowns", C.c_int32), ("t_build_ms", C.c_double),
                 ("t_mg_build_ms", C.c_double), ("t_solve_ms", C.c_double),
                 ("t_total_ms", C.c_double)]
 
@@ -226,10 +227,12 @@ class SolveOptions:
     omega: float = 0.0
     inner_tolerance: float = 0.0
     max_refinements: int = 0
+    coarse_fp16: int = 0
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
-                         self.omega, self.inner_tolerance, self.max_refinements, 0)
+                         self.omega, self.inner_tolerance, self.max_refinements,
+                         self.coarse_fp16)
 
 
 @dataclass
@@ -276,6 +279,8 @@ class CgInfo:
     matvecs_lowp: int
     refinements: int
     ng: int
+    mixed_fallback: bool
+    inner_breakdowns: int
     t_build_ms: float
     t_mg_build_ms: float
     t_solve_ms: float
@@ -285,7 +290,8 @@ class CgInfo:
     def _from(cls, c: _CgInfo):
         return cls(bool(c.converged), c.iterations, c.residual, bool(c.used_multigrid),
                    c.mg_levels, bool(c.hier_built), c.mg_cycles_attempted, c.matvecs,
-                   c.matvecs_lowp, c.refinements, c.ng, c.t_build_ms, c.t_mg_build_ms,
+                   c.matvecs_lowp, c.refinements, c.ng, bool(c.mixed_fallback),
+                   c.inner_breakdowns, c.t_build_ms, c.t_mg_build_ms,
                    c.t_solve_ms, c.t_total_ms)
 
 

@@ -134,6 +134,8 @@ void fill_info(tg_cg_info* info, const SolverStats& st, const FineProblem& fp, d
   info->matvecs_lowp = st.matvecs_lowp;
   info->refinements = st.refinements;
   info->ng = int32_t(fp.ng);
+  info->mixed_fallback = st.mixed_fallback;
+  info->inner_breakdowns = st.inner_breakdowns;
   info->t_build_ms = t_build;
   info->t_mg_build_ms = st.t_mg_build_ms;
   info->t_solve_ms = st.t_solve_ms;

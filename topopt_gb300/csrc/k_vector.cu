@@ -88,7 +88,10 @@ __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __
                                const T* __restrict__ ap, const double* __restrict__ rz,
                                const double* __restrict__ pap, int64_t n,
                                double* __restrict__ part) {
-  const double alpha = *rz / *pap;
+  // A non-positive or non-finite pAp is a breakdown the host reports; leave the
+  // iterate untouched so the last good x survives.
+  const double pp = *pap;
+  const double alpha = (pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0;
   const T a = T(alpha);
   double s = 0.0;
   for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;

@@ -258,6 +258,7 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   omega_ = opt.omega > 0.0 ? opt.omega : 0.6;
   budget_ = opt.mg_iter_budget > 0 ? opt.mg_iter_budget : 300;
   mixed_ = opt.precision == TG_PREC_MIXED;
+  half_coarse_ = opt.coarse_fp16 > 0;
   const size_t n = size_t(fp.g.ndof);
   for (DBuf<double>* b : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_}) b->alloc(n);
   part_n_ = std::max({kRedBlocks, fine_op_blocks(fp.g, true), fine_op_blocks(fp.g, false),
@@ -679,7 +680,10 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
     launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
     double sc[2];
     read_scalars(7, 2, sc);
-    if (!(sc[0] > 0.0) || !std::isfinite(sc[0])) return k > 1;
+    if (!(sc[0] > 0.0) || !std::isfinite(sc[0])) {  // breakdown: x, r were left untouched
+      ++st.inner_breakdowns;
+      return k > 1;
+    }
     *iters = k;
     if (std::sqrt(sc[1]) <= thr) return true;
     z = vcycle<float>(rf_.p);
@@ -816,6 +820,7 @@ SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u
       if (warm) seed();
       solved = mixed_refine(tol, std::min(cap, budget_), warm, st);
     }
+    if (mixed_ && !solved) st.mixed_fallback = true;
     if (!solved && (!mixed_ || build_numeric<double>())) {
       if (warm) seed();
       solved = mgpcg(tol, std::min(cap, budget_), warm, st);

@@ -45,6 +45,8 @@ struct SolverStats {
   double residual = 0.0;
   bool converged = false, used_mg = false, hier_built = false;
   int mg_levels = 0, mg_cycles = 0, refinements = 0;
+  bool mixed_fallback = false;
+  int inner_breakdowns = 0;
   int64_t matvecs = 0, matvecs_lowp = 0;
   double t_mg_build_ms = 0.0, t_solve_ms = 0.0;
 };
@@ -108,7 +110,7 @@ class Solver {
   DBuf<float> kebf_, Gf_;
   bool have_mg_ = false, numeric_ok_ = false, numeric_[2] = {false, false};
   double mg_build_ms_ = 0.0;
-  bool half_coarse_ = true;  // mixed form: FP16 scaled stencils on levels 1..L-2
+  bool half_coarse_ = false;  // mixed form: FP16 scaled stencils on levels 1..L-2 (opt-in)
   int64_t fine_matvecs_ = 0, lowp_matvecs_ = 0;
   int nc_ = 0;
   DBuf<int> cidx_, chol_fail_;
