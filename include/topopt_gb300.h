@@ -224,6 +224,22 @@ int64_t tg_job_device_bytes(const tg_job* job);
 int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* options);
 void tg_job_destroy(tg_job* job);
 
+/* ---- the density filter without device allocation ----
+ * No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc when they filter (allocator-free serving or real-time loops, hosts
+ * whose device memory belongs to another runtime's arena).  Same result as
+ * tg_filter, bit for bit; inputs and outputs are the caller's DEVICE buffers
+ * (d_tags: one VoxelTag byte per voxel, NULL = all solid; d_x, d_out: voxels),
+ * enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream) and
+ * not synchronised.  Scratch lives in one fixed device array of the library:
+ * at most 1,048,576 voxels and a radius of at most 6 voxels (TG_EINVAL beyond);
+ * every GPU that loads the library holds the array (~17 MB) until exit.  Calls
+ * share it, so calls that overlap on the GPU race -- keep them on one stream.
+ * The first call on each device sets up the array's address (make it before any
+ * stream capture); no call allocates, frees or leaves state for the next. */
+int tg_filter_noalloc(int32_t nx, int32_t ny, int32_t nz, const uint8_t* d_tags, double radius,
+                      int32_t adjoint, const double* d_x, double* d_out, void* stream);
+
 /* ---- measurement (no reference counterpart) ---- */
 /* Average device time of one fine-operator launch (y = A x on the job's current
  * element factors), precision TG_PREC_FP64 or TG_PREC_MIXED (FP32), over `reps`

@@ -43,6 +43,7 @@ double now_ms() {
 }  // namespace
 
 void raise(int code, const std::string& msg) { throw Error(code, msg); }
+void set_last_error(const std::string& msg) { g_err = msg; }
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {

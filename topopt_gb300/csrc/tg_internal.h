@@ -27,6 +27,7 @@ struct Error : std::runtime_error {
 };
 
 [[noreturn]] void raise(int code, const std::string& msg);
+void set_last_error(const std::string& msg);
 void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
 #define TG_CUDA(call)                                                  \
