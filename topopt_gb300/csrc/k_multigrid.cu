@@ -27,6 +27,8 @@
 #include "tg_internal.h"
 #include "tg_multigrid.h"
 
+#include <algorithm>
+
 namespace tg {
 
 namespace {
@@ -241,55 +243,49 @@ __global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int6
 }
 
 // Stencil operator: y = A x / b - A x / x + w D^-1 (b - A x), masked by act.
+// Three warps per 32 nodes: a warp owns one output component c1 of 32
+// consecutive nodes, so its reads of A (entry (d, c1, c2) of 32 nodes) are
+// contiguous, and each thread's chain is 27 x 3 multiply-adds with all loads
+// independent (the neighbour loop is unrolled, out-of-grid neighbours predicated).
+constexpr int kStencilNodes = 64;  // nodes per CTA; blockDim = 3 * kStencilNodes
 template <class T, int MODE>
-__global__ void __launch_bounds__(kThreads) k_stencil_op(MgDims d, const T* __restrict__ A,
-                                                         const uint8_t* __restrict__ act,
-                                                         const T* __restrict__ x,
-                                                         const T* __restrict__ b,
-                                                         const T* __restrict__ invdiag, T omega,
-                                                         T* __restrict__ y) {
+__global__ void __launch_bounds__(3 * kStencilNodes, 3) k_stencil_op(MgDims d, const T* __restrict__ A,
+                                                                  const uint8_t* __restrict__ act,
+                                                                  const T* __restrict__ x,
+                                                                  const T* __restrict__ b,
+                                                                  const T* __restrict__ invdiag,
+                                                                  T omega, T* __restrict__ y) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
-       n += int64_t(gridDim.x) * kThreads) {
+  const int c1 = threadIdx.x / kStencilNodes;
+  for (int64_t n = blockIdx.x * int64_t(kStencilNodes) + threadIdx.x % kStencilNodes; n < nn;
+       n += int64_t(gridDim.x) * kStencilNodes) {
     const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny),
               c = int(n / (int64_t(d.nnx) * d.nny));
-    T s0 = 0, s1 = 0, s2 = 0;
-    for (int dz = -1; dz <= 1; ++dz) {
-      const int k = c + dz;
-      if (k < 0 || k >= d.nnz) continue;
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int j = bb + dy;
-        if (j < 0 || j >= d.nny) continue;
-#pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int i = a + dx;
-          if (i < 0 || i >= d.nnx) continue;
-          const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
-          const int64_t m = (int64_t(k) * d.nny + j) * d.nnx + i;
-          const T x0 = x[3 * m], x1 = x[3 * m + 1], x2 = x[3 * m + 2];
-          const T* Ab = A + int64_t(di * 9) * nn + n;
-          s0 += Ab[0] * x0 + Ab[nn] * x1 + Ab[2 * nn] * x2;
-          s1 += Ab[3 * nn] * x0 + Ab[4 * nn] * x1 + Ab[5 * nn] * x2;
-          s2 += Ab[6 * nn] * x0 + Ab[7 * nn] * x1 + Ab[8 * nn] * x2;
-        }
-      }
+    T acc = T(0);
+#pragma unroll 9
+    for (int di = 0; di < 27; ++di) {
+      const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
+      const bool in = (a + dx) >= 0 && (a + dx) < d.nnx && (bb + dy) >= 0 && (bb + dy) < d.nny &&
+                      (c + dz) >= 0 && (c + dz) < d.nnz;
+      const int64_t m = in ? n + (int64_t(dz) * d.nny + dy) * d.nnx + dx : n;
+      const T* Ab = A + int64_t(di * 9 + c1 * 3) * nn + n;
+      const T a0 = Ab[0], a1 = Ab[nn], a2 = Ab[2 * nn];
+      const T x0 = x[3 * m], x1 = x[3 * m + 1], x2 = x[3 * m + 2];
+      const T t = a0 * x0 + a1 * x1 + a2 * x2;
+      acc += in ? t : T(0);
     }
-    const T s[3] = {s0, s1, s2};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int64_t dof = 3 * n + k;
-      T out;
-      if (!act[dof]) {
-        out = T(0);
-      } else if (MODE == kApply) {
-        out = s[k];
-      } else if (MODE == kResidual) {
-        out = b[dof] - s[k];
-      } else {
-        out = x[dof] + omega * invdiag[dof] * (b[dof] - s[k]);
-      }
-      y[dof] = out;
+    const int64_t dof = 3 * n + c1;
+    T out;
+    if (!act[dof]) {
+      out = T(0);
+    } else if (MODE == kApply) {
+      out = acc;
+    } else if (MODE == kResidual) {
+      out = b[dof] - acc;
+    } else {
+      out = x[dof] + omega * invdiag[dof] * (b[dof] - acc);
     }
+    y[dof] = out;
   }
 }
 
@@ -558,6 +554,48 @@ __global__ void k_chol_update(double* __restrict__ D, int nc, int k0) {
   }
 }
 
+// Explicit inverse of the coarsest operator from its Cholesky factor, for small
+// coarsest levels: thread j forms column j of L^-1 by forward substitution, then
+// Ainv = L^-T L^-1 (both FP64).  Each V-cycle then needs one dense matvec.
+__global__ void k_chol_invert_L(const double* __restrict__ L, int nc, double* __restrict__ Li) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nc) return;
+  for (int i = 0; i < j; ++i) Li[int64_t(i) * nc + j] = 0.0;
+  for (int i = j; i < nc; ++i) {
+    double v = (i == j) ? 1.0 : 0.0;
+    for (int k = j; k < i; ++k) v -= L[int64_t(i) * nc + k] * Li[int64_t(k) * nc + j];
+    Li[int64_t(i) * nc + j] = v / L[int64_t(i) * nc + i];
+  }
+}
+
+__global__ void k_chol_inverse(const double* __restrict__ Li, int nc, double* __restrict__ Ainv) {
+  const int i = blockIdx.y * 16 + threadIdx.y, j = blockIdx.x * 16 + threadIdx.x;
+  if (i >= nc || j >= nc) return;
+  double s = 0.0;
+  for (int k = max(i, j); k < nc; ++k) s += Li[int64_t(k) * nc + i] * Li[int64_t(k) * nc + j];
+  Ainv[int64_t(i) * nc + j] = s;
+}
+
+// x = Ainv b on the compact numbering, gathered from / scattered to the level
+// vector; one warp per row of Ainv.
+template <class T>
+__global__ void k_coarse_inv_apply(const double* __restrict__ Ainv, int nc,
+                                   const int* __restrict__ cidx, const int* __restrict__ cdof,
+                                   int64_t ndof, const T* __restrict__ b, T* __restrict__ x) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t dd = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; dd < ndof;
+       dd += int64_t(gridDim.x) * blockDim.x)
+    if (cidx[dd] < 0) x[dd] = T(0);
+  for (int r = warp; r < nc; r += nwarps) {
+    double s = 0.0;
+    for (int k = lane; k < nc; k += 32) s += Ainv[int64_t(r) * nc + k] * double(b[cdof[k]]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) x[cdof[r]] = T(s);
+  }
+}
+
 // Forward and backward substitution with the factor, one CTA; the coarsest
 // right-hand side is gathered from / scattered to the stencil-level vector.
 template <class T>
@@ -630,13 +668,14 @@ template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  const int nb = nblk(nn);
+  const int nb = nblk(nn, kStencilNodes);
+  const int nt = 3 * kStencilNodes;
   if (mode == kApply)
-    k_stencil_op<T, kApply><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else if (mode == kResidual)
-    k_stencil_op<T, kResidual><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kResidual><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else
-    k_stencil_op<T, kSmooth><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kSmooth><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   TG_LAUNCH_CHECK();
 }
 
@@ -709,6 +748,21 @@ void mg_cholesky(double* D, int nc, int* fail, cudaStream_t s) {
   }
 }
 
+void mg_chol_inverse(const double* L, int nc, double* Li, double* Ainv, cudaStream_t s) {
+  k_chol_invert_L<<<(nc + 127) / 128, 128, 0, s>>>(L, nc, Li);
+  TG_LAUNCH_CHECK();
+  const dim3 grid((nc + 15) / 16, (nc + 15) / 16);
+  k_chol_inverse<<<grid, dim3(16, 16), 0, s>>>(Li, nc, Ainv);
+  TG_LAUNCH_CHECK();
+}
+
+template <class T>
+void mg_coarse_inv_apply(const double* Ainv, int nc, const int* cidx, const int* cdof,
+                         int64_t ndof, const T* b, T* x, cudaStream_t s) {
+  k_coarse_inv_apply<T><<<std::max(1, std::min(152, (nc + 7) / 8)), 256, 0, s>>>(Ainv, nc, cidx, cdof, ndof, b, x);
+  TG_LAUNCH_CHECK();
+}
+
 template <class T>
 void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const T* b, T* x,
                    double* work, cudaStream_t s) {
@@ -726,6 +780,8 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
                                   cudaStream_t);                                              \
   template void mg_chol_solve<T>(const double*, int, const int*, int64_t, const T*, T*,       \
                                  double*, cudaStream_t);                                      \
+  template void mg_coarse_inv_apply<T>(const double*, int, const int*, const int*, int64_t,    \
+                                       const T*, T*, cudaStream_t);                           \
   template void mg_galerkin_level1<T>(const MgDims&, const MgDims&, const T*, const uint8_t*,  \
                                       const uint8_t*, const T*, const T*, T*, cudaStream_t);  \
   template void mg_galerkin_coarse<T>(const MgDims&, const MgDims&, const T*, const uint8_t*,  \

@@ -63,6 +63,17 @@ __device__ __forceinline__ double clamp_density(double rho, double rho_min) {
   return (lo < 1.0) ? lo : 1.0;                       // std::min(1.0, lo)
 }
 
+// rho^p: integral exponents (the SIMP default p = 3) by repeated multiplication,
+// which needs a few FP64 multiplies instead of a pow() evaluation; other
+// exponents through pow().
+__device__ __forceinline__ double powp(double r, double p) {
+  if (p == 3.0) return r * r * r;
+  if (p == 2.0) return r * r;
+  if (p == 1.0) return r;
+  if (p == 4.0) { const double r2 = r * r; return r2 * r2; }
+  return pow(r, p);
+}
+
 __global__ void k_modulus(const double* __restrict__ rho, const uint8_t* __restrict__ elem,
                           int64_t n, double E0, double p, double rho_min, int law, double emin,
                           double* __restrict__ E) {
@@ -71,9 +82,9 @@ __global__ void k_modulus(const double* __restrict__ rho, const uint8_t* __restr
     double v = 0.0;
     if (elem[e]) {
       if (law == 0)
-        v = pow(clamp_density(rho[e], rho_min), p) * E0;
+        v = powp(clamp_density(rho[e], rho_min), p) * E0;
       else
-        v = emin + pow(rho[e], p) * (E0 - emin);
+        v = emin + powp(rho[e], p) * (E0 - emin);
     }
     E[e] = v;
   }
@@ -182,12 +193,12 @@ __global__ void k_sensitivity(GridDev g, Modal64 mc, const double* __restrict__ 
       const double q = modal_energy(mc, ux, uy, uz);
       if (law == 0) {
         const double r = clamp_density(rho[e], rho_min);
-        csum += pow(r, p) * E0 * q;
-        d = -p * pow(r, p - 1.0) * E0 * q;
+        csum += powp(r, p) * E0 * q;
+        d = -p * powp(r, p - 1.0) * E0 * q;
       } else {
         const double r = rho[e];
-        csum += (emin + pow(r, p) * (E0 - emin)) * q;
-        d = -p * pow(r, p - 1.0) * (E0 - emin) * q;
+        csum += (emin + powp(r, p) * (E0 - emin)) * q;
+        d = -p * powp(r, p - 1.0) * (E0 - emin) * q;
       }
     }
     dc[e] = d;

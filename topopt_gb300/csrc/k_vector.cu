@@ -56,14 +56,17 @@ __device__ __forceinline__ double block_max256(double v) {
   return s;
 }
 
+// FP32 vectors are summed in FP32 along each thread's grid-stride run (a few
+// dozen terms) and in FP64 across threads and blocks: on GB300 an FP64 multiply
+// per element would make these streaming kernels FP64-pipe-bound.
 template <class T>
 __global__ void k_dot(const T* __restrict__ a, const T* __restrict__ b, int64_t n,
                       double* __restrict__ part) {
-  double s = 0.0;
+  T t = T(0);
   for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * kThreads)
-    s += double(a[i]) * double(b[i]);
-  s = block_sum256(s);
+    t += a[i] * b[i];
+  const double s = block_sum256(double(t));
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
@@ -93,15 +96,15 @@ __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __
   const double pp = *pap;
   const double alpha = (pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0;
   const T a = T(alpha);
-  double s = 0.0;
+  T t = T(0);
   for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * kThreads) {
     x[i] += a * p[i];
     const T ri = r[i] - a * ap[i];
     r[i] = ri;
-    s += double(ri) * double(ri);
+    t += ri * ri;
   }
-  s = block_sum256(s);
+  const double s = block_sum256(double(t));
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 

@@ -33,7 +33,8 @@ const int kLocToBit[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 const double kXi[8] = {-1, +1, +1, -1, -1, +1, +1, -1};
 const double kEta[8] = {-1, -1, +1, +1, -1, -1, +1, +1};
 const double kZeta[8] = {-1, -1, -1, -1, +1, +1, +1, +1};
-constexpr int kMaxCoarseDof = 8192;  // dense coarsest factor <= 512 MB
+constexpr int kMaxCoarseDof = 8192;   // dense coarsest factor <= 512 MB
+constexpr int kMaxInverseDof = 512;   // explicit coarsest inverse up to here
 
 MgDims dims_of(int ex, int ey, int ez) { return MgDims{ex, ey, ez, ex + 1, ey + 1, ez + 1}; }
 }  // namespace
@@ -282,6 +283,7 @@ size_t Solver::device_bytes() const {
   for (const DBuf<double>* d : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_, &part_,
                                 &scal_, &keb_, &G_, &chol_, &chol_work_})
     b += d->bytes();
+  b += chol_li_.bytes() + chol_inv_.bytes() + cdof_.bytes();
   for (const DBuf<float>* d : {&Ef_, &invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_})
     b += d->bytes();
   for (const auto& L : levels_) b += L->bytes();
@@ -352,6 +354,15 @@ void Solver::build_structure() {
   }
   cidx_.alloc(size_t(C.ndof));
   TG_CUDA(cudaMemcpyAsync(cidx_.p, cidx.data(), cidx_.bytes(), cudaMemcpyHostToDevice, s_));
+  std::vector<int> cdof(static_cast<size_t>(nc_));
+  for (int64_t d = 0; d < C.ndof; ++d)
+    if (cidx[size_t(d)] >= 0) cdof[size_t(cidx[size_t(d)])] = int(d);
+  cdof_.alloc(size_t(nc_));
+  TG_CUDA(cudaMemcpyAsync(cdof_.p, cdof.data(), cdof_.bytes(), cudaMemcpyHostToDevice, s_));
+  if (nc_ <= kMaxInverseDof) {
+    chol_li_.alloc(size_t(nc_) * nc_);
+    chol_inv_.alloc(size_t(nc_) * nc_);
+  }
   chol_.alloc(size_t(nc_) * nc_);
   chol_work_.alloc(size_t(nc_));
   chol_fail_.alloc(1);
@@ -528,6 +539,7 @@ bool Solver::build_numeric() {
   int fail = 0;
   TG_CUDA(cudaMemcpyAsync(&fail, chol_fail_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
   TG_CUDA(cudaStreamSynchronize(s_));
+  if (fail == 0 && chol_inv_.p) mg_chol_inverse(chol_.p, nc_, chol_li_.p, chol_inv_.p, s_);
   numeric_[sizeof(T) == 8 ? 1 : 0] = (fail == 0);
   return fail == 0;
 }
@@ -537,7 +549,10 @@ template <class T>
 void Solver::vcycle_level(size_t l) {
   Level& L = *levels_[l - 1];
   if (l == levels_.size()) {
-    mg_chol_solve<T>(chol_.p, nc_, cidx_.p, L.ndof, L.B<T>(), L.X<T>(), chol_work_.p, s_);
+    if (chol_inv_.p)
+      mg_coarse_inv_apply<T>(chol_inv_.p, nc_, cidx_.p, cdof_.p, L.ndof, L.B<T>(), L.X<T>(), s_);
+    else
+      mg_chol_solve<T>(chol_.p, nc_, cidx_.p, L.ndof, L.B<T>(), L.X<T>(), chol_work_.p, s_);
     return;
   }
   Level& N = *levels_[l];

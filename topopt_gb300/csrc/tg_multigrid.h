@@ -42,6 +42,12 @@ template <class T>
 void mg_dense_from_stencil(const MgDims& d, const T* A, const int* cidx, int nc, double* D,
                            cudaStream_t s);
 void mg_cholesky(double* D, int nc, int* fail, cudaStream_t s);
+// Explicit inverse of the coarsest operator from its factor (small levels).
+void mg_chol_inverse(const double* L, int nc, double* Li, double* Ainv, cudaStream_t s);
+// x = Ainv b over the compact numbering (cidx: dof -> compact, cdof: compact -> dof).
+template <class T>
+void mg_coarse_inv_apply(const double* Ainv, int nc, const int* cidx, const int* cdof,
+                         int64_t ndof, const T* b, T* x, cudaStream_t s);
 template <class T>
 void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const T* b, T* x,
                    double* work, cudaStream_t s);

@@ -113,8 +113,8 @@ class Solver {
   bool half_coarse_ = false;  // mixed form: FP16 scaled stencils on levels 1..L-2 (opt-in)
   int64_t fine_matvecs_ = 0, lowp_matvecs_ = 0;
   int nc_ = 0;
-  DBuf<int> cidx_, chol_fail_;
-  DBuf<double> chol_, chol_work_;
+  DBuf<int> cidx_, cdof_, chol_fail_;
+  DBuf<double> chol_, chol_work_, chol_li_, chol_inv_;
 };
 
 }  // namespace tg
