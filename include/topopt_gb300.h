@@ -89,9 +89,6 @@ typedef struct {
   double omega;            /* 0 = 0.6 */
   double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve, 0 = 1e-3 */
   int32_t max_refinements; /* mixed: outer FP64 refinement steps, 0 = 20 */
-  int32_t coarse_fp16;     /* mixed: coarse stencils in diagonally scaled FP16 (1 = on; default 0 =
-                              FP32).  FP16 rounding breaks the stencils' zero row sums (the
-                              rigid-translation null space) and the V-cycle can lose definiteness. */
 } tg_solve_options;
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */

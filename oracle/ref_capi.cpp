@@ -36,6 +36,20 @@ VoxelGrid make_grid(int nx, int ny, int nz, double h, const uint8_t* solid) {
   return g;
 }
 
+// A grid with the caller's raw tags (VoxelTag values; NULL = all Interior).
+VoxelGrid make_grid_tags(int nx, int ny, int nz, double h, const uint8_t* tags) {
+  VoxelGrid g = make_grid(nx, ny, nz, h, nullptr);
+  if (tags)
+    for (std::size_t e = 0; e < g.tags.size(); ++e) g.tags[e] = static_cast<VoxelTag>(tags[e]);
+  return g;
+}
+
+DesignMask make_mask(std::size_t nv, const uint8_t* mask) {
+  DesignMask m(nv);
+  for (std::size_t e = 0; e < nv; ++e) m[e] = static_cast<MaskValue>(mask[e]);
+  return m;
+}
+
 std::vector<DirichletBC> make_bcs(int n, const int* node, const int* comp, const double* val) {
   std::vector<DirichletBC> v(static_cast<std::size_t>(n));
   for (int i = 0; i < n; ++i) v[i] = DirichletBC{node[i], comp[i], val[i]};
@@ -239,6 +253,74 @@ int ref_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, do
     o.solver = SolverKind::MultigridCG_Matfree;
     const SimpOptimizeResult r = simp_optimize(g, p, make_bcs(nbc, bc_node, bc_comp, bc_val),
                                                make_loads(nload, ld_node, ld_comp, ld_val), o);
+    for (std::size_t i = 0; i < r.history.size(); ++i) {
+      hist_c[i] = r.history[i].compliance;
+      hist_change[i] = r.history[i].change;
+      hist_vf[i] = r.history[i].volume_fraction;
+    }
+    std::memcpy(design, r.design.data(), r.design.size() * sizeof(double));
+    std::memcpy(phys, r.physical_density.data(), r.physical_density.size() * sizeof(double));
+    out_scalars[0] = r.compliance;
+    out_scalars[1] = r.volume_fraction;
+    out_scalars[2] = r.initial_compliance;
+    out_ints[0] = r.iterations;
+    out_ints[1] = r.converged ? 1 : 0;
+    out_ints[2] = r.non_convergent ? 1 : 0;
+    out_ints[3] = r.infeasible ? 1 : 0;
+  });
+}
+
+int ref_effective_design_mask(int nx, int ny, int nz, const uint8_t* tags, const uint8_t* mask,
+                              uint8_t* eff) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, 1.0, tags);
+    const DesignMask m = effective_design_mask(g, make_mask(g.voxel_count(), mask));
+    for (std::size_t e = 0; e < m.size(); ++e) eff[e] = static_cast<uint8_t>(m[e]);
+  });
+}
+
+// make_density_filter(grid, radius, mask) with raw tags and a caller mask.
+int ref_filter_masked(int nx, int ny, int nz, const uint8_t* tags, const uint8_t* mask,
+                      double radius, int adjoint, const double* x, double* out) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, 1.0, tags);
+    const DensityFilter f = make_density_filter(g, radius, make_mask(g.voxel_count(), mask));
+    std::vector<double> xv(x, x + g.voxel_count());
+    const std::vector<double> o = adjoint ? f.filter_sensitivity(xv) : f.filter_density(xv);
+    std::memcpy(out, o.data(), o.size() * sizeof(double));
+  });
+}
+
+// The masked simp_optimize overload (OC, no projection, MultigridCG_Matfree).
+int ref_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tags,
+                             const uint8_t* mask, double E0, double nu, double penal,
+                             double rho_min, int nbc, const int* bc_node, const int* bc_comp,
+                             const double* bc_val, int nload, const int* ld_node,
+                             const int* ld_comp, const double* ld_val, double volfrac,
+                             double radius, double move, int max_it, double change_tol,
+                             double cg_tol, int cg_max_it, double* hist_c, double* hist_change,
+                             double* hist_vf, double* design, double* phys,
+                             double* out_scalars, int* out_ints) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, h, tags);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    SimpOptions o;
+    o.volume_fraction = volfrac;
+    o.filter_radius = radius;
+    o.move = move;
+    o.max_iterations = max_it;
+    o.change_tol = change_tol;
+    o.cg_tolerance = cg_tol;
+    o.cg_max_iterations = cg_max_it;
+    o.solver = SolverKind::MultigridCG_Matfree;
+    const SimpOptimizeResult r =
+        simp_optimize(g, p, make_bcs(nbc, bc_node, bc_comp, bc_val),
+                      make_loads(nload, ld_node, ld_comp, ld_val), o,
+                      make_mask(g.voxel_count(), mask));
     for (std::size_t i = 0; i < r.history.size(); ++i) {
       hist_c[i] = r.history[i].compliance;
       hist_change[i] = r.history[i].change;

@@ -590,19 +590,21 @@ void or_filter_sensitivity(const or_filter* f, const double* s, double* out) {
 /* ------------------------------------------------------------------- OC */
 typedef struct {
   int nx, ny, nz;
-  const uint8_t* solid;
+  const uint8_t* solid; /* the design set: solid voxels, or Active voxels (masked) */
   const or_filter* f;
   const double *x, *dc, *dv;
   double move, rho_min;
   double *xnew, *xp;
+  int masked; /* oc_update_masked: carry frozen x, sum the whole filtered field */
 } oc_ctx;
 
-/* candidate(lambda) of simp.cpp:980-1000. */
+/* candidate(lambda) of simp.cpp:980-1000; the masked form (simp.cpp:2684-2701)
+ * starts from a copy of the design, so frozen entries keep their pinned x. */
 static void oc_candidate(oc_ctx* c, double lambda) {
   const size_t nv = (size_t)c->nx * c->ny * c->nz;
 #pragma omp parallel for schedule(static)
   for (size_t e = 0; e < nv; ++e) {
-    c->xnew[e] = 0.0;
+    c->xnew[e] = c->masked ? c->x[e] : 0.0;
     if (!is_solid(c->solid, e)) continue;
     const double xe = c->x[e];
     double be = 0.0;
@@ -618,19 +620,21 @@ static void oc_candidate(oc_ctx* c, double lambda) {
 }
 
 /* phys_vol of simp.cpp:1003-1011: sequential FP64 sum of the filtered candidate
- * over solid voxels in grid order. */
+ * over solid voxels in grid order; the masked form (simp.cpp:2705-2710) sums the
+ * whole filtered field (zero off the Active set). */
 static double oc_phys_vol(oc_ctx* c) {
   or_filter_density(c->f, c->xnew, c->xp);
   const size_t nv = (size_t)c->nx * c->ny * c->nz;
   double v = 0.0;
   for (size_t e = 0; e < nv; ++e)
-    if (is_solid(c->solid, e)) v += c->xp[e];
+    if (c->masked || is_solid(c->solid, e)) v += c->xp[e];
   return v;
 }
 
-int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* f,
-                 const double* density, const double* dc, double volfrac, double move,
-                 double rho_min, double* x_new, double* lambda_out, int* nvol_out) {
+static int oc_update_common(int nx, int ny, int nz, const uint8_t* design, int masked,
+                            const or_filter* f, const double* density, const double* dc,
+                            double volfrac, double move, double rho_min, double* x_new,
+                            double* lambda_out, int* nvol_out) {
   if (!(volfrac > 0.0 && volfrac <= 1.0))
     return fail(OR_EINVAL, "oc_update: volume_fraction must be in (0, 1]");
   if (!(move > 0.0)) return fail(OR_EINVAL, "oc_update: move must be > 0");
@@ -644,13 +648,13 @@ int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* 
   size_t n_design = 0;
   or_filter_sensitivity(f, dc, dcf);
   for (size_t e = 0; e < nv; ++e)
-    if (is_solid(solid, e)) {
+    if (is_solid(design, e)) {
       ones[e] = 1.0;
       ++n_design;
     }
   or_filter_sensitivity(f, ones, dv);
   const double target = volfrac * (double)n_design;
-  oc_ctx c = {nx, ny, nz, solid, f, density, dcf, dv, move, rho_min, x_new, xp};
+  oc_ctx c = {nx, ny, nz, design, f, density, dcf, dv, move, rho_min, x_new, xp, masked};
   double l1 = 0.0, l2 = 1.0;
   int nvol = 0;
   for (;;) {
@@ -675,6 +679,38 @@ int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* 
   if (nvol_out) *nvol_out = nvol;
   free(dcf); free(ones); free(dv); free(xp);
   return OR_OK;
+}
+
+int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* f,
+                 const double* density, const double* dc, double volfrac, double move,
+                 double rho_min, double* x_new, double* lambda_out, int* nvol_out) {
+  return oc_update_common(nx, ny, nz, solid, 0, f, density, dc, volfrac, move, rho_min, x_new,
+                          lambda_out, nvol_out);
+}
+
+/* effective_design_mask (simp.cpp:2610-2633): Empty -> FrozenVoid, Load and
+ * Fixture -> FrozenSolid, everything else keeps the caller's entry. */
+void or_effective_design_mask(int nx, int ny, int nz, const uint8_t* tags, const uint8_t* mask,
+                              uint8_t* eff) {
+  const size_t nv = (size_t)nx * ny * nz;
+  for (size_t e = 0; e < nv; ++e) {
+    const uint8_t t = tags ? tags[e] : 1;
+    eff[e] = mask[e];
+    if (t == 0) eff[e] = OR_FROZEN_VOID;
+    else if (t == 4 || t == 5) eff[e] = OR_FROZEN_SOLID;
+  }
+}
+
+int or_oc_update_masked(int nx, int ny, int nz, const uint8_t* eff, const or_filter* f,
+                        const double* density, const double* dc, double volfrac, double move,
+                        double rho_min, double* x_new, double* lambda_out, int* nvol_out) {
+  const size_t nv = (size_t)nx * ny * nz;
+  uint8_t* design = malloc(nv);
+  for (size_t e = 0; e < nv; ++e) design[e] = eff[e] == OR_ACTIVE;
+  const int st = oc_update_common(nx, ny, nz, design, 1, f, density, dc, volfrac, move, rho_min,
+                                  x_new, lambda_out, nvol_out);
+  free(design);
+  return st;
 }
 
 /* ---------------------------------------------------------- simp loop */
@@ -702,39 +738,80 @@ static int rung_infeasible(const double* c, const int* cg, int n) {
   return (hi - lo) / lo <= flat_tol;
 }
 
-int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
-                     double nu, double penal, double rho_min, int nbc, const int* bc_node,
-                     const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
-                     const int* ld_comp, const double* ld_val, const or_simp_options* o,
-                     double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
-                     double* design, double* phys, or_simp_result* res) {
+/* apply_mask_pins (simp.cpp:2648-2654): FrozenSolid -> 1, FrozenVoid -> 0. */
+static void mask_pins(const uint8_t* eff, size_t nv, double* xphys) {
+  for (size_t e = 0; e < nv; ++e) {
+    if (eff[e] == OR_FROZEN_SOLID) xphys[e] = 1.0;
+    else if (eff[e] == OR_FROZEN_VOID) xphys[e] = 0.0;
+  }
+}
+
+/* The plain loop (simp.cpp:2018-2592) when mask is NULL; the masked overload
+ * (simp.cpp:2989-3640) otherwise: the effective mask, the Active-only filter,
+ * the analysis grid without FrozenVoid voxels, pins after every filter pass and
+ * the Active budget. */
+static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
+                       const uint8_t* mask, double E0, double nu, double penal, double rho_min,
+                       int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                       int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                       const or_simp_options* o, double* hist_c, double* hist_change,
+                       double* hist_vf, int* hist_cg, double* design, double* phys,
+                       or_simp_result* res) {
   memset(res, 0, sizeof *res);
   if (!(o->volume_fraction > 0.0 && o->volume_fraction <= 1.0))
     return fail(OR_EINVAL, "simp_optimize: volume_fraction must be in (0, 1]");
   if (!(o->move > 0.0)) return fail(OR_EINVAL, "simp_optimize: move must be > 0");
   if (o->max_iterations < 1)
     return fail(OR_EINVAL, "simp_optimize: max_iterations must be >= 1");
-  or_filter* f = or_filter_make(nx, ny, nz, solid, NULL, o->filter_radius);
-  if (!f) return OR_EINVAL;
   const size_t nv = (size_t)nx * ny * nz;
   const size_t ndof = 3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  uint8_t* eff = NULL;        /* effective mask (masked loop only) */
+  uint8_t* active = NULL;     /* Active voxels: the filter's and OC's design set */
+  uint8_t* analysis = NULL;   /* solid voxels of the analysis grid */
+  const uint8_t* asolid = solid;
+  if (mask) {
+    eff = malloc(nv);
+    active = malloc(nv);
+    analysis = malloc(nv);
+    or_effective_design_mask(nx, ny, nz, solid, mask, eff);
+    for (size_t e = 0; e < nv; ++e) {
+      active[e] = eff[e] == OR_ACTIVE;
+      analysis[e] = is_solid(solid, e) && eff[e] != OR_FROZEN_VOID;
+    }
+    asolid = analysis;
+  }
+  or_filter* f = or_filter_make(nx, ny, nz, solid, active, o->filter_radius);
+  if (!f) {
+    free(eff); free(active); free(analysis);
+    return OR_EINVAL;
+  }
   double n_design = 0.0;
   double* x = calloc(nv, sizeof(double));
   double* xphys = malloc(nv * sizeof(double));
   double* xnew = malloc(nv * sizeof(double));
   double* dc = malloc(nv * sizeof(double));
   double* u = malloc(ndof * sizeof(double));
-  for (size_t e = 0; e < nv; ++e)
-    if (is_solid(solid, e)) {
+  for (size_t e = 0; e < nv; ++e) {
+    if (mask) {
+      /* simp.cpp:3066-3072: Active at the target, FrozenSolid at 1, else 0. */
+      if (eff[e] == OR_ACTIVE) {
+        x[e] = o->volume_fraction;
+        n_design += 1.0;
+      } else if (eff[e] == OR_FROZEN_SOLID) {
+        x[e] = 1.0;
+      }
+    } else if (is_solid(solid, e)) {
       x[e] = o->volume_fraction; /* simp_uniform_density (simp.cpp:305-312) */
       n_design += 1.0;
     }
+  }
   int st = OR_OK;
   for (int it = 0; it < o->max_iterations; ++it) {
     or_filter_density(f, x, xphys);
+    if (mask) mask_pins(eff, nv, xphys);
     double c = 0.0, resid = 0.0;
     int cgit = 0;
-    st = or_simp_compliance(nx, ny, nz, h, solid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
+    st = or_simp_compliance(nx, ny, nz, h, asolid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
                             bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
                             o->cg_max_iterations, u, dc, &c, &cgit, &resid);
     if (st == OR_ENONCONV) {
@@ -743,8 +820,10 @@ int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, dou
       break;
     }
     if (st) goto out;
-    st = or_oc_update(nx, ny, nz, solid, f, x, dc, o->volume_fraction, o->move, rho_min, xnew,
-                      NULL, NULL);
+    st = mask ? or_oc_update_masked(nx, ny, nz, eff, f, x, dc, o->volume_fraction, o->move,
+                                    rho_min, xnew, NULL, NULL)
+              : or_oc_update(nx, ny, nz, solid, f, x, dc, o->volume_fraction, o->move, rho_min,
+                             xnew, NULL, NULL);
     if (st) goto out;
     double change = 0.0;
     for (size_t e = 0; e < nv; ++e) change = fmax(change, fabs(xnew[e] - x[e]));
@@ -769,12 +848,15 @@ int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, dou
   }
   memcpy(design, x, nv * sizeof(double));
   or_filter_density(f, x, phys);
+  double vol_final = 0.0; /* of the unpinned field (simp.cpp:3614, :3652) */
+  for (size_t e = 0; e < nv; ++e) vol_final += phys[e];
+  if (mask) mask_pins(eff, nv, phys);
   if (res->infeasible || res->non_convergent) {
     res->compliance = res->iterations ? hist_c[res->iterations - 1] : 0.0;
   } else {
     double resid = 0.0;
     int cgit = 0;
-    st = or_simp_compliance(nx, ny, nz, h, solid, E0, nu, penal, rho_min, phys, nbc, bc_node,
+    st = or_simp_compliance(nx, ny, nz, h, asolid, E0, nu, penal, rho_min, phys, nbc, bc_node,
                             bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
                             o->cg_max_iterations, u, dc, &res->compliance, &cgit, &resid);
     if (st == OR_ENONCONV) {
@@ -784,13 +866,34 @@ int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, dou
       st = OR_OK;
     }
   }
-  {
-    double vol = 0.0;
-    for (size_t e = 0; e < nv; ++e) vol += phys[e];
-    res->volume_fraction = n_design > 0.0 ? vol / n_design : 0.0;
-  }
+  res->volume_fraction = n_design > 0.0 ? vol_final / n_design : 0.0;
 out:
   free(x); free(xphys); free(xnew); free(dc); free(u);
+  free(eff); free(active); free(analysis);
   or_filter_free(f);
   return st;
+}
+
+int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                     double nu, double penal, double rho_min, int nbc, const int* bc_node,
+                     const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+                     const int* ld_comp, const double* ld_val, const or_simp_options* o,
+                     double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
+                     double* design, double* phys, or_simp_result* res) {
+  return simp_common(nx, ny, nz, h, solid, NULL, E0, nu, penal, rho_min, nbc, bc_node, bc_comp,
+                     bc_val, nload, ld_node, ld_comp, ld_val, o, hist_c, hist_change, hist_vf,
+                     hist_cg, design, phys, res);
+}
+
+int or_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tags,
+                            const uint8_t* mask, double E0, double nu, double penal,
+                            double rho_min, int nbc, const int* bc_node, const int* bc_comp,
+                            const double* bc_val, int nload, const int* ld_node,
+                            const int* ld_comp, const double* ld_val, const or_simp_options* o,
+                            double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
+                            double* design, double* phys, or_simp_result* res) {
+  if (!mask) return fail(OR_EINVAL, "simp_optimize: mask size != voxel_count");
+  return simp_common(nx, ny, nz, h, tags, mask, E0, nu, penal, rho_min, nbc, bc_node, bc_comp,
+                     bc_val, nload, ld_node, ld_comp, ld_val, o, hist_c, hist_change, hist_vf,
+                     hist_cg, design, phys, res);
 }

@@ -105,6 +105,19 @@ int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* 
                  double move, double rho_min, double* x_new,
                  double* lambda_out, int* nvol_out);
 
+/* MaskValue (core/include/topopt/voxel.hpp:42-46). */
+enum { OR_ACTIVE = 0, OR_FROZEN_SOLID = 1, OR_FROZEN_VOID = 2 };
+
+/* effective_design_mask (simp.cpp:2610-2633).  tags NULL = all Interior. */
+void or_effective_design_mask(int nx, int ny, int nz, const uint8_t* tags, const uint8_t* mask,
+                              uint8_t* eff);
+
+/* oc_update_masked (simp.cpp:2662-2720): eff is an effective mask and f the
+ * Active-only filter (or_filter_make with active = eff == Active). */
+int or_oc_update_masked(int nx, int ny, int nz, const uint8_t* eff, const or_filter* f,
+                        const double* density, const double* dc, double volfrac, double move,
+                        double rho_min, double* x_new, double* lambda_out, int* nvol_out);
+
 /* Plain simp_optimize with the OC updater and no projection (simp.cpp:2018-2592).
  * The solve is the exact Jacobi-PCG above.  hist_* have room for max_it rows.
  * Guards: change_tol stop; rung-infeasibility window (simp.cpp:1140-1186) with
@@ -124,6 +137,17 @@ int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid,
                      const or_simp_options* opt, double* hist_c, double* hist_change,
                      double* hist_vf, int* hist_cg, double* design, double* phys,
                      or_simp_result* res);
+
+/* The masked simp_optimize overload (simp.cpp:2989-3640), OC, no projection:
+ * tags are the voxel tags (0 Empty, 4 Load, 5 Fixture ...), mask the caller's
+ * MaskValue per voxel.  phys receives the pinned physical density. */
+int or_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tags,
+                            const uint8_t* mask, double E0, double nu, double penal,
+                            double rho_min, int nbc, const int* bc_node, const int* bc_comp,
+                            const double* bc_val, int nload, const int* ld_node,
+                            const int* ld_comp, const double* ld_val, const or_simp_options* o,
+                            double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
+                            double* design, double* phys, or_simp_result* res);
 
 #ifdef __cplusplus
 }

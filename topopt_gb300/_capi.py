@@ -59,8 +59,7 @@ class _Params(C.Structure):
 class _SolveOpt(C.Structure):
     _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("mg_levels", C.c_int32),
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
-                ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
-                ("coarse_fp16", C.c_int32)]
+                ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -227,12 +226,10 @@ class SolveOptions:
     omega: float = 0.0
     inner_tolerance: float = 0.0
     max_refinements: int = 0
-    coarse_fp16: int = 0
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
-                         self.omega, self.inner_tolerance, self.max_refinements,
-                         self.coarse_fp16)
+                         self.omega, self.inner_tolerance, self.max_refinements)
 
 
 @dataclass

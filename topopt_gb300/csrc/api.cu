@@ -815,11 +815,11 @@ int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* option
   const double ndof = 3.0 * (grid->nx + 1.0) * (grid->ny + 1.0) * (grid->nz + 1.0);
   const bool mixed = options && options->solve.precision == TG_PREC_MIXED;
   // Fine: 9 FP64 DOF vectors + kept/f/up; ~12 voxel arrays.  Hierarchy: the
-  // level-1 element matrices (576 doubles per 8 voxels) and stencils (243
+  // level-1 element matrices (576 doubles per 8 voxels) and stencils (126
   // doubles per node / 8), a geometric series over the coarser levels.
   double b = ndof * (9 * 8 + 1 + 16) + nv * (12 * 8 + 2);
-  b += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 243 * 8 * 8.0 / 7.0;
-  if (mixed) b += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 243 * 4 * 8.0 / 7.0 + nv * 4;
+  b += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 126 * 8 * 8.0 / 7.0;
+  if (mixed) b += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 126 * 4 * 8.0 / 7.0 + nv * 4;
   return int64_t(b * 1.05) + (64 << 20);
 }
 

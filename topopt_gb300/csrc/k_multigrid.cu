@@ -18,10 +18,12 @@
 // coincident fine node lies beyond the grid is inactive, which reproduces the
 // reference's index-space padding (multigrid.cpp:391-459).
 //
-// Coarse levels are applied as assembled 27-point node stencils stored as
-// structure of arrays A[243][nnodes] (block (d, c1, c2) for neighbour offset d),
-// so a thread per node reads coalesced rows.
-#include <cuda_fp16.h>
+// Coarse levels are applied as assembled 27-point node stencils.  The operator
+// is symmetric, so only the self block and the 13 "forward" neighbour blocks
+// (positive linear offset) are stored, as structure of arrays A[126][nnodes]
+// (entry (j*3 + c1)*3 + c2 for block j): a thread per node reads its own rows
+// coalesced and the backward blocks, transposed, from the neighbour's rows.
+// Half the bytes of the full 243-entry stencil, the bound of the coarse apply.
 #include <cuda_runtime.h>
 
 #include "tg_internal.h"
@@ -179,8 +181,9 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
   }
 }
 
-// Node stencil from the element matrices around each node.  Entry index
-// q = (d*3 + c1)*3 + c2, d = (dz+1)*9 + (dy+1)*3 + (dx+1).
+// Node stencil from the element matrices around each node: the self block and
+// the forward blocks only.  Entry index q = (j*3 + c1)*3 + c2 with
+// j = d - 13, d = (dz+1)*9 + (dy+1)*3 + (dx+1) >= 13.
 template <class T>
 __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
                                    const uint8_t* __restrict__ act, T* __restrict__ A,
@@ -195,6 +198,8 @@ __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
       for (int dy = -1; dy <= 1; ++dy)
         for (int dx = -1; dx <= 1; ++dx) {
           const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
+          if (di < 13) continue;  // backward blocks: the neighbour's forward block, transposed
+          const int j = di - 13;
           T blk[9];
 #pragma unroll
           for (int k = 0; k < 9; ++k) blk[k] = T(0);
@@ -225,8 +230,8 @@ __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
           for (int c1 = 0; c1 < 3; ++c1)
 #pragma unroll
             for (int c2 = 0; c2 < 3; ++c2)
-              A[int64_t(di * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : T(0);
-          if (di == 13)
+              A[int64_t(j * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : T(0);
+          if (j == 0)
             for (int k = 0; k < 3; ++k) {
               const T dg = blk[k * 3 + k];
               invdiag[3 * n + k] = (ra[k] && dg > T(0)) ? T(1) / dg : T(0);
@@ -243,137 +248,70 @@ __global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int6
 }
 
 // Stencil operator: y = A x / b - A x / x + w D^-1 (b - A x), masked by act.
-// Three warps per 32 nodes: a warp owns one output component c1 of 32
-// consecutive nodes, so its reads of A (entry (d, c1, c2) of 32 nodes) are
-// contiguous, and each thread's chain is 27 x 3 multiply-adds with all loads
-// independent (the neighbour loop is unrolled, out-of-grid neighbours predicated).
-constexpr int kStencilNodes = 64;  // nodes per CTA; blockDim = 3 * kStencilNodes
+// A thread per node and all three output components.  Forward block j of node n
+// couples n to n + off_j; the backward coupling of n to n - off_j is the forward
+// block j of node n - off_j, transposed.  All 13 block pairs are unrolled so the
+// loads are independent; out-of-grid neighbours are predicated (the stored
+// forward block of a node whose neighbour lies outside the grid is zero, and the
+// backward term is selected away).
 template <class T, int MODE>
-__global__ void __launch_bounds__(3 * kStencilNodes, 3) k_stencil_op(MgDims d, const T* __restrict__ A,
-                                                                  const uint8_t* __restrict__ act,
-                                                                  const T* __restrict__ x,
-                                                                  const T* __restrict__ b,
-                                                                  const T* __restrict__ invdiag,
-                                                                  T omega, T* __restrict__ y) {
+__global__ void __launch_bounds__(kThreads) k_stencil_op(MgDims d, const T* __restrict__ A,
+                                                         const uint8_t* __restrict__ act,
+                                                         const T* __restrict__ x,
+                                                         const T* __restrict__ b,
+                                                         const T* __restrict__ invdiag, T omega,
+                                                         T* __restrict__ y) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  const int c1 = threadIdx.x / kStencilNodes;
-  for (int64_t n = blockIdx.x * int64_t(kStencilNodes) + threadIdx.x % kStencilNodes; n < nn;
-       n += int64_t(gridDim.x) * kStencilNodes) {
-    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny),
-              c = int(n / (int64_t(d.nnx) * d.nny));
-    T acc = T(0);
-#pragma unroll 9
-    for (int di = 0; di < 27; ++di) {
-      const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
-      const bool in = (a + dx) >= 0 && (a + dx) < d.nnx && (bb + dy) >= 0 && (bb + dy) < d.nny &&
-                      (c + dz) >= 0 && (c + dz) < d.nnz;
-      const int64_t m = in ? n + (int64_t(dz) * d.nny + dy) * d.nnx + dx : n;
-      const T* Ab = A + int64_t(di * 9 + c1 * 3) * nn + n;
-      const T a0 = Ab[0], a1 = Ab[nn], a2 = Ab[2 * nn];
-      const T x0 = x[3 * m], x1 = x[3 * m + 1], x2 = x[3 * m + 2];
-      const T t = a0 * x0 + a1 * x1 + a2 * x2;
-      acc += in ? t : T(0);
-    }
-    const int64_t dof = 3 * n + c1;
-    T out;
-    if (!act[dof]) {
-      out = T(0);
-    } else if (MODE == kApply) {
-      out = acc;
-    } else if (MODE == kResidual) {
-      out = b[dof] - acc;
-    } else {
-      out = x[dof] + omega * invdiag[dof] * (b[dof] - acc);
-    }
-    y[dof] = out;
-  }
-}
-
-// Diagonally scaled FP16 copy of an FP32 stencil: Ah = S A S with
-// S = diag(1/sqrt(diag A)), so every entry lies in [-1, 1] (A is SPD) and the
-// diagonal is 1 -- the range FP16 represents best.  sc receives S.
-__global__ void k_scale_vector(const float* __restrict__ invd, int64_t n, float* __restrict__ sc) {
-  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * kThreads)
-    sc[i] = sqrtf(invd[i]);
-}
-
-__global__ void k_normalize_stencil(MgDims d, const float* __restrict__ A,
-                                    const float* __restrict__ sc, __half* __restrict__ Ah) {
-  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  const int64_t sy = d.nnx, sz = int64_t(d.nnx) * d.nny;
   for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
        n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
-    for (int di = 0; di < 27; ++di) {
+    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny), c = int(n / sz);
+    const T* An = A + n;
+    const T xs0 = x[3 * n], xs1 = x[3 * n + 1], xs2 = x[3 * n + 2];
+    T s0 = An[0] * xs0 + An[nn] * xs1 + An[2 * nn] * xs2;
+    T s1 = An[3 * nn] * xs0 + An[4 * nn] * xs1 + An[5 * nn] * xs2;
+    T s2 = An[6 * nn] * xs0 + An[7 * nn] * xs1 + An[8 * nn] * xs2;
+#pragma unroll
+    for (int j = 1; j < 14; ++j) {
+      const int di = 13 + j;
       const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
-      const int i = a + dx, j = bb + dy, k = c + dz;
-      const bool in = i >= 0 && i < d.nnx && j >= 0 && j < d.nny && k >= 0 && k < d.nnz;
-      const int64_t m = in ? (int64_t(k) * d.nny + j) * d.nnx + i : n;
-#pragma unroll
-      for (int c1 = 0; c1 < 3; ++c1)
-#pragma unroll
-        for (int c2 = 0; c2 < 3; ++c2) {
-          const int64_t q = int64_t(di * 9 + c1 * 3 + c2) * nn + n;
-          const float v = in ? sc[3 * n + c1] * A[q] * sc[3 * m + c2] : 0.0f;
-          Ah[q] = __float2half_rn(v);
-        }
+      const int64_t off = dz * sz + dy * sy + dx;
+      const bool fin = (a + dx) < d.nnx && (a + dx) >= 0 && (bb + dy) < d.nny && (bb + dy) >= 0 &&
+                       (c + dz) < d.nnz;
+      const bool bin = (a - dx) >= 0 && (a - dx) < d.nnx && (bb - dy) >= 0 && (bb - dy) < d.nny &&
+                       (c - dz) >= 0;
+      const int64_t m = fin ? n + off : n;
+      const int64_t p = bin ? n - off : n;
+      const T* Af = An + int64_t(j * 9) * nn;
+      const T* Ab = A + int64_t(j * 9) * nn + p;
+      const T f0 = x[3 * m], f1 = x[3 * m + 1], f2 = x[3 * m + 2];
+      const T g0 = x[3 * p], g1 = x[3 * p + 1], g2 = x[3 * p + 2];
+      const T u0 = Af[0] * f0 + Af[nn] * f1 + Af[2 * nn] * f2;
+      const T u1 = Af[3 * nn] * f0 + Af[4 * nn] * f1 + Af[5 * nn] * f2;
+      const T u2 = Af[6 * nn] * f0 + Af[7 * nn] * f1 + Af[8 * nn] * f2;
+      const T v0 = Ab[0] * g0 + Ab[3 * nn] * g1 + Ab[6 * nn] * g2;
+      const T v1 = Ab[nn] * g0 + Ab[4 * nn] * g1 + Ab[7 * nn] * g2;
+      const T v2 = Ab[2 * nn] * g0 + Ab[5 * nn] * g1 + Ab[8 * nn] * g2;
+      s0 += fin ? u0 : T(0);
+      s1 += fin ? u1 : T(0);
+      s2 += fin ? u2 : T(0);
+      s0 += bin ? v0 : T(0);
+      s1 += bin ? v1 : T(0);
+      s2 += bin ? v2 : T(0);
     }
-  }
-}
-
-// Stencil operator on the scaled FP16 copy: (A x)_n = s_n * sum_m Ah_nm (s_m x_m),
-// FP32 arithmetic; same modes and masking as k_stencil_op.
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_stencil_op_h(MgDims d, const __half* __restrict__ A,
-                                                           const float* __restrict__ sc,
-                                                           const uint8_t* __restrict__ act,
-                                                           const float* __restrict__ x,
-                                                           const float* __restrict__ b,
-                                                           const float* __restrict__ invdiag,
-                                                           float omega, float* __restrict__ y) {
-  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
-       n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny),
-              c = int(n / (int64_t(d.nnx) * d.nny));
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    for (int dz = -1; dz <= 1; ++dz) {
-      const int k = c + dz;
-      if (k < 0 || k >= d.nnz) continue;
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int j = bb + dy;
-        if (j < 0 || j >= d.nny) continue;
-#pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int i = a + dx;
-          if (i < 0 || i >= d.nnx) continue;
-          const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
-          const int64_t m = (int64_t(k) * d.nny + j) * d.nnx + i;
-          const float x0 = sc[3 * m] * x[3 * m], x1 = sc[3 * m + 1] * x[3 * m + 1],
-                      x2 = sc[3 * m + 2] * x[3 * m + 2];
-          const __half* Ab = A + int64_t(di * 9) * nn + n;
-          s0 += __half2float(Ab[0]) * x0 + __half2float(Ab[nn]) * x1 + __half2float(Ab[2 * nn]) * x2;
-          s1 += __half2float(Ab[3 * nn]) * x0 + __half2float(Ab[4 * nn]) * x1 +
-                __half2float(Ab[5 * nn]) * x2;
-          s2 += __half2float(Ab[6 * nn]) * x0 + __half2float(Ab[7 * nn]) * x1 +
-                __half2float(Ab[8 * nn]) * x2;
-        }
-      }
-    }
-    const float sv[3] = {s0, s1, s2};
+    const T sv[3] = {s0, s1, s2};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int64_t dof = 3 * n + k;
-      const float ax = sc[dof] * sv[k];
-      float out;
+      T out;
       if (!act[dof]) {
-        out = 0.f;
+        out = T(0);
       } else if (MODE == kApply) {
-        out = ax;
+        out = sv[k];
       } else if (MODE == kResidual) {
-        out = b[dof] - ax;
+        out = b[dof] - sv[k];
       } else {
-        out = x[dof] + omega * invdiag[dof] * (b[dof] - ax);
+        out = x[dof] + omega * invdiag[dof] * (b[dof] - sv[k]);
       }
       y[dof] = out;
     }
@@ -459,8 +397,9 @@ __global__ void k_prolong_add(MgDims fd, MgDims cd, const T* __restrict__ ec,
 }
 
 // ---------------------------------------------------------- coarsest solve
-// Dense lower-triangular A (row-major, nc x nc) from the coarsest stencil over
-// the compact numbering cidx (-1 = inactive).
+// Dense A (row-major, nc x nc) from the coarsest stencil over the compact
+// numbering cidx (-1 = inactive): node n writes its self block and, for every
+// forward block, the entry and its transpose -- each entry exactly once.
 template <class T>
 __global__ void k_dense_from_stencil(MgDims d, const T* __restrict__ A,
                                      const int* __restrict__ cidx, int nc,
@@ -469,22 +408,22 @@ __global__ void k_dense_from_stencil(MgDims d, const T* __restrict__ A,
   for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
        n += int64_t(gridDim.x) * kThreads) {
     const int a = int(n % d.nnx), b = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
-    for (int c1 = 0; c1 < 3; ++c1) {
-      const int row = cidx[3 * n + c1];
-      if (row < 0) continue;
-      for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-          for (int dx = -1; dx <= 1; ++dx) {
-            const int i = a + dx, j = b + dy, k = c + dz;
-            if (i < 0 || i >= d.nnx || j < 0 || j >= d.nny || k < 0 || k >= d.nnz) continue;
-            const int64_t m = (int64_t(k) * d.nny + j) * d.nnx + i;
-            const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
-            for (int c2 = 0; c2 < 3; ++c2) {
-              const int col = cidx[3 * m + c2];
-              if (col < 0) continue;
-              D[int64_t(row) * nc + col] = double(A[int64_t(di * 9 + c1 * 3 + c2) * nn + n]);
-            }
-          }
+    for (int j = 0; j < 14; ++j) {
+      const int di = 13 + j;
+      const int i = a + di % 3 - 1, jj = b + (di / 3) % 3 - 1, k = c + di / 9 - 1;
+      if (i < 0 || i >= d.nnx || jj < 0 || jj >= d.nny || k >= d.nnz) continue;
+      const int64_t m = (int64_t(k) * d.nny + jj) * d.nnx + i;
+      for (int c1 = 0; c1 < 3; ++c1) {
+        const int row = cidx[3 * n + c1];
+        if (row < 0) continue;
+        for (int c2 = 0; c2 < 3; ++c2) {
+          const int col = cidx[3 * m + c2];
+          if (col < 0) continue;
+          const double v = double(A[int64_t(j * 9 + c1 * 3 + c2) * nn + n]);
+          D[int64_t(row) * nc + col] = v;
+          if (j > 0) D[int64_t(col) * nc + row] = v;
+        }
+      }
     }
   }
 }
@@ -668,38 +607,13 @@ template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  const int nb = nblk(nn, kStencilNodes);
-  const int nt = 3 * kStencilNodes;
-  if (mode == kApply)
-    k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
-  else if (mode == kResidual)
-    k_stencil_op<T, kResidual><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
-  else
-    k_stencil_op<T, kSmooth><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
-  TG_LAUNCH_CHECK();
-}
-
-void mg_normalize_stencil(const MgDims& d, const float* A, const float* invd, float* sc,
-                          void* Ah, cudaStream_t s) {
-  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  k_scale_vector<<<nblk(3 * nn), kThreads, 0, s>>>(invd, 3 * nn, sc);
-  TG_LAUNCH_CHECK();
-  k_normalize_stencil<<<nblk(nn), kThreads, 0, s>>>(d, A, sc, static_cast<__half*>(Ah));
-  TG_LAUNCH_CHECK();
-}
-
-void mg_stencil_op_h(int mode, const MgDims& d, const void* Ah, const float* sc,
-                     const uint8_t* act, const float* x, const float* b, const float* invdiag,
-                     float omega, float* y, cudaStream_t s) {
-  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   const int nb = nblk(nn);
-  const __half* A = static_cast<const __half*>(Ah);
   if (mode == kApply)
-    k_stencil_op_h<kApply><<<nb, kThreads, 0, s>>>(d, A, sc, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kApply><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else if (mode == kResidual)
-    k_stencil_op_h<kResidual><<<nb, kThreads, 0, s>>>(d, A, sc, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kResidual><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else
-    k_stencil_op_h<kSmooth><<<nb, kThreads, 0, s>>>(d, A, sc, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kSmooth><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   TG_LAUNCH_CHECK();
 }
 

@@ -59,6 +59,25 @@ ModalT<T> to_modal(const ModalConsts& c) {
   return m;
 }
 
+// Two FP32 lanes per thread: Blackwell's packed FP32x2 instructions
+// (FADD2 / FMUL2 / FFMA2) evaluate two elements per instruction.
+struct F2 {
+  float2 v;
+  F2() = default;
+  __device__ __forceinline__ explicit F2(float s) : v(make_float2(s, s)) {}
+  __device__ __forceinline__ F2(float2 x) : v(x) {}
+};
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
+  return F2(__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v));  // a - b, exact negation
+}
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2& operator+=(F2& a, F2 b) { return a = a + b; }
+// a * b + c
+__device__ __forceinline__ F2 mad(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
+__device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+
 // Forward Walsh transform of one component: v[idx], idx = sx | sy<<1 | sz<<2
 // with s = 1 on the + side, becomes the unnormalised mode coefficients
 // 8*m[mask], mask bit i set when axis i is in the monomial.
@@ -104,9 +123,9 @@ __device__ __forceinline__ void modal_apply(const ModalT<T>& mc, T f, T (&ux)[8]
   // |T| = 0: the constant-gradient block.
   {
     const T Ltr = L0 * (ux[1] + uy[2] + uz[4]);
-    gx[1] = Ltr + M02 * ux[1];
-    gy[2] = Ltr + M02 * uy[2];
-    gz[4] = Ltr + M02 * uz[4];
+    gx[1] = mad(M02, ux[1], Ltr);
+    gy[2] = mad(M02, uy[2], Ltr);
+    gz[4] = mad(M02, uz[4], Ltr);
     const T txy = M0 * (uy[1] + ux[2]);
     const T txz = M0 * (uz[1] + ux[4]);
     const T tyz = M0 * (uz[2] + uy[4]);
@@ -119,31 +138,31 @@ __device__ __forceinline__ void modal_apply(const ModalT<T>& mc, T f, T (&ux)[8]
     const T Ltr = L1 * (uy[3] + uz[5]);  // T = {x}: rows y (mode 3), z (mode 5)
     const T t = M1 * (uz[3] + uy[5]);
     gx[3] = M1 * ux[3];
-    gy[3] = Ltr + M12 * uy[3];
+    gy[3] = mad(M12, uy[3], Ltr);
     gz[3] = t;
     gx[5] = M1 * ux[5];
     gy[5] = t;
-    gz[5] = Ltr + M12 * uz[5];
+    gz[5] = mad(M12, uz[5], Ltr);
   }
   {
     const T Ltr = L1 * (ux[3] + uz[6]);  // T = {y}: rows x (mode 3), z (mode 6)
     const T t = M1 * (uz[3] + ux[6]);
-    gx[3] += Ltr + M12 * ux[3];
-    gy[3] += M1 * uy[3];
-    gz[3] += t;
+    gx[3] = gx[3] + mad(M12, ux[3], Ltr);
+    gy[3] = mad(M1, uy[3], gy[3]);
+    gz[3] = gz[3] + t;
     gx[6] = t;
     gy[6] = M1 * uy[6];
-    gz[6] = Ltr + M12 * uz[6];
+    gz[6] = mad(M12, uz[6], Ltr);
   }
   {
     const T Ltr = L1 * (ux[5] + uy[6]);  // T = {z}: rows x (mode 5), y (mode 6)
     const T t = M1 * (uy[5] + ux[6]);
-    gx[5] += Ltr + M12 * ux[5];
-    gy[5] += t;
-    gz[5] += M1 * uz[5];
-    gx[6] += t;
-    gy[6] += Ltr + M12 * uy[6];
-    gz[6] += M1 * uz[6];
+    gx[5] = gx[5] + mad(M12, ux[5], Ltr);
+    gy[5] = gy[5] + t;
+    gz[5] = mad(M1, uz[5], gz[5]);
+    gx[6] = gx[6] + t;
+    gy[6] = gy[6] + mad(M12, uy[6], Ltr);
+    gz[6] = mad(M1, uz[6], gz[6]);
   }
   // |T| = 2: the trilinear mode.
   gx[7] = LM2 * ux[7];

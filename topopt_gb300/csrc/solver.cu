@@ -186,8 +186,7 @@ struct Solver::Level {
   // FP64 operators and vectors (plain form, and the FP64 retry of the mixed form).
   DBuf<double> Kel, A, invd, xa, xb, b;
   // FP32 operators and vectors (mixed form).
-  DBuf<float> Kelf, Af, invdf, fxa, fxb, fb, scf;
-  DBuf<uint16_t> Ah;  // FP16 scaled stencil (mixed form, levels above the coarsest)
+  DBuf<float> Kelf, Af, invdf, fxa, fxb, fb;
   double *x = nullptr, *r = nullptr;
   float *xf = nullptr, *rf = nullptr;
   template <class T>
@@ -207,14 +206,14 @@ struct Solver::Level {
   size_t bytes() const {
     return act.bytes() + Kel.bytes() + A.bytes() + invd.bytes() + xa.bytes() + xb.bytes() +
            b.bytes() + Kelf.bytes() + Af.bytes() + invdf.bytes() + fxa.bytes() + fxb.bytes() +
-           fb.bytes() + scf.bytes() + Ah.bytes();
+           fb.bytes();
   }
 };
 template <>
 void Solver::Level::ensure<double>() {
   if (Kel.p) return;
   Kel.alloc(size_t(nel) * 576);
-  A.alloc(size_t(nn) * 243);
+  A.alloc(size_t(nn) * kStencilEntries);
   for (DBuf<double>* v : {&invd, &xa, &xb, &b}) v->alloc(size_t(ndof));
   x = xa.p;
   r = xb.p;
@@ -223,7 +222,7 @@ template <>
 void Solver::Level::ensure<float>() {
   if (Kelf.p) return;
   Kelf.alloc(size_t(nel) * 576);
-  Af.alloc(size_t(nn) * 243);
+  Af.alloc(size_t(nn) * kStencilEntries);
   for (DBuf<float>* v : {&invdf, &fxa, &fxb, &fb}) v->alloc(size_t(ndof));
   xf = fxa.p;
   rf = fxb.p;
@@ -259,7 +258,6 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   omega_ = opt.omega > 0.0 ? opt.omega : 0.6;
   budget_ = opt.mg_iter_budget > 0 ? opt.mg_iter_budget : 300;
   mixed_ = opt.precision == TG_PREC_MIXED;
-  half_coarse_ = opt.coarse_fp16 > 0;
   const size_t n = size_t(fp.g.ndof);
   for (DBuf<double>* b : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_}) b->alloc(n);
   part_n_ = std::max({kRedBlocks, fine_op_blocks(fp.g, true), fine_op_blocks(fp.g, false),
@@ -522,14 +520,6 @@ bool Solver::build_numeric() {
     else
       mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
     mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, L.Am<T>(), L.Dinv<T>(), s_);
-    if (sizeof(T) == 4 && half_coarse_ && l + 1 < levels_.size()) {
-      if (!L.Ah.p) {
-        L.Ah.alloc(size_t(L.nn) * 243);
-        L.scf.alloc(size_t(L.ndof));
-      }
-      mg_normalize_stencil(L.d, reinterpret_cast<const float*>(L.Am<T>()),
-                           reinterpret_cast<const float*>(L.Dinv<T>()), L.scf.p, L.Ah.p, s_);
-    }
     pd = L.d;
   }
   Level& C = *levels_.back();
@@ -557,16 +547,9 @@ void Solver::vcycle_level(size_t l) {
   }
   Level& N = *levels_[l];
   const T w = T(omega_);
-  const bool half = sizeof(T) == 4 && L.Ah.p != nullptr;
   auto op = [&](int mode) {
-    if (half)
-      mg_stencil_op_h(mode, L.d, L.Ah.p, L.scf.p, L.act.p, reinterpret_cast<const float*>(L.X<T>()),
-                      reinterpret_cast<const float*>(L.B<T>()),
-                      reinterpret_cast<const float*>(L.Dinv<T>()), float(omega_),
-                      reinterpret_cast<float*>(L.R<T>()), s_);
-    else
-      mg_stencil_op<T>(mode, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
-                       L.R<T>(), s_);
+    mg_stencil_op<T>(mode, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w, L.R<T>(),
+                     s_);
   };
   mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);
   op(kResidual);

@@ -6,6 +6,10 @@
 
 namespace tg {
 
+// Entries per node of a stored coarse stencil: the self block and the 13 forward
+// neighbour blocks, 3x3 each (the backward blocks are their transposes).
+constexpr int kStencilEntries = 14 * 9;
+
 // Element and node extents of one hierarchy level.
 struct MgDims {
   int ex, ey, ez, nnx, nny, nnz;
@@ -24,12 +28,6 @@ void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s);
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s);
-// FP16 diagonally scaled copy of an FP32 stencil (Ah: 243*nn halves, sc: 3*nn).
-void mg_normalize_stencil(const MgDims& d, const float* A, const float* invd, float* sc,
-                          void* Ah, cudaStream_t s);
-void mg_stencil_op_h(int mode, const MgDims& d, const void* Ah, const float* sc,
-                     const uint8_t* act, const float* x, const float* b, const float* invdiag,
-                     float omega, float* y, cudaStream_t s);
 template <class T>
 void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cudaStream_t s);
 template <class T>

@@ -110,7 +110,6 @@ class Solver {
   DBuf<float> kebf_, Gf_;
   bool have_mg_ = false, numeric_ok_ = false, numeric_[2] = {false, false};
   double mg_build_ms_ = 0.0;
-  bool half_coarse_ = false;  // mixed form: FP16 scaled stencils on levels 1..L-2 (opt-in)
   int64_t fine_matvecs_ = 0, lowp_matvecs_ = 0;
   int nc_ = 0;
   DBuf<int> cidx_, cdof_, chol_fail_;
