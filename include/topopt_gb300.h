@@ -190,6 +190,28 @@ int tg_oc_update(const tg_grid* grid, double radius, const double* density,
                  const double* dcompliance, double volume_fraction, double move,
                  double density_min, double* x_new);
 
+/* ---- design masks (passive regions) ----
+ * Mask bytes are MaskValue (core/include/topopt/voxel.hpp:42-46): 0 Active,
+ * 1 FrozenSolid, 2 FrozenVoid, one per voxel; other values are rejected. */
+
+/* effective_design_mask (simp.hpp:462; simp.cpp:2610-2633): Empty voxels become
+ * FrozenVoid, Load (tag 4) and Fixture (tag 5) voxels FrozenSolid. */
+int tg_effective_design_mask(const tg_grid* grid, const uint8_t* mask, uint8_t* eff_out);
+
+/* The mask-aware density filter, make_density_filter(grid, radius, mask)
+ * (simp.hpp:444-446; simp.cpp:834-890) with one forward or adjoint pass: only
+ * solid voxels whose mask entry is Active are filter voxels. */
+int tg_filter_masked(const tg_grid* grid, const uint8_t* mask, double radius, int32_t adjoint,
+                     const double* x, double* out);
+
+/* oc_update_masked (simp.cpp:2662-2720) under the effective mask of `mask` and
+ * its Active-only filter: only Active voxels move, frozen voxels keep their x,
+ * the budget is volume_fraction * (Active voxels).  Bit-identical. */
+int tg_oc_update_masked(const tg_grid* grid, const uint8_t* mask, double radius,
+                        const double* density, const double* dcompliance,
+                        double volume_fraction, double move, double density_min,
+                        double* x_new);
+
 /* simp_optimize (core/include/topopt/simp.hpp:1783-1786; simp.cpp:2018-2592):
  * the OC loop with no projection.  history (max_iterations rows), design_out and
  * phys_out (voxels) may be NULL; cancel (may be NULL) is polled once per
@@ -201,6 +223,18 @@ int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
                      tg_simp_iteration* history, double* design_out, double* phys_out,
                      tg_simp_result* result);
 
+/* The masked overload, simp_optimize(grid, params, bcs, loads, options, mask)
+ * (simp.hpp:1820-1824; simp.cpp:2989-3640), OC, no projection: the analysis
+ * grid drops FrozenVoid voxels, the physical density is pinned (FrozenSolid 1,
+ * FrozenVoid 0) before each solve and in phys_out, and volume fractions are
+ * over the Active voxels. */
+int tg_simp_optimize_masked(const tg_grid* grid, const tg_simp_params* params,
+                            const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                            int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                            tg_progress_fn progress, void* progress_ctx,
+                            const volatile int32_t* cancel, tg_simp_iteration* history,
+                            double* design_out, double* phys_out, tg_simp_result* result);
+
 /* ---- resident jobs: state stays on the device between design iterations ---- */
 typedef struct tg_job tg_job;
 
@@ -209,6 +243,11 @@ typedef struct tg_job tg_job;
 int tg_job_create(const tg_grid* grid, const tg_simp_params* params,
                   const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
                   int32_t nloads, const tg_simp_options* options, tg_job** job_out);
+/* tg_job_create for the masked overload (see tg_simp_optimize_masked). */
+int tg_job_create_masked(const tg_grid* grid, const tg_simp_params* params,
+                         const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                         int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                         tg_job** job_out);
 /* One design iteration on the device: filter, solve, sensitivities, OC update. */
 int tg_job_step(tg_job* job, tg_simp_iteration* row);
 /* Copy the current design x and physical density filter(x) to the host. */

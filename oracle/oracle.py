@@ -146,6 +146,16 @@ class OracleLib:
                 [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
                                  C.c_void_p, _dp, _dp, _dp, _ip, _dp, _dp, C.c_void_p])
+            L.or_effective_design_mask.argtypes = [C.c_int] * 3 + [C.c_void_p, _bp, _bp]
+            L.or_effective_design_mask.restype = None
+            L.or_oc_update_masked.argtypes = [C.c_int] * 3 + [_bp, C.c_void_p, _dp, _dp,
+                                                              C.c_double, C.c_double, C.c_double,
+                                                              _dp, C.POINTER(C.c_double),
+                                                              C.POINTER(C.c_int)]
+            L.or_simp_optimize_masked.argtypes = (
+                [C.c_int] * 3 + [C.c_double, C.c_void_p, _bp, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                 C.c_void_p, _dp, _dp, _dp, _ip, _dp, _dp, C.c_void_p])
             L.or_sensitivity.argtypes = [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double,
                                                          C.c_double, C.c_double, C.c_double, _dp,
                                                          _dp, _dp, C.POINTER(C.c_double)]
@@ -155,6 +165,14 @@ class OracleLib:
             L.ref_oc_update.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_double, _dp, _dp,
                                                         C.c_double, C.c_double, C.c_double, _dp]
             L.ref_set_threads.argtypes = [C.c_int]
+            L.ref_effective_design_mask.argtypes = [C.c_int] * 3 + [C.c_void_p, _bp, _bp]
+            L.ref_filter_masked.argtypes = [C.c_int] * 3 + [C.c_void_p, _bp, C.c_double, C.c_int,
+                                                            _dp, _dp]
+            L.ref_simp_optimize_masked.argtypes = (
+                [C.c_int] * 3 + [C.c_double, C.c_void_p, _bp, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                 C.c_double, C.c_double, C.c_double, C.c_int, C.c_double,
+                                 C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip])
             L.ref_simp_optimize.argtypes = (
                 [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
@@ -280,6 +298,89 @@ class OracleLib:
             self._check(self.lib.ref_oc_update(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), radius, d,
                                                g, volfrac, move, rho_min, xn))
         return xn
+
+    # ---- design masks: pb.solid holds the raw voxel tags (0 Empty, 4 Load, 5 Fixture ...)
+    def effective_design_mask(self, pb: Problem, mask):
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        eff = np.zeros(pb.nv, np.uint8)
+        if self.kind == "port":
+            self.lib.or_effective_design_mask(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), m, eff)
+        else:
+            self._check(self.lib.ref_effective_design_mask(pb.nx, pb.ny, pb.nz,
+                                                           self._ptr(pb.solid), m, eff))
+        return eff
+
+    def filter_masked(self, pb: Problem, mask, x, radius=1.5, adjoint=False):
+        """make_density_filter(grid, radius, mask) and one pass."""
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(pb.nv)
+        if self.kind == "port":
+            act = (m == 0).astype(np.uint8)
+            f = self.lib.or_filter_make(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid),
+                                        act.ctypes.data_as(C.c_void_p), radius)
+            if not f:
+                self._check(1)
+            try:
+                (self.lib.or_filter_sensitivity if adjoint else self.lib.or_filter_density)(f, x, out)
+            finally:
+                self.lib.or_filter_free(f)
+        else:
+            self._check(self.lib.ref_filter_masked(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), m,
+                                                   radius, int(adjoint), x, out))
+        return out
+
+    def oc_update_masked(self, pb: Problem, mask, density, dc, volfrac, radius=1.5, move=0.2,
+                         rho_min=1e-3):
+        """oc_update_masked under the effective mask (port only: the reference's
+        is internal to simp.cpp and is pinned through simp_optimize_masked)."""
+        if self.kind != "port":
+            raise NotImplementedError("oc_update_masked is internal to the reference")
+        eff = self.effective_design_mask(pb, mask)
+        act = (eff == 0).astype(np.uint8)
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        g = np.ascontiguousarray(dc, dtype=np.float64)
+        xn = np.zeros(pb.nv)
+        f = self.lib.or_filter_make(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid),
+                                    act.ctypes.data_as(C.c_void_p), radius)
+        lam, nvol = C.c_double(0), C.c_int(0)
+        try:
+            self._check(self.lib.or_oc_update_masked(pb.nx, pb.ny, pb.nz, eff, f, d, g, volfrac,
+                                                     move, rho_min, xn, C.byref(lam),
+                                                     C.byref(nvol)))
+        finally:
+            self.lib.or_filter_free(f)
+        return xn
+
+    def simp_optimize_masked(self, pb: Problem, mask, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3,
+                             volfrac=0.3, radius=1.5, move=0.2, max_it=50, change_tol=0.01,
+                             cg_tol=1e-8, cg_max_it=0):
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        hc, hch, hvf = np.zeros(max_it), np.zeros(max_it), np.zeros(max_it)
+        design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+        if self.kind == "reference":
+            sc, ints = np.zeros(3), np.zeros(4, np.int32)
+            self._check(self.lib.ref_simp_optimize_masked(
+                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), m, E0, nu, penal, rho_min,
+                *pb.bc_args(), volfrac, radius, move, max_it, change_tol, cg_tol, cg_max_it, hc,
+                hch, hvf, design, phys, sc, ints))
+            n = int(ints[0])
+            return dict(compliance=sc[0], volume_fraction=sc[1], initial_compliance=sc[2],
+                        iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
+                        infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
+                        hist_vf=hvf[:n], design=design, phys=phys)
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it)
+        res = _OrSimpResult()
+        hcg = np.zeros(max_it, np.int32)
+        self._check(self.lib.or_simp_optimize_masked(
+            pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), m, E0, nu, penal, rho_min,
+            *pb.bc_args(), C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        n = res.iterations
+        return dict(compliance=res.compliance, volume_fraction=res.volume_fraction,
+                    initial_compliance=res.initial_compliance, iterations=n,
+                    converged=bool(res.converged), non_convergent=bool(res.non_convergent),
+                    infeasible=bool(res.infeasible), hist_c=hc[:n], hist_change=hch[:n],
+                    hist_vf=hvf[:n], hist_cg=hcg[:n], design=design, phys=phys)
 
     def simp_optimize(self, pb: Problem, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3, volfrac=0.3,
                       radius=1.5, move=0.2, max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0):

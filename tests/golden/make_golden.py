@@ -89,6 +89,33 @@ def main():
                simp_hist_change=s["hist_change"], simp_hist_vf=s["hist_vf"],
                simp_design=s["design"], simp_phys=s["phys"],
                simp_compliance=np.array(s["compliance"]), simp_iterations=np.array(s["iterations"]))
+
+    # Design masks (the masked simp_optimize overload): raw voxel tags with Empty
+    # pockets, a Fixture slab at x = 0 and a Load slab at the loaded edge; a
+    # mask with FrozenSolid and FrozenVoid islands.
+    mx, my, mz = 14, 6, 5
+    tags = np.ones((mz, my, mx), np.uint8)
+    tags[rng.random((mz, my, mx)) < 0.08] = 0
+    tags[:, :, 0] = 5
+    tags[mz // 2 - 1:mz // 2 + 1, :, mx - 1] = 4
+    tags = tags.ravel()
+    mask = np.zeros(mx * my * mz, np.uint8)
+    rr = rng.random(mask.size)
+    mask[rr < 0.10] = 1
+    mask[(rr >= 0.10) & (rr < 0.18)] = 2
+    pbm = cantilever(mx, my, mz, solid=tags)
+    xm = rng.random(pbm.nv)
+    out.update(mask_dims=np.array([mx, my, mz]), mask_tags=tags, mask_mask=mask,
+               mask_eff=R.effective_design_mask(pbm, mask), mask_x=xm,
+               mask_filt_fwd=R.filter_masked(pbm, mask, xm, 1.5, False),
+               mask_filt_adj=R.filter_masked(pbm, mask, xm, 1.5, True))
+    sm = R.simp_optimize_masked(pbm, mask, volfrac=0.35, radius=1.5, move=0.2, max_it=15,
+                                change_tol=0.01, cg_tol=1e-10)
+    out.update(msimp_hist_c=sm["hist_c"], msimp_hist_change=sm["hist_change"],
+               msimp_hist_vf=sm["hist_vf"], msimp_design=sm["design"], msimp_phys=sm["phys"],
+               msimp_compliance=np.array(sm["compliance"]),
+               msimp_volume_fraction=np.array(sm["volume_fraction"]),
+               msimp_iterations=np.array(sm["iterations"]))
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
 

@@ -84,6 +84,39 @@ def test_simp_loop_golden(port, golden):
     assert s["compliance"] == float(golden["simp_compliance"])
 
 
+def _masked_problem(golden):
+    mx, my, mz = (int(v) for v in golden["mask_dims"])
+    return cantilever(mx, my, mz, solid=golden["mask_tags"]), golden["mask_mask"]
+
+
+def test_masked_filter_golden(port, golden):
+    """effective_design_mask and the mask-aware filter, bit-identical."""
+    pb, mask = _masked_problem(golden)
+    assert np.array_equal(port.effective_design_mask(pb, mask), golden["mask_eff"])
+    x = golden["mask_x"]
+    assert np.array_equal(port.filter_masked(pb, mask, x, 1.5, False), golden["mask_filt_fwd"])
+    assert np.array_equal(port.filter_masked(pb, mask, x, 1.5, True), golden["mask_filt_adj"])
+
+
+def test_masked_simp_loop_golden(port, golden):
+    """The masked simp_optimize overload (oc_update_masked, pins, Active budget,
+    FrozenVoid removed from the analysis grid), bit-identical trajectory."""
+    pb, mask = _masked_problem(golden)
+    s = port.simp_optimize_masked(pb, mask, volfrac=0.35, radius=1.5, move=0.2, max_it=15,
+                                  change_tol=0.01, cg_tol=1e-10)
+    assert s["iterations"] == int(golden["msimp_iterations"])
+    assert np.array_equal(s["hist_c"], golden["msimp_hist_c"])
+    assert np.array_equal(s["hist_change"], golden["msimp_hist_change"])
+    assert np.array_equal(s["hist_vf"], golden["msimp_hist_vf"])
+    assert np.array_equal(s["design"], golden["msimp_design"])
+    assert np.array_equal(s["phys"], golden["msimp_phys"])
+    assert s["compliance"] == float(golden["msimp_compliance"])
+    assert s["volume_fraction"] == float(golden["msimp_volume_fraction"])
+    eff = golden["mask_eff"]
+    assert np.all(s["phys"][eff == 1] == 1.0) and np.all(s["phys"][eff == 2] == 0.0)
+    assert np.all(s["design"][eff == 1] == 1.0) and np.all(s["design"][eff == 2] == 0.0)
+
+
 def test_filter_properties(port):
     """Partition of unity and the adjoint identity (test_simp.cpp:312-386)."""
     rng = np.random.default_rng(3)

@@ -25,6 +25,7 @@ from ._capi import (  # noqa: F401
     SolveOptions,
     SolverNonConvergence,
     device_fma_peaks,
+    effective_design_mask,
     fea_build_reduced,
     kernel_launches,
     fea_matfree_apply,
@@ -34,8 +35,12 @@ from ._capi import (  # noqa: F401
     library_path,
     make_density_filter,
     oc_update,
+    oc_update_masked,
     simp_compliance,
     simp_optimize,
+    MASK_ACTIVE,
+    MASK_FROZEN_SOLID,
+    MASK_FROZEN_VOID,
     PREC_FP64,
     PREC_MIXED,
     SOLVER_MGCG,

@@ -131,7 +131,13 @@ def lib():
         "tg_oc_update": ([vp, dbl, vp, vp, dbl, dbl, dbl, vp], C.c_int),
         "tg_simp_optimize": ([vp, vp, vp, i32, vp, i32, vp, _PROGRESS, vp, vp, vp, vp, vp, vp],
                              C.c_int),
+        "tg_effective_design_mask": ([vp, vp, vp], C.c_int),
+        "tg_filter_masked": ([vp, vp, dbl, i32, vp, vp], C.c_int),
+        "tg_oc_update_masked": ([vp, vp, dbl, vp, vp, dbl, dbl, dbl, vp], C.c_int),
+        "tg_simp_optimize_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, _PROGRESS, vp, vp, vp, vp,
+                                     vp, vp], C.c_int),
         "tg_job_create": ([vp, vp, vp, i32, vp, i32, vp, vp], C.c_int),
+        "tg_job_create_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_job_step": ([vp, vp], C.c_int),
         "tg_job_read": ([vp, vp, vp], C.c_int),
         "tg_job_write_design": ([vp, vp], C.c_int),
@@ -357,29 +363,54 @@ def simp_compliance(pb: Problem, params: SimpParams, density, tolerance=1e-8, ma
     return dict(u=u, dcompliance=dc, compliance=c.value, cg=CgInfo._from(info))
 
 
-class DensityFilter:
-    """make_density_filter(grid, radius) (simp.cpp:834-896) over the solid voxels."""
+# MaskValue (voxel.hpp:42-46).
+MASK_ACTIVE, MASK_FROZEN_SOLID, MASK_FROZEN_VOID = 0, 1, 2
 
-    def __init__(self, pb: Problem, radius: float):
+
+def _mask(pb: Problem, mask):
+    m = np.ascontiguousarray(mask, dtype=np.uint8).ravel()
+    if m.size != pb.nv:
+        raise ValueError("mask size != voxel_count")
+    return m
+
+
+class DensityFilter:
+    """make_density_filter(grid, radius[, mask]) (simp.cpp:834-896): over the
+    solid voxels, or with a mask over the solid Active voxels."""
+
+    def __init__(self, pb: Problem, radius: float, mask=None):
         self.pb, self.radius = pb, float(radius)
+        self.mask = None if mask is None else _mask(pb, mask)
+
+    def _run(self, v, adjoint):
+        v = _f64(v, self.pb.nv)
+        out = np.zeros(self.pb.nv)
+        if self.mask is None:
+            _check(lib().tg_filter(C.byref(self.pb._grid), self.radius, adjoint, _p(v), _p(out)))
+        else:
+            _check(lib().tg_filter_masked(C.byref(self.pb._grid), _p(self.mask), self.radius,
+                                          adjoint, _p(v), _p(out)))
+        return out
 
     def filter_density(self, x):
-        x = _f64(x, self.pb.nv)
-        out = np.zeros(self.pb.nv)
-        _check(lib().tg_filter(C.byref(self.pb._grid), self.radius, 0, _p(x), _p(out)))
-        return out
+        return self._run(x, 0)
 
     def filter_sensitivity(self, s):
-        s = _f64(s, self.pb.nv)
-        out = np.zeros(self.pb.nv)
-        _check(lib().tg_filter(C.byref(self.pb._grid), self.radius, 1, _p(s), _p(out)))
-        return out
+        return self._run(s, 1)
 
 
-def make_density_filter(pb: Problem, radius: float) -> DensityFilter:
+def make_density_filter(pb: Problem, radius: float, mask=None) -> DensityFilter:
     if not (radius > 0.0):
         raise ValueError("make_density_filter: radius must be > 0")
-    return DensityFilter(pb, radius)
+    return DensityFilter(pb, radius, mask)
+
+
+def effective_design_mask(pb: Problem, mask):
+    """simp.cpp:2610-2633: Empty -> FrozenVoid, Load/Fixture -> FrozenSolid."""
+    m = _mask(pb, mask)
+    out = np.zeros(pb.nv, np.uint8)
+    _check(lib().tg_effective_design_mask(C.byref(pb._grid), _p(m), _p(out)))
+    return out
 
 
 def oc_update(pb: Problem, filt: DensityFilter, density, dcompliance, volume_fraction, move=0.2,
@@ -389,6 +420,18 @@ def oc_update(pb: Problem, filt: DensityFilter, density, dcompliance, volume_fra
     out = np.zeros(pb.nv)
     _check(lib().tg_oc_update(C.byref(pb._grid), filt.radius, _p(d), _p(dc), volume_fraction, move,
                               density_min, _p(out)))
+    return out
+
+
+def oc_update_masked(pb: Problem, radius, mask, density, dcompliance, volume_fraction, move=0.2,
+                     density_min=1e-3):
+    """oc_update_masked (simp.cpp:2662-2720) under effective_design_mask(mask) and
+    its Active-only filter: bit-identical to the reference."""
+    m = _mask(pb, mask)
+    d, dc = _f64(density, pb.nv), _f64(dcompliance, pb.nv)
+    out = np.zeros(pb.nv)
+    _check(lib().tg_oc_update_masked(C.byref(pb._grid), _p(m), float(radius), _p(d), _p(dc),
+                                     volume_fraction, move, density_min, _p(out)))
     return out
 
 
@@ -409,9 +452,10 @@ def _rows(hist, n):
 
 
 def simp_optimize(pb: Problem, params: SimpParams, options: SimpOptions, progress=None,
-                  cancel=None):
-    """simp.hpp:1783-1786 (OC, no projection).  ``cancel`` may be a one-element
-    int32 numpy array polled once per iteration."""
+                  cancel=None, mask=None):
+    """simp.hpp:1783-1786 (OC, no projection); with ``mask`` the masked overload
+    (simp.hpp:1820-1824).  ``cancel`` may be a one-element int32 numpy array
+    polled once per iteration."""
     prm, opt = params._c(), options._c()
     hist = (_Iter * options.max_iterations)()
     design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
@@ -419,8 +463,15 @@ def simp_optimize(pb: Problem, params: SimpParams, options: SimpOptions, progres
     cb = _PROGRESS(lambda ctx, it, c, ch: progress(it, c, ch)) if progress else _PROGRESS()
     cptr = None if cancel is None else cancel.ctypes.data_as(C.c_void_p)
     g, b, nb, l, nl = pb._args()
-    rc = lib().tg_simp_optimize(g, C.byref(prm), b, nb, l, nl, C.byref(opt), cb, None, cptr,
-                                C.cast(hist, C.c_void_p), _p(design), _p(phys), C.byref(res))
+    if mask is None:
+        rc = lib().tg_simp_optimize(g, C.byref(prm), b, nb, l, nl, C.byref(opt), cb, None, cptr,
+                                    C.cast(hist, C.c_void_p), _p(design), _p(phys),
+                                    C.byref(res))
+    else:
+        m = _mask(pb, mask)
+        rc = lib().tg_simp_optimize_masked(g, C.byref(prm), b, nb, l, nl, C.byref(opt), _p(m),
+                                           cb, None, cptr, C.cast(hist, C.c_void_p), _p(design),
+                                           _p(phys), C.byref(res))
     _check(rc)
     return dict(design=design, physical_density=phys, compliance=res.compliance,
                 initial_compliance=res.initial_compliance, volume_fraction=res.volume_fraction,
@@ -433,13 +484,19 @@ class SimpJob:
     """A resident optimisation job: density, displacement and the multigrid
     hierarchy stay on the device between ``step()`` calls."""
 
-    def __init__(self, pb: Problem, params: SimpParams, options: SimpOptions):
+    def __init__(self, pb: Problem, params: SimpParams, options: SimpOptions, mask=None):
         self.pb = pb
         self._prm, self._opt = params._c(), options._c()
         self._h = C.c_void_p()
         g, b, nb, l, nl = pb._args()
-        _check(lib().tg_job_create(g, C.byref(self._prm), b, nb, l, nl, C.byref(self._opt),
-                                   C.byref(self._h)))
+        if mask is None:
+            _check(lib().tg_job_create(g, C.byref(self._prm), b, nb, l, nl, C.byref(self._opt),
+                                       C.byref(self._h)))
+        else:
+            self._mask = _mask(pb, mask)
+            _check(lib().tg_job_create_masked(g, C.byref(self._prm), b, nb, l, nl,
+                                              C.byref(self._opt), _p(self._mask),
+                                              C.byref(self._h)))
 
     def step(self):
         row = _Iter()

@@ -107,6 +107,24 @@ void validate_params(const tg_simp_params* p) {
     raise(TG_EINVAL, "simp: e_min must be in (0, E0) for the modified law");
 }
 
+// effective_design_mask (simp.cpp:2610-2633): Empty voxels -> FrozenVoid (2),
+// Load (4) and Fixture (5) voxels -> FrozenSolid (1), the caller's entry
+// elsewhere.  Mask bytes are MaskValue (voxel.hpp:42-46): 0 Active, 1 FrozenSolid,
+// 2 FrozenVoid; any other byte is rejected.
+std::vector<uint8_t> effective_mask(const tg_grid* g, const uint8_t* mask, const char* who) {
+  if (!mask) raise(TG_EINVAL, std::string(who) + ": mask size != voxel_count");
+  const int64_t nv = int64_t(g->nx) * g->ny * g->nz;
+  std::vector<uint8_t> eff(static_cast<size_t>(nv));
+  for (int64_t e = 0; e < nv; ++e) {
+    if (mask[e] > 2)
+      raise(TG_EINVAL, std::string(who) +
+                           ": mask values must be 0 (Active), 1 (FrozenSolid) or 2 (FrozenVoid)");
+    const uint8_t t = g->tags ? g->tags[e] : uint8_t(1);
+    eff[size_t(e)] = t == 0 ? uint8_t(2) : ((t == 4 || t == 5) ? uint8_t(1) : mask[e]);
+  }
+  return eff;
+}
+
 tg_solve_options default_solve(const tg_solve_options* o) {
   tg_solve_options d;
   std::memset(&d, 0, sizeof d);
@@ -177,6 +195,7 @@ struct OcState {
   std::vector<double> h_xp;
   int64_t n_solid = 0;
   int fallbacks = 0, evals = 0;
+  bool carry = false;  // oc_update_masked: voxels outside the design set keep x
   void init(const Grid& g, cudaStream_t) {
     for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi}) d->alloc(size_t(g.nv));
     vpart.alloc(size_t(kRedBlocks));
@@ -277,7 +296,7 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
       }
     }
     ++oc.exact_evals;
-    launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, lam, move, rho_min, xnew, s);
+    launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, lam, move, rho_min, oc.carry, xnew, s);
     fs.fwd(g, act, xnew, oc.xp.p, s);
     return volume_exceeds(oc, g, act, act_h, target, s);
   };
@@ -290,7 +309,8 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
     else
       l2 = lmid;
   }
-  launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, 0.5 * (l1 + l2), move, rho_min, xnew, s);
+  launch_oc_candidate(x, oc.dcf.p, oc.dvf.p, act, g.nv, 0.5 * (l1 + l2), move, rho_min, oc.carry,
+                      xnew, s);
 }
 
 }  // namespace tg
@@ -306,8 +326,11 @@ struct tg_job {
   std::unique_ptr<Solver> solver;
   FilterState filt;
   OcState oc;
-  DBuf<uint8_t> solid;
+  DBuf<uint8_t> solid;          // the design set: solid voxels, or Active voxels (masked)
   std::vector<uint8_t> solid_h;
+  bool masked = false;          // the masked overload (simp.cpp:2989-3640)
+  DBuf<uint8_t> eff;            // effective design mask (masked jobs)
+  std::vector<uint8_t> eff_h;
   DBuf<double> x, xnew, xphys, E, u, dc, part, scal;
   double* h_scal = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -325,7 +348,7 @@ struct tg_job {
     if (s) cudaStreamDestroy(s);
   }
   size_t bytes() const {
-    size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes();
+    size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes() + eff.bytes();
     for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal}) b += d->bytes();
     return b + (solver ? solver->device_bytes() : 0);
   }
@@ -334,9 +357,13 @@ struct tg_job {
 namespace tg {
 namespace {
 
+// Job setup.  With a mask (the masked overload, simp.cpp:3017-3072): the
+// effective mask, the analysis grid with FrozenVoid voxels made Empty, the
+// Active-only filter and design set, and the start design Active = volfrac,
+// FrozenSolid = 1, else 0.
 void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
               const tg_dirichlet_bc* bcs, int nbc, const tg_nodal_load* loads, int nloads,
-              const tg_simp_options* options) {
+              const tg_simp_options* options, const uint8_t* mask = nullptr) {
   validate_grid(grid);
   validate_params(params);
   if (!options) raise(TG_EINVAL, "options is null");
@@ -355,10 +382,26 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   TG_CUDA(cudaEventCreate(&j->ev0));
   TG_CUDA(cudaEventCreate(&j->ev1));
   cudaStream_t s = j->s;
-  j->fp.build(*grid, params->poisson, bcs, nbc, loads, nloads, nullptr, s);
+  tg_grid analysis = *grid;
+  std::vector<uint8_t> atags;
+  j->masked = mask != nullptr;
+  if (j->masked) {
+    j->eff_h = effective_mask(grid, mask, "simp_optimize");
+    atags.resize(j->eff_h.size());
+    for (size_t e = 0; e < atags.size(); ++e)
+      atags[e] = j->eff_h[e] == 2 ? uint8_t(0) : (grid->tags ? grid->tags[e] : uint8_t(1));
+    analysis.tags = atags.data();
+  }
+  j->fp.build(analysis, params->poisson, bcs, nbc, loads, nloads, nullptr, s);
   const Grid& g = j->fp.g;
   j->solver = std::make_unique<Solver>(j->fp, j->opt.solve, s);
-  j->solid_h = j->fp.elem_h;  // no active mask on this path: elem == solid
+  if (j->masked) {
+    j->solid_h.resize(j->eff_h.size());
+    for (size_t e = 0; e < j->eff_h.size(); ++e) j->solid_h[e] = j->eff_h[e] == 0;
+    upload(j->eff, j->eff_h.data(), j->eff_h.size(), s);
+  } else {
+    j->solid_h = j->fp.elem_h;  // no mask on this path: the design set is the solid set
+  }
   j->n_solid = 0;
   for (uint8_t v : j->solid_h) j->n_solid += v;
   upload(j->solid, j->solid_h.data(), j->solid_h.size(), s);
@@ -370,13 +413,17 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   j->filt.init(g, o.filter_radius, j->solid.p, s);
   j->oc.init(g, s);
   j->oc.n_solid = j->n_solid;
+  j->oc.carry = j->masked;
   // dv = filter_sensitivity(ones on solid voxels) (simp.cpp:967-976): fixed.
   std::vector<double> ones(size_t(g.nv));
   for (int64_t e = 0; e < g.nv; ++e) ones[size_t(e)] = j->solid_h[size_t(e)] ? 1.0 : 0.0;
   TG_CUDA(cudaMemcpyAsync(j->xnew.p, ones.data(), j->xnew.bytes(), cudaMemcpyHostToDevice, s));
   j->filt.adj(g, j->solid.p, j->xnew.p, j->oc.dvf.p, s);
-  // simp_uniform_density (simp.cpp:305-312).
-  for (int64_t e = 0; e < g.nv; ++e) ones[size_t(e)] = j->solid_h[size_t(e)] ? o.volume_fraction : 0.0;
+  // simp_uniform_density (simp.cpp:305-312); masked: simp.cpp:3066-3072.
+  for (int64_t e = 0; e < g.nv; ++e) {
+    ones[size_t(e)] = j->solid_h[size_t(e)] ? o.volume_fraction : 0.0;
+    if (j->masked && j->eff_h[size_t(e)] == 1) ones[size_t(e)] = 1.0;
+  }
   TG_CUDA(cudaMemcpyAsync(j->x.p, ones.data(), j->x.bytes(), cudaMemcpyHostToDevice, s));
   TG_CUDA(cudaStreamSynchronize(s));
 }
@@ -408,8 +455,12 @@ SolverStats job_solve(tg_job* j, double tol, int max_it) {
   return j->solver->solve(tol, max_it, nullptr, j->u.p);
 }
 
+// xPhys = filter(x), then the mask pins (simp.cpp:3200-3204).  Volume sums run
+// over the Active set only, which the pins never touch, so they see the
+// unpinned field as the reference's active_volfrac does.
 void job_filter_x(tg_job* j) {
   j->filt.fwd(j->fp.g, j->solid.p, j->x.p, j->xphys.p, j->s);
+  if (j->masked) launch_mask_pins(j->eff.p, j->fp.g.nv, j->xphys.p, j->s);
   j->xphys_valid = true;
 }
 
@@ -494,6 +545,72 @@ bool rung_infeasible(const std::vector<double>& c, const std::vector<int>& cg) {
   return (hi - lo) / lo <= 1e-3;
 }
 
+
+// make_density_filter(grid, radius[, mask]) and one filter pass: the design set
+// is the solid voxels, and with a mask the solid voxels whose entry is Active
+// (simp.cpp:846-849).
+void filter_call(const tg_grid* grid, const uint8_t* mask, double radius, int adjoint,
+                 const double* x, double* out) {
+  validate_grid(grid);
+  if (!x || !out) raise(TG_EINVAL, "x and out must be non-null");
+  CallStream cs;
+  const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+  std::vector<uint8_t> act(size_t(g.nv));
+  for (int64_t e = 0; e < g.nv; ++e)
+    act[size_t(e)] = (grid->tags == nullptr || grid->tags[e] != 0) && (!mask || mask[e] == 0);
+  DBuf<uint8_t> dact;
+  DBuf<double> dx, dout(size_t(g.nv));
+  upload(dact, act.data(), act.size(), cs.s);
+  upload(dx, x, size_t(g.nv), cs.s);
+  FilterState fs;
+  fs.init(g, radius, dact.p, cs.s);
+  if (adjoint)
+    fs.adj(g, dact.p, dx.p, dout.p, cs.s);
+  else
+    fs.fwd(g, dact.p, dx.p, dout.p, cs.s);
+  TG_CUDA(cudaMemcpyAsync(out, dout.p, dout.bytes(), cudaMemcpyDeviceToHost, cs.s));
+  TG_CUDA(cudaStreamSynchronize(cs.s));
+}
+
+// oc_update (simp.cpp:948-1025) when eff is null; oc_update_masked
+// (simp.cpp:2662-2720) with the effective mask eff: the design set is the
+// Active voxels, the filter is Active-only and frozen voxels keep their x.
+void oc_call(const tg_grid* grid, const uint8_t* eff, double radius, const double* density,
+             const double* dc, double volfrac, double move, double rho_min, double* x_new) {
+  validate_grid(grid);
+  if (!density || !dc || !x_new) raise(TG_EINVAL, "density, dc and x_new must be non-null");
+  if (!(volfrac > 0.0 && volfrac <= 1.0))
+    raise(TG_EINVAL, "oc_update: volume_fraction must be in (0, 1]");
+  if (!(move > 0.0)) raise(TG_EINVAL, "oc_update: move must be > 0");
+  if (!(rho_min > 0.0 && rho_min <= 1.0))
+    raise(TG_EINVAL, "oc_update: density_min must be in (0, 1]");
+  CallStream cs;
+  const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+  std::vector<uint8_t> act(size_t(g.nv));
+  int64_t n_design = 0;
+  for (int64_t e = 0; e < g.nv; ++e) {
+    act[size_t(e)] = eff ? eff[e] == 0 : (grid->tags == nullptr || grid->tags[e] != 0);
+    n_design += act[size_t(e)];
+  }
+  DBuf<uint8_t> dact;
+  DBuf<double> dx, ddc, dxn(size_t(g.nv)), ones;
+  upload(dact, act.data(), act.size(), cs.s);
+  upload(dx, density, size_t(g.nv), cs.s);
+  upload(ddc, dc, size_t(g.nv), cs.s);
+  std::vector<double> o1(size_t(g.nv));
+  for (int64_t e = 0; e < g.nv; ++e) o1[size_t(e)] = act[size_t(e)] ? 1.0 : 0.0;
+  upload(ones, o1.data(), o1.size(), cs.s);
+  FilterState fs;
+  fs.init(g, radius, dact.p, cs.s);
+  OcState oc;
+  oc.init(g, cs.s);
+  oc.n_solid = n_design;
+  oc.carry = eff != nullptr;
+  fs.adj(g, dact.p, ones.p, oc.dvf.p, cs.s);
+  oc_update_device(oc, fs, g, dact.p, act, dx.p, ddc.p, volfrac, move, rho_min, dxn.p, cs.s);
+  TG_CUDA(cudaMemcpyAsync(x_new, dxn.p, dxn.bytes(), cudaMemcpyDeviceToHost, cs.s));
+  TG_CUDA(cudaStreamSynchronize(cs.s));
+}
 }  // namespace
 }  // namespace tg
 
@@ -701,63 +818,40 @@ int tg_simp_compliance(const tg_grid* grid, const tg_simp_params* params, const 
 }
 
 int tg_filter(const tg_grid* grid, double radius, int32_t adjoint, const double* x, double* out) {
+  return guarded([&] { filter_call(grid, nullptr, radius, adjoint, x, out); });
+}
+
+int tg_filter_masked(const tg_grid* grid, const uint8_t* mask, double radius, int32_t adjoint,
+                     const double* x, double* out) {
   return guarded([&] {
     validate_grid(grid);
-    if (!x || !out) raise(TG_EINVAL, "x and out must be non-null");
-    CallStream cs;
-    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
-    std::vector<uint8_t> act(size_t(g.nv));
-    for (int64_t e = 0; e < g.nv; ++e) act[size_t(e)] = grid->tags == nullptr || grid->tags[e] != 0;
-    DBuf<uint8_t> dact;
-    DBuf<double> dx, dout(size_t(g.nv));
-    upload(dact, act.data(), act.size(), cs.s);
-    upload(dx, x, size_t(g.nv), cs.s);
-    FilterState fs;
-    fs.init(g, radius, dact.p, cs.s);
-    if (adjoint)
-      fs.adj(g, dact.p, dx.p, dout.p, cs.s);
-    else
-      fs.fwd(g, dact.p, dx.p, dout.p, cs.s);
-    TG_CUDA(cudaMemcpyAsync(out, dout.p, dout.bytes(), cudaMemcpyDeviceToHost, cs.s));
-    TG_CUDA(cudaStreamSynchronize(cs.s));
+    if (!mask) raise(TG_EINVAL, "make_density_filter: mask size != voxel_count");
+    filter_call(grid, mask, radius, adjoint, x, out);
   });
 }
 
 int tg_oc_update(const tg_grid* grid, double radius, const double* density, const double* dc,
                  double volfrac, double move, double rho_min, double* x_new) {
+  return guarded(
+      [&] { oc_call(grid, nullptr, radius, density, dc, volfrac, move, rho_min, x_new); });
+}
+
+int tg_oc_update_masked(const tg_grid* grid, const uint8_t* mask, double radius,
+                        const double* density, const double* dc, double volfrac, double move,
+                        double rho_min, double* x_new) {
   return guarded([&] {
     validate_grid(grid);
-    if (!density || !dc || !x_new) raise(TG_EINVAL, "density, dc and x_new must be non-null");
-    if (!(volfrac > 0.0 && volfrac <= 1.0))
-      raise(TG_EINVAL, "oc_update: volume_fraction must be in (0, 1]");
-    if (!(move > 0.0)) raise(TG_EINVAL, "oc_update: move must be > 0");
-    if (!(rho_min > 0.0 && rho_min <= 1.0))
-      raise(TG_EINVAL, "oc_update: density_min must be in (0, 1]");
-    CallStream cs;
-    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
-    std::vector<uint8_t> act(size_t(g.nv));
-    int64_t n_solid = 0;
-    for (int64_t e = 0; e < g.nv; ++e) {
-      act[size_t(e)] = grid->tags == nullptr || grid->tags[e] != 0;
-      n_solid += act[size_t(e)];
-    }
-    DBuf<uint8_t> dact;
-    DBuf<double> dx, ddc, dxn(size_t(g.nv)), ones;
-    upload(dact, act.data(), act.size(), cs.s);
-    upload(dx, density, size_t(g.nv), cs.s);
-    upload(ddc, dc, size_t(g.nv), cs.s);
-    std::vector<double> o1(size_t(g.nv));
-    for (int64_t e = 0; e < g.nv; ++e) o1[size_t(e)] = act[size_t(e)] ? 1.0 : 0.0;
-    upload(ones, o1.data(), o1.size(), cs.s);
-    FilterState fs;
-    fs.init(g, radius, dact.p, cs.s);
-    OcState oc;
-    oc.init(g, cs.s);
-    oc.n_solid = n_solid;
-    fs.adj(g, dact.p, ones.p, oc.dvf.p, cs.s);
-    oc_update_device(oc, fs, g, dact.p, act, dx.p, ddc.p, volfrac, move, rho_min, dxn.p, cs.s);
-    TG_CUDA(cudaMemcpyAsync(x_new, dxn.p, dxn.bytes(), cudaMemcpyDeviceToHost, cs.s));
-    TG_CUDA(cudaStreamSynchronize(cs.s));
+    const std::vector<uint8_t> eff = effective_mask(grid, mask, "oc_update_masked");
+    oc_call(grid, eff.data(), radius, density, dc, volfrac, move, rho_min, x_new);
+  });
+}
+
+int tg_effective_design_mask(const tg_grid* grid, const uint8_t* mask, uint8_t* eff_out) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!eff_out) raise(TG_EINVAL, "eff_out is null");
+    const std::vector<uint8_t> eff = effective_mask(grid, mask, "effective_design_mask");
+    std::memcpy(eff_out, eff.data(), eff.size());
   });
 }
 
@@ -768,6 +862,20 @@ int tg_job_create(const tg_grid* grid, const tg_simp_params* params, const tg_di
     if (!job_out) raise(TG_EINVAL, "job_out is null");
     auto j = std::make_unique<tg_job>();
     job_init(j.get(), grid, params, bcs, nbc, loads, nloads, options);
+    *job_out = j.release();
+  });
+}
+
+int tg_job_create_masked(const tg_grid* grid, const tg_simp_params* params,
+                         const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                         int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                         tg_job** job_out) {
+  return guarded([&] {
+    if (!job_out) raise(TG_EINVAL, "job_out is null");
+    validate_grid(grid);
+    if (!mask) raise(TG_EINVAL, "simp_optimize: mask size != voxel_count");
+    auto j = std::make_unique<tg_job>();
+    job_init(j.get(), grid, params, bcs, nbc, loads, nloads, options, mask);
     *job_out = j.release();
   });
 }
@@ -847,17 +955,17 @@ int tg_device_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
   });
 }
 
-int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
-                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
-                     int32_t nloads, const tg_simp_options* options, tg_progress_fn progress,
-                     void* progress_ctx, const volatile int32_t* cancel,
-                     tg_simp_iteration* history, double* design_out, double* phys_out,
-                     tg_simp_result* result) {
+static int simp_optimize_impl(const tg_grid* grid, const tg_simp_params* params,
+                              const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                              int32_t nloads, const tg_simp_options* options,
+                              const uint8_t* mask, tg_progress_fn progress, void* progress_ctx,
+                              const volatile int32_t* cancel, tg_simp_iteration* history,
+                              double* design_out, double* phys_out, tg_simp_result* result) {
   tg_simp_result res;
   std::memset(&res, 0, sizeof res);
   const int rc = guarded([&] {
     auto jp = std::make_unique<tg_job>();
-    job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, options);
+    job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, options, mask);
     tg_job* j = jp.get();
     const tg_simp_options& o = j->opt;
     for (int it = 0; it < o.max_iterations; ++it) {
@@ -914,6 +1022,31 @@ int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
   });
   if (result) *result = res;
   return rc;
+}
+
+int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, const tg_simp_options* options, tg_progress_fn progress,
+                     void* progress_ctx, const volatile int32_t* cancel,
+                     tg_simp_iteration* history, double* design_out, double* phys_out,
+                     tg_simp_result* result) {
+  return simp_optimize_impl(grid, params, bcs, nbc, loads, nloads, options, nullptr, progress,
+                            progress_ctx, cancel, history, design_out, phys_out, result);
+}
+
+int tg_simp_optimize_masked(const tg_grid* grid, const tg_simp_params* params,
+                            const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                            int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                            tg_progress_fn progress, void* progress_ctx,
+                            const volatile int32_t* cancel, tg_simp_iteration* history,
+                            double* design_out, double* phys_out, tg_simp_result* result) {
+  if (!mask) {
+    tg::set_last_error("simp_optimize: mask size != voxel_count");
+    if (result) std::memset(result, 0, sizeof *result);
+    return TG_EINVAL;
+  }
+  return simp_optimize_impl(grid, params, bcs, nbc, loads, nloads, options, mask, progress,
+                            progress_ctx, cancel, history, design_out, phys_out, result);
 }
 
 }  // extern "C"

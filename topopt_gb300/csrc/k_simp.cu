@@ -293,11 +293,11 @@ __global__ void k_filter_adj(GridDev g, const StencilEntry* __restrict__ st, int
 // --------------------------------------------------------------------- OC
 __global__ void k_oc_candidate(const double* __restrict__ x, const double* __restrict__ dcf,
                                const double* __restrict__ dvf, const uint8_t* __restrict__ act,
-                               int64_t n, double lambda, double move, double rho_min,
+                               int64_t n, double lambda, double move, double rho_min, int carry,
                                double* __restrict__ xnew) {
   for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
        e += int64_t(gridDim.x) * kThreads) {
-    double xt = 0.0;
+    double xt = carry ? x[e] : 0.0;
     if (act[e]) {
       const double xe = x[e];
       double be = 0.0;
@@ -311,6 +311,16 @@ __global__ void k_oc_candidate(const double* __restrict__ x, const double* __res
       if (xt > hi) xt = hi;
     }
     xnew[e] = xt;
+  }
+}
+
+// apply_mask_pins (simp.cpp:2648-2654): FrozenSolid -> 1, FrozenVoid -> 0.
+__global__ void k_mask_pins(const uint8_t* __restrict__ eff, int64_t n, double* __restrict__ xphys) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    const uint8_t m = eff[e];
+    if (m == 1) xphys[e] = 1.0;
+    else if (m == 2) xphys[e] = 0.0;
   }
 }
 
@@ -524,9 +534,14 @@ void launch_filter_adj(const Grid& g, const void* st, int ns, const uint8_t* act
 
 void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
                          const uint8_t* act, int64_t n, double lambda, double move,
-                         double rho_min, double* xnew, cudaStream_t s) {
+                         double rho_min, bool carry, double* xnew, cudaStream_t s) {
   k_oc_candidate<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, lambda, move, rho_min,
-                                                     xnew);
+                                                     carry ? 1 : 0, xnew);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t s) {
+  k_mask_pins<<<grid_blocks(n), kThreads, 0, s>>>(eff, n, xphys);
   TG_LAUNCH_CHECK();
 }
 

@@ -178,7 +178,9 @@ void launch_filter_adj(const Grid& g, const void* st, int ns, const uint8_t* act
                        cudaStream_t s);
 void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
                          const uint8_t* act, int64_t n, double lambda, double move,
-                         double rho_min, double* xnew, cudaStream_t s);
+                         double rho_min, bool carry, double* xnew, cudaStream_t s);
+// FrozenSolid (1) -> 1, FrozenVoid (2) -> 0 on the physical density.
+void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t s);
 // Exact (fixed-point, order independent) sum of a non-negative field over the
 // solid voxels; returns per-block 192-bit partials, then the final total.
 int exact_sum_blocks();
