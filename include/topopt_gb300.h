@@ -235,6 +235,31 @@ int tg_simp_optimize_masked(const tg_grid* grid, const tg_simp_params* params,
                             const volatile int32_t* cancel, tg_simp_iteration* history,
                             double* design_out, double* phys_out, tg_simp_result* result);
 
+/* ---- periodic homogenization of unit cells ---- */
+typedef struct {
+  int32_t iterations_max;    /* largest CG iteration count over the batch */
+  int32_t converged;         /* 1 when every system met the tolerance */
+  int32_t systems;           /* cells x solved strain columns */
+  int64_t iterations_total;  /* sum of the CG iteration counts */
+  double t_setup_ms, t_solve_ms, t_total_ms;
+} tg_homog_info;
+
+/* Periodic strain homogenization of a batch of unit cells, the homogenize()
+ * of core/tests/harness/lattice_homog_probe.cpp:290-412 (a harness library;
+ * no production caller): cells of nx*ny*nz voxels with opposite faces
+ * identified, tags ncell*nx*ny*nz bytes (cell c at c*nx*ny*nz, 0 = void,
+ * voids carry no element), Hex8 elements of modulus E, Poisson nu, edge
+ * spacing.  cases_mask selects the Voigt strain columns [xx,yy,zz,gxy,gyz,gzx]
+ * solved (bit J; 0x3F = all six).  Each system is solved by Jacobi-PCG to
+ * |r| < tolerance |b| (max_iterations <= 0: min(2 ndof, 200000)).  ch_out
+ * receives ncell 6x6 tensors, row-major, CH[I][J] filled for the solved
+ * columns J (others 0).  TG_ENONCONV when a system missed the tolerance (the
+ * tensors are still written). */
+int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, double spacing,
+                  double youngs_modulus, double poisson, const uint8_t* tags,
+                  int32_t cases_mask, double tolerance, int32_t max_iterations,
+                  double* ch_out, tg_homog_info* info);
+
 /* ---- resident jobs: state stays on the device between design iterations ---- */
 typedef struct tg_job tg_job;
 

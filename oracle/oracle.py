@@ -156,6 +156,10 @@ class OracleLib:
                 [C.c_int] * 3 + [C.c_double, C.c_void_p, _bp, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
                                  C.c_void_p, _dp, _dp, _dp, _ip, _dp, _dp, C.c_void_p])
+            L.or_homogenize.argtypes = [C.c_int] * 3 + [C.c_double, C.c_double, C.c_double,
+                                                        C.c_void_p, C.c_int, C.c_double, C.c_int,
+                                                        _dp, C.POINTER(C.c_int),
+                                                        C.POINTER(C.c_int)]
             L.or_sensitivity.argtypes = [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double,
                                                          C.c_double, C.c_double, C.c_double, _dp,
                                                          _dp, _dp, C.POINTER(C.c_double)]
@@ -298,6 +302,19 @@ class OracleLib:
             self._check(self.lib.ref_oc_update(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), radius, d,
                                                g, volfrac, move, rho_min, xn))
         return xn
+
+    def homogenize(self, nx, ny, nz, solid=None, h=1.0, E=1.0, nu=0.3, cases=0x3F, tol=1e-9,
+                   max_it=0):
+        """Periodic homogenization of one cell (port only: the reference's is a
+        harness built on Eigen, absent here).  Returns (CH 6x6, iters, converged)."""
+        if self.kind != "port":
+            raise NotImplementedError("the reference homogenization harness needs Eigen")
+        CH = np.zeros(36)
+        it, conv = C.c_int(0), C.c_int(0)
+        sp = None if solid is None else np.ascontiguousarray(solid, dtype=np.uint8)
+        self._check(self.lib.or_homogenize(nx, ny, nz, h, E, nu, self._ptr(sp), cases, tol, max_it,
+                                           CH, C.byref(it), C.byref(conv)))
+        return CH.reshape(6, 6), it.value, bool(conv.value)
 
     # ---- design masks: pb.solid holds the raw voxel tags (0 Empty, 4 Load, 5 Fixture ...)
     def effective_design_mask(self, pb: Problem, mask):

@@ -897,3 +897,184 @@ int or_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tag
                      bc_val, nload, ld_node, ld_comp, ld_val, o, hist_c, hist_change, hist_vf,
                      hist_cg, design, phys, res);
 }
+
+/* -------------------------------------------------------- homogenization */
+/* Periodic (torus) strain homogenization of one unit cell, restating
+ * core/tests/harness/lattice_homog_probe.cpp:290-412: Hex8 elements with opposite
+ * faces identified; the six Voigt unit strains [xx,yy,zz,gxy,gyz,gzx]
+ * (engineering shear) give element vectors chi0 (:240-265) and right-hand sides
+ * F_J = sum_e ke chi0_J; node 0's three DOFs and every DOF touched by no solid
+ * element are pinned (zero row/column, unit diagonal, zero rhs); K chi_J = F_J is
+ * solved by Jacobi-preconditioned CG (Eigen's ConjugateGradient with its
+ * default diagonal preconditioner, :344-356: stop when |r|^2 < tol^2 |b|^2, at
+ * most min(2 n, 200000) iterations); then
+ *   CH[I][J] = (1/|Y|) sum_e chi0_I^T ke (chi0_J - chi_J,e),
+ * |Y| the full cell volume (:368-398).  The operator is applied element by
+ * element (not assembled); Eigen itself is not available here. */
+static const int kHexOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                  {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+typedef struct {
+  int nx, ny, nz;
+  const uint8_t* solid;
+  const double* ke;
+  const uint8_t* pinned;
+  size_t nd;
+} homog_sys;
+
+static void homog_gd(const homog_sys* s, int i, int j, int k, size_t gd[24]) {
+  for (int a = 0; a < 8; ++a) {
+    const int aa = (i + kHexOff[a][0]) % s->nx, bb = (j + kHexOff[a][1]) % s->ny,
+              cc = (k + kHexOff[a][2]) % s->nz;
+    const size_t p = ((size_t)cc * s->ny + bb) * s->nx + aa;
+    gd[3 * a] = 3 * p;
+    gd[3 * a + 1] = 3 * p + 1;
+    gd[3 * a + 2] = 3 * p + 2;
+  }
+}
+
+/* y = K u with the pins (pinned rows/cols -> identity). */
+static void homog_apply(const homog_sys* s, const double* u, double* y) {
+  memset(y, 0, s->nd * sizeof(double));
+  for (int k = 0; k < s->nz; ++k)
+    for (int j = 0; j < s->ny; ++j)
+      for (int i = 0; i < s->nx; ++i) {
+        if (!is_solid(s->solid, ((size_t)k * s->ny + j) * s->nx + i)) continue;
+        size_t gd[24];
+        homog_gd(s, i, j, k, gd);
+        double ue[24];
+        for (int c = 0; c < 24; ++c) ue[c] = s->pinned[gd[c]] ? 0.0 : u[gd[c]];
+        for (int r = 0; r < 24; ++r) {
+          if (s->pinned[gd[r]]) continue;
+          double acc = 0.0;
+          for (int c = 0; c < 24; ++c) acc += s->ke[r * 24 + c] * ue[c];
+          y[gd[r]] += acc;
+        }
+      }
+  for (size_t d = 0; d < s->nd; ++d)
+    if (s->pinned[d]) y[d] = u[d];
+}
+
+int or_homogenize(int nx, int ny, int nz, double h, double E, double nu, const uint8_t* solid,
+                  int cases_mask, double cg_tol, int max_it, double* CH, int* iters_max,
+                  int* converged_out) {
+  if (nx < 1 || ny < 1 || nz < 1) return fail(OR_EINVAL, "homogenize: grid dimensions must be >= 1");
+  double ke[576];
+  int st = or_hex8_stiffness(E, nu, h, ke);
+  if (st) return st;
+  const size_t np = (size_t)nx * ny * nz, nd = 3 * np;
+  double chi0[24][6];
+  memset(chi0, 0, sizeof chi0);
+  for (int a = 0; a < 8; ++a) {
+    const double X = kHexOff[a][0] * h, Y = kHexOff[a][1] * h, Z = kHexOff[a][2] * h;
+    chi0[3 * a][0] = X;
+    chi0[3 * a + 1][1] = Y;
+    chi0[3 * a + 2][2] = Z;
+    chi0[3 * a][3] = Y;
+    chi0[3 * a + 1][4] = Z;
+    chi0[3 * a + 2][5] = X;
+  }
+  uint8_t* pinned = malloc(nd);
+  uint8_t* touched = calloc(nd, 1);
+  double* F = calloc(nd * 6, sizeof(double));
+  double* diag = calloc(nd, sizeof(double));
+  homog_sys s = {nx, ny, nz, solid, ke, pinned, nd};
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!is_solid(solid, ((size_t)k * ny + j) * nx + i)) continue;
+        size_t gd[24];
+        homog_gd(&s, i, j, k, gd);
+        for (int r = 0; r < 24; ++r) {
+          touched[gd[r]] = 1;
+          diag[gd[r]] += ke[r * 24 + r];
+          for (int J = 0; J < 6; ++J) {
+            double f = 0.0;
+            for (int c = 0; c < 24; ++c) f += ke[r * 24 + c] * chi0[c][J];
+            F[gd[r] * 6 + J] += f;
+          }
+        }
+      }
+  for (size_t d = 0; d < nd; ++d) pinned[d] = (d < 3) || !touched[d];
+  double* X = calloc(nd * 6, sizeof(double));
+  double* b = malloc(nd * sizeof(double));
+  double* x = malloc(nd * sizeof(double));
+  double* r = malloc(nd * sizeof(double));
+  double* p = malloc(nd * sizeof(double));
+  double* z = malloc(nd * sizeof(double));
+  double* t = malloc(nd * sizeof(double));
+  const long cap = (long)(2 * nd) < 200000 ? (long)(2 * nd) : 200000;
+  const int maxIters = max_it > 0 ? max_it : (int)cap;
+  int itmax = 0, conv = 1;
+  for (int J = 0; J < 6; ++J) {
+    if (!((cases_mask >> J) & 1)) continue;
+    for (size_t d = 0; d < nd; ++d) {
+      b[d] = pinned[d] ? 0.0 : F[d * 6 + J];
+      x[d] = 0.0;
+    }
+    double rhs2 = 0.0;
+    for (size_t d = 0; d < nd; ++d) rhs2 += b[d] * b[d];
+    int it = 0;
+    if (rhs2 > 0.0) {
+      double threshold = cg_tol * cg_tol * rhs2;
+      if (threshold < DBL_MIN) threshold = DBL_MIN;
+      for (size_t d = 0; d < nd; ++d) r[d] = b[d];
+      double rn2 = rhs2;
+      for (size_t d = 0; d < nd; ++d) p[d] = r[d] / (pinned[d] ? 1.0 : diag[d]);
+      double absNew = 0.0;
+      for (size_t d = 0; d < nd; ++d) absNew += r[d] * p[d];
+      while (it < maxIters) {
+        homog_apply(&s, p, t);
+        double pt = 0.0;
+        for (size_t d = 0; d < nd; ++d) pt += p[d] * t[d];
+        const double alpha = absNew / pt;
+        for (size_t d = 0; d < nd; ++d) {
+          x[d] += alpha * p[d];
+          r[d] -= alpha * t[d];
+        }
+        rn2 = 0.0;
+        for (size_t d = 0; d < nd; ++d) rn2 += r[d] * r[d];
+        if (rn2 < threshold) break;
+        for (size_t d = 0; d < nd; ++d) z[d] = r[d] / (pinned[d] ? 1.0 : diag[d]);
+        const double absOld = absNew;
+        absNew = 0.0;
+        for (size_t d = 0; d < nd; ++d) absNew += r[d] * z[d];
+        const double beta = absNew / absOld;
+        for (size_t d = 0; d < nd; ++d) p[d] = z[d] + beta * p[d];
+        ++it;
+      }
+      if (!(sqrt(rn2 / rhs2) <= cg_tol)) conv = 0;
+    }
+    if (it > itmax) itmax = it;
+    for (size_t d = 0; d < nd; ++d) X[d * 6 + J] = x[d];
+  }
+  memset(CH, 0, 36 * sizeof(double));
+  const double vol = (double)nx * ny * nz * h * h * h;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!is_solid(solid, ((size_t)k * ny + j) * nx + i)) continue;
+        size_t gd[24];
+        homog_gd(&s, i, j, k, gd);
+        for (int J = 0; J < 6; ++J) {
+          if (!((cases_mask >> J) & 1)) continue;
+          double diffJ[24], kd[24];
+          for (int q = 0; q < 24; ++q) diffJ[q] = chi0[q][J] - X[gd[q] * 6 + J];
+          for (int q = 0; q < 24; ++q) {
+            double acc = 0.0;
+            for (int c = 0; c < 24; ++c) acc += ke[q * 24 + c] * diffJ[c];
+            kd[q] = acc;
+          }
+          for (int I = 0; I < 6; ++I) {
+            double acc = 0.0;
+            for (int q = 0; q < 24; ++q) acc += chi0[q][I] * kd[q];
+            CH[I * 6 + J] += acc / vol;
+          }
+        }
+      }
+  if (iters_max) *iters_max = itmax;
+  if (converged_out) *converged_out = conv;
+  free(pinned); free(touched); free(F); free(diag); free(X); free(b); free(x); free(r);
+  free(p); free(z); free(t);
+  return OR_OK;
+}

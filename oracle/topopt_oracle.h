@@ -149,6 +149,15 @@ int or_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tag
                             double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
                             double* design, double* phys, or_simp_result* res);
 
+/* Periodic homogenization of one unit cell (lattice_homog_probe.cpp:290-412):
+ * solid (NULL = all solid) selects the elements, cases_mask the Voigt strain
+ * columns solved (bit J = column J; 0x3F all six), CH receives the 6x6 tensor
+ * row-major (CH[I*6+J]; unsolved columns 0).  Jacobi-PCG at cg_tol, max_it <= 0
+ * = min(2n, 200000). */
+int or_homogenize(int nx, int ny, int nz, double h, double E, double nu, const uint8_t* solid,
+                  int cases_mask, double cg_tol, int max_it, double* CH, int* iters_max,
+                  int* converged);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,7 @@ from ._capi import (  # noqa: F401
     fea_matfree_apply,
     fea_solve_mgcg_matfree,
     hex8_stiffness,
+    homogenize,
     lib,
     library_path,
     make_density_filter,

@@ -136,6 +136,7 @@ def lib():
         "tg_oc_update_masked": ([vp, vp, dbl, vp, vp, dbl, dbl, dbl, vp], C.c_int),
         "tg_simp_optimize_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, _PROGRESS, vp, vp, vp, vp,
                                      vp, vp], C.c_int),
+        "tg_homogenize": ([i32, i32, i32, i32, dbl, dbl, dbl, vp, i32, dbl, i32, vp, vp], C.c_int),
         "tg_job_create": ([vp, vp, vp, i32, vp, i32, vp, vp], C.c_int),
         "tg_job_create_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_job_step": ([vp, vp], C.c_int),
@@ -433,6 +434,33 @@ def oc_update_masked(pb: Problem, radius, mask, density, dcompliance, volume_fra
     _check(lib().tg_oc_update_masked(C.byref(pb._grid), _p(m), float(radius), _p(d), _p(dc),
                                      volume_fraction, move, density_min, _p(out)))
     return out
+
+
+class _HomogInfo(C.Structure):
+    _fields_ = [("iterations_max", C.c_int32), ("converged", C.c_int32), ("systems", C.c_int32),
+                ("iterations_total", C.c_int64), ("t_setup_ms", C.c_double),
+                ("t_solve_ms", C.c_double), ("t_total_ms", C.c_double)]
+
+
+def homogenize(cells, spacing=1.0, youngs_modulus=1.0, poisson=0.3, cases=0x3F, tolerance=1e-9,
+               max_iterations=0, check=True):
+    """Periodic homogenization (lattice_homog_probe.cpp:290-412) of a batch of unit
+    cells: ``cells`` is a uint8 array (ncell, nz, ny, nx) or (nz, ny, nx) of voxel
+    tags (0 = void).  Returns (CH of shape (ncell, 6, 6), info dict)."""
+    t = np.ascontiguousarray(cells, dtype=np.uint8)
+    if t.ndim == 3:
+        t = t[None]
+    if t.ndim != 4:
+        raise ValueError("cells must be (ncell, nz, ny, nx) or (nz, ny, nx)")
+    nc, nz, ny, nx = t.shape
+    ch = np.zeros((nc, 6, 6))
+    info = _HomogInfo()
+    rc = lib().tg_homogenize(nc, nx, ny, nz, spacing, youngs_modulus, poisson, _p(t), cases,
+                             tolerance, max_iterations, _p(ch), C.byref(info))
+    d = {f[0]: getattr(info, f[0]) for f in _HomogInfo._fields_}
+    if check or rc != TG_ENONCONV:
+        _check(rc)
+    return ch, d
 
 
 def kernel_launches() -> int:

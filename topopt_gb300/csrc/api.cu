@@ -43,6 +43,7 @@ double now_ms() {
 }  // namespace
 
 void raise(int code, const std::string& msg) { throw Error(code, msg); }
+int device_ordinal() { return g_device; }
 void set_last_error(const std::string& msg) { g_err = msg; }
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 

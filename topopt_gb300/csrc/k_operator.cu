@@ -23,6 +23,8 @@
 // per-node summation order is fixed -- the apply is deterministic run to run.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "tg_internal.h"
 
 namespace tg {
@@ -184,6 +186,19 @@ struct GridDev {
   int nx, ny, nz, nnx, nny, nnz;
 };
 
+// Batched periodic applies (homogenization): system bi of the batch reads x, b,
+// y at bi * sx and the cell fields (factors, kept mask, inverse diagonal) of
+// cell bi / nrhs.  On the torus nodes and elements coincide (nnx == nx ...).
+struct BatchDev {
+  int nrhs, nzc;         // systems per cell; z-chunks per system
+  int64_t sx, se, sk;    // strides: DOF vectors, element factors, per-cell DOF fields
+};
+
+__device__ __forceinline__ int wrap_index(int a, int n) {
+  a %= n;
+  return a < 0 ? a + n : a;
+}
+
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double red[32];
 #pragma unroll
@@ -224,10 +239,15 @@ struct Pencil<float> {
   static constexpr int PY = 8, KZ = 16, MINB = 3;
 };
 
-template <class T>
+template <class T, bool PER = false>
 __device__ __forceinline__ void load_node(const GridDev& g, const T* __restrict__ x, int a, int b,
                                           int c, T (&v)[3]) {
-  if (a >= 0 && a < g.nnx && b >= 0 && b < g.nny && c >= 0 && c < g.nnz) {
+  if (PER) {
+    a = wrap_index(a, g.nnx);
+    b = wrap_index(b, g.nny);
+    c = wrap_index(c, g.nnz);
+  }
+  if (PER || (a >= 0 && a < g.nnx && b >= 0 && b < g.nny && c >= 0 && c < g.nnz)) {
     const T* p = x + 3 * ((int64_t(c) * g.nny + b) * g.nnx + a);
     v[0] = p[0];
     v[1] = p[1];
@@ -240,14 +260,14 @@ __device__ __forceinline__ void load_node(const GridDev& g, const T* __restrict_
 // Raw loads of layer c for the lane's own column: nodes (ex, ey, c), (ex, ey+1, c)
 // and, for lane 31, (ex+1, ey, c), (ex+1, ey+1, c).  Issued one step ahead so
 // their latency overlaps the current layer's arithmetic.
-template <class T>
+template <class T, bool PER = false>
 __device__ __forceinline__ void load_raw(const GridDev& g, const T* __restrict__ x, int ex, int ey,
                                          int c, int lane, T (&r)[2][2][3]) {
-  load_node(g, x, ex, ey, c, r[0][0]);
-  load_node(g, x, ex, ey + 1, c, r[1][0]);
+  load_node<T, PER>(g, x, ex, ey, c, r[0][0]);
+  load_node<T, PER>(g, x, ex, ey + 1, c, r[1][0]);
   if (lane == 31) {
-    load_node(g, x, ex + 1, ey, c, r[0][1]);
-    load_node(g, x, ex + 1, ey + 1, c, r[1][1]);
+    load_node<T, PER>(g, x, ex + 1, ey, c, r[0][1]);
+    load_node<T, PER>(g, x, ex + 1, ey + 1, c, r[1][1]);
   }
 }
 
@@ -265,31 +285,47 @@ __device__ __forceinline__ void finish_layer(int lane, const T (&r)[2][2][3], T 
     }
 }
 
-template <class T, int PY, int KZ, int MINB, int MODE>
+// PER: the periodic (torus) grid of a batch of systems (BatchDev); nodes and
+// elements wrap around, so every element exists and the halo lanes read the
+// opposite face.  The non-periodic instantiations compile the PER branches away.
+template <class T, int PY, int KZ, int MINB, int MODE, bool PER = false>
 __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> mc,
                                                      const T* __restrict__ ef,
                                                      const uint8_t* __restrict__ kept,
                                                      const T* __restrict__ x, const T* __restrict__ b,
                                                      const T* __restrict__ invdiag, T omega,
-                                                     T* __restrict__ y, double* __restrict__ dot_part) {
+                                                     T* __restrict__ y, double* __restrict__ dot_part,
+                                                     BatchDev bd = BatchDev{}) {
   __shared__ T sy[2][PY][6][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int ex = blockIdx.x * 31 - 1 + lane;
   const int ey = blockIdx.y * (PY - 1) - 1 + w;
-  const int k0 = blockIdx.z * KZ;
+  int k0 = blockIdx.z * KZ;
+  if (PER) {
+    const int bi = blockIdx.z / bd.nzc, cell = bi / bd.nrhs;
+    k0 = (blockIdx.z - bi * bd.nzc) * KZ;
+    x += bi * bd.sx;
+    y += bi * bd.sx;
+    if (b) b += bi * bd.sx;
+    ef += cell * bd.se;
+    if (kept) kept += cell * bd.sk;
+    if (invdiag) invdiag += cell * bd.sk;
+  }
   const bool own_xy = lane >= 1 && w >= 1 && ex < g.nnx && ey < g.nny;
-  const bool exy_ok = ex >= 0 && ex < g.nx && ey >= 0 && ey < g.ny;
+  const bool exy_ok = PER || (ex >= 0 && ex < g.nx && ey >= 0 && ey < g.ny);
+  const int64_t exy = PER ? int64_t(wrap_index(ey, g.ny)) * g.nx + wrap_index(ex, g.nx)
+                          : int64_t(ey) * g.nx + ex;
   T cur[2][2][3], nxt[2][2][3], raw[2][2][3];
-  load_raw(g, x, ex, ey, k0 - 1, lane, raw);
+  load_raw<T, PER>(g, x, ex, ey, k0 - 1, lane, raw);
   finish_layer(lane, raw, cur);
-  load_raw(g, x, ex, ey, k0, lane, raw);
+  load_raw<T, PER>(g, x, ex, ey, k0, lane, raw);
   T pend[3] = {T(0), T(0), T(0)};
   double dsum = 0.0;
 #pragma unroll 1
   for (int s = 0; s <= KZ; ++s) {
     const int ez = k0 - 1 + s;
     finish_layer(lane, raw, nxt);
-    if (s < KZ) load_raw(g, x, ex, ey, ez + 2, lane, raw);
+    if (s < KZ) load_raw<T, PER>(g, x, ex, ey, ez + 2, lane, raw);
     T ux[8], uy[8], uz[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -298,7 +334,11 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
       uy[c] = zb ? nxt[yb][xb][1] : cur[yb][xb][1];
       uz[c] = zb ? nxt[yb][xb][2] : cur[yb][xb][2];
     }
-    const T f = (exy_ok && ez >= 0 && ez < g.nz) ? ef[(int64_t(ez) * g.ny + ey) * g.nx + ex] : T(0);
+    T f;
+    if (PER)
+      f = ef[int64_t(wrap_index(ez, g.nz)) * g.ny * g.nx + exy];
+    else
+      f = (exy_ok && ez >= 0 && ez < g.nz) ? ef[int64_t(ez) * g.ny * g.nx + exy] : T(0);
     if (f != T(0)) {
       modal_apply(mc, f, ux, uy, uz);
     } else {
@@ -412,6 +452,56 @@ template void launch_fine_op<double>(int, const Grid&, const ModalConsts&, const
 template void launch_fine_op<float>(int, const Grid&, const ModalConsts&, const float*,
                                     const uint8_t*, const float*, const float*, const float*,
                                     float, float*, double*, int*, cudaStream_t);
+
+// Periodic batched apply: nsys systems on the nx*ny*nz torus; system bi uses
+// x/b/y at bi*ndof and the factors / kept mask / inverse diagonal of cell
+// bi / nrhs.  dot_part (kApply) receives one partial of x.y per CTA, the CTAs of
+// a system contiguous: periodic_op_blocks() per system.
+int periodic_op_blocks(int nx, int ny, int nz) {
+  using P = Pencil<double>;
+  return ((nx + 30) / 31) * ((ny + P::PY - 2) / (P::PY - 1)) * ((nz + P::KZ - 1) / P::KZ);
+}
+
+template <int MODE>
+static void launch_periodic_mode(int nx, int ny, int nz, const ModalConsts& c, const double* ef,
+                                 const uint8_t* kept, const double* x, const double* b,
+                                 const double* invdiag, double omega, double* y, double* dot_part,
+                                 int nsys, int nrhs, cudaStream_t s) {
+  using P = Pencil<double>;
+  const GridDev gd{nx, ny, nz, nx, ny, nz};
+  const int nzc = (nz + P::KZ - 1) / P::KZ;
+  const int64_t ndof = 3 * int64_t(nx) * ny * nz, nv = int64_t(nx) * ny * nz;
+  // gridDim.z <= 65535: whole cells per launch.
+  const int cells_per = std::max(1, 65535 / (nzc * nrhs));
+  const int ncell = nsys / nrhs;
+  for (int c0 = 0; c0 < ncell; c0 += cells_per) {
+    const int nc = std::min(cells_per, ncell - c0);
+    const int64_t s0 = int64_t(c0) * nrhs;
+    const BatchDev bd{nrhs, nzc, ndof, nv, ndof};
+    const dim3 grid((nx + 30) / 31, (ny + P::PY - 2) / (P::PY - 1), nzc * nc * nrhs);
+    k_fine_op<double, P::PY, P::KZ, P::MINB, MODE, true><<<grid, 32 * P::PY, 0, s>>>(
+        gd, to_modal<double>(c), ef + c0 * nv, kept ? kept + c0 * ndof : nullptr,
+        x + s0 * ndof, b ? b + s0 * ndof : nullptr, invdiag ? invdiag + c0 * ndof : nullptr, omega,
+        y + s0 * ndof,
+        dot_part ? dot_part + s0 * periodic_op_blocks(nx, ny, nz) : nullptr, bd);
+    TG_LAUNCH_CHECK();
+  }
+}
+
+void launch_periodic_op(int mode, int nx, int ny, int nz, const ModalConsts& c, const double* ef,
+                        const uint8_t* kept, const double* x, const double* b,
+                        const double* invdiag, double omega, double* y, double* dot_part,
+                        int nsys, int nrhs, cudaStream_t s) {
+  if (mode == kApply)
+    launch_periodic_mode<kApply>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part, nsys,
+                                 nrhs, s);
+  else if (mode == kResidual)
+    launch_periodic_mode<kResidual>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part,
+                                    nsys, nrhs, s);
+  else
+    launch_periodic_mode<kSmooth>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part,
+                                  nsys, nrhs, s);
+}
 
 // diag(A) at every DOF = kdiag * (sum of the adjacent element factors), summed
 // in a fixed element order; invdiag = 1/diag on kept DOFs, 0 elsewhere

@@ -28,6 +28,7 @@ struct Error : std::runtime_error {
 
 [[noreturn]] void raise(int code, const std::string& msg);
 void set_last_error(const std::string& msg);
+int device_ordinal();  // the device tg_set_device selected (0 by default)
 void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
 #define TG_CUDA(call)                                                  \
@@ -115,6 +116,13 @@ void launch_fine_op(int mode, const Grid& g, const ModalConsts& mc, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
                     T* y, double* dot_part, int* nblocks_out, cudaStream_t s);
 int fine_op_blocks(const Grid& g, bool fp64);
+// Batched FP64 apply on the periodic nx*ny*nz torus (nodes = elements per axis);
+// see k_operator.cu.
+int periodic_op_blocks(int nx, int ny, int nz);
+void launch_periodic_op(int mode, int nx, int ny, int nz, const ModalConsts& c, const double* ef,
+                        const uint8_t* kept, const double* x, const double* b,
+                        const double* invdiag, double omega, double* y, double* dot_part,
+                        int nsys, int nrhs, cudaStream_t s);
 
 // Jacobi diagonal of the fine operator: diag = kdiag * sum of adjacent factors.
 void launch_fine_invdiag(const Grid& g, double kdiag, const double* ef, const uint8_t* kept,
