@@ -260,6 +260,51 @@ int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, double spac
                   int32_t cases_mask, double tolerance, int32_t max_iterations,
                   double* ch_out, tg_homog_info* info);
 
+/* ---- serving: continuous batching of optimisation jobs ----
+ * No reference counterpart as one interface: the GB300 form of the callers that
+ * run simp_optimize once per request (minimize_plastic, the app bridge,
+ * TopOptBridge.hpp:262-269).  Jobs queue in arrival order and are admitted,
+ * head first, when a slot is free and their device-memory estimate
+ * (tg_job_estimate_bytes) fits in the remaining HBM budget; each admitted job
+ * runs tg_simp_optimize(_masked) on its own worker thread and CUDA stream, so
+ * the jobs in flight overlap on the GPU, and a job's result is the same alone
+ * and in the mix. */
+typedef struct tg_server tg_server;
+typedef struct {
+  int64_t hbm_budget_bytes; /* admission budget: sum of the admitted jobs' estimates */
+  int32_t max_active;       /* concurrent jobs (worker threads), >= 1 */
+  int32_t device;           /* CUDA device ordinal */
+} tg_server_config;
+typedef struct {
+  int64_t ticket;
+  int32_t status;           /* the job's tg_simp_optimize status */
+  int64_t estimate_bytes;
+  double t_queue_ms;        /* submission to admission */
+  double t_run_ms;          /* admission to completion */
+  double t_latency_ms;      /* submission to completion */
+  tg_simp_result result;
+} tg_server_result;
+typedef struct {
+  int64_t submitted, admitted, completed, rejected, queued;
+  int32_t active, peak_active;
+  int64_t bytes_in_use, peak_bytes;
+  double uptime_ms, busy_ms; /* busy: time with at least one job running */
+} tg_server_counters;
+
+int tg_server_create(const tg_server_config* cfg, tg_server** out);
+/* Copies the problem; TG_ENOMEM when its estimate exceeds the whole budget. */
+int tg_server_submit(tg_server* server, const tg_grid* grid, const tg_simp_params* params,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                     int64_t* ticket_out);
+/* Blocks until the job is done; returns its status and releases the ticket.
+ * design_out / phys_out (voxels) may be NULL. */
+int tg_server_wait(tg_server* server, int64_t ticket, tg_server_result* out,
+                   double* design_out, double* phys_out);
+int tg_server_stats(tg_server* server, tg_server_counters* out);
+/* Drops queued jobs, waits for the admitted ones, frees the server. */
+void tg_server_destroy(tg_server* server);
+
 /* ---- resident jobs: state stays on the device between design iterations ---- */
 typedef struct tg_job tg_job;
 

@@ -19,6 +19,7 @@ from ._capi import (  # noqa: F401
     DeviceError,
     LibraryMissing,
     Problem,
+    Server,
     SimpJob,
     SimpParams,
     SimpOptions,
@@ -31,6 +32,7 @@ from ._capi import (  # noqa: F401
     fea_matfree_apply,
     fea_solve_mgcg_matfree,
     hex8_stiffness,
+    job_estimate_bytes,
     homogenize,
     lib,
     library_path,

@@ -137,6 +137,11 @@ def lib():
         "tg_simp_optimize_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, _PROGRESS, vp, vp, vp, vp,
                                      vp, vp], C.c_int),
         "tg_homogenize": ([i32, i32, i32, i32, dbl, dbl, dbl, vp, i32, dbl, i32, vp, vp], C.c_int),
+        "tg_server_create": ([vp, vp], C.c_int),
+        "tg_server_submit": ([vp, vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
+        "tg_server_wait": ([vp, C.c_int64, vp, vp, vp], C.c_int),
+        "tg_server_stats": ([vp, vp], C.c_int),
+        "tg_server_destroy": ([vp], None),
         "tg_job_create": ([vp, vp, vp, i32, vp, i32, vp, vp], C.c_int),
         "tg_job_create_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_job_step": ([vp, vp], C.c_int),
@@ -506,6 +511,80 @@ def simp_optimize(pb: Problem, params: SimpParams, options: SimpOptions, progres
                 iterations=res.iterations, converged=bool(res.converged),
                 cancelled=bool(res.cancelled), infeasible=bool(res.infeasible),
                 non_convergent=bool(res.non_convergent), history=_rows(hist, res.iterations))
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_active", C.c_int32), ("device", C.c_int32)]
+
+
+class _ServerResult(C.Structure):
+    _fields_ = [("ticket", C.c_int64), ("status", C.c_int32), ("estimate_bytes", C.c_int64),
+                ("t_queue_ms", C.c_double), ("t_run_ms", C.c_double),
+                ("t_latency_ms", C.c_double), ("result", _Result)]
+
+
+class _ServerCounters(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
+                ("rejected", C.c_int64), ("queued", C.c_int64), ("active", C.c_int32),
+                ("peak_active", C.c_int32), ("bytes_in_use", C.c_int64),
+                ("peak_bytes", C.c_int64), ("uptime_ms", C.c_double), ("busy_ms", C.c_double)]
+
+
+class Server:
+    """Continuous batching of optimisation jobs (tg_server_*): jobs are admitted
+    in arrival order by HBM budget and free slots, each runs resident on its own
+    stream, and their work overlaps on the GPU."""
+
+    def __init__(self, hbm_budget_bytes: int, max_active: int = 8, device: int = 0):
+        cfg = _ServerConfig(int(hbm_budget_bytes), int(max_active), int(device))
+        self._h = C.c_void_p()
+        _check(lib().tg_server_create(C.byref(cfg), C.byref(self._h)))
+        self._nv = {}
+
+    def submit(self, pb: Problem, params: SimpParams, options: SimpOptions, mask=None) -> int:
+        prm, opt = params._c(), options._c()
+        m = None if mask is None else _mask(pb, mask)
+        t = C.c_int64(0)
+        g, b, nb, l, nl = pb._args()
+        _check(lib().tg_server_submit(self._h, g, C.byref(prm), b, nb, l, nl, C.byref(opt), _p(m),
+                                      C.byref(t)))
+        self._nv[t.value] = pb.nv
+        return t.value
+
+    def wait(self, ticket: int, fields=True):
+        nv = self._nv.pop(ticket)
+        r = _ServerResult()
+        design, phys = (np.zeros(nv), np.zeros(nv)) if fields else (None, None)
+        rc = lib().tg_server_wait(self._h, ticket, C.byref(r), _p(design), _p(phys))
+        _check(rc)
+        res = r.result
+        return dict(ticket=r.ticket, estimate_bytes=r.estimate_bytes, t_queue_ms=r.t_queue_ms,
+                    t_run_ms=r.t_run_ms, t_latency_ms=r.t_latency_ms, design=design,
+                    physical_density=phys, compliance=res.compliance,
+                    volume_fraction=res.volume_fraction, iterations=res.iterations,
+                    converged=bool(res.converged), non_convergent=bool(res.non_convergent),
+                    infeasible=bool(res.infeasible))
+
+    def stats(self):
+        c = _ServerCounters()
+        _check(lib().tg_server_stats(self._h, C.byref(c)))
+        return {f[0]: getattr(c, f[0]) for f in _ServerCounters._fields_}
+
+    def close(self):
+        if self._h:
+            lib().tg_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def job_estimate_bytes(pb: Problem, options: SimpOptions) -> int:
+    opt = options._c()
+    return int(lib().tg_job_estimate_bytes(C.byref(pb._grid), C.byref(opt)))
 
 
 class SimpJob:
