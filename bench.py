@@ -19,6 +19,21 @@ vectors alone are 100 MB each), so no L2 flush is needed.
 --impl reference times the CPU implementation of the same step on the host
 cores: the oracle's C restatement of the reference (the reference tree itself is
 not present on the GPU host), measured on a bounded sample and scaled.
+
+Secondary workloads (--workload; one JSON line each, not the headline):
+  batch  -- 64 seeded designs of the batched workload (nx in [32,128], ny, nz in
+            [16,64]) run concurrently through the serving loop, mixed precision;
+            value = aggregate design iterations/s; beside it the plain FP64 form
+            one design at a time on a sample of the same designs.
+  homog  -- periodic homogenization of 512 seeded 32^3 gyroid/octet cells at
+            relative densities U[0.1, 0.4], six strain columns each, tol 1e-8,
+            mixed precision; value = cells/s; the FP64 form on a sample of the
+            cells beside it, with the tensors' relative difference.
+  serve  -- an open-loop Poisson stream (4 jobs/s, --serve-seconds of arrivals;
+            the reference's 10-minute stream is shortened so the run stays within
+            minutes) of jobs log-uniform between 24^3 and 192x96x96 elements, 40
+            design iterations each, 150 GB HBM budget; p50/p99 latency, jobs/s and
+            GPU occupancy, beside the plain FP64 one-at-a-time service time.
 """
 from __future__ import annotations
 
@@ -364,6 +379,129 @@ def run_op_only(args):
     print(json.dumps({"op_only": args.op_only, "checksum": float(np.abs(y).sum())}))
 
 
+# ------------------------------------------------------ secondary workloads
+def _pctl(v, q):
+    return float(np.percentile(np.asarray(v, dtype=float), q)) if len(v) else None
+
+
+def run_batch(args):
+    import topopt_gb300 as tg
+    from topopt_gb300 import workloads
+    from topopt_gb300.build import build
+    build()
+    K = args.steps
+    jobs = [workloads.design(s, precision=tg.PREC_MIXED, iterations=K) for s in range(64)]
+    # Warm-up: one small job through the library.
+    pb, prm, opt = workloads.design(999, iterations=2, sizes=(32, 16, 16))
+    tg.simp_optimize(pb, prm, opt)
+    srv = tg.Server(hbm_budget_bytes=150 << 30, max_active=args.max_active)
+    with ClockSampler(0) as cs:
+        t0 = time.perf_counter()
+        tickets = [srv.submit(pb, prm, opt) for pb, prm, opt in jobs]
+        res = [srv.wait(t, fields=False) for t in tickets]
+        wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    iters = sum(r["iterations"] for r in res)
+    # Plain FP64, one design at a time, on a sample.
+    sample = [workloads.design(s, precision=tg.PREC_FP64, iterations=K) for s in range(4)]
+    t0 = time.perf_counter()
+    for pb, prm, opt in sample:
+        tg.simp_optimize(pb, prm, opt)
+    t64 = time.perf_counter() - t0
+    line = {"metric": "design_iters_per_s", "value": iters / wall, "unit": "design_iters/s",
+            "n_gpus": 1, "steps": K, "warmup": 1, "higher_is_better": True, "dtype": "f32+f64",
+            "data": "synthetic (64 seeded designs)", "impl": "ours",
+            "config": {"workload": "batched SIMP, 64 designs, nx in [32,128], ny,nz in [16,64]",
+                       "elements_total": int(sum(pb.nv for pb, _, _ in jobs)),
+                       "form": "mixed, concurrent resident jobs (serving loop)",
+                       "max_active": args.max_active},
+            "wall_s": wall, "clocks": cs.summary(), "server": st,
+            "fp64_one_at_a_time": {"design_iters_per_s": 4 * K / t64, "designs": 4},
+            "speedup_vs_fp64_one_at_a_time": (iters / wall) / (4 * K / t64)}
+    print(json.dumps(line), flush=True)
+
+
+def run_homog(args):
+    import topopt_gb300 as tg
+    from topopt_gb300 import lattice
+    from topopt_gb300.build import build
+    build()
+    cells, meta = lattice.batch(args.cells, vpc=32, seed=0)
+    tg.homogenize(cells[:1], tolerance=1e-8, precision=tg.PREC_MIXED)  # warm-up
+    with ClockSampler(0) as cs:
+        t0 = time.perf_counter()
+        ch32, info = tg.homogenize(cells, tolerance=1e-8, precision=tg.PREC_MIXED)
+        wall = time.perf_counter() - t0
+    ns = min(args.cells, 32)
+    t0 = time.perf_counter()
+    ch64, info64 = tg.homogenize(cells[:ns], tolerance=1e-8, precision=tg.PREC_FP64)
+    t64 = time.perf_counter() - t0
+    err = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(ch32[:ns], ch64))
+    line = {"metric": "cells_per_s", "value": args.cells / wall, "unit": "cells/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32+f64", "impl": "ours",
+            "data": "synthetic (seeded gyroid/octet cells)",
+            "config": {"workload": f"periodic homogenization, {args.cells} cells of 32^3, 6 strains",
+                       "tol": 1e-8, "solver": "batched Jacobi-PCG (FP32 inner, FP64 refinement)"},
+            "wall_s": wall, "clocks": cs.summary(), "info": info,
+            "fp64": {"cells_per_s": ns / t64, "cells": ns, "info": info64},
+            "ch_rel_err_mixed_vs_fp64": err,
+            "mean_density": float(np.mean([m[2] for m in meta]))}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    import threading
+    import topopt_gb300 as tg
+    from topopt_gb300 import workloads
+    from topopt_gb300.build import build
+    build()
+    stream = workloads.stream(0, rate=4.0, duration=args.serve_seconds, precision=tg.PREC_MIXED)
+    pb, prm, opt = workloads.design(999, iterations=2, sizes=(32, 16, 16))
+    tg.simp_optimize(pb, prm, opt)  # warm-up
+    srv = tg.Server(hbm_budget_bytes=150 << 30, max_active=args.max_active)
+    tickets = []
+    with ClockSampler(0) as cs:
+        t0 = time.perf_counter()
+
+        def feeder():
+            for at, pb, prm, opt in stream:
+                d = at - (time.perf_counter() - t0)
+                if d > 0:
+                    time.sleep(d)
+                tickets.append(srv.submit(pb, prm, opt))
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        res = [srv.wait(t, fields=False) for t in tickets]
+        wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = [r["t_latency_ms"] for r in res]
+    # The plain FP64 form, one job at a time, on a sample of the same stream.
+    sample = [(p, q, o) for _, p, q, o in stream[:6]]
+    t1 = time.perf_counter()
+    for p, q, o in sample:
+        o.solve = tg.SolveOptions(precision=tg.PREC_FP64)
+        tg.simp_optimize(p, q, o)
+    svc64 = (time.perf_counter() - t1) / len(sample)
+    line = {"metric": "p50_p99_job_latency_ms", "value": _pctl(lat, 50), "p99_ms": _pctl(lat, 99),
+            "unit": "ms", "n_gpus": 1, "higher_is_better": False, "dtype": "f32+f64",
+            "impl": "ours", "data": "synthetic (seeded Poisson job stream)",
+            "config": {"workload": "serving: Poisson 4 jobs/s, 24^3..192x96x96, 40 iterations",
+                       "arrival_seconds": args.serve_seconds, "jobs": len(stream),
+                       "hbm_budget_gb": 150, "max_active": args.max_active},
+            "jobs_per_s": len(res) / wall, "wall_s": wall,
+            "gpu_occupancy": st["busy_ms"] / st["uptime_ms"] if st["uptime_ms"] else None,
+            "queue_ms_p50": _pctl([r["t_queue_ms"] for r in res], 50),
+            "queue_ms_p99": _pctl([r["t_queue_ms"] for r in res], 99),
+            "server": st, "clocks": cs.summary(),
+            "fp64_one_at_a_time": {"mean_service_s": svc64, "jobs_per_s": 1.0 / svc64,
+                                   "sample_jobs": len(sample)}}
+    print(json.dumps(line), flush=True)
+
+
 def _phys_of(tg, pb, design):
     return tg.make_density_filter(pb, 1.5).filter_density(design)
 
@@ -385,7 +523,20 @@ def main():
                     help="profiling aid: run only the fine operator (fea_matfree_apply) 3 times")
     ap.add_argument("--profile", action="store_true",
                     help="profiling aid: allow warmup < 3, skip e2e and the CPU baseline")
+    ap.add_argument("--workload", choices=["cantilever", "batch", "homog", "serve"],
+                    default="cantilever")
+    ap.add_argument("--cells", type=int, default=512)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--max-active", type=int, default=16)
     args = ap.parse_args()
+    if args.workload != "cantilever":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "secondary workloads are GPU-only; the CPU baseline is reported on "
+                              "the cantilever workload"}), flush=True)
+            return
+        {"batch": run_batch, "homog": run_homog, "serve": run_serve}[args.workload](args)
+        return
     if args.op_only:
         run_op_only(args)
         return

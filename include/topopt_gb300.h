@@ -240,7 +240,8 @@ typedef struct {
   int32_t iterations_max;    /* largest CG iteration count over the batch */
   int32_t converged;         /* 1 when every system met the tolerance */
   int32_t systems;           /* cells x solved strain columns */
-  int64_t iterations_total;  /* sum of the CG iteration counts */
+  int64_t iterations_total;  /* sum of the CG iteration counts (inner ones, mixed) */
+  int32_t refinements;       /* mixed: FP64 refinement steps */
   double t_setup_ms, t_solve_ms, t_total_ms;
 } tg_homog_info;
 
@@ -251,14 +252,16 @@ typedef struct {
  * voids carry no element), Hex8 elements of modulus E, Poisson nu, edge
  * spacing.  cases_mask selects the Voigt strain columns [xx,yy,zz,gxy,gyz,gzx]
  * solved (bit J; 0x3F = all six).  Each system is solved by Jacobi-PCG to
- * |r| < tolerance |b| (max_iterations <= 0: min(2 ndof, 200000)).  ch_out
+ * |r| < tolerance |b| (max_iterations <= 0: min(2 ndof, 200000)); precision
+ * TG_PREC_MIXED runs FP32 inner Jacobi-PCG solves (relative 1e-3) inside FP64
+ * iterative refinement judged on the FP64 residual.  ch_out
  * receives ncell 6x6 tensors, row-major, CH[I][J] filled for the solved
  * columns J (others 0).  TG_ENONCONV when a system missed the tolerance (the
  * tensors are still written). */
 int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, double spacing,
                   double youngs_modulus, double poisson, const uint8_t* tags,
                   int32_t cases_mask, double tolerance, int32_t max_iterations,
-                  double* ch_out, tg_homog_info* info);
+                  int32_t precision, double* ch_out, tg_homog_info* info);
 
 /* ---- serving: continuous batching of optimisation jobs ----
  * No reference counterpart as one interface: the GB300 form of the callers that

@@ -87,3 +87,17 @@ def test_gpu_homogenize_errors(tg):
         tg.homogenize(np.ones((4, 4, 4), np.uint8), cases=0x40)
     with pytest.raises(tg.SolverNonConvergence):
         tg.homogenize(np.ones((6, 6, 6), np.uint8), tolerance=1e-14, max_iterations=2)
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_matches_fp64(tg):
+    """Mixed precision (FP32 inner Jacobi-PCG, FP64 refinement on the FP64
+    residual) reaches the same tolerance: tensors agree with the FP64 form."""
+    cells, _ = lattice.batch(4, vpc=16, seed=9)
+    c64, i64 = tg.homogenize(cells, tolerance=1e-10)
+    c32, i32 = tg.homogenize(cells, tolerance=1e-10, precision=tg.PREC_MIXED)
+    assert i64["converged"] and i32["converged"] and i32["refinements"] >= 2
+    for a, b in zip(c32, c64):
+        assert relerr(a, b) < 1e-8
+    solo, _ = tg.homogenize(cells[1], tolerance=1e-10, precision=tg.PREC_MIXED)
+    assert np.array_equal(solo[0], c32[1])

@@ -136,7 +136,8 @@ def lib():
         "tg_oc_update_masked": ([vp, vp, dbl, vp, vp, dbl, dbl, dbl, vp], C.c_int),
         "tg_simp_optimize_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, _PROGRESS, vp, vp, vp, vp,
                                      vp, vp], C.c_int),
-        "tg_homogenize": ([i32, i32, i32, i32, dbl, dbl, dbl, vp, i32, dbl, i32, vp, vp], C.c_int),
+        "tg_homogenize": ([i32, i32, i32, i32, dbl, dbl, dbl, vp, i32, dbl, i32, i32, vp, vp],
+                          C.c_int),
         "tg_server_create": ([vp, vp], C.c_int),
         "tg_server_submit": ([vp, vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_server_wait": ([vp, C.c_int64, vp, vp, vp], C.c_int),
@@ -443,12 +444,13 @@ def oc_update_masked(pb: Problem, radius, mask, density, dcompliance, volume_fra
 
 class _HomogInfo(C.Structure):
     _fields_ = [("iterations_max", C.c_int32), ("converged", C.c_int32), ("systems", C.c_int32),
-                ("iterations_total", C.c_int64), ("t_setup_ms", C.c_double),
+                ("iterations_total", C.c_int64), ("refinements", C.c_int32),
+                ("t_setup_ms", C.c_double),
                 ("t_solve_ms", C.c_double), ("t_total_ms", C.c_double)]
 
 
 def homogenize(cells, spacing=1.0, youngs_modulus=1.0, poisson=0.3, cases=0x3F, tolerance=1e-9,
-               max_iterations=0, check=True):
+               max_iterations=0, precision=PREC_FP64, check=True):
     """Periodic homogenization (lattice_homog_probe.cpp:290-412) of a batch of unit
     cells: ``cells`` is a uint8 array (ncell, nz, ny, nx) or (nz, ny, nx) of voxel
     tags (0 = void).  Returns (CH of shape (ncell, 6, 6), info dict)."""
@@ -461,7 +463,7 @@ def homogenize(cells, spacing=1.0, youngs_modulus=1.0, poisson=0.3, cases=0x3F, 
     ch = np.zeros((nc, 6, 6))
     info = _HomogInfo()
     rc = lib().tg_homogenize(nc, nx, ny, nz, spacing, youngs_modulus, poisson, _p(t), cases,
-                             tolerance, max_iterations, _p(ch), C.byref(info))
+                             tolerance, max_iterations, precision, _p(ch), C.byref(info))
     d = {f[0]: getattr(info, f[0]) for f in _HomogInfo._fields_}
     if check or rc != TG_ENONCONV:
         _check(rc)

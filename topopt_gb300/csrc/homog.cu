@@ -16,7 +16,9 @@
 // advance in lock step through the batched periodic operator (k_operator.cu,
 // PER instantiation) and batched vector kernels with per-system scalars, and a
 // converged system freezes (its own iteration count and iterate are exactly what
-// a solo solve would give).  The CH sum is evaluated as
+// a solo solve would give).  Mixed precision: FP64 iterative refinement (FP64
+// residual b - A x) around lock-step FP32 Jacobi-PCG inner solves on the
+// unit-norm residual, FP64 dot products throughout.  The CH sum is evaluated as
 //   CH[I][J] = (n_solid chi0_I^T ke chi0_J - F_I . chi_J) / |Y|,
 // the same sum regrouped: sum_e chi0_I^T ke chi_J,e = F_I . chi_J.
 #include <cuda_runtime.h>
@@ -113,19 +115,19 @@ __device__ __forceinline__ double bred(double v, double* sh) {
   return s;
 }
 
-// rr = r.r, rz = r.(D^-1 r) per system (initial residual).
-__global__ void k_b_rr_rz(const double* __restrict__ R, const double* __restrict__ invd,
-                          int64_t nd, int nrhs, double* __restrict__ prr,
-                          double* __restrict__ prz) {
+// rr = r.r, rz = r.(D^-1 r) per system.
+template <class T>
+__global__ void k_b_rr_rz(const T* __restrict__ R, const T* __restrict__ invd, int64_t nd,
+                          int nrhs, double* __restrict__ prr, double* __restrict__ prz) {
   __shared__ double sh[32];
   const int bi = blockIdx.y, P = gridDim.x;
-  const double* r = R + bi * nd;
-  const double* iv = invd + (bi / nrhs) * nd;
+  const T* r = R + bi * nd;
+  const T* iv = invd + (bi / nrhs) * nd;
   double a = 0.0, b = 0.0;
   for (int64_t d = blockIdx.x * int64_t(kT) + threadIdx.x; d < nd; d += int64_t(P) * kT) {
-    const double v = r[d];
+    const double v = double(r[d]);
     a += v * v;
-    b += v * (iv[d] * v);
+    b += v * (double(iv[d]) * v);
   }
   a = bred(a, sh);
   b = bred(b, sh);
@@ -156,47 +158,69 @@ __global__ void k_bsum(const double* __restrict__ part, int P, int B, double* __
   }
 }
 
-// Start: R = F[cell][J], X = 0, P = D^-1 R.
-__global__ void k_b_start(const double* __restrict__ F, const double* __restrict__ invd,
-                          const int* __restrict__ jlist, int64_t nd, int nrhs,
-                          double* __restrict__ X, double* __restrict__ R,
-                          double* __restrict__ Pv) {
+// Start: Bv = R = F[cell][J], X = 0.
+__global__ void k_b_start(const double* __restrict__ F, const int* __restrict__ jlist, int64_t nd,
+                          int nrhs, double* __restrict__ Bv, double* __restrict__ X,
+                          double* __restrict__ R) {
   const int bi = blockIdx.y;
   const int cell = bi / nrhs, J = jlist[bi - cell * nrhs];
   const double* f = F + (int64_t(cell) * 6 + J) * nd;
-  const double* iv = invd + int64_t(cell) * nd;
   for (int64_t d = blockIdx.x * int64_t(kT) + threadIdx.x; d < nd;
        d += int64_t(gridDim.x) * kT) {
     const double r = f[d];
+    Bv[bi * nd + d] = r;
     X[bi * nd + d] = 0.0;
     R[bi * nd + d] = r;
+  }
+}
+
+// Inner start of system bi when it runs (run[bi] != 0): X = 0, P = D^-1 R;
+// with a scale (mixed form) R is first set to float(r64 / |r64|).
+template <class T>
+__global__ void k_b_begin(const double* __restrict__ r64, const double* __restrict__ rn,
+                          const T* __restrict__ invd, int64_t nd, int nrhs,
+                          const int* __restrict__ run, T* __restrict__ X, T* __restrict__ R,
+                          T* __restrict__ Pv) {
+  const int bi = blockIdx.y;
+  if (run && !run[bi]) return;
+  const T* iv = invd + (bi / nrhs) * nd;
+  const double inv = r64 ? 1.0 / rn[bi] : 1.0;
+  for (int64_t d = blockIdx.x * int64_t(kT) + threadIdx.x; d < nd;
+       d += int64_t(gridDim.x) * kT) {
+    const T r = r64 ? T(r64[bi * nd + d] * inv) : R[bi * nd + d];
+    R[bi * nd + d] = r;
+    X[bi * nd + d] = T(0);
     Pv[bi * nd + d] = iv[d] * r;
   }
 }
 
 // Per-system CG state: act 1 = iterating, 0 = converged, 2 = stopped
-// (iteration budget or breakdown).
+// (iteration budget or breakdown), -1 = not run (run[bi] == 0).
 __global__ void k_b_init(int B, const double* __restrict__ rr, const double* __restrict__ rz,
-                         double tol, int* __restrict__ act, int* __restrict__ it,
-                         double* __restrict__ thr, double* __restrict__ rhs2,
-                         double* __restrict__ absn) {
+                         double tol, const int* __restrict__ run, int* __restrict__ act,
+                         int* __restrict__ it, double* __restrict__ thr,
+                         double* __restrict__ rhs2, double* __restrict__ absn) {
   const int bi = blockIdx.x * blockDim.x + threadIdx.x;
   if (bi >= B) return;
+  it[bi] = 0;
+  if (run && !run[bi]) {
+    act[bi] = -1;
+    return;
+  }
   const double b2 = rr[bi];
   double t = tol * tol * b2;
   if (t < DBL_MIN) t = DBL_MIN;
   thr[bi] = t;
   rhs2[bi] = b2;
   absn[bi] = rz[bi];
-  it[bi] = 0;
   act[bi] = (b2 > 0.0 && !(b2 < t)) ? 1 : 0;
 }
 
 // x += alpha p, r -= alpha t for iterating systems (alpha = absNew / p.Ap), with
 // the partials of r.r and r.(D^-1 r) of the updated residual.
-__global__ void k_b_xr(double* __restrict__ X, double* __restrict__ R,
-                       const double* __restrict__ Pv, const double* __restrict__ T,
-                       const double* __restrict__ invd, int64_t nd, int nrhs,
+template <class T>
+__global__ void k_b_xr(T* __restrict__ X, T* __restrict__ R, const T* __restrict__ Pv,
+                       const T* __restrict__ Tv, const T* __restrict__ invd, int64_t nd, int nrhs,
                        const double* __restrict__ absn, const double* __restrict__ pap,
                        const int* __restrict__ act, double* __restrict__ prr,
                        double* __restrict__ prz) {
@@ -205,18 +229,19 @@ __global__ void k_b_xr(double* __restrict__ X, double* __restrict__ R,
   double a = 0.0, b = 0.0;
   if (act[bi] == 1) {
     const double pa = pap[bi];
-    const double alpha = pa > 0.0 ? absn[bi] / pa : 0.0;
-    const double* iv = invd + (bi / nrhs) * nd;
-    double* x = X + bi * nd;
-    double* r = R + bi * nd;
-    const double* p = Pv + bi * nd;
-    const double* t = T + bi * nd;
+    const T alpha = T(pa > 0.0 ? absn[bi] / pa : 0.0);
+    const T* iv = invd + (bi / nrhs) * nd;
+    T* x = X + bi * nd;
+    T* r = R + bi * nd;
+    const T* p = Pv + bi * nd;
+    const T* t = Tv + bi * nd;
     for (int64_t d = blockIdx.x * int64_t(kT) + threadIdx.x; d < nd; d += int64_t(P) * kT) {
       x[d] += alpha * p[d];
-      const double v = r[d] - alpha * t[d];
+      const T v = r[d] - alpha * t[d];
       r[d] = v;
-      a += v * v;
-      b += v * (iv[d] * v);
+      const double vd = double(v);
+      a += vd * vd;
+      b += vd * (double(iv[d]) * vd);
     }
   }
   a = bred(a, sh);
@@ -257,18 +282,50 @@ __global__ void k_b_scalars(int B, const double* __restrict__ rr, const double* 
 }
 
 // p = D^-1 r + beta p for iterating systems.
-__global__ void k_b_p(double* __restrict__ Pv, const double* __restrict__ R,
-                      const double* __restrict__ invd, int64_t nd, int nrhs,
-                      const double* __restrict__ beta, const int* __restrict__ act) {
+template <class T>
+__global__ void k_b_p(T* __restrict__ Pv, const T* __restrict__ R, const T* __restrict__ invd,
+                      int64_t nd, int nrhs, const double* __restrict__ beta,
+                      const int* __restrict__ act) {
   const int bi = blockIdx.y;
   if (act[bi] != 1) return;
-  const double bt = beta[bi];
-  const double* iv = invd + (bi / nrhs) * nd;
-  double* p = Pv + bi * nd;
-  const double* r = R + bi * nd;
+  const T bt = T(beta[bi]);
+  const T* iv = invd + (bi / nrhs) * nd;
+  T* p = Pv + bi * nd;
+  const T* r = R + bi * nd;
   for (int64_t d = blockIdx.x * int64_t(kT) + threadIdx.x; d < nd;
        d += int64_t(gridDim.x) * kT)
     p[d] = iv[d] * r[d] + bt * p[d];
+}
+
+// Mixed form: X64 += |r| * X32 for the systems that ran.
+__global__ void k_b_correct(double* __restrict__ X, const float* __restrict__ Xf,
+                            const double* __restrict__ rn, const int* __restrict__ run,
+                            int64_t nd) {
+  const int bi = blockIdx.y;
+  if (!run[bi]) return;
+  const double sc = rn[bi];
+  for (int64_t d = blockIdx.x * int64_t(kT) + threadIdx.x; d < nd;
+       d += int64_t(gridDim.x) * kT)
+    X[bi * nd + d] += sc * double(Xf[bi * nd + d]);
+}
+
+// Refinement bookkeeping per system: run the inner solve when the FP64
+// residual is above the threshold; rn = |r|.
+__global__ void k_b_refine(int B, const double* __restrict__ rr, const double* __restrict__ thr,
+                           int* __restrict__ run, double* __restrict__ rn,
+                           int* __restrict__ nrun) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi >= B) return;
+  const double v = rr[bi];
+  const int go = (v >= thr[bi] && v > 0.0 && isfinite(v)) ? 1 : 0;
+  run[bi] = go;
+  rn[bi] = sqrt(v);
+  if (go) atomicAdd(nrun, 1);
+}
+
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(kT) + threadIdx.x; i < n; i += int64_t(gridDim.x) * kT)
+    b[i] = float(a[i]);
 }
 
 // Partials of F[cell][I] . X[bi] for I = 0..5 (grid.z = I).
@@ -292,13 +349,92 @@ double now_ms() {
       .count();
 }
 
+// Shapes and per-system scratch of one batched solve.
+struct Batch {
+  int nx, ny, nz, nrhs, B, P;
+  int64_t nd;
+  ModalConsts mc;
+  const uint8_t* kept;
+  cudaStream_t s;
+  DBuf<double> prr, prz, ppap, rr, rz, pap, thr, rhs2, absn, beta, rn;
+  DBuf<int> act, it, nact, run, nrun;
+  int64_t iterations_total = 0;
+  int iterations_max = 0;
+  void init(int B_, int64_t nd_, int P_) {
+    B = B_;
+    nd = nd_;
+    P = P_;
+    const int Pop = std::max(periodic_op_blocks<double>(nx, ny, nz),
+                             periodic_op_blocks<float>(nx, ny, nz));
+    prr.alloc(size_t(B) * P);
+    prz.alloc(size_t(B) * P);
+    ppap.alloc(size_t(B) * Pop);
+    for (DBuf<double>* d : {&rr, &rz, &pap, &thr, &rhs2, &absn, &beta, &rn}) d->alloc(size_t(B));
+    for (DBuf<int>* d : {&act, &it, &run}) d->alloc(size_t(B));
+    nact.alloc(1);
+    nrun.alloc(1);
+  }
+  dim3 g2() const { return dim3(static_cast<unsigned>(P), static_cast<unsigned>(B)); }
+  int sb() const { return (B + 255) / 256; }
+  int wb() const { return (B * 32 + 255) / 256; }
+
+  // Lock-step Jacobi-PCG on A X = R (R holds b on entry; X, P, Tv scratch);
+  // systems with run[bi] == 0 (when run is given) do nothing.  With r64 the
+  // right-hand side is float(r64 / rn) (the mixed inner solve).
+  template <class T>
+  int pcg(T* X, T* R, T* Pv, T* Tv, const T* ef, const T* invd, double tol, int max_it,
+          const int* runp, const double* r64) {
+    k_b_begin<T><<<g2(), kT, 0, s>>>(r64, rn.p, invd, nd, nrhs, runp, X, R, Pv);
+    TG_LAUNCH_CHECK();
+    k_b_rr_rz<T><<<g2(), kT, 0, s>>>(R, invd, nd, nrhs, prr.p, prz.p);
+    TG_LAUNCH_CHECK();
+    k_bsum<<<wb(), 256, 0, s>>>(prr.p, P, B, rr.p, prz.p, rz.p);
+    TG_LAUNCH_CHECK();
+    k_b_init<<<sb(), 256, 0, s>>>(B, rr.p, rz.p, tol, runp, act.p, it.p, thr.p, rhs2.p, absn.p);
+    TG_LAUNCH_CHECK();
+    const int Pop = periodic_op_blocks<T>(nx, ny, nz);
+    int host_nact = B;
+    for (int k = 0; k < max_it && host_nact > 0; ++k) {
+      launch_periodic_op<T>(kApply, nx, ny, nz, mc, ef, kept, Pv, nullptr, nullptr, T(0), Tv,
+                            ppap.p, B, nrhs, s);
+      k_bsum<<<wb(), 256, 0, s>>>(ppap.p, Pop, B, pap.p, nullptr, nullptr);
+      TG_LAUNCH_CHECK();
+      k_b_xr<T><<<g2(), kT, 0, s>>>(X, R, Pv, Tv, invd, nd, nrhs, absn.p, pap.p, act.p, prr.p,
+                                    prz.p);
+      TG_LAUNCH_CHECK();
+      k_bsum<<<wb(), 256, 0, s>>>(prr.p, P, B, rr.p, prz.p, rz.p);
+      TG_LAUNCH_CHECK();
+      TG_CUDA(cudaMemsetAsync(nact.p, 0, sizeof(int), s));
+      k_b_scalars<<<sb(), 256, 0, s>>>(B, rr.p, rz.p, thr.p, pap.p, max_it, act.p, it.p, absn.p,
+                                       beta.p, nact.p);
+      TG_LAUNCH_CHECK();
+      k_b_p<T><<<g2(), kT, 0, s>>>(Pv, R, invd, nd, nrhs, beta.p, act.p);
+      TG_LAUNCH_CHECK();
+      if ((k & 7) == 7) {
+        TG_CUDA(cudaMemcpyAsync(&host_nact, nact.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaStreamSynchronize(s));
+      }
+    }
+    std::vector<int> hit(static_cast<size_t>(B));
+    TG_CUDA(cudaMemcpyAsync(hit.data(), it.p, sizeof(int) * B, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    int mx = 0;
+    for (int v : hit) {
+      iterations_total += v;
+      mx = std::max(mx, v);
+    }
+    iterations_max = std::max(iterations_max, mx);
+    return mx;
+  }
+};
+
 }  // namespace
 }  // namespace tg
 
 extern "C" int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, double spacing,
                              double youngs_modulus, double poisson, const uint8_t* tags,
                              int32_t cases_mask, double tolerance, int32_t max_iterations,
-                             double* ch_out, tg_homog_info* info) {
+                             int32_t precision, double* ch_out, tg_homog_info* info) {
   using namespace tg;
   tg_homog_info inf;
   std::memset(&inf, 0, sizeof inf);
@@ -314,6 +450,8 @@ extern "C" int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, 
     if ((cases_mask & 0x3F) == 0 || (cases_mask & ~0x3F) != 0)
       raise(TG_EINVAL, "homogenize: cases_mask must select strain columns 0..5 (bits 0x3F)");
     if (!(tolerance > 0.0)) raise(TG_EINVAL, "homogenize: tolerance must be > 0");
+    if (precision != TG_PREC_FP64 && precision != TG_PREC_MIXED)
+      raise(TG_EINVAL, "homogenize: unknown precision");
     if (!tags || !ch_out) raise(TG_EINVAL, "homogenize: tags and ch_out must be non-null");
     const int64_t np = int64_t(nx) * ny * nz, nd = 3 * np;
     if (nd > (int64_t(1) << 31) - 1) raise(TG_EINVAL, "homogenize: cell too large");
@@ -334,7 +472,7 @@ extern "C" int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, 
       ~StreamGuard() { cudaStreamDestroy(s); }
     } sg{s};
 
-    // Element matrix, chi0 and the per-corner loads (unit modulus, scaled by E).
+    // Element matrix, chi0 and the per-corner loads (scaled by E).
     std::vector<double> ke(576);
     hex8_ke(1.0, poisson, spacing, ke.data());
     double chi0[24][6];
@@ -363,79 +501,117 @@ extern "C" int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, 
         for (int r = 0; r < 24; ++r) acc += chi0[r][I] * cl.fe[J][r / 3][r % 3];
         c0[I][J] = acc;
       }
-    ModalConsts mc = ModalConsts::make(poisson, spacing);
-    mc.kdiag = ke[0];
     std::vector<int64_t> nsolid(static_cast<size_t>(ncell), 0);
     for (int c = 0; c < ncell; ++c)
       for (int64_t e = 0; e < np; ++e) nsolid[size_t(c)] += tags[c * np + e] != 0;
 
+    Batch bt;
+    bt.nx = nx;
+    bt.ny = ny;
+    bt.nz = nz;
+    bt.nrhs = nrhs;
+    bt.mc = ModalConsts::make(poisson, spacing);
+    bt.mc.kdiag = ke[0];
+    bt.s = s;
     DBuf<uint8_t> dtags, kept;
-    DBuf<double> ef, invd, F, X, R, Pv, T;
+    DBuf<double> ef, invd, F, Bv, X, R, Pv, Tv;
     dtags.alloc(size_t(ncell * np));
     TG_CUDA(cudaMemcpyAsync(dtags.p, tags, size_t(ncell * np), cudaMemcpyHostToDevice, s));
     ef.alloc(size_t(ncell * np));
     kept.alloc(size_t(ncell * nd));
     invd.alloc(size_t(ncell * nd));
     F.alloc(size_t(ncell * 6 * nd));
-    for (DBuf<double>* v : {&X, &R, &Pv, &T}) v->alloc(size_t(B) * size_t(nd));
+    for (DBuf<double>* v : {&Bv, &X, &R}) v->alloc(size_t(B) * size_t(nd));
     const int nb_cell = int(std::min<int64_t>((ncell * np + kT - 1) / kT, 152 * 64));
-    k_homog_cell<<<nb_cell, kT, 0, s>>>(dtags.p, ncell, nx, ny, nz, youngs_modulus, mc.kdiag, cl,
-                                         ef.p, kept.p, invd.p, F.p);
+    k_homog_cell<<<nb_cell, kT, 0, s>>>(dtags.p, ncell, nx, ny, nz, youngs_modulus, bt.mc.kdiag,
+                                         cl, ef.p, kept.p, invd.p, F.p);
     TG_LAUNCH_CHECK();
-
-    // Per-system state.
+    bt.kept = kept.p;
     const int P = int(std::max<int64_t>(1, std::min<int64_t>(64, (nd + kT * 8 - 1) / (kT * 8))));
-    const int Pop = periodic_op_blocks(nx, ny, nz);
-    DBuf<double> prr(size_t(B) * P), prz(size_t(B) * P), ppap(size_t(B) * Pop),
-        pfx(size_t(B) * 6 * P);
-    DBuf<double> rr(B), rz(B), pap(B), thr(B), rhs2(B), absn(B), beta(B), fx(size_t(B) * 6);
-    DBuf<int> act(B), it(B), nact(1), djl(B);
+    bt.init(B, nd, P);
+    DBuf<int> djl(static_cast<size_t>(B));
     std::vector<int> jl_sys(static_cast<size_t>(B));
     for (int bi = 0; bi < B; ++bi) jl_sys[size_t(bi)] = jl[size_t(bi % nrhs)];
     TG_CUDA(cudaMemcpyAsync(djl.p, jl_sys.data(), sizeof(int) * B, cudaMemcpyHostToDevice, s));
-    const int sb = (B + 255) / 256;
-    const int wb = (B * 32 + 255) / 256;
-    const double t_setup0 = now_ms();
-    {
-      const dim3 g(static_cast<unsigned>(P), static_cast<unsigned>(B));
-      k_b_start<<<g, kT, 0, s>>>(F.p, invd.p, djl.p, nd, nrhs, X.p, R.p, Pv.p);
-      TG_LAUNCH_CHECK();
-      k_b_rr_rz<<<g, kT, 0, s>>>(R.p, invd.p, nd, nrhs, prr.p, prz.p);
-      TG_LAUNCH_CHECK();
-      k_bsum<<<wb, 256, 0, s>>>(prr.p, P, B, rr.p, prz.p, rz.p);
-      TG_LAUNCH_CHECK();
-      k_b_init<<<sb, 256, 0, s>>>(B, rr.p, rz.p, tolerance, act.p, it.p, thr.p, rhs2.p, absn.p);
-      TG_LAUNCH_CHECK();
-    }
+    k_b_start<<<bt.g2(), kT, 0, s>>>(F.p, djl.p, nd, nrhs, Bv.p, X.p, R.p);
+    TG_LAUNCH_CHECK();
     TG_CUDA(cudaStreamSynchronize(s));
     inf.t_setup_ms = now_ms() - t0;
     const double ts = now_ms();
-    // Lock-step iterations; the host polls the number of iterating systems every
-    // few iterations (the trajectories do not depend on the polling).
-    int host_nact = B;
-    for (int k = 0; k < max_it && host_nact > 0; ++k) {
-      const dim3 g(static_cast<unsigned>(P), static_cast<unsigned>(B));
-      launch_periodic_op(kApply, nx, ny, nz, mc, ef.p, kept.p, Pv.p, nullptr, nullptr, 0.0, T.p,
-                         ppap.p, B, nrhs, s);
-      k_bsum<<<wb, 256, 0, s>>>(ppap.p, Pop, B, pap.p, nullptr, nullptr);
+    bool all_ok = true;
+    if (precision == TG_PREC_FP64) {
+      Pv.alloc(size_t(B) * size_t(nd));
+      Tv.alloc(size_t(B) * size_t(nd));
+      bt.pcg<double>(X.p, R.p, Pv.p, Tv.p, ef.p, invd.p, tolerance, max_it, nullptr, nullptr);
+      std::vector<double> hrr(static_cast<size_t>(B)), hb2(static_cast<size_t>(B));
+      std::vector<int> hact(static_cast<size_t>(B));
+      TG_CUDA(cudaMemcpyAsync(hrr.data(), bt.rr.p, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+      TG_CUDA(cudaMemcpyAsync(hb2.data(), bt.rhs2.p, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+      TG_CUDA(cudaMemcpyAsync(hact.data(), bt.act.p, sizeof(int) * B, cudaMemcpyDeviceToHost, s));
+      TG_CUDA(cudaStreamSynchronize(s));
+      for (int bi = 0; bi < B; ++bi)
+        if (!(hact[size_t(bi)] == 0 &&
+              (hb2[size_t(bi)] == 0.0 || std::sqrt(hrr[size_t(bi)] / hb2[size_t(bi)]) <= tolerance)))
+          all_ok = false;
+    } else {
+      // FP64 refinement around FP32 inner solves (relative 1e-3 each).
+      DBuf<float> eff32, invd32, Xf, Rf, Pf, Tf;
+      eff32.alloc(size_t(ncell * np));
+      invd32.alloc(size_t(ncell * nd));
+      for (DBuf<float>* v : {&Xf, &Rf, &Pf, &Tf}) v->alloc(size_t(B) * size_t(nd));
+      k_to_f32<<<nb_cell, kT, 0, s>>>(ef.p, eff32.p, ncell * np);
       TG_LAUNCH_CHECK();
-      k_b_xr<<<g, kT, 0, s>>>(X.p, R.p, Pv.p, T.p, invd.p, nd, nrhs, absn.p, pap.p, act.p, prr.p,
-                              prz.p);
+      k_to_f32<<<nb_cell, kT, 0, s>>>(invd.p, invd32.p, ncell * nd);
       TG_LAUNCH_CHECK();
-      k_bsum<<<wb, 256, 0, s>>>(prr.p, P, B, rr.p, prz.p, rz.p);
+      DBuf<double> thr_o(static_cast<size_t>(B)), b2(static_cast<size_t>(B));
+      // |b|^2 and the outer threshold tol^2 |b|^2.
+      k_b_rr_rz<double><<<bt.g2(), kT, 0, s>>>(R.p, invd.p, nd, nrhs, bt.prr.p, bt.prz.p);
       TG_LAUNCH_CHECK();
-      TG_CUDA(cudaMemsetAsync(nact.p, 0, sizeof(int), s));
-      k_b_scalars<<<sb, 256, 0, s>>>(B, rr.p, rz.p, thr.p, pap.p, max_it, act.p, it.p, absn.p,
-                                     beta.p, nact.p);
+      k_bsum<<<bt.wb(), 256, 0, s>>>(bt.prr.p, P, B, b2.p, nullptr, nullptr);
       TG_LAUNCH_CHECK();
-      k_b_p<<<g, kT, 0, s>>>(Pv.p, R.p, invd.p, nd, nrhs, beta.p, act.p);
-      TG_LAUNCH_CHECK();
-      if ((k & 7) == 7) {
-        TG_CUDA(cudaMemcpyAsync(&host_nact, nact.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      std::vector<double> hb2(static_cast<size_t>(B)), hthr(static_cast<size_t>(B));
+      TG_CUDA(cudaMemcpyAsync(hb2.data(), b2.p, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+      TG_CUDA(cudaStreamSynchronize(s));
+      for (int bi = 0; bi < B; ++bi)
+        hthr[size_t(bi)] = std::max(tolerance * tolerance * hb2[size_t(bi)], DBL_MIN);
+      TG_CUDA(cudaMemcpyAsync(thr_o.p, hthr.data(), sizeof(double) * B, cudaMemcpyHostToDevice, s));
+      std::vector<double> hrr(static_cast<size_t>(B));
+      const int max_ref = 30;
+      int budget = max_it;
+      for (int ref = 0;; ++ref) {
+        // r = b - A x (FP64) -- the first residual is b itself (x = 0).
+        if (ref > 0)
+          launch_periodic_op<double>(kResidual, nx, ny, nz, bt.mc, ef.p, kept.p, X.p, Bv.p,
+                                     nullptr, 0.0, R.p, nullptr, B, nrhs, s);
+        k_b_rr_rz<double><<<bt.g2(), kT, 0, s>>>(R.p, invd.p, nd, nrhs, bt.prr.p, bt.prz.p);
+        TG_LAUNCH_CHECK();
+        k_bsum<<<bt.wb(), 256, 0, s>>>(bt.prr.p, P, B, bt.rr.p, nullptr, nullptr);
+        TG_LAUNCH_CHECK();
+        TG_CUDA(cudaMemsetAsync(bt.nrun.p, 0, sizeof(int), s));
+        k_b_refine<<<bt.sb(), 256, 0, s>>>(B, bt.rr.p, thr_o.p, bt.run.p, bt.rn.p, bt.nrun.p);
+        TG_LAUNCH_CHECK();
+        int nrun = 0;
+        TG_CUDA(cudaMemcpyAsync(&nrun, bt.nrun.p, sizeof(int), cudaMemcpyDeviceToHost, s));
         TG_CUDA(cudaStreamSynchronize(s));
+        if (nrun == 0) break;
+        if (ref == max_ref || budget <= 0) {
+          all_ok = false;
+          break;
+        }
+        ++inf.refinements;
+        budget -= bt.pcg<float>(Xf.p, Rf.p, Pf.p, Tf.p, eff32.p, invd32.p, 1e-3, budget, bt.run.p,
+                                R.p);
+        k_b_correct<<<bt.g2(), kT, 0, s>>>(X.p, Xf.p, bt.rn.p, bt.run.p, nd);
+        TG_LAUNCH_CHECK();
       }
+      // Converged: every final FP64 residual below its threshold (NaN fails).
+      TG_CUDA(cudaMemcpyAsync(hrr.data(), bt.rr.p, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+      TG_CUDA(cudaStreamSynchronize(s));
+      for (int bi = 0; bi < B; ++bi)
+        if (!(hrr[size_t(bi)] < hthr[size_t(bi)]) && hb2[size_t(bi)] > 0.0) all_ok = false;
     }
     // CH from F_I . chi_J.
+    DBuf<double> pfx(size_t(B) * 6 * P), fx(size_t(B) * 6);
     {
       const dim3 g(static_cast<unsigned>(P), static_cast<unsigned>(B), 6u);
       k_b_fx<<<g, kT, 0, s>>>(F.p, X.p, nd, nrhs, pfx.p);
@@ -443,29 +619,15 @@ extern "C" int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, 
       k_bsum<<<(B * 6 * 32 + 255) / 256, 256, 0, s>>>(pfx.p, P, B * 6, fx.p, nullptr, nullptr);
       TG_LAUNCH_CHECK();
     }
-    std::vector<double> hfx(static_cast<size_t>(B) * 6), hrr(static_cast<size_t>(B)), hb2(static_cast<size_t>(B));
-    std::vector<int> hact(static_cast<size_t>(B)), hit(static_cast<size_t>(B));
+    std::vector<double> hfx(static_cast<size_t>(B) * 6);
     TG_CUDA(cudaMemcpyAsync(hfx.data(), fx.p, sizeof(double) * B * 6, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaMemcpyAsync(hrr.data(), rr.p, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaMemcpyAsync(hb2.data(), rhs2.p, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaMemcpyAsync(hact.data(), act.p, sizeof(int) * B, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaMemcpyAsync(hit.data(), it.p, sizeof(int) * B, cudaMemcpyDeviceToHost, s));
     TG_CUDA(cudaStreamSynchronize(s));
     inf.t_solve_ms = now_ms() - ts;
-    (void)t_setup0;
-    const double vol = double(np) * spacing * spacing * spacing;
     inf.systems = B;
-    inf.converged = 1;
-    for (int bi = 0; bi < B; ++bi) {
-      inf.iterations_max = std::max(inf.iterations_max, hit[size_t(bi)]);
-      inf.iterations_total += hit[size_t(bi)];
-      // converged: reached the threshold (act 0) with a finite relative residual
-      // within the tolerance (the rhs-zero case converges trivially).
-      const bool ok = hact[size_t(bi)] == 0 &&
-                      (hb2[size_t(bi)] == 0.0 ||
-                       std::sqrt(hrr[size_t(bi)] / hb2[size_t(bi)]) <= tolerance);
-      if (!ok) inf.converged = 0;
-    }
+    inf.iterations_max = bt.iterations_max;
+    inf.iterations_total = bt.iterations_total;
+    inf.converged = all_ok ? 1 : 0;
+    const double vol = double(np) * spacing * spacing * spacing;
     for (int c = 0; c < ncell; ++c) {
       double* ch = ch_out + int64_t(c) * 36;
       std::fill(ch, ch + 36, 0.0);

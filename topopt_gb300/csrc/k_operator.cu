@@ -372,6 +372,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
     // z: node layer ez is complete (element layers ez-1 and ez).
     if (s >= 1 && own_xy && ez < g.nnz) {
       const int64_t d0 = 3 * ((int64_t(ez) * g.nny + ey) * g.nnx + ex);
+      T node_dot = T(0);  // x.y over the node's 3 DOFs, accumulated in FP64 below
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int64_t d = d0 + k;
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
         T out;
         if (MODE == kApply) {
           out = kk ? ax : T(0);
-          dsum += double(xv) * double(out);
+          node_dot += xv * out;
         } else if (MODE == kResidual) {
           out = kk ? T(b[d] - ax) : T(0);
         } else {
@@ -389,6 +390,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
         }
         y[d] = out;
       }
+      if (MODE == kApply) dsum += double(node_dot);
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) pend[k] = N[1][k];
@@ -456,52 +458,62 @@ template void launch_fine_op<float>(int, const Grid&, const ModalConsts&, const 
 // Periodic batched apply: nsys systems on the nx*ny*nz torus; system bi uses
 // x/b/y at bi*ndof and the factors / kept mask / inverse diagonal of cell
 // bi / nrhs.  dot_part (kApply) receives one partial of x.y per CTA, the CTAs of
-// a system contiguous: periodic_op_blocks() per system.
+// a system contiguous: periodic_op_blocks<T>() per system.
+template <class T>
 int periodic_op_blocks(int nx, int ny, int nz) {
-  using P = Pencil<double>;
+  using P = Pencil<T>;
   return ((nx + 30) / 31) * ((ny + P::PY - 2) / (P::PY - 1)) * ((nz + P::KZ - 1) / P::KZ);
 }
+template int periodic_op_blocks<double>(int, int, int);
+template int periodic_op_blocks<float>(int, int, int);
 
-template <int MODE>
-static void launch_periodic_mode(int nx, int ny, int nz, const ModalConsts& c, const double* ef,
-                                 const uint8_t* kept, const double* x, const double* b,
-                                 const double* invdiag, double omega, double* y, double* dot_part,
-                                 int nsys, int nrhs, cudaStream_t s) {
-  using P = Pencil<double>;
+template <class T, int MODE>
+static void launch_periodic_mode(int nx, int ny, int nz, const ModalConsts& c, const T* ef,
+                                 const uint8_t* kept, const T* x, const T* b, const T* invdiag,
+                                 T omega, T* y, double* dot_part, int nsys, int nrhs,
+                                 cudaStream_t s) {
+  using P = Pencil<T>;
   const GridDev gd{nx, ny, nz, nx, ny, nz};
   const int nzc = (nz + P::KZ - 1) / P::KZ;
   const int64_t ndof = 3 * int64_t(nx) * ny * nz, nv = int64_t(nx) * ny * nz;
   // gridDim.z <= 65535: whole cells per launch.
   const int cells_per = std::max(1, 65535 / (nzc * nrhs));
   const int ncell = nsys / nrhs;
+  const int nblk = periodic_op_blocks<T>(nx, ny, nz);
   for (int c0 = 0; c0 < ncell; c0 += cells_per) {
     const int nc = std::min(cells_per, ncell - c0);
     const int64_t s0 = int64_t(c0) * nrhs;
     const BatchDev bd{nrhs, nzc, ndof, nv, ndof};
     const dim3 grid((nx + 30) / 31, (ny + P::PY - 2) / (P::PY - 1), nzc * nc * nrhs);
-    k_fine_op<double, P::PY, P::KZ, P::MINB, MODE, true><<<grid, 32 * P::PY, 0, s>>>(
-        gd, to_modal<double>(c), ef + c0 * nv, kept ? kept + c0 * ndof : nullptr,
-        x + s0 * ndof, b ? b + s0 * ndof : nullptr, invdiag ? invdiag + c0 * ndof : nullptr, omega,
-        y + s0 * ndof,
-        dot_part ? dot_part + s0 * periodic_op_blocks(nx, ny, nz) : nullptr, bd);
+    k_fine_op<T, P::PY, P::KZ, P::MINB, MODE, true><<<grid, 32 * P::PY, 0, s>>>(
+        gd, to_modal<T>(c), ef + c0 * nv, kept ? kept + c0 * ndof : nullptr, x + s0 * ndof,
+        b ? b + s0 * ndof : nullptr, invdiag ? invdiag + c0 * ndof : nullptr, omega,
+        y + s0 * ndof, dot_part ? dot_part + s0 * nblk : nullptr, bd);
     TG_LAUNCH_CHECK();
   }
 }
 
-void launch_periodic_op(int mode, int nx, int ny, int nz, const ModalConsts& c, const double* ef,
-                        const uint8_t* kept, const double* x, const double* b,
-                        const double* invdiag, double omega, double* y, double* dot_part,
-                        int nsys, int nrhs, cudaStream_t s) {
+template <class T>
+void launch_periodic_op(int mode, int nx, int ny, int nz, const ModalConsts& c, const T* ef,
+                        const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
+                        T* y, double* dot_part, int nsys, int nrhs, cudaStream_t s) {
   if (mode == kApply)
-    launch_periodic_mode<kApply>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part, nsys,
-                                 nrhs, s);
-  else if (mode == kResidual)
-    launch_periodic_mode<kResidual>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part,
+    launch_periodic_mode<T, kApply>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part,
                                     nsys, nrhs, s);
+  else if (mode == kResidual)
+    launch_periodic_mode<T, kResidual>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y,
+                                       dot_part, nsys, nrhs, s);
   else
-    launch_periodic_mode<kSmooth>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part,
-                                  nsys, nrhs, s);
+    launch_periodic_mode<T, kSmooth>(nx, ny, nz, c, ef, kept, x, b, invdiag, omega, y, dot_part,
+                                     nsys, nrhs, s);
 }
+template void launch_periodic_op<double>(int, int, int, int, const ModalConsts&, const double*,
+                                         const uint8_t*, const double*, const double*,
+                                         const double*, double, double*, double*, int, int,
+                                         cudaStream_t);
+template void launch_periodic_op<float>(int, int, int, int, const ModalConsts&, const float*,
+                                        const uint8_t*, const float*, const float*, const float*,
+                                        float, float*, double*, int, int, cudaStream_t);
 
 // diag(A) at every DOF = kdiag * (sum of the adjacent element factors), summed
 // in a fixed element order; invdiag = 1/diag on kept DOFs, 0 elsewhere

@@ -116,13 +116,14 @@ void launch_fine_op(int mode, const Grid& g, const ModalConsts& mc, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
                     T* y, double* dot_part, int* nblocks_out, cudaStream_t s);
 int fine_op_blocks(const Grid& g, bool fp64);
-// Batched FP64 apply on the periodic nx*ny*nz torus (nodes = elements per axis);
-// see k_operator.cu.
+// Batched apply on the periodic nx*ny*nz torus (nodes = elements per axis); see
+// k_operator.cu.
+template <class T>
 int periodic_op_blocks(int nx, int ny, int nz);
-void launch_periodic_op(int mode, int nx, int ny, int nz, const ModalConsts& c, const double* ef,
-                        const uint8_t* kept, const double* x, const double* b,
-                        const double* invdiag, double omega, double* y, double* dot_part,
-                        int nsys, int nrhs, cudaStream_t s);
+template <class T>
+void launch_periodic_op(int mode, int nx, int ny, int nz, const ModalConsts& c, const T* ef,
+                        const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
+                        T* y, double* dot_part, int nsys, int nrhs, cudaStream_t s);
 
 // Jacobi diagonal of the fine operator: diag = kdiag * sum of adjacent factors.
 void launch_fine_invdiag(const Grid& g, double kdiag, const double* ef, const uint8_t* kept,
