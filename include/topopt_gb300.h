@@ -81,6 +81,13 @@ typedef enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 } tg_precision;
  * grid allows, the reference's iteration budget of 300 MG cycles before the
  * Jacobi-PCG fallback (multigrid.cpp:122), damped Jacobi w = 0.6 with 1+1 sweeps
  * (multigrid.cpp:72-76). */
+/* Multigrid coarsening of odd axes.  REFERENCE: the reference's index-space
+ * padding (multigrid.cpp:391-459; the plain FP64 form's default).  ALIGNED: the
+ * last coarse node sits on the last fine node (the mixed form's default):
+ * the same Galerkin method with a coarse space that keeps the smooth modes at
+ * odd boundaries -- far fewer iterations on odd grids, same solution. */
+enum { TG_COARSEN_DEFAULT = 0, TG_COARSEN_REFERENCE = 1, TG_COARSEN_ALIGNED = 2 };
+
 typedef struct {
   int32_t solver;          /* tg_solver_kind */
   int32_t precision;       /* tg_precision */
@@ -89,6 +96,7 @@ typedef struct {
   double omega;            /* 0 = 0.6 */
   double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve, 0 = 1e-3 */
   int32_t max_refinements; /* mixed: outer FP64 refinement steps, 0 = 20 */
+  int32_t coarsening;      /* odd-axis coarsening: TG_COARSEN_* (0 = the form's default) */
 } tg_solve_options;
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */

@@ -195,3 +195,22 @@ def test_nonconvergence_raises(tg):
         tg.fea_solve_mgcg_matfree(pb, np.ones(pb.nv), tolerance=1e-12, max_iterations=1,
                                   options=tg.SolveOptions(solver=tg.SOLVER_JACOBI_CG))
     assert e.value.iterations >= 1
+
+
+@pytest.mark.parametrize("dims", [(63, 31, 31), (45, 22, 17)])
+def test_aligned_coarsening_odd_grids(tg, dims):
+    """Boundary-aligned coarsening of odd axes: the same solution as the
+    reference's padded hierarchy, in fewer MG-PCG iterations."""
+    pb = tg.Problem.cantilever(*dims)
+    E = smooth_modulus(pb)
+    u_ref, i_ref = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        coarsening=tg.COARSEN_REFERENCE))
+    u_al, i_al = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        coarsening=tg.COARSEN_ALIGNED))
+    assert i_ref.used_multigrid and i_al.used_multigrid
+    assert rel(u_al, u_ref) < 1e-8
+    assert i_al.iterations < i_ref.iterations
+    u_mx, i_mx = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        precision=tg.PREC_MIXED))
+    assert not i_mx.mixed_fallback
+    assert rel(u_mx, u_ref) < 1e-8

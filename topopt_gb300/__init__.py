@@ -41,6 +41,9 @@ from ._capi import (  # noqa: F401
     oc_update_masked,
     simp_compliance,
     simp_optimize,
+    COARSEN_ALIGNED,
+    COARSEN_DEFAULT,
+    COARSEN_REFERENCE,
     MASK_ACTIVE,
     MASK_FROZEN_SOLID,
     MASK_FROZEN_VOID,

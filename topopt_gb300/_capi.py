@@ -59,7 +59,8 @@ class _Params(C.Structure):
 class _SolveOpt(C.Structure):
     _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("mg_levels", C.c_int32),
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
-                ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32)]
+                ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
+                ("coarsening", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -239,10 +240,12 @@ class SolveOptions:
     omega: float = 0.0
     inner_tolerance: float = 0.0
     max_refinements: int = 0
+    coarsening: int = 0  # COARSEN_DEFAULT / COARSEN_REFERENCE / COARSEN_ALIGNED
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
-                         self.omega, self.inner_tolerance, self.max_refinements)
+                         self.omega, self.inner_tolerance, self.max_refinements,
+                         self.coarsening)
 
 
 @dataclass
@@ -369,6 +372,8 @@ def simp_compliance(pb: Problem, params: SimpParams, density, tolerance=1e-8, ma
     _check(rc, info)
     return dict(u=u, dcompliance=dc, compliance=c.value, cg=CgInfo._from(info))
 
+
+COARSEN_DEFAULT, COARSEN_REFERENCE, COARSEN_ALIGNED = 0, 1, 2
 
 # MaskValue (voxel.hpp:42-46).
 MASK_ACTIVE, MASK_FROZEN_SOLID, MASK_FROZEN_VOID = 0, 1, 2

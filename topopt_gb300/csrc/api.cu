@@ -136,6 +136,8 @@ tg_solve_options default_solve(const tg_solve_options* o) {
     raise(TG_EINVAL, "solve options: unknown precision");
   if (d.precision == TG_PREC_MIXED && d.solver != TG_SOLVER_MGCG)
     raise(TG_EINVAL, "solve options: mixed precision needs the multigrid solver");
+  if (d.coarsening < TG_COARSEN_DEFAULT || d.coarsening > TG_COARSEN_ALIGNED)
+    raise(TG_EINVAL, "solve options: unknown coarsening");
   return d;
 }
 

@@ -50,11 +50,14 @@ __device__ __forceinline__ int cz(int c) { return c >> 2; }
 // product over axes of 1 (pos 0 with t 0, or pos 2 with t 1), 1/2 (pos 1) or 0,
 // with pos = ch_axis + sc_axis.  Integer logic only: the FP pipes see just the
 // multiply-adds by the nonzero weights.
-__device__ __forceinline__ int wexp(int ch, int sc, int t) {
+// hm: axes (bit a) on which the coarse element is a boundary-aligned half
+// element (one child spanning it, sub-corner sc sits at position 2*sc).
+__device__ __forceinline__ int wexp(int ch, int sc, int t, int hm = 0) {
   int e = 0;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const int pos = ((ch >> a) & 1) + ((sc >> a) & 1), ta = (t >> a) & 1;
+    const int pos = ((hm >> a) & 1) ? 2 * ((sc >> a) & 1) : ((ch >> a) & 1) + ((sc >> a) & 1);
+    const int ta = (t >> a) & 1;
     if (pos == 1) {
       ++e;
     } else if ((pos == 0) != (ta == 0)) {
@@ -94,6 +97,9 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
   for (int64_t ce = blockIdx.x * int64_t(NW) + warp; ce < nce; ce += int64_t(gridDim.x) * NW) {
     const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
               K = int(ce / (int64_t(cd.ex) * cd.ey));
+    const int hm = cd.align ? ((2 * I + 1 == fd.ex) | ((2 * J + 1 == fd.ey) << 1) |
+                               ((2 * K + 1 == fd.ez) << 2))
+                            : 0;
     T acc[24];
 #pragma unroll
     for (int r = 0; r < 24; ++r) acc[r] = T(0);
@@ -114,7 +120,7 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
           if (fact[3 * node + comp]) mm = 1u << lane;
         }
         m = __reduce_or_sync(0xffffffffu, mm);
-        if (m == 0xffffffu) {
+        if (m == 0xffffffu && hm == 0) {
           if (lane < 24)
 #pragma unroll
             for (int r = 0; r < 24; ++r) acc[r] += f * G[ch * 576 + r * 24 + lane];
@@ -133,7 +139,7 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
           T xa = 0, xb = 0, xc = 0;
 #pragma unroll
           for (int sc = 0; sc < 8; ++sc) {
-            const int e = wexp(ch, sc, t);
+            const int e = wexp(ch, sc, t, hm);
             if (e < 0) continue;
             const T w = wval<T>(e);
             xa += S[lane * 24 + 3 * sc] * w;
@@ -152,7 +158,7 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
           T ya = 0, yb = 0, yc = 0;
 #pragma unroll
           for (int sc = 0; sc < 8; ++sc) {
-            const int e = wexp(ch, sc, t1);
+            const int e = wexp(ch, sc, t1, hm);
             if (e < 0) continue;
             const T w = wval<T>(e);
             ya += w * X[(3 * sc) * 24 + lane];
@@ -327,6 +333,18 @@ __global__ void k_jacobi_first(const T* __restrict__ b, const T* __restrict__ in
     x[i] = omega * invdiag[i] * b[i];
 }
 
+// Boundary-aligned coarsening (MgDims::align): on an odd fine axis the last
+// fine node (index Ef) is the coincident node of coarse node (Ef + 1) / 2.
+__device__ __forceinline__ bool tail_node(int i, int Ef, int align) {
+  return align && (Ef & 1) && i == Ef;
+}
+// Weight of fine node i (= 2N + d) in coarse node N along one axis.
+template <class T>
+__device__ __forceinline__ T axis_w(int i, int N, int d, int Ef, int align) {
+  if (tail_node(i, Ef, align)) return N == (Ef + 1) / 2 ? T(1) : T(0);
+  return d == 0 ? T(1) : T(0.5);
+}
+
 // Restriction R = P^T: coarse node N gathers the (up to 27) fine nodes
 // 2N + delta, delta in {-1,0,1}^3, weight prod(1 or 1/2).  Inactive coarse DOFs
 // get 0; fine residuals are already 0 on inactive fine DOFs.
@@ -341,15 +359,15 @@ __global__ void k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
     for (int dz = -1; dz <= 1; ++dz) {
       const int k = 2 * c + dz;
       if (k < 0 || k >= fd.nnz) continue;
-      const T wz = dz == 0 ? T(1) : T(0.5);
+      const T wz = axis_w<T>(k, c, dz, fd.ez, cd.align);
       for (int dy = -1; dy <= 1; ++dy) {
         const int j = 2 * b + dy;
         if (j < 0 || j >= fd.nny) continue;
-        const T wy = dy == 0 ? T(1) : T(0.5);
+        const T wy = axis_w<T>(j, b, dy, fd.ey, cd.align);
         for (int dx = -1; dx <= 1; ++dx) {
           const int i = 2 * a + dx;
           if (i < 0 || i >= fd.nnx) continue;
-          const T w = (dx == 0 ? T(1) : T(0.5)) * wy * wz;
+          const T w = axis_w<T>(i, a, dx, fd.ex, cd.align) * wy * wz;
           const int64_t m = (int64_t(k) * fd.nny + j) * fd.nnx + i;
           s0 += w * rf[3 * m];
           s1 += w * rf[3 * m + 1];
@@ -371,15 +389,21 @@ __global__ void k_prolong_add(MgDims fd, MgDims cd, const T* __restrict__ ec,
   for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
        n += int64_t(gridDim.x) * kThreads) {
     const int a = int(n % fd.nnx), b = int((n / fd.nnx) % fd.nny), c = int(n / (int64_t(fd.nnx) * fd.nny));
-    const int ia0 = a >> 1, ia1 = (a + 1) >> 1, ib0 = b >> 1, ib1 = (b + 1) >> 1;
-    const int ic0 = c >> 1, ic1 = (c + 1) >> 1;
-    const T wa = (a & 1) ? T(0.5) : T(1), wb = (b & 1) ? T(0.5) : T(1), wc = (c & 1) ? T(0.5) : T(1);
+    // Per axis: one coarse node (even fine node, or the aligned tail node) or two
+    // at weight 1/2.
+    const bool ta = tail_node(a, fd.ex, cd.align), tb = tail_node(b, fd.ey, cd.align),
+               tc = tail_node(c, fd.ez, cd.align);
+    const int na = (a & 1) && !ta ? 2 : 1, nb = (b & 1) && !tb ? 2 : 1, ncz = (c & 1) && !tc ? 2 : 1;
+    const int ia0 = ta ? (a + 1) >> 1 : a >> 1, ia1 = (a + 1) >> 1;
+    const int ib0 = tb ? (b + 1) >> 1 : b >> 1, ib1 = (b + 1) >> 1;
+    const int ic0 = tc ? (c + 1) >> 1 : c >> 1, ic1 = (c + 1) >> 1;
+    const T wa = na == 2 ? T(0.5) : T(1), wb = nb == 2 ? T(0.5) : T(1), wc = ncz == 2 ? T(0.5) : T(1);
     T s0 = 0, s1 = 0, s2 = 0;
-    for (int zz = 0; zz < ((c & 1) ? 2 : 1); ++zz) {
+    for (int zz = 0; zz < ncz; ++zz) {
       const int k = zz ? ic1 : ic0;
-      for (int yy = 0; yy < ((b & 1) ? 2 : 1); ++yy) {
+      for (int yy = 0; yy < nb; ++yy) {
         const int j = yy ? ib1 : ib0;
-        for (int xx = 0; xx < ((a & 1) ? 2 : 1); ++xx) {
+        for (int xx = 0; xx < na; ++xx) {
           const int i = xx ? ia1 : ia0;
           if (i >= cd.nnx || j >= cd.nny || k >= cd.nnz) continue;
           const int64_t m = (int64_t(k) * cd.nny + j) * cd.nnx + i;

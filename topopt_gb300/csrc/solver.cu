@@ -291,6 +291,10 @@ size_t Solver::device_bytes() const {
 void Solver::build_structure() {
   const Grid& g = fp_.g;
   const int max_levels = opt_.mg_levels > 0 ? opt_.mg_levels : 64;
+  // Odd axes: the reference's padding (the plain form's default) or the
+  // boundary-aligned coarse grid (the mixed form's default); see MgDims::align.
+  const int align = opt_.coarsening == TG_COARSEN_ALIGNED ||
+                    (opt_.coarsening == TG_COARSEN_DEFAULT && mixed_);
   std::vector<MgDims> dims{dims_of(g.nx, g.ny, g.nz)};
   // Halve (rounding up) while every coarse axis keeps >= 2 elements
   // (kMgMinCoarseElems, coarsen.hpp:80); a requested depth below what keeps the
@@ -302,6 +306,7 @@ void Solver::build_structure() {
     const int64_t dof_here = 3 * int64_t(d.nnx) * d.nny * d.nnz;
     if (int(dims.size()) >= max_levels && dof_here <= kMaxCoarseDof) break;
     dims.push_back(dims_of(cx, cy, cz));
+    dims.back().align = align;
   }
   if (dims.size() < 2) return;
   std::vector<uint8_t> prev = fp_.kept_h;
@@ -316,8 +321,12 @@ void Solver::build_structure() {
     for (int c = 0; c < L->d.nnz; ++c)
       for (int b = 0; b < L->d.nny; ++b)
         for (int a = 0; a < L->d.nnx; ++a) {
-          if (2 * a >= pd.nnx || 2 * b >= pd.nny || 2 * c >= pd.nnz) continue;  // pad node
-          const int64_t fn = (int64_t(2 * c) * pd.nny + 2 * b) * pd.nnx + 2 * a;
+          // Coincident fine node; on an aligned odd axis the last coarse node
+          // sits on the last fine node.
+          auto co = [&](int i, int ef) { return (align && (ef & 1) && i == (ef + 1) / 2) ? ef : 2 * i; };
+          const int fa = co(a, pd.ex), fb = co(b, pd.ey), fc = co(c, pd.ez);
+          if (fa >= pd.nnx || fb >= pd.nny || fc >= pd.nnz) continue;  // pad node
+          const int64_t fn = (int64_t(fc) * pd.nny + fb) * pd.nnx + fa;
           const int64_t cn = (int64_t(c) * L->d.nny + b) * L->d.nnx + a;
           for (int k = 0; k < 3; ++k)
             if (prev[size_t(3 * fn + k)]) {

@@ -10,9 +10,17 @@ namespace tg {
 // neighbour blocks, 3x3 each (the backward blocks are their transposes).
 constexpr int kStencilEntries = 14 * 9;
 
-// Element and node extents of one hierarchy level.
+// Element and node extents of one hierarchy level.  align (coarse levels): how
+// an odd finer axis (2m+1 elements) is coarsened.  0 -- the reference's
+// index-space padding: coarse node m+1 would coincide with fine node 2m+2,
+// beyond the grid, so it is inactive and the last fine node interpolates half
+// of coarse node m only (multigrid.cpp:391-459).  1 -- boundary-aligned: coarse
+// node m+1 coincides with the last fine node 2m+1 (prolongation weight 1) and
+// the last coarse element spans a single fine element, so the coarse space keeps
+// the rigid and smooth modes up to the boundary.
 struct MgDims {
   int ex, ey, ez, nnx, nny, nnz;
+  int align = 0;
 };
 
 template <class T>
