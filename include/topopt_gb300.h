@@ -87,6 +87,7 @@ typedef enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 } tg_precision;
  * the same Galerkin method with a coarse space that keeps the smooth modes at
  * odd boundaries -- far fewer iterations on odd grids, same solution. */
 enum { TG_COARSEN_DEFAULT = 0, TG_COARSEN_REFERENCE = 1, TG_COARSEN_ALIGNED = 2 };
+enum { TG_GRAPH_ON = 0, TG_GRAPH_OFF = 1 };
 
 typedef struct {
   int32_t solver;          /* tg_solver_kind */
@@ -97,6 +98,9 @@ typedef struct {
   double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve, 0 = 1e-3 */
   int32_t max_refinements; /* mixed: outer FP64 refinement steps, 0 = 20 */
   int32_t coarsening;      /* odd-axis coarsening: TG_COARSEN_* (0 = the form's default) */
+  int32_t graph_mode;      /* mixed: TG_GRAPH_ON (default, 0) runs the inner PCG loop as one
+                              CUDA graph with a device-side loop condition; TG_GRAPH_OFF
+                              drives it from the host (same arithmetic, same results) */
 } tg_solve_options;
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */

@@ -214,3 +214,18 @@ def test_aligned_coarsening_odd_grids(tg, dims):
         precision=tg.PREC_MIXED))
     assert not i_mx.mixed_fallback
     assert rel(u_mx, u_ref) < 1e-8
+
+
+@pytest.mark.parametrize("dims", [(48, 24, 24), (37, 19, 13)])
+def test_graph_inner_loop_matches_host_loop(tg, dims):
+    """The mixed inner PCG loop run as one CUDA graph (device-side loop
+    condition) gives bit-identical results to the host-driven loop."""
+    pb = tg.Problem.cantilever(*dims)
+    E = smooth_modulus(pb)
+    ug, ig = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        precision=tg.PREC_MIXED, graph_mode=tg.GRAPH_ON))
+    uh, ih = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        precision=tg.PREC_MIXED, graph_mode=tg.GRAPH_OFF))
+    assert np.array_equal(ug, uh)
+    assert ig.iterations == ih.iterations and ig.matvecs_lowp == ih.matvecs_lowp
+    assert ig.refinements == ih.refinements

@@ -44,6 +44,8 @@ from ._capi import (  # noqa: F401
     COARSEN_ALIGNED,
     COARSEN_DEFAULT,
     COARSEN_REFERENCE,
+    GRAPH_OFF,
+    GRAPH_ON,
     MASK_ACTIVE,
     MASK_FROZEN_SOLID,
     MASK_FROZEN_VOID,

@@ -60,7 +60,7 @@ class _SolveOpt(C.Structure):
     _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("mg_levels", C.c_int32),
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
                 ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
-                ("coarsening", C.c_int32)]
+                ("coarsening", C.c_int32), ("graph_mode", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -241,11 +241,12 @@ class SolveOptions:
     inner_tolerance: float = 0.0
     max_refinements: int = 0
     coarsening: int = 0  # COARSEN_DEFAULT / COARSEN_REFERENCE / COARSEN_ALIGNED
+    graph_mode: int = 0  # GRAPH_ON / GRAPH_OFF
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
                          self.omega, self.inner_tolerance, self.max_refinements,
-                         self.coarsening)
+                         self.coarsening, self.graph_mode)
 
 
 @dataclass
@@ -374,6 +375,7 @@ def simp_compliance(pb: Problem, params: SimpParams, density, tolerance=1e-8, ma
 
 
 COARSEN_DEFAULT, COARSEN_REFERENCE, COARSEN_ALIGNED = 0, 1, 2
+GRAPH_ON, GRAPH_OFF = 0, 1
 
 # MaskValue (voxel.hpp:42-46).
 MASK_ACTIVE, MASK_FROZEN_SOLID, MASK_FROZEN_VOID = 0, 1, 2

@@ -45,7 +45,15 @@ double now_ms() {
 void raise(int code, const std::string& msg) { throw Error(code, msg); }
 int device_ordinal() { return g_device; }
 void set_last_error(const std::string& msg) { g_err = msg; }
-void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+namespace {
+thread_local int64_t t_launches = 0;  // this thread's launches (graph capture accounting)
+}
+void note_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  ++t_launches;
+}
+int64_t kernel_launch_count() { return t_launches; }
+void add_kernel_launches(int64_t delta) { g_launches.fetch_add(delta, std::memory_order_relaxed); }
 
 void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
   char buf[512];
@@ -138,6 +146,8 @@ tg_solve_options default_solve(const tg_solve_options* o) {
     raise(TG_EINVAL, "solve options: mixed precision needs the multigrid solver");
   if (d.coarsening < TG_COARSEN_DEFAULT || d.coarsening > TG_COARSEN_ALIGNED)
     raise(TG_EINVAL, "solve options: unknown coarsening");
+  if (d.graph_mode != TG_GRAPH_ON && d.graph_mode != TG_GRAPH_OFF)
+    raise(TG_EINVAL, "solve options: unknown graph_mode");
   return d;
 }
 

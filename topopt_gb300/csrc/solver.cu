@@ -265,6 +265,9 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   part_.alloc(size_t(part_n_));
   scal_.alloc(32);
   TG_CUDA(cudaMallocHost(&h_scal_, 32 * sizeof(double)));
+  istate_.alloc(4);
+  TG_CUDA(cudaMallocHost(&h_ist_, 4 * sizeof(int)));
+  use_graph_ = opt.graph_mode != TG_GRAPH_OFF;
   if (mixed_) {
     Ef_.alloc(size_t(fp.g.nv));
     for (DBuf<float>* b : {&invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_}) b->alloc(n);
@@ -272,8 +275,20 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   if (opt.solver == TG_SOLVER_MGCG) build_structure();
 }
 
+struct Solver::InnerGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t body_launches = 0;  // kernels per body execution
+  ~InnerGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
 Solver::~Solver() {
+  ig_.reset();
   if (h_scal_) cudaFreeHost(h_scal_);
+  if (h_ist_) cudaFreeHost(h_ist_);
 }
 
 size_t Solver::device_bytes() const {
@@ -664,6 +679,92 @@ bool Solver::mgpcg(double tol, int max_it, bool warm, SolverStats& st) {
 
 // FP32 inner MG-PCG on the unit-norm residual held in zf_; solution in xf_.
 // FP64 dot products; stops at relative residual rel_tol or max_it.
+// The decision at the end of one graph-resident inner PCG iteration, exactly the
+// host loop's: breakdown (p.Ap <= 0 or not finite) stops without counting the
+// iteration; otherwise it is counted and the loop continues while
+// ||r|| > thr and the budget allows.  scal[7] = p.Ap, scal[8] = r.r,
+// scal[11] = thr; st[0] = iterations done, st[1] = budget, st[2] = breakdown.
+__global__ void k_inner_cond(cudaGraphConditionalHandle h, const double* __restrict__ scal,
+                             int* __restrict__ st) {
+  const double pap = scal[7], rr = scal[8], thr = scal[11];
+  if (!(pap > 0.0) || !isfinite(pap)) {
+    st[2] = 1;
+    cudaGraphSetConditional(h, 0u);
+    return;
+  }
+  const int k = st[0] + 1;
+  st[0] = k;
+  cudaGraphSetConditional(h, (!(sqrt(rr) <= thr) && k < st[1]) ? 1u : 0u);
+}
+
+// Captures iterations 2.. of inner_pcg<float> into a WHILE conditional node.
+// All pointers the body uses (fine vectors, level buffers, scalars) live as
+// long as the solver, so the graph is built once and replayed for every inner
+// solve.  On any capture error the solver keeps the host-driven loop.
+bool Solver::build_inner_graph() {
+  if (ig_failed_) return false;
+  if (ig_) return true;
+  const Grid& g = fp_.g;
+  const int64_t n = g.ndof;
+  auto ig = std::make_unique<InnerGraph>();
+  bool ok = cudaGraphCreate(&ig->graph, 0) == cudaSuccess;
+  cudaGraphConditionalHandle h{};
+  cudaGraph_t body = nullptr;
+  if (ok)
+    ok = cudaGraphConditionalHandleCreate(&h, ig->graph, 1u, cudaGraphCondAssignDefault) ==
+         cudaSuccess;
+  if (ok) {
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    ok = cudaGraphAddNode(&node, ig->graph, nullptr, nullptr, 0, &cp) == cudaSuccess;
+    if (ok) body = cp.conditional.phGraph_out[0];
+  }
+  if (ok)
+    ok = cudaStreamBeginCaptureToGraph(s_, body, nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    const int64_t l0 = kernel_launch_count();
+    const int64_t m0 = lowp_matvecs_;
+    bool cap_ok = true;
+    try {
+      float* z = vcycle<float>(rf_.p);
+      launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 9, s_);
+      launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
+      TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice,
+                              s_));
+      int nb = 0;
+      launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
+                            apf_.p, part_.p, &nb, s_);
+      launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
+      launch_cg_update_xr<float>(xf_.p, rf_.p, pf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n,
+                                 part_.p, s_);
+      launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
+      k_inner_cond<<<1, 1, 0, s_>>>(h, scal_.p, istate_.p);
+      TG_LAUNCH_CHECK();
+    } catch (const Error&) {
+      cap_ok = false;
+    }
+    cudaGraph_t out = nullptr;
+    const bool end_ok = cudaStreamEndCapture(s_, &out) == cudaSuccess;
+    ig->body_launches = kernel_launch_count() - l0;
+    add_kernel_launches(-ig->body_launches);  // captured, not launched
+    lowp_matvecs_ = m0;
+    ok = cap_ok && end_ok;
+  }
+  if (ok) ok = cudaGraphInstantiate(&ig->exec, ig->graph, 0) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();  // clear a capture error; the host loop runs instead
+    ig_failed_ = true;
+    return false;
+  }
+  ig_ = std::move(ig);
+  return true;
+}
+
 template <>
 bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* iters) {
   const Grid& g = fp_.g;
@@ -693,6 +794,26 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
     }
     *iters = k;
     if (std::sqrt(sc[1]) <= thr) return true;
+    if (k == 1 && max_it > 1 && use_graph_ && build_inner_graph()) {
+      // Iterations 2.. on the device: one graph launch, one read-back.
+      h_scal_[11] = thr;
+      h_ist_[0] = 1;
+      h_ist_[1] = max_it;
+      h_ist_[2] = 0;
+      TG_CUDA(cudaMemcpyAsync(scal_.p + 11, h_scal_ + 11, sizeof(double), cudaMemcpyHostToDevice,
+                              s_));
+      TG_CUDA(cudaMemcpyAsync(istate_.p, h_ist_, 3 * sizeof(int), cudaMemcpyHostToDevice, s_));
+      TG_CUDA(cudaGraphLaunch(ig_->exec, s_));
+      TG_CUDA(cudaMemcpyAsync(h_ist_, istate_.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s_));
+      TG_CUDA(cudaStreamSynchronize(s_));
+      const int done = h_ist_[0], broke = h_ist_[2];
+      const int64_t runs = int64_t(done - 1) + broke;  // body executions
+      add_kernel_launches(runs * ig_->body_launches);
+      lowp_matvecs_ += 3 * runs;
+      *iters = done;
+      if (broke) ++st.inner_breakdowns;
+      return true;
+    }
     z = vcycle<float>(rf_.p);
     launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 9, s_);
     launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);

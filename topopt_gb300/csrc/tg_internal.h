@@ -37,6 +37,8 @@ void cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     if (tg_e_ != cudaSuccess) ::tg::cuda_fail(tg_e_, #call, __FILE__, __LINE__); \
   } while (0)
 void note_launch();
+int64_t kernel_launch_count();            // launches noted by the calling thread
+void add_kernel_launches(int64_t delta);  // graph replays / captures
 #define TG_LAUNCH_CHECK()          \
   do {                             \
     ::tg::note_launch();           \

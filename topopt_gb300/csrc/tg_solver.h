@@ -88,6 +88,7 @@ class Solver {
   void vcycle_level(size_t l);
   template <class T>
   bool inner_pcg(int max_it, double rel_tol, SolverStats& st, int* iters);
+  bool build_inner_graph();
   double read_scalar(int idx);
   void read_scalars(int idx0, int n, double* out);
 
@@ -114,6 +115,14 @@ class Solver {
   int nc_ = 0;
   DBuf<int> cidx_, cdof_, chol_fail_;
   DBuf<double> chol_, chol_work_, chol_li_, chol_inv_;
+  // The mixed inner PCG loop as one CUDA graph: a conditional WHILE node whose
+  // body is one PCG iteration (V-cycle, update, apply) ending in a kernel that
+  // decides, on the device, whether another iteration runs.
+  struct InnerGraph;
+  std::unique_ptr<InnerGraph> ig_;
+  bool ig_failed_ = false, use_graph_ = true;
+  DBuf<int> istate_;           // [0] iterations done, [1] budget, [2] breakdown
+  int* h_ist_ = nullptr;       // pinned mirror of istate_
 };
 
 }  // namespace tg
