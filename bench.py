@@ -269,7 +269,9 @@ def run_ours(args, world, rank, local, pg):
     def opts(prec, K):
         return tg.SimpOptions(volume_fraction=0.3, filter_radius=1.5, move=0.2, change_tol=0.0,
                               cg_tolerance=1e-8, max_iterations=K,
-                              solve=tg.SolveOptions(precision=prec, mg_levels=args.mg_levels))
+                              solve=tg.SolveOptions(precision=prec, mg_levels=args.mg_levels,
+                                                    graph_mode=tg.GRAPH_OFF if args.no_graph
+                                                    else tg.GRAPH_ON))
 
     fp64_peak, fp32_peak = tg.device_fma_peaks()
     forms = {}
@@ -523,6 +525,9 @@ def main():
                     help="profiling aid: run only the fine operator (fea_matfree_apply) 3 times")
     ap.add_argument("--profile", action="store_true",
                     help="profiling aid: allow warmup < 3, skip e2e and the CPU baseline")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="profiling aid: drive the mixed inner PCG loop from the host (same "
+                         "kernels, same results) instead of one CUDA graph")
     ap.add_argument("--workload", choices=["cantilever", "batch", "homog", "serve"],
                     default="cantilever")
     ap.add_argument("--cells", type=int, default=512)
