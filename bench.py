@@ -63,6 +63,20 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def committed_traffic(nx, ny, nz):
+    """DRAM bytes per launch of the FP32 fine operator from the committed ncu
+    capture of the same workload (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", f"fine_op_fp32_{nx}x{ny}x{nz}.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def cantilever_random_load(nx, ny, nz, seed=0):
     """Clamped x = 0 face; unit -z load at a seeded point of the x = nx face."""
     rng = np.random.default_rng(seed)
@@ -273,7 +287,7 @@ def run_ours(args, world, rank, local, pg):
                                                     graph_mode=tg.GRAPH_OFF if args.no_graph
                                                     else tg.GRAPH_ON))
 
-    fp64_peak, fp32_peak = tg.device_fma_peaks()
+    fp64_peak, fp32_peak = tg.device_fma_peaks() if not args.profile else (None, None)
     forms = {}
     order = ["mixed", "fp64"] if not args.skip_fp64 else ["mixed"]
     for form in order:
@@ -348,7 +362,10 @@ def run_ours(args, world, rank, local, pg):
                 "includes": "problem upload + job setup + K iterations + certification solve + read-back"},
         "roofline": {"bound": "hbm", "kernel": "fine operator apply, FP32 (mixed V-cycle)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "bytes_per_launch": op_bytes32, "traffic": None,
+                     "peak_source": src, "bytes_per_launch": op_bytes32,
+                     "traffic": committed_traffic(nx, ny, nz),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one "
+                                       "launch of the same workload (committed capture)",
                      "ms_per_launch": m["op_fp32_ms"]},
         "fp64_operator": {"ms_per_launch": m["op_fp64_ms"],
                           "reference_flops_per_launch": fp64_alg_flops,

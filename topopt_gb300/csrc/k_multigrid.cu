@@ -261,7 +261,7 @@ __global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int6
 // forward block of a node whose neighbour lies outside the grid is zero, and the
 // backward term is selected away).
 template <class T, int MODE>
-__global__ void __launch_bounds__(kThreads) k_stencil_op(MgDims d, const T* __restrict__ A,
+__global__ void __launch_bounds__(256, 5) k_stencil_op(MgDims d, const T* __restrict__ A,
                                                          const uint8_t* __restrict__ act,
                                                          const T* __restrict__ x,
                                                          const T* __restrict__ b,
@@ -269,9 +269,10 @@ __global__ void __launch_bounds__(kThreads) k_stencil_op(MgDims d, const T* __re
                                                          T* __restrict__ y) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   const int64_t sy = d.nnx, sz = int64_t(d.nnx) * d.nny;
-  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
-       n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny), c = int(n / sz);
+  // One node per thread on a 3D grid (x fastest).
+  const int a = blockIdx.x * 32 + threadIdx.x, bb = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
+  if (a < d.nnx && bb < d.nny) {
+    const int64_t n = c * sz + bb * sy + a;
     const T* An = A + n;
     const T xs0 = x[3 * n], xs1 = x[3 * n + 1], xs2 = x[3 * n + 2];
     T s0 = An[0] * xs0 + An[nn] * xs1 + An[2 * nn] * xs2;
@@ -347,77 +348,86 @@ __device__ __forceinline__ T axis_w(int i, int N, int d, int Ef, int align) {
 
 // Restriction R = P^T: coarse node N gathers the (up to 27) fine nodes
 // 2N + delta, delta in {-1,0,1}^3, weight prod(1 or 1/2).  Inactive coarse DOFs
-// get 0; fine residuals are already 0 on inactive fine DOFs.
+// get 0; fine residuals are already 0 on inactive fine DOFs.  One thread per
+// coarse node on a 3D grid (x fastest), 32-bit index arithmetic.
 template <class T>
-__global__ void k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
-                           const uint8_t* __restrict__ cact, T* __restrict__ bc) {
-  const int64_t nn = int64_t(cd.nnx) * cd.nny * cd.nnz;
-  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
-       n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % cd.nnx), b = int((n / cd.nnx) % cd.nny), c = int(n / (int64_t(cd.nnx) * cd.nny));
-    T s0 = 0, s1 = 0, s2 = 0;
-    for (int dz = -1; dz <= 1; ++dz) {
-      const int k = 2 * c + dz;
-      if (k < 0 || k >= fd.nnz) continue;
-      const T wz = axis_w<T>(k, c, dz, fd.ez, cd.align);
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int j = 2 * b + dy;
-        if (j < 0 || j >= fd.nny) continue;
-        const T wy = axis_w<T>(j, b, dy, fd.ey, cd.align);
-        for (int dx = -1; dx <= 1; ++dx) {
-          const int i = 2 * a + dx;
-          if (i < 0 || i >= fd.nnx) continue;
-          const T w = axis_w<T>(i, a, dx, fd.ex, cd.align) * wy * wz;
-          const int64_t m = (int64_t(k) * fd.nny + j) * fd.nnx + i;
-          s0 += w * rf[3 * m];
-          s1 += w * rf[3 * m + 1];
-          s2 += w * rf[3 * m + 2];
-        }
+__global__ void __launch_bounds__(256) k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
+                                                  const uint8_t* __restrict__ cact,
+                                                  T* __restrict__ bc) {
+  const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
+  if (a >= cd.nnx || b >= cd.nny) return;
+  T s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int k = 2 * c + dz;
+    if (k < 0 || k >= fd.nnz) continue;
+    const T wz = axis_w<T>(k, c, dz, fd.ez, cd.align);
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int j = 2 * b + dy;
+      if (j < 0 || j >= fd.nny) continue;
+      const T wy = axis_w<T>(j, b, dy, fd.ey, cd.align) * wz;
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int i = 2 * a + dx;
+        if (i < 0 || i >= fd.nnx) continue;
+        const T w = axis_w<T>(i, a, dx, fd.ex, cd.align) * wy;
+        const T* q = rf + 3 * ((int64_t(k) * fd.nny + j) * fd.nnx + i);
+        s0 += w * q[0];
+        s1 += w * q[1];
+        s2 += w * q[2];
       }
     }
-    bc[3 * n] = cact[3 * n] ? s0 : T(0);
-    bc[3 * n + 1] = cact[3 * n + 1] ? s1 : T(0);
-    bc[3 * n + 2] = cact[3 * n + 2] ? s2 : T(0);
   }
+  const int64_t n = (int64_t(c) * cd.nny + b) * cd.nnx + a;
+  bc[3 * n] = cact[3 * n] ? s0 : T(0);
+  bc[3 * n + 1] = cact[3 * n + 1] ? s1 : T(0);
+  bc[3 * n + 2] = cact[3 * n + 2] ? s2 : T(0);
 }
 
-// Prolongation + correction: x_f += P e_c on active fine DOFs.
+// Prolongation + correction: x_f += P e_c on active fine DOFs.  One thread per
+// fine node on a 3D grid.
 template <class T>
-__global__ void k_prolong_add(MgDims fd, MgDims cd, const T* __restrict__ ec,
-                              const uint8_t* __restrict__ fact, T* __restrict__ xf) {
-  const int64_t nn = int64_t(fd.nnx) * fd.nny * fd.nnz;
-  for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
-       n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % fd.nnx), b = int((n / fd.nnx) % fd.nny), c = int(n / (int64_t(fd.nnx) * fd.nny));
-    // Per axis: one coarse node (even fine node, or the aligned tail node) or two
-    // at weight 1/2.
-    const bool ta = tail_node(a, fd.ex, cd.align), tb = tail_node(b, fd.ey, cd.align),
-               tc = tail_node(c, fd.ez, cd.align);
-    const int na = (a & 1) && !ta ? 2 : 1, nb = (b & 1) && !tb ? 2 : 1, ncz = (c & 1) && !tc ? 2 : 1;
-    const int ia0 = ta ? (a + 1) >> 1 : a >> 1, ia1 = (a + 1) >> 1;
-    const int ib0 = tb ? (b + 1) >> 1 : b >> 1, ib1 = (b + 1) >> 1;
-    const int ic0 = tc ? (c + 1) >> 1 : c >> 1, ic1 = (c + 1) >> 1;
-    const T wa = na == 2 ? T(0.5) : T(1), wb = nb == 2 ? T(0.5) : T(1), wc = ncz == 2 ? T(0.5) : T(1);
-    T s0 = 0, s1 = 0, s2 = 0;
-    for (int zz = 0; zz < ncz; ++zz) {
-      const int k = zz ? ic1 : ic0;
-      for (int yy = 0; yy < nb; ++yy) {
-        const int j = yy ? ib1 : ib0;
-        for (int xx = 0; xx < na; ++xx) {
-          const int i = xx ? ia1 : ia0;
-          if (i >= cd.nnx || j >= cd.nny || k >= cd.nnz) continue;
-          const int64_t m = (int64_t(k) * cd.nny + j) * cd.nnx + i;
-          const T w = wa * wb * wc;
-          s0 += w * ec[3 * m];
-          s1 += w * ec[3 * m + 1];
-          s2 += w * ec[3 * m + 2];
-        }
+__global__ void __launch_bounds__(256) k_prolong_add(MgDims fd, MgDims cd,
+                                                     const T* __restrict__ ec,
+                                                     const uint8_t* __restrict__ fact,
+                                                     T* __restrict__ xf) {
+  const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
+  if (a >= fd.nnx || b >= fd.nny) return;
+  // Per axis: one coarse node (even fine node, or the aligned tail node) or two
+  // at weight 1/2.
+  const bool ta = tail_node(a, fd.ex, cd.align), tb = tail_node(b, fd.ey, cd.align),
+             tc = tail_node(c, fd.ez, cd.align);
+  const int na = (a & 1) && !ta ? 2 : 1, nb = (b & 1) && !tb ? 2 : 1, ncz = (c & 1) && !tc ? 2 : 1;
+  const int ia0 = ta ? (a + 1) >> 1 : a >> 1, ia1 = (a + 1) >> 1;
+  const int ib0 = tb ? (b + 1) >> 1 : b >> 1, ib1 = (b + 1) >> 1;
+  const int ic0 = tc ? (c + 1) >> 1 : c >> 1, ic1 = (c + 1) >> 1;
+  const T w = (na == 2 ? T(0.5) : T(1)) * (nb == 2 ? T(0.5) : T(1)) * (ncz == 2 ? T(0.5) : T(1));
+  T s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+  for (int zz = 0; zz < 2; ++zz) {
+    if (zz >= ncz) continue;
+    const int k = zz ? ic1 : ic0;
+#pragma unroll
+    for (int yy = 0; yy < 2; ++yy) {
+      if (yy >= nb) continue;
+      const int j = yy ? ib1 : ib0;
+#pragma unroll
+      for (int xx = 0; xx < 2; ++xx) {
+        if (xx >= na) continue;
+        const int i = xx ? ia1 : ia0;
+        if (i >= cd.nnx || j >= cd.nny || k >= cd.nnz) continue;
+        const T* q = ec + 3 * ((int64_t(k) * cd.nny + j) * cd.nnx + i);
+        s0 += w * q[0];
+        s1 += w * q[1];
+        s2 += w * q[2];
       }
     }
-    if (fact[3 * n]) xf[3 * n] += s0;
-    if (fact[3 * n + 1]) xf[3 * n + 1] += s1;
-    if (fact[3 * n + 2]) xf[3 * n + 2] += s2;
   }
+  const int64_t n = (int64_t(c) * fd.nny + b) * fd.nnx + a;
+  if (fact[3 * n]) xf[3 * n] += s0;
+  if (fact[3 * n + 1]) xf[3 * n + 1] += s1;
+  if (fact[3 * n + 2]) xf[3 * n + 2] += s2;
 }
 
 // ---------------------------------------------------------- coarsest solve
@@ -630,14 +640,13 @@ void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s) {
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s) {
-  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
-  const int nb = nblk(nn);
+  const dim3 nb((d.nnx + 31) / 32, (d.nny + 7) / 8, d.nnz), nt(32, 8);
   if (mode == kApply)
-    k_stencil_op<T, kApply><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else if (mode == kResidual)
-    k_stencil_op<T, kResidual><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kResidual><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else
-    k_stencil_op<T, kSmooth><<<nb, kThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kSmooth><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   TG_LAUNCH_CHECK();
 }
 
@@ -650,16 +659,16 @@ void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cud
 template <class T>
 void mg_restrict(const MgDims& fd, const MgDims& cd, const T* rf, const uint8_t* cact, T* bc,
                  cudaStream_t s) {
-  const int64_t nn = int64_t(cd.nnx) * cd.nny * cd.nnz;
-  k_restrict<T><<<nblk(nn), kThreads, 0, s>>>(fd, cd, rf, cact, bc);
+  const dim3 grid((cd.nnx + 31) / 32, (cd.nny + 7) / 8, cd.nnz);
+  k_restrict<T><<<grid, dim3(32, 8), 0, s>>>(fd, cd, rf, cact, bc);
   TG_LAUNCH_CHECK();
 }
 
 template <class T>
 void mg_prolong_add(const MgDims& fd, const MgDims& cd, const T* ec, const uint8_t* fact, T* xf,
                     cudaStream_t s) {
-  const int64_t nn = int64_t(fd.nnx) * fd.nny * fd.nnz;
-  k_prolong_add<T><<<nblk(nn), kThreads, 0, s>>>(fd, cd, ec, fact, xf);
+  const dim3 grid((fd.nnx + 31) / 32, (fd.nny + 7) / 8, fd.nnz);
+  k_prolong_add<T><<<grid, dim3(32, 8), 0, s>>>(fd, cd, ec, fact, xf);
   TG_LAUNCH_CHECK();
 }
 

@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
   finish_layer(lane, raw, cur);
   load_raw<T, PER>(g, x, ex, ey, k0, lane, raw);
   T pend[3] = {T(0), T(0), T(0)};
-  double dsum = 0.0;
+  T dsum = T(0);  // this thread's share of x.y: a few dozen nodes, then FP64 across the CTA
 #pragma unroll 1
   for (int s = 0; s <= KZ; ++s) {
     const int ez = k0 - 1 + s;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
         }
         y[d] = out;
       }
-      if (MODE == kApply) dsum += double(node_dot);
+      if (MODE == kApply) dsum += node_dot;
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) pend[k] = N[1][k];
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
         for (int k = 0; k < 3; ++k) cur[yb][xb][k] = nxt[yb][xb][k];
   }
   if (MODE == kApply && dot_part != nullptr) {
-    const double sum = block_sum(dsum);
+    const double sum = block_sum(double(dsum));
     if (threadIdx.x == 0)
       dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sum;
   }

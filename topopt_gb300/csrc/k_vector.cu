@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "tg_internal.h"
 
@@ -97,7 +98,30 @@ __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __
   const double alpha = (pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0;
   const T a = T(alpha);
   T t = T(0);
-  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+  int64_t i0 = 0;
+  if (std::is_same<T, float>::value) {
+    // FP32: 16-byte vector accesses (the buffers are cudaMalloc-aligned).
+    const int64_t n4 = n >> 2;
+    float4* x4 = reinterpret_cast<float4*>(x);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    const float4* a4 = reinterpret_cast<const float4*>(ap);
+    const float af = float(alpha);
+    float tf = 0.0f;
+    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n4;
+         i += int64_t(gridDim.x) * kThreads) {
+      float4 xv = x4[i], rv = r4[i];
+      const float4 pv = p4[i], qv = a4[i];
+      xv.x += af * pv.x; xv.y += af * pv.y; xv.z += af * pv.z; xv.w += af * pv.w;
+      rv.x -= af * qv.x; rv.y -= af * qv.y; rv.z -= af * qv.z; rv.w -= af * qv.w;
+      x4[i] = xv;
+      r4[i] = rv;
+      tf += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+    }
+    t = T(tf);
+    i0 = n4 << 2;
+  }
+  for (int64_t i = i0 + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * kThreads) {
     x[i] += a * p[i];
     const T ri = r[i] - a * ap[i];
@@ -129,13 +153,26 @@ __global__ void k_cg_update_p(T* __restrict__ p, const T* __restrict__ z,
                               const double* __restrict__ rz_new, const double* __restrict__ rz_old,
                               int64_t n) {
   const T beta = T(*rz_new / *rz_old);
-  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+  int64_t i0 = 0;
+  if (std::is_same<T, float>::value) {
+    const int64_t n4 = n >> 2;
+    float4* p4 = reinterpret_cast<float4*>(p);
+    const float4* z4 = reinterpret_cast<const float4*>(z);
+    const float b = float(beta);
+    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n4;
+         i += int64_t(gridDim.x) * kThreads) {
+      float4 pv = p4[i];
+      const float4 zv = z4[i];
+      pv.x = zv.x + b * pv.x; pv.y = zv.y + b * pv.y; pv.z = zv.z + b * pv.z; pv.w = zv.w + b * pv.w;
+      p4[i] = pv;
+    }
+    i0 = n4 << 2;
+  }
+  for (int64_t i = i0 + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * kThreads)
     p[i] = z[i] + beta * p[i];
 }
 
-// Scale a float vector by 1/sqrt(*nrm2) (mixed-precision inner solves run on a
-// unit-norm residual) while converting from double.
 __global__ void k_scale_d2f(float* __restrict__ d, const double* __restrict__ s,
                             const double* __restrict__ nrm2, int64_t n) {
   const double inv = *nrm2 > 0.0 ? 1.0 / sqrt(*nrm2) : 0.0;

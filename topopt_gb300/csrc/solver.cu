@@ -861,7 +861,11 @@ bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
     if (ref == max_ref || total_inner >= max_it) break;
     launch_scale_d2f(zf_.p, r_.p, scal_.p + 5, n, s_);
     int it = 0;
-    inner_pcg<float>(std::min(budget_, max_it - total_inner), inner_tol, st, &it);
+    // Default inner tolerance: 1e-3, relaxed to 0.3x the reduction still needed
+    // when that is less (the last refinement usually needs far less than 1e-3).
+    const double itol = opt_.inner_tolerance > 0.0 ? inner_tol
+                                                   : std::min(0.1, std::max(inner_tol, 0.3 * threshold / rn));
+    inner_pcg<float>(std::min(budget_, max_it - total_inner), itol, st, &it);
     total_inner += it;
     launch_axpy_scaled_f2d(x_.p, xf_.p, scal_.p + 5, n, s_);
     launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x_.p, rhs_.p, nullptr, 0.0, r_.p,
