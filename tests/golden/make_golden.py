@@ -27,7 +27,7 @@ def main():
     if build_reference() is None:
         raise SystemExit("reference tree not available; nothing generated")
     R = OracleLib("reference")
-    R.set_threads(1)
+    R.set_threads(int(os.environ.get("GOLDEN_THREADS", "1")))
     rng = np.random.default_rng(20261203)
     out = {}
     # Element stiffness, pinned to the reference's own JSON fixture too.
@@ -116,6 +116,17 @@ def main():
                msimp_compliance=np.array(sm["compliance"]),
                msimp_volume_fraction=np.array(sm["volume_fraction"]),
                msimp_iterations=np.array(sm["iterations"]))
+
+    # The reference's CPU-runnable configuration: 60x20x20 cantilever, volume
+    # fraction 0.3, rmin 1.5, move 0.2, 50 design iterations (change_tol 0 so all
+    # 50 run), solves at 1e-10.
+    pb0 = cantilever(60, 20, 20)
+    s0 = R.simp_optimize(pb0, volfrac=0.3, radius=1.5, move=0.2, max_it=50, change_tol=0.0,
+                         cg_tol=1e-10)
+    out.update(cfg0_hist_c=s0["hist_c"], cfg0_hist_change=s0["hist_change"],
+               cfg0_hist_vf=s0["hist_vf"], cfg0_design=s0["design"],
+               cfg0_compliance=np.array(s0["compliance"]),
+               cfg0_iterations=np.array(s0["iterations"]))
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
 

@@ -229,3 +229,22 @@ def test_graph_inner_loop_matches_host_loop(tg, dims):
     assert np.array_equal(ug, uh)
     assert ig.iterations == ih.iterations and ig.matvecs_lowp == ih.matvecs_lowp
     assert ig.refinements == ih.refinements
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_cfg0_fifty_iterations(tg, golden, prec):
+    """The reference's CPU-runnable configuration end to end: 60x20x20
+    cantilever, volume fraction 0.3, rmin 1.5, move 0.2, 50 design iterations,
+    solves at 1e-10 -- against the reference's own 50-iteration run."""
+    o = cantilever(60, 20, 20)
+    pb = tg.Problem(60, 20, 20, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                    list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+    s = tg.simp_optimize(pb, tg.SimpParams(), tg.SimpOptions(
+        volume_fraction=0.3, filter_radius=1.5, move=0.2, change_tol=0.0, max_iterations=50,
+        cg_tolerance=1e-10, solve=tg.SolveOptions(precision=prec)))
+    hc = np.array([h["compliance"] for h in s["history"]])
+    assert s["iterations"] == 50
+    assert abs(hc[0] - golden["cfg0_hist_c"][0]) <= 1e-9 * hc[0]
+    assert rel(hc, golden["cfg0_hist_c"]) < 1e-6
+    assert rel(s["design"], golden["cfg0_design"]) < 1e-4
+    assert abs(s["compliance"] - float(golden["cfg0_compliance"])) <= 1e-6 * s["compliance"]

@@ -46,29 +46,24 @@ __device__ __forceinline__ int cx(int c) { return c & 1; }
 __device__ __forceinline__ int cy(int c) { return (c >> 1) & 1; }
 __device__ __forceinline__ int cz(int c) { return c >> 2; }
 
-// Trilinear weight of coarse corner t for child-corner sc of child ch: the
-// product over axes of 1 (pos 0 with t 0, or pos 2 with t 1), 1/2 (pos 1) or 0,
-// with pos = ch_axis + sc_axis.  Integer logic only: the FP pipes see just the
-// multiply-adds by the nonzero weights.
-// hm: axes (bit a) on which the coarse element is a boundary-aligned half
-// element (one child spanning it, sub-corner sc sits at position 2*sc).
-__device__ __forceinline__ int wexp(int ch, int sc, int t, int hm = 0) {
-  int e = 0;
+// v[3*corner + comp] <- sum_sc v[3*sc + comp] * prod_a M_a[sc_a][t_a] for every
+// parent corner t: three 2x2 passes over the corner bits (x, y, z).
+template <class T>
+__device__ __forceinline__ void kron_map(const T (&mw)[3][4], T (&v)[24]) {
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const int pos = ((hm >> a) & 1) ? 2 * ((sc >> a) & 1) : ((ch >> a) & 1) + ((sc >> a) & 1);
-    const int ta = (t >> a) & 1;
-    if (pos == 1) {
-      ++e;
-    } else if ((pos == 0) != (ta == 0)) {
-      return -1;
+    const int bit = 1 << a;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (i & bit) continue;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T lo = v[3 * i + c], hi = v[3 * (i | bit) + c];
+        v[3 * i + c] = mw[a][0] * lo + mw[a][2] * hi;
+        v[3 * (i | bit) + c] = mw[a][1] * lo + mw[a][3] * hi;
+      }
     }
   }
-  return e;  // weight = 2^-e, or -1 for zero
-}
-template <class T>
-__device__ __forceinline__ T wval(int e) {
-  return e == 0 ? T(1) : (e == 1 ? T(0.5) : (e == 2 ? T(0.25) : T(0.125)));
 }
 
 // One warp per coarse element; lane c < 24 owns column c of the coarse element
@@ -88,8 +83,9 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
                                                   const T* __restrict__ Kf,
                                                   T* __restrict__ Kc) {
   constexpr int NW = 4;
-  __shared__ T sS[NW][576];
-  __shared__ T sX[NW][576];
+  constexpr int LD = 25;  // padded row stride: row and column walks are bank-conflict free
+  __shared__ T sS[NW][24 * LD];
+  __shared__ T sX[NW][24 * LD];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* S = sS[warp];
   T* X = sX[warp];
@@ -128,47 +124,42 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
         }
         for (int e = lane; e < 576; e += 32) {
           const int r = e / 24, c2 = e % 24;
-          S[e] = ((m >> r) & 1u) && ((m >> c2) & 1u) ? f * Ke[e] : T(0);
+          S[r * LD + c2] = ((m >> r) & 1u) && ((m >> c2) & 1u) ? f * Ke[e] : T(0);
         }
       } else {
-        for (int e = lane; e < 576; e += 32) S[e] = Kf[fe * 576 + e];
+        for (int e = lane; e < 576; e += 32) S[(e / 24) * LD + e % 24] = Kf[fe * 576 + e];
       }
       __syncwarp();
-      if (lane < 24) {  // X = S W: lane = row
-        for (int t = 0; t < 8; ++t) {
-          T xa = 0, xb = 0, xc = 0;
+      // W = W_x (x) W_y (x) W_z on the corner index (times I3 on components):
+      // per axis a 2x2 map from the child's sub-corner bit to the parent's
+      // corner bit -- [[1,0],[1/2,1/2]] for child bit 0, [[1/2,1/2],[0,1]] for
+      // child bit 1, the identity on an aligned half element.  X = S W and
+      // Y += W^T X are three 2x2 passes each instead of a dense 8x8 product.
+      T mw[3][4];  // per axis: M[sc][t] as {m00, m01, m10, m11}; warp-uniform
 #pragma unroll
-          for (int sc = 0; sc < 8; ++sc) {
-            const int e = wexp(ch, sc, t, hm);
-            if (e < 0) continue;
-            const T w = wval<T>(e);
-            xa += S[lane * 24 + 3 * sc] * w;
-            xb += S[lane * 24 + 3 * sc + 1] * w;
-            xc += S[lane * 24 + 3 * sc + 2] * w;
-          }
-          X[lane * 24 + 3 * t] = xa;
-          X[lane * 24 + 3 * t + 1] = xb;
-          X[lane * 24 + 3 * t + 2] = xc;
-        }
+      for (int a = 0; a < 3; ++a) {
+        const bool half = (hm >> a) & 1, hi = (ch >> a) & 1;
+        mw[a][0] = half ? T(1) : (hi ? T(0.5) : T(1));
+        mw[a][1] = half ? T(0) : (hi ? T(0.5) : T(0));
+        mw[a][2] = half ? T(0) : (hi ? T(0) : T(0.5));
+        mw[a][3] = half ? T(1) : (hi ? T(1) : T(0.5));
+      }
+      if (lane < 24) {  // X = S W: lane = row
+        T v[24];
+#pragma unroll
+        for (int j = 0; j < 24; ++j) v[j] = S[lane * LD + j];
+        kron_map(mw, v);
+#pragma unroll
+        for (int j = 0; j < 24; ++j) X[lane * LD + j] = v[j];
       }
       __syncwarp();
       if (lane < 24) {  // Y += W^T X: lane = column
+        T v[24];
 #pragma unroll
-        for (int t1 = 0; t1 < 8; ++t1) {
-          T ya = 0, yb = 0, yc = 0;
+        for (int j = 0; j < 24; ++j) v[j] = X[j * LD + lane];
+        kron_map(mw, v);
 #pragma unroll
-          for (int sc = 0; sc < 8; ++sc) {
-            const int e = wexp(ch, sc, t1, hm);
-            if (e < 0) continue;
-            const T w = wval<T>(e);
-            ya += w * X[(3 * sc) * 24 + lane];
-            yb += w * X[(3 * sc + 1) * 24 + lane];
-            yc += w * X[(3 * sc + 2) * 24 + lane];
-          }
-          acc[3 * t1] += ya;
-          acc[3 * t1 + 1] += yb;
-          acc[3 * t1 + 2] += yc;
-        }
+        for (int j = 0; j < 24; ++j) acc[j] += v[j];
       }
       __syncwarp();
     }

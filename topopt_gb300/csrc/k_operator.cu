@@ -271,6 +271,24 @@ __device__ __forceinline__ void load_raw(const GridDev& g, const T* __restrict__
   }
 }
 
+// The same loads for the non-periodic grid with the column's x/y validity
+// (m[yb][xb]) and base offset hoisted out of the z march: layer c adds
+// 3*c*nnx*nny to the offset and tests only its own z range.
+template <class T>
+__device__ __forceinline__ void load_raw_np(const T* __restrict__ x, int64_t o, int snx, bool vc,
+                                            const bool (&m)[2][2], int lane, T (&r)[2][2][3]) {
+#pragma unroll
+  for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+    for (int xb = 0; xb < 2; ++xb) {
+      if (xb == 1 && lane != 31) continue;
+      const bool ok = vc && m[yb][xb];
+      const T* p = x + (o + yb * snx + 3 * xb);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) r[yb][xb][k] = ok ? p[k] : T(0);
+    }
+}
+
 // Completes a layer: v[yb][xb][comp] for nodes (ex + xb, ey + yb); the +x nodes
 // come from the next lane (lane 31 loaded its own).
 template <class T>
@@ -315,17 +333,37 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
   const bool exy_ok = PER || (ex >= 0 && ex < g.nx && ey >= 0 && ey < g.ny);
   const int64_t exy = PER ? int64_t(wrap_index(ey, g.ny)) * g.nx + wrap_index(ex, g.nx)
                           : int64_t(ey) * g.nx + ex;
+  // Non-periodic: hoisted column validity and running offsets (nodes: o_x,
+  // outputs: o_y, element factors: o_e).
+  const int64_t plane3 = 3 * int64_t(g.nnx) * g.nny, eplane = int64_t(g.nx) * g.ny;
+  const int snx = 3 * g.nnx;
+  const bool vx0 = ex >= 0 && ex < g.nnx, vx1 = ex + 1 < g.nnx;
+  const bool vy0 = ey >= 0 && ey < g.nny, vy1 = ey + 1 < g.nny;
+  const bool msk[2][2] = {{vx0 && vy0, vx1 && vy0}, {vx0 && vy1, vx1 && vy1}};
+  const int64_t oxy = 3 * (int64_t(ey) * g.nnx + ex);
   T cur[2][2][3], nxt[2][2][3], raw[2][2][3];
-  load_raw<T, PER>(g, x, ex, ey, k0 - 1, lane, raw);
+  if (PER) {
+    load_raw<T, PER>(g, x, ex, ey, k0 - 1, lane, raw);
+  } else {
+    load_raw_np(x, oxy + (k0 - 1) * plane3, snx, k0 - 1 >= 0 && k0 - 1 < g.nnz, msk, lane, raw);
+  }
   finish_layer(lane, raw, cur);
-  load_raw<T, PER>(g, x, ex, ey, k0, lane, raw);
+  if (PER)
+    load_raw<T, PER>(g, x, ex, ey, k0, lane, raw);
+  else
+    load_raw_np(x, oxy + k0 * plane3, snx, k0 < g.nnz, msk, lane, raw);
   T pend[3] = {T(0), T(0), T(0)};
   T dsum = T(0);  // this thread's share of x.y: a few dozen nodes, then FP64 across the CTA
 #pragma unroll 1
   for (int s = 0; s <= KZ; ++s) {
     const int ez = k0 - 1 + s;
     finish_layer(lane, raw, nxt);
-    if (s < KZ) load_raw<T, PER>(g, x, ex, ey, ez + 2, lane, raw);
+    if (s < KZ) {
+      if (PER)
+        load_raw<T, PER>(g, x, ex, ey, ez + 2, lane, raw);
+      else
+        load_raw_np(x, oxy + (ez + 2) * plane3, snx, ez + 2 < g.nnz, msk, lane, raw);
+    }
     T ux[8], uy[8], uz[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -338,7 +376,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
     if (PER)
       f = ef[int64_t(wrap_index(ez, g.nz)) * g.ny * g.nx + exy];
     else
-      f = (exy_ok && ez >= 0 && ez < g.nz) ? ef[int64_t(ez) * g.ny * g.nx + exy] : T(0);
+      f = (exy_ok && ez >= 0 && ez < g.nz) ? ef[ez * eplane + exy] : T(0);
     if (f != T(0)) {
       modal_apply(mc, f, ux, uy, uz);
     } else {
@@ -371,7 +409,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
         N[zb][k] = L[0][zb][k] + (w >= 1 ? sy[buf][w - 1][zb * 3 + k][lane] : T(0));
     // z: node layer ez is complete (element layers ez-1 and ez).
     if (s >= 1 && own_xy && ez < g.nnz) {
-      const int64_t d0 = 3 * ((int64_t(ez) * g.nny + ey) * g.nnx + ex);
+      const int64_t d0 = oxy + ez * plane3;
       T node_dot = T(0);  // x.y over the node's 3 DOFs, accumulated in FP64 below
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
