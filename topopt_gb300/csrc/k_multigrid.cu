@@ -84,11 +84,19 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
                                                   T* __restrict__ Kc) {
   constexpr int NW = 4;
   constexpr int LD = 25;  // padded row stride: row and column walks are bank-conflict free
+  // Level 1 in FP32: the 8 child blocks G_c live in shared memory (18 KB per CTA).
+  constexpr bool kSmemG = LEVEL1 && sizeof(T) == 4;
   __shared__ T sS[NW][24 * LD];
   __shared__ T sX[NW][24 * LD];
+  __shared__ T sG[kSmemG ? 8 * 576 : 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* S = sS[warp];
   T* X = sX[warp];
+  if (kSmemG) {
+    for (int e = threadIdx.x; e < 8 * 576; e += blockDim.x) sG[e] = G[e];
+    __syncthreads();
+    G = sG;
+  }
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
   for (int64_t ce = blockIdx.x * int64_t(NW) + warp; ce < nce; ce += int64_t(gridDim.x) * NW) {
     const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),

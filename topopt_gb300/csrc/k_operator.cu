@@ -62,22 +62,7 @@ ModalT<T> to_modal(const ModalConsts& c) {
   return m;
 }
 
-// Two FP32 lanes per thread: Blackwell's packed FP32x2 instructions
-// (FADD2 / FMUL2 / FFMA2) evaluate two elements per instruction.
-struct F2 {
-  float2 v;
-  F2() = default;
-  __device__ __forceinline__ explicit F2(float s) : v(make_float2(s, s)) {}
-  __device__ __forceinline__ F2(float2 x) : v(x) {}
-};
-__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
-__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
-  return F2(__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v));  // a - b, exact negation
-}
-__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
-__device__ __forceinline__ F2& operator+=(F2& a, F2 b) { return a = a + b; }
-// a * b + c
-__device__ __forceinline__ F2 mad(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
+// a * b + c, spelled out so the modal arithmetic below maps to fused multiply-adds.
 __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
 
@@ -236,8 +221,8 @@ struct Pencil<double> {
   static constexpr int PY = 8, KZ = 16, MINB = 2;
 };
 template <>
-struct Pencil<float> {  // KZ odd: the paired-layer kernel (k_fine_op_f2) shares this grid
-  static constexpr int PY = 8, KZ = 15, MINB = 3;
+struct Pencil<float> {
+  static constexpr int PY = 8, KZ = 16, MINB = 3;
 };
 
 template <class T, bool PER = false>
@@ -447,154 +432,6 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
   }
 }
 
-// FP32 operator on pairs of element layers (non-periodic grid).  The pencil
-// schedule above with two element layers per step, ezA = k0 - 1 + 2t and ezA+1,
-// evaluated together in Blackwell's packed FP32x2 instructions: corner c of the
-// pair is (u of element ezA, u of element ezA+1), both elements' modal products
-// cost one FFMA2/FADD2/FMUL2 stream.  The pair's shared node layer ezA+1 is
-// combined inside the thread before the x shuffles and the y exchange, so a step
-// moves three node layers (ezA: element ezA-1 is in pend; ezA+1: complete;
-// ezA+2: the next step's pend) with one __syncthreads for two element layers.
-// KZF odd: (KZF+1)/2 pairs cover element layers k0-1 .. k0+KZF-1 and write node
-// layers k0 .. k0+KZF-1.
-constexpr int kF2PY = 8, kF2KZ = 15, kF2MinB = 2;
-
-__device__ __forceinline__ F2 pk(float a, float b) { return F2(make_float2(a, b)); }
-
-template <int MODE>
-__global__ void __launch_bounds__(32 * kF2PY, kF2MinB)
-    k_fine_op_f2(GridDev g, ModalT<float> mcs, const float* __restrict__ ef,
-                 const uint8_t* __restrict__ kept, const float* __restrict__ x,
-                 const float* __restrict__ b, const float* __restrict__ invdiag, float omega,
-                 float* __restrict__ y, double* __restrict__ dot_part) {
-  constexpr int PY = kF2PY, KZ = kF2KZ;
-  __shared__ float sy[2][PY][9][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int ex = blockIdx.x * 31 - 1 + lane;
-  const int ey = blockIdx.y * (PY - 1) - 1 + w;
-  const int k0 = blockIdx.z * KZ;
-  const bool own_xy = lane >= 1 && w >= 1 && ex < g.nnx && ey < g.nny;
-  const bool exy_ok = ex >= 0 && ex < g.nx && ey >= 0 && ey < g.ny;
-  const int64_t exy = int64_t(ey) * g.nx + ex;
-  const int64_t plane3 = 3 * int64_t(g.nnx) * g.nny, eplane = int64_t(g.nx) * g.ny;
-  const int snx = 3 * g.nnx;
-  const bool vx0 = ex >= 0 && ex < g.nnx, vx1 = ex + 1 < g.nnx;
-  const bool vy0 = ey >= 0 && ey < g.nny, vy1 = ey + 1 < g.nny;
-  const bool msk[2][2] = {{vx0 && vy0, vx1 && vy0}, {vx0 && vy1, vx1 && vy1}};
-  const int64_t oxy = 3 * (int64_t(ey) * g.nnx + ex);
-  ModalT<F2> mc;
-  mc.L0 = F2(mcs.L0);
-  mc.L1 = F2(mcs.L1);
-  mc.M0 = F2(mcs.M0);
-  mc.M1 = F2(mcs.M1);
-  mc.M02 = F2(mcs.M02);
-  mc.M12 = F2(mcs.M12);
-  mc.LM2 = F2(mcs.LM2);
-
-  float L0[2][2][3], L1[2][2][3], L2[2][2][3], rawA[2][2][3], rawB[2][2][3];
-  load_raw_np(x, oxy + (k0 - 1) * plane3, snx, k0 - 1 >= 0 && k0 - 1 < g.nnz, msk, lane, rawA);
-  finish_layer(lane, rawA, L0);
-  load_raw_np(x, oxy + k0 * plane3, snx, k0 < g.nnz, msk, lane, rawA);
-  load_raw_np(x, oxy + (k0 + 1) * plane3, snx, k0 + 1 < g.nnz, msk, lane, rawB);
-  float pend[3] = {0.0f, 0.0f, 0.0f};
-  float dsum = 0.0f;
-#pragma unroll 1
-  for (int t = 0; t < (KZ + 1) / 2; ++t) {
-    const int ezA = k0 - 1 + 2 * t;
-    finish_layer(lane, rawA, L1);
-    finish_layer(lane, rawB, L2);
-    if (2 * t + 2 < KZ + 1) {
-      load_raw_np(x, oxy + (ezA + 3) * plane3, snx, ezA + 3 < g.nnz, msk, lane, rawA);
-      load_raw_np(x, oxy + (ezA + 4) * plane3, snx, ezA + 4 < g.nnz, msk, lane, rawB);
-    }
-    F2 ux[8], uy[8], uz[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      const int xb = c & 1, yb = (c >> 1) & 1, zb = c >> 2;
-      const float(&lo)[2][2][3] = zb ? L1 : L0;
-      const float(&hi)[2][2][3] = zb ? L2 : L1;
-      ux[c] = pk(lo[yb][xb][0], hi[yb][xb][0]);
-      uy[c] = pk(lo[yb][xb][1], hi[yb][xb][1]);
-      uz[c] = pk(lo[yb][xb][2], hi[yb][xb][2]);
-    }
-    const float fA = (exy_ok && ezA >= 0 && ezA < g.nz) ? ef[ezA * eplane + exy] : 0.0f;
-    const float fB = (exy_ok && ezA + 1 < g.nz) ? ef[(ezA + 1) * eplane + exy] : 0.0f;
-    if (fA != 0.0f || fB != 0.0f) {
-      modal_apply(mc, pk(fA, fB), ux, uy, uz);
-    } else {
-#pragma unroll
-      for (int c = 0; c < 8; ++c) ux[c] = uy[c] = uz[c] = F2(0.0f);
-    }
-    // Pair z-combine, then x: lay 0 = node layer ezA (element ezA's bottom),
-    // 1 = ezA+1 (A's top + B's bottom), 2 = ezA+2 (B's top).
-    float Lx[2][3][3];  // [yb][lay][comp] at node x = ex
-#pragma unroll
-    for (int yb = 0; yb < 2; ++yb)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const F2* u = k == 0 ? ux : (k == 1 ? uy : uz);
-        const int c0 = yb << 1;
-        const float m0 = u[c0].v.x, m1 = u[c0 | 4].v.x + u[c0].v.y, m2 = u[c0 | 4].v.y;
-        const float p0 = u[c0 | 1].v.x, p1 = u[c0 | 5].v.x + u[c0 | 1].v.y, p2 = u[c0 | 5].v.y;
-        Lx[yb][0][k] = m0 + __shfl_up_sync(0xffffffffu, p0, 1);
-        Lx[yb][1][k] = m1 + __shfl_up_sync(0xffffffffu, p1, 1);
-        Lx[yb][2][k] = m2 + __shfl_up_sync(0xffffffffu, p2, 1);
-      }
-    const int buf = t & 1;
-#pragma unroll
-    for (int lay = 0; lay < 3; ++lay)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) sy[buf][w][lay * 3 + k][lane] = Lx[1][lay][k];
-    __syncthreads();
-    float N[3][3];
-#pragma unroll
-    for (int lay = 0; lay < 3; ++lay)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        N[lay][k] = Lx[0][lay][k] + (w >= 1 ? sy[buf][w - 1][lay * 3 + k][lane] : 0.0f);
-    if (own_xy) {
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int ez = ezA + half;
-        if ((half == 0 && t == 0) || ez >= g.nnz) continue;
-        const int64_t d0 = oxy + ez * plane3;
-        float node_dot = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const int64_t d = d0 + k;
-          const bool kk = kept == nullptr || kept[d] != 0;
-          const float ax = half == 0 ? pend[k] + N[0][k] : N[1][k];
-          const float xv = half == 0 ? L0[0][0][k] : L1[0][0][k];
-          float out;
-          if (MODE == kApply) {
-            out = kk ? ax : 0.0f;
-            node_dot += xv * out;
-          } else if (MODE == kResidual) {
-            out = kk ? b[d] - ax : 0.0f;
-          } else {
-            out = kk ? xv + omega * invdiag[d] * (b[d] - ax) : 0.0f;
-          }
-          y[d] = out;
-        }
-        if (MODE == kApply) dsum += node_dot;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) pend[k] = N[2][k];
-#pragma unroll
-    for (int yb = 0; yb < 2; ++yb)
-#pragma unroll
-      for (int xb = 0; xb < 2; ++xb)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) L0[yb][xb][k] = L2[yb][xb][k];
-  }
-  if (MODE == kApply && dot_part != nullptr) {
-    const double sum = block_sum(double(dsum));
-    if (threadIdx.x == 0)
-      dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sum;
-  }
-}
-
 template <class T>
 static dim3 pencil_grid(const Grid& g) {
   using P = Pencil<T>;
@@ -612,17 +449,8 @@ static void launch_mode(const Grid& g, const ModalConsts& c, const T* ef, const 
                         double* dot_part, cudaStream_t s) {
   using P = Pencil<T>;
   const GridDev gd{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz};
-  if (std::is_same<T, float>::value) {
-    static_assert(Pencil<float>::PY == kF2PY && Pencil<float>::KZ == kF2KZ, "shared grid");
-    k_fine_op_f2<MODE><<<pencil_grid<float>(g), 32 * kF2PY, 0, s>>>(
-        gd, to_modal<float>(c), reinterpret_cast<const float*>(ef), kept,
-        reinterpret_cast<const float*>(x), reinterpret_cast<const float*>(b),
-        reinterpret_cast<const float*>(invdiag), float(omega), reinterpret_cast<float*>(y),
-        dot_part);
-  } else {
-    k_fine_op<T, P::PY, P::KZ, P::MINB, MODE><<<pencil_grid<T>(g), 32 * P::PY, 0, s>>>(
-        gd, to_modal<T>(c), ef, kept, x, b, invdiag, omega, y, dot_part);
-  }
+  k_fine_op<T, P::PY, P::KZ, P::MINB, MODE><<<pencil_grid<T>(g), 32 * P::PY, 0, s>>>(
+      gd, to_modal<T>(c), ef, kept, x, b, invdiag, omega, y, dot_part);
   TG_LAUNCH_CHECK();
 }
 
