@@ -133,6 +133,7 @@ typedef struct {
   double t_filter_ms, t_solve_ms, t_sensitivity_ms, t_update_ms, t_total_ms;
   double t_device_ms; /* CUDA-event time of the iteration on the job's stream */
   int64_t fine_matvecs, fine_matvecs_lowp;
+  int32_t oc_volume_passes; /* passes over the fields that evaluated the bisection's volumes */
 } tg_simp_iteration;
 
 typedef struct {

@@ -89,7 +89,7 @@ class _Iter(C.Structure):
                 ("t_solve_ms", C.c_double), ("t_sensitivity_ms", C.c_double),
                 ("t_update_ms", C.c_double), ("t_total_ms", C.c_double),
                 ("t_device_ms", C.c_double), ("fine_matvecs", C.c_int64),
-                ("fine_matvecs_lowp", C.c_int64)]
+                ("fine_matvecs_lowp", C.c_int64), ("oc_volume_passes", C.c_int32)]
 
 
 class _Result(C.Structure):

@@ -206,13 +206,15 @@ struct OcState {
   DBuf<int> inexact;
   uint64_t* h_total = nullptr;  // pinned: 3 limbs + flag
   std::vector<double> h_xp;
+  double* h_v = nullptr;  // pinned: kOcMulti candidate volumes
   int64_t n_solid = 0;
-  int fallbacks = 0, evals = 0;
+  int fallbacks = 0, evals = 0, passes = 0;
   bool carry = false;  // oc_update_masked: voxels outside the design set keep x
   void init(const Grid& g, cudaStream_t) {
     for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi}) d->alloc(size_t(g.nv));
-    vpart.alloc(size_t(kRedBlocks));
-    vsum.alloc(1);
+    vpart.alloc(size_t(kRedBlocks) * kOcMulti);
+    vsum.alloc(kOcMulti);
+    TG_CUDA(cudaMallocHost(&h_v, kOcMulti * sizeof(double)));
     part.alloc(size_t(3 * exact_sum_blocks()));
     total.alloc(3);
     inexact.alloc(1);
@@ -220,6 +222,7 @@ struct OcState {
   }
   ~OcState() {
     if (h_total) cudaFreeHost(h_total);
+    if (h_v) cudaFreeHost(h_v);
   }
   size_t bytes() const {
     return dcf.bytes() + dvf.bytes() + xp.bytes() + sq.bytes() + lo.bytes() + hi.bytes() +
@@ -289,14 +292,38 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   const double m = double(fs.st.n);
   const double eps =
       (n + 2.0 * (m + 1.0) + 12.0 + n / (double(kRedBlocks) * 256.0) + 64.0) * u * 1.01;
+  // Fast volumes are computed ahead, kOcMulti lambdas per pass over the fields:
+  // the next doublings while bracketing, the next three levels of the bisection
+  // tree (7 midpoints) while bisecting.  Every branch is still decided one at a
+  // time, in the reference's order, from the volume of exactly the lambda the
+  // sequential loop would test, so the speculation changes no decision.
+  std::vector<std::pair<double, double>> known;  // (lambda, fast volume)
+  auto lookup = [&](double lam, double* V) {
+    for (const auto& kv : known)
+      if (kv.first == lam) {
+        *V = kv.second;
+        return true;
+      }
+    return false;
+  };
+  auto batch = [&](const std::vector<double>& lams) {
+    OcCands cs;
+    cs.k = int(std::min<size_t>(lams.size(), size_t(kOcMulti)));
+    for (int k = 0; k < cs.k; ++k) cs.c[k] = 1.0 / std::sqrt(lams[size_t(k)]);
+    launch_oc_volume_multi(oc.sq.p, oc.lo.p, oc.hi.p, oc.dvf.p, g.nv, cs, oc.vpart.p, oc.vsum.p,
+                           s);
+    TG_CUDA(cudaMemcpyAsync(oc.h_v, oc.vsum.p, sizeof(double) * cs.k, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    ++oc.passes;
+    for (int k = 0; k < cs.k; ++k) known.emplace_back(lams[size_t(k)], oc.h_v[k]);
+  };
   auto eval = [&](double lam) {
     ++oc.evals;
-    launch_oc_volume(oc.sq.p, oc.lo.p, oc.hi.p, oc.dvf.p, g.nv, 1.0 / std::sqrt(lam), oc.vpart.p,
-                     oc.vsum.p, s);
     double V = 0.0;
-    TG_CUDA(cudaMemcpyAsync(oc.h_total, oc.vsum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaStreamSynchronize(s));
-    std::memcpy(&V, oc.h_total, sizeof(double));
+    if (!lookup(lam, &V)) {
+      batch({lam});
+      lookup(lam, &V);
+    }
     const double bound = eps * V / (1.0 - eps) + 1e-300;
     if (std::isfinite(V)) {
       if (V - target > bound) {
@@ -314,9 +341,35 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
     return volume_exceeds(oc, g, act, act_h, target, s);
   };
   double l1 = 0.0, l2 = 1.0;
-  while (l2 < 1e30 && eval(l2)) l2 *= 2.0;
+  double Vtmp = 0.0;
+  while (l2 < 1e30) {
+    if (!lookup(l2, &Vtmp)) {
+      std::vector<double> c;
+      for (double t = l2; int(c.size()) < kOcMulti && t < 1e30; t *= 2.0) c.push_back(t);
+      batch(c);
+    }
+    if (!eval(l2)) break;
+    l2 *= 2.0;
+  }
   for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
     const double lmid = 0.5 * (l1 + l2);
+    if (!lookup(lmid, &Vtmp)) {
+      // The midpoints the next three bisection steps can reach, computed with the
+      // loop's own arithmetic.
+      std::vector<double> c;
+      std::vector<std::pair<double, double>> lv{{l1, l2}};
+      for (int depth = 0; depth < 3; ++depth) {
+        std::vector<std::pair<double, double>> nx;
+        for (const auto& iv : lv) {
+          const double m = 0.5 * (iv.first + iv.second);
+          c.push_back(m);
+          nx.emplace_back(iv.first, m);
+          nx.emplace_back(m, iv.second);
+        }
+        lv.swap(nx);
+      }
+      batch(c);
+    }
     if (eval(lmid))
       l1 = lmid;
     else
@@ -498,7 +551,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   }
   const double c = job_sensitivity(j);
   const double t3 = now_ms();
-  const int fb0 = j->oc.evals;
+  const int fb0 = j->oc.evals, ps0 = j->oc.passes;
   oc_update_device(j->oc, j->filt, g, j->solid.p, j->solid_h, j->x.p, j->dc.p, o.volume_fraction,
                    o.move, j->params.density_min, j->xnew.p, j->s);
   launch_absdiff_max(j->xnew.p, j->x.p, g.nv, j->part.p, j->scal.p + 1, j->s);
@@ -521,6 +574,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   r.mg_levels = st.mg_levels;
   r.used_multigrid = st.used_mg;
   r.oc_volume_evals = j->oc.evals - fb0;
+  r.oc_volume_passes = j->oc.passes - ps0;
   r.t_filter_ms = t1 - t0;
   r.t_solve_ms = t2 - t1;
   r.t_sensitivity_ms = t3 - t2;

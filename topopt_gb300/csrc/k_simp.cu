@@ -353,20 +353,40 @@ __global__ void k_oc_prepare(const double* __restrict__ x, const double* __restr
   }
 }
 
-__global__ void k_oc_volume(const double* __restrict__ sq, const double* __restrict__ lo,
-                            const double* __restrict__ hi, const double* __restrict__ dvf,
-                            int64_t n, double c, double* __restrict__ part) {
-  double acc = 0.0;
+// The linear volume sum_e dv_e clamp(sq_e c, lo_e, hi_e) for up to kOcMulti
+// candidates c = 1/sqrt(lambda) in one pass over the fields (each candidate
+// summed in a fixed per-thread order and tree).
+__global__ void k_oc_volume_multi(const double* __restrict__ sq, const double* __restrict__ lo,
+                                  const double* __restrict__ hi, const double* __restrict__ dvf,
+                                  int64_t n, OcCands cs, double* __restrict__ part) {
+  double acc[kOcMulti];
+#pragma unroll
+  for (int k = 0; k < kOcMulti; ++k) acc[k] = 0.0;
   for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
        e += int64_t(gridDim.x) * kThreads) {
-    double xt = sq[e] * c;
-    const double l = lo[e], h = hi[e];
-    xt = xt < l ? l : xt;
-    xt = xt > h ? h : xt;
-    acc += dvf[e] * xt;
+    const double s = sq[e], l = lo[e], h = hi[e], d = dvf[e];
+#pragma unroll
+    for (int k = 0; k < kOcMulti; ++k) {
+      if (k >= cs.k) break;
+      double xt = s * cs.c[k];
+      xt = xt < l ? l : xt;
+      xt = xt > h ? h : xt;
+      acc[k] += d * xt;
+    }
   }
-  acc = block_sum256(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  for (int k = 0; k < cs.k; ++k) {
+    const double v = block_sum256(acc[k]);
+    if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+// out[k] = sum of part[k][0..n) -- block k, the k_sum_partials tree.
+__global__ void k_sum_partials_multi(const double* __restrict__ part, int n,
+                                     double* __restrict__ out) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) s += part[blockIdx.x * n + i];
+  s = block_sum256(s);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
 
 // Exact fixed-point accumulation: value = A * 2^-128, A a 192-bit unsigned
@@ -547,18 +567,20 @@ void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t
 
 int exact_sum_blocks() { return kRedBlocks; }
 
+void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi,
+                            const double* dvf, int64_t n, const OcCands& cs, double* part,
+                            double* out, cudaStream_t s) {
+  k_oc_volume_multi<<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, cs, part);
+  TG_LAUNCH_CHECK();
+  k_sum_partials_multi<<<cs.k, kThreads, 0, s>>>(part, kRedBlocks, out);
+  TG_LAUNCH_CHECK();
+}
+
 void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, const uint8_t* act,
                        int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
                        cudaStream_t s) {
   k_oc_prepare<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, move, rho_min, sq, lo, hi);
   TG_LAUNCH_CHECK();
-}
-
-void launch_oc_volume(const double* sq, const double* lo, const double* hi, const double* dvf,
-                      int64_t n, double c, double* part, double* out, cudaStream_t s) {
-  k_oc_volume<<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, c, part);
-  TG_LAUNCH_CHECK();
-  launch_sum_partials(part, kRedBlocks, out, s);
 }
 
 void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,

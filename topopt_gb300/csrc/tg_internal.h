@@ -187,6 +187,16 @@ void launch_filter_fwd(const Grid& g, const void* st, int ns, const uint8_t* act
 void launch_filter_adj(const Grid& g, const void* st, int ns, const uint8_t* act,
                        const double* hs, const double* s_in, double* tmp, double* out,
                        cudaStream_t s);
+// Up to kOcMulti bisection candidates (c = 1/sqrt(lambda)) evaluated in one pass.
+constexpr int kOcMulti = 8;
+struct OcCands {
+  int k;
+  double c[kOcMulti];
+};
+// out[k] = sum_e dvf_e clamp(sq_e c_k, lo_e, hi_e); part holds k * kRedBlocks partials.
+void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi,
+                            const double* dvf, int64_t n, const OcCands& cs, double* part,
+                            double* out, cudaStream_t s);
 void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
                          const uint8_t* act, int64_t n, double lambda, double move,
                          double rho_min, bool carry, double* xnew, cudaStream_t s);
@@ -198,8 +208,6 @@ int exact_sum_blocks();
 void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, const uint8_t* act,
                        int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
                        cudaStream_t s);
-void launch_oc_volume(const double* sq, const double* lo, const double* hi, const double* dvf,
-                      int64_t n, double c, double* part, double* out, cudaStream_t s);
 void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,
                       uint64_t* total, int* inexact, cudaStream_t s);
 double fma_probe_tflops(bool fp64);
