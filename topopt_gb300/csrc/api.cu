@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -43,6 +44,53 @@ double now_ms() {
 }  // namespace
 
 void raise(int code, const std::string& msg) { throw Error(code, msg); }
+
+namespace {
+thread_local cudaStream_t t_alloc_stream = nullptr;
+std::mutex g_pin_mu;
+std::vector<char*> g_pin_free;  // free 256-byte pinned slots
+bool g_pool_tuned[64] = {};
+}  // namespace
+
+cudaStream_t alloc_stream() { return t_alloc_stream; }
+
+AllocScope::AllocScope(cudaStream_t s) : prev(t_alloc_stream) {
+  t_alloc_stream = s;
+  // Keep freed blocks in the device pool for the next job instead of returning
+  // them to the system at every synchronisation (process-local pool setting).
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    if (!g_pool_tuned[dev]) {
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = ~uint64_t(0);
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+      g_pool_tuned[dev] = true;
+    }
+  }
+}
+AllocScope::~AllocScope() { t_alloc_stream = prev; }
+
+void* pinned_scalars(size_t bytes) {
+  if (bytes > 256) raise(TG_EINVAL, "pinned_scalars: request above 256 bytes");
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  if (g_pin_free.empty()) {
+    void* slab = nullptr;
+    TG_CUDA(cudaMallocHost(&slab, 64 * 256));  // kept for the life of the process
+    for (int i = 0; i < 64; ++i) g_pin_free.push_back(static_cast<char*>(slab) + 256 * i);
+  }
+  char* p = g_pin_free.back();
+  g_pin_free.pop_back();
+  return p;
+}
+
+void pinned_release(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free.push_back(static_cast<char*>(p));
+}
 int device_ordinal() { return g_device; }
 void set_last_error(const std::string& msg) { g_err = msg; }
 namespace {
@@ -214,15 +262,15 @@ struct OcState {
     for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi}) d->alloc(size_t(g.nv));
     vpart.alloc(size_t(kRedBlocks) * kOcMulti);
     vsum.alloc(kOcMulti);
-    TG_CUDA(cudaMallocHost(&h_v, kOcMulti * sizeof(double)));
+    h_v = static_cast<double*>(pinned_scalars(kOcMulti * sizeof(double)));
     part.alloc(size_t(3 * exact_sum_blocks()));
     total.alloc(3);
     inexact.alloc(1);
-    TG_CUDA(cudaMallocHost(&h_total, 4 * sizeof(uint64_t)));
+    h_total = static_cast<uint64_t*>(pinned_scalars(4 * sizeof(uint64_t)));
   }
   ~OcState() {
-    if (h_total) cudaFreeHost(h_total);
-    if (h_v) cudaFreeHost(h_v);
+    pinned_release(h_total);
+    pinned_release(h_v);
   }
   size_t bytes() const {
     return dcf.bytes() + dvf.bytes() + xp.bytes() + sq.bytes() + lo.bytes() + hi.bytes() +
@@ -385,6 +433,14 @@ using namespace tg;
 
 // ------------------------------------------------------------------ the job
 struct tg_job {
+  // Declared first, destroyed last: every buffer below is allocated
+  // stream-ordered on this stream and freed on it before it goes.
+  struct OwnedStream {
+    cudaStream_t s = nullptr;
+    ~OwnedStream() {
+      if (s) cudaStreamDestroy(s);
+    }
+  } owned;
   cudaStream_t s = nullptr;
   tg_simp_params params{};
   tg_simp_options opt{};
@@ -410,8 +466,7 @@ struct tg_job {
     solver.reset();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    if (h_scal) cudaFreeHost(h_scal);
-    if (s) cudaStreamDestroy(s);
+    pinned_release(h_scal);
   }
   size_t bytes() const {
     size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes() + eff.bytes();
@@ -444,10 +499,12 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   j->params = *params;
   j->opt = o;
   j->opt.solve = default_solve(&o.solve);
-  TG_CUDA(cudaStreamCreateWithFlags(&j->s, cudaStreamNonBlocking));
+  TG_CUDA(cudaStreamCreateWithFlags(&j->owned.s, cudaStreamNonBlocking));
+  j->s = j->owned.s;
   TG_CUDA(cudaEventCreate(&j->ev0));
   TG_CUDA(cudaEventCreate(&j->ev1));
   cudaStream_t s = j->s;
+  AllocScope scope(s);
   tg_grid analysis = *grid;
   std::vector<uint8_t> atags;
   j->masked = mask != nullptr;
@@ -475,7 +532,7 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   j->u.alloc(size_t(g.ndof));
   j->part.alloc(size_t(4 * kRedBlocks + 152 * 32));
   j->scal.alloc(8);
-  TG_CUDA(cudaMallocHost(&j->h_scal, 8 * sizeof(double)));
+  j->h_scal = static_cast<double*>(pinned_scalars(8 * sizeof(double)));
   j->filt.init(g, o.filter_radius, j->solid.p, s);
   j->oc.init(g, s);
   j->oc.n_solid = j->n_solid;
@@ -513,6 +570,7 @@ double job_sensitivity(tg_job* j) {
 
 // Penalised solve at the current physical density.
 SolverStats job_solve(tg_job* j, double tol, int max_it) {
+  AllocScope scope(j->s);  // lazily built state (FP64 fallback hierarchy) is the job's
   const Grid& g = j->fp.g;
   const tg_simp_params& p = j->params;
   launch_modulus(j->xphys.p, j->fp.elem.p, g.nv, p.youngs_modulus, p.penalty, p.density_min,
@@ -532,6 +590,7 @@ void job_filter_x(tg_job* j) {
 
 // One design iteration of simp_optimize's loop body (simp.cpp:2158-2340).
 int job_step(tg_job* j, tg_simp_iteration* row) {
+  AllocScope scope(j->s);
   const Grid& g = j->fp.g;
   const tg_simp_options& o = j->opt;
   tg_simp_iteration r;
@@ -1003,6 +1062,7 @@ void tg_job_destroy(tg_job* job) { delete job; }
 int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* avg_ms) {
   return guarded([&] {
     if (!job || !avg_ms || reps < 1) raise(TG_EINVAL, "job, avg_ms and reps >= 1 required");
+    AllocScope scope(job->s);
     if (!job->xphys_valid) job_filter_x(job);
     const Grid& g = job->fp.g;
     const tg_simp_params& p = job->params;

@@ -471,6 +471,7 @@ extern "C" int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, 
       cudaStream_t s;
       ~StreamGuard() { cudaStreamDestroy(s); }
     } sg{s};
+    AllocScope scope(s);  // buffers below are stream-ordered on s and freed before it
 
     // Element matrix, chi0 and the per-corner loads (scaled by E).
     std::vector<double> ke(576);

@@ -264,9 +264,9 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
                       152 * 32});
   part_.alloc(size_t(part_n_));
   scal_.alloc(32);
-  TG_CUDA(cudaMallocHost(&h_scal_, 32 * sizeof(double)));
+  h_scal_ = static_cast<double*>(pinned_scalars(32 * sizeof(double)));
   istate_.alloc(4);
-  TG_CUDA(cudaMallocHost(&h_ist_, 4 * sizeof(int)));
+  h_ist_ = static_cast<int*>(pinned_scalars(4 * sizeof(int)));
   use_graph_ = opt.graph_mode != TG_GRAPH_OFF;
   if (mixed_) {
     Ef_.alloc(size_t(fp.g.nv));
@@ -287,8 +287,8 @@ struct Solver::InnerGraph {
 
 Solver::~Solver() {
   ig_.reset();
-  if (h_scal_) cudaFreeHost(h_scal_);
-  if (h_ist_) cudaFreeHost(h_ist_);
+  pinned_release(h_scal_);
+  pinned_release(h_ist_);
 }
 
 size_t Solver::device_bytes() const {

@@ -45,38 +45,75 @@ void add_kernel_launches(int64_t delta);  // graph replays / captures
     TG_CUDA(cudaGetLastError());   \
   } while (0)
 
-// Owning device buffer (cudaMallocAsync on the job's stream would tie lifetime to
-// a stream; plain cudaMalloc keeps ownership simple for long-lived job state).
+// Stream-ordered allocation scope.  While an AllocScope is alive on a thread,
+// DBuf allocates with cudaMallocAsync on its stream and later frees with
+// cudaFreeAsync on the same stream; outside any scope it uses cudaMalloc /
+// cudaFree.  cudaMalloc and cudaFree are device-wide serialisation points
+// (cudaFree waits for every stream), so resident jobs that come and go while
+// others run -- the serving loop -- allocate stream-ordered from the device's
+// memory pool instead.  A scope's stream must outlive every buffer allocated in
+// it.
+cudaStream_t alloc_stream();
+struct AllocScope {
+  cudaStream_t prev;
+  explicit AllocScope(cudaStream_t s);
+  ~AllocScope();
+  AllocScope(const AllocScope&) = delete;
+  AllocScope& operator=(const AllocScope&) = delete;
+};
+
+// Pinned host scalars from a process-wide pool (page-locked allocation is also
+// a device-wide serialisation point, so it happens once per slab, not per job).
+void* pinned_scalars(size_t bytes);  // bytes <= 256
+void pinned_release(void* p);
+
+// Owning device buffer.
 template <class T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;  // non-null: stream-ordered allocation on s
   DBuf() = default;
   explicit DBuf(size_t count) { alloc(count); }
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; o.s = nullptr; }
   DBuf& operator=(DBuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    if (this != &o) {
+      release();
+      p = o.p; n = o.n; s = o.s;
+      o.p = nullptr; o.n = 0; o.s = nullptr;
+    }
     return *this;
   }
   ~DBuf() { release(); }
   void alloc(size_t count) {
     release();
     if (count) {
-      cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+      const cudaStream_t as = alloc_stream();
+      void* q = nullptr;
+      cudaError_t e = as ? cudaMallocAsync(&q, count * sizeof(T), as)
+                         : cudaMalloc(&q, count * sizeof(T));
       if (e != cudaSuccess) {
         p = nullptr;
-        raise(TG_ENOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
-                             cudaGetErrorString(e));
+        raise(TG_ENOMEM, "device allocation of " + std::to_string(count * sizeof(T)) +
+                             " bytes failed: " + cudaGetErrorString(e));
       }
+      p = static_cast<T*>(q);
+      s = as;
     }
     n = count;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s)
+        cudaFreeAsync(p, s);
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    s = nullptr;
   }
   size_t bytes() const { return n * sizeof(T); }
 };
