@@ -476,6 +476,7 @@ def run_serve(args):
     from topopt_gb300 import workloads
     from topopt_gb300.build import build
     build()
+    tg.set_sync_mode(args.sync_mode)
     stream = workloads.stream(0, rate=4.0, duration=args.serve_seconds, precision=tg.PREC_MIXED)
     pb, prm, opt = workloads.design(999, iterations=2, sizes=(32, 16, 16))
     tg.simp_optimize(pb, prm, opt)  # warm-up
@@ -553,6 +554,8 @@ def main():
     ap.add_argument("--cells", type=int, default=512)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--max-active", type=int, default=16)
+    ap.add_argument("--sync-mode", type=int, default=0,
+                    help="host wait mode for the serving workloads: 0 default, 2 yield, 3 blocking")
     args = ap.parse_args()
     if args.workload != "cantilever":
         if args.impl == "reference":

@@ -276,6 +276,11 @@ int tg_homogenize(int32_t ncell, int32_t nx, int32_t ny, int32_t nz, double spac
                   int32_t cases_mask, double tolerance, int32_t max_iterations,
                   int32_t precision, double* ch_out, tg_homog_info* info);
 
+/* How host threads wait for the GPU (this process, the current device): 0 the
+ * CUDA default, 1 spin, 2 yield, 3 block on a synchronisation primitive.  Many
+ * concurrent jobs on few host cores wait better with 2 or 3. */
+int tg_set_sync_mode(int32_t mode);
+
 /* ---- serving: continuous batching of optimisation jobs ----
  * No reference counterpart as one interface: the GB300 form of the callers that
  * run simp_optimize once per request (minimize_plastic, the app bridge,

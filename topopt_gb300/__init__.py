@@ -41,6 +41,7 @@ from ._capi import (  # noqa: F401
     oc_update_masked,
     simp_compliance,
     simp_optimize,
+    set_sync_mode,
     COARSEN_ALIGNED,
     COARSEN_DEFAULT,
     COARSEN_REFERENCE,

@@ -139,6 +139,7 @@ def lib():
                                      vp, vp], C.c_int),
         "tg_homogenize": ([i32, i32, i32, i32, dbl, dbl, dbl, vp, i32, dbl, i32, i32, vp, vp],
                           C.c_int),
+        "tg_set_sync_mode": ([i32], C.c_int),
         "tg_server_create": ([vp, vp], C.c_int),
         "tg_server_submit": ([vp, vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_server_wait": ([vp, C.c_int64, vp, vp, vp], C.c_int),
@@ -589,6 +590,11 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def set_sync_mode(mode: int):
+    """How host threads wait for the GPU: 0 default, 1 spin, 2 yield, 3 blocking."""
+    _check(lib().tg_set_sync_mode(int(mode)))
 
 
 def job_estimate_bytes(pb: Problem, options: SimpOptions) -> int:

@@ -341,8 +341,8 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   const double eps =
       (n + 2.0 * (m + 1.0) + 12.0 + n / (double(kRedBlocks) * 256.0) + 64.0) * u * 1.01;
   // Fast volumes are computed ahead, kOcMulti lambdas per pass over the fields:
-  // the next doublings while bracketing, the next three levels of the bisection
-  // tree (7 midpoints) while bisecting.  Every branch is still decided one at a
+  // the next doublings while bracketing, the next four levels of the bisection
+  // tree (15 midpoints) while bisecting.  Every branch is still decided one at a
   // time, in the reference's order, from the volume of exactly the lambda the
   // sequential loop would test, so the speculation changes no decision.
   std::vector<std::pair<double, double>> known;  // (lambda, fast volume)
@@ -402,11 +402,11 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
     const double lmid = 0.5 * (l1 + l2);
     if (!lookup(lmid, &Vtmp)) {
-      // The midpoints the next three bisection steps can reach, computed with the
+      // The midpoints the next four bisection steps can reach, computed with the
       // loop's own arithmetic.
       std::vector<double> c;
       std::vector<std::pair<double, double>> lv{{l1, l2}};
-      for (int depth = 0; depth < 3; ++depth) {
+      for (int depth = 0; depth < 4; ++depth) {
         std::vector<std::pair<double, double>> nx;
         for (const auto& iv : lv) {
           const double m = 0.5 * (iv.first + iv.second);
@@ -455,7 +455,7 @@ struct tg_job {
   std::vector<uint8_t> eff_h;
   DBuf<double> x, xnew, xphys, E, u, dc, part, scal;
   double* h_scal = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evf = nullptr;
   int64_t n_solid = 0;
   int iteration = 0;
   bool xphys_valid = false;
@@ -466,6 +466,7 @@ struct tg_job {
     solver.reset();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (evf) cudaEventDestroy(evf);
     pinned_release(h_scal);
   }
   size_t bytes() const {
@@ -503,6 +504,7 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   j->s = j->owned.s;
   TG_CUDA(cudaEventCreate(&j->ev0));
   TG_CUDA(cudaEventCreate(&j->ev1));
+  TG_CUDA(cudaEventCreate(&j->evf));
   cudaStream_t s = j->s;
   AllocScope scope(s);
   tg_grid analysis = *grid;
@@ -598,7 +600,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   const double t0 = now_ms();
   TG_CUDA(cudaEventRecord(j->ev0, j->s));
   if (!j->xphys_valid) job_filter_x(j);
-  TG_CUDA(cudaStreamSynchronize(j->s));
+  TG_CUDA(cudaEventRecord(j->evf, j->s));  // filter time from events, no host wait here
   const double t1 = now_ms();
   SolverStats st = job_solve(j, o.cg_tolerance, o.cg_max_iterations);
   const double t2 = now_ms();
@@ -621,8 +623,9 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   const double vol = exact_volume(j->oc, g, j->solid.p, j->xphys.p, &exact, j->s);
   TG_CUDA(cudaEventRecord(j->ev1, j->s));
   TG_CUDA(cudaEventSynchronize(j->ev1));
-  float dev_ms = 0.0f;
+  float dev_ms = 0.0f, filt_ms = 0.0f;
   TG_CUDA(cudaEventElapsedTime(&dev_ms, j->ev0, j->ev1));
+  TG_CUDA(cudaEventElapsedTime(&filt_ms, j->ev0, j->evf));
   const double t4 = now_ms();
   j->iteration += 1;
   r.iteration = j->iteration;
@@ -634,7 +637,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   r.used_multigrid = st.used_mg;
   r.oc_volume_evals = j->oc.evals - fb0;
   r.oc_volume_passes = j->oc.passes - ps0;
-  r.t_filter_ms = t1 - t0;
+  r.t_filter_ms = filt_ms;
   r.t_solve_ms = t2 - t1;
   r.t_sensitivity_ms = t3 - t2;
   r.t_update_ms = t4 - t3;
@@ -756,6 +759,16 @@ int tg_set_device(int32_t device) {
 }
 
 const char* tg_version(void) { return "topopt_gb300 0.1 (sm_103a)"; }
+
+int tg_set_sync_mode(int32_t mode) {
+  static const unsigned kFlags[4] = {cudaDeviceScheduleAuto, cudaDeviceScheduleSpin,
+                                     cudaDeviceScheduleYield, cudaDeviceScheduleBlockingSync};
+  if (mode < 0 || mode > 3) {
+    tg::g_err = "tg_set_sync_mode: mode must be 0..3";
+    return TG_EINVAL;
+  }
+  return guarded([&] { TG_CUDA(cudaSetDeviceFlags(kFlags[mode])); });
+}
 
 int tg_hex8_stiffness(double E, double nu, double h, double* ke) {
   try {

@@ -225,7 +225,7 @@ void launch_filter_adj(const Grid& g, const void* st, int ns, const uint8_t* act
                        const double* hs, const double* s_in, double* tmp, double* out,
                        cudaStream_t s);
 // Up to kOcMulti bisection candidates (c = 1/sqrt(lambda)) evaluated in one pass.
-constexpr int kOcMulti = 8;
+constexpr int kOcMulti = 16;
 struct OcCands {
   int k;
   double c[kOcMulti];
