@@ -949,8 +949,11 @@ SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u
   bool solved = false;
   if (have_mg_ && numeric_ok_) {
     if (mixed_) {
+      // The mixed form's inner FP32 iterations are budgeted at 3x the MG budget:
+      // each refinement restarts CG (about 1.3x the iterations of one FP64 run)
+      // and an FP32 iteration costs about 1/6 of the FP64 retry's.
       if (warm) seed();
-      solved = mixed_refine(tol, std::min(cap, budget_), warm, st);
+      solved = mixed_refine(tol, std::min(cap, 3 * budget_), warm, st);
     }
     if (mixed_ && !solved) st.mixed_fallback = true;
     if (!solved && (!mixed_ || build_numeric<double>())) {
