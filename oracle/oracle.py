@@ -156,6 +156,10 @@ class OracleLib:
                 [C.c_int] * 3 + [C.c_double, C.c_void_p, _bp, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
                                  C.c_void_p, _dp, _dp, _dp, _ip, _dp, _dp, C.c_void_p])
+            L.or_heaviside_project.argtypes = [C.c_double] * 3
+            L.or_heaviside_project.restype = C.c_double
+            L.or_heaviside_project_derivative.argtypes = [C.c_double] * 3
+            L.or_heaviside_project_derivative.restype = C.c_double
             L.or_homogenize.argtypes = [C.c_int] * 3 + [C.c_double, C.c_double, C.c_double,
                                                         C.c_void_p, C.c_int, C.c_double, C.c_int,
                                                         _dp, C.POINTER(C.c_int),
@@ -169,6 +173,14 @@ class OracleLib:
             L.ref_oc_update.argtypes = [C.c_int] * 3 + [C.c_void_p, C.c_double, _dp, _dp,
                                                         C.c_double, C.c_double, C.c_double, _dp]
             L.ref_set_threads.argtypes = [C.c_int]
+            L.ref_simp_optimize_projected.argtypes = (
+                [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                 C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                 _dp, _dp, _dp, _dp, _dp, _dp, _ip])
+            L.ref_project.argtypes = [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
             L.ref_effective_design_mask.argtypes = [C.c_int] * 3 + [C.c_void_p, _bp, _bp]
             L.ref_filter_masked.argtypes = [C.c_int] * 3 + [C.c_void_p, _bp, C.c_double, C.c_int,
                                                             _dp, _dp]
@@ -303,6 +315,15 @@ class OracleLib:
                                                g, volfrac, move, rho_min, xn))
         return xn
 
+    def project(self, rt, beta, eta=0.5):
+        """(heaviside_project, its derivative) at rt."""
+        if self.kind == "port":
+            return (self.lib.or_heaviside_project(rt, beta, eta),
+                    self.lib.or_heaviside_project_derivative(rt, beta, eta))
+        v, d = C.c_double(0), C.c_double(0)
+        self._check(self.lib.ref_project(rt, beta, eta, C.byref(v), C.byref(d)))
+        return v.value, d.value
+
     def homogenize(self, nx, ny, nz, solid=None, h=1.0, E=1.0, nu=0.3, cases=0x3F, tol=1e-9,
                    max_it=0):
         """Periodic homogenization of one cell (port only: the reference's is a
@@ -386,7 +407,8 @@ class OracleLib:
                         iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
                         infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
                         hist_vf=hvf[:n], design=design, phys=phys)
-        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it)
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, 0,
+                             None, None, None, 0.5)
         res = _OrSimpResult()
         hcg = np.zeros(max_it, np.int32)
         self._check(self.lib.or_simp_optimize_masked(
@@ -400,26 +422,38 @@ class OracleLib:
                     hist_vf=hvf[:n], hist_cg=hcg[:n], design=design, phys=phys)
 
     def simp_optimize(self, pb: Problem, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3, volfrac=0.3,
-                      radius=1.5, move=0.2, max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0):
-        hc, hch, hvf = np.zeros(max_it), np.zeros(max_it), np.zeros(max_it)
+                      radius=1.5, move=0.2, max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0,
+                      stages=None, eta=0.5):
+        total = sum(s[2] for s in stages) if stages else max_it
+        hc, hch, hvf = np.zeros(total), np.zeros(total), np.zeros(total)
         design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+        ns, sb, sm, si, keep = _stage_arrays(stages)
         if self.kind == "reference":
             sc, ints = np.zeros(3), np.zeros(4, np.int32)
-            self._check(self.lib.ref_simp_optimize(
-                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
-                *pb.bc_args(), volfrac, radius, move, max_it, change_tol, cg_tol, cg_max_it, hc,
-                hch, hvf, design, phys, sc, ints))
+            if stages:
+                self._check(self.lib.ref_simp_optimize_projected(
+                    pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                    *pb.bc_args(), volfrac, radius, change_tol, cg_tol, cg_max_it, ns,
+                    self._ptr(sb), self._ptr(sm), self._ptr(si), eta, hc, hch, hvf, design, phys,
+                    sc, ints))
+            else:
+                self._check(self.lib.ref_simp_optimize(
+                    pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                    *pb.bc_args(), volfrac, radius, move, max_it, change_tol, cg_tol, cg_max_it,
+                    hc, hch, hvf, design, phys, sc, ints))
             n = int(ints[0])
             return dict(compliance=sc[0], volume_fraction=sc[1], initial_compliance=sc[2],
                         iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
                         infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
                         hist_vf=hvf[:n], design=design, phys=phys)
-        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it)
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, ns,
+                             self._ptr(sb), self._ptr(sm), self._ptr(si), eta)
         res = _OrSimpResult()
-        hcg = np.zeros(max_it, np.int32)
+        hcg = np.zeros(total, np.int32)
         self._check(self.lib.or_simp_optimize(
             pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min, *pb.bc_args(),
             C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        del keep
         n = res.iterations
         return dict(compliance=res.compliance, volume_fraction=res.volume_fraction,
                     initial_compliance=res.initial_compliance, iterations=n,
@@ -431,7 +465,23 @@ class OracleLib:
 class _OrSimpOptions(C.Structure):
     _fields_ = [("volume_fraction", C.c_double), ("filter_radius", C.c_double),
                 ("move", C.c_double), ("change_tol", C.c_double), ("cg_tolerance", C.c_double),
-                ("max_iterations", C.c_int), ("cg_max_iterations", C.c_int)]
+                ("max_iterations", C.c_int), ("cg_max_iterations", C.c_int),
+                ("nstages", C.c_int), ("stage_beta", C.c_void_p), ("stage_move", C.c_void_p),
+                ("stage_iterations", C.c_void_p), ("eta", C.c_double)]
+
+
+# heaviside_continuation_schedule (simp.cpp:367-373): (beta, move, iterations).
+CONTINUATION = [(1.0, 0.2, 50), (2.0, 0.2, 50), (4.0, 0.2, 50), (8.0, 0.2, 50), (16.0, 0.1, 50),
+                (32.0, 0.05, 50)]
+
+
+def _stage_arrays(stages):
+    if not stages:
+        return 0, None, None, None, []
+    b = np.ascontiguousarray([s[0] for s in stages], dtype=np.float64)
+    m = np.ascontiguousarray([s[1] for s in stages], dtype=np.float64)
+    it = np.ascontiguousarray([s[2] for s in stages], dtype=np.int32)
+    return len(stages), b, m, it, [b, m, it]
 
 
 class _OrSimpResult(C.Structure):
@@ -451,3 +501,45 @@ def cantilever(nx, ny, nz, total_load=-1.0, spacing=1.0, solid=None):
     nodes = [pb.node(nx, b, cmid) for b in range(ny + 1)]
     loads = [(n, 2, total_load / len(nodes)) for n in nodes]
     return Problem(nx, ny, nz, spacing, solid, bcs, loads)
+
+
+# The Gate V2 benchmark problems and metrics (core/tests/validation/test_gate_v2.cpp:
+# 430-466 for the problems, 275-350 for the metrics).  Both run the locked
+# projected formulation: filter radius 2.5, eta 0.5, CONTINUATION, change_tol 0,
+# solves at 1e-9, volume fraction 0.3, E0 = 1, nu = 0.3, p = 3, rho_min = 1e-3.
+GATE_V2 = ("cantilever_24x8x8", "clamped_beam_48x8x8")
+
+
+def gate_v2_problem(name: str) -> Problem:
+    """cantilever_24x8x8: the x = 0 face clamped, Fz = -1/81 on every node of the
+    x = nx face.  clamped_beam_48x8x8: both end faces clamped, Fz = -1/9 on the
+    nodes (nx/2, b, nz) of the top centre line."""
+    nx = {"cantilever_24x8x8": 24, "clamped_beam_48x8x8": 48}[name]
+    ny = nz = 8
+    pb = Problem(nx, ny, nz)
+
+    def clamp(a):
+        return [(pb.node(a, b, c), k, 0.0) for c in range(nz + 1) for b in range(ny + 1)
+                for k in range(3)]
+
+    if name == "cantilever_24x8x8":
+        bcs = clamp(0)
+        fz = -1.0 / ((ny + 1) * (nz + 1))
+        loads = [(pb.node(nx, b, c), 2, fz) for c in range(nz + 1) for b in range(ny + 1)]
+    else:
+        bcs = clamp(0) + clamp(nx)
+        fz = -1.0 / (ny + 1)
+        loads = [(pb.node(nx // 2, b, nz), 2, fz) for b in range(ny + 1)]
+    return Problem(nx, ny, nz, 1.0, None, bcs, loads)
+
+
+def gate_v2_metrics(nx, ny, nz, rho):
+    """(components, M_nd, y-symmetry error) of a projected density on a solid
+    grid: 6-connected components of rho > 0.5, the mean of 4 rho (1 - rho), and
+    max |rho(i, j, k) - rho(i, ny-1-j, k)|."""
+    from scipy import ndimage
+    r = np.asarray(rho, dtype=np.float64).reshape(nz, ny, nx)
+    _, ncomp = ndimage.label(r > 0.5)
+    mnd = float(np.mean(4.0 * r * (1.0 - r)))
+    ysym = float(np.abs(r - r[:, ::-1, :]).max())
+    return int(ncomp), mnd, ysym

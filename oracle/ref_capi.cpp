@@ -338,4 +338,64 @@ int ref_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* ta
   });
 }
 
+int ref_project(double rt, double beta, double eta, double* value, double* derivative) {
+  return guarded([&] {
+    *value = heaviside_project(rt, beta, eta);
+    *derivative = heaviside_project_derivative(rt, beta, eta);
+  });
+}
+
+// simp_optimize with OC and a Heaviside projection schedule (the projected
+// formulation of simp.cpp:2018-2592), MultigridCG_Matfree.
+int ref_simp_optimize_projected(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                                double nu, double penal, double rho_min, int nbc,
+                                const int* bc_node, const int* bc_comp, const double* bc_val,
+                                int nload, const int* ld_node, const int* ld_comp,
+                                const double* ld_val, double volfrac, double radius,
+                                double change_tol, double cg_tol, int cg_max_it, int nstages,
+                                const double* beta, const double* move, const int* iters,
+                                double eta, double* hist_c, double* hist_change, double* hist_vf,
+                                double* design, double* phys, double* out_scalars,
+                                int* out_ints) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid(nx, ny, nz, h, solid);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    SimpOptions o;
+    o.volume_fraction = volfrac;
+    o.filter_radius = radius;
+    o.change_tol = change_tol;
+    o.cg_tolerance = cg_tol;
+    o.cg_max_iterations = cg_max_it;
+    o.solver = SolverKind::MultigridCG_Matfree;
+    o.projection_eta = eta;
+    for (int k = 0; k < nstages; ++k) {
+      ProjectionStage ps;
+      ps.beta = beta[k];
+      ps.move = move[k];
+      ps.iterations = iters[k];
+      o.projection.push_back(ps);
+    }
+    const SimpOptimizeResult r = simp_optimize(g, p, make_bcs(nbc, bc_node, bc_comp, bc_val),
+                                               make_loads(nload, ld_node, ld_comp, ld_val), o);
+    for (std::size_t i = 0; i < r.history.size(); ++i) {
+      hist_c[i] = r.history[i].compliance;
+      hist_change[i] = r.history[i].change;
+      hist_vf[i] = r.history[i].volume_fraction;
+    }
+    std::memcpy(design, r.design.data(), r.design.size() * sizeof(double));
+    std::memcpy(phys, r.physical_density.data(), r.physical_density.size() * sizeof(double));
+    out_scalars[0] = r.compliance;
+    out_scalars[1] = r.volume_fraction;
+    out_scalars[2] = r.initial_compliance;
+    out_ints[0] = r.iterations;
+    out_ints[1] = r.converged ? 1 : 0;
+    out_ints[2] = r.non_convergent ? 1 : 0;
+    out_ints[3] = r.infeasible ? 1 : 0;
+  });
+}
+
 }  // extern "C"

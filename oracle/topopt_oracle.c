@@ -688,6 +688,109 @@ int or_oc_update(int nx, int ny, int nz, const uint8_t* solid, const or_filter* 
                           lambda_out, nvol_out);
 }
 
+/* heaviside_project / _derivative (simp.cpp:352-365): the tanh threshold. */
+double or_heaviside_project(double rt, double beta, double eta) {
+  const double denom = tanh(beta * eta) + tanh(beta * (1.0 - eta));
+  return (tanh(beta * eta) + tanh(beta * (rt - eta))) / denom;
+}
+double or_heaviside_project_derivative(double rt, double beta, double eta) {
+  const double denom = tanh(beta * eta) + tanh(beta * (1.0 - eta));
+  const double ch = cosh(beta * (rt - eta));
+  return beta / (ch * ch * denom);
+}
+
+/* project_solid / project_active (simp.cpp:1638-1648, :2789): project the design
+ * voxels of a filtered field in place. */
+static void project_design(const uint8_t* design, size_t nv, double* x, double beta, double eta) {
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(design, e)) x[e] = or_heaviside_project(x[e], beta, eta);
+}
+
+/* oc_update_projected (simp.cpp:1665-1726; the masked twin simp.cpp:2798-):
+ * derivative chained before the filter transpose, UNCLAMPED dv with a
+ * non-finite ratio holding the voxel, the volume constraint on the projected
+ * candidate.  masked: frozen voxels keep x and the projected volume sums the
+ * design set (projection of the filter's zeros off the design set is skipped,
+ * as project_active projects Active voxels only). */
+static int oc_update_projected_common(int nx, int ny, int nz, const uint8_t* design, int masked,
+                                      const or_filter* f, const double* density,
+                                      const double* xtilde, const double* dcomp, double beta,
+                                      double eta, double volfrac, double move, double rho_min,
+                                      double* x_new) {
+  const size_t nv = (size_t)nx * ny * nz;
+  double* dc_phys = calloc(nv, sizeof(double));
+  double* dproj = calloc(nv, sizeof(double));
+  double* dc = malloc(nv * sizeof(double));
+  double* dv = malloc(nv * sizeof(double));
+  double* xp = malloc(nv * sizeof(double));
+  size_t n_design = 0;
+  for (size_t e = 0; e < nv; ++e) {
+    if (!is_solid(design, e)) continue;
+    dproj[e] = or_heaviside_project_derivative(xtilde[e], beta, eta);
+    dc_phys[e] = dcomp[e] * dproj[e];
+    ++n_design;
+  }
+  or_filter_sensitivity(f, dc_phys, dc);
+  or_filter_sensitivity(f, dproj, dv);
+  const double target = volfrac * (double)n_design;
+#define CAND(lambda)                                                     \
+  for (size_t e = 0; e < nv; ++e) {                                      \
+    x_new[e] = masked ? density[e] : 0.0;                                \
+    if (!is_solid(design, e)) continue;                                  \
+    const double xe = density[e];                                        \
+    double be = -dc[e] / ((lambda) * dv[e]);                             \
+    if (!isfinite(be)) be = 1.0;                                         \
+    if (be < 0.0) be = 0.0;                                              \
+    double xt = xe * sqrt(be);                                           \
+    const double lo = (rho_min < xe - move) ? xe - move : rho_min;       \
+    const double hi = (xe + move < 1.0) ? xe + move : 1.0;               \
+    if (xt < lo) xt = lo;                                                \
+    if (xt > hi) xt = hi;                                                \
+    x_new[e] = xt;                                                       \
+  }
+#define PVOL(out)                                                        \
+  do {                                                                   \
+    or_filter_density(f, x_new, xp);                                     \
+    double v_ = 0.0;                                                     \
+    for (size_t e = 0; e < nv; ++e)                                      \
+      if (is_solid(design, e)) v_ += or_heaviside_project(xp[e], beta, eta); \
+    (out) = v_;                                                          \
+  } while (0)
+  double l1 = 0.0, l2 = 1.0, V = 0.0;
+  for (;;) {
+    if (!(l2 < 1e30)) break;
+    CAND(l2);
+    PVOL(V);
+    if (!(V > target)) break;
+    l2 *= 2.0;
+  }
+  for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
+    const double lmid = 0.5 * (l1 + l2);
+    CAND(lmid);
+    PVOL(V);
+    if (V > target)
+      l1 = lmid;
+    else
+      l2 = lmid;
+  }
+  {
+    const double lam = 0.5 * (l1 + l2);
+    CAND(lam);
+  }
+#undef CAND
+#undef PVOL
+  free(dc_phys); free(dproj); free(dc); free(dv); free(xp);
+  return OR_OK;
+}
+
+int or_oc_update_projected(int nx, int ny, int nz, const uint8_t* solid, const or_filter* f,
+                           const double* density, const double* xtilde, const double* dc,
+                           double beta, double eta, double volfrac, double move,
+                           double rho_min, double* x_new) {
+  return oc_update_projected_common(nx, ny, nz, solid, 0, f, density, xtilde, dc, beta, eta,
+                                    volfrac, move, rho_min, x_new);
+}
+
 /* effective_design_mask (simp.cpp:2610-2633): Empty -> FrozenVoid, Load and
  * Fixture -> FrozenSolid, everything else keeps the caller's entry. */
 void or_effective_design_mask(int nx, int ny, int nz, const uint8_t* tags, const uint8_t* mask,
@@ -805,49 +908,72 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
       n_design += 1.0;
     }
   }
-  int st = OR_OK;
-  for (int it = 0; it < o->max_iterations; ++it) {
-    or_filter_density(f, x, xphys);
-    if (mask) mask_pins(eff, nv, xphys);
-    double c = 0.0, resid = 0.0;
-    int cgit = 0;
-    st = or_simp_compliance(nx, ny, nz, h, asolid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
-                            bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
-                            o->cg_max_iterations, u, dc, &c, &cgit, &resid);
-    if (st == OR_ENONCONV) {
-      res->non_convergent = 1;
-      st = OR_OK;
-      break;
+  /* The stage plan (build_stage_plan, simp.cpp:1053-1068): one unprojected stage
+   * of max_iterations, or one projected stage per (beta, move, iterations). */
+  const int nst = o->nstages > 0 ? o->nstages : 1;
+  const uint8_t* dset = mask ? active : solid; /* the design set */
+  int st = OR_OK, stop = 0;
+  for (int si = 0; si < nst && !stop; ++si) {
+    const int project = o->nstages > 0;
+    const double beta = project ? o->stage_beta[si] : 0.0;
+    const double move = project ? o->stage_move[si] : o->move;
+    const int iters = project ? o->stage_iterations[si] : o->max_iterations;
+    int stage_conv = 0;
+    for (int it = 0; it < iters; ++it) {
+      or_filter_density(f, x, xphys);
+      if (project) project_design(dset, nv, xphys, beta, o->eta);
+      if (mask) mask_pins(eff, nv, xphys);
+      double c = 0.0, resid = 0.0;
+      int cgit = 0;
+      st = or_simp_compliance(nx, ny, nz, h, asolid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
+                              bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
+                              o->cg_max_iterations, u, dc, &c, &cgit, &resid);
+      if (st == OR_ENONCONV) {
+        res->non_convergent = 1;
+        st = OR_OK;
+        stop = 1;
+        break;
+      }
+      if (st) goto out;
+      if (project) {
+        or_filter_density(f, x, xphys); /* xtilde: the unprojected filtered design */
+        st = oc_update_projected_common(nx, ny, nz, dset, mask != NULL, f, x, xphys, dc, beta,
+                                        o->eta, o->volume_fraction, move, rho_min, xnew);
+      } else {
+        st = mask ? or_oc_update_masked(nx, ny, nz, eff, f, x, dc, o->volume_fraction, move,
+                                        rho_min, xnew, NULL, NULL)
+                  : or_oc_update(nx, ny, nz, solid, f, x, dc, o->volume_fraction, move, rho_min,
+                                 xnew, NULL, NULL);
+      }
+      if (st) goto out;
+      double change = 0.0;
+      for (size_t e = 0; e < nv; ++e) change = fmax(change, fabs(xnew[e] - x[e]));
+      memcpy(x, xnew, nv * sizeof(double));
+      if (res->iterations == 0) res->initial_compliance = c;
+      const int n = res->iterations++;
+      or_filter_density(f, x, xphys);
+      if (project) project_design(dset, nv, xphys, beta, o->eta);
+      double vol = 0.0;
+      for (size_t e = 0; e < nv; ++e) vol += xphys[e];
+      hist_c[n] = c;
+      hist_change[n] = change;
+      hist_vf[n] = n_design > 0.0 ? vol / n_design : 0.0;
+      hist_cg[n] = cgit;
+      if (rung_infeasible(hist_c, hist_cg, res->iterations)) {
+        res->infeasible = 1;
+        stop = 1;
+        break;
+      }
+      if (change < o->change_tol) { /* stage_should_stop: on to the next stage */
+        stage_conv = 1;
+        break;
+      }
     }
-    if (st) goto out;
-    st = mask ? or_oc_update_masked(nx, ny, nz, eff, f, x, dc, o->volume_fraction, o->move,
-                                    rho_min, xnew, NULL, NULL)
-              : or_oc_update(nx, ny, nz, solid, f, x, dc, o->volume_fraction, o->move, rho_min,
-                             xnew, NULL, NULL);
-    if (st) goto out;
-    double change = 0.0;
-    for (size_t e = 0; e < nv; ++e) change = fmax(change, fabs(xnew[e] - x[e]));
-    memcpy(x, xnew, nv * sizeof(double));
-    if (res->iterations == 0) res->initial_compliance = c;
-    const int n = res->iterations++;
-    or_filter_density(f, x, xphys);
-    double vol = 0.0;
-    for (size_t e = 0; e < nv; ++e) vol += xphys[e];
-    hist_c[n] = c;
-    hist_change[n] = change;
-    hist_vf[n] = n_design > 0.0 ? vol / n_design : 0.0;
-    hist_cg[n] = cgit;
-    if (rung_infeasible(hist_c, hist_cg, res->iterations)) {
-      res->infeasible = 1;
-      break;
-    }
-    if (change < o->change_tol) {
-      res->converged = 1;
-      break;
-    }
+    res->converged = stage_conv;
   }
   memcpy(design, x, nv * sizeof(double));
   or_filter_density(f, x, phys);
+  if (o->nstages > 0) project_design(dset, nv, phys, o->stage_beta[nst - 1], o->eta);
   double vol_final = 0.0; /* of the unpinned field (simp.cpp:3614, :3652) */
   for (size_t e = 0; e < nv; ++e) vol_final += phys[e];
   if (mask) mask_pins(eff, nv, phys);

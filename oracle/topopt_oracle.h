@@ -118,14 +118,32 @@ int or_oc_update_masked(int nx, int ny, int nz, const uint8_t* eff, const or_fil
                         const double* density, const double* dc, double volfrac, double move,
                         double rho_min, double* x_new, double* lambda_out, int* nvol_out);
 
-/* Plain simp_optimize with the OC updater and no projection (simp.cpp:2018-2592).
+/* Plain simp_optimize with the OC updater (simp.cpp:2018-2592), with or
+ * without a projection schedule.
  * The solve is the exact Jacobi-PCG above.  hist_* have room for max_it rows.
  * Guards: change_tol stop; rung-infeasibility window (simp.cpp:1140-1186) with
  * the reference defaults; non-convergence ends the run. */
 typedef struct {
   double volume_fraction, filter_radius, move, change_tol, cg_tolerance;
   int max_iterations, cg_max_iterations;
+  /* Heaviside projection schedule (SimpOptions::projection, simp.hpp:519-525,
+   * :1443-1444): nstages = 0 is the unprojected loop; otherwise stage k runs
+   * stage_iterations[k] OC iterations at (stage_beta[k], stage_move[k]). */
+  int nstages;
+  const double* stage_beta;
+  const double* stage_move;
+  const int* stage_iterations;
+  double eta;
 } or_simp_options;
+
+/* heaviside_project and its derivative (simp.cpp:352-365). */
+double or_heaviside_project(double rt, double beta, double eta);
+double or_heaviside_project_derivative(double rt, double beta, double eta);
+/* oc_update_projected (simp.cpp:1665-1726); xtilde = filter_density(density). */
+int or_oc_update_projected(int nx, int ny, int nz, const uint8_t* solid, const or_filter* f,
+                           const double* density, const double* xtilde, const double* dc,
+                           double beta, double eta, double volfrac, double move,
+                           double rho_min, double* x_new);
 typedef struct {
   int iterations, converged, non_convergent, infeasible;
   double compliance, volume_fraction, initial_compliance;

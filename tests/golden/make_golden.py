@@ -18,9 +18,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
 
-from oracle.oracle import OracleLib, Problem, build_reference, cantilever  # noqa: E402
+from oracle.oracle import (CONTINUATION, GATE_V2, OracleLib, Problem, build_reference,  # noqa: E402
+                           cantilever, gate_v2_problem)
 
 REF_KE_JSON = "/root/reference/core/tests/fixtures/fea/hex_stiffness_reference.json"
+BENCH_JSON = "/root/reference/core/tests/fixtures/benchmarks.json"
 
 
 def main():
@@ -127,6 +129,75 @@ def main():
                cfg0_hist_vf=s0["hist_vf"], cfg0_design=s0["design"],
                cfg0_compliance=np.array(s0["compliance"]),
                cfg0_iterations=np.array(s0["iterations"]))
+
+    # Heaviside projection: value and derivative at the fixture's spot values
+    # and on a dense grid of rho_tilde, from the reference's own functions.
+    rts = np.concatenate([[0.0, 0.3, 0.5, 0.7, 1.0], np.linspace(0.0, 1.0, 41)])
+    betas = np.array([1.0, 2.0, 4.0, 8.0, 16.0, 32.0, 64.0])
+    pv = np.zeros((betas.size, rts.size))
+    pd = np.zeros_like(pv)
+    for i, b in enumerate(betas):
+        for j, rt in enumerate(rts):
+            pv[i, j], pd[i, j] = R.project(float(rt), float(b), 0.5)
+    out.update(proj_rt=rts, proj_beta=betas, proj_value=pv, proj_deriv=pd)
+    bench = json.load(open(BENCH_JSON))
+    unit = bench["projection_unit_reference"]
+    for b in (1, 8, 32):
+        for rt in ("0.0", "0.3", "0.5", "0.7", "1.0"):
+            spot = unit[f"beta_{b}"][f"rt_{rt}"]
+            v, d = R.project(float(rt), float(b), 0.5)
+            assert abs(v - spot["value"]) <= 1e-12 * max(abs(spot["value"]), 1e-300) + \
+                (1e-12 if spot["value"] == 0.0 else 0.0), (b, rt)
+            assert abs(d - spot["derivative"]) <= 1e-12 * abs(spot["derivative"]), (b, rt)
+
+    # A short projected run (three continuation stages) on the 12x4x4 cantilever.
+    pstages = [(1.0, 0.2, 8), (4.0, 0.2, 8), (16.0, 0.1, 6)]
+    sp = R.simp_optimize(pb3, volfrac=0.3, radius=1.5, change_tol=0.0, cg_tol=1e-10,
+                         stages=pstages)
+    out.update(psimp_stages=np.array(pstages), psimp_hist_c=sp["hist_c"],
+               psimp_hist_change=sp["hist_change"], psimp_hist_vf=sp["hist_vf"],
+               psimp_design=sp["design"], psimp_phys=sp["phys"],
+               psimp_compliance=np.array(sp["compliance"]),
+               psimp_volume_fraction=np.array(sp["volume_fraction"]),
+               psimp_iterations=np.array(sp["iterations"]))
+
+    # Gate V2: the two benchmark problems under the locked projected formulation,
+    # run by the reference (300 iterations), and the fixture's gates.
+    for name in GATE_V2:
+        key = "gv2c" if name.startswith("cantilever") else "gv2b"
+        g = gate_v2_problem(name)
+        r = R.simp_optimize(g, volfrac=0.3, radius=2.5, change_tol=0.0, cg_tol=1e-9,
+                            stages=CONTINUATION)
+        b = bench["benchmarks"][name]
+        ref, gates = b["reference"], b["gates"]
+        se = ref["stage_end_compliance"]
+        band = gates.get("final_analysis_compliance_band")
+        final = gates.get("final_analysis_compliance")
+        out.update({
+            f"{key}_hist_c": r["hist_c"], f"{key}_hist_change": r["hist_change"],
+            f"{key}_design": r["design"], f"{key}_phys": r["phys"],
+            f"{key}_compliance": np.array(r["compliance"]),
+            f"{key}_volume_fraction": np.array(r["volume_fraction"]),
+            f"{key}_fix_stage_end": np.array([se[k] for k in ("1", "2", "4", "8", "16", "32")]),
+            f"{key}_fix_final": np.array(ref["final_analysis_compliance"]),
+            f"{key}_fix_vf": np.array(ref["achieved_projected_volume_fraction"]),
+            f"{key}_gate_rel": np.array([gates["stage_end_compliance_beta_1"]["rel_tolerance"],
+                                         gates["stage_end_compliance_beta_8"]["rel_tolerance"]]),
+            f"{key}_gate_final": np.array(band if band else
+                                          [final["value"], final["rel_tolerance"]]),
+            f"{key}_gate_final_is_band": np.array(band is not None),
+            f"{key}_gate_vf_abs": np.array(gates["achieved_projected_volume_fraction_abs_tolerance"]),
+            f"{key}_gate_components": np.array(gates["connected_components_at_0p5"]),
+            f"{key}_gate_ysym": np.array(gates["y_symmetry_error_max"]),
+            f"{key}_gate_mnd": np.array(gates["discreteness_Mnd_max"]),
+        })
+
+    old = os.path.join(HERE, "golden.npz")
+    if os.path.exists(old):  # regenerating must not move any earlier vector
+        with np.load(old) as z:
+            for k in z.files:
+                if k in out and not np.array_equal(z[k], out[k]):
+                    raise SystemExit(f"golden array {k} changed on regeneration")
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
 

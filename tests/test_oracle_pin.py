@@ -155,3 +155,85 @@ def test_cfg0_trajectory_prefix(port, golden):
     assert np.array_equal(s["hist_c"], golden["cfg0_hist_c"][:10])
     assert np.array_equal(s["hist_change"], golden["cfg0_hist_change"][:10])
     assert np.array_equal(s["hist_vf"], golden["cfg0_hist_vf"][:10])
+
+
+BENCH_JSON = "/root/reference/core/tests/fixtures/benchmarks.json"
+
+
+def test_projection_golden(port, golden):
+    """heaviside_project and its derivative (simp.cpp projection helpers) on a
+    grid of rho_tilde and beta, against the reference's own values."""
+    for i, b in enumerate(golden["proj_beta"]):
+        for j, rt in enumerate(golden["proj_rt"]):
+            v, d = port.project(float(rt), float(b), 0.5)
+            assert abs(v - golden["proj_value"][i, j]) <= 1e-15 * max(1.0, abs(v))
+            assert abs(d - golden["proj_deriv"][i, j]) <= 1e-14 * max(1e-300, abs(d))
+
+
+@pytest.mark.skipif(not os.path.exists(BENCH_JSON), reason="reference tree not mounted")
+def test_projection_unit_reference_fixture(port):
+    """The 15 analytic spot values of benchmarks.json at rel 1e-12
+    (test_gate_v2.cpp:371-392)."""
+    unit = json.load(open(BENCH_JSON))["projection_unit_reference"]
+    n = 0
+    for bkey, spots in unit.items():
+        if not bkey.startswith("beta_"):
+            continue
+        b = float(bkey[5:])
+        for rkey, spot in spots.items():
+            v, d = port.project(float(rkey[3:]), b, 0.5)
+            for got, want in ((v, spot["value"]), (d, spot["derivative"])):
+                assert abs(got - want) <= 1e-12 * (abs(want) if want != 0.0 else 1.0)
+            n += 1
+    assert n == 15
+
+
+def test_projected_simp_loop_golden(port, golden):
+    """simp_optimize with a three-stage beta continuation (oc_update_projected,
+    the stage loop, the final projection) bit-identical to the reference."""
+    pb = cantilever(12, 4, 4)
+    stages = [tuple(s) for s in golden["psimp_stages"].tolist()]
+    stages = [(b, m, int(it)) for b, m, it in stages]
+    s = port.simp_optimize(pb, volfrac=0.3, radius=1.5, change_tol=0.0, cg_tol=1e-10,
+                           stages=stages)
+    assert s["iterations"] == int(golden["psimp_iterations"]) == 22
+    for k in ("hist_c", "hist_change", "hist_vf", "design", "phys"):
+        assert np.array_equal(s[k], golden["psimp_" + k]), k
+    assert s["compliance"] == float(golden["psimp_compliance"])
+    assert s["volume_fraction"] == float(golden["psimp_volume_fraction"])
+
+
+def test_gate_v2_first_stage_prefix(port, golden):
+    """The Gate V2 cantilever (24x8x8, rmin 2.5, solves at 1e-9): the beta = 1
+    stage of the oracle's loop equals the reference's, all 50 iterations."""
+    from oracle.oracle import CONTINUATION, gate_v2_problem
+    s = port.simp_optimize(gate_v2_problem("cantilever_24x8x8"), volfrac=0.3, radius=2.5,
+                           change_tol=0.0, cg_tol=1e-9, stages=CONTINUATION[:1])
+    assert np.array_equal(s["hist_c"], golden["gv2c_hist_c"][:50])
+    assert np.array_equal(s["hist_change"], golden["gv2c_hist_change"][:50])
+
+
+@pytest.mark.parametrize("key", ["gv2c", "gv2b"])
+def test_gate_v2_reference_runs_pass_gates(golden, key):
+    """The reference's own 300-iteration runs in the golden file satisfy the
+    fixture's gates (the gates the CUDA path is held to)."""
+    from oracle.oracle import gate_v2_metrics
+    hc = golden[key + "_hist_c"]
+    se = golden[key + "_fix_stage_end"]
+    rel1, rel8 = golden[key + "_gate_rel"]
+    assert hc.size == 300
+    assert abs(hc[49] - se[0]) <= rel1 * se[0]
+    assert abs(hc[199] - se[3]) <= rel8 * se[3]
+    c = float(golden[key + "_compliance"])
+    g = golden[key + "_gate_final"]
+    if bool(golden[key + "_gate_final_is_band"]):
+        assert g[0] <= c <= g[1]
+    else:
+        assert abs(c - g[0]) <= g[1] * g[0]
+    assert abs(float(golden[key + "_volume_fraction"]) - float(golden[key + "_fix_vf"])) <= \
+        float(golden[key + "_gate_vf_abs"])
+    nx = 24 if key == "gv2c" else 48
+    ncomp, mnd, ysym = gate_v2_metrics(nx, 8, 8, golden[key + "_phys"])
+    assert ncomp == int(golden[key + "_gate_components"])
+    assert ysym <= float(golden[key + "_gate_ysym"])
+    assert mnd <= float(golden[key + "_gate_mnd"])
