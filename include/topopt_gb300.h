@@ -117,11 +117,30 @@ typedef struct {
   double t_build_ms, t_mg_build_ms, t_solve_ms, t_total_ms;
 } tg_cg_info;
 
-/* The OC subset of SimpOptions (core/include/topopt/simp.hpp:1028-1138). */
+/* One stage of the Heaviside beta continuation (ProjectionStage,
+ * core/include/topopt/simp.hpp:519-523). */
+typedef struct {
+  double beta;        /* projection sharpness, finite and > 0 */
+  double move;        /* OC move limit of the stage, > 0 */
+  int32_t iterations; /* OC iterations of the stage, >= 1 */
+} tg_projection_stage;
+
+/* The OC subset of SimpOptions (core/include/topopt/simp.hpp:1028-1138,
+ * projection and projection_eta :1426-1444).  projection NULL or
+ * projection_stages 0: the unprojected loop, governed by move and
+ * max_iterations.  Otherwise the stages run in order, each its own iterations
+ * at its own beta and move (a stage ends early when the design change drops
+ * below change_tol), the analysis density is heaviside_project(filter(x), beta,
+ * projection_eta) on the design voxels and the volume constraint is on that
+ * projected density; projection_eta must then be in (0, 1) (the reference's
+ * default is 0.5). */
 typedef struct {
   double volume_fraction, filter_radius, move, change_tol, cg_tolerance;
   int32_t max_iterations, cg_max_iterations;
   tg_solve_options solve;
+  const tg_projection_stage* projection;
+  int32_t projection_stages;
+  double projection_eta;
 } tg_simp_options;
 
 /* One row of the per-iteration record (SimpIteration + the observation fields
@@ -134,6 +153,7 @@ typedef struct {
   double t_device_ms; /* CUDA-event time of the iteration on the job's stream */
   int64_t fine_matvecs, fine_matvecs_lowp;
   int32_t oc_volume_passes; /* passes over the fields that evaluated the bisection's volumes */
+  double beta; /* projection sharpness of this iteration's stage; 0 when unprojected */
 } tg_simp_iteration;
 
 typedef struct {
@@ -225,10 +245,35 @@ int tg_oc_update_masked(const tg_grid* grid, const uint8_t* mask, double radius,
                         double volume_fraction, double move, double density_min,
                         double* x_new);
 
+/* heaviside_project and heaviside_project_derivative (simp.hpp:506-514;
+ * simp.cpp:352-365) of n values of rho_tilde, on the device: value and
+ * derivative may each be NULL.  beta must be finite and > 0, eta in (0, 1).
+ * Computed with the device's tanh and cosh, so within a few units in the last
+ * place of the host library's values. */
+int tg_heaviside_project(int64_t n, const double* rho_tilde, double beta, double eta,
+                         double* value, double* derivative);
+
+/* heaviside_continuation_schedule (simp.hpp:530; simp.cpp:367-374): the locked
+ * six-stage schedule, beta 1 -> 32 doubling, 50 iterations each, move 0.2 up to
+ * beta 8, 0.1 at 16, 0.05 at 32.  Writes min(cap, 6) stages to out (may be NULL
+ * with cap 0) and returns 6. */
+int32_t tg_heaviside_continuation_schedule(tg_projection_stage* out, int32_t cap);
+
+/* oc_update_projected (simp.cpp:1665-1726): the projection derivative at xtilde
+ * (= filter(density)) chained before the filter transpose for dc and dv, the
+ * ratio -dc/(lambda dv) with unclamped dv (a non-finite ratio holds the voxel),
+ * and the bisection on the projected volume sum heaviside_project(filter(x_new))
+ * over the solid voxels. */
+int tg_oc_update_projected(const tg_grid* grid, double radius, const double* density,
+                           const double* xtilde, const double* dcompliance, double beta,
+                           double eta, double volume_fraction, double move, double density_min,
+                           double* x_new);
+
 /* simp_optimize (core/include/topopt/simp.hpp:1783-1786; simp.cpp:2018-2592):
- * the OC loop with no projection.  history (max_iterations rows), design_out and
- * phys_out (voxels) may be NULL; cancel (may be NULL) is polled once per
- * iteration, before the solve (simp.cpp:2161). */
+ * the OC loop, unprojected or with a beta-continuation plan in
+ * options->projection.  history (max_iterations rows, or the plan's total
+ * iterations), design_out and phys_out (voxels) may be NULL; cancel (may be
+ * NULL) is polled once per iteration, before the solve (simp.cpp:2161). */
 int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
                      const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
                      int32_t nloads, const tg_simp_options* options, tg_progress_fn progress,
@@ -237,7 +282,8 @@ int tg_simp_optimize(const tg_grid* grid, const tg_simp_params* params,
                      tg_simp_result* result);
 
 /* The masked overload, simp_optimize(grid, params, bcs, loads, options, mask)
- * (simp.hpp:1820-1824; simp.cpp:2989-3640), OC, no projection: the analysis
+ * (simp.hpp:1820-1824; simp.cpp:2989-3640), OC with or without projection (the
+ * projection acts on the Active voxels, project_active simp.cpp:2789): the analysis
  * grid drops FrozenVoid voxels, the physical density is pinned (FrozenSolid 1,
  * FrozenVoid 0) before each solve and in phys_out, and volume fractions are
  * over the Active voxels. */
@@ -339,9 +385,15 @@ int tg_job_create_masked(const tg_grid* grid, const tg_simp_params* params,
                          const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
                          int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
                          tg_job** job_out);
-/* One design iteration on the device: filter, solve, sensitivities, OC update. */
+/* One design iteration on the device: filter, solve, sensitivities, OC update
+ * (projected, at the current stage's beta and move, when the options carry a
+ * projection plan). */
 int tg_job_step(tg_job* job, tg_simp_iteration* row);
-/* Copy the current design x and physical density filter(x) to the host. */
+/* Select the stage of the options' projection plan the next steps run
+ * (0 <= stage < projection_stages; stage 0 at creation). */
+int tg_job_set_stage(tg_job* job, int32_t stage);
+/* Copy the current design x and physical density (filter(x), projected at the
+ * current stage's beta, pinned for masked jobs) to the host. */
 int tg_job_read(tg_job* job, double* design_out, double* phys_out);
 /* Replace the design with a host field (voxels). */
 int tg_job_write_design(tg_job* job, const double* design);

@@ -156,6 +156,8 @@ class OracleLib:
                 [C.c_int] * 3 + [C.c_double, C.c_void_p, _bp, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
                                  C.c_void_p, _dp, _dp, _dp, _ip, _dp, _dp, C.c_void_p])
+            L.or_oc_update_projected.argtypes = ([C.c_int] * 3 + [C.c_void_p, C.c_void_p] +
+                                                 [_dp] * 3 + [C.c_double] * 5 + [_dp])
             L.or_heaviside_project.argtypes = [C.c_double] * 3
             L.or_heaviside_project.restype = C.c_double
             L.or_heaviside_project_derivative.argtypes = [C.c_double] * 3
@@ -315,6 +317,22 @@ class OracleLib:
                                                g, volfrac, move, rho_min, xn))
         return xn
 
+    def oc_update_projected(self, pb: Problem, density, xtilde, dc, beta, volfrac, radius=1.5,
+                            move=0.2, rho_min=1e-3, eta=0.5):
+        """oc_update_projected (simp.cpp:1665-1726), port only."""
+        if self.kind != "port":
+            raise OracleError(1, "oc_update_projected: port only")
+        xn = np.zeros(pb.nv)
+        d, xt, g = (np.ascontiguousarray(a, dtype=np.float64) for a in (density, xtilde, dc))
+        f = self.lib.or_filter_make(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), None, radius)
+        try:
+            self._check(self.lib.or_oc_update_projected(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid),
+                                                        f, d, xt, g, beta, eta, volfrac, move,
+                                                        rho_min, xn))
+        finally:
+            self.lib.or_filter_free(f)
+        return xn
+
     def project(self, rt, beta, eta=0.5):
         """(heaviside_project, its derivative) at rt."""
         if self.kind == "port":
@@ -392,8 +410,13 @@ class OracleLib:
 
     def simp_optimize_masked(self, pb: Problem, mask, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3,
                              volfrac=0.3, radius=1.5, move=0.2, max_it=50, change_tol=0.01,
-                             cg_tol=1e-8, cg_max_it=0):
+                             cg_tol=1e-8, cg_max_it=0, stages=None, eta=0.5):
         m = np.ascontiguousarray(mask, dtype=np.uint8)
+        if stages:
+            if self.kind != "port":
+                raise OracleError(1, "simp_optimize_masked with stages: port only")
+            max_it = sum(s[2] for s in stages)
+        ns, sb, sm, si, keep = _stage_arrays(stages)
         hc, hch, hvf = np.zeros(max_it), np.zeros(max_it), np.zeros(max_it)
         design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
         if self.kind == "reference":
@@ -407,13 +430,14 @@ class OracleLib:
                         iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
                         infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
                         hist_vf=hvf[:n], design=design, phys=phys)
-        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, 0,
-                             None, None, None, 0.5)
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, ns,
+                             self._ptr(sb), self._ptr(sm), self._ptr(si), eta)
         res = _OrSimpResult()
         hcg = np.zeros(max_it, np.int32)
         self._check(self.lib.or_simp_optimize_masked(
             pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), m, E0, nu, penal, rho_min,
             *pb.bc_args(), C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        del keep
         n = res.iterations
         return dict(compliance=res.compliance, volume_fraction=res.volume_fraction,
                     initial_compliance=res.initial_compliance, iterations=n,

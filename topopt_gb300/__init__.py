@@ -39,6 +39,9 @@ from ._capi import (  # noqa: F401
     make_density_filter,
     oc_update,
     oc_update_masked,
+    oc_update_projected,
+    heaviside_project,
+    heaviside_continuation_schedule,
     simp_compliance,
     simp_optimize,
     set_sync_mode,

@@ -74,11 +74,16 @@ class _CgInfo(C.Structure):
                 ("t_total_ms", C.c_double)]
 
 
+class _ProjStage(C.Structure):
+    _fields_ = [("beta", C.c_double), ("move", C.c_double), ("iterations", C.c_int32)]
+
+
 class _SimpOpt(C.Structure):
     _fields_ = [("volume_fraction", C.c_double), ("filter_radius", C.c_double),
                 ("move", C.c_double), ("change_tol", C.c_double), ("cg_tolerance", C.c_double),
                 ("max_iterations", C.c_int32), ("cg_max_iterations", C.c_int32),
-                ("solve", _SolveOpt)]
+                ("solve", _SolveOpt), ("projection", C.POINTER(_ProjStage)),
+                ("projection_stages", C.c_int32), ("projection_eta", C.c_double)]
 
 
 class _Iter(C.Structure):
@@ -89,7 +94,8 @@ class _Iter(C.Structure):
                 ("t_solve_ms", C.c_double), ("t_sensitivity_ms", C.c_double),
                 ("t_update_ms", C.c_double), ("t_total_ms", C.c_double),
                 ("t_device_ms", C.c_double), ("fine_matvecs", C.c_int64),
-                ("fine_matvecs_lowp", C.c_int64), ("oc_volume_passes", C.c_int32)]
+                ("fine_matvecs_lowp", C.c_int64), ("oc_volume_passes", C.c_int32),
+                ("beta", C.c_double)]
 
 
 class _Result(C.Structure):
@@ -140,6 +146,10 @@ def lib():
         "tg_homogenize": ([i32, i32, i32, i32, dbl, dbl, dbl, vp, i32, dbl, i32, i32, vp, vp],
                           C.c_int),
         "tg_set_sync_mode": ([i32], C.c_int),
+        "tg_heaviside_project": ([C.c_int64, vp, dbl, dbl, vp, vp], C.c_int),
+        "tg_heaviside_continuation_schedule": ([vp, i32], C.c_int32),
+        "tg_oc_update_projected": ([vp, dbl, vp, vp, vp, dbl, dbl, dbl, dbl, dbl, vp], C.c_int),
+        "tg_job_set_stage": ([vp, i32], C.c_int),
         "tg_server_create": ([vp, vp], C.c_int),
         "tg_server_submit": ([vp, vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_server_wait": ([vp, C.c_int64, vp, vp, vp], C.c_int),
@@ -274,11 +284,35 @@ class SimpOptions:
     max_iterations: int = 200
     cg_max_iterations: int = 0
     solve: SolveOptions = field(default_factory=SolveOptions)
+    # Heaviside projection + beta continuation (simp.hpp:1426-1444): a list of
+    # (beta, move, iterations) stages; empty = the unprojected loop.
+    projection: list = field(default_factory=list)
+    projection_eta: float = 0.5
+
+    def total_iterations(self) -> int:
+        if self.projection:
+            return int(sum(int(s[2]) for s in self.projection))
+        return int(self.max_iterations)
 
     def _c(self):
-        return _SimpOpt(self.volume_fraction, self.filter_radius, self.move, self.change_tol,
-                        self.cg_tolerance, self.max_iterations, self.cg_max_iterations,
-                        self.solve._c())
+        o = _SimpOpt(self.volume_fraction, self.filter_radius, self.move, self.change_tol,
+                     self.cg_tolerance, self.max_iterations, self.cg_max_iterations,
+                     self.solve._c())
+        if self.projection:
+            arr = (_ProjStage * len(self.projection))(
+                *[_ProjStage(float(b), float(m), int(it)) for b, m, it in self.projection])
+            o.projection = C.cast(arr, C.POINTER(_ProjStage))  # kept alive by o._objects
+            o._stages = arr
+            o.projection_stages = len(self.projection)
+        o.projection_eta = self.projection_eta
+        return o
+
+
+def heaviside_continuation_schedule():
+    """heaviside_continuation_schedule (simp.hpp:530): [(beta, move, iterations)]."""
+    buf = (_ProjStage * 8)()
+    n = lib().tg_heaviside_continuation_schedule(C.cast(buf, C.c_void_p), 8)
+    return [(buf[i].beta, buf[i].move, buf[i].iterations) for i in range(n)]
 
 
 @dataclass
@@ -450,6 +484,26 @@ def oc_update_masked(pb: Problem, radius, mask, density, dcompliance, volume_fra
     return out
 
 
+def heaviside_project(rho_tilde, beta, eta=0.5):
+    """heaviside_project and its derivative (simp.hpp:506-514) of an array, on
+    the device: returns (value, derivative)."""
+    rt = _f64(rho_tilde)
+    v, d = np.zeros(rt.size), np.zeros(rt.size)
+    _check(lib().tg_heaviside_project(rt.size, _p(rt), float(beta), float(eta), _p(v), _p(d)))
+    return v, d
+
+
+def oc_update_projected(pb: Problem, radius, density, xtilde, dcompliance, beta, eta,
+                        volume_fraction, move=0.2, density_min=1e-3):
+    """oc_update_projected (simp.cpp:1665-1726) on the solid voxels of ``pb``."""
+    d, xt, dc = _f64(density, pb.nv), _f64(xtilde, pb.nv), _f64(dcompliance, pb.nv)
+    out = np.zeros(pb.nv)
+    _check(lib().tg_oc_update_projected(C.byref(pb._grid), float(radius), _p(d), _p(xt), _p(dc),
+                                        float(beta), float(eta), volume_fraction, move,
+                                        density_min, _p(out)))
+    return out
+
+
 class _HomogInfo(C.Structure):
     _fields_ = [("iterations_max", C.c_int32), ("converged", C.c_int32), ("systems", C.c_int32),
                 ("iterations_total", C.c_int64), ("refinements", C.c_int32),
@@ -496,11 +550,11 @@ def _rows(hist, n):
 
 def simp_optimize(pb: Problem, params: SimpParams, options: SimpOptions, progress=None,
                   cancel=None, mask=None):
-    """simp.hpp:1783-1786 (OC, no projection); with ``mask`` the masked overload
-    (simp.hpp:1820-1824).  ``cancel`` may be a one-element int32 numpy array
+    """simp.hpp:1783-1786 (OC; projected when ``options.projection`` holds a
+    stage plan); with ``mask`` the masked overload (simp.hpp:1820-1824).  ``cancel`` may be a one-element int32 numpy array
     polled once per iteration."""
     prm, opt = params._c(), options._c()
-    hist = (_Iter * options.max_iterations)()
+    hist = (_Iter * options.total_iterations())()
     design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
     res = _Result()
     cb = _PROGRESS(lambda ctx, it, c, ch: progress(it, c, ch)) if progress else _PROGRESS()
@@ -624,6 +678,10 @@ class SimpJob:
         row = _Iter()
         _check(lib().tg_job_step(self._h, C.byref(row)))
         return {f[0]: getattr(row, f[0]) for f in _Iter._fields_}
+
+    def set_stage(self, stage: int):
+        """Run the next steps at stage ``stage`` of the options' projection plan."""
+        _check(lib().tg_job_set_stage(self._h, int(stage)))
 
     def read(self):
         x, xp = np.zeros(self.pb.nv), np.zeros(self.pb.nv)

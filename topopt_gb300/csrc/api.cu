@@ -246,6 +246,13 @@ struct FilterState {
 };
 
 // ------------------------------------------------------------ OC update
+// Candidate fields of one projected bisection pass: up to kOcMulti, at most
+// 128 MB of them.
+int projected_candidates(int64_t nv) {
+  const int64_t cap = (int64_t(128) << 20) / (8 * std::max<int64_t>(nv, 1));
+  return int(std::max<int64_t>(1, std::min<int64_t>(kOcMulti, cap)));
+}
+
 struct OcState {
   DBuf<double> dcf, dvf, xp, sq, lo, hi, vpart, vsum;
   int fast_evals = 0, exact_evals = 0;
@@ -258,6 +265,14 @@ struct OcState {
   int64_t n_solid = 0;
   int fallbacks = 0, evals = 0, passes = 0;
   bool carry = false;  // oc_update_masked: voxels outside the design set keep x
+  // Projected bisection: kproj candidate fields evaluated per pass.
+  DBuf<double> cand;
+  int kproj = 0;
+  void init_projected(const Grid& g) {
+    if (kproj > 0) return;
+    kproj = projected_candidates(g.nv);
+    cand.alloc(size_t(kproj) * size_t(g.nv));
+  }
   void init(const Grid& g, cudaStream_t) {
     for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi}) d->alloc(size_t(g.nv));
     vpart.alloc(size_t(kRedBlocks) * kOcMulti);
@@ -274,7 +289,8 @@ struct OcState {
   }
   size_t bytes() const {
     return dcf.bytes() + dvf.bytes() + xp.bytes() + sq.bytes() + lo.bytes() + hi.bytes() +
-           vpart.bytes() + vsum.bytes() + part.bytes() + total.bytes() + inexact.bytes();
+           vpart.bytes() + vsum.bytes() + part.bytes() + total.bytes() + inexact.bytes() +
+           cand.bytes();
   }
 };
 
@@ -427,6 +443,100 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
                       xnew, s);
 }
 
+// oc_update_projected (simp.cpp:1665-1726) on device-resident fields: the
+// projection derivative at xtilde chained before the filter transpose (dproj and
+// dc * dproj staged in sq and lo, which the projected update does not otherwise
+// use), then the reference's bracketing and bisection, every branch decided by
+// the projected volume sum_e heaviside_project(filter(x_new(lambda)))_e over the
+// design voxels.  The volumes of up to kproj multipliers come from one pass
+// (the next doublings while bracketing, the next bisection levels' midpoints
+// while bisecting); each branch is still decided one at a time, in the
+// reference's order, from the volume of exactly the multiplier it tests.  The
+// projection uses the device's tanh, so a volume can differ from the host's in
+// the last bits and a branch on a near-tie may go the other way: this form is
+// held to the reference within tolerance, not bit for bit.
+void oc_update_projected_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t* act,
+                                const double* x, const double* xtilde, const double* dc,
+                                double beta, double eta, double volfrac, double move,
+                                double rho_min, double* xnew, cudaStream_t s) {
+  oc.init_projected(g);
+  launch_proj_chain(xtilde, dc, act, g.nv, beta, eta, oc.sq.p, oc.lo.p, s);
+  fs.adj(g, act, oc.lo.p, oc.dcf.p, s);
+  fs.adj(g, act, oc.sq.p, oc.dvf.p, s);
+  const double target = volfrac * double(oc.n_solid);
+  std::vector<std::pair<double, double>> known;  // (lambda, projected volume)
+  auto lookup = [&](double lam, double* V) {
+    for (const auto& kv : known)
+      if (kv.first == lam) {
+        *V = kv.second;
+        return true;
+      }
+    return false;
+  };
+  auto batch = [&](const std::vector<double>& lams) {
+    ProjLambdas ls;
+    ls.k = int(std::min<size_t>(lams.size(), size_t(oc.kproj)));
+    for (int k = 0; k < ls.k; ++k) ls.lam[k] = lams[size_t(k)];
+    launch_oc_candidates_projected(x, oc.dcf.p, oc.dvf.p, act, g.nv, ls, move, rho_min, oc.carry,
+                                   oc.cand.p, s);
+    launch_proj_volume(g, fs.st_dev, fs.st.n, act, fs.hs.p, oc.cand.p, ls.k, beta, eta,
+                       oc.vpart.p, oc.vsum.p, s);
+    TG_CUDA(cudaMemcpyAsync(oc.h_v, oc.vsum.p, sizeof(double) * ls.k, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    ++oc.passes;
+    for (int k = 0; k < ls.k; ++k) known.emplace_back(ls.lam[k], oc.h_v[k]);
+  };
+  auto exceeds = [&](double lam) {
+    ++oc.evals;
+    double V = 0.0;
+    if (!lookup(lam, &V)) {
+      batch({lam});
+      lookup(lam, &V);
+    }
+    return V > target;
+  };
+  double l1 = 0.0, l2 = 1.0, Vtmp = 0.0;
+  while (l2 < 1e30) {
+    if (!lookup(l2, &Vtmp)) {
+      std::vector<double> c;
+      for (double t = l2; int(c.size()) < oc.kproj && t < 1e30; t *= 2.0) c.push_back(t);
+      batch(c);
+    }
+    if (!exceeds(l2)) break;
+    l2 *= 2.0;
+  }
+  for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
+    const double lmid = 0.5 * (l1 + l2);
+    if (!lookup(lmid, &Vtmp)) {
+      // Midpoints of the next bisection levels, breadth first, as many as one
+      // pass holds (the loop's own arithmetic).
+      std::vector<double> c;
+      std::vector<std::pair<double, double>> lv{{l1, l2}};
+      while (!lv.empty() && int(c.size()) < oc.kproj) {
+        std::vector<std::pair<double, double>> nx;
+        for (const auto& iv : lv) {
+          if (int(c.size()) >= oc.kproj) break;
+          const double m = 0.5 * (iv.first + iv.second);
+          c.push_back(m);
+          nx.emplace_back(iv.first, m);
+          nx.emplace_back(m, iv.second);
+        }
+        lv.swap(nx);
+      }
+      batch(c);
+    }
+    if (exceeds(lmid))
+      l1 = lmid;
+    else
+      l2 = lmid;
+  }
+  ProjLambdas last;
+  last.k = 1;
+  last.lam[0] = 0.5 * (l1 + l2);
+  launch_oc_candidates_projected(x, oc.dcf.p, oc.dvf.p, act, g.nv, last, move, rho_min, oc.carry,
+                                 xnew, s);
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -454,6 +564,12 @@ struct tg_job {
   DBuf<uint8_t> eff;            // effective design mask (masked jobs)
   std::vector<uint8_t> eff_h;
   DBuf<double> x, xnew, xphys, E, u, dc, part, scal;
+  // The projection plan (simp.cpp:1053-1068); empty for the unprojected loop.
+  std::vector<tg_projection_stage> stages;
+  double eta = 0.5;
+  int stage = 0;        // the stage the next steps run
+  DBuf<double> xtilde;  // filter(x), before the projection (projected jobs)
+  bool projecting() const { return !stages.empty(); }
   double* h_scal = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evf = nullptr;
   int64_t n_solid = 0;
@@ -471,7 +587,8 @@ struct tg_job {
   }
   size_t bytes() const {
     size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes() + eff.bytes();
-    for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal}) b += d->bytes();
+    for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal, &xtilde})
+      b += d->bytes();
     return b + (solver ? solver->device_bytes() : 0);
   }
 };
@@ -497,8 +614,26 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   if (o.change_tol < 0.0) raise(TG_EINVAL, "simp_optimize: change_tol must be >= 0");
   if (!(o.filter_radius > 0.0)) raise(TG_EINVAL, "make_density_filter: radius must be > 0");
   if (!(o.cg_tolerance > 0.0)) raise(TG_EINVAL, "simp_optimize: cg_tolerance must be > 0");
+  // validate_projection_options (simp.cpp:59-74).
+  if (o.projection_stages < 0 || (o.projection_stages > 0 && !o.projection))
+    raise(TG_EINVAL, "simp_optimize: projection must hold projection_stages stages");
+  if (o.projection_stages > 0) {
+    if (!(o.projection_eta > 0.0 && o.projection_eta < 1.0))
+      raise(TG_EINVAL, "simp_optimize: projection_eta must be in (0, 1)");
+    for (int i = 0; i < o.projection_stages; ++i) {
+      const tg_projection_stage& ps = o.projection[i];
+      if (!(ps.beta > 0.0) || !std::isfinite(ps.beta))
+        raise(TG_EINVAL, "simp_optimize: projection stage beta must be finite and > 0");
+      if (!(ps.move > 0.0)) raise(TG_EINVAL, "simp_optimize: projection stage move must be > 0");
+      if (ps.iterations < 1)
+        raise(TG_EINVAL, "simp_optimize: projection stage iterations must be >= 1");
+    }
+    j->stages.assign(o.projection, o.projection + o.projection_stages);
+    j->eta = o.projection_eta;
+  }
   j->params = *params;
   j->opt = o;
+  j->opt.projection = nullptr;  // the job keeps its own copy of the plan
   j->opt.solve = default_solve(&o.solve);
   TG_CUDA(cudaStreamCreateWithFlags(&j->owned.s, cudaStreamNonBlocking));
   j->s = j->owned.s;
@@ -531,6 +666,7 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   for (uint8_t v : j->solid_h) j->n_solid += v;
   upload(j->solid, j->solid_h.data(), j->solid_h.size(), s);
   for (DBuf<double>* d : {&j->x, &j->xnew, &j->xphys, &j->E, &j->dc}) d->alloc(size_t(g.nv));
+  if (j->projecting()) j->xtilde.alloc(size_t(g.nv));
   j->u.alloc(size_t(g.ndof));
   j->part.alloc(size_t(4 * kRedBlocks + 152 * 32));
   j->scal.alloc(8);
@@ -581,12 +717,20 @@ SolverStats job_solve(tg_job* j, double tol, int max_it) {
   return j->solver->solve(tol, max_it, nullptr, j->u.p);
 }
 
-// xPhys = filter(x), then the mask pins (simp.cpp:3200-3204).  Volume sums run
-// over the Active set only, which the pins never touch, so they see the
-// unpinned field as the reference's active_volfrac does.
+// xPhys = filter(x), projected on the design voxels at the current stage's beta
+// when projecting (simp.cpp:2197-2199, :3200-3203), then the mask pins.  Volume
+// sums run over the design set only, which the pins never touch, so they see
+// the unpinned field as the reference's active_volfrac does.
 void job_filter_x(tg_job* j) {
-  j->filt.fwd(j->fp.g, j->solid.p, j->x.p, j->xphys.p, j->s);
-  if (j->masked) launch_mask_pins(j->eff.p, j->fp.g.nv, j->xphys.p, j->s);
+  const Grid& g = j->fp.g;
+  if (j->projecting()) {
+    j->filt.fwd(g, j->solid.p, j->x.p, j->xtilde.p, j->s);
+    launch_project(j->xtilde.p, j->solid.p, g.nv, j->stages[size_t(j->stage)].beta, j->eta,
+                   j->xphys.p, nullptr, j->s);
+  } else {
+    j->filt.fwd(g, j->solid.p, j->x.p, j->xphys.p, j->s);
+  }
+  if (j->masked) launch_mask_pins(j->eff.p, g.nv, j->xphys.p, j->s);
   j->xphys_valid = true;
 }
 
@@ -613,8 +757,18 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   const double c = job_sensitivity(j);
   const double t3 = now_ms();
   const int fb0 = j->oc.evals, ps0 = j->oc.passes;
-  oc_update_device(j->oc, j->filt, g, j->solid.p, j->solid_h, j->x.p, j->dc.p, o.volume_fraction,
-                   o.move, j->params.density_min, j->xnew.p, j->s);
+  double beta = 0.0;
+  if (j->projecting()) {
+    // xtilde = filter(x) is current: job_filter_x ran for this x.
+    const tg_projection_stage& ps = j->stages[size_t(j->stage)];
+    beta = ps.beta;
+    oc_update_projected_device(j->oc, j->filt, g, j->solid.p, j->x.p, j->xtilde.p, j->dc.p,
+                               ps.beta, j->eta, o.volume_fraction, ps.move,
+                               j->params.density_min, j->xnew.p, j->s);
+  } else {
+    oc_update_device(j->oc, j->filt, g, j->solid.p, j->solid_h, j->x.p, j->dc.p,
+                     o.volume_fraction, o.move, j->params.density_min, j->xnew.p, j->s);
+  }
   launch_absdiff_max(j->xnew.p, j->x.p, g.nv, j->part.p, j->scal.p + 1, j->s);
   const double change = read1(j, j->scal.p + 1);
   std::swap(j->x.p, j->xnew.p);
@@ -645,6 +799,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   r.t_device_ms = dev_ms;
   r.fine_matvecs = st.matvecs;
   r.fine_matvecs_lowp = st.matvecs_lowp;
+  r.beta = beta;
   j->hist_c.push_back(c);
   j->hist_cg.push_back(st.iterations);
   if (row) *row = r;
@@ -985,6 +1140,74 @@ int tg_oc_update_masked(const tg_grid* grid, const uint8_t* mask, double radius,
   });
 }
 
+int tg_heaviside_project(int64_t n, const double* rho_tilde, double beta, double eta,
+                         double* value, double* derivative) {
+  return guarded([&] {
+    // validate_projection_args (simp.cpp:49-55).
+    if (!(beta > 0.0) || !std::isfinite(beta))
+      raise(TG_EINVAL, "heaviside_project: beta must be finite and > 0");
+    if (!(eta > 0.0 && eta < 1.0)) raise(TG_EINVAL, "heaviside_project: eta must be in (0, 1)");
+    if (n < 0 || (n > 0 && !rho_tilde)) raise(TG_EINVAL, "rho_tilde must hold n values");
+    if (n == 0 || (!value && !derivative)) return;
+    CallStream cs;
+    DBuf<double> drt, dv, dd;
+    upload(drt, rho_tilde, size_t(n), cs.s);
+    if (value) dv.alloc(size_t(n));
+    if (derivative) dd.alloc(size_t(n));
+    launch_project(drt.p, nullptr, n, beta, eta, dv.p, dd.p, cs.s);
+    if (value)
+      TG_CUDA(cudaMemcpyAsync(value, dv.p, dv.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    if (derivative)
+      TG_CUDA(cudaMemcpyAsync(derivative, dd.p, dd.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+}
+
+int32_t tg_heaviside_continuation_schedule(tg_projection_stage* out, int32_t cap) {
+  static const tg_projection_stage kSchedule[6] = {
+      {1.0, 0.2, 50}, {2.0, 0.2, 50}, {4.0, 0.2, 50}, {8.0, 0.2, 50}, {16.0, 0.1, 50},
+      {32.0, 0.05, 50}};
+  for (int i = 0; out && i < cap && i < 6; ++i) out[i] = kSchedule[i];
+  return 6;
+}
+
+int tg_oc_update_projected(const tg_grid* grid, double radius, const double* density,
+                           const double* xtilde, const double* dcompliance, double beta,
+                           double eta, double volume_fraction, double move, double density_min,
+                           double* x_new) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!density || !xtilde || !dcompliance || !x_new)
+      raise(TG_EINVAL, "density, xtilde, dcompliance and x_new must be non-null");
+    if (!(beta > 0.0) || !std::isfinite(beta))
+      raise(TG_EINVAL, "heaviside_project: beta must be finite and > 0");
+    if (!(eta > 0.0 && eta < 1.0)) raise(TG_EINVAL, "heaviside_project: eta must be in (0, 1)");
+    CallStream cs;
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    std::vector<uint8_t> act(size_t(g.nv));
+    int64_t n_design = 0;
+    for (int64_t e = 0; e < g.nv; ++e) {
+      act[size_t(e)] = grid->tags == nullptr || grid->tags[e] != 0;
+      n_design += act[size_t(e)];
+    }
+    DBuf<uint8_t> dact;
+    DBuf<double> dx, dxt, ddc, dxn(size_t(g.nv));
+    upload(dact, act.data(), act.size(), cs.s);
+    upload(dx, density, size_t(g.nv), cs.s);
+    upload(dxt, xtilde, size_t(g.nv), cs.s);
+    upload(ddc, dcompliance, size_t(g.nv), cs.s);
+    FilterState fs;
+    fs.init(g, radius, dact.p, cs.s);
+    OcState oc;
+    oc.init(g, cs.s);
+    oc.n_solid = n_design;
+    oc_update_projected_device(oc, fs, g, dact.p, dx.p, dxt.p, ddc.p, beta, eta, volume_fraction,
+                               move, density_min, dxn.p, cs.s);
+    TG_CUDA(cudaMemcpyAsync(x_new, dxn.p, dxn.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+}
+
 int tg_effective_design_mask(const tg_grid* grid, const uint8_t* mask, uint8_t* eff_out) {
   return guarded([&] {
     validate_grid(grid);
@@ -1030,6 +1253,18 @@ int tg_job_step(tg_job* job, tg_simp_iteration* row) {
   return rc;
 }
 
+int tg_job_set_stage(tg_job* job, int32_t stage) {
+  return guarded([&] {
+    if (!job) raise(TG_EINVAL, "job is null");
+    if (stage < 0 || stage >= std::max<int>(1, int(job->stages.size())))
+      raise(TG_EINVAL, "tg_job_set_stage: stage outside the projection plan");
+    if (job->stage != stage) {
+      job->stage = stage;
+      job->xphys_valid = false;
+    }
+  });
+}
+
 int tg_job_read(tg_job* job, double* design_out, double* phys_out) {
   return guarded([&] {
     if (!job) raise(TG_EINVAL, "job is null");
@@ -1067,6 +1302,8 @@ int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* option
   double b = ndof * (9 * 8 + 1 + 16) + nv * (12 * 8 + 2);
   b += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 126 * 8 * 8.0 / 7.0;
   if (mixed) b += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 126 * 4 * 8.0 / 7.0 + nv * 4;
+  if (options && options->projection_stages > 0)  // xtilde and the candidate fields
+    b += nv * 8.0 * (1 + projected_candidates(int64_t(nv)));
   return int64_t(b * 1.05) + (64 << 20);
 }
 
@@ -1108,33 +1345,55 @@ static int simp_optimize_impl(const tg_grid* grid, const tg_simp_params* params,
     job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, options, mask);
     tg_job* j = jp.get();
     const tg_simp_options& o = j->opt;
-    for (int it = 0; it < o.max_iterations; ++it) {
-      if (cancel && *cancel) {
-        res.cancelled = 1;
-        break;
+    // The stage plan (simp.cpp:2158-2507): one unprojected stage of
+    // max_iterations, or the projection stages in order, each ended early by
+    // change < change_tol; the run is converged iff its last stage was.
+    const int nst = j->projecting() ? int(j->stages.size()) : 1;
+    bool stop = false;
+    int nrow = 0;
+    for (int si = 0; si < nst && !stop; ++si) {
+      if (j->projecting() && j->stage != si) {
+        j->stage = si;
+        j->xphys_valid = false;  // xPhys is projected at the new stage's beta
       }
-      tg_simp_iteration row;
-      try {
-        job_step(j, &row);
-      } catch (const Error& e) {
-        if (e.code != TG_ENONCONV) throw;
-        res.non_convergent = 1;  // simp.cpp:2254-2266: ends the run, no throw
-        break;
+      const int iters = j->projecting() ? j->stages[size_t(si)].iterations : o.max_iterations;
+      bool stage_conv = false;
+      for (int it = 0; it < iters; ++it) {
+        if (cancel && *cancel) {
+          res.cancelled = 1;
+          stop = true;
+          break;
+        }
+        tg_simp_iteration row;
+        try {
+          job_step(j, &row);
+        } catch (const Error& e) {
+          if (e.code != TG_ENONCONV) throw;
+          res.non_convergent = 1;  // simp.cpp:2254-2266: ends the run, no throw
+          stop = true;
+          break;
+        }
+        if (history) history[nrow] = row;
+        if (nrow == 0) res.initial_compliance = row.compliance;
+        ++nrow;
+        res.iterations = j->iteration;
+        if (progress) progress(progress_ctx, row.iteration, row.compliance, row.change);
+        if (rung_infeasible(j->hist_c, j->hist_cg)) {
+          res.infeasible = 1;
+          stop = true;
+          break;
+        }
+        if (row.change < o.change_tol) {
+          stage_conv = true;
+          break;
+        }
       }
-      if (history) history[it] = row;
-      if (it == 0) res.initial_compliance = row.compliance;
-      res.iterations = j->iteration;
-      if (progress) progress(progress_ctx, row.iteration, row.compliance, row.change);
-      if (rung_infeasible(j->hist_c, j->hist_cg)) {
-        res.infeasible = 1;
-        break;
-      }
-      if (row.change < o.change_tol) {
-        res.converged = 1;
-        break;
-      }
+      res.converged = stage_conv ? 1 : 0;
     }
     const Grid& g = j->fp.g;
+    // physical_density = filter(design), projected at the LAST stage's beta
+    // (simp.cpp:2514-2517), whatever stage the loop stopped in.
+    if (j->projecting()) j->stage = nst - 1;
     job_filter_x(j);
     if (res.infeasible || res.non_convergent || res.cancelled) {
       res.compliance = j->hist_c.empty() ? 0.0 : j->hist_c.back();

@@ -389,6 +389,132 @@ __global__ void k_sum_partials_multi(const double* __restrict__ part, int n,
   if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
 
+// ------------------------------------------------------------ projection
+// heaviside_project / heaviside_project_derivative (simp.cpp:352-365).  The
+// constants tanh(beta eta) and tanh(beta eta) + tanh(beta (1 - eta)) come from
+// the host's tanh (the reference's own values); only tanh / cosh of
+// beta (rt - eta) are the device's.  No product here feeds an add, so nothing
+// fuses: each operation rounds as the reference's does.
+struct ProjConsts {
+  double beta, eta, t_eta, denom;
+};
+__device__ __forceinline__ double proj_value(const ProjConsts& c, double rt) {
+  return (c.t_eta + tanh(c.beta * (rt - c.eta))) / c.denom;
+}
+__device__ __forceinline__ double proj_deriv(const ProjConsts& c, double rt) {
+  const double ch = cosh(c.beta * (rt - c.eta));
+  return c.beta / (ch * ch * c.denom);
+}
+
+// project_solid / project_active (simp.cpp:1638-1648, :2789): out = projected
+// xt on the design voxels, xt elsewhere; deriv (optional) = the derivative on
+// the design voxels, 0 elsewhere.
+__global__ void k_project(const double* __restrict__ xt, const uint8_t* __restrict__ act,
+                          int64_t n, ProjConsts c, double* __restrict__ out,
+                          double* __restrict__ deriv) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    const double v = xt[e];
+    const bool a = act == nullptr || act[e];
+    if (out) out[e] = a ? proj_value(c, v) : v;
+    if (deriv) deriv[e] = a ? proj_deriv(c, v) : 0.0;
+  }
+}
+
+// oc_update_projected's chain (simp.cpp:1670-1680): dproj = derivative(xtilde)
+// and dcp = dc * dproj on the design voxels, 0 elsewhere.
+__global__ void k_proj_chain(const double* __restrict__ xtilde, const double* __restrict__ dc,
+                             const uint8_t* __restrict__ act, int64_t n, ProjConsts c,
+                             double* __restrict__ dproj, double* __restrict__ dcp) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    double d = 0.0, g = 0.0;
+    if (act[e]) {
+      d = proj_deriv(c, xtilde[e]);
+      g = __dmul_rn(dc[e], d);
+    }
+    dproj[e] = d;
+    dcp[e] = g;
+  }
+}
+
+// The projected OC candidate (simp.cpp:1684-1702) for cs.k multipliers at once:
+// B = -dc / (lambda dv) with UNCLAMPED dv, a non-finite B holds the voxel
+// (B = 1), B < 0 -> 0; x sqrt(B) clamped to the move window.  Candidate j goes
+// to cand + j * n.
+__global__ void k_oc_candidates_projected(const double* __restrict__ x,
+                                          const double* __restrict__ dcf,
+                                          const double* __restrict__ dvf,
+                                          const uint8_t* __restrict__ act, int64_t n,
+                                          ProjLambdas ls, double move, double rho_min, int carry,
+                                          double* __restrict__ cand) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    const double xe = x[e];
+    if (!act[e]) {
+      const double v = carry ? xe : 0.0;
+      for (int j = 0; j < ls.k; ++j) cand[j * n + e] = v;
+      continue;
+    }
+    const double mdc = -dcf[e], dv = dvf[e];
+    const double xm = __dsub_rn(xe, move), xp = __dadd_rn(xe, move);
+    const double lo = (rho_min < xm) ? xm : rho_min;
+    const double hi = (xp < 1.0) ? xp : 1.0;
+    for (int j = 0; j < ls.k; ++j) {
+      double be = __ddiv_rn(mdc, __dmul_rn(ls.lam[j], dv));
+      if (!isfinite(be)) be = 1.0;
+      if (be < 0.0) be = 0.0;
+      double xt = __dmul_rn(xe, __dsqrt_rn(be));
+      if (xt < lo) xt = lo;
+      if (xt > hi) xt = hi;
+      cand[j * n + e] = xt;
+    }
+  }
+}
+
+// proj_vol (simp.cpp:1707-1716) of k candidates in one pass: for every design
+// voxel, the density filter of each candidate (the k_filter_fwd arithmetic,
+// neighbour bookkeeping shared by the k fields), projected, summed per block.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_proj_volume(GridDev g, const StencilEntry* __restrict__ st,
+                                                          int ns, const uint8_t* __restrict__ act,
+                                                          const double* __restrict__ hs,
+                                                          const double* __restrict__ cand, int k,
+                                                          ProjConsts c, double* __restrict__ part) {
+  const int64_t n = int64_t(g.nx) * g.ny * g.nz;
+  double vol[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) vol[j] = 0.0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    if (!act[e]) continue;
+    const double h = hs[e];
+    const int i = int(e % g.nx), jy = int((e / g.nx) % g.ny), kz = int(e / (int64_t(g.nx) * g.ny));
+    double acc[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) acc[j] = 0.0;
+    for (int q = 0; q < ns; ++q) {
+      const int ii = i + st[q].di, jj = jy + st[q].dj, kk = kz + st[q].dk;
+      if (!in_grid(g, ii, jj, kk)) continue;
+      const int64_t nb = (int64_t(kk) * g.ny + jj) * g.nx + ii;
+      if (!act[nb]) continue;
+      const double w = st[q].w;
+#pragma unroll
+      for (int j = 0; j < K; ++j)
+        if (j < k) acc[j] = __dadd_rn(acc[j], __dmul_rn(w, cand[j * n + nb]));
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (j < k) vol[j] += proj_value(c, __ddiv_rn(acc[j], h));
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    if (j >= k) break;  // k is uniform over the block
+    const double v = block_sum256(vol[j]);
+    if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = v;
+  }
+}
+
 // Exact fixed-point accumulation: value = A * 2^-128, A a 192-bit unsigned
 // integer in three 64-bit limbs.  Integer addition is associative, so the total
 // is the same whatever the summation order -- the exact sum, not an
@@ -580,6 +706,53 @@ void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, co
                        int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
                        cudaStream_t s) {
   k_oc_prepare<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, move, rho_min, sq, lo, hi);
+  TG_LAUNCH_CHECK();
+}
+
+namespace {
+ProjConsts proj_consts(double beta, double eta) {
+  // The reference's own constants, from the host's tanh.
+  const double t = std::tanh(beta * eta);
+  return ProjConsts{beta, eta, t, t + std::tanh(beta * (1.0 - eta))};
+}
+}  // namespace
+
+void launch_project(const double* xt, const uint8_t* act, int64_t n, double beta, double eta,
+                    double* out, double* deriv, cudaStream_t s) {
+  k_project<<<grid_blocks(n), kThreads, 0, s>>>(xt, act, n, proj_consts(beta, eta), out, deriv);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_proj_chain(const double* xtilde, const double* dc, const uint8_t* act, int64_t n,
+                       double beta, double eta, double* dproj, double* dcp, cudaStream_t s) {
+  k_proj_chain<<<grid_blocks(n), kThreads, 0, s>>>(xtilde, dc, act, n, proj_consts(beta, eta),
+                                                   dproj, dcp);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_oc_candidates_projected(const double* x, const double* dcf, const double* dvf,
+                                    const uint8_t* act, int64_t n, const ProjLambdas& ls,
+                                    double move, double rho_min, bool carry, double* cand,
+                                    cudaStream_t s) {
+  k_oc_candidates_projected<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, ls, move,
+                                                                rho_min, carry ? 1 : 0, cand);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_proj_volume(const Grid& g, const void* st, int ns, const uint8_t* act,
+                        const double* hs, const double* cand, int k, double beta, double eta,
+                        double* part, double* out, cudaStream_t s) {
+  const auto* se = static_cast<const StencilEntry*>(st);
+  const ProjConsts c = proj_consts(beta, eta);
+  if (k <= 1)
+    k_proj_volume<1><<<kRedBlocks, kThreads, 0, s>>>(dev(g), se, ns, act, hs, cand, k, c, part);
+  else if (k <= 4)
+    k_proj_volume<4><<<kRedBlocks, kThreads, 0, s>>>(dev(g), se, ns, act, hs, cand, k, c, part);
+  else
+    k_proj_volume<kOcMulti><<<kRedBlocks, kThreads, 0, s>>>(dev(g), se, ns, act, hs, cand, k, c,
+                                                            part);
+  TG_LAUNCH_CHECK();
+  k_sum_partials_multi<<<k, kThreads, 0, s>>>(part, kRedBlocks, out);
   TG_LAUNCH_CHECK();
 }
 

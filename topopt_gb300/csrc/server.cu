@@ -44,6 +44,7 @@ struct Request {
   std::vector<tg_dirichlet_bc> bcs;
   std::vector<tg_nodal_load> loads;
   tg_simp_options options{};
+  std::vector<tg_projection_stage> stages;  // options.projection, copied
   int64_t estimate = 0;
   std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
   // Outcome.
@@ -117,6 +118,7 @@ struct tg_server {
     r.phys.assign(size_t(nv), 0.0);
     tg_grid g = r.grid;
     g.tags = r.has_tags ? r.tags.data() : nullptr;
+    r.options.projection = r.stages.empty() ? nullptr : r.stages.data();
     const int rc =
         r.has_mask
             ? tg_simp_optimize_masked(&g, &r.params, r.bcs.data(), int32_t(r.bcs.size()),
@@ -177,6 +179,9 @@ int tg_server_submit(tg_server* s, const tg_grid* grid, const tg_simp_params* pa
   r->bcs.assign(bcs, bcs + nbc);
   r->loads.assign(loads, loads + nloads);
   r->options = *options;
+  if (options->projection && options->projection_stages > 0)
+    r->stages.assign(options->projection, options->projection + options->projection_stages);
+  r->options.projection = nullptr;
   r->estimate = tg_job_estimate_bytes(grid, options);
   r->t_submit = std::chrono::steady_clock::now();
   std::lock_guard<std::mutex> lk(s->mu);

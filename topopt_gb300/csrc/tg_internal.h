@@ -237,6 +237,28 @@ void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi
 void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
                          const uint8_t* act, int64_t n, double lambda, double move,
                          double rho_min, bool carry, double* xnew, cudaStream_t s);
+// Heaviside projection (simp.cpp:352-365): out = projected xt on the design
+// voxels (act; every voxel when act is null), xt elsewhere; deriv (optional)
+// the derivative there, 0 elsewhere.  Either output may be null.
+void launch_project(const double* xt, const uint8_t* act, int64_t n, double beta, double eta,
+                    double* out, double* deriv, cudaStream_t s);
+// dproj = derivative(xtilde), dcp = dc * dproj on the design voxels, 0 elsewhere.
+void launch_proj_chain(const double* xtilde, const double* dc, const uint8_t* act, int64_t n,
+                       double beta, double eta, double* dproj, double* dcp, cudaStream_t s);
+// Projected OC candidates for ls.k multipliers; candidate j at cand + j * n.
+struct ProjLambdas {
+  int k;
+  double lam[kOcMulti];
+};
+void launch_oc_candidates_projected(const double* x, const double* dcf, const double* dvf,
+                                    const uint8_t* act, int64_t n, const ProjLambdas& ls,
+                                    double move, double rho_min, bool carry, double* cand,
+                                    cudaStream_t s);
+// out[j] = sum over design voxels of heaviside_project(filter(cand_j)), j < k;
+// part holds k * kRedBlocks partials.
+void launch_proj_volume(const Grid& g, const void* st, int ns, const uint8_t* act,
+                        const double* hs, const double* cand, int k, double beta, double eta,
+                        double* part, double* out, cudaStream_t s);
 // FrozenSolid (1) -> 1, FrozenVoid (2) -> 0 on the physical density.
 void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t s);
 // Exact (fixed-point, order independent) sum of a non-negative field over the
