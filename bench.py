@@ -34,6 +34,9 @@ Secondary workloads (--workload; one JSON line each, not the headline):
             minutes) of jobs log-uniform between 24^3 and 192x96x96 elements, 40
             design iterations each, 150 GB HBM budget; p50/p99 latency, jobs/s and
             GPU occupancy, beside the plain FP64 one-at-a-time service time.
+  gatev2 -- the two Gate V2 problems (cantilever 24x8x8, clamped beam 48x8x8)
+            under the locked projected formulation, 300 iterations each, in
+            both forms with their gate metrics; the oracle's time beside them.
 """
 from __future__ import annotations
 
@@ -523,6 +526,61 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gatev2(args):
+    """The Gate V2 benchmark problems end to end (300 projected OC iterations,
+    beta 1 -> 32) in both forms, their gates, and the oracle's time for the same
+    run on one host core."""
+    import topopt_gb300 as tg
+    from oracle.oracle import CONTINUATION, GATE_V2, OracleLib, gate_v2_metrics, gate_v2_problem
+    from topopt_gb300.build import build
+    build()
+    out = {}
+    for name in GATE_V2:
+        o = gate_v2_problem(name)
+        pb = tg.Problem(o.nx, o.ny, o.nz, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                        list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+        row = {}
+        for form, prec in (("mixed", tg.PREC_MIXED), ("fp64", tg.PREC_FP64)):
+            opt = tg.SimpOptions(volume_fraction=0.3, filter_radius=2.5, change_tol=0.0,
+                                 cg_tolerance=1e-9, projection=list(CONTINUATION),
+                                 solve=tg.SolveOptions(precision=prec))
+            tg.simp_optimize(pb, tg.SimpParams(), tg.SimpOptions(
+                volume_fraction=0.3, filter_radius=2.5, change_tol=0.0, cg_tolerance=1e-9,
+                projection=[(1.0, 0.2, 3)], solve=tg.SolveOptions(precision=prec)))  # warm-up
+            t0 = time.perf_counter()
+            s = tg.simp_optimize(pb, tg.SimpParams(), opt)
+            wall = time.perf_counter() - t0
+            hc = [h["compliance"] for h in s["history"]]
+            ncomp, mnd, ysym = gate_v2_metrics(o.nx, o.ny, o.nz, s["physical_density"])
+            row[form] = {"wall_s": wall, "iters_per_s": s["iterations"] / wall,
+                         "stage_end_compliance": [hc[50 * k + 49] for k in range(6)],
+                         "final_compliance": s["compliance"],
+                         "volume_fraction": s["volume_fraction"], "components": ncomp,
+                         "mnd": mnd, "y_symmetry": ysym,
+                         "oc_volume_passes": int(sum(h["oc_volume_passes"]
+                                                     for h in s["history"])),
+                         "cg_iterations": int(sum(h["cg_iterations"] for h in s["history"]))}
+        if not args.no_cpu:
+            t0 = time.perf_counter()
+            r = OracleLib("port").simp_optimize(o, volfrac=0.3, radius=2.5, change_tol=0.0,
+                                                cg_tol=1e-9, stages=CONTINUATION)
+            row["cpu_port"] = {"wall_s": time.perf_counter() - t0, "cores": 1,
+                               "final_compliance": r["compliance"]}
+        out[name] = row
+    tot = sum(r["mixed"]["wall_s"] for r in out.values())
+    line = {"metric": "gate_v2_runs_per_s", "value": len(out) / tot, "unit": "runs/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f32+f64", "impl": "ours",
+            "data": "the Gate V2 benchmark problems (cantilever 24x8x8, clamped beam 48x8x8)",
+            "config": {"workload": "projected SIMP, 6 stages x 50 OC iterations, rmin 2.5, "
+                                   "cg_tol 1e-9", "form": "mixed (fp64 beside it)"},
+            "runs": out}
+    if not args.no_cpu:
+        cpu = sum(r["cpu_port"]["wall_s"] for r in out.values())
+        line["cpu_baseline"] = {"value": len(out) / cpu, "unit": "runs/s", "cores": 1,
+                                "kind": "port", "sample": "both problems, full 300 iterations"}
+    print(json.dumps(line), flush=True)
+
+
 def _phys_of(tg, pb, design):
     return tg.make_density_filter(pb, 1.5).filter_density(design)
 
@@ -549,7 +607,7 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="profiling aid: drive the mixed inner PCG loop from the host (same "
                          "kernels, same results) instead of one CUDA graph")
-    ap.add_argument("--workload", choices=["cantilever", "batch", "homog", "serve"],
+    ap.add_argument("--workload", choices=["cantilever", "batch", "homog", "serve", "gatev2"],
                     default="cantilever")
     ap.add_argument("--cells", type=int, default=512)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -563,7 +621,8 @@ def main():
                               "secondary workloads are GPU-only; the CPU baseline is reported on "
                               "the cantilever workload"}), flush=True)
             return
-        {"batch": run_batch, "homog": run_homog, "serve": run_serve}[args.workload](args)
+        {"batch": run_batch, "homog": run_homog, "serve": run_serve,
+         "gatev2": run_gatev2}[args.workload](args)
         return
     if args.op_only:
         run_op_only(args)
