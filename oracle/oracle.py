@@ -317,6 +317,130 @@ class OracleLib:
                                                g, volfrac, move, rho_min, xn))
         return xn
 
+    # ---------------------------------------------------- stress and ladder
+    def _sig(self, name, args, res=C.c_int):
+        f = getattr(self.lib, self._p + name)
+        f.argtypes = args
+        f.restype = res
+        return f
+
+    def hex8_stress(self, E, nu, h, ue, xi=0.0, eta=0.0, zeta=0.0):
+        """hex8_stress (hex_element.cpp:242-316): (sigma[6], von_mises)."""
+        ue = np.ascontiguousarray(ue, dtype=np.float64)
+        sig, vm = np.zeros(6), C.c_double(0)
+        f = self._sig("hex8_stress", [C.c_double] * 3 + [_dp] + [C.c_double] * 3 +
+                      [_dp, C.POINTER(C.c_double)])
+        self._check(f(E, nu, h, ue, xi, eta, zeta, sig, C.byref(vm)))
+        return sig, vm.value
+
+    def stress_margin(self, yield_strength, z_knockdown, max_vm, max_il):
+        """compute_stress_margin: (in_plane, interlayer, worst_case)."""
+        out = np.zeros(3)
+        f = self._sig("stress_margin", [C.c_double] * 4 + [_dp])
+        self._check(f(yield_strength, z_knockdown, max_vm, max_il, out))
+        return tuple(out)
+
+    def load_path_connected(self, pb: Problem, density, iso=0.5):
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        if self.kind == "port":
+            f = self._sig("load_path_connected", [C.c_int] * 3 + [C.c_void_p, _dp, C.c_double])
+            return bool(f(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), d, iso))
+        out = C.c_int(0)
+        f = self._sig("load_path_connected", [C.c_int] * 3 + [C.c_void_p, _dp, C.c_double,
+                                                              C.POINTER(C.c_int)])
+        self._check(f(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), d, iso, C.byref(out)))
+        return bool(out.value)
+
+    def analyze_fixed_design(self, pb: Problem, density, E0=1.0, nu=0.3, penal=3.0,
+                             rho_min=1e-3, yield_strength=50.0, z_knockdown=1.0,
+                             build_dir=(0.0, 0.0, 1.0), iso=0.5, infill_knockdown=1.0,
+                             margin_stop=1.5, cg_tol=1e-8, cg_max_it=0):
+        """The solid-posture analyze_fixed_design: dict + von Mises field."""
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        vm = np.zeros(pb.nv)
+        if self.kind == "port":
+            st = _OrStrength(yield_strength, z_knockdown, (C.c_double * 3)(*build_dir), iso,
+                             infill_knockdown, margin_stop)
+            out = _OrAnalysis()
+            f = self._sig("analyze_fixed_design",
+                          [C.c_int] * 3 + [C.c_double, C.c_void_p] + [C.c_double] * 4 +
+                          [_dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_void_p,
+                           C.c_double, C.c_int, C.c_void_p, _dp])
+            self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                          d, *pb.bc_args(), C.byref(st), cg_tol, cg_max_it, C.byref(out), vm))
+            return _analysis_dict(out), vm
+        od, oi = np.zeros(7), np.zeros(4, np.int32)
+        bd = np.ascontiguousarray(build_dir, dtype=np.float64)
+        f = self._sig("analyze_fixed_design",
+                      [C.c_int] * 3 + [C.c_double, C.c_void_p] + [C.c_double] * 4 +
+                      [_dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_double,
+                       C.c_double, _dp] + [C.c_double] * 4 + [C.c_int, _dp, _ip, _dp])
+        self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min, d,
+                      *pb.bc_args(), yield_strength, z_knockdown, bd, iso, infill_knockdown,
+                      margin_stop, cg_tol, cg_max_it, od, oi, vm))
+        return dict(non_convergent=int(oi[0]), printed_voxels=int(oi[1]),
+                    load_path_ok=int(oi[2]), accepted=int(oi[3]), compliance=od[0],
+                    max_von_mises=od[1], max_interlayer=od[2], margin_in_plane=od[3],
+                    margin_interlayer=od[4], margin_worst=od[5], margin_effective=od[6]), vm
+
+    def ladder(self, pb: Problem, mask, ladder, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3,
+               radius=1.5, move=0.2, max_it=30, change_tol=0.01, cg_tol=1e-8, cg_max_it=0,
+               inherit=True, yield_strength=50.0, z_knockdown=1.0, build_dir=(0.0, 0.0, 1.0),
+               iso=0.5, infill_knockdown=1.0, margin_stop=1.5):
+        """The ladder walk (minimize_plastic.cpp:1402-2742, OC): per-rung records,
+        the recommended rung, and its design and physical density."""
+        lad = np.ascontiguousarray(ladder, dtype=np.float64)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+        n = lad.size
+        if self.kind == "port":
+            opt = _OrSimpOptions(0.5, radius, move, change_tol, cg_tol, max_it, cg_max_it, 0,
+                                 None, None, None, 0.5, None)
+            st = _OrStrength(yield_strength, z_knockdown, (C.c_double * 3)(*build_dir), iso,
+                             infill_knockdown, margin_stop)
+            rungs = (_OrRung * n)()
+            ev, rec, stop = C.c_int(0), C.c_int(-1), C.c_int(0)
+            f = self._sig("ladder", [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p] +
+                          [C.c_double] * 4 + [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                              C.c_void_p, _dp, C.c_int, C.c_int, C.c_void_p,
+                                              C.c_void_p, C.POINTER(C.c_int),
+                                              C.POINTER(C.c_int), C.POINTER(C.c_int), _dp, _dp])
+            self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(m), E0, nu,
+                          penal, rho_min, *pb.bc_args(), C.byref(opt), lad, n, int(inherit),
+                          C.byref(st), C.cast(rungs, C.c_void_p), C.byref(ev), C.byref(rec),
+                          C.byref(stop), design, phys))
+            out = []
+            for r in range(ev.value):
+                g = rungs[r]
+                out.append(dict(volume_fraction=g.volume_fraction, iterations=g.iterations,
+                                trajectory_ok=g.trajectory_ok, analysed=g.analysed,
+                                accepted=g.accepted, compliance=g.compliance,
+                                analysis=_analysis_dict(g.analysis)))
+            return dict(rungs=out, evaluated=ev.value, recommended=rec.value,
+                        stopped_on_margin=bool(stop.value), design=design, phys=phys)
+        rd, ri, oi = np.zeros(8 * n), np.zeros(6 * n, np.int32), np.zeros(3, np.int32)
+        bd = np.ascontiguousarray(build_dir, dtype=np.float64)
+        f = self._sig("ladder", [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p] +
+                      [C.c_double] * 4 + [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                          C.c_double, C.c_double, C.c_int, C.c_double,
+                                          C.c_double, C.c_int, _dp, C.c_int, C.c_int,
+                                          C.c_double, C.c_double, _dp, C.c_double, C.c_double,
+                                          C.c_double, _dp, _ip, _ip, _dp, _dp])
+        self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(m), E0, nu, penal,
+                      rho_min, *pb.bc_args(), radius, move, max_it, change_tol, cg_tol, cg_max_it,
+                      lad, n, int(inherit), yield_strength, z_knockdown, bd, iso,
+                      infill_knockdown, margin_stop, rd, ri, oi, design, phys))
+        out = []
+        for r in range(int(oi[0])):
+            d, i = rd[8 * r:8 * r + 8], ri[6 * r:6 * r + 6]
+            out.append(dict(volume_fraction=d[0], iterations=int(i[0]), trajectory_ok=int(i[1]),
+                            analysed=int(i[2]), accepted=int(i[3]), compliance=d[1],
+                            analysis=dict(max_von_mises=d[2], max_interlayer=d[3],
+                                          margin_worst=d[4], margin_effective=d[5],
+                                          load_path_ok=int(i[4]), non_convergent=int(i[5]))))
+        return dict(rungs=out, evaluated=int(oi[0]), recommended=int(oi[1]),
+                    stopped_on_margin=bool(oi[2]), design=design, phys=phys)
+
     def oc_update_projected(self, pb: Problem, density, xtilde, dc, beta, volfrac, radius=1.5,
                             move=0.2, rho_min=1e-3, eta=0.5):
         """oc_update_projected (simp.cpp:1665-1726), port only."""
@@ -491,7 +615,33 @@ class _OrSimpOptions(C.Structure):
                 ("move", C.c_double), ("change_tol", C.c_double), ("cg_tolerance", C.c_double),
                 ("max_iterations", C.c_int), ("cg_max_iterations", C.c_int),
                 ("nstages", C.c_int), ("stage_beta", C.c_void_p), ("stage_move", C.c_void_p),
-                ("stage_iterations", C.c_void_p), ("eta", C.c_double)]
+                ("stage_iterations", C.c_void_p), ("eta", C.c_double),
+                ("initial_design", C.c_void_p)]
+
+
+class _OrAnalysis(C.Structure):
+    _fields_ = [("non_convergent", C.c_int), ("cg_iterations", C.c_int),
+                ("load_path_ok", C.c_int), ("accepted", C.c_int),
+                ("printed_voxels", C.c_longlong), ("compliance", C.c_double),
+                ("max_von_mises", C.c_double), ("max_interlayer", C.c_double),
+                ("margin_in_plane", C.c_double), ("margin_interlayer", C.c_double),
+                ("margin_worst", C.c_double), ("margin_effective", C.c_double)]
+
+
+class _OrStrength(C.Structure):
+    _fields_ = [("yield_strength", C.c_double), ("z_knockdown", C.c_double),
+                ("build_dir", C.c_double * 3), ("iso", C.c_double),
+                ("infill_knockdown", C.c_double), ("margin_stop", C.c_double)]
+
+
+class _OrRung(C.Structure):
+    _fields_ = [("volume_fraction", C.c_double), ("iterations", C.c_int),
+                ("trajectory_ok", C.c_int), ("analysed", C.c_int), ("accepted", C.c_int),
+                ("compliance", C.c_double), ("analysis", _OrAnalysis)]
+
+
+def _analysis_dict(a):
+    return {f[0]: getattr(a, f[0]) for f in _OrAnalysis._fields_}
 
 
 # heaviside_continuation_schedule (simp.cpp:367-373): (beta, move, iterations).

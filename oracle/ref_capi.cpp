@@ -13,9 +13,14 @@
 #include <string>
 #include <vector>
 
+#include <array>
+
 #include "fea/fea_matfree.hpp"
 #include "topopt/fea.hpp"
+#include "topopt/orient.hpp"
+#include "topopt/report.hpp"
 #include "topopt/simp.hpp"
+#include "topopt/voxel.hpp"
 
 using namespace topopt;
 
@@ -395,6 +400,203 @@ int ref_simp_optimize_projected(int nx, int ny, int nz, double h, const uint8_t*
     out_ints[1] = r.converged ? 1 : 0;
     out_ints[2] = r.non_convergent ? 1 : 0;
     out_ints[3] = r.infeasible ? 1 : 0;
+  });
+}
+
+
+// hex8_stress (hex_element.cpp:242-316).
+int ref_hex8_stress(double E, double nu, double h, const double* ue, double xi, double eta,
+                    double zeta, double* sigma6, double* von_mises) {
+  return guarded([&] {
+    std::array<double, 24> u{};
+    for (int q = 0; q < 24; ++q) u[static_cast<std::size_t>(q)] = ue[q];
+    const Hex8Stress st = hex8_stress(E, nu, h, u, xi, eta, zeta);
+    for (int r = 0; r < 6; ++r) sigma6[r] = st.sigma[static_cast<std::size_t>(r)];
+    *von_mises = st.von_mises;
+  });
+}
+
+// compute_stress_margin (settings/report.cpp:464-491).
+int ref_stress_margin(double yield, double zk, double vm, double il, double* out3) {
+  return guarded([&] {
+    const StressMargin m = compute_stress_margin(yield, zk, vm, il);
+    out3[0] = m.in_plane;
+    out3[1] = m.interlayer;
+    out3[2] = m.worst_case;
+  });
+}
+
+// load_path_connected (voxelize.cpp:609-726).
+int ref_load_path_connected(int nx, int ny, int nz, const uint8_t* tags, const double* density,
+                            double iso, int* out) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, 1.0, tags);
+    *out = load_path_connected(g, std::vector<double>(density, density + g.voxel_count()), iso)
+               ? 1
+               : 0;
+  });
+}
+
+// The solid-posture core of analyze_fixed_design (analyze.cpp:145-440) from the
+// reference's own pieces: simp_compliance at cg_tol with the matrix-free
+// multigrid, hex8_stress at every printed voxel's centre with the solid modulus,
+// max_interlayer_tension, compute_stress_margin, load_path_connected.
+// out_d = {compliance, max_vm, max_il, in_plane, interlayer, worst, effective};
+// out_i = {non_convergent, printed_voxels, load_path_ok, accepted}.
+namespace {
+void ref_analysis(const VoxelGrid& g, const SimpParams& p, const std::vector<double>& rho,
+                  const std::vector<DirichletBC>& bcs, const std::vector<NodalLoad>& loads,
+                  double yield, double zk, const double* bdir, double iso, double knock,
+                  double margin_stop, double cg_tol, int cg_max_it, double* out_d, int* out_i,
+                  double* vm_field) {
+  for (int q = 0; q < 7; ++q) out_d[q] = 0.0;
+  for (int q = 0; q < 4; ++q) out_i[q] = 0;
+  SimpCompliance sc;
+  try {
+    sc = simp_compliance(g, p, rho, bcs, loads, cg_tol, cg_max_it, nullptr, nullptr,
+                         SolverKind::MultigridCG_Matfree);
+  } catch (const SolverNonConvergence&) {
+    out_i[0] = 1;
+    return;
+  }
+  out_d[0] = sc.compliance;
+  std::vector<std::array<double, 6>> stress(g.voxel_count(), std::array<double, 6>{});
+  double max_vm = 0.0;
+  int printed = 0;
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) {
+        if (!g.solid(i, j, k)) continue;
+        const std::size_t idx = g.index(i, j, k);
+        if (!(rho[idx] > iso)) continue;
+        ++printed;
+        const std::array<int, 8> en = fea_element_nodes(g, i, j, k);
+        std::array<double, 24> ue{};
+        for (int a = 0; a < 8; ++a)
+          for (int c = 0; c < 3; ++c)
+            ue[static_cast<std::size_t>(3 * a + c)] = sc.solution.at(en[static_cast<std::size_t>(a)], c);
+        const Hex8Stress st = hex8_stress(p.youngs_modulus, p.poisson, g.spacing, ue);
+        stress[idx] = st.sigma;
+        if (vm_field) vm_field[idx] = st.von_mises;
+        if (st.von_mises > max_vm) max_vm = st.von_mises;
+      }
+  const double max_il = max_interlayer_tension(g, stress, Vec3{bdir[0], bdir[1], bdir[2]});
+  const StressMargin m = compute_stress_margin(yield, zk, max_vm, max_il);
+  out_d[1] = max_vm;
+  out_d[2] = max_il;
+  out_d[3] = m.in_plane;
+  out_d[4] = m.interlayer;
+  out_d[5] = m.worst_case;
+  out_d[6] = m.worst_case * knock;
+  out_i[1] = printed;
+  out_i[2] = load_path_connected(g, rho, iso) ? 1 : 0;
+  out_i[3] = (out_i[2] && out_d[6] >= margin_stop) ? 1 : 0;
+}
+}  // namespace
+
+int ref_analyze_fixed_design(int nx, int ny, int nz, double h, const uint8_t* tags, double E0,
+                             double nu, double penal, double rho_min, const double* density,
+                             int nbc, const int* bc_node, const int* bc_comp,
+                             const double* bc_val, int nload, const int* ld_node,
+                             const int* ld_comp, const double* ld_val, double yield, double zk,
+                             const double* bdir, double iso, double knock, double margin_stop,
+                             double cg_tol, int cg_max_it, double* out_d, int* out_i,
+                             double* vm_field) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, h, tags);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    ref_analysis(g, p, std::vector<double>(density, density + g.voxel_count()),
+                 make_bcs(nbc, bc_node, bc_comp, bc_val), make_loads(nload, ld_node, ld_comp, ld_val),
+                 yield, zk, bdir, iso, knock, margin_stop, cg_tol, cg_max_it, out_d, out_i,
+                 vm_field);
+  });
+}
+
+// The ladder walk of minimize_plastic (minimize_plastic.cpp:1402-2742) for the
+// OC updater, driven through the reference's own simp_optimize (masked
+// overload, SimpOptions::initial_design as the warm seed) and the analysis
+// above.  Per rung r: rung_d[8r..] = {vf, compliance, max_vm, max_il, worst,
+// effective, 0, 0}, rung_i[6r..] = {iterations, trajectory_ok, analysed,
+// accepted, load_path_ok, non_convergent_analysis}.  out_i = {evaluated,
+// recommended, stopped_on_margin}.
+int ref_ladder(int nx, int ny, int nz, double h, const uint8_t* tags, const uint8_t* mask,
+               double E0, double nu, double penal, double rho_min, int nbc, const int* bc_node,
+               const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+               const int* ld_comp, const double* ld_val, double radius, double move, int max_it,
+               double change_tol, double cg_tol, int cg_max_it, const double* ladder, int nrungs,
+               int inherit, double yield, double zk, const double* bdir, double iso,
+               double knock, double margin_stop, double* rung_d, int* rung_i, int* out_i,
+               double* design, double* phys) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, h, tags);
+    const std::size_t nv = g.voxel_count();
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    const auto bcs = make_bcs(nbc, bc_node, bc_comp, bc_val);
+    const auto loads = make_loads(nload, ld_node, ld_comp, ld_val);
+    std::vector<uint8_t> zeros;
+    if (!mask) {
+      zeros.assign(nv, 0);
+      mask = zeros.data();
+    }
+    const DesignMask dm = make_mask(nv, mask);
+    std::vector<double> seed;
+    out_i[0] = 0;
+    out_i[1] = -1;
+    out_i[2] = 0;
+    for (int r = 0; r < nrungs; ++r) {
+      SimpOptions o;
+      o.volume_fraction = ladder[r];
+      o.filter_radius = radius;
+      o.move = move;
+      o.max_iterations = max_it;
+      o.change_tol = change_tol;
+      o.cg_tolerance = cg_tol;
+      o.cg_max_iterations = cg_max_it;
+      o.solver = SolverKind::MultigridCG_Matfree;
+      o.initial_design = seed;
+      const SimpOptimizeResult res = simp_optimize(g, p, bcs, loads, o, dm);
+      double* d = rung_d + 8 * r;
+      int* ii = rung_i + 6 * r;
+      for (int q = 0; q < 8; ++q) d[q] = 0.0;
+      for (int q = 0; q < 6; ++q) ii[q] = 0;
+      d[0] = ladder[r];
+      d[1] = res.compliance;
+      ii[0] = res.iterations;
+      out_i[0] = r + 1;
+      if (res.infeasible || res.non_convergent) continue;
+      ii[1] = 1;
+      const std::vector<double>& rho = res.physical_density;
+      if (load_path_connected(g, rho, iso)) seed = inherit ? rho : std::vector<double>();
+      double ad[7];
+      int ai[4];
+      ref_analysis(g, p, rho, bcs, loads, yield, zk, bdir, iso, knock, margin_stop, cg_tol,
+                   cg_max_it, ad, ai, nullptr);
+      d[2] = ad[1];
+      d[3] = ad[2];
+      d[4] = ad[5];
+      d[5] = ad[6];
+      ii[4] = ai[2];
+      ii[5] = ai[0];
+      if (ai[0]) continue;
+      ii[2] = 1;
+      ii[3] = ai[3];
+      if (ai[3]) {
+        out_i[1] = r;
+        if (design) std::memcpy(design, res.design.data(), nv * sizeof(double));
+        if (phys) std::memcpy(phys, rho.data(), nv * sizeof(double));
+      } else if (!(ad[6] >= margin_stop)) {
+        out_i[2] = 1;
+        break;
+      }
+    }
   });
 }
 

@@ -908,6 +908,38 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
       n_design += 1.0;
     }
   }
+  if (o->initial_design) {
+    /* warm_start_design (simp.cpp:324-344): the seed's sequential mean over the
+     * design set scaled to the target, clamped to [rho_min, 1], one filter pass;
+     * masked: FrozenSolid -> 1 and every other non-Active voxel -> 0 after it
+     * (simp.cpp:3083-3090). */
+    const uint8_t* dset0 = mask ? active : solid;
+    double sum = 0.0;
+    size_t n = 0;
+    for (size_t e = 0; e < nv; ++e)
+      if (is_solid(dset0, e) && (mask == NULL || active[e])) {
+        sum += o->initial_design[e];
+        ++n;
+      }
+    const double mean = n > 0 ? sum / (double)n : 0.0;
+    double* raw = calloc(nv, sizeof(double));
+    for (size_t e = 0; e < nv; ++e) {
+      if (!(is_solid(dset0, e) && (mask == NULL || active[e]))) continue;
+      if (mean > 1e-12) {
+        const double v = (o->volume_fraction / mean) * o->initial_design[e];
+        raw[e] = fmin(1.0, fmax(rho_min, v));
+      } else {
+        raw[e] = o->volume_fraction;
+      }
+    }
+    or_filter_density(f, raw, x);
+    free(raw);
+    if (mask)
+      for (size_t e = 0; e < nv; ++e) {
+        if (eff[e] == OR_FROZEN_SOLID) x[e] = 1.0;
+        else if (eff[e] != OR_ACTIVE) x[e] = 0.0;
+      }
+  }
   /* The stage plan (build_stage_plan, simp.cpp:1053-1068): one unprojected stage
    * of max_iterations, or one projected stage per (beta, move, iterations). */
   const int nst = o->nstages > 0 ? o->nstages : 1;
@@ -1022,6 +1054,272 @@ int or_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tag
   return simp_common(nx, ny, nz, h, tags, mask, E0, nu, penal, rho_min, nbc, bc_node, bc_comp,
                      bc_val, nload, ld_node, ld_comp, ld_val, o, hist_c, hist_change, hist_vf,
                      hist_cg, design, phys, res);
+}
+
+/* ------------------------------------------------ stress and the ladder */
+int or_hex8_stress(double E, double nu, double h, const double* ue, double xi, double eta,
+                   double zeta, double* sigma6, double* von_mises) {
+  if (!(E > 0.0)) return fail(OR_EINVAL, "hex8_stress: youngs_modulus must be > 0");
+  if (!(h > 0.0)) return fail(OR_EINVAL, "hex8_stress: element_size must be > 0");
+  if (!(nu > -1.0 && nu < 0.5)) return fail(OR_EINVAL, "hex8_stress: poisson must be in (-1, 0.5)");
+  /* The isotropic D of or_hex8_stiffness. */
+  double D[6][6];
+  memset(D, 0, sizeof D);
+  const double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  D[0][0] = D[1][1] = D[2][2] = c * (1.0 - nu);
+  D[0][1] = D[0][2] = D[1][0] = D[1][2] = D[2][0] = D[2][1] = c * nu;
+  const double G = c * (1.0 - 2.0 * nu) / 2.0;
+  D[3][3] = D[4][4] = D[5][5] = G;
+  /* Shape-function gradients at (xi, eta, zeta), d/dx = (2/h) d/dxi. */
+  const double s2 = 2.0 / h;
+  double gx[8], gy[8], gz[8];
+  for (int a = 0; a < 8; ++a) {
+    const double xa = kXi[a], ea = kEta[a], za = kZeta[a];
+    gx[a] = s2 * (0.125 * xa * (1.0 + eta * ea) * (1.0 + zeta * za));
+    gy[a] = s2 * (0.125 * ea * (1.0 + xi * xa) * (1.0 + zeta * za));
+    gz[a] = s2 * (0.125 * za * (1.0 + xi * xa) * (1.0 + eta * ea));
+  }
+  /* B (6 x 24), engineering strain = B ue summed over the 24 columns in order. */
+  double B[6][24];
+  memset(B, 0, sizeof B);
+  for (int a = 0; a < 8; ++a) {
+    const int x = 3 * a, y = 3 * a + 1, z = 3 * a + 2;
+    B[0][x] = gx[a];
+    B[1][y] = gy[a];
+    B[2][z] = gz[a];
+    B[3][x] = gy[a];
+    B[3][y] = gx[a];
+    B[4][y] = gz[a];
+    B[4][z] = gy[a];
+    B[5][x] = gz[a];
+    B[5][z] = gx[a];
+  }
+  double eps[6], sig[6];
+  for (int r = 0; r < 6; ++r) {
+    double acc = 0.0;
+    for (int col = 0; col < 24; ++col) acc += B[r][col] * ue[col];
+    eps[r] = acc;
+  }
+  for (int r = 0; r < 6; ++r) {
+    double acc = 0.0;
+    for (int m = 0; m < 6; ++m) acc += D[r][m] * eps[m];
+    sig[r] = acc;
+  }
+  if (sigma6) memcpy(sigma6, sig, sizeof sig);
+  const double dxy = sig[0] - sig[1], dyz = sig[1] - sig[2], dzx = sig[2] - sig[0];
+  if (von_mises)
+    *von_mises = sqrt(0.5 * (dxy * dxy + dyz * dyz + dzx * dzx) +
+                      3.0 * (sig[3] * sig[3] + sig[4] * sig[4] + sig[5] * sig[5]));
+  return OR_OK;
+}
+
+int or_stress_margin(double yield_strength, double z_knockdown, double max_von_mises,
+                     double max_interlayer, double* out3) {
+  if (!(isfinite(yield_strength) && yield_strength > 0.0))
+    return fail(OR_EINVAL, "stress margin: yield_strength_mpa must be finite and > 0");
+  if (!(isfinite(z_knockdown) && z_knockdown > 0.0 && z_knockdown <= 1.0))
+    return fail(OR_EINVAL, "stress margin: z_knockdown must be in (0, 1]");
+  if (!(isfinite(max_von_mises) && max_von_mises >= 0.0))
+    return fail(OR_EINVAL, "stress margin: max_von_mises_stress must be finite and >= 0");
+  if (!(isfinite(max_interlayer) && max_interlayer >= 0.0))
+    return fail(OR_EINVAL, "stress margin: max_interlayer_tension must be finite and >= 0");
+  const double ip = max_von_mises > 0.0 ? yield_strength / max_von_mises : INFINITY;
+  const double il = max_interlayer > 0.0 ? (z_knockdown * yield_strength) / max_interlayer
+                                         : INFINITY;
+  out3[0] = ip;
+  out3[1] = il;
+  out3[2] = il < ip ? il : ip;
+  return OR_OK;
+}
+
+int or_load_path_connected(int nx, int ny, int nz, const uint8_t* tags, const double* density,
+                           double iso) {
+  if (tags == NULL) return 1;
+  const size_t nv = (size_t)nx * ny * nz;
+  size_t nload = 0, nfix = 0;
+  for (size_t e = 0; e < nv; ++e) {
+    nload += tags[e] == 4;
+    nfix += tags[e] == 5;
+  }
+  if (nload == 0 || nfix == 0) return 1;
+  uint8_t* seen = calloc(nv, 1);
+  size_t* queue = malloc(nv * sizeof(size_t));
+  size_t head = 0, tail = 0, reached = 0;
+#define PRINTED(e) (tags[e] != 0 && density[e] > iso)
+  for (size_t e = 0; e < nv; ++e)
+    if (tags[e] == 5 && PRINTED(e)) {
+      seen[e] = 1;
+      queue[tail++] = e;
+      reached += tags[e] == 4;
+    }
+  while (head < tail) {
+    const size_t e = queue[head++];
+    const int i = (int)(e % (size_t)nx), j = (int)((e / (size_t)nx) % (size_t)ny),
+              k = (int)(e / ((size_t)nx * ny));
+    for (int dk = -1; dk <= 1; ++dk)
+      for (int dj = -1; dj <= 1; ++dj)
+        for (int di = -1; di <= 1; ++di) {
+          const int a = i + di, b = j + dj, c = k + dk;
+          if (a < 0 || b < 0 || c < 0 || a >= nx || b >= ny || c >= nz) continue;
+          const size_t q = IDX(a, b, c);
+          if (seen[q] || !PRINTED(q)) continue;
+          seen[q] = 1;
+          queue[tail++] = q;
+          reached += tags[q] == 4;
+        }
+  }
+#undef PRINTED
+  free(seen);
+  free(queue);
+  return reached == nload;
+}
+
+int or_analyze_fixed_design(int nx, int ny, int nz, double h, const uint8_t* tags, double E0,
+                            double nu, double penal, double rho_min, const double* density,
+                            int nbc, const int* bc_node, const int* bc_comp,
+                            const double* bc_val, int nload, const int* ld_node,
+                            const int* ld_comp, const double* ld_val, const or_strength* st,
+                            double cg_tol, int cg_max_it, or_analysis* out, double* von_mises) {
+  memset(out, 0, sizeof *out);
+  if (!(st->iso > 0.0 && st->iso < 1.0))
+    return fail(OR_EINVAL, "analyze_fixed_design: printed_iso must be in (0, 1)");
+  const double bl = sqrt(st->build_dir[0] * st->build_dir[0] +
+                         st->build_dir[1] * st->build_dir[1] +
+                         st->build_dir[2] * st->build_dir[2]);
+  if (bl < 1e-12) return fail(OR_EINVAL, "max_interlayer_tension: build_dir is zero length");
+  const size_t nv = (size_t)nx * ny * nz;
+  const size_t ndof = 3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+  double* u = malloc(ndof * sizeof(double));
+  double* dc = malloc(nv * sizeof(double));
+  double resid = 0.0;
+  int st_c = or_simp_compliance(nx, ny, nz, h, tags, E0, nu, penal, rho_min, density, nbc,
+                                bc_node, bc_comp, bc_val, nload, ld_node, ld_comp, ld_val,
+                                cg_tol, cg_max_it, u, dc, &out->compliance, &out->cg_iterations,
+                                &resid);
+  free(dc);
+  if (st_c == OR_ENONCONV) {
+    out->non_convergent = 1;
+    free(u);
+    return OR_OK;
+  }
+  if (st_c) {
+    free(u);
+    return st_c;
+  }
+  /* max_interlayer_tension (orient.cpp:234-263): unit build direction. */
+  const double n0 = st->build_dir[0] / bl, n1 = st->build_dir[1] / bl, n2 = st->build_dir[2] / bl;
+  if (von_mises) memset(von_mises, 0, nv * sizeof(double));
+  double max_vm = 0.0, max_il = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t e = IDX(i, j, k);
+        if (!is_solid(tags, e) || !(density[e] > st->iso)) continue;
+        ++out->printed_voxels;
+        int edof[24];
+        double ue[24], sig[6], vm = 0.0;
+        elem_dofs(nx, ny, i, j, k, edof);
+        for (int q = 0; q < 24; ++q) ue[q] = u[edof[q]];
+        or_hex8_stress(E0, nu, h, ue, 0.0, 0.0, 0.0, sig, &vm);
+        if (von_mises) von_mises[e] = vm;
+        if (vm > max_vm) max_vm = vm;
+        const double t = n0 * n0 * sig[0] + n1 * n1 * sig[1] + n2 * n2 * sig[2] +
+                         2.0 * n0 * n1 * sig[3] + 2.0 * n1 * n2 * sig[4] +
+                         2.0 * n2 * n0 * sig[5];
+        if (t > max_il) max_il = t;
+      }
+  free(u);
+  out->max_von_mises = max_vm;
+  out->max_interlayer = max_il;
+  double m[3];
+  const int sm = or_stress_margin(st->yield_strength, st->z_knockdown, max_vm, max_il, m);
+  if (sm) return sm;
+  out->margin_in_plane = m[0];
+  out->margin_interlayer = m[1];
+  out->margin_worst = m[2];
+  /* gate_margin_effective (analyze.cpp:84-118), scalar posture. */
+  out->margin_effective = m[2] * st->infill_knockdown;
+  out->load_path_ok = or_load_path_connected(nx, ny, nz, tags, density, st->iso);
+  out->accepted = out->load_path_ok && out->margin_effective >= st->margin_stop;
+  return OR_OK;
+}
+
+int or_ladder(int nx, int ny, int nz, double h, const uint8_t* tags, const uint8_t* mask,
+              double E0, double nu, double penal, double rho_min, int nbc, const int* bc_node,
+              const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+              const int* ld_comp, const double* ld_val, const or_simp_options* o,
+              const double* ladder, int nrungs, int warm_start_inherit, const or_strength* st,
+              or_rung* rungs_out, int* evaluated, int* recommended, int* stopped_on_margin,
+              double* design, double* phys) {
+  /* minimize_plastic.cpp:394-452: a non-empty, strictly descending ladder in
+   * (0, 1]; margin_stop finite and >= 0. */
+  if (nrungs < 1) return fail(OR_EINVAL, "minimize_plastic: volume_fraction_ladder is empty");
+  for (int r = 0; r < nrungs; ++r) {
+    if (!isfinite(ladder[r]) || !(ladder[r] > 0.0) || !(ladder[r] <= 1.0))
+      return fail(OR_EINVAL, "minimize_plastic: a ladder volume fraction is not in (0, 1]");
+    if (r > 0 && !(ladder[r] < ladder[r - 1]))
+      return fail(OR_EINVAL, "minimize_plastic: volume_fraction_ladder is not strictly descending");
+  }
+  if (!isfinite(st->margin_stop) || st->margin_stop < 0.0)
+    return fail(OR_EINVAL, "minimize_plastic: margin_stop must be finite and >= 0");
+  const size_t nv = (size_t)nx * ny * nz;
+  uint8_t* all_active = NULL;
+  if (mask == NULL) mask = all_active = calloc(nv, 1); /* no mask: every voxel Active */
+  int total = o->nstages > 0 ? 0 : o->max_iterations;
+  for (int s = 0; s < o->nstages; ++s) total += o->stage_iterations[s];
+  double* hc = malloc(sizeof(double) * (size_t)total);
+  double* hch = malloc(sizeof(double) * (size_t)total);
+  double* hvf = malloc(sizeof(double) * (size_t)total);
+  int* hcg = malloc(sizeof(int) * (size_t)total);
+  double* x = malloc(nv * sizeof(double));
+  double* rho = malloc(nv * sizeof(double));
+  double* seed = malloc(nv * sizeof(double));
+  int have_seed = 0, status = OR_OK;
+  *evaluated = 0;
+  *recommended = -1;
+  *stopped_on_margin = 0;
+  for (int r = 0; r < nrungs; ++r) {
+    or_simp_options opt = *o;
+    opt.volume_fraction = ladder[r];
+    opt.initial_design = have_seed ? seed : NULL;
+    or_simp_result res;
+    status = or_simp_optimize_masked(nx, ny, nz, h, tags, mask, E0, nu, penal, rho_min, nbc,
+                                     bc_node, bc_comp, bc_val, nload, ld_node, ld_comp, ld_val,
+                                     &opt, hc, hch, hvf, hcg, x, rho, &res);
+    if (status) break;
+    or_rung* rg = &rungs_out[r];
+    memset(rg, 0, sizeof *rg);
+    rg->volume_fraction = ladder[r];
+    rg->iterations = res.iterations;
+    rg->compliance = res.compliance;
+    *evaluated = r + 1;
+    if (res.infeasible || res.non_convergent) continue; /* no analysis, seed kept */
+    rg->trajectory_ok = 1;
+    const int lp = or_load_path_connected(nx, ny, nz, tags, rho, st->iso);
+    if (lp) {
+      have_seed = warm_start_inherit;
+      if (have_seed) memcpy(seed, rho, nv * sizeof(double));
+    }
+    status = or_analyze_fixed_design(nx, ny, nz, h, tags, E0, nu, penal, rho_min, rho, nbc,
+                                     bc_node, bc_comp, bc_val, nload, ld_node, ld_comp, ld_val,
+                                     st, o->cg_tolerance, o->cg_max_iterations, &rg->analysis,
+                                     NULL);
+    if (status) break;
+    if (rg->analysis.non_convergent) continue;
+    rg->analysed = 1;
+    rg->accepted = rg->analysis.accepted;
+    if (rg->accepted) {
+      *recommended = r;
+      if (design) memcpy(design, x, nv * sizeof(double));
+      if (phys) memcpy(phys, rho, nv * sizeof(double));
+    } else if (!(rg->analysis.margin_effective >= st->margin_stop)) {
+      *stopped_on_margin = 1;
+      break;
+    }
+  }
+  free(hc); free(hch); free(hvf); free(hcg); free(x); free(rho); free(seed);
+  free(all_active);
+  return status;
 }
 
 /* -------------------------------------------------------- homogenization */

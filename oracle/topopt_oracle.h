@@ -134,6 +134,11 @@ typedef struct {
   const double* stage_move;
   const int* stage_iterations;
   double eta;
+  /* Warm start (SimpOptions::initial_design, simp.hpp:1557-1575): NULL is the
+   * uniform start; otherwise a raw seed density per voxel, rescaled to the
+   * target mean over the design set, clamped and filtered once
+   * (warm_start_design, simp.cpp:324-344). */
+  const double* initial_design;
 } or_simp_options;
 
 /* heaviside_project and its derivative (simp.cpp:352-365). */
@@ -166,6 +171,70 @@ int or_simp_optimize_masked(int nx, int ny, int nz, double h, const uint8_t* tag
                             const int* ld_comp, const double* ld_val, const or_simp_options* o,
                             double* hist_c, double* hist_change, double* hist_vf, int* hist_cg,
                             double* design, double* phys, or_simp_result* res);
+
+/* ------------------------------------------------ stress and the ladder */
+/* hex8_stress (hex_element.cpp:242-316): Cauchy stress (Voigt xx,yy,zz,xy,yz,zx,
+ * true shear) and von Mises at natural coordinates (xi, eta, zeta) of a cubic
+ * element with nodal displacements ue (24, hex8 order). */
+int or_hex8_stress(double E, double nu, double h, const double* ue, double xi, double eta,
+                   double zeta, double* sigma6, double* von_mises);
+/* compute_stress_margin (settings/report.cpp:464-491): out = {in_plane,
+ * interlayer, worst_case}; a zero stress is an unbounded (+inf) margin. */
+int or_stress_margin(double yield_strength, double z_knockdown, double max_von_mises,
+                     double max_interlayer, double* out3);
+/* load_path_connected (voxelize.cpp:609-726): 26-connected flood fill over the
+ * printed voxels (tag != Empty and density > iso) from the printed Fixture
+ * (tag 5) voxels; 1 when it reaches every Load (tag 4) voxel, and vacuously 1
+ * when the grid has no Load or no Fixture voxel.  tags NULL: no tags (1). */
+int or_load_path_connected(int nx, int ny, int nz, const uint8_t* tags, const double* density,
+                           double iso);
+
+/* analyze_fixed_design (analyze.cpp:145-440), the solid-material posture: the
+ * certification solve of the fixed density at cg_tol, the stress of every
+ * printed voxel (solid, density > iso) at its centre with the SOLID modulus E0,
+ * the peak von Mises and interlayer tension max(0, n.sigma.n) along build_dir,
+ * the margins, the load-path belt, and accepted = load_path_ok && worst_case *
+ * infill_knockdown >= margin_stop. */
+typedef struct {
+  int non_convergent, cg_iterations, load_path_ok, accepted;
+  long long printed_voxels;
+  double compliance, max_von_mises, max_interlayer;
+  double margin_in_plane, margin_interlayer, margin_worst, margin_effective;
+} or_analysis;
+typedef struct {
+  double yield_strength, z_knockdown, build_dir[3], iso, infill_knockdown, margin_stop;
+} or_strength;
+int or_analyze_fixed_design(int nx, int ny, int nz, double h, const uint8_t* tags, double E0,
+                            double nu, double penal, double rho_min, const double* density,
+                            int nbc, const int* bc_node, const int* bc_comp,
+                            const double* bc_val, int nload, const int* ld_node,
+                            const int* ld_comp, const double* ld_val, const or_strength* st,
+                            double cg_tol, int cg_max_it, or_analysis* out, double* von_mises);
+
+/* The ladder walk of minimize_plastic (minimize_plastic.cpp:1402-2742) for the
+ * OC updater with no lattice, box or product options: rung r runs the masked
+ * simp_optimize at volume_fraction ladder[r] (seeded from the warm seed), then
+ *   cancelled/infeasible/non-convergent trajectory -> rejected, no analysis, the
+ *     seed untouched, the walk continues;
+ *   load_path_ok -> the seed becomes this rung's physical density when
+ *     warm_start_inherit, else is cleared;
+ *   the analysis; non-convergent certification -> rejected, continue;
+ *   accepted -> recommended = r; else stop when the margin failed
+ *     (stopped_on_margin), continue when only the load path did.
+ * rungs_out[r] per evaluated rung; design/phys of the recommended rung. */
+typedef struct {
+  double volume_fraction;
+  int iterations, trajectory_ok, analysed, accepted;
+  double compliance;
+  or_analysis analysis;
+} or_rung;
+int or_ladder(int nx, int ny, int nz, double h, const uint8_t* tags, const uint8_t* mask,
+              double E0, double nu, double penal, double rho_min, int nbc, const int* bc_node,
+              const int* bc_comp, const double* bc_val, int nload, const int* ld_node,
+              const int* ld_comp, const double* ld_val, const or_simp_options* o,
+              const double* ladder, int nrungs, int warm_start_inherit, const or_strength* st,
+              or_rung* rungs_out, int* evaluated, int* recommended, int* stopped_on_margin,
+              double* design, double* phys);
 
 /* Periodic homogenization of one unit cell (lattice_homog_probe.cpp:290-412):
  * solid (NULL = all solid) selects the elements, cases_mask the Voigt strain

@@ -192,6 +192,56 @@ def main():
             f"{key}_gate_mnd": np.array(gates["discreteness_Mnd_max"]),
         })
 
+    # Element stress (hex8_stress) at the centre and at random natural points.
+    ues = rng.standard_normal((8, 24))
+    mats = np.column_stack([rng.uniform(0.5, 3.0, 8), rng.uniform(0.0, 0.45, 8),
+                            rng.uniform(0.3, 2.0, 8)])
+    pts = np.vstack([np.zeros((4, 3)), rng.uniform(-1.0, 1.0, (4, 3))])
+    sig = np.zeros((8, 6))
+    vms = np.zeros(8)
+    for q in range(8):
+        sig[q], vms[q] = R.hex8_stress(*mats[q], ues[q], *pts[q])
+    out.update(stress_ue=ues, stress_mat=mats, stress_pts=pts, stress_sigma=sig, stress_vm=vms)
+
+    # The ladder walk and the fixed-design analysis on a tagged bracket: a
+    # Fixture slab at x = 0, Load voxels at the loaded tip edge.
+    lx, ly, lz = 20, 6, 8
+    ltags = np.ones((lz, ly, lx), np.uint8)
+    ltags[:, :, 0] = 5
+    ltags[lz // 2 - 1:lz // 2 + 1, :, lx - 1] = 4
+    ltags = ltags.ravel()
+    pbl = cantilever(lx, ly, lz, solid=ltags)
+    lad = [0.6, 0.45, 0.3, 0.2, 0.12]
+    for tag, ms in (("a", 1.0), ("b", 25.0)):
+        L = R.ladder(pbl, None, lad, max_it=25, yield_strength=30.0, margin_stop=ms, cg_tol=1e-9)
+        out[f"lad{tag}_rung_d"] = np.array([[r["volume_fraction"], r["compliance"],
+                                             r["analysis"]["max_von_mises"],
+                                             r["analysis"]["max_interlayer"],
+                                             r["analysis"]["margin_worst"],
+                                             r["analysis"]["margin_effective"]]
+                                            for r in L["rungs"]])
+        out[f"lad{tag}_rung_i"] = np.array([[r["iterations"], r["trajectory_ok"], r["analysed"],
+                                             r["accepted"], r["analysis"]["load_path_ok"]]
+                                            for r in L["rungs"]])
+        out[f"lad{tag}_out"] = np.array([L["evaluated"], L["recommended"],
+                                         int(L["stopped_on_margin"])])
+        out[f"lad{tag}_design"] = L["design"]
+        out[f"lad{tag}_phys"] = L["phys"]
+    out.update(lad_dims=np.array([lx, ly, lz]), lad_tags=ltags, lad_ladder=np.array(lad))
+    dfix = out["lada_phys"]
+    an, vmf = R.analyze_fixed_design(pbl, dfix, yield_strength=30.0, margin_stop=25.0,
+                                     build_dir=(0.3, -0.2, 0.9), cg_tol=1e-10)
+    out.update(ana_density=dfix, ana_vm=vmf,
+               ana_d=np.array([an["compliance"], an["max_von_mises"], an["max_interlayer"],
+                               an["margin_in_plane"], an["margin_interlayer"],
+                               an["margin_worst"]]),
+               ana_i=np.array([an["printed_voxels"], an["load_path_ok"], an["accepted"]]))
+    # Load-path belt on a severed copy (the x = 10 slab carved away).
+    sev = dfix.reshape(lz, ly, lx).copy()
+    sev[:, :, 10] = 0.0
+    out["lp_connected"] = np.array([R.load_path_connected(pbl, dfix),
+                                    R.load_path_connected(pbl, sev.ravel())])
+
     old = os.path.join(HERE, "golden.npz")
     if os.path.exists(old):  # regenerating must not move any earlier vector
         with np.load(old) as z:

@@ -237,3 +237,70 @@ def test_gate_v2_reference_runs_pass_gates(golden, key):
     assert ncomp == int(golden[key + "_gate_components"])
     assert ysym <= float(golden[key + "_gate_ysym"])
     assert mnd <= float(golden[key + "_gate_mnd"])
+
+
+def test_hex8_stress_golden(port, golden):
+    """hex8_stress (hex_element.cpp:242-316) bit-identical to the reference, at
+    the centre and at random natural points."""
+    for q in range(golden["stress_ue"].shape[0]):
+        sig, vm = port.hex8_stress(*golden["stress_mat"][q], golden["stress_ue"][q],
+                                   *golden["stress_pts"][q])
+        assert np.array_equal(sig, golden["stress_sigma"][q])
+        assert vm == golden["stress_vm"][q]
+
+
+def test_stress_margin_rules(port):
+    """compute_stress_margin (report.cpp:464-491): zero stress = unbounded
+    margin, z_knockdown scales the interlayer term, invalid inputs refused."""
+    from oracle.oracle import OracleError
+    assert port.stress_margin(50.0, 0.7, 10.0, 3.0) == (5.0, 0.7 * 50.0 / 3.0, 5.0)
+    assert port.stress_margin(50.0, 1.0, 0.0, 0.0) == (np.inf, np.inf, np.inf)
+    assert port.stress_margin(50.0, 1.0, 0.0, 2.0)[2] == 25.0
+    for bad in ((0.0, 1.0, 1.0, 1.0), (50.0, 1.5, 1.0, 1.0), (50.0, 1.0, -1.0, 1.0)):
+        with pytest.raises(OracleError):
+            port.stress_margin(*bad)
+
+
+def _ladder_problem(golden):
+    nx, ny, nz = (int(v) for v in golden["lad_dims"])
+    return cantilever(nx, ny, nz, solid=golden["lad_tags"])
+
+
+def test_analysis_and_load_path_golden(port, golden):
+    """The fixed-design analysis (certification solve, printed-voxel stress,
+    interlayer tension along a tilted build direction, margins) and the
+    load-path belt, bit-identical to the reference's own pieces."""
+    pb = _ladder_problem(golden)
+    a, vm = port.analyze_fixed_design(pb, golden["ana_density"], yield_strength=30.0,
+                                      margin_stop=25.0, build_dir=(0.3, -0.2, 0.9),
+                                      cg_tol=1e-10)
+    assert np.array_equal(vm, golden["ana_vm"])
+    got = [a["compliance"], a["max_von_mises"], a["max_interlayer"], a["margin_in_plane"],
+           a["margin_interlayer"], a["margin_worst"]]
+    assert np.array_equal(np.array(got), golden["ana_d"])
+    assert [a["printed_voxels"], a["load_path_ok"], a["accepted"]] == golden["ana_i"].tolist()
+    d = golden["ana_density"].reshape(8, 6, 20).copy()
+    assert port.load_path_connected(pb, d.ravel()) == bool(golden["lp_connected"][0])
+    d[:, :, 10] = 0.0
+    assert port.load_path_connected(pb, d.ravel()) == bool(golden["lp_connected"][1]) is False
+
+
+@pytest.mark.parametrize("tag,margin_stop", [("a", 1.0), ("b", 25.0)])
+def test_ladder_walk_golden(port, golden, tag, margin_stop):
+    """The minimize_plastic ladder walk (OC, warm-start inheritance): every
+    rung's trajectory, analysis and verdict, the severed rung rejected without
+    stopping (a) and the margin stop (b), bit-identical to the reference."""
+    pb = _ladder_problem(golden)
+    L = port.ladder(pb, None, golden["lad_ladder"], max_it=25, yield_strength=30.0,
+                    margin_stop=margin_stop, cg_tol=1e-9)
+    rd = np.array([[r["volume_fraction"], r["compliance"], r["analysis"]["max_von_mises"],
+                    r["analysis"]["max_interlayer"], r["analysis"]["margin_worst"],
+                    r["analysis"]["margin_effective"]] for r in L["rungs"]])
+    ri = np.array([[r["iterations"], r["trajectory_ok"], r["analysed"], r["accepted"],
+                    r["analysis"]["load_path_ok"]] for r in L["rungs"]])
+    assert np.array_equal(rd, golden[f"lad{tag}_rung_d"])
+    assert np.array_equal(ri, golden[f"lad{tag}_rung_i"])
+    assert [L["evaluated"], L["recommended"], int(L["stopped_on_margin"])] == \
+        golden[f"lad{tag}_out"].tolist()
+    assert np.array_equal(L["design"], golden[f"lad{tag}_design"])
+    assert np.array_equal(L["phys"], golden[f"lad{tag}_phys"])
