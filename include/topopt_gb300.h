@@ -141,6 +141,11 @@ typedef struct {
   const tg_projection_stage* projection;
   int32_t projection_stages;
   double projection_eta;
+  /* Warm start (SimpOptions::initial_design, simp.hpp:1557-1575): NULL is the
+   * uniform start; otherwise a raw seed density per voxel whose mean over the
+   * design set is rescaled to volume_fraction, clamped to [density_min, 1] and
+   * filtered once (warm_start_design, simp.cpp:324-344). */
+  const double* initial_design;
 } tg_simp_options;
 
 /* One row of the per-iteration record (SimpIteration + the observation fields
@@ -293,6 +298,111 @@ int tg_simp_optimize_masked(const tg_grid* grid, const tg_simp_params* params,
                             tg_progress_fn progress, void* progress_ctx,
                             const volatile int32_t* cancel, tg_simp_iteration* history,
                             double* design_out, double* phys_out, tg_simp_result* result);
+
+/* ---- stress, strength margins and the volume-fraction ladder ---- */
+
+/* The strength side of analyze_fixed_design (analyze.cpp:145-440) in its
+ * solid-material posture: Material::yield_strength_mpa and z_knockdown, the
+ * build direction, the printed-set threshold, KnockdownSpec::infill_knockdown
+ * and the acceptance threshold. */
+typedef struct {
+  double yield_strength;   /* finite, > 0 */
+  double z_knockdown;      /* (0, 1] */
+  double build_dir[3];     /* non-zero; normalised internally */
+  double printed_iso;      /* printed voxels: density > printed_iso, in (0, 1) (0.5) */
+  double infill_knockdown; /* scales the worst-case margin at the gate (1 = solid) */
+  double margin_stop;      /* accepted: margin_effective >= margin_stop (finite, >= 0) */
+} tg_strength_spec;
+
+typedef struct {
+  int32_t non_convergent;  /* the certification solve failed: never accepted */
+  int32_t cg_iterations, load_path_ok, accepted;
+  int64_t printed_voxels;
+  double compliance, max_von_mises, max_interlayer_tension;
+  double margin_in_plane, margin_interlayer, margin_worst_case, margin_effective;
+} tg_fixed_design_analysis;
+
+/* The stress field of a displacement (hex8_stress, hex_element.cpp:242-316, at
+ * each voxel's centre, on the device): for every solid voxel whose density
+ * exceeds iso (density NULL: every solid voxel), the Cauchy stress (Voigt
+ * xx,yy,zz,xy,yz,zx, true shear) into sigma_out[6 e..] and von Mises into
+ * von_mises_out[e]; other voxels 0.  u has 3 (nx+1)(ny+1)(nz+1) entries.  Either
+ * output may be NULL.  Rounds exactly like the reference. */
+int tg_element_stress(const tg_grid* grid, double youngs_modulus, double poisson,
+                      const double* u, const double* density, double iso, double* sigma_out,
+                      double* von_mises_out);
+
+/* load_path_connected (voxel.hpp:359-361; voxelize.cpp:609-726): whether the
+ * printed voxels (tag != Empty, density > iso) connect, 26-connected, every
+ * Load (tag 4) voxel to a printed Fixture (tag 5) voxel; vacuously 1 without
+ * Load or Fixture voxels. */
+int tg_load_path_connected(const tg_grid* grid, const double* density, double iso,
+                           int32_t* connected);
+
+/* analyze_fixed_design, solid posture: the certification solve of the fixed
+ * density at cg_tolerance (a failure sets non_convergent and returns TG_OK),
+ * the stress of every printed voxel with the SOLID modulus, the peak von Mises
+ * and interlayer tension max(0, n.sigma.n) along the build direction,
+ * compute_stress_margin (report.cpp:464-491), the load-path belt and the gate.
+ * von_mises_out (nv) and stress_out (6 nv) may be NULL. */
+int tg_analyze_fixed_design(const tg_grid* grid, const tg_simp_params* params,
+                            const double* density, const tg_dirichlet_bc* bcs, int32_t nbc,
+                            const tg_nodal_load* loads, int32_t nloads,
+                            const tg_strength_spec* strength, double cg_tolerance,
+                            int32_t cg_max_iterations, const tg_solve_options* solve,
+                            tg_fixed_design_analysis* out, double* von_mises_out,
+                            double* stress_out);
+
+/* self_weight_loads (fea.hpp:215; assembly.cpp) and its masked form
+ * (minimize_plastic.cpp:132-143, FrozenVoid voxels weigh nothing): gravity *
+ * density * voxel volume / 8 on each corner node of every solid voxel along the
+ * unit direction, one load per (node, non-zero component) in node order.
+ * Writes min(count, cap) loads to out (may be NULL with cap 0) and returns the
+ * count, or -1 on invalid arguments (tg_last_error). */
+int64_t tg_self_weight_loads(const tg_grid* grid, const uint8_t* mask, double density,
+                             double gravity, const double direction[3], tg_nodal_load* out,
+                             int64_t cap);
+
+/* The volume-fraction ladder of minimize_plastic (pipeline.hpp:113-1060;
+ * minimize_plastic.cpp:1402-2742) for the OC updater, without lattice, design
+ * box or product options: volume_fractions strictly descending in (0, 1]. */
+typedef struct {
+  const double* volume_fractions;
+  int32_t rungs;
+  int32_t warm_start_inherit; /* seed each rung from the last connected rung's density */
+  tg_strength_spec strength;
+} tg_ladder_options;
+
+typedef struct {
+  double volume_fraction;
+  int32_t trajectory_ok; /* 0: infeasible or non-convergent trajectory, not analysed */
+  int32_t analysed;      /* the certification solve converged */
+  int32_t accepted;
+  tg_simp_result optimization;
+  tg_fixed_design_analysis analysis;
+} tg_ladder_rung;
+
+typedef struct {
+  int32_t evaluated;         /* rungs run */
+  int32_t recommended;       /* the last accepted rung (the lightest that passed), or -1 */
+  int32_t stopped_on_margin; /* a rung's margin fell below margin_stop */
+  int32_t cancelled;
+} tg_ladder_result;
+
+/* The ladder walk: rung r runs the masked simp_optimize at volume_fractions[r]
+ * (mask NULL: every voxel Active), seeded from the warm seed; an infeasible or
+ * non-convergent trajectory is rejected unanalysed and the walk continues; a
+ * connected rung becomes the seed (warm_start_inherit) ; the analysis on the
+ * caller's grid; a rejected rung stops the walk only when its margin failed.
+ * rungs_out has room for ladder->rungs entries; design_out / phys_out receive
+ * the recommended rung's fields (untouched when none was accepted). */
+int tg_minimize_plastic(const tg_grid* grid, const tg_simp_params* params,
+                        const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                        int32_t nloads, const tg_simp_options* simp, const uint8_t* mask,
+                        const tg_ladder_options* ladder, tg_progress_fn progress,
+                        void* progress_ctx, const volatile int32_t* cancel,
+                        tg_ladder_rung* rungs_out, tg_ladder_result* result, double* design_out,
+                        double* phys_out);
 
 /* ---- periodic homogenization of unit cells ---- */
 typedef struct {

@@ -49,3 +49,73 @@ def test_python_face_mirrors_reference_names(tg):
               "make_density_filter", "oc_update", "simp_optimize", "SimpJob",
               "SolverNonConvergence"):
         assert hasattr(tg, n)
+
+
+def test_self_weight_loads_host(tg):
+    """self_weight_loads (fea.hpp:215) and its masked form: each solid voxel's
+    weight lumped equally to its 8 corners along the unit direction, FrozenVoid
+    voxels weightless; host-only (the reference's is built on Eigen, absent
+    here, so this is checked by its defining properties)."""
+    import numpy as np
+    nx, ny, nz, h = 5, 4, 3, 0.5
+    rng = np.random.default_rng(2)
+    tags = (rng.random(nx * ny * nz) > 0.3).astype(np.uint8)
+    pb = tg.Problem(nx, ny, nz, h, tags)
+    rho, grav = 1.25, 9.81e-3
+    loads = tg.self_weight_loads(pb, rho, grav, (0.0, 0.0, -2.0))
+    assert all(c == 2 for _, c, _ in loads)
+    nodes = [n for n, _, _ in loads]
+    assert nodes == sorted(nodes) and len(set(nodes)) == len(nodes)
+    total = sum(v for _, _, v in loads)
+    assert abs(total + grav * rho * h ** 3 * tags.sum()) <= 1e-12 * grav * rho * tags.sum()
+    per = grav * rho * (h * h * h) / 8.0
+    f = np.zeros((nz + 1) * (ny + 1) * (nx + 1))
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                if tags[(k * ny + j) * nx + i]:
+                    for dk in (0, 1):
+                        for dj in (0, 1):
+                            for di in (0, 1):
+                                f[((k + dk) * (ny + 1) + j + dj) * (nx + 1) + i + di] += 1
+    for n, _, v in loads:
+        assert abs(v + per * f[n]) <= 1e-15 * per * 8
+    mask = np.where(rng.random(tags.size) < 0.2, tg.MASK_FROZEN_VOID, 0).astype(np.uint8)
+    masked = tg.self_weight_loads(pb, rho, grav, (0.0, 0.0, -1.0), mask=mask)
+    tot_m = sum(v for _, _, v in masked)
+    live = int(((tags > 0) & (mask != tg.MASK_FROZEN_VOID)).sum())
+    assert abs(tot_m + grav * rho * h ** 3 * live) <= 1e-12 * grav * rho * live
+    tilted = tg.self_weight_loads(pb, rho, grav, (1.0, 1.0, 0.0))
+    assert {c for _, c, _ in tilted} == {0, 1}
+    with pytest.raises(ValueError, match="direction"):
+        tg.self_weight_loads(pb, rho, grav, (0.0, 0.0, 0.0))
+    with pytest.raises(ValueError, match="density"):
+        tg.self_weight_loads(pb, -1.0, grav)
+
+
+def test_load_path_host_matches_oracle(tg, port):
+    """load_path_connected on random tagged designs: the library's host walk
+    agrees with the oracle's (itself pinned to the reference)."""
+    import numpy as np
+    from oracle.oracle import cantilever
+    rng = np.random.default_rng(9)
+    nx, ny, nz = 12, 5, 6
+    tags = np.ones((nz, ny, nx), np.uint8)
+    tags[:, :, 0] = 5
+    tags[2:4, :, nx - 1] = 4
+    tags[rng.random(tags.shape) < 0.05] = 0
+    tags[:, :, 0] = 5
+    tags = tags.ravel()
+    o = cantilever(nx, ny, nz, solid=tags)
+    pb = tg.Problem(nx, ny, nz, 1.0, tags)
+    seen = set()
+    for t in range(40):
+        d = rng.random(tags.size) * (0.5 + 0.02 * t)
+        d[tags == 4] = 1.0  # an unprinted Load voxel is never reached
+        if t % 3 == 0:
+            d[tags == 5] = 1.0
+        want = port.load_path_connected(o, d)
+        assert tg.load_path_connected(pb, d) == want
+        seen.add(want)
+    assert seen == {True, False}
+    assert tg.load_path_connected(tg.Problem(nx, ny, nz), np.zeros(tags.size))  # vacuous

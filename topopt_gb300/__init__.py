@@ -40,6 +40,12 @@ from ._capi import (  # noqa: F401
     oc_update,
     oc_update_masked,
     oc_update_projected,
+    StrengthSpec,
+    element_stress,
+    load_path_connected,
+    analyze_fixed_design,
+    self_weight_loads,
+    minimize_plastic,
     heaviside_project,
     heaviside_continuation_schedule,
     simp_compliance,

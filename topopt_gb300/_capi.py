@@ -83,7 +83,8 @@ class _SimpOpt(C.Structure):
                 ("move", C.c_double), ("change_tol", C.c_double), ("cg_tolerance", C.c_double),
                 ("max_iterations", C.c_int32), ("cg_max_iterations", C.c_int32),
                 ("solve", _SolveOpt), ("projection", C.POINTER(_ProjStage)),
-                ("projection_stages", C.c_int32), ("projection_eta", C.c_double)]
+                ("projection_stages", C.c_int32), ("projection_eta", C.c_double),
+                ("initial_design", C.c_void_p)]
 
 
 class _Iter(C.Structure):
@@ -150,6 +151,13 @@ def lib():
         "tg_heaviside_continuation_schedule": ([vp, i32], C.c_int32),
         "tg_oc_update_projected": ([vp, dbl, vp, vp, vp, dbl, dbl, dbl, dbl, dbl, vp], C.c_int),
         "tg_job_set_stage": ([vp, i32], C.c_int),
+        "tg_element_stress": ([vp, dbl, dbl, vp, vp, dbl, vp, vp], C.c_int),
+        "tg_load_path_connected": ([vp, vp, dbl, vp], C.c_int),
+        "tg_analyze_fixed_design": ([vp, vp, vp, vp, i32, vp, i32, vp, dbl, i32, vp, vp, vp,
+                                     vp], C.c_int),
+        "tg_self_weight_loads": ([vp, vp, dbl, dbl, vp, vp, C.c_int64], C.c_int64),
+        "tg_minimize_plastic": ([vp, vp, vp, i32, vp, i32, vp, vp, vp, _PROGRESS, vp, vp, vp,
+                                 vp, vp, vp], C.c_int),
         "tg_server_create": ([vp, vp], C.c_int),
         "tg_server_submit": ([vp, vp, vp, vp, i32, vp, i32, vp, vp, vp], C.c_int),
         "tg_server_wait": ([vp, C.c_int64, vp, vp, vp], C.c_int),
@@ -288,6 +296,8 @@ class SimpOptions:
     # (beta, move, iterations) stages; empty = the unprojected loop.
     projection: list = field(default_factory=list)
     projection_eta: float = 0.5
+    # Warm start (simp.hpp:1557-1575): a raw seed density per voxel, or None.
+    initial_design: object = None
 
     def total_iterations(self) -> int:
         if self.projection:
@@ -305,6 +315,10 @@ class SimpOptions:
             o._stages = arr
             o.projection_stages = len(self.projection)
         o.projection_eta = self.projection_eta
+        if self.initial_design is not None:
+            seed = np.ascontiguousarray(self.initial_design, dtype=np.float64).ravel()
+            o._seed = seed  # kept alive with the struct
+            o.initial_design = seed.ctypes.data_as(C.c_void_p)
         return o
 
 
@@ -501,6 +515,147 @@ def oc_update_projected(pb: Problem, radius, density, xtilde, dcompliance, beta,
     _check(lib().tg_oc_update_projected(C.byref(pb._grid), float(radius), _p(d), _p(xt), _p(dc),
                                         float(beta), float(eta), volume_fraction, move,
                                         density_min, _p(out)))
+    return out
+
+
+# ------------------------------------------------- stress and the ladder
+@dataclass
+class StrengthSpec:
+    """Material strength and the acceptance gate of analyze_fixed_design
+    (analyze.cpp:145-440, solid posture)."""
+    yield_strength: float = 50.0
+    z_knockdown: float = 1.0
+    build_dir: tuple = (0.0, 0.0, 1.0)
+    printed_iso: float = 0.5
+    infill_knockdown: float = 1.0
+    margin_stop: float = 1.5
+
+    def _c(self):
+        return _Strength(self.yield_strength, self.z_knockdown,
+                         (C.c_double * 3)(*[float(v) for v in self.build_dir]), self.printed_iso,
+                         self.infill_knockdown, self.margin_stop)
+
+
+class _Strength(C.Structure):
+    _fields_ = [("yield_strength", C.c_double), ("z_knockdown", C.c_double),
+                ("build_dir", C.c_double * 3), ("printed_iso", C.c_double),
+                ("infill_knockdown", C.c_double), ("margin_stop", C.c_double)]
+
+
+class _Analysis(C.Structure):
+    _fields_ = [("non_convergent", C.c_int32), ("cg_iterations", C.c_int32),
+                ("load_path_ok", C.c_int32), ("accepted", C.c_int32),
+                ("printed_voxels", C.c_int64), ("compliance", C.c_double),
+                ("max_von_mises", C.c_double), ("max_interlayer_tension", C.c_double),
+                ("margin_in_plane", C.c_double), ("margin_interlayer", C.c_double),
+                ("margin_worst_case", C.c_double), ("margin_effective", C.c_double)]
+
+
+class _LadderOpt(C.Structure):
+    _fields_ = [("volume_fractions", C.c_void_p), ("rungs", C.c_int32),
+                ("warm_start_inherit", C.c_int32), ("strength", _Strength)]
+
+
+class _LadderRung(C.Structure):
+    _fields_ = [("volume_fraction", C.c_double), ("trajectory_ok", C.c_int32),
+                ("analysed", C.c_int32), ("accepted", C.c_int32), ("optimization", _Result),
+                ("analysis", _Analysis)]
+
+
+class _LadderResult(C.Structure):
+    _fields_ = [("evaluated", C.c_int32), ("recommended", C.c_int32),
+                ("stopped_on_margin", C.c_int32), ("cancelled", C.c_int32)]
+
+
+def _struct_dict(st):
+    out = {}
+    for name, _ in st._fields_:
+        v = getattr(st, name)
+        out[name] = _struct_dict(v) if isinstance(v, C.Structure) else v
+    return out
+
+
+def element_stress(pb: Problem, youngs_modulus, poisson, u, density=None, iso=0.5):
+    """hex8_stress at every voxel centre (on the device): (sigma (nv, 6), von Mises)."""
+    uu = _f64(u, pb.ndof)
+    d = None if density is None else _f64(density, pb.nv)
+    sig, vm = np.zeros(6 * pb.nv), np.zeros(pb.nv)
+    _check(lib().tg_element_stress(C.byref(pb._grid), youngs_modulus, poisson, _p(uu), _p(d), iso,
+                                   _p(sig), _p(vm)))
+    return sig.reshape(pb.nv, 6), vm
+
+
+def load_path_connected(pb: Problem, density, iso=0.5) -> bool:
+    """load_path_connected (voxel.hpp:359-361) on the problem's tags."""
+    d = _f64(density, pb.nv)
+    out = C.c_int32(0)
+    _check(lib().tg_load_path_connected(C.byref(pb._grid), _p(d), iso, C.byref(out)))
+    return bool(out.value)
+
+
+def analyze_fixed_design(pb: Problem, params: SimpParams, density, strength: StrengthSpec,
+                         cg_tolerance=1e-8, cg_max_iterations=0, solve: SolveOptions | None = None,
+                         fields=False):
+    """analyze_fixed_design (analyze.cpp:145-440), solid posture: a dict of the
+    certification solve, peak stresses, margins and the verdict (+ the von Mises
+    and stress fields with fields=True)."""
+    d = _f64(density, pb.nv)
+    prm, st = params._c(), strength._c()
+    so = (solve or SolveOptions())._c()
+    out = _Analysis()
+    vm = np.zeros(pb.nv) if fields else None
+    sig = np.zeros(6 * pb.nv) if fields else None
+    g, b, nb, l, nl = pb._args()
+    _check(lib().tg_analyze_fixed_design(g, C.byref(prm), _p(d), b, nb, l, nl, C.byref(st),
+                                         cg_tolerance, cg_max_iterations, C.byref(so),
+                                         C.byref(out), _p(vm), _p(sig)))
+    res = _struct_dict(out)
+    if fields:
+        res["von_mises"] = vm
+        res["stress"] = sig.reshape(pb.nv, 6)
+    return res
+
+
+def self_weight_loads(pb: Problem, density, gravity=9.81e-3, direction=(0.0, 0.0, -1.0),
+                      mask=None):
+    """self_weight_loads (fea.hpp:215; masked form minimize_plastic.cpp:132-143):
+    a list of (node, component, value)."""
+    m = None if mask is None else _mask(pb, mask)
+    dv = (C.c_double * 3)(*[float(v) for v in direction])
+    n = lib().tg_self_weight_loads(C.byref(pb._grid), _p(m), float(density), float(gravity), dv,
+                                   None, 0)
+    if n < 0:
+        raise ValueError(lib().tg_last_error().decode())
+    buf = (_Bc * max(int(n), 1))()  # tg_nodal_load has the same layout
+    lib().tg_self_weight_loads(C.byref(pb._grid), _p(m), float(density), float(gravity), dv,
+                               C.cast(buf, C.c_void_p), int(n))
+    return [(buf[i].node, buf[i].component, buf[i].value) for i in range(int(n))]
+
+
+def minimize_plastic(pb: Problem, params: SimpParams, options: SimpOptions, ladder,
+                     strength: StrengthSpec, mask=None, warm_start_inherit=True, progress=None,
+                     cancel=None):
+    """The volume-fraction ladder walk of minimize_plastic
+    (minimize_plastic.cpp:1402-2742, OC): per-rung records, the recommended
+    (lightest accepted) rung and its design / physical density."""
+    lad = np.ascontiguousarray(ladder, dtype=np.float64)
+    prm, opt = params._c(), options._c()
+    lo = _LadderOpt(lad.ctypes.data_as(C.c_void_p), lad.size, int(bool(warm_start_inherit)),
+                    strength._c())
+    rungs = (_LadderRung * lad.size)()
+    res = _LadderResult()
+    design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+    m = None if mask is None else _mask(pb, mask)
+    cb = _PROGRESS(lambda ctx, it, c, ch: progress(it, c, ch)) if progress else _PROGRESS()
+    cptr = None if cancel is None else cancel.ctypes.data_as(C.c_void_p)
+    g, b, nb, l, nl = pb._args()
+    _check(lib().tg_minimize_plastic(g, C.byref(prm), b, nb, l, nl, C.byref(opt), _p(m),
+                                     C.byref(lo), cb, None, cptr, C.cast(rungs, C.c_void_p),
+                                     C.byref(res), _p(design), _p(phys)))
+    out = _struct_dict(res)
+    out["rungs"] = [_struct_dict(rungs[i]) for i in range(res.evaluated)]
+    if res.recommended >= 0:
+        out["design"], out["physical_density"] = design, phys
     return out
 
 

@@ -41,8 +41,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     cc = nvcc()
+    # Host code computes constants the reference computes (D, weights, the OC
+    # bisection); no multiply/add pair may fuse there, on any host ISA.
     flags = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                    "-Xcompiler", "-Wall", "--expt-relaxed-constexpr"]
+                    "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off",
+                    "--expt-relaxed-constexpr"]
 
     def compile_one(src: str) -> str:
         obj = os.path.join(OBJ, src.replace(".cu", ".o"))

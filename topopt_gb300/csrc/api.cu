@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -111,9 +112,9 @@ void cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 }
 
 template <class F>
-int guarded(F&& fn) {
+int guarded(F&& fn, bool device = true) {
   try {
-    TG_CUDA(cudaSetDevice(g_device));
+    if (device) TG_CUDA(cudaSetDevice(g_device));
     fn();
     return TG_OK;
   } catch (const Error& e) {
@@ -685,8 +686,42 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
     ones[size_t(e)] = j->solid_h[size_t(e)] ? o.volume_fraction : 0.0;
     if (j->masked && j->eff_h[size_t(e)] == 1) ones[size_t(e)] = 1.0;
   }
-  TG_CUDA(cudaMemcpyAsync(j->x.p, ones.data(), j->x.bytes(), cudaMemcpyHostToDevice, s));
+  if (o.initial_design) {
+    // warm_start_design (simp.cpp:324-344): the seed's mean over the design set
+    // (summed in voxel order, on the host, as the reference sums it) rescaled to
+    // the target, each design entry clamped to [density_min, 1], one pass of the
+    // loop's filter; masked jobs then pin FrozenSolid to 1 and every other
+    // non-Active voxel to 0 (simp.cpp:3083-3090).
+    const double* seed = o.initial_design;
+    double sum = 0.0;
+    int64_t n = 0;
+    for (int64_t e = 0; e < g.nv; ++e)
+      if (j->solid_h[size_t(e)]) {
+        sum += seed[e];
+        ++n;
+      }
+    const double mean = n > 0 ? sum / double(n) : 0.0;
+    const double rho_min = params->density_min;
+    for (int64_t e = 0; e < g.nv; ++e) {
+      double v = 0.0;
+      if (j->solid_h[size_t(e)]) {
+        if (mean > 1e-12) {
+          const double scale = o.volume_fraction / mean;
+          v = std::min(1.0, std::max(rho_min, scale * seed[e]));
+        } else {
+          v = o.volume_fraction;
+        }
+      }
+      ones[size_t(e)] = v;
+    }
+    TG_CUDA(cudaMemcpyAsync(j->xnew.p, ones.data(), j->xnew.bytes(), cudaMemcpyHostToDevice, s));
+    j->filt.fwd(g, j->solid.p, j->xnew.p, j->x.p, s);
+    if (j->masked) launch_mask_pins(j->eff.p, g.nv, j->x.p, s);
+  } else {
+    TG_CUDA(cudaMemcpyAsync(j->x.p, ones.data(), j->x.bytes(), cudaMemcpyHostToDevice, s));
+  }
   TG_CUDA(cudaStreamSynchronize(s));
+  j->opt.initial_design = nullptr;  // consumed; the caller's buffer need not outlive the call
 }
 
 double read1(tg_job* j, const double* dptr) {
@@ -829,6 +864,139 @@ bool rung_infeasible(const std::vector<double>& c, const std::vector<int>& cg) {
   return (hi - lo) / lo <= 1e-3;
 }
 
+
+// ------------------------------------------------------ strength analysis
+void validate_strength(const tg_strength_spec* sp) {
+  if (!sp) raise(TG_EINVAL, "strength spec is null");
+  if (!(sp->printed_iso > 0.0 && sp->printed_iso < 1.0))
+    raise(TG_EINVAL, "analyze_fixed_design: printed_iso must be in (0, 1)");
+  const double* b = sp->build_dir;
+  if (!(std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) >= 1e-12))
+    raise(TG_EINVAL, "max_interlayer_tension: build_dir is zero length");
+  if (!(std::isfinite(sp->yield_strength) && sp->yield_strength > 0.0))
+    raise(TG_EINVAL, "stress margin: yield_strength_mpa must be finite and > 0");
+  if (!(std::isfinite(sp->z_knockdown) && sp->z_knockdown > 0.0 && sp->z_knockdown <= 1.0))
+    raise(TG_EINVAL, "stress margin: z_knockdown must be in (0, 1]");
+}
+
+// load_path_connected (voxelize.cpp:609-726): breadth-first flood fill over the
+// printed voxels from the printed Fixture voxels, 26-connected; connected when
+// every Load voxel is reached; vacuous without Load or Fixture voxels.
+bool load_path_host(const Grid& g, const uint8_t* tags, const double* rho, double iso) {
+  if (!tags) return true;
+  int64_t nload = 0, nfix = 0;
+  for (int64_t e = 0; e < g.nv; ++e) {
+    nload += tags[e] == 4;
+    nfix += tags[e] == 5;
+  }
+  if (nload == 0 || nfix == 0) return true;
+  auto printed = [&](int64_t e) { return tags[e] != 0 && rho[e] > iso; };
+  std::vector<uint8_t> seen(size_t(g.nv), 0);
+  std::vector<int64_t> queue;
+  int64_t reached = 0;
+  for (int64_t e = 0; e < g.nv; ++e)
+    if (tags[e] == 5 && printed(e)) {
+      seen[size_t(e)] = 1;
+      queue.push_back(e);
+    }
+  for (size_t h = 0; h < queue.size(); ++h) {
+    const int64_t e = queue[h];
+    reached += tags[e] == 4;
+    const int i = int(e % g.nx), jj = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+    for (int dk = -1; dk <= 1; ++dk)
+      for (int dj = -1; dj <= 1; ++dj)
+        for (int di = -1; di <= 1; ++di) {
+          const int a = i + di, b = jj + dj, c = k + dk;
+          if (a < 0 || b < 0 || c < 0 || a >= g.nx || b >= g.ny || c >= g.nz) continue;
+          const int64_t q = (int64_t(c) * g.ny + b) * g.nx + a;
+          if (seen[size_t(q)] || !printed(q)) continue;
+          seen[size_t(q)] = 1;
+          queue.push_back(q);
+        }
+  }
+  return reached == nload;
+}
+
+// compute_stress_margin (report.cpp:464-491) and the scalar gate
+// (gate_margin_effective, analyze.cpp:84-118).
+void fill_margins(tg_fixed_design_analysis* a, const tg_strength_spec& sp) {
+  const double inf = std::numeric_limits<double>::infinity();
+  const double vm = a->max_von_mises, il = a->max_interlayer_tension;
+  if (!(std::isfinite(vm) && vm >= 0.0))
+    raise(TG_EINVAL, "stress margin: max_von_mises_stress must be finite and >= 0");
+  if (!(std::isfinite(il) && il >= 0.0))
+    raise(TG_EINVAL, "stress margin: max_interlayer_tension must be finite and >= 0");
+  a->margin_in_plane = vm > 0.0 ? sp.yield_strength / vm : inf;
+  a->margin_interlayer = il > 0.0 ? (sp.z_knockdown * sp.yield_strength) / il : inf;
+  a->margin_worst_case = std::min(a->margin_in_plane, a->margin_interlayer);
+  a->margin_effective = a->margin_worst_case * sp.infill_knockdown;
+}
+
+// analyze_fixed_design on a job built for the analysis grid: the density goes
+// to xPhys, the certification solve at the job's tolerance, the stresses of the
+// printed voxels with the solid modulus, the margins, the load-path belt and
+// the gate.  rho_host is the same density on the host (for the belt).
+void analyze_on_job(tg_job* aj, const double* rho_host, const uint8_t* tags,
+                    const tg_strength_spec& sp, tg_fixed_design_analysis* out,
+                    double* vm_out, double* stress_out) {
+  AllocScope scope(aj->s);
+  std::memset(out, 0, sizeof *out);
+  const Grid& g = aj->fp.g;
+  TG_CUDA(cudaMemcpyAsync(aj->xphys.p, rho_host, aj->xphys.bytes(), cudaMemcpyHostToDevice,
+                          aj->s));
+  aj->xphys_valid = true;
+  const SolverStats st = job_solve(aj, aj->opt.cg_tolerance, aj->opt.cg_max_iterations);
+  out->cg_iterations = st.iterations;
+  if (!st.converged) {
+    out->non_convergent = 1;  // never accepted (analyze.cpp:270-283)
+    return;
+  }
+  out->compliance = job_sensitivity(aj);
+  DBuf<uint64_t> peaks(3);
+  DBuf<double> vm_d, sig_d;
+  if (vm_out) vm_d.alloc(size_t(g.nv));
+  if (stress_out) sig_d.alloc(size_t(6 * g.nv));
+  TG_CUDA(cudaMemsetAsync(peaks.p, 0, 3 * sizeof(uint64_t), aj->s));
+  launch_element_stress(g, aj->fp.elem.p, aj->xphys.p, aj->u.p, aj->params.youngs_modulus,
+                        aj->params.poisson, g.h, sp.build_dir, sp.printed_iso, vm_d.p, sig_d.p,
+                        peaks.p, aj->s);
+  uint64_t h[3];
+  TG_CUDA(cudaMemcpyAsync(h, peaks.p, sizeof h, cudaMemcpyDeviceToHost, aj->s));
+  if (vm_out)
+    TG_CUDA(cudaMemcpyAsync(vm_out, vm_d.p, vm_d.bytes(), cudaMemcpyDeviceToHost, aj->s));
+  if (stress_out)
+    TG_CUDA(cudaMemcpyAsync(stress_out, sig_d.p, sig_d.bytes(), cudaMemcpyDeviceToHost, aj->s));
+  TG_CUDA(cudaStreamSynchronize(aj->s));
+  double vm = 0.0, il = 0.0;
+  std::memcpy(&vm, &h[0], sizeof vm);
+  std::memcpy(&il, &h[1], sizeof il);
+  out->max_von_mises = vm;
+  out->max_interlayer_tension = il;
+  out->printed_voxels = int64_t(h[2]);
+  fill_margins(out, sp);
+  out->load_path_ok = load_path_host(g, tags, rho_host, sp.printed_iso) ? 1 : 0;
+  out->accepted = out->load_path_ok && out->margin_effective >= sp.margin_stop;
+}
+
+// A job that only solves: the analysis grid, its BCs and loads, the solve form
+// and tolerance (tg_simp_compliance builds the same).
+std::unique_ptr<tg_job> solve_only_job(const tg_grid* grid, const tg_simp_params* params,
+                                       const tg_dirichlet_bc* bcs, int nbc,
+                                       const tg_nodal_load* loads, int nloads, double tol,
+                                       int max_it, const tg_solve_options* solve) {
+  tg_simp_options o;
+  std::memset(&o, 0, sizeof o);
+  o.volume_fraction = 0.5;
+  o.filter_radius = 1.5;
+  o.move = 0.2;
+  o.max_iterations = 1;
+  o.cg_tolerance = tol > 0.0 ? tol : 1e-8;
+  o.cg_max_iterations = max_it;
+  if (solve) o.solve = *solve;
+  auto jp = std::make_unique<tg_job>();
+  job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, &o);
+  return jp;
+}
 
 // make_density_filter(grid, radius[, mask]) and one filter pass: the design set
 // is the solid voxels, and with a mask the solid voxels whose entry is Active
@@ -1081,18 +1249,9 @@ int tg_simp_compliance(const tg_grid* grid, const tg_simp_params* params, const 
     validate_grid(grid);
     validate_params(params);
     if (!density) raise(TG_EINVAL, "density is null");
-    tg_simp_options o;
-    std::memset(&o, 0, sizeof o);
-    o.volume_fraction = 0.5;
-    o.filter_radius = 1.5;
-    o.move = 0.2;
-    o.max_iterations = 1;
-    o.cg_tolerance = tol > 0.0 ? tol : 1e-8;
-    o.cg_max_iterations = max_it;
-    if (options) o.solve = *options;
-    jp = std::make_unique<tg_job>();
-    job_init(jp.get(), grid, params, bcs, nbc, loads, nloads, &o);
+    jp = solve_only_job(grid, params, bcs, nbc, loads, nloads, tol, max_it, options);
     tg_job* j = jp.get();
+    const tg_simp_options& o = j->opt;
     const Grid& g = j->fp.g;
     TG_CUDA(cudaMemcpyAsync(j->xphys.p, density, j->xphys.bytes(), cudaMemcpyHostToDevice, j->s));
     j->xphys_valid = true;
@@ -1446,6 +1605,185 @@ int tg_simp_optimize_masked(const tg_grid* grid, const tg_simp_params* params,
   }
   return simp_optimize_impl(grid, params, bcs, nbc, loads, nloads, options, mask, progress,
                             progress_ctx, cancel, history, design_out, phys_out, result);
+}
+
+int tg_element_stress(const tg_grid* grid, double youngs_modulus, double poisson,
+                      const double* u, const double* density, double iso, double* sigma_out,
+                      double* von_mises_out) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!u) raise(TG_EINVAL, "u is null");
+    if (!(youngs_modulus > 0.0)) raise(TG_EINVAL, "hex8_stress: youngs_modulus must be > 0");
+    if (!(grid->spacing > 0.0)) raise(TG_EINVAL, "hex8_stress: element_size must be > 0");
+    if (!(poisson > -1.0 && poisson < 0.5))
+      raise(TG_EINVAL, "hex8_stress: poisson must be in (-1, 0.5)");
+    CallStream cs;
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    std::vector<uint8_t> solid(size_t(g.nv));
+    for (int64_t e = 0; e < g.nv; ++e) solid[size_t(e)] = grid->tags == nullptr || grid->tags[e];
+    DBuf<uint8_t> dsolid;
+    DBuf<double> du, drho, dvm, dsig;
+    upload(dsolid, solid.data(), solid.size(), cs.s);
+    upload(du, u, size_t(g.ndof), cs.s);
+    if (density) upload(drho, density, size_t(g.nv), cs.s);
+    if (von_mises_out) dvm.alloc(size_t(g.nv));
+    if (sigma_out) dsig.alloc(size_t(6 * g.nv));
+    const double zdir[3] = {0.0, 0.0, 1.0};
+    launch_element_stress(g, dsolid.p, drho.p, du.p, youngs_modulus, poisson, g.h, zdir, iso,
+                          dvm.p, dsig.p, nullptr, cs.s);
+    if (von_mises_out)
+      TG_CUDA(cudaMemcpyAsync(von_mises_out, dvm.p, dvm.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    if (sigma_out)
+      TG_CUDA(cudaMemcpyAsync(sigma_out, dsig.p, dsig.bytes(), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+  });
+}
+
+int tg_load_path_connected(const tg_grid* grid, const double* density, double iso,
+                           int32_t* connected) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!density || !connected) raise(TG_EINVAL, "density and connected must be non-null");
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    *connected = load_path_host(g, grid->tags, density, iso) ? 1 : 0;
+  }, /*device=*/false);
+}
+
+int tg_analyze_fixed_design(const tg_grid* grid, const tg_simp_params* params,
+                            const double* density, const tg_dirichlet_bc* bcs, int32_t nbc,
+                            const tg_nodal_load* loads, int32_t nloads,
+                            const tg_strength_spec* strength, double cg_tolerance,
+                            int32_t cg_max_iterations, const tg_solve_options* solve,
+                            tg_fixed_design_analysis* out, double* von_mises_out,
+                            double* stress_out) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!density || !out) raise(TG_EINVAL, "density and out must be non-null");
+    validate_strength(strength);
+    auto aj = solve_only_job(grid, params, bcs, nbc, loads, nloads, cg_tolerance,
+                             cg_max_iterations, solve);
+    analyze_on_job(aj.get(), density, grid->tags, *strength, out, von_mises_out, stress_out);
+  });
+}
+
+int64_t tg_self_weight_loads(const tg_grid* grid, const uint8_t* mask, double density,
+                             double gravity, const double direction[3], tg_nodal_load* out,
+                             int64_t cap) {
+  int64_t count = -1;
+  const int rc = guarded([&] {
+    validate_grid(grid);
+    if (!direction) raise(TG_EINVAL, "self_weight_loads: direction is null");
+    if (density < 0.0) raise(TG_EINVAL, "self_weight_loads: density must be >= 0");
+    if (gravity < 0.0) raise(TG_EINVAL, "self_weight_loads: gravity must be >= 0");
+    const double len = std::sqrt(direction[0] * direction[0] + direction[1] * direction[1] +
+                                 direction[2] * direction[2]);
+    if (!(len > 1e-12)) raise(TG_EINVAL, "self_weight_loads: direction must have non-zero length");
+    const double d[3] = {direction[0] / len, direction[1] / len, direction[2] / len};
+    const Grid g = Grid::make(grid->nx, grid->ny, grid->nz, grid->spacing);
+    const double h = grid->spacing;
+    const double per_node = gravity * density * (h * h * h) / 8.0;
+    std::vector<double> nodef(size_t(g.ndof), 0.0);
+    for (int k = 0; k < g.nz; ++k)
+      for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i) {
+          const int64_t e = (int64_t(k) * g.ny + j) * g.nx + i;
+          if (grid->tags && grid->tags[e] == 0) continue;
+          if (mask && mask[e] == 2) continue;  // FrozenVoid weighs nothing
+          for (int a = 0; a < 8; ++a) {
+            const int ox = (a ^ (a >> 1)) & 1, oy = (a >> 1) & 1, oz = a >> 2;
+            const int64_t n = (int64_t(k + oz) * g.nny + (j + oy)) * g.nnx + (i + ox);
+            for (int c = 0; c < 3; ++c) nodef[size_t(3 * n + c)] += per_node * d[c];
+          }
+        }
+    count = 0;
+    for (int64_t n = 0; n < g.nnodes; ++n)
+      for (int c = 0; c < 3; ++c) {
+        const double v = nodef[size_t(3 * n + c)];
+        if (v == 0.0) continue;
+        if (out && count < cap) out[count] = tg_nodal_load{int32_t(n), c, v};
+        ++count;
+      }
+  }, /*device=*/false);
+  return rc == TG_OK ? count : -1;
+}
+
+int tg_minimize_plastic(const tg_grid* grid, const tg_simp_params* params,
+                        const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                        int32_t nloads, const tg_simp_options* simp, const uint8_t* mask,
+                        const tg_ladder_options* ladder, tg_progress_fn progress,
+                        void* progress_ctx, const volatile int32_t* cancel,
+                        tg_ladder_rung* rungs_out, tg_ladder_result* result, double* design_out,
+                        double* phys_out) {
+  tg_ladder_result res{};
+  res.recommended = -1;
+  const int rc = guarded([&] {
+    validate_grid(grid);
+    if (!simp || !ladder || !rungs_out) raise(TG_EINVAL, "simp, ladder and rungs_out must be non-null");
+    // minimize_plastic.cpp:394-452.
+    if (ladder->rungs < 1 || !ladder->volume_fractions)
+      raise(TG_EINVAL, "minimize_plastic: volume_fraction_ladder is empty");
+    const double* vf = ladder->volume_fractions;
+    for (int r = 0; r < ladder->rungs; ++r) {
+      if (!std::isfinite(vf[r]) || !(vf[r] > 0.0) || !(vf[r] <= 1.0))
+        raise(TG_EINVAL, "minimize_plastic: a ladder volume fraction is not in (0, 1]");
+      if (r > 0 && !(vf[r] < vf[r - 1]))
+        raise(TG_EINVAL, "minimize_plastic: volume_fraction_ladder is not strictly descending");
+    }
+    const tg_strength_spec& sp = ladder->strength;
+    if (!std::isfinite(sp.margin_stop) || sp.margin_stop < 0.0)
+      raise(TG_EINVAL, "minimize_plastic: margin_stop must be finite and >= 0");
+    validate_strength(&sp);
+    const int64_t nv = int64_t(grid->nx) * grid->ny * grid->nz;
+    std::vector<uint8_t> all_active;
+    if (!mask) {
+      all_active.assign(size_t(nv), uint8_t(0));  // every voxel Active
+      mask = all_active.data();
+    }
+    // The analysis runs on the caller's grid (its tags, FrozenVoid voxels still
+    // soft elements), built once for the whole ladder.
+    auto aj = solve_only_job(grid, params, bcs, nbc, loads, nloads, simp->cg_tolerance,
+                             simp->cg_max_iterations, &simp->solve);
+    std::vector<double> seed, design(static_cast<size_t>(nv)), phys(static_cast<size_t>(nv));
+    for (int r = 0; r < ladder->rungs; ++r) {
+      tg_ladder_rung& rg = rungs_out[r];
+      std::memset(&rg, 0, sizeof rg);
+      rg.volume_fraction = vf[r];
+      tg_simp_options opt = *simp;
+      opt.volume_fraction = vf[r];
+      opt.initial_design = seed.empty() ? nullptr : seed.data();
+      const int src = simp_optimize_impl(grid, params, bcs, nbc, loads, nloads, &opt, mask,
+                                         progress, progress_ctx, cancel, nullptr, design.data(),
+                                         phys.data(), &rg.optimization);
+      if (src != TG_OK) throw Error(src, g_err);
+      res.evaluated = r + 1;
+      if (rg.optimization.cancelled) {  // the terminal rung, unanalysed
+        res.cancelled = 1;
+        break;
+      }
+      if (rg.optimization.infeasible || rg.optimization.non_convergent) continue;
+      rg.trajectory_ok = 1;
+      if (load_path_host(aj->fp.g, grid->tags, phys.data(), sp.printed_iso)) {
+        if (ladder->warm_start_inherit)
+          seed = phys;
+        else
+          seed.clear();
+      }
+      analyze_on_job(aj.get(), phys.data(), grid->tags, sp, &rg.analysis, nullptr, nullptr);
+      if (rg.analysis.non_convergent) continue;
+      rg.analysed = 1;
+      rg.accepted = rg.analysis.accepted;
+      if (rg.accepted) {
+        res.recommended = r;
+        if (design_out) std::memcpy(design_out, design.data(), design.size() * sizeof(double));
+        if (phys_out) std::memcpy(phys_out, phys.data(), phys.size() * sizeof(double));
+      } else if (!(rg.analysis.margin_effective >= sp.margin_stop)) {
+        res.stopped_on_margin = 1;
+        break;
+      }
+    }
+  });
+  if (result) *result = res;
+  return rc;
 }
 
 }  // extern "C"

@@ -515,6 +515,85 @@ __global__ void __launch_bounds__(kThreads) k_proj_volume(GridDev g, const Stenc
   }
 }
 
+// ---------------------------------------------------------------- stress
+// hex8_stress at the element centre (hex_element.cpp:242-316).  At the centre
+// every shape-function gradient is +-q, q = (2/h) * 0.125 exactly, with the
+// signs of the natural coordinates of the node (bottom face CCW, then top).
+// The strain sums run over the 24 columns of B in order (the zero columns add
+// nothing), the stress over the 6 columns of D, and every product and sum is a
+// separate IEEE operation, so the result is the reference's bit for bit.
+struct StressConsts {
+  double q, d_diag, d_off, shear;  // (2/h)/8; c(1-nu), c nu, c(1-2nu)/2
+  double w[6];                     // n.sigma.n weights: nx^2, ny^2, nz^2, 2nxny, 2nynz, 2nznx
+  double iso;
+};
+
+__global__ void k_element_stress(GridDev g, const uint8_t* __restrict__ solid,
+                                 const double* __restrict__ rho, const double* __restrict__ u,
+                                 StressConsts c, double* __restrict__ vm_out,
+                                 double* __restrict__ sig_out,
+                                 unsigned long long* __restrict__ peaks) {
+  const int64_t n = int64_t(g.nx) * g.ny * g.nz;
+  double vmax = 0.0, tmax = 0.0;
+  unsigned long long printed = 0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    const bool on = solid[e] && (rho == nullptr || rho[e] > c.iso);
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, vm = 0.0;
+    if (on) {
+      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      double ex = 0.0, ey = 0.0, ez = 0.0, gxy = 0.0, gyz = 0.0, gzx = 0.0;
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        // Node a: x offset (a ^ (a >> 1)) & 1, y offset (a >> 1) & 1, z offset a >> 2.
+        const int ox = (a ^ (a >> 1)) & 1, oy = (a >> 1) & 1, oz = a >> 2;
+        const int64_t node = (int64_t(k + oz) * g.nny + (j + oy)) * g.nnx + (i + ox);
+        const double ux = u[3 * node], uy = u[3 * node + 1], uz = u[3 * node + 2];
+        const double gx = ox ? c.q : -c.q, gy = oy ? c.q : -c.q, gz = oz ? c.q : -c.q;
+        ex = __dadd_rn(ex, __dmul_rn(gx, ux));
+        ey = __dadd_rn(ey, __dmul_rn(gy, uy));
+        ez = __dadd_rn(ez, __dmul_rn(gz, uz));
+        gxy = __dadd_rn(__dadd_rn(gxy, __dmul_rn(gy, ux)), __dmul_rn(gx, uy));
+        gyz = __dadd_rn(__dadd_rn(gyz, __dmul_rn(gz, uy)), __dmul_rn(gy, uz));
+        gzx = __dadd_rn(__dadd_rn(gzx, __dmul_rn(gz, ux)), __dmul_rn(gx, uz));
+      }
+      s[0] = __dadd_rn(__dadd_rn(__dmul_rn(c.d_diag, ex), __dmul_rn(c.d_off, ey)),
+                       __dmul_rn(c.d_off, ez));
+      s[1] = __dadd_rn(__dadd_rn(__dmul_rn(c.d_off, ex), __dmul_rn(c.d_diag, ey)),
+                       __dmul_rn(c.d_off, ez));
+      s[2] = __dadd_rn(__dadd_rn(__dmul_rn(c.d_off, ex), __dmul_rn(c.d_off, ey)),
+                       __dmul_rn(c.d_diag, ez));
+      s[3] = __dmul_rn(c.shear, gxy);
+      s[4] = __dmul_rn(c.shear, gyz);
+      s[5] = __dmul_rn(c.shear, gzx);
+      const double a01 = __dsub_rn(s[0], s[1]), a12 = __dsub_rn(s[1], s[2]),
+                   a20 = __dsub_rn(s[2], s[0]);
+      const double nrm = __dadd_rn(__dadd_rn(__dmul_rn(a01, a01), __dmul_rn(a12, a12)),
+                                   __dmul_rn(a20, a20));
+      const double shr = __dadd_rn(__dadd_rn(__dmul_rn(s[3], s[3]), __dmul_rn(s[4], s[4])),
+                                   __dmul_rn(s[5], s[5]));
+      vm = __dsqrt_rn(__dadd_rn(__dmul_rn(0.5, nrm), __dmul_rn(3.0, shr)));
+      double t = __dmul_rn(c.w[0], s[0]);
+#pragma unroll
+      for (int r = 1; r < 6; ++r) t = __dadd_rn(t, __dmul_rn(c.w[r], s[r]));
+      if (vm > vmax) vmax = vm;
+      if (t > tmax) tmax = t;
+      ++printed;
+    }
+    if (vm_out) vm_out[e] = vm;
+    if (sig_out)
+#pragma unroll
+      for (int r = 0; r < 6; ++r) sig_out[6 * e + r] = s[r];
+  }
+  // Peaks of non-negative doubles order like their bit patterns: an integer max
+  // is the exact max, whatever the order.
+  if (peaks) {
+    if (vmax > 0.0) atomicMax(&peaks[0], (unsigned long long)__double_as_longlong(vmax));
+    if (tmax > 0.0) atomicMax(&peaks[1], (unsigned long long)__double_as_longlong(tmax));
+    if (printed) atomicAdd(&peaks[2], printed);
+  }
+}
+
 // Exact fixed-point accumulation: value = A * 2^-128, A a 192-bit unsigned
 // integer in three 64-bit limbs.  Integer addition is associative, so the total
 // is the same whatever the summation order -- the exact sum, not an
@@ -753,6 +832,32 @@ void launch_proj_volume(const Grid& g, const void* st, int ns, const uint8_t* ac
                                                             part);
   TG_LAUNCH_CHECK();
   k_sum_partials_multi<<<k, kThreads, 0, s>>>(part, kRedBlocks, out);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_element_stress(const Grid& g, const uint8_t* solid, const double* rho,
+                           const double* u, double E, double nu, double h, const double* bdir,
+                           double iso, double* vm_out, double* sig_out, uint64_t* peaks,
+                           cudaStream_t s) {
+  // The reference's D (hex_element.cpp:261-267) and gradient scale, on the host.
+  const double c = E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  StressConsts k{};
+  k.q = (2.0 / h) * 0.125;
+  k.d_diag = c * (1.0 - nu);
+  k.d_off = c * nu;
+  k.shear = c * (1.0 - 2.0 * nu) / 2.0;
+  // max_interlayer_tension (orient.cpp:234-263): n = build_dir / |build_dir|.
+  const double bl = std::sqrt(bdir[0] * bdir[0] + bdir[1] * bdir[1] + bdir[2] * bdir[2]);
+  const double n0 = bdir[0] / bl, n1 = bdir[1] / bl, n2 = bdir[2] / bl;
+  k.w[0] = n0 * n0;
+  k.w[1] = n1 * n1;
+  k.w[2] = n2 * n2;
+  k.w[3] = 2.0 * n0 * n1;
+  k.w[4] = 2.0 * n1 * n2;
+  k.w[5] = 2.0 * n2 * n0;
+  k.iso = iso;
+  k_element_stress<<<grid_blocks(g.nv), kThreads, 0, s>>>(
+      dev(g), solid, rho, u, k, vm_out, sig_out, reinterpret_cast<unsigned long long*>(peaks));
   TG_LAUNCH_CHECK();
 }
 

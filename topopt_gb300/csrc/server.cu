@@ -45,6 +45,7 @@ struct Request {
   std::vector<tg_nodal_load> loads;
   tg_simp_options options{};
   std::vector<tg_projection_stage> stages;  // options.projection, copied
+  std::vector<double> seed;                  // options.initial_design, copied
   int64_t estimate = 0;
   std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
   // Outcome.
@@ -119,6 +120,7 @@ struct tg_server {
     tg_grid g = r.grid;
     g.tags = r.has_tags ? r.tags.data() : nullptr;
     r.options.projection = r.stages.empty() ? nullptr : r.stages.data();
+    r.options.initial_design = r.seed.empty() ? nullptr : r.seed.data();
     const int rc =
         r.has_mask
             ? tg_simp_optimize_masked(&g, &r.params, r.bcs.data(), int32_t(r.bcs.size()),
@@ -182,6 +184,8 @@ int tg_server_submit(tg_server* s, const tg_grid* grid, const tg_simp_params* pa
   if (options->projection && options->projection_stages > 0)
     r->stages.assign(options->projection, options->projection + options->projection_stages);
   r->options.projection = nullptr;
+  if (options->initial_design) r->seed.assign(options->initial_design, options->initial_design + nv);
+  r->options.initial_design = nullptr;
   r->estimate = tg_job_estimate_bytes(grid, options);
   r->t_submit = std::chrono::steady_clock::now();
   std::lock_guard<std::mutex> lk(s->mu);

@@ -259,6 +259,14 @@ void launch_oc_candidates_projected(const double* x, const double* dcf, const do
 void launch_proj_volume(const Grid& g, const void* st, int ns, const uint8_t* act,
                         const double* hs, const double* cand, int k, double beta, double eta,
                         double* part, double* out, cudaStream_t s);
+// hex8_stress at every voxel centre where solid[e] and (rho null or rho[e] >
+// iso): von Mises and the 6 stresses (either output may be null; 0 elsewhere),
+// and into peaks[0..2] (zeroed by the caller) the bit patterns of the peak von
+// Mises and interlayer tension along bdir, and the printed-voxel count.
+void launch_element_stress(const Grid& g, const uint8_t* solid, const double* rho,
+                           const double* u, double E, double nu, double h, const double* bdir,
+                           double iso, double* vm_out, double* sig_out, uint64_t* peaks,
+                           cudaStream_t s);
 // FrozenSolid (1) -> 1, FrozenVoid (2) -> 0 on the physical density.
 void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t s);
 // Exact (fixed-point, order independent) sum of a non-negative field over the
