@@ -159,6 +159,8 @@ typedef struct {
   int64_t fine_matvecs, fine_matvecs_lowp;
   int32_t oc_volume_passes; /* passes over the fields that evaluated the bisection's volumes */
   double beta; /* projection sharpness of this iteration's stage; 0 when unprojected */
+  int32_t hier_built;          /* a multigrid hierarchy was built for this solve */
+  int32_t mg_cycles_attempted; /* V-cycles this solve ran */
 } tg_simp_iteration;
 
 typedef struct {
@@ -344,14 +346,16 @@ int tg_load_path_connected(const tg_grid* grid, const double* density, double is
  * the stress of every printed voxel with the SOLID modulus, the peak von Mises
  * and interlayer tension max(0, n.sigma.n) along the build direction,
  * compute_stress_margin (report.cpp:464-491), the load-path belt and the gate.
- * von_mises_out (nv) and stress_out (6 nv) may be NULL. */
+ * von_mises_out (nv), stress_out (6 nv) and displacement_out (3 (nx+1)(ny+1)(nz+1):
+ * the solve's displacement at the nodes of printed voxels, 0 elsewhere,
+ * analyze.cpp:385-394) may be NULL. */
 int tg_analyze_fixed_design(const tg_grid* grid, const tg_simp_params* params,
                             const double* density, const tg_dirichlet_bc* bcs, int32_t nbc,
                             const tg_nodal_load* loads, int32_t nloads,
                             const tg_strength_spec* strength, double cg_tolerance,
                             int32_t cg_max_iterations, const tg_solve_options* solve,
                             tg_fixed_design_analysis* out, double* von_mises_out,
-                            double* stress_out);
+                            double* stress_out, double* displacement_out);
 
 /* self_weight_loads (fea.hpp:215; assembly.cpp) and its masked form
  * (minimize_plastic.cpp:132-143, FrozenVoid voxels weigh nothing): gravity *
@@ -403,6 +407,90 @@ int tg_minimize_plastic(const tg_grid* grid, const tg_simp_params* params,
                         void* progress_ctx, const volatile int32_t* cancel,
                         tg_ladder_rung* rungs_out, tg_ladder_result* result, double* design_out,
                         double* phys_out);
+
+/* ---- on-disk formats: design.bin, fields.bin, iterations.csv ---- */
+
+/* The solved grid a container indexes to (VoxelGrid's dims, origin, spacing). */
+typedef struct {
+  int32_t nx, ny, nz;
+  double origin[3];
+  double spacing;
+} tg_grid_frame;
+
+/* One design.bin v1 variant block (design_store.hpp:44-78, StoredDesign
+ * :111-128); density has nx*ny*nz entries. */
+typedef struct {
+  double requested_volume_fraction, achieved_volume_fraction;
+  double margin_worst_case, margin_effective, max_von_mises;
+  int32_t accepted, iterations;
+  double applied_build_dir[3];
+  int32_t build_direction_auto_applied, export_baked;
+  uint64_t fingerprint; /* filled by the reader; the writer computes its own */
+  const double* density;
+} tg_design_variant;
+
+/* design_fingerprint (design_store.hpp:102; design_store.cpp): FNV-1a 64 over
+ * the density's little-endian bytes. */
+uint64_t tg_design_fingerprint(const double* density, int64_t count);
+
+/* write_design_file (design_store.hpp:154-181): the v1 container, written to
+ * "<path>.part" and renamed onto path.  Returns the blocks written, or -1
+ * (tg_last_error). */
+int32_t tg_write_design_file(const char* path, const tg_grid_frame* frame,
+                             const tg_design_variant* variants, int32_t count);
+
+/* read_design_file (design_store.hpp:183): checks the version, the header, each
+ * block's density count and fingerprint.  Fills frame and *count; the first
+ * min(count, cap) variants go to variants_out with their densities copied into
+ * density_out (cap * nx*ny*nz doubles) and pointed at there.  Either output
+ * may be NULL with cap 0 (a header probe).  Returns TG_OK or TG_EINVAL. */
+int tg_read_design_file(const char* path, tg_grid_frame* frame, int32_t* count,
+                        tg_design_variant* variants_out, int32_t cap, double* density_out);
+
+/* One fields.bin v1 block (fields.hpp:40-75): the per-voxel von Mises (nx*ny*nz)
+ * and per-node displacement (3 (nx+1)(ny+1)(nz+1)), narrowed to float32 on
+ * write; the stress tensor is absent in v1. */
+typedef struct {
+  double requested_volume_fraction, mass_grams;
+  int32_t support_volume_voxels;
+  const double* von_mises;
+  const double* displacement;
+} tg_fields_variant;
+
+/* write_fields_file (fields.hpp:96-118) over the blocks given (the caller picks
+ * the accepted variants).  Returns the blocks written, or -1. */
+int32_t tg_write_fields_file(const char* path, const tg_grid_frame* frame,
+                             const tg_fields_variant* variants, int32_t count);
+
+/* One iterations.csv row (observability.hpp:72-184; SimpIterationObservation,
+ * simp.hpp:920-1000, with IterationPhaseTimes :873-918). */
+typedef struct {
+  int32_t iteration;
+  double compliance, volume_fraction;
+  int32_t plateau, cg_iterations, cg_multigrid;
+  double beta;
+  int32_t hier_built, mg_cycles_attempted, infeasible, recycle_dim;
+  double active_fraction;
+  double total_ms, tail_prev_ms, filter_ms, project_ms, solve_ms, fea_ms, sens_ms, update_ms,
+      analysis_ms, observe_ms, residual_ms;
+  double solver_build_ms, mg_build_ms, mg_ms, cg_ms, geneo_setup_ms, geneo_apply_ms, recycle_ms;
+  int64_t fea_solves, matvecs;
+  int32_t geneo_dim, geneo_action, geneo_burn, geneo_threshold;
+  double rss_mb, peak_rss_mb, compressed_mb, available_mb;
+  int64_t major_faults, swapins;
+} tg_iteration_record;
+
+/* kIterationCsvHeader (observability.cpp:252-264), without the newline. */
+const char* tg_iteration_csv_header(void);
+/* The record of one library iteration: the solve and update phases from the
+ * row's timings, the rest at the reference's "absent" values (memory -1). */
+void tg_iteration_record_from(const tg_simp_iteration* row, int32_t infeasible,
+                              tg_iteration_record* out);
+/* IterationCsvWriter::append_at's row (observability.cpp:282-331), newline
+ * included, into buf; returns its length (or the length needed when cap is too
+ * small, buf then untouched). */
+int64_t tg_iteration_csv_row(int64_t rung, const tg_iteration_record* rec, int64_t wall_ms,
+                             char* buf, int64_t cap);
 
 /* ---- periodic homogenization of unit cells ---- */
 typedef struct {

@@ -17,7 +17,7 @@ fi
 mkdir -p "$OUT/obj"
 CORE="$REF/core"
 # The Eigen-free translation units of the path and the base files they pull in.
-SRCS="fea/hex_element fea/matfree fea/recycle simp/simp voxel/voxelize simp/observability orient/orient settings/report settings/gate_diagnosis_report
+SRCS="fea/hex_element fea/matfree fea/recycle simp/simp voxel/voxelize simp/observability orient/orient settings/report settings/gate_diagnosis_report io/design_store io/fields
       simp/mma_joint simp/semdot fea/lattice_material mesh/mesh fea/lattice"
 CXXFLAGS="-std=c++17 -O3 -fPIC -I$CORE/include -I$CORE/src"
 pids=()

@@ -16,7 +16,11 @@
 #include <array>
 
 #include "fea/fea_matfree.hpp"
+#include "topopt/design_store.hpp"
 #include "topopt/fea.hpp"
+#include "topopt/fields.hpp"
+#include "topopt/observability.hpp"
+#include "topopt/pipeline.hpp"
 #include "topopt/orient.hpp"
 #include "topopt/report.hpp"
 #include "topopt/simp.hpp"
@@ -600,4 +604,116 @@ int ref_ladder(int nx, int ny, int nz, double h, const uint8_t* tags, const uint
   });
 }
 
+
+// The reference's own writers of design.bin (design_store.cpp), fields.bin
+// (fields.cpp) and one iterations.csv row (IterationCsvWriter::append_at), fed
+// variants built from flat arrays.  Per design variant: d = {requested vf,
+// achieved vf, worst, effective, max vm, dir x, y, z}, i = {accepted,
+// iterations, auto applied, export baked}.
+int ref_write_design_file(const char* path, int nx, int ny, int nz, const double* origin,
+                          double spacing, int nvar, const double* d, const int* ii,
+                          const double* dens) {
+  return guarded([&] {
+    VoxelGrid g = make_grid(nx, ny, nz, spacing, nullptr);
+    g.origin = Vec3{origin[0], origin[1], origin[2]};
+    const std::size_t nv = g.voxel_count();
+    std::vector<MinimizePlasticVariant> vs(static_cast<std::size_t>(nvar));
+    std::vector<const MinimizePlasticVariant*> ptrs;
+    for (int k = 0; k < nvar; ++k) {
+      MinimizePlasticVariant& v = vs[static_cast<std::size_t>(k)];
+      const double* dk = d + 8 * k;
+      const int* ik = ii + 4 * k;
+      v.requested_volume_fraction = dk[0];
+      v.optimization.volume_fraction = dk[1];
+      v.report.margin.worst_case = dk[2];
+      v.report.margin_effective = dk[3];
+      v.report.max_stress_mpa = dk[4];
+      v.applied_build_dir = Vec3{dk[5], dk[6], dk[7]};
+      v.accepted = ik[0] != 0;
+      v.optimization.iterations = ik[1];
+      v.build_direction_auto_applied = ik[2] != 0;
+      v.export_baked = ik[3] != 0;
+      v.optimization.physical_density.assign(dens + std::size_t(k) * nv,
+                                             dens + std::size_t(k + 1) * nv);
+      ptrs.push_back(&v);
+    }
+    write_design_file(path, ptrs, g);
+  });
+}
+
+uint64_t ref_design_fingerprint(const double* d, long long n) {
+  return design_fingerprint(std::vector<double>(d, d + n));
+}
+
+// fields.bin: per variant d = {requested vf, mass}, i = {support voxels}.
+int ref_write_fields_file(const char* path, int nx, int ny, int nz, const double* origin,
+                          double spacing, int nvar, const double* d, const int* ii,
+                          const double* vm, const double* disp) {
+  return guarded([&] {
+    VoxelGrid g = make_grid(nx, ny, nz, spacing, nullptr);
+    g.origin = Vec3{origin[0], origin[1], origin[2]};
+    const std::size_t nv = g.voxel_count();
+    const std::size_t nd = 3 * std::size_t(fea_node_count(g));
+    std::vector<MinimizePlasticVariant> vs(static_cast<std::size_t>(nvar));
+    std::vector<const MinimizePlasticVariant*> ptrs;
+    for (int k = 0; k < nvar; ++k) {
+      MinimizePlasticVariant& v = vs[static_cast<std::size_t>(k)];
+      v.accepted = true;
+      v.requested_volume_fraction = d[2 * k];
+      v.mass_grams = d[2 * k + 1];
+      v.support_volume_voxels = ii[k];
+      v.von_mises_field.assign(vm + std::size_t(k) * nv, vm + std::size_t(k + 1) * nv);
+      v.displacement_field.assign(disp + std::size_t(k) * nd, disp + std::size_t(k + 1) * nd);
+      ptrs.push_back(&v);
+    }
+    write_fields_file(path, ptrs, g);
+  });
+}
+
+// One iterations.csv (header + one row) from an observation given as flat
+// arrays: od = {compliance, volume_fraction, beta, active_fraction, 18 phase
+// times in schema order, rss, peak_rss, compressed, available}; oi =
+// {iteration, plateau, cg_iters, cg_multigrid, hier_built, mg_cycles,
+// infeasible, recycle_dim, geneo_dim, geneo_action, geneo_burn,
+// geneo_threshold}; ol = {fea_solves, matvecs, major_faults, swapins}.
+int ref_iteration_csv(const char* path, long long rung, const double* od, const int* oi,
+                      const long long* ol, long long wall_ms) {
+  return guarded([&] {
+    SimpIterationObservation o;
+    o.compliance = od[0];
+    o.volume_fraction = od[1];
+    o.beta = od[2];
+    o.active_fraction = od[3];
+    double* ph[18] = {&o.phases.total_ms, &o.phases.tail_prev_ms, &o.phases.filter_ms,
+                      &o.phases.project_ms, &o.phases.solve_ms, &o.phases.fea_ms,
+                      &o.phases.sens_ms, &o.phases.update_ms, &o.phases.analysis_ms,
+                      &o.phases.observe_ms, &o.phases.residual_ms, &o.phases.solver_build_ms,
+                      &o.phases.solver_mg_build_ms, &o.phases.solver_mg_ms,
+                      &o.phases.solver_cg_ms, &o.phases.solver_geneo_setup_ms,
+                      &o.phases.solver_geneo_apply_ms, &o.phases.solver_recycle_ms};
+    for (int q = 0; q < 18; ++q) *ph[q] = od[4 + q];
+    o.phases.rss_mb = od[22];
+    o.phases.peak_rss_mb = od[23];
+    o.phases.compressed_mb = od[24];
+    o.phases.available_mb = od[25];
+    o.iteration = oi[0];
+    o.plateau = oi[1] != 0;
+    o.cg_iterations = oi[2];
+    o.cg_used_multigrid = oi[3] != 0;
+    o.cg_hier_built = oi[4] != 0;
+    o.cg_mg_cycles_attempted = oi[5];
+    o.infeasible = oi[6] != 0;
+    o.cg_recycle_dim = oi[7];
+    o.cg_geneo_dim = oi[8];
+    o.cg_geneo_action = oi[9];
+    o.cg_geneo_burn = oi[10];
+    o.cg_geneo_threshold = oi[11];
+    o.phases.fea_solves = ol[0];
+    o.phases.matvecs = ol[1];
+    o.phases.major_faults = ol[2];
+    o.phases.swapins = ol[3];
+    IterationCsvWriter w(path);
+    w.append_at(static_cast<std::size_t>(rung), o, wall_ms);
+  });
+}
 }  // extern "C"

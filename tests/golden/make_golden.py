@@ -242,6 +242,9 @@ def main():
     out["lp_connected"] = np.array([R.load_path_connected(pbl, dfix),
                                     R.load_path_connected(pbl, sev.ravel())])
 
+    # On-disk formats, written by the reference's own writers.
+    out.update(_formats(R, rng))
+
     old = os.path.join(HERE, "golden.npz")
     if os.path.exists(old):  # regenerating must not move any earlier vector
         with np.load(old) as z:
@@ -250,6 +253,53 @@ def main():
                     raise SystemExit(f"golden array {k} changed on regeneration")
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
+
+
+def _formats(R, rng):
+    import ctypes as C
+    import tempfile
+    L = R.lib
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+    lp = np.ctypeslib.ndpointer(np.int64, flags="C")
+    L.ref_write_design_file.argtypes = [C.c_char_p] + [C.c_int] * 3 + [dp, C.c_double, C.c_int,
+                                                                      dp, ip, dp]
+    L.ref_write_fields_file.argtypes = [C.c_char_p] + [C.c_int] * 3 + [dp, C.c_double, C.c_int,
+                                                                      dp, ip, dp, dp]
+    L.ref_iteration_csv.argtypes = [C.c_char_p, C.c_longlong, dp, ip, lp, C.c_longlong]
+    L.ref_design_fingerprint.argtypes = [dp, C.c_longlong]
+    L.ref_design_fingerprint.restype = C.c_uint64
+    nx, ny, nz, h = 5, 4, 3, 0.8
+    origin = np.array([1.5, -2.0, 0.25])
+    nv, nd = nx * ny * nz, 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    dd = np.array([[0.6, 0.6012, 2.25, 2.0, 13.75, 0.0, 0.6, 0.8],
+                   [0.45, 0.4497, 1.1, 0.9, 27.5, 0.0, 0.0, 1.0]])
+    di = np.array([[1, 40, 0, 1], [0, 37, 1, 0]], np.int32)
+    dens = rng.random(2 * nv)
+    fd = np.array([0.6, 12.5, 0.45, 9.25])
+    fi = np.array([17, 3], np.int32)
+    vm = rng.random(2 * nv) * 40.0
+    disp = rng.standard_normal(2 * nd) * 1e-3
+    od = np.concatenate([[1234.5678901234, 0.3012345, 4.0, 0.875], rng.random(18) * 100.0,
+                         [512.25, 600.5, -1.0, 8000.125]])
+    oi = np.array([7, 0, 42, 1, 1, 9, 0, 0, 0, 0, 0, 0], np.int32)
+    ol = np.array([1, 130, -1, 3], np.int64)
+    with tempfile.TemporaryDirectory() as tmp:
+        pd, pf, pc = (os.path.join(tmp, n) for n in ("design.bin", "fields.bin", "it.csv"))
+        assert L.ref_write_design_file(pd.encode(), nx, ny, nz, origin, h, 2, dd.ravel(),
+                                       di.ravel(), dens) == 0
+        assert L.ref_write_fields_file(pf.encode(), nx, ny, nz, origin, h, 2, fd, fi, vm,
+                                       disp) == 0
+        assert L.ref_iteration_csv(pc.encode(), 2, od, oi, ol, 1733000000123) == 0
+        bd, bf, bc = (np.frombuffer(open(q, "rb").read(), np.uint8) for q in (pd, pf, pc))
+    return dict(fmt_dims=np.array([nx, ny, nz]), fmt_spacing=np.array(h), fmt_origin=origin,
+                fmt_design_d=dd, fmt_design_i=di, fmt_design_dens=dens,
+                fmt_design_bytes=bd, fmt_design_fp=np.array(
+                    [L.ref_design_fingerprint(dens[:nv].copy(), nv),
+                     L.ref_design_fingerprint(dens[nv:].copy(), nv)], np.uint64),
+                fmt_fields_d=fd, fmt_fields_i=fi, fmt_fields_vm=vm, fmt_fields_disp=disp,
+                fmt_fields_bytes=bf, fmt_csv_od=od, fmt_csv_oi=oi, fmt_csv_ol=ol,
+                fmt_csv_bytes=bc)
 
 
 if __name__ == "__main__":

@@ -155,3 +155,42 @@ def test_ladder_matches_reference(tg, golden, tag, margin_stop, prec):
     rec = L["recommended"]
     assert rec >= 0
     assert rel(L["physical_density"], golden[f"lad{tag}_phys"]) < 1e-4
+
+
+def test_ladder_outputs_round_trip(tg, golden, tmp_path):
+    """The ladder's recommended design through design.bin and fields.bin: the
+    stored field re-certifies to the recorded margin bit for bit (the
+    reproduction check of the reference's re-lattice path), and the fields
+    container carries the analysis's von Mises and printed-node displacement."""
+    pb = _ladder_problem(tg, golden)
+    strength = tg.StrengthSpec(yield_strength=30.0, margin_stop=25.0)
+    L = tg.minimize_plastic(
+        pb, tg.SimpParams(), tg.SimpOptions(filter_radius=1.5, max_iterations=25,
+                                            cg_tolerance=1e-9), golden["lad_ladder"], strength)
+    rec = L["rungs"][L["recommended"]]
+    a = tg.analyze_fixed_design(pb, tg.SimpParams(), L["physical_density"], strength,
+                                cg_tolerance=1e-9, fields=True)
+    assert a["margin_worst_case"] == rec["analysis"]["margin_worst_case"]
+    dims = (pb.nx, pb.ny, pb.nz)
+    tg.write_design_file(tmp_path / "design.bin", dims, [dict(
+        requested_volume_fraction=rec["volume_fraction"],
+        achieved_volume_fraction=rec["optimization"]["volume_fraction"],
+        margin_worst_case=rec["analysis"]["margin_worst_case"],
+        margin_effective=rec["analysis"]["margin_effective"],
+        max_von_mises=rec["analysis"]["max_von_mises"], accepted=1,
+        iterations=rec["optimization"]["iterations"], density=L["physical_density"])])
+    back = tg.read_design_file(tmp_path / "design.bin")["variants"][0]
+    again = tg.analyze_fixed_design(pb, tg.SimpParams(), back["density"], strength,
+                                    cg_tolerance=1e-9)
+    assert again["margin_worst_case"] == back["margin_worst_case"]
+    tg.write_fields_file(tmp_path / "fields.bin", dims, [dict(
+        requested_volume_fraction=rec["volume_fraction"], von_mises=a["von_mises"],
+        displacement=a["displacement"])])
+    raw = (tmp_path / "fields.bin").read_bytes()
+    nv, nd = pb.nv, pb.ndof
+    hdr = 1 + 3 + 12 + 24 + 8 + 8 + 8
+    vm32 = np.frombuffer(raw, np.float32, nv, hdr + 8 + 8 + 8 + 24)
+    assert np.array_equal(vm32, a["von_mises"].astype(np.float32))
+    d32 = np.frombuffer(raw, np.float32, nd, hdr + 8 + 8 + 8 + 24 + 4 * nv)
+    assert np.array_equal(d32, a["displacement"].astype(np.float32))
+    assert np.any(a["displacement"] != 0.0) and np.any(a["displacement"] == 0.0)

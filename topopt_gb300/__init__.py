@@ -40,6 +40,13 @@ from ._capi import (  # noqa: F401
     oc_update,
     oc_update_masked,
     oc_update_projected,
+    design_fingerprint,
+    write_design_file,
+    read_design_file,
+    write_fields_file,
+    iteration_csv_header,
+    iteration_csv_row,
+    write_iterations_csv,
     StrengthSpec,
     element_stress,
     load_path_connected,

@@ -11,6 +11,7 @@ reference's exception classes: ``ValueError`` for std::invalid_argument,
 from __future__ import annotations
 
 import ctypes as C
+import time
 import os
 from dataclasses import dataclass, field
 
@@ -96,7 +97,8 @@ class _Iter(C.Structure):
                 ("t_update_ms", C.c_double), ("t_total_ms", C.c_double),
                 ("t_device_ms", C.c_double), ("fine_matvecs", C.c_int64),
                 ("fine_matvecs_lowp", C.c_int64), ("oc_volume_passes", C.c_int32),
-                ("beta", C.c_double)]
+                ("beta", C.c_double), ("hier_built", C.c_int32),
+                ("mg_cycles_attempted", C.c_int32)]
 
 
 class _Result(C.Structure):
@@ -151,10 +153,17 @@ def lib():
         "tg_heaviside_continuation_schedule": ([vp, i32], C.c_int32),
         "tg_oc_update_projected": ([vp, dbl, vp, vp, vp, dbl, dbl, dbl, dbl, dbl, vp], C.c_int),
         "tg_job_set_stage": ([vp, i32], C.c_int),
+        "tg_design_fingerprint": ([vp, C.c_int64], C.c_uint64),
+        "tg_write_design_file": ([C.c_char_p, vp, vp, i32], C.c_int32),
+        "tg_read_design_file": ([C.c_char_p, vp, vp, vp, i32, vp], C.c_int),
+        "tg_write_fields_file": ([C.c_char_p, vp, vp, i32], C.c_int32),
+        "tg_iteration_csv_header": ([], C.c_char_p),
+        "tg_iteration_record_from": ([vp, i32, vp], None),
+        "tg_iteration_csv_row": ([C.c_int64, vp, C.c_int64, vp, C.c_int64], C.c_int64),
         "tg_element_stress": ([vp, dbl, dbl, vp, vp, dbl, vp, vp], C.c_int),
         "tg_load_path_connected": ([vp, vp, dbl, vp], C.c_int),
         "tg_analyze_fixed_design": ([vp, vp, vp, vp, i32, vp, i32, vp, dbl, i32, vp, vp, vp,
-                                     vp], C.c_int),
+                                     vp, vp], C.c_int),
         "tg_self_weight_loads": ([vp, vp, dbl, dbl, vp, vp, C.c_int64], C.c_int64),
         "tg_minimize_plastic": ([vp, vp, vp, i32, vp, i32, vp, vp, vp, _PROGRESS, vp, vp, vp,
                                  vp, vp, vp], C.c_int),
@@ -605,14 +614,16 @@ def analyze_fixed_design(pb: Problem, params: SimpParams, density, strength: Str
     out = _Analysis()
     vm = np.zeros(pb.nv) if fields else None
     sig = np.zeros(6 * pb.nv) if fields else None
+    disp = np.zeros(pb.ndof) if fields else None
     g, b, nb, l, nl = pb._args()
     _check(lib().tg_analyze_fixed_design(g, C.byref(prm), _p(d), b, nb, l, nl, C.byref(st),
                                          cg_tolerance, cg_max_iterations, C.byref(so),
-                                         C.byref(out), _p(vm), _p(sig)))
+                                         C.byref(out), _p(vm), _p(sig), _p(disp)))
     res = _struct_dict(out)
     if fields:
         res["von_mises"] = vm
         res["stress"] = sig.reshape(pb.nv, 6)
+        res["displacement"] = disp
     return res
 
 
@@ -657,6 +668,164 @@ def minimize_plastic(pb: Problem, params: SimpParams, options: SimpOptions, ladd
     if res.recommended >= 0:
         out["design"], out["physical_density"] = design, phys
     return out
+
+
+# ------------------------------------------- design.bin / fields.bin / csv
+class _Frame(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("origin", C.c_double * 3), ("spacing", C.c_double)]
+
+
+class _DesignVariant(C.Structure):
+    _fields_ = [("requested_volume_fraction", C.c_double),
+                ("achieved_volume_fraction", C.c_double), ("margin_worst_case", C.c_double),
+                ("margin_effective", C.c_double), ("max_von_mises", C.c_double),
+                ("accepted", C.c_int32), ("iterations", C.c_int32),
+                ("applied_build_dir", C.c_double * 3),
+                ("build_direction_auto_applied", C.c_int32), ("export_baked", C.c_int32),
+                ("fingerprint", C.c_uint64), ("density", C.c_void_p)]
+
+
+class _FieldsVariant(C.Structure):
+    _fields_ = [("requested_volume_fraction", C.c_double), ("mass_grams", C.c_double),
+                ("support_volume_voxels", C.c_int32), ("von_mises", C.c_void_p),
+                ("displacement", C.c_void_p)]
+
+
+class _IterRecord(C.Structure):
+    _fields_ = ([("iteration", C.c_int32), ("compliance", C.c_double),
+                 ("volume_fraction", C.c_double), ("plateau", C.c_int32),
+                 ("cg_iterations", C.c_int32), ("cg_multigrid", C.c_int32),
+                 ("beta", C.c_double), ("hier_built", C.c_int32),
+                 ("mg_cycles_attempted", C.c_int32), ("infeasible", C.c_int32),
+                 ("recycle_dim", C.c_int32), ("active_fraction", C.c_double)] +
+                [(n, C.c_double) for n in (
+                    "total_ms", "tail_prev_ms", "filter_ms", "project_ms", "solve_ms", "fea_ms",
+                    "sens_ms", "update_ms", "analysis_ms", "observe_ms", "residual_ms",
+                    "solver_build_ms", "mg_build_ms", "mg_ms", "cg_ms", "geneo_setup_ms",
+                    "geneo_apply_ms", "recycle_ms")] +
+                [("fea_solves", C.c_int64), ("matvecs", C.c_int64), ("geneo_dim", C.c_int32),
+                 ("geneo_action", C.c_int32), ("geneo_burn", C.c_int32),
+                 ("geneo_threshold", C.c_int32), ("rss_mb", C.c_double),
+                 ("peak_rss_mb", C.c_double), ("compressed_mb", C.c_double),
+                 ("available_mb", C.c_double), ("major_faults", C.c_int64),
+                 ("swapins", C.c_int64)])
+
+
+def _frame(dims, spacing=1.0, origin=(0.0, 0.0, 0.0)):
+    nx, ny, nz = (int(v) for v in dims)
+    return _Frame(nx, ny, nz, (C.c_double * 3)(*[float(v) for v in origin]), float(spacing))
+
+
+def design_fingerprint(density) -> int:
+    """design_fingerprint (design_store.hpp:102): FNV-1a 64 over the bytes."""
+    d = _f64(density)
+    return int(lib().tg_design_fingerprint(_p(d), d.size))
+
+
+def write_design_file(path, dims, variants, spacing=1.0, origin=(0.0, 0.0, 0.0)) -> int:
+    """design.bin v1 (design_store.hpp:40-90).  ``variants``: dicts with
+    requested_volume_fraction, achieved_volume_fraction, margin_worst_case,
+    margin_effective, max_von_mises, accepted, iterations, density (and
+    optionally applied_build_dir, build_direction_auto_applied, export_baked)."""
+    fr = _frame(dims, spacing, origin)
+    nv = fr.nx * fr.ny * fr.nz
+    arr = (_DesignVariant * max(len(variants), 1))()
+    keep = []
+    for i, v in enumerate(variants):
+        d = _f64(v["density"], nv)
+        keep.append(d)
+        arr[i] = _DesignVariant(
+            v["requested_volume_fraction"], v.get("achieved_volume_fraction", 0.0),
+            v.get("margin_worst_case", 0.0), v.get("margin_effective", 0.0),
+            v.get("max_von_mises", 0.0), int(bool(v.get("accepted", False))),
+            int(v.get("iterations", 0)),
+            (C.c_double * 3)(*v.get("applied_build_dir", (0.0, 0.0, 1.0))),
+            int(bool(v.get("build_direction_auto_applied", False))),
+            int(bool(v.get("export_baked", False))), 0, d.ctypes.data_as(C.c_void_p))
+    n = lib().tg_write_design_file(str(path).encode(), C.byref(fr), C.cast(arr, C.c_void_p),
+                                   len(variants))
+    if n < 0:
+        raise ValueError(lib().tg_last_error().decode())
+    return int(n)
+
+
+def read_design_file(path):
+    """read_design_file (design_store.hpp:183): frame and variants (version,
+    counts and fingerprints checked)."""
+    fr, cnt = _Frame(), C.c_int32(0)
+    _check(lib().tg_read_design_file(str(path).encode(), C.byref(fr), C.byref(cnt), None, 0,
+                                     None))
+    nv = fr.nx * fr.ny * fr.nz
+    arr = (_DesignVariant * max(cnt.value, 1))()
+    dens = np.zeros(max(cnt.value, 1) * nv)
+    _check(lib().tg_read_design_file(str(path).encode(), C.byref(fr), C.byref(cnt),
+                                     C.cast(arr, C.c_void_p), cnt.value, _p(dens)))
+    out = []
+    for i in range(cnt.value):
+        v = {f[0]: getattr(arr[i], f[0]) for f in _DesignVariant._fields_ if f[0] != "density"}
+        v["applied_build_dir"] = tuple(arr[i].applied_build_dir)
+        v["density"] = dens[i * nv:(i + 1) * nv].copy()
+        out.append(v)
+    return dict(dims=(fr.nx, fr.ny, fr.nz), origin=tuple(fr.origin), spacing=fr.spacing,
+                variants=out)
+
+
+def write_fields_file(path, dims, variants, spacing=1.0, origin=(0.0, 0.0, 0.0)) -> int:
+    """fields.bin v1 (fields.hpp:33-75): dicts with requested_volume_fraction,
+    mass_grams, support_volume_voxels, von_mises (nv), displacement (ndof)."""
+    fr = _frame(dims, spacing, origin)
+    nv = fr.nx * fr.ny * fr.nz
+    ndof = 3 * (fr.nx + 1) * (fr.ny + 1) * (fr.nz + 1)
+    arr = (_FieldsVariant * max(len(variants), 1))()
+    keep = []
+    for i, v in enumerate(variants):
+        vm, dp = _f64(v["von_mises"], nv), _f64(v["displacement"], ndof)
+        keep += [vm, dp]
+        arr[i] = _FieldsVariant(v["requested_volume_fraction"], v.get("mass_grams", 0.0),
+                                int(v.get("support_volume_voxels", 0)),
+                                vm.ctypes.data_as(C.c_void_p), dp.ctypes.data_as(C.c_void_p))
+    n = lib().tg_write_fields_file(str(path).encode(), C.byref(fr), C.cast(arr, C.c_void_p),
+                                   len(variants))
+    if n < 0:
+        raise ValueError(lib().tg_last_error().decode())
+    return int(n)
+
+
+def iteration_csv_header() -> str:
+    return lib().tg_iteration_csv_header().decode()
+
+
+def iteration_csv_row(rung, record, wall_ms=0) -> str:
+    """One iterations.csv row: ``record`` is a dict of tg_iteration_record fields
+    (missing fields at the schema's absent values) or a history row of
+    simp_optimize (converted by tg_iteration_record_from)."""
+    rec = _IterRecord()
+    if "t_total_ms" in record:
+        row = _Iter(**{f[0]: record[f[0]] for f in _Iter._fields_ if f[0] in record})
+        lib().tg_iteration_record_from(C.byref(row), int(record.get("infeasible", 0)),
+                                       C.byref(rec))
+    else:
+        rec.active_fraction = 1.0
+        for k in ("rss_mb", "peak_rss_mb", "compressed_mb", "available_mb"):
+            setattr(rec, k, -1.0)
+        rec.major_faults = rec.swapins = -1
+        for k, v in record.items():
+            setattr(rec, k, v)
+    buf = C.create_string_buffer(1024)
+    n = lib().tg_iteration_csv_row(int(rung), C.byref(rec), int(wall_ms), buf, 1024)
+    if n < 0:
+        raise ValueError("iteration_csv_row: formatting failed")
+    return buf.value.decode()
+
+
+def write_iterations_csv(path, rows, wall_ms=None):
+    """iterations.csv: the header and one row per (rung, history row)."""
+    with open(path, "w") as f:
+        f.write(iteration_csv_header() + "\n")
+        for rung, row in rows:
+            f.write(iteration_csv_row(rung, row, int(time.time() * 1000)
+                                      if wall_ms is None else wall_ms))
 
 
 class _HomogInfo(C.Structure):

@@ -835,6 +835,8 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   r.fine_matvecs = st.matvecs;
   r.fine_matvecs_lowp = st.matvecs_lowp;
   r.beta = beta;
+  r.hier_built = st.hier_built ? 1 : 0;
+  r.mg_cycles_attempted = st.mg_cycles;
   j->hist_c.push_back(c);
   j->hist_cg.push_back(st.iterations);
   if (row) *row = r;
@@ -938,7 +940,7 @@ void fill_margins(tg_fixed_design_analysis* a, const tg_strength_spec& sp) {
 // the gate.  rho_host is the same density on the host (for the belt).
 void analyze_on_job(tg_job* aj, const double* rho_host, const uint8_t* tags,
                     const tg_strength_spec& sp, tg_fixed_design_analysis* out,
-                    double* vm_out, double* stress_out) {
+                    double* vm_out, double* stress_out, double* disp_out = nullptr) {
   AllocScope scope(aj->s);
   std::memset(out, 0, sizeof *out);
   const Grid& g = aj->fp.g;
@@ -976,6 +978,25 @@ void analyze_on_job(tg_job* aj, const double* rho_host, const uint8_t* tags,
   fill_margins(out, sp);
   out->load_path_ok = load_path_host(g, tags, rho_host, sp.printed_iso) ? 1 : 0;
   out->accepted = out->load_path_ok && out->margin_effective >= sp.margin_stop;
+  if (disp_out) {
+    // The displacement on printed nodes exactly as solved, 0 on nodes attached
+    // only to non-printed voxels (analyze.cpp:385-394).
+    TG_CUDA(cudaMemcpyAsync(disp_out, aj->u.p, aj->u.bytes(), cudaMemcpyDeviceToHost, aj->s));
+    TG_CUDA(cudaStreamSynchronize(aj->s));
+    std::vector<uint8_t> printed(size_t(g.nnodes), 0);
+    for (int k = 0; k < g.nz; ++k)
+      for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i) {
+          const int64_t e = (int64_t(k) * g.ny + j) * g.nx + i;
+          if ((tags && tags[e] == 0) || !(rho_host[e] > sp.printed_iso)) continue;
+          for (int a = 0; a < 8; ++a) {
+            const int ox = a & 1, oy = (a >> 1) & 1, oz = a >> 2;
+            printed[size_t((int64_t(k + oz) * g.nny + (j + oy)) * g.nnx + (i + ox))] = 1;
+          }
+        }
+    for (int64_t n = 0; n < g.nnodes; ++n)
+      if (!printed[size_t(n)]) disp_out[3 * n] = disp_out[3 * n + 1] = disp_out[3 * n + 2] = 0.0;
+  }
 }
 
 // A job that only solves: the analysis grid, its BCs and loads, the solve form
@@ -1655,14 +1676,15 @@ int tg_analyze_fixed_design(const tg_grid* grid, const tg_simp_params* params,
                             const tg_strength_spec* strength, double cg_tolerance,
                             int32_t cg_max_iterations, const tg_solve_options* solve,
                             tg_fixed_design_analysis* out, double* von_mises_out,
-                            double* stress_out) {
+                            double* stress_out, double* displacement_out) {
   return guarded([&] {
     validate_grid(grid);
     if (!density || !out) raise(TG_EINVAL, "density and out must be non-null");
     validate_strength(strength);
     auto aj = solve_only_job(grid, params, bcs, nbc, loads, nloads, cg_tolerance,
                              cg_max_iterations, solve);
-    analyze_on_job(aj.get(), density, grid->tags, *strength, out, von_mises_out, stress_out);
+    analyze_on_job(aj.get(), density, grid->tags, *strength, out, von_mises_out, stress_out,
+                   displacement_out);
   });
 }
 
