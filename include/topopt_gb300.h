@@ -146,7 +146,18 @@ typedef struct {
    * design set is rescaled to volume_fraction, clamped to [density_min, 1] and
    * filtered once (warm_start_design, simp.cpp:324-344). */
   const double* initial_design;
+  /* The design updater (SimpOptions::updater, simp.hpp:1119): TG_UPDATER_OC (0,
+   * the default) or TG_UPDATER_MMA (Svanberg's MMA, simp.cpp:1420-1489,
+   * mma_joint.cpp; no projection plan).  MMA ends a run on the objective plateau
+   * (mma_objective_plateau, simp.cpp:1081-1134) when mma_plateau_window > 0
+   * (the reference's defaults are 10, 1e-3, 0.05, 3), else on change_tol. */
+  int32_t updater;
+  int32_t mma_plateau_window;
+  double mma_plateau_tol, mma_plateau_min_drop;
+  int32_t mma_plateau_flat_windows;
 } tg_simp_options;
+
+enum { TG_UPDATER_OC = 0, TG_UPDATER_MMA = 1 };
 
 /* One row of the per-iteration record (SimpIteration + the observation fields
  * of simp.hpp:913-960 that the iterations.csv schema carries). */

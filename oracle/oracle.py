@@ -383,6 +383,53 @@ class OracleLib:
                     max_von_mises=od[1], max_interlayer=od[2], margin_in_plane=od[3],
                     margin_interlayer=od[4], margin_worst=od[5], margin_effective=od[6]), vm
 
+    def simp_optimize_mma(self, pb: Problem, mask=None, E0=1.0, nu=0.3, penal=3.0,
+                          rho_min=1e-3, volfrac=0.3, radius=1.5, move=0.2, max_it=50,
+                          change_tol=0.01, cg_tol=1e-8, cg_max_it=0, plateau_window=10,
+                          plateau_tol=1e-3, plateau_min_drop=0.05, plateau_flat_windows=3):
+        """simp_optimize with the MMA updater (plain, or masked with mask)."""
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        hc, hch, hvf = np.zeros(max_it), np.zeros(max_it), np.zeros(max_it)
+        design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+        if self.kind == "reference":
+            sc, ints = np.zeros(3), np.zeros(4, np.int32)
+            f = self._sig("simp_optimize_mma",
+                          [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p] +
+                          [C.c_double] * 4 + [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp,
+                                              C.c_double, C.c_double, C.c_double, C.c_int,
+                                              C.c_double, C.c_double, C.c_int, C.c_int,
+                                              C.c_double, C.c_double, C.c_int, _dp, _dp, _dp,
+                                              _dp, _dp, _dp, _ip])
+            self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(m), E0, nu,
+                          penal, rho_min, *pb.bc_args(), volfrac, radius, move, max_it,
+                          change_tol, cg_tol, cg_max_it, plateau_window, plateau_tol,
+                          plateau_min_drop, plateau_flat_windows, hc, hch, hvf, design, phys,
+                          sc, ints))
+            n = int(ints[0])
+            return dict(compliance=sc[0], volume_fraction=sc[1], initial_compliance=sc[2],
+                        iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
+                        infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
+                        hist_vf=hvf[:n], design=design, phys=phys)
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, 0,
+                             None, None, None, 0.5, None, 1, plateau_window, plateau_tol,
+                             plateau_min_drop, plateau_flat_windows)
+        res = _OrSimpResult()
+        hcg = np.zeros(max_it, np.int32)
+        if m is None:
+            self._check(self.lib.or_simp_optimize(
+                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                *pb.bc_args(), C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        else:
+            self._check(self.lib.or_simp_optimize_masked(
+                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), m, E0, nu, penal, rho_min,
+                *pb.bc_args(), C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        n = res.iterations
+        return dict(compliance=res.compliance, volume_fraction=res.volume_fraction,
+                    initial_compliance=res.initial_compliance, iterations=n,
+                    converged=bool(res.converged), non_convergent=bool(res.non_convergent),
+                    infeasible=bool(res.infeasible), hist_c=hc[:n], hist_change=hch[:n],
+                    hist_vf=hvf[:n], hist_cg=hcg[:n], design=design, phys=phys)
+
     def ladder(self, pb: Problem, mask, ladder, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3,
                radius=1.5, move=0.2, max_it=30, change_tol=0.01, cg_tol=1e-8, cg_max_it=0,
                inherit=True, yield_strength=50.0, z_knockdown=1.0, build_dir=(0.0, 0.0, 1.0),
@@ -616,7 +663,9 @@ class _OrSimpOptions(C.Structure):
                 ("max_iterations", C.c_int), ("cg_max_iterations", C.c_int),
                 ("nstages", C.c_int), ("stage_beta", C.c_void_p), ("stage_move", C.c_void_p),
                 ("stage_iterations", C.c_void_p), ("eta", C.c_double),
-                ("initial_design", C.c_void_p)]
+                ("initial_design", C.c_void_p), ("updater", C.c_int),
+                ("mma_plateau_window", C.c_int), ("mma_plateau_tol", C.c_double),
+                ("mma_plateau_min_drop", C.c_double), ("mma_plateau_flat_windows", C.c_int)]
 
 
 class _OrAnalysis(C.Structure):

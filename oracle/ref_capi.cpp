@@ -716,4 +716,59 @@ int ref_iteration_csv(const char* path, long long rung, const double* od, const 
     w.append_at(static_cast<std::size_t>(rung), o, wall_ms);
   });
 }
+
+// simp_optimize with the MMA updater (SimpUpdater::MMA, simp.cpp:2305-2311 and
+// the masked :3350-3357), plain when mask is NULL, MultigridCG_Matfree, with the
+// plateau options mma_plateau_{window, tol, min_drop, flat_windows}.
+int ref_simp_optimize_mma(int nx, int ny, int nz, double h, const uint8_t* tags,
+                          const uint8_t* mask, double E0, double nu, double penal,
+                          double rho_min, int nbc, const int* bc_node, const int* bc_comp,
+                          const double* bc_val, int nload, const int* ld_node,
+                          const int* ld_comp, const double* ld_val, double volfrac,
+                          double radius, double move, int max_it, double change_tol,
+                          double cg_tol, int cg_max_it, int pw, double ptol, double pdrop,
+                          int pflat, double* hist_c, double* hist_change, double* hist_vf,
+                          double* design, double* phys, double* out_scalars, int* out_ints) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, h, tags);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    SimpOptions o;
+    o.volume_fraction = volfrac;
+    o.filter_radius = radius;
+    o.move = move;
+    o.max_iterations = max_it;
+    o.change_tol = change_tol;
+    o.cg_tolerance = cg_tol;
+    o.cg_max_iterations = cg_max_it;
+    o.solver = SolverKind::MultigridCG_Matfree;
+    o.updater = SimpUpdater::MMA;
+    o.mma_plateau_window = pw;
+    o.mma_plateau_tol = ptol;
+    o.mma_plateau_min_drop = pdrop;
+    o.mma_plateau_flat_windows = pflat;
+    const auto bcs = make_bcs(nbc, bc_node, bc_comp, bc_val);
+    const auto loads = make_loads(nload, ld_node, ld_comp, ld_val);
+    const SimpOptimizeResult r =
+        mask ? simp_optimize(g, p, bcs, loads, o, make_mask(g.voxel_count(), mask))
+             : simp_optimize(g, p, bcs, loads, o);
+    for (std::size_t i = 0; i < r.history.size(); ++i) {
+      hist_c[i] = r.history[i].compliance;
+      hist_change[i] = r.history[i].change;
+      hist_vf[i] = r.history[i].volume_fraction;
+    }
+    std::memcpy(design, r.design.data(), r.design.size() * sizeof(double));
+    std::memcpy(phys, r.physical_density.data(), r.physical_density.size() * sizeof(double));
+    out_scalars[0] = r.compliance;
+    out_scalars[1] = r.volume_fraction;
+    out_scalars[2] = r.initial_compliance;
+    out_ints[0] = r.iterations;
+    out_ints[1] = r.converged ? 1 : 0;
+    out_ints[2] = r.non_convergent ? 1 : 0;
+    out_ints[3] = r.infeasible ? 1 : 0;
+  });
+}
 }  // extern "C"

@@ -791,6 +791,176 @@ int or_oc_update_projected(int nx, int ny, int nz, const uint8_t* solid, const o
                                     volfrac, move, rho_min, x_new);
 }
 
+/* ------------------------------------------------------------------ MMA */
+/* mma_update_joint (mma_joint.cpp) for one uniformly boxed block [rho_min, 1]
+ * with mma_update's chain (simp.cpp:1433-1489): dc and dv through the filter
+ * transpose, dc scaled by its largest magnitude over the design set, g0 the
+ * filtered volume minus the target; Svanberg's asymptotes (asyinit 0.5, incr
+ * 1.2, decr 0.7, the [0.01, 10] x-range clamp), the separable coefficients with
+ * raa0 = 1e-5, the move box (albefa 0.1, move * xrange), and the 1-D dual on the
+ * volume constraint by doubling and bisection to 1e-9 (1 + l1 + l2). */
+int or_mma_update(int nx, int ny, int nz, const uint8_t* design, const or_filter* f,
+                  or_mma_state* st, int iter, const double* density, const double* dcomp,
+                  double volfrac, double move, double rho_min, double* x_new,
+                  double* lambda_out) {
+  const size_t nv = (size_t)nx * ny * nz;
+  double* dc = malloc(nv * sizeof(double));
+  double* dv = malloc(nv * sizeof(double));
+  double* ones = calloc(nv, sizeof(double));
+  double* xphys = malloc(nv * sizeof(double));
+  size_t ndof = 0;
+  or_filter_sensitivity(f, dcomp, dc);
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(design, e)) {
+      ones[e] = 1.0;
+      ++ndof;
+    }
+  or_filter_sensitivity(f, ones, dv);
+  const double target = volfrac * (double)ndof;
+  double scale = 0.0;
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(design, e)) scale = fmax(scale, fabs(dc[e]));
+  if (scale > 0.0)
+    for (size_t e = 0; e < nv; ++e)
+      if (is_solid(design, e)) dc[e] /= scale;
+  or_filter_density(f, density, xphys);
+  double vol = 0.0;
+  for (size_t e = 0; e < nv; ++e) vol += xphys[e];
+  const double g0 = vol - target;
+  const double asyinit = 0.5, asyincr = 1.2, asydecr = 0.7, albefa = 0.1, raa0 = 1e-5;
+  const double xmin = rho_min, xmax = 1.0;
+  for (size_t e = 0; e < nv; ++e) {
+    if (!is_solid(design, e)) continue;
+    const double xe = density[e];
+    const double xr = xmax - xmin;
+    if (iter <= 2) {
+      st->low[e] = xe - asyinit * xr;
+      st->upp[e] = xe + asyinit * xr;
+    } else {
+      const double sgn = (xe - st->xold1[e]) * (st->xold1[e] - st->xold2[e]);
+      const double gam = sgn < 0.0 ? asydecr : (sgn > 0.0 ? asyincr : 1.0);
+      double L = xe - gam * (st->xold1[e] - st->low[e]);
+      double U = xe + gam * (st->upp[e] - st->xold1[e]);
+      L = fmin(L, xe - 0.01 * xr);
+      L = fmax(L, xe - 10.0 * xr);
+      U = fmax(U, xe + 0.01 * xr);
+      U = fmin(U, xe + 10.0 * xr);
+      st->low[e] = L;
+      st->upp[e] = U;
+    }
+  }
+  double* p0 = calloc(nv, sizeof(double));
+  double* q0 = calloc(nv, sizeof(double));
+  double* p1 = calloc(nv, sizeof(double));
+  double* q1 = calloc(nv, sizeof(double));
+  double* al = calloc(nv, sizeof(double));
+  double* be = calloc(nv, sizeof(double));
+  double b = -g0;
+  for (size_t e = 0; e < nv; ++e) {
+    if (!is_solid(design, e)) continue;
+    const double xe = density[e], xr = xmax - xmin;
+    const double L = st->low[e], U = st->upp[e];
+    const double ux1 = U - xe, xl1 = xe - L;
+    const double dcp = fmax(dc[e], 0.0), dcm = fmax(-dc[e], 0.0);
+    const double dvp = fmax(dv[e], 0.0), dvm = fmax(-dv[e], 0.0);
+    p0[e] = ux1 * ux1 * (1.001 * dcp + 0.001 * dcm + raa0 / xr);
+    q0[e] = xl1 * xl1 * (0.001 * dcp + 1.001 * dcm + raa0 / xr);
+    p1[e] = ux1 * ux1 * (1.001 * dvp + 0.001 * dvm + raa0 / xr);
+    q1[e] = xl1 * xl1 * (0.001 * dvp + 1.001 * dvm + raa0 / xr);
+    b += p1[e] / ux1 + q1[e] / xl1;
+    /* std::max({a, b, c}) / std::min({...}): the first extreme in order. */
+    double a = xmin;
+    const double a2 = L + albefa * (xe - L), a3 = xe - move * xr;
+    if (a < a2) a = a2;
+    if (a < a3) a = a3;
+    double c = xmax;
+    const double c2 = U - albefa * (U - xe), c3 = xe + move * xr;
+    if (c2 < c) c = c2;
+    if (c3 < c) c = c3;
+    al[e] = a;
+    be[e] = c;
+  }
+#define MMA_CAND(lam, out)                                              \
+  for (size_t e = 0; e < nv; ++e) {                                     \
+    (out)[e] = 0.0;                                                     \
+    if (!is_solid(design, e)) continue;                                 \
+    const double pl = sqrt(p0[e] + (lam) * p1[e]);                      \
+    const double ql = sqrt(q0[e] + (lam) * q1[e]);                      \
+    double xt = (pl * st->low[e] + ql * st->upp[e]) / (pl + ql);        \
+    if (xt < al[e]) xt = al[e];                                         \
+    if (xt > be[e]) xt = be[e];                                         \
+    (out)[e] = xt;                                                      \
+  }
+#define MMA_G(xc, out)                                                  \
+  do {                                                                  \
+    double s_ = 0.0;                                                    \
+    for (size_t e = 0; e < nv; ++e)                                     \
+      if (is_solid(design, e))                                          \
+        s_ += p1[e] / (st->upp[e] - (xc)[e]) + q1[e] / ((xc)[e] - st->low[e]); \
+    (out) = s_ - b;                                                     \
+  } while (0)
+  double lambda = 0.0, g = 0.0;
+  MMA_CAND(0.0, x_new);
+  MMA_G(x_new, g);
+  if (g > 0.0) {
+    double l1 = 0.0, l2 = 1.0;
+    for (;;) {
+      if (!(l2 < 1e30)) break;
+      MMA_CAND(l2, x_new);
+      MMA_G(x_new, g);
+      if (!(g > 0.0)) break;
+      l2 *= 2.0;
+    }
+    for (int it = 0; it < 100 && (l2 - l1) > 1e-9 * (1.0 + l1 + l2); ++it) {
+      const double lmid = 0.5 * (l1 + l2);
+      MMA_CAND(lmid, x_new);
+      MMA_G(x_new, g);
+      if (g > 0.0)
+        l1 = lmid;
+      else
+        l2 = lmid;
+    }
+    lambda = 0.5 * (l1 + l2);
+  }
+  MMA_CAND(lambda, x_new);
+#undef MMA_CAND
+#undef MMA_G
+  /* xold2 = xold1; xold1 = x. */
+  memcpy(st->xold2, st->xold1, nv * sizeof(double));
+  memcpy(st->xold1, density, nv * sizeof(double));
+  if (lambda_out) *lambda_out = lambda;
+  free(dc); free(dv); free(ones); free(xphys);
+  free(p0); free(q0); free(p1); free(q1); free(al); free(be);
+  return OR_OK;
+}
+
+int or_mma_objective_plateau(const double* c, int n, int window, double rel_tol, double min_drop,
+                             int min_flat_windows) {
+  if (window <= 0) return 0;
+  if (n < window + 1) return 0;
+  double best_now = c[0];
+  for (int i = 1; i < n; ++i)
+    if (c[i] < best_now) best_now = c[i];
+  if (min_drop > 0.0 && !(best_now <= c[0] * (1.0 - min_drop))) {
+    int escape = 0;
+    if (min_flat_windows > 0) {
+      const int flat_span = min_flat_windows * window;
+      if (n >= flat_span + 1) {
+        double best_before = c[0];
+        for (int i = 1; i < n - flat_span; ++i)
+          if (c[i] < best_before) best_before = c[i];
+        if (best_before > 0.0) escape = (best_before - best_now) / best_before < rel_tol;
+      }
+    }
+    if (!escape) return 0;
+  }
+  double best_prev = c[0];
+  for (int i = 1; i < n - window; ++i)
+    if (c[i] < best_prev) best_prev = c[i];
+  if (!(best_prev > 0.0)) return 0;
+  return (best_prev - best_now) / best_prev < rel_tol;
+}
+
 /* effective_design_mask (simp.cpp:2610-2633): Empty -> FrozenVoid, Load and
  * Fixture -> FrozenSolid, everything else keeps the caller's entry. */
 void or_effective_design_mask(int nx, int ny, int nz, const uint8_t* tags, const uint8_t* mask,
@@ -945,6 +1115,20 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
   const int nst = o->nstages > 0 ? o->nstages : 1;
   const uint8_t* dset = mask ? active : solid; /* the design set */
   int st = OR_OK, stop = 0;
+  or_mma_state mma = {NULL, NULL, NULL, NULL};
+  int mma_iter = 0;
+  /* validate_updater_options (simp.cpp:83-88). */
+  if (o->updater == 1 && o->nstages > 0) {
+    st = fail(OR_EINVAL, "simp_optimize: MMA updater does not support a Heaviside projection "
+                         "schedule; use OC or clear options.projection");
+    goto out;
+  }
+  if (o->updater == 1) {
+    mma.low = calloc(nv, sizeof(double));
+    mma.upp = calloc(nv, sizeof(double));
+    mma.xold1 = calloc(nv, sizeof(double));
+    mma.xold2 = calloc(nv, sizeof(double));
+  }
   for (int si = 0; si < nst && !stop; ++si) {
     const int project = o->nstages > 0;
     const double beta = project ? o->stage_beta[si] : 0.0;
@@ -971,6 +1155,9 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
         or_filter_density(f, x, xphys); /* xtilde: the unprojected filtered design */
         st = oc_update_projected_common(nx, ny, nz, dset, mask != NULL, f, x, xphys, dc, beta,
                                         o->eta, o->volume_fraction, move, rho_min, xnew);
+      } else if (o->updater == 1) {
+        st = or_mma_update(nx, ny, nz, dset, f, &mma, ++mma_iter, x, dc, o->volume_fraction,
+                           move, rho_min, xnew, NULL);
       } else {
         st = mask ? or_oc_update_masked(nx, ny, nz, eff, f, x, dc, o->volume_fraction, move,
                                         rho_min, xnew, NULL, NULL)
@@ -996,7 +1183,15 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
         stop = 1;
         break;
       }
-      if (change < o->change_tol) { /* stage_should_stop: on to the next stage */
+      /* stage_should_stop (simp.cpp:1219-1233): MMA on the objective plateau,
+       * otherwise change_tol; either ends the stage. */
+      const int plateau_stop =
+          o->updater == 1 && o->mma_plateau_window > 0
+              ? or_mma_objective_plateau(hist_c, res->iterations, o->mma_plateau_window,
+                                         o->mma_plateau_tol, o->mma_plateau_min_drop,
+                                         o->mma_plateau_flat_windows)
+              : change < o->change_tol;
+      if (plateau_stop) {
         stage_conv = 1;
         break;
       }
@@ -1026,6 +1221,7 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
   }
   res->volume_fraction = n_design > 0.0 ? vol_final / n_design : 0.0;
 out:
+  free(mma.low); free(mma.upp); free(mma.xold1); free(mma.xold2);
   free(x); free(xphys); free(xnew); free(dc); free(u);
   free(eff); free(active); free(analysis);
   or_filter_free(f);

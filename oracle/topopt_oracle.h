@@ -139,7 +139,30 @@ typedef struct {
    * target mean over the design set, clamped and filtered once
    * (warm_start_design, simp.cpp:324-344). */
   const double* initial_design;
+  /* The design updater (SimpOptions::updater, simp.hpp:1119): 0 OC, 1 MMA.
+   * MMA stops a run on the objective plateau (mma_objective_plateau,
+   * simp.cpp:1081-1134) when mma_plateau_window > 0, else on change_tol. */
+  int updater;
+  int mma_plateau_window;
+  double mma_plateau_tol, mma_plateau_min_drop;
+  int mma_plateau_flat_windows;
 } or_simp_options;
+
+/* The MMA state across one run (MmaJointState): asymptotes and the last two
+ * designs, nv each; iter the 1-based MMA iteration. */
+typedef struct {
+  double *low, *upp, *xold1, *xold2;
+} or_mma_state;
+/* mma_update / mma_update_masked (simp.cpp:1433-1489, :2736-2784) with the
+ * subproblem mma_update_joint (mma_joint.cpp): design is the design set (solid
+ * voxels, or Active voxels with the Active-only filter f). */
+int or_mma_update(int nx, int ny, int nz, const uint8_t* design, const or_filter* f,
+                  or_mma_state* st, int iter, const double* density, const double* dc,
+                  double volfrac, double move, double rho_min, double* x_new,
+                  double* lambda_out);
+/* mma_objective_plateau (simp.cpp:1081-1134). */
+int or_mma_objective_plateau(const double* c, int n, int window, double rel_tol, double min_drop,
+                             int min_flat_windows);
 
 /* heaviside_project and its derivative (simp.cpp:352-365). */
 double or_heaviside_project(double rt, double beta, double eta);

@@ -242,6 +242,18 @@ def main():
     out["lp_connected"] = np.array([R.load_path_connected(pbl, dfix),
                                     R.load_path_connected(pbl, sev.ravel())])
 
+    # The MMA updater: a plateau-stopped plain run and a masked run.
+    mp = R.simp_optimize_mma(pb3, max_it=200, cg_tol=1e-10)
+    out.update(mma_hist_c=mp["hist_c"], mma_hist_change=mp["hist_change"],
+               mma_hist_vf=mp["hist_vf"], mma_design=mp["design"], mma_phys=mp["phys"],
+               mma_compliance=np.array(mp["compliance"]),
+               mma_out=np.array([mp["iterations"], int(mp["converged"])]))
+    mm = R.simp_optimize_mma(pbm, mask=mask, volfrac=0.35, max_it=40, cg_tol=1e-10)
+    out.update(mmam_hist_c=mm["hist_c"], mmam_hist_change=mm["hist_change"],
+               mmam_design=mm["design"], mmam_phys=mm["phys"],
+               mmam_compliance=np.array(mm["compliance"]),
+               mmam_volume_fraction=np.array(mm["volume_fraction"]))
+
     # On-disk formats, written by the reference's own writers.
     out.update(_formats(R, rng))
 

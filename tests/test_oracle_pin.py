@@ -304,3 +304,26 @@ def test_ladder_walk_golden(port, golden, tag, margin_stop):
         golden[f"lad{tag}_out"].tolist()
     assert np.array_equal(L["design"], golden[f"lad{tag}_design"])
     assert np.array_equal(L["phys"], golden[f"lad{tag}_phys"])
+
+
+def test_mma_plateau_run_golden(port, golden):
+    """simp_optimize with the MMA updater (Svanberg's asymptotes, the separable
+    subproblem and its 1-D dual, mma_joint.cpp) stopped by the objective plateau
+    (mma_objective_plateau, defaults 10 / 1e-3 / 0.05 / 3): bit-identical."""
+    s = port.simp_optimize_mma(cantilever(12, 4, 4), max_it=200, cg_tol=1e-10)
+    assert [s["iterations"], int(s["converged"])] == golden["mma_out"].tolist()
+    assert s["iterations"] < 200 and s["converged"]
+    for k in ("hist_c", "hist_change", "hist_vf", "design", "phys"):
+        assert np.array_equal(s[k], golden["mma_" + k]), k
+    assert s["compliance"] == float(golden["mma_compliance"])
+
+
+def test_mma_masked_run_golden(port, golden):
+    """mma_update_masked (simp.cpp:2736-2784): only Active voxels move, the rest
+    of x_new is 0, pins on the physical density; bit-identical."""
+    pb, mask = _masked_problem(golden)
+    s = port.simp_optimize_mma(pb, mask=mask, volfrac=0.35, max_it=40, cg_tol=1e-10)
+    for k in ("hist_c", "hist_change", "design", "phys"):
+        assert np.array_equal(s[k], golden["mmam_" + k]), k
+    assert s["compliance"] == float(golden["mmam_compliance"])
+    assert s["volume_fraction"] == float(golden["mmam_volume_fraction"])

@@ -68,6 +68,8 @@ from ._capi import (  # noqa: F401
     MASK_FROZEN_VOID,
     PREC_FP64,
     PREC_MIXED,
+    UPDATER_MMA,
+    UPDATER_OC,
     SOLVER_MGCG,
     SOLVER_JACOBI_CG,
 )

@@ -23,6 +23,7 @@ _LIB_PATH = os.path.join(HERE, "libtopopt_gb300.so")
 TG_OK, TG_EINVAL, TG_ESINGULAR, TG_ENONCONV, TG_EDEADLINE, TG_EDEVICE, TG_ENOMEM, TG_ECANCELLED = range(8)
 SOLVER_MGCG, SOLVER_JACOBI_CG = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+UPDATER_OC, UPDATER_MMA = 0, 1
 
 
 class LibraryMissing(RuntimeError):
@@ -85,7 +86,9 @@ class _SimpOpt(C.Structure):
                 ("max_iterations", C.c_int32), ("cg_max_iterations", C.c_int32),
                 ("solve", _SolveOpt), ("projection", C.POINTER(_ProjStage)),
                 ("projection_stages", C.c_int32), ("projection_eta", C.c_double),
-                ("initial_design", C.c_void_p)]
+                ("initial_design", C.c_void_p), ("updater", C.c_int32),
+                ("mma_plateau_window", C.c_int32), ("mma_plateau_tol", C.c_double),
+                ("mma_plateau_min_drop", C.c_double), ("mma_plateau_flat_windows", C.c_int32)]
 
 
 class _Iter(C.Structure):
@@ -307,6 +310,13 @@ class SimpOptions:
     projection_eta: float = 0.5
     # Warm start (simp.hpp:1557-1575): a raw seed density per voxel, or None.
     initial_design: object = None
+    # The updater (simp.hpp:1119): UPDATER_OC or UPDATER_MMA, and MMA's plateau
+    # stop (simp.hpp:1241-1277 defaults).
+    updater: int = 0
+    mma_plateau_window: int = 10
+    mma_plateau_tol: float = 1e-3
+    mma_plateau_min_drop: float = 0.05
+    mma_plateau_flat_windows: int = 3
 
     def total_iterations(self) -> int:
         if self.projection:
@@ -324,6 +334,11 @@ class SimpOptions:
             o._stages = arr
             o.projection_stages = len(self.projection)
         o.projection_eta = self.projection_eta
+        o.updater = self.updater
+        o.mma_plateau_window = self.mma_plateau_window
+        o.mma_plateau_tol = self.mma_plateau_tol
+        o.mma_plateau_min_drop = self.mma_plateau_min_drop
+        o.mma_plateau_flat_windows = self.mma_plateau_flat_windows
         if self.initial_design is not None:
             seed = np.ascontiguousarray(self.initial_design, dtype=np.float64).ravel()
             o._seed = seed  # kept alive with the struct

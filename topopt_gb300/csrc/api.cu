@@ -538,6 +538,106 @@ void oc_update_projected_device(OcState& oc, FilterState& fs, const Grid& g, con
                                  xnew, s);
 }
 
+// mma_update / mma_update_masked (simp.cpp:1433-1489, :2736-2784) with the
+// subproblem of mma_update_joint (mma_joint.cpp) on device-resident fields: dc
+// through the filter transpose (bit-exact), the fixed dv, the coefficients and
+// box (bit-exact per voxel), g0 = the exact sum of the filtered design over the
+// design set minus the target, and the dual's doubling and bisection to
+// 1e-9 (1 + l1 + l2), up to kOcMulti multipliers per pass, each branch decided
+// in the reference's order.  The dual sums are fixed-order device sums, not the
+// reference's sequential ones, so a branch on a near-tie may differ: this
+// updater is held to the reference within tolerance.
+void mma_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t* act,
+                       MmaFields& m, int iter, DBuf<uint64_t>& scale, const double* x,
+                       const double* xphys, const double* dc, double volfrac, double move,
+                       double rho_min, double* xnew, cudaStream_t s) {
+  fs.adj(g, act, dc, oc.dcf.p, s);
+  bool exact = false;
+  const double vol = exact_volume(oc, g, act, xphys, &exact, s);
+  const double g0 = vol - volfrac * double(oc.n_solid);
+  launch_mma_prepare(m, x, oc.dcf.p, oc.dvf.p, act, g.nv, iter, move, rho_min, scale.p,
+                     oc.vpart.p, oc.vsum.p, s);
+  TG_CUDA(cudaMemcpyAsync(oc.h_v, oc.vsum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  TG_CUDA(cudaStreamSynchronize(s));
+  const double b = -g0 + oc.h_v[0];
+  std::vector<std::pair<double, double>> known;  // (lambda, constraint sum)
+  auto lookup = [&](double lam, double* v) {
+    for (const auto& kv : known)
+      if (kv.first == lam) {
+        *v = kv.second;
+        return true;
+      }
+    return false;
+  };
+  const int kmax = g.nv > (int64_t(1) << 22) ? 4 : kOcMulti;
+  auto batch = [&](const std::vector<double>& lams) {
+    ProjLambdas ls;
+    ls.k = int(std::min<size_t>(lams.size(), size_t(kmax)));
+    for (int k = 0; k < ls.k; ++k) ls.lam[k] = lams[size_t(k)];
+    launch_mma_dual(m, act, g.nv, ls, oc.vpart.p, oc.vsum.p, s);
+    TG_CUDA(cudaMemcpyAsync(oc.h_v, oc.vsum.p, sizeof(double) * ls.k, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    ++oc.passes;
+    for (int k = 0; k < ls.k; ++k) known.emplace_back(ls.lam[k], oc.h_v[k]);
+  };
+  auto positive = [&](double lam) {  // gval(candidate(lam)) > 0
+    ++oc.evals;
+    double v = 0.0;
+    if (!lookup(lam, &v)) {
+      batch({lam});
+      lookup(lam, &v);
+    }
+    return (v - b) > 0.0;
+  };
+  // lambda = 0 and the first doublings in one pass.
+  {
+    std::vector<double> c{0.0};
+    for (double t = 1.0; int(c.size()) < kmax; t *= 2.0) c.push_back(t);
+    batch(c);
+  }
+  double lambda = 0.0, tmp = 0.0;
+  if (positive(0.0)) {
+    double l1 = 0.0, l2 = 1.0;
+    while (l2 < 1e30) {
+      if (!lookup(l2, &tmp)) {
+        std::vector<double> c;
+        for (double t = l2; int(c.size()) < kmax && t < 1e30; t *= 2.0) c.push_back(t);
+        batch(c);
+      }
+      if (!positive(l2)) break;
+      l2 *= 2.0;
+    }
+    for (int it = 0; it < 100 && (l2 - l1) > 1e-9 * (1.0 + l1 + l2); ++it) {
+      const double lmid = 0.5 * (l1 + l2);
+      if (!lookup(lmid, &tmp)) {
+        std::vector<double> c;
+        std::vector<std::pair<double, double>> lv{{l1, l2}};
+        while (!lv.empty() && int(c.size()) < kmax) {
+          std::vector<std::pair<double, double>> nx;
+          for (const auto& iv : lv) {
+            if (int(c.size()) >= kmax) break;
+            const double mm = 0.5 * (iv.first + iv.second);
+            c.push_back(mm);
+            nx.emplace_back(iv.first, mm);
+            nx.emplace_back(mm, iv.second);
+          }
+          lv.swap(nx);
+        }
+        batch(c);
+      }
+      if (positive(lmid))
+        l1 = lmid;
+      else
+        l2 = lmid;
+    }
+    lambda = 0.5 * (l1 + l2);
+  }
+  launch_mma_candidate(m, act, g.nv, lambda, xnew, s);
+  // xold2 = xold1; xold1 = x.
+  std::swap(m.xold1, m.xold2);
+  TG_CUDA(cudaMemcpyAsync(m.xold1, x, size_t(g.nv) * sizeof(double), cudaMemcpyDeviceToDevice, s));
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -571,6 +671,13 @@ struct tg_job {
   int stage = 0;        // the stage the next steps run
   DBuf<double> xtilde;  // filter(x), before the projection (projected jobs)
   bool projecting() const { return !stages.empty(); }
+  // MMA (updater == TG_UPDATER_MMA): the run's asymptotes, last two designs and
+  // the subproblem's fields.
+  bool mma = false;
+  int mma_iter = 0;
+  DBuf<double> mma_buf;  // 10 fields of nv
+  DBuf<uint64_t> mma_scale;
+  MmaFields mf{};
   double* h_scal = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evf = nullptr;
   int64_t n_solid = 0;
@@ -588,7 +695,7 @@ struct tg_job {
   }
   size_t bytes() const {
     size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes() + eff.bytes();
-    for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal, &xtilde})
+    for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal, &xtilde, &mma_buf})
       b += d->bytes();
     return b + (solver ? solver->device_bytes() : 0);
   }
@@ -632,6 +739,13 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
     j->stages.assign(o.projection, o.projection + o.projection_stages);
     j->eta = o.projection_eta;
   }
+  if (o.updater != TG_UPDATER_OC && o.updater != TG_UPDATER_MMA)
+    raise(TG_EINVAL, "simp_optimize: updater must be TG_UPDATER_OC or TG_UPDATER_MMA");
+  // validate_updater_options (simp.cpp:83-88).
+  if (o.updater == TG_UPDATER_MMA && o.projection_stages > 0)
+    raise(TG_EINVAL, "simp_optimize: MMA updater does not support a Heaviside projection "
+                     "schedule; use OC or clear options.projection");
+  j->mma = o.updater == TG_UPDATER_MMA;
   j->params = *params;
   j->opt = o;
   j->opt.projection = nullptr;  // the job keeps its own copy of the plan
@@ -668,6 +782,15 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   upload(j->solid, j->solid_h.data(), j->solid_h.size(), s);
   for (DBuf<double>* d : {&j->x, &j->xnew, &j->xphys, &j->E, &j->dc}) d->alloc(size_t(g.nv));
   if (j->projecting()) j->xtilde.alloc(size_t(g.nv));
+  if (j->mma) {
+    const size_t n = size_t(g.nv);
+    j->mma_buf.alloc(10 * n);
+    j->mma_scale.alloc(1);
+    TG_CUDA(cudaMemsetAsync(j->mma_buf.p, 0, j->mma_buf.bytes(), s));
+    double* b = j->mma_buf.p;
+    j->mf = MmaFields{b, b + n, b + 2 * n, b + 3 * n, b + 4 * n,
+                      b + 5 * n, b + 6 * n, b + 7 * n, b + 8 * n, b + 9 * n};
+  }
   j->u.alloc(size_t(g.ndof));
   j->part.alloc(size_t(4 * kRedBlocks + 152 * 32));
   j->scal.alloc(8);
@@ -800,6 +923,10 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
     oc_update_projected_device(j->oc, j->filt, g, j->solid.p, j->x.p, j->xtilde.p, j->dc.p,
                                ps.beta, j->eta, o.volume_fraction, ps.move,
                                j->params.density_min, j->xnew.p, j->s);
+  } else if (j->mma) {
+    mma_update_device(j->oc, j->filt, g, j->solid.p, j->mf, ++j->mma_iter, j->mma_scale,
+                      j->x.p, j->xphys.p, j->dc.p, o.volume_fraction, o.move,
+                      j->params.density_min, j->xnew.p, j->s);
   } else {
     oc_update_device(j->oc, j->filt, g, j->solid.p, j->solid_h, j->x.p, j->dc.p,
                      o.volume_fraction, o.move, j->params.density_min, j->xnew.p, j->s);
@@ -866,6 +993,33 @@ bool rung_infeasible(const std::vector<double>& c, const std::vector<int>& cg) {
   return (hi - lo) / lo <= 1e-3;
 }
 
+
+// mma_objective_plateau (simp.cpp:1081-1134): the running-minimum improvement
+// over the trailing window below tol, behind the min_drop progress gate with
+// its flatness escape over min_flat_windows windows.
+bool mma_objective_plateau(const std::vector<double>& c, const tg_simp_options& o) {
+  const int window = o.mma_plateau_window;
+  if (window <= 0) return false;
+  const int n = int(c.size());
+  if (n < window + 1) return false;
+  double best_now = c[0];
+  for (int i = 1; i < n; ++i) best_now = c[size_t(i)] < best_now ? c[size_t(i)] : best_now;
+  const double min_drop = o.mma_plateau_min_drop, tol = o.mma_plateau_tol;
+  if (min_drop > 0.0 && !(best_now <= c[0] * (1.0 - min_drop))) {
+    bool escape = false;
+    const int flat = o.mma_plateau_flat_windows;
+    if (flat > 0 && n >= flat * window + 1) {
+      double before = c[0];
+      for (int i = 1; i < n - flat * window; ++i) before = c[size_t(i)] < before ? c[size_t(i)] : before;
+      if (before > 0.0) escape = (before - best_now) / before < tol;
+    }
+    if (!escape) return false;
+  }
+  double best_prev = c[0];
+  for (int i = 1; i < n - window; ++i) best_prev = c[size_t(i)] < best_prev ? c[size_t(i)] : best_prev;
+  if (!(best_prev > 0.0)) return false;
+  return (best_prev - best_now) / best_prev < tol;
+}
 
 // ------------------------------------------------------ strength analysis
 void validate_strength(const tg_strength_spec* sp) {
@@ -1484,6 +1638,7 @@ int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* option
   if (mixed) b += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 126 * 4 * 8.0 / 7.0 + nv * 4;
   if (options && options->projection_stages > 0)  // xtilde and the candidate fields
     b += nv * 8.0 * (1 + projected_candidates(int64_t(nv)));
+  if (options && options->updater == TG_UPDATER_MMA) b += nv * 8.0 * 10;  // MMA fields
   return int64_t(b * 1.05) + (64 << 20);
 }
 
@@ -1563,7 +1718,11 @@ static int simp_optimize_impl(const tg_grid* grid, const tg_simp_params* params,
           stop = true;
           break;
         }
-        if (row.change < o.change_tol) {
+        // stage_should_stop (simp.cpp:1219-1233): MMA on the objective plateau.
+        const bool stop_here = (j->mma && o.mma_plateau_window > 0)
+                                   ? mma_objective_plateau(j->hist_c, o)
+                                   : row.change < o.change_tol;
+        if (stop_here) {
           stage_conv = true;
           break;
         }

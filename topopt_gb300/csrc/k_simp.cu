@@ -515,6 +515,154 @@ __global__ void __launch_bounds__(kThreads) k_proj_volume(GridDev g, const Stenc
   }
 }
 
+// ------------------------------------------------------------------ MMA
+// The MMA subproblem of mma_update_joint (mma_joint.cpp) on the design voxels,
+// every operation a separate IEEE one in the reference's order, so coefficients,
+// candidates and terms are the reference's bit for bit for the same inputs.
+struct MmaConsts {
+  double xmin, xmax, move;
+  int iter;
+};
+
+// |v| peak over the design set as the bit pattern of a non-negative double.
+__global__ void k_absmax_design(const double* __restrict__ v, const uint8_t* __restrict__ act,
+                                int64_t n, unsigned long long* __restrict__ out) {
+  double m = 0.0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads)
+    if (act[e]) m = fmax(m, fabs(v[e]));
+  if (m > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// Asymptotes (Svanberg's rule with asyinit 0.5, incr 1.2, decr 0.7 and the
+// [0.01, 10] x-range clamp), the separable coefficients p0, q0, p1, q1 (raa0 =
+// 1e-5, dc scaled by its design-set peak), the move box (albefa 0.1), and per
+// block the partial sums of p1 / (U - x) + q1 / (x - L).
+__global__ void k_mma_prepare(const double* __restrict__ x, const double* __restrict__ dcf,
+                              const double* __restrict__ dvf, const uint8_t* __restrict__ act,
+                              int64_t n, MmaConsts c, const unsigned long long* __restrict__ scale_bits,
+                              double* __restrict__ low, double* __restrict__ upp,
+                              const double* __restrict__ xold1, const double* __restrict__ xold2,
+                              double* __restrict__ p0, double* __restrict__ q0,
+                              double* __restrict__ p1, double* __restrict__ q1,
+                              double* __restrict__ al, double* __restrict__ be,
+                              double* __restrict__ part) {
+  const double scale = __longlong_as_double((long long)*scale_bits);
+  const double xr = __dsub_rn(c.xmax, c.xmin);
+  const double reg = __ddiv_rn(1e-5, xr);
+  double tsum = 0.0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    if (!act[e]) {
+      p0[e] = q0[e] = p1[e] = q1[e] = al[e] = be[e] = 0.0;
+      continue;
+    }
+    const double xe = x[e];
+    double L, U;
+    if (c.iter <= 2) {
+      L = __dsub_rn(xe, __dmul_rn(0.5, xr));
+      U = __dadd_rn(xe, __dmul_rn(0.5, xr));
+    } else {
+      const double o1 = xold1[e], o2 = xold2[e];
+      const double sg = __dmul_rn(__dsub_rn(xe, o1), __dsub_rn(o1, o2));
+      const double gam = sg < 0.0 ? 0.7 : (sg > 0.0 ? 1.2 : 1.0);
+      L = __dsub_rn(xe, __dmul_rn(gam, __dsub_rn(o1, low[e])));
+      U = __dadd_rn(xe, __dmul_rn(gam, __dsub_rn(upp[e], o1)));
+      L = fmin(L, __dsub_rn(xe, __dmul_rn(0.01, xr)));
+      L = fmax(L, __dsub_rn(xe, __dmul_rn(10.0, xr)));
+      U = fmax(U, __dadd_rn(xe, __dmul_rn(0.01, xr)));
+      U = fmin(U, __dadd_rn(xe, __dmul_rn(10.0, xr)));
+    }
+    low[e] = L;
+    upp[e] = U;
+    const double d = scale > 0.0 ? __ddiv_rn(dcf[e], scale) : dcf[e];
+    const double dv = dvf[e];
+    const double ux1 = __dsub_rn(U, xe), xl1 = __dsub_rn(xe, L);
+    const double dcp = fmax(d, 0.0), dcm = fmax(-d, 0.0);
+    const double dvp = fmax(dv, 0.0), dvm = fmax(-dv, 0.0);
+    const double u2 = __dmul_rn(ux1, ux1), l2 = __dmul_rn(xl1, xl1);
+    const double a0 = __dmul_rn(u2, __dadd_rn(__dadd_rn(__dmul_rn(1.001, dcp), __dmul_rn(0.001, dcm)), reg));
+    const double b0 = __dmul_rn(l2, __dadd_rn(__dadd_rn(__dmul_rn(0.001, dcp), __dmul_rn(1.001, dcm)), reg));
+    const double a1 = __dmul_rn(u2, __dadd_rn(__dadd_rn(__dmul_rn(1.001, dvp), __dmul_rn(0.001, dvm)), reg));
+    const double b1 = __dmul_rn(l2, __dadd_rn(__dadd_rn(__dmul_rn(0.001, dvp), __dmul_rn(1.001, dvm)), reg));
+    p0[e] = a0;
+    q0[e] = b0;
+    p1[e] = a1;
+    q1[e] = b1;
+    tsum += __dadd_rn(__ddiv_rn(a1, ux1), __ddiv_rn(b1, xl1));
+    // std::max({xmin, L + albefa (x - L), x - move xr}) and the min for beta:
+    // the first extreme in order.
+    double lo = c.xmin;
+    const double lo2 = __dadd_rn(L, __dmul_rn(0.1, __dsub_rn(xe, L)));
+    const double lo3 = __dsub_rn(xe, __dmul_rn(c.move, xr));
+    if (lo < lo2) lo = lo2;
+    if (lo < lo3) lo = lo3;
+    double hi = c.xmax;
+    const double hi2 = __dsub_rn(U, __dmul_rn(0.1, __dsub_rn(U, xe)));
+    const double hi3 = __dadd_rn(xe, __dmul_rn(c.move, xr));
+    if (hi2 < hi) hi = hi2;
+    if (hi3 < hi) hi = hi3;
+    al[e] = lo;
+    be[e] = hi;
+  }
+  const double v = block_sum256(tsum);
+  if (threadIdx.x == 0) part[blockIdx.x] = v;
+}
+
+__device__ __forceinline__ double mma_candidate(double lam, double p0, double q0, double p1,
+                                                double q1, double L, double U, double lo,
+                                                double hi) {
+  const double pl = __dsqrt_rn(__dadd_rn(p0, __dmul_rn(lam, p1)));
+  const double ql = __dsqrt_rn(__dadd_rn(q0, __dmul_rn(lam, q1)));
+  double xt = __ddiv_rn(__dadd_rn(__dmul_rn(pl, L), __dmul_rn(ql, U)), __dadd_rn(pl, ql));
+  if (xt < lo) xt = lo;
+  if (xt > hi) xt = hi;
+  return xt;
+}
+
+// The dual's constraint sums sum_e p1/(U - x(lambda)) + q1/(x(lambda) - L) for
+// up to K multipliers in one pass over the coefficients.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_mma_dual(
+    const double* __restrict__ p0, const double* __restrict__ q0, const double* __restrict__ p1,
+    const double* __restrict__ q1, const double* __restrict__ low, const double* __restrict__ upp,
+    const double* __restrict__ al, const double* __restrict__ be, const uint8_t* __restrict__ act,
+    int64_t n, ProjLambdas ls, double* __restrict__ part) {
+  double acc[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) acc[j] = 0.0;
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads) {
+    if (!act[e]) continue;
+    const double a0 = p0[e], b0 = q0[e], a1 = p1[e], b1 = q1[e], L = low[e], U = upp[e];
+    const double lo = al[e], hi = be[e];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (j >= ls.k) break;
+      const double xt = mma_candidate(ls.lam[j], a0, b0, a1, b1, L, U, lo, hi);
+      acc[j] += __dadd_rn(__ddiv_rn(a1, __dsub_rn(U, xt)), __ddiv_rn(b1, __dsub_rn(xt, L)));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    if (j >= ls.k) break;
+    const double v = block_sum256(acc[j]);
+    if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+__global__ void k_mma_candidate(const double* __restrict__ p0, const double* __restrict__ q0,
+                                const double* __restrict__ p1, const double* __restrict__ q1,
+                                const double* __restrict__ low, const double* __restrict__ upp,
+                                const double* __restrict__ al, const double* __restrict__ be,
+                                const uint8_t* __restrict__ act, int64_t n, double lam,
+                                double* __restrict__ xnew) {
+  for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
+       e += int64_t(gridDim.x) * kThreads)
+    xnew[e] = act[e] ? mma_candidate(lam, p0[e], q0[e], p1[e], q1[e], low[e], upp[e], al[e], be[e])
+                     : 0.0;
+}
+
 // ---------------------------------------------------------------- stress
 // hex8_stress at the element centre (hex_element.cpp:242-316).  At the centre
 // every shape-function gradient is +-q, q = (2/h) * 0.125 exactly, with the
@@ -832,6 +980,42 @@ void launch_proj_volume(const Grid& g, const void* st, int ns, const uint8_t* ac
                                                             part);
   TG_LAUNCH_CHECK();
   k_sum_partials_multi<<<k, kThreads, 0, s>>>(part, kRedBlocks, out);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_mma_prepare(const MmaFields& m, const double* x, const double* dcf, const double* dvf,
+                        const uint8_t* act, int64_t n, int iter, double move, double xmin,
+                        uint64_t* scale_bits, double* part, double* tsum, cudaStream_t s) {
+  TG_CUDA(cudaMemsetAsync(scale_bits, 0, sizeof(uint64_t), s));
+  k_absmax_design<<<kRedBlocks, kThreads, 0, s>>>(dcf, act, n,
+                                                  reinterpret_cast<unsigned long long*>(scale_bits));
+  TG_LAUNCH_CHECK();
+  const MmaConsts c{xmin, 1.0, move, iter};
+  k_mma_prepare<<<kRedBlocks, kThreads, 0, s>>>(
+      x, dcf, dvf, act, n, c, reinterpret_cast<const unsigned long long*>(scale_bits), m.low,
+      m.upp, m.xold1, m.xold2, m.p0, m.q0, m.p1, m.q1, m.al, m.be, part);
+  TG_LAUNCH_CHECK();
+  k_sum_partials_multi<<<1, kThreads, 0, s>>>(part, kRedBlocks, tsum);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_mma_dual(const MmaFields& m, const uint8_t* act, int64_t n, const ProjLambdas& ls,
+                     double* part, double* out, cudaStream_t s) {
+  if (ls.k <= 4)
+    k_mma_dual<4><<<kRedBlocks, kThreads, 0, s>>>(m.p0, m.q0, m.p1, m.q1, m.low, m.upp, m.al, m.be,
+                                                  act, n, ls, part);
+  else
+    k_mma_dual<kOcMulti><<<kRedBlocks, kThreads, 0, s>>>(m.p0, m.q0, m.p1, m.q1, m.low, m.upp,
+                                                         m.al, m.be, act, n, ls, part);
+  TG_LAUNCH_CHECK();
+  k_sum_partials_multi<<<ls.k, kThreads, 0, s>>>(part, kRedBlocks, out);
+  TG_LAUNCH_CHECK();
+}
+
+void launch_mma_candidate(const MmaFields& m, const uint8_t* act, int64_t n, double lam,
+                          double* xnew, cudaStream_t s) {
+  k_mma_candidate<<<grid_blocks(n), kThreads, 0, s>>>(m.p0, m.q0, m.p1, m.q1, m.low, m.upp, m.al,
+                                                      m.be, act, n, lam, xnew);
   TG_LAUNCH_CHECK();
 }
 

@@ -259,6 +259,21 @@ void launch_oc_candidates_projected(const double* x, const double* dcf, const do
 void launch_proj_volume(const Grid& g, const void* st, int ns, const uint8_t* act,
                         const double* hs, const double* cand, int k, double beta, double eta,
                         double* part, double* out, cudaStream_t s);
+// MMA (mma_joint.cpp): the per-voxel fields of one run's subproblem.
+struct MmaFields {
+  double *low, *upp, *xold1, *xold2, *p0, *q0, *p1, *q1, *al, *be;
+};
+// Asymptotes, coefficients and move box from x, dcf (unscaled), dvf; tsum[0] =
+// sum over the design set of p1/(U - x) + q1/(x - L).  scale_bits: 1 scratch word.
+void launch_mma_prepare(const MmaFields& m, const double* x, const double* dcf, const double* dvf,
+                        const uint8_t* act, int64_t n, int iter, double move, double xmin,
+                        uint64_t* scale_bits, double* part, double* tsum, cudaStream_t s);
+// out[j] = the dual's constraint sum at ls.lam[j], j < ls.k.
+void launch_mma_dual(const MmaFields& m, const uint8_t* act, int64_t n, const ProjLambdas& ls,
+                     double* part, double* out, cudaStream_t s);
+// x_new(lambda) on the design set, 0 elsewhere.
+void launch_mma_candidate(const MmaFields& m, const uint8_t* act, int64_t n, double lam,
+                          double* xnew, cudaStream_t s);
 // hex8_stress at every voxel centre where solid[e] and (rho null or rho[e] >
 // iso): von Mises and the 6 stresses (either output may be null; 0 elsewhere),
 // and into peaks[0..2] (zeroed by the caller) the bit patterns of the peak von
