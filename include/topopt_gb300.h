@@ -172,6 +172,8 @@ typedef struct {
   double beta; /* projection sharpness of this iteration's stage; 0 when unprojected */
   int32_t hier_built;          /* a multigrid hierarchy was built for this solve */
   int32_t mg_cycles_attempted; /* V-cycles this solve ran */
+  int32_t oc_exact_evals;      /* bisection branches the fast volume bound could not decide */
+  int32_t oc_host_fallbacks;   /* of those, decided by the host's sequential sum */
 } tg_simp_iteration;
 
 typedef struct {

@@ -101,7 +101,8 @@ class _Iter(C.Structure):
                 ("t_device_ms", C.c_double), ("fine_matvecs", C.c_int64),
                 ("fine_matvecs_lowp", C.c_int64), ("oc_volume_passes", C.c_int32),
                 ("beta", C.c_double), ("hier_built", C.c_int32),
-                ("mg_cycles_attempted", C.c_int32)]
+                ("mg_cycles_attempted", C.c_int32), ("oc_exact_evals", C.c_int32),
+                ("oc_host_fallbacks", C.c_int32)]
 
 
 class _Result(C.Structure):

@@ -357,11 +357,15 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   const double m = double(fs.st.n);
   const double eps =
       (n + 2.0 * (m + 1.0) + 12.0 + n / (double(kRedBlocks) * 256.0) + 64.0) * u * 1.01;
-  // Fast volumes are computed ahead, kOcMulti lambdas per pass over the fields:
-  // the next doublings while bracketing, the next four levels of the bisection
-  // tree (15 midpoints) while bisecting.  Every branch is still decided one at a
+  // Fast volumes are computed ahead, kmax lambdas per pass over the fields: the
+  // next doublings while bracketing, the next levels of the bisection tree
+  // (breadth first) while bisecting.  Every branch is still decided one at a
   // time, in the reference's order, from the volume of exactly the lambda the
-  // sequential loop would test, so the speculation changes no decision.
+  // sequential loop would test, so the speculation changes no decision.  A
+  // candidate costs a few FP64 operations per voxel: on large grids the pass is
+  // FP64-bound, and 4 per pass (two bisection levels and one more midpoint)
+  // wastes less work than 16 (four levels, of which one path is used).
+  const int kmax = g.nv > (int64_t(1) << 20) ? 4 : kOcMulti;
   std::vector<std::pair<double, double>> known;  // (lambda, fast volume)
   auto lookup = [&](double lam, double* V) {
     for (const auto& kv : known)
@@ -373,7 +377,7 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   };
   auto batch = [&](const std::vector<double>& lams) {
     OcCands cs;
-    cs.k = int(std::min<size_t>(lams.size(), size_t(kOcMulti)));
+    cs.k = int(std::min<size_t>(lams.size(), size_t(kmax)));
     for (int k = 0; k < cs.k; ++k) cs.c[k] = 1.0 / std::sqrt(lams[size_t(k)]);
     launch_oc_volume_multi(oc.sq.p, oc.lo.p, oc.hi.p, oc.dvf.p, g.nv, cs, oc.vpart.p, oc.vsum.p,
                            s);
@@ -410,7 +414,7 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   while (l2 < 1e30) {
     if (!lookup(l2, &Vtmp)) {
       std::vector<double> c;
-      for (double t = l2; int(c.size()) < kOcMulti && t < 1e30; t *= 2.0) c.push_back(t);
+      for (double t = l2; int(c.size()) < kmax && t < 1e30; t *= 2.0) c.push_back(t);
       batch(c);
     }
     if (!eval(l2)) break;
@@ -419,13 +423,14 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
   for (int it = 0; it < 100 && (l2 - l1) > 1e-6 * (l1 + l2); ++it) {
     const double lmid = 0.5 * (l1 + l2);
     if (!lookup(lmid, &Vtmp)) {
-      // The midpoints the next four bisection steps can reach, computed with the
-      // loop's own arithmetic.
+      // The midpoints the next bisection steps can reach, breadth first,
+      // computed with the loop's own arithmetic.
       std::vector<double> c;
       std::vector<std::pair<double, double>> lv{{l1, l2}};
-      for (int depth = 0; depth < 4; ++depth) {
+      while (!lv.empty() && int(c.size()) < kmax) {
         std::vector<std::pair<double, double>> nx;
         for (const auto& iv : lv) {
+          if (int(c.size()) >= kmax) break;
           const double m = 0.5 * (iv.first + iv.second);
           c.push_back(m);
           nx.emplace_back(iv.first, m);
@@ -914,7 +919,8 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   }
   const double c = job_sensitivity(j);
   const double t3 = now_ms();
-  const int fb0 = j->oc.evals, ps0 = j->oc.passes;
+  const int fb0 = j->oc.evals, ps0 = j->oc.passes, ex0 = j->oc.exact_evals,
+            hf0 = j->oc.fallbacks;
   double beta = 0.0;
   if (j->projecting()) {
     // xtilde = filter(x) is current: job_filter_x ran for this x.
@@ -964,6 +970,8 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   r.beta = beta;
   r.hier_built = st.hier_built ? 1 : 0;
   r.mg_cycles_attempted = st.mg_cycles;
+  r.oc_exact_evals = j->oc.exact_evals - ex0;
+  r.oc_host_fallbacks = j->oc.fallbacks - hf0;
   j->hist_c.push_back(c);
   j->hist_cg.push_back(st.iterations);
   if (row) *row = r;

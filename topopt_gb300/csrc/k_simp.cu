@@ -33,6 +33,23 @@ struct GridDev {
 };
 GridDev dev(const Grid& g) { return GridDev{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz}; }
 
+// Voxel coordinates of a linear index.  32-bit unsigned division (a fraction of
+// the 64-bit sequence) whenever the index fits, which is every grid of fewer
+// than 2^32 voxels.
+__device__ __forceinline__ void vox_ijk(const GridDev& g, int64_t e, int& i, int& j, int& k) {
+  if (e <= int64_t(0xffffffffu)) {
+    const unsigned ue = unsigned(e), nx = unsigned(g.nx), ny = unsigned(g.ny);
+    const unsigned q = ue / nx, r = q / ny;
+    i = int(ue - q * nx);
+    j = int(q - r * ny);
+    k = int(r);
+  } else {
+    i = int(e % g.nx);
+    j = int((e / g.nx) % g.ny);
+    k = int(e / (int64_t(g.nx) * g.ny));
+  }
+}
+
 int grid_blocks(int64_t n) {
   const int64_t b = (n + kThreads - 1) / kThreads;
   return int(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
@@ -180,7 +197,8 @@ __global__ void k_sensitivity(GridDev g, Modal64 mc, const double* __restrict__ 
        e += int64_t(gridDim.x) * kThreads) {
     double d = 0.0;
     if (elem[e]) {
-      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      int i, j, k;
+      vox_ijk(g, e, i, j, k);
       double ux[8], uy[8], uz[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
@@ -224,7 +242,8 @@ __global__ void k_weight_sum(GridDev g, const StencilEntry* __restrict__ st, int
        e += int64_t(gridDim.x) * kThreads) {
     double s = 0.0;
     if (act[e]) {
-      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      int i, j, k;
+      vox_ijk(g, e, i, j, k);
       for (int q = 0; q < ns; ++q) {
         const int ii = i + st[q].di, jj = j + st[q].dj, kk = k + st[q].dk;
         if (!in_grid(g, ii, jj, kk)) continue;
@@ -245,7 +264,8 @@ __global__ void k_filter_fwd(GridDev g, const StencilEntry* __restrict__ st, int
     double v = 0.0;
     const double h = hs[e];
     if (h > 0.0) {
-      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      int i, j, k;
+      vox_ijk(g, e, i, j, k);
       double acc = 0.0;
       for (int q = 0; q < ns; ++q) {
         const int ii = i + st[q].di, jj = j + st[q].dj, kk = k + st[q].dk;
@@ -277,7 +297,8 @@ __global__ void k_filter_adj(GridDev g, const StencilEntry* __restrict__ st, int
        e += int64_t(gridDim.x) * kThreads) {
     double acc = 0.0;
     if (act[e]) {
-      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      int i, j, k;
+      vox_ijk(g, e, i, j, k);
       for (int q = 0; q < ns; ++q) {
         const int ii = i + st[q].di, jj = j + st[q].dj, kk = k + st[q].dk;
         if (!in_grid(g, ii, jj, kk)) continue;
@@ -356,17 +377,18 @@ __global__ void k_oc_prepare(const double* __restrict__ x, const double* __restr
 // The linear volume sum_e dv_e clamp(sq_e c, lo_e, hi_e) for up to kOcMulti
 // candidates c = 1/sqrt(lambda) in one pass over the fields (each candidate
 // summed in a fixed per-thread order and tree).
-__global__ void k_oc_volume_multi(const double* __restrict__ sq, const double* __restrict__ lo,
-                                  const double* __restrict__ hi, const double* __restrict__ dvf,
-                                  int64_t n, OcCands cs, double* __restrict__ part) {
-  double acc[kOcMulti];
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_oc_volume_multi(
+    const double* __restrict__ sq, const double* __restrict__ lo, const double* __restrict__ hi,
+    const double* __restrict__ dvf, int64_t n, OcCands cs, double* __restrict__ part) {
+  double acc[K];
 #pragma unroll
-  for (int k = 0; k < kOcMulti; ++k) acc[k] = 0.0;
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
   for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
        e += int64_t(gridDim.x) * kThreads) {
     const double s = sq[e], l = lo[e], h = hi[e], d = dvf[e];
 #pragma unroll
-    for (int k = 0; k < kOcMulti; ++k) {
+    for (int k = 0; k < K; ++k) {
       if (k >= cs.k) break;
       double xt = s * cs.c[k];
       xt = xt < l ? l : xt;
@@ -374,7 +396,9 @@ __global__ void k_oc_volume_multi(const double* __restrict__ sq, const double* _
       acc[k] += d * xt;
     }
   }
-  for (int k = 0; k < cs.k; ++k) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (k >= cs.k) break;  // cs.k is uniform over the block
     const double v = block_sum256(acc[k]);
     if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = v;
   }
@@ -489,7 +513,8 @@ __global__ void __launch_bounds__(kThreads) k_proj_volume(GridDev g, const Stenc
        e += int64_t(gridDim.x) * kThreads) {
     if (!act[e]) continue;
     const double h = hs[e];
-    const int i = int(e % g.nx), jy = int((e / g.nx) % g.ny), kz = int(e / (int64_t(g.nx) * g.ny));
+    int i, jy, kz;
+    vox_ijk(g, e, i, jy, kz);
     double acc[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) acc[j] = 0.0;
@@ -689,7 +714,8 @@ __global__ void k_element_stress(GridDev g, const uint8_t* __restrict__ solid,
     const bool on = solid[e] && (rho == nullptr || rho[e] > c.iso);
     double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, vm = 0.0;
     if (on) {
-      const int i = int(e % g.nx), j = int((e / g.nx) % g.ny), k = int(e / (int64_t(g.nx) * g.ny));
+      int i, j, k;
+      vox_ijk(g, e, i, j, k);
       double ex = 0.0, ey = 0.0, ez = 0.0, gxy = 0.0, gyz = 0.0, gzx = 0.0;
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
@@ -923,7 +949,10 @@ int exact_sum_blocks() { return kRedBlocks; }
 void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi,
                             const double* dvf, int64_t n, const OcCands& cs, double* part,
                             double* out, cudaStream_t s) {
-  k_oc_volume_multi<<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, cs, part);
+  if (cs.k <= 4)
+    k_oc_volume_multi<4><<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, cs, part);
+  else
+    k_oc_volume_multi<kOcMulti><<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, cs, part);
   TG_LAUNCH_CHECK();
   k_sum_partials_multi<<<cs.k, kThreads, 0, s>>>(part, kRedBlocks, out);
   TG_LAUNCH_CHECK();
