@@ -95,12 +95,15 @@ typedef struct {
   int32_t mg_levels;       /* 0 = deepest (coarsest axis >= 2 elements) */
   int32_t mg_iter_budget;  /* 0 = 300 */
   double omega;            /* 0 = 0.6 */
-  double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve, 0 = 1e-3 */
+  double inner_tolerance;  /* mixed: relative tolerance of each FP32 inner solve; 0 = 0.3x the
+                              reduction still needed, within [1e-5, 0.1] */
   int32_t max_refinements; /* mixed: outer FP64 refinement steps, 0 = 20 */
   int32_t coarsening;      /* odd-axis coarsening: TG_COARSEN_* (0 = the form's default) */
   int32_t graph_mode;      /* mixed: TG_GRAPH_ON (default, 0) runs the inner PCG loop as one
                               CUDA graph with a device-side loop condition; TG_GRAPH_OFF
                               drives it from the host (same arithmetic, same results) */
+  int32_t smooth_sweeps;   /* damped-Jacobi sweeps before and after the coarse correction
+                              on every level (0 = 1, the reference's smoother) */
 } tg_solve_options;
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */

@@ -62,7 +62,8 @@ class _SolveOpt(C.Structure):
     _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("mg_levels", C.c_int32),
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
                 ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
-                ("coarsening", C.c_int32), ("graph_mode", C.c_int32)]
+                ("coarsening", C.c_int32), ("graph_mode", C.c_int32),
+                ("smooth_sweeps", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -274,11 +275,12 @@ class SolveOptions:
     max_refinements: int = 0
     coarsening: int = 0  # COARSEN_DEFAULT / COARSEN_REFERENCE / COARSEN_ALIGNED
     graph_mode: int = 0  # GRAPH_ON / GRAPH_OFF
+    smooth_sweeps: int = 0  # Jacobi sweeps per side of the coarse correction (0 = 1)
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
                          self.omega, self.inner_tolerance, self.max_refinements,
-                         self.coarsening, self.graph_mode)
+                         self.coarsening, self.graph_mode, self.smooth_sweeps)
 
 
 @dataclass

@@ -197,6 +197,8 @@ tg_solve_options default_solve(const tg_solve_options* o) {
     raise(TG_EINVAL, "solve options: unknown coarsening");
   if (d.graph_mode != TG_GRAPH_ON && d.graph_mode != TG_GRAPH_OFF)
     raise(TG_EINVAL, "solve options: unknown graph_mode");
+  if (d.smooth_sweeps < 0 || d.smooth_sweeps > 8)
+    raise(TG_EINVAL, "solve options: smooth_sweeps must be in [0, 8]");
   return d;
 }
 

@@ -257,6 +257,7 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
     : fp_(fp), opt_(opt), s_(s) {
   omega_ = opt.omega > 0.0 ? opt.omega : 0.6;
   budget_ = opt.mg_iter_budget > 0 ? opt.mg_iter_budget : 300;
+  sweeps_ = opt.smooth_sweeps > 0 ? opt.smooth_sweeps : 1;
   mixed_ = opt.precision == TG_PREC_MIXED;
   const size_t n = size_t(fp.g.ndof);
   for (DBuf<double>* b : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_}) b->alloc(n);
@@ -575,13 +576,21 @@ void Solver::vcycle_level(size_t l) {
     mg_stencil_op<T>(mode, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w, L.R<T>(),
                      s_);
   };
+  // sweeps_ damped-Jacobi sweeps on each side (the first from a zero iterate);
+  // every sweep leaves the iterate in X.
   mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);
+  for (int k = 1; k < sweeps_; ++k) {
+    op(kSmooth);
+    std::swap(L.X<T>(), L.R<T>());
+  }
   op(kResidual);
   mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
   vcycle_level<T>(l + 1);
   mg_prolong_add<T>(L.d, N.d, N.X<T>(), L.act.p, L.X<T>(), s_);
-  op(kSmooth);
-  std::swap(L.X<T>(), L.R<T>());
+  for (int k = 0; k < sweeps_; ++k) {
+    op(kSmooth);
+    std::swap(L.X<T>(), L.R<T>());
+  }
 }
 
 template <>
@@ -591,16 +600,21 @@ double* Solver::vcycle<double>(const double* b) {
   const MgDims fd = dims_of(g.nx, g.ny, g.nz);
   double* x = t1_.p;
   double* r = t0_.p;
+  auto smooth = [&] {
+    launch_fine_op<double>(kSmooth, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
+                           nullptr, nullptr, s_);
+    std::swap(x, r);
+  };
   mg_jacobi_first<double>(b, invdiag_.p, omega_, g.ndof, x, s_);
+  for (int k = 1; k < sweeps_; ++k) smooth();
   launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
                          nullptr, nullptr, s_);
   mg_restrict<double>(fd, N.d, r, N.act.p, N.B<double>(), s_);
   vcycle_level<double>(1);
   mg_prolong_add<double>(fd, N.d, N.X<double>(), fp_.kept.p, x, s_);
-  launch_fine_op<double>(kSmooth, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
-                         nullptr, nullptr, s_);
-  fine_matvecs_ += 2;
-  return r;
+  for (int k = 0; k < sweeps_; ++k) smooth();
+  fine_matvecs_ += 2 * sweeps_;
+  return x;
 }
 
 template <>
@@ -611,16 +625,21 @@ float* Solver::vcycle<float>(const float* b) {
   float* x = t1f_.p;
   float* r = t0f_.p;
   const float w = float(omega_);
+  auto smooth = [&] {
+    launch_fine_op<float>(kSmooth, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
+                          nullptr, s_);
+    std::swap(x, r);
+  };
   mg_jacobi_first<float>(b, invdiagf_.p, w, g.ndof, x, s_);
+  for (int k = 1; k < sweeps_; ++k) smooth();
   launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
                         nullptr, s_);
   mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_);
   vcycle_level<float>(1);
   mg_prolong_add<float>(fd, N.d, N.X<float>(), fp_.kept.p, x, s_);
-  launch_fine_op<float>(kSmooth, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
-                        nullptr, s_);
-  lowp_matvecs_ += 2;
-  return r;
+  for (int k = 0; k < sweeps_; ++k) smooth();
+  lowp_matvecs_ += 2 * sweeps_;
+  return x;
 }
 
 // ------------------------------------------------------------------ MG-PCG
@@ -845,7 +864,12 @@ bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
     launch_fill<double>(x_.p, 0.0, n, s_);
     TG_CUDA(cudaMemcpyAsync(r_.p, rhs_.p, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, s_));
   }
-  const double inner_tol = opt_.inner_tolerance > 0.0 ? opt_.inner_tolerance : 1e-3;
+  // Default: the inner FP32 solve targets 0.3x the reduction still needed, down
+  // to 1e-5 -- one refinement usually finishes a warm-started solve, so the FP64
+  // residual (FP64-bound, ~20x an FP32 apply) runs twice per solve, not three
+  // times.  A recursive FP32 residual reaches 1e-5 whatever the true one does;
+  // when the FP64 residual shows it fell short, another refinement follows.
+  const double inner_tol = opt_.inner_tolerance > 0.0 ? opt_.inner_tolerance : 1e-5;
   const int max_ref = opt_.max_refinements > 0 ? opt_.max_refinements : 20;
   int total_inner = 0;
   for (int ref = 0; ref <= max_ref; ++ref) {
@@ -861,8 +885,8 @@ bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
     if (ref == max_ref || total_inner >= max_it) break;
     launch_scale_d2f(zf_.p, r_.p, scal_.p + 5, n, s_);
     int it = 0;
-    // Default inner tolerance: 1e-3, relaxed to 0.3x the reduction still needed
-    // when that is less (the last refinement usually needs far less than 1e-3).
+    // Default inner tolerance: 0.3x the reduction still needed, within
+    // [1e-5, 0.1].
     const double itol = opt_.inner_tolerance > 0.0 ? inner_tol
                                                    : std::min(0.1, std::max(inner_tol, 0.3 * threshold / rn));
     inner_pcg<float>(std::min(budget_, max_it - total_inner), itol, st, &it);

@@ -97,6 +97,7 @@ class Solver {
   cudaStream_t s_;
   double omega_ = 0.6;
   int budget_ = 300;
+  int sweeps_ = 1;  // damped-Jacobi sweeps per side of the coarse correction
   bool mixed_ = false;
   // fine state
   const double* E_ = nullptr;
