@@ -253,75 +253,62 @@ __global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int6
 }
 
 // Stencil operator: y = A x / b - A x / x + w D^-1 (b - A x), masked by act.
-// A thread per node and all three output components.  Forward block j of node n
-// couples n to n + off_j; the backward coupling of n to n - off_j is the forward
-// block j of node n - off_j, transposed.  All 13 block pairs are unrolled so the
-// loads are independent; out-of-grid neighbours are predicated (the stored
-// forward block of a node whose neighbour lies outside the grid is zero, and the
-// backward term is selected away).
+// A thread per (node, output component r): row r of every 3x3 block.  Forward
+// block j of node n couples n to n + off_j; the backward coupling of n to
+// n - off_j is the forward block j of node n - off_j, transposed (its column r).
+// Three threads per node keep the per-thread register count low and the number
+// of independent coefficient loads in flight high: the kernel streams the
+// stencil once from HBM (the backward re-reads hit L2) and is bound by how many
+// of those loads are outstanding.  Out-of-grid neighbours are predicated (the
+// stored forward block of a node whose neighbour lies outside the grid is zero,
+// and the backward term is selected away).  Per output the terms are summed in
+// a fixed order: the self block, then per j the forward and backward term.
 template <class T, int MODE>
-__global__ void __launch_bounds__(256, 5) k_stencil_op(MgDims d, const T* __restrict__ A,
-                                                         const uint8_t* __restrict__ act,
-                                                         const T* __restrict__ x,
-                                                         const T* __restrict__ b,
-                                                         const T* __restrict__ invdiag, T omega,
-                                                         T* __restrict__ y) {
+__global__ void __launch_bounds__(192) k_stencil_op(MgDims d, const T* __restrict__ A,
+                                                    const uint8_t* __restrict__ act,
+                                                    const T* __restrict__ x,
+                                                    const T* __restrict__ b,
+                                                    const T* __restrict__ invdiag, T omega,
+                                                    T* __restrict__ y) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   const int64_t sy = d.nnx, sz = int64_t(d.nnx) * d.nny;
-  // One node per thread on a 3D grid (x fastest).
-  const int a = blockIdx.x * 32 + threadIdx.x, bb = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
-  if (a < d.nnx && bb < d.nny) {
-    const int64_t n = c * sz + bb * sy + a;
-    const T* An = A + n;
-    const T xs0 = x[3 * n], xs1 = x[3 * n + 1], xs2 = x[3 * n + 2];
-    T s0 = An[0] * xs0 + An[nn] * xs1 + An[2 * nn] * xs2;
-    T s1 = An[3 * nn] * xs0 + An[4 * nn] * xs1 + An[5 * nn] * xs2;
-    T s2 = An[6 * nn] * xs0 + An[7 * nn] * xs1 + An[8 * nn] * xs2;
+  // Block (32, 3, 2): x the node along x, y the component, z the node row along y.
+  const int a = blockIdx.x * 32 + threadIdx.x, r = threadIdx.y;
+  const int bb = blockIdx.y * 2 + threadIdx.z, c = blockIdx.z;
+  if (a >= d.nnx || bb >= d.nny) return;
+  const int64_t n = c * sz + bb * sy + a;
+  const T* An = A + n + int64_t(3 * r) * nn;  // row r of the self block
+  T s = An[0] * x[3 * n] + An[nn] * x[3 * n + 1] + An[2 * nn] * x[3 * n + 2];
 #pragma unroll
-    for (int j = 1; j < 14; ++j) {
-      const int di = 13 + j;
-      const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
-      const int64_t off = dz * sz + dy * sy + dx;
-      const bool fin = (a + dx) < d.nnx && (a + dx) >= 0 && (bb + dy) < d.nny && (bb + dy) >= 0 &&
-                       (c + dz) < d.nnz;
-      const bool bin = (a - dx) >= 0 && (a - dx) < d.nnx && (bb - dy) >= 0 && (bb - dy) < d.nny &&
-                       (c - dz) >= 0;
-      const int64_t m = fin ? n + off : n;
-      const int64_t p = bin ? n - off : n;
-      const T* Af = An + int64_t(j * 9) * nn;
-      const T* Ab = A + int64_t(j * 9) * nn + p;
-      const T f0 = x[3 * m], f1 = x[3 * m + 1], f2 = x[3 * m + 2];
-      const T g0 = x[3 * p], g1 = x[3 * p + 1], g2 = x[3 * p + 2];
-      const T u0 = Af[0] * f0 + Af[nn] * f1 + Af[2 * nn] * f2;
-      const T u1 = Af[3 * nn] * f0 + Af[4 * nn] * f1 + Af[5 * nn] * f2;
-      const T u2 = Af[6 * nn] * f0 + Af[7 * nn] * f1 + Af[8 * nn] * f2;
-      const T v0 = Ab[0] * g0 + Ab[3 * nn] * g1 + Ab[6 * nn] * g2;
-      const T v1 = Ab[nn] * g0 + Ab[4 * nn] * g1 + Ab[7 * nn] * g2;
-      const T v2 = Ab[2 * nn] * g0 + Ab[5 * nn] * g1 + Ab[8 * nn] * g2;
-      s0 += fin ? u0 : T(0);
-      s1 += fin ? u1 : T(0);
-      s2 += fin ? u2 : T(0);
-      s0 += bin ? v0 : T(0);
-      s1 += bin ? v1 : T(0);
-      s2 += bin ? v2 : T(0);
-    }
-    const T sv[3] = {s0, s1, s2};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int64_t dof = 3 * n + k;
-      T out;
-      if (!act[dof]) {
-        out = T(0);
-      } else if (MODE == kApply) {
-        out = sv[k];
-      } else if (MODE == kResidual) {
-        out = b[dof] - sv[k];
-      } else {
-        out = x[dof] + omega * invdiag[dof] * (b[dof] - sv[k]);
-      }
-      y[dof] = out;
-    }
+  for (int j = 1; j < 14; ++j) {
+    const int di = 13 + j;
+    const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
+    const int64_t off = dz * sz + dy * sy + dx;
+    const bool fin = (a + dx) < d.nnx && (a + dx) >= 0 && (bb + dy) < d.nny && (bb + dy) >= 0 &&
+                     (c + dz) < d.nnz;
+    const bool bin = (a - dx) >= 0 && (a - dx) < d.nnx && (bb - dy) >= 0 && (bb - dy) < d.nny &&
+                     (c - dz) >= 0;
+    const int64_t m = fin ? n + off : n;
+    const int64_t p = bin ? n - off : n;
+    const T* Af = An + int64_t(j * 9) * nn;
+    const T* Ab = A + int64_t(j * 9 + r) * nn + p;
+    const T u = Af[0] * x[3 * m] + Af[nn] * x[3 * m + 1] + Af[2 * nn] * x[3 * m + 2];
+    const T v = Ab[0] * x[3 * p] + Ab[3 * nn] * x[3 * p + 1] + Ab[6 * nn] * x[3 * p + 2];
+    s += fin ? u : T(0);
+    s += bin ? v : T(0);
   }
+  const int64_t dof = 3 * n + r;
+  T out;
+  if (!act[dof]) {
+    out = T(0);
+  } else if (MODE == kApply) {
+    out = s;
+  } else if (MODE == kResidual) {
+    out = b[dof] - s;
+  } else {
+    out = x[dof] + omega * invdiag[dof] * (b[dof] - s);
+  }
+  y[dof] = out;
 }
 
 // x = omega * invdiag .* b (the first smoother sweep from a zero iterate).
@@ -639,7 +626,7 @@ void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s) {
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s) {
-  const dim3 nb((d.nnx + 31) / 32, (d.nny + 7) / 8, d.nnz), nt(32, 8);
+  const dim3 nb((d.nnx + 31) / 32, (d.nny + 1) / 2, d.nnz), nt(32, 3, 2);
   if (mode == kApply)
     k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
   else if (mode == kResidual)
