@@ -324,6 +324,8 @@ def run_ours(args, world, rank, local, pg):
         # Dominant-kernel timing (CUDA events, job stream).
         forms[form]["op_fp64_ms"] = job.time_operator(tg.PREC_FP64, 5)
         if form == "mixed":
+            forms[form]["op_df_residual_ms"] = job.time_operator(2, 5)
+        if form == "mixed":
             forms[form]["op_fp32_ms"] = job.time_operator(tg.PREC_MIXED, 20)
             design, _ = job.read()
         job.close()

@@ -76,6 +76,9 @@ typedef struct {
 
 typedef enum { TG_SOLVER_MGCG = 0, TG_SOLVER_JACOBI_CG = 1 } tg_solver_kind;
 typedef enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 } tg_precision;
+/* tg_matfree_apply only: the FP64 operator evaluated in double-float arithmetic
+ * (the mixed form's refinement residual kernel). */
+enum { TG_APPLY_DF = 2 };
 
 /* Solver knobs.  Zero-initialised means: MG-PCG, FP64, the deepest hierarchy the
  * grid allows, the reference's iteration budget of 300 MG cycles before the
@@ -104,7 +107,13 @@ typedef struct {
                               drives it from the host (same arithmetic, same results) */
   int32_t smooth_sweeps;   /* damped-Jacobi sweeps before and after the coarse correction
                               on every level (0 = 1, the reference's smoother) */
+  int32_t mixed_residual;  /* mixed: how the FP64 refinement residual b - A x is evaluated:
+                              TG_RESIDUAL_DF (0, default) in double-float arithmetic (FP32
+                              pairs, ~48 significant bits, on the FP32 pipe), TG_RESIDUAL_FP64
+                              with the native FP64 operator */
 } tg_solve_options;
+
+enum { TG_RESIDUAL_DF = 0, TG_RESIDUAL_FP64 = 1 };
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */
 typedef struct {
@@ -200,7 +209,8 @@ int tg_hex8_stiffness(double youngs_modulus, double poisson, double element_size
 
 /* fea_matfree_apply (core/include/topopt/fea.hpp:760-766; matfree.cpp:1079-1098):
  * y = K u over the full grid.  youngs_per_voxel NULL -> uniform youngs_modulus.
- * precision TG_PREC_MIXED runs the FP32 operator (inputs rounded to float). */
+ * precision TG_PREC_MIXED runs the FP32 operator (inputs rounded to float),
+ * TG_APPLY_DF the double-float one. */
 int tg_matfree_apply(const tg_grid* grid, double youngs_modulus, double poisson,
                      const double* youngs_per_voxel, int32_t precision, const double* u,
                      double* y);
@@ -635,7 +645,8 @@ int tg_filter_noalloc(int32_t nx, int32_t ny, int32_t nz, const uint8_t* d_tags,
 
 /* ---- measurement (no reference counterpart) ---- */
 /* Average device time of one fine-operator launch (y = A x on the job's current
- * element factors), precision TG_PREC_FP64 or TG_PREC_MIXED (FP32), over `reps`
+ * element factors), precision TG_PREC_FP64, TG_PREC_MIXED (FP32) or TG_APPLY_DF
+ * (the double-float residual kernel), over `reps`
  * back-to-back launches timed with CUDA events on the job's stream. */
 int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* avg_ms);
 /* Kernels this library has launched in the process so far. */

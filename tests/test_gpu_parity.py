@@ -248,3 +248,37 @@ def test_cfg0_fifty_iterations(tg, golden, prec):
     assert rel(hc, golden["cfg0_hist_c"]) < 1e-6
     assert rel(s["design"], golden["cfg0_design"]) < 1e-4
     assert abs(s["compliance"] - float(golden["cfg0_compliance"])) <= 1e-6 * s["compliance"]
+
+
+def test_double_float_operator_matches_fp64(tg, golden):
+    """The double-float (FP32-pair) evaluation of the FP64 operator, the mixed
+    form's refinement residual: within 1e-13 of the FP64 operator relative to
+    its largest entry, on the reference's golden graded case and a random one."""
+    pb, _ = _pb(tg, golden)
+    y = tg.fea_matfree_apply(pb, golden["apply_u"], youngs_per_voxel=golden["apply_factor"],
+                             precision=2)
+    assert rel(y, golden["apply_y_graded"]) < 1e-13
+    rng = np.random.default_rng(11)
+    nx, ny, nz = 70, 33, 20
+    pb2 = tg.Problem(nx, ny, nz)
+    f = np.clip(rng.random(pb2.nv), 1e-3, 1.0) ** 3
+    u = rng.standard_normal(pb2.ndof)
+    y64 = tg.fea_matfree_apply(pb2, u, youngs_per_voxel=f)
+    ydf = tg.fea_matfree_apply(pb2, u, youngs_per_voxel=f, precision=2)
+    assert rel(ydf, y64) < 1e-13
+
+
+@pytest.mark.parametrize("residual", [0, 1])
+def test_mixed_solve_residual_forms_agree(tg, residual):
+    """The mixed solve with the double-float and the FP64 refinement residual:
+    both converge to the FP64 solve's solution at the tolerance."""
+    nx, ny, nz = 48, 24, 24
+    o = cantilever(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                    list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+    E = smooth_modulus(pb)
+    u64, _ = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10)
+    um, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+        precision=tg.PREC_MIXED, mixed_residual=residual))
+    assert info.converged and info.residual <= 1e-10
+    assert rel(um, u64) < 1e-8

@@ -69,6 +69,8 @@ from ._capi import (  # noqa: F401
     PREC_FP64,
     PREC_MIXED,
     UPDATER_MMA,
+    RESIDUAL_DF,
+    RESIDUAL_FP64,
     UPDATER_OC,
     SOLVER_MGCG,
     SOLVER_JACOBI_CG,

@@ -24,6 +24,7 @@ TG_OK, TG_EINVAL, TG_ESINGULAR, TG_ENONCONV, TG_EDEADLINE, TG_EDEVICE, TG_ENOMEM
 SOLVER_MGCG, SOLVER_JACOBI_CG = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 UPDATER_OC, UPDATER_MMA = 0, 1
+RESIDUAL_DF, RESIDUAL_FP64 = 0, 1
 
 
 class LibraryMissing(RuntimeError):
@@ -63,7 +64,7 @@ class _SolveOpt(C.Structure):
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
                 ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
                 ("coarsening", C.c_int32), ("graph_mode", C.c_int32),
-                ("smooth_sweeps", C.c_int32)]
+                ("smooth_sweeps", C.c_int32), ("mixed_residual", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -276,11 +277,13 @@ class SolveOptions:
     coarsening: int = 0  # COARSEN_DEFAULT / COARSEN_REFERENCE / COARSEN_ALIGNED
     graph_mode: int = 0  # GRAPH_ON / GRAPH_OFF
     smooth_sweeps: int = 0  # Jacobi sweeps per side of the coarse correction (0 = 1)
+    mixed_residual: int = 0  # RESIDUAL_DF (double-float, default) / RESIDUAL_FP64
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
                          self.omega, self.inner_tolerance, self.max_refinements,
-                         self.coarsening, self.graph_mode, self.smooth_sweeps)
+                         self.coarsening, self.graph_mode, self.smooth_sweeps,
+                         self.mixed_residual)
 
 
 @dataclass

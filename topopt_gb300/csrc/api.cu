@@ -199,6 +199,8 @@ tg_solve_options default_solve(const tg_solve_options* o) {
     raise(TG_EINVAL, "solve options: unknown graph_mode");
   if (d.smooth_sweeps < 0 || d.smooth_sweeps > 8)
     raise(TG_EINVAL, "solve options: smooth_sweeps must be in [0, 8]");
+  if (d.mixed_residual != TG_RESIDUAL_DF && d.mixed_residual != TG_RESIDUAL_FP64)
+    raise(TG_EINVAL, "solve options: unknown mixed_residual");
   return d;
 }
 
@@ -1327,6 +1329,16 @@ int tg_matfree_apply(const tg_grid* grid, double E, double nu, const double* you
       for (int64_t d = 0; d < g.ndof; ++d) y[d] = double(hy[size_t(d)]);
       return;
     }
+    if (precision == TG_APPLY_DF) {
+      // y = -(0 - A u): the double-float residual kernel with b = 0.
+      DBuf<double> zero(size_t(g.ndof));
+      TG_CUDA(cudaMemsetAsync(zero.p, 0, zero.bytes(), cs.s));
+      launch_fine_residual_df(g, mc, df.p, nullptr, du.p, zero.p, dy.p, cs.s);
+      TG_CUDA(cudaMemcpyAsync(y, dy.p, dy.bytes(), cudaMemcpyDeviceToHost, cs.s));
+      TG_CUDA(cudaStreamSynchronize(cs.s));
+      for (int64_t d = 0; d < g.ndof; ++d) y[d] = -y[d];
+      return;
+    }
     launch_fine_op<double>(kApply, g, mc, df.p, nullptr, du.p, nullptr, nullptr, 0.0, dy.p,
                            nullptr, nullptr, cs.s);
     TG_CUDA(cudaMemcpyAsync(y, dy.p, dy.bytes(), cudaMemcpyDeviceToHost, cs.s));
@@ -1664,7 +1676,10 @@ int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* a
     launch_modulus(job->xphys.p, job->fp.elem.p, g.nv, p.youngs_modulus, p.penalty,
                    p.density_min, p.material_law, p.e_min, job->E.p, job->s);
     job->solver->set_modulus(job->E.p);
-    *avg_ms = job->solver->time_operator(precision == TG_PREC_MIXED, reps);
+    *avg_ms = job->solver->time_operator(precision == TG_PREC_MIXED ? 1
+                                         : precision == TG_APPLY_DF   ? 2
+                                                                      : 0,
+                                         reps);
   });
 }
 

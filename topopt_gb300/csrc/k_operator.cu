@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "tg_df.h"
 #include "tg_internal.h"
 
 namespace tg {
@@ -49,16 +50,53 @@ struct ModalT {
   T L0, L1, M0, M1, M02, M12, LM2;  // per unit modulus; M02 = 2*M0, LM2 = L2 + 4*M2
 };
 
+// Storage (T) to compute (C) and back: the identity, except that a double is
+// carried as a double-float (tg_df.h) by the residual-only instantiation.
+template <class C>
+__host__ __device__ __forceinline__ C cvt(double v) {
+  return C(v);
+}
+template <>
+__host__ __device__ __forceinline__ df cvt<df>(double v) {
+  return df_from(v);
+}
+template <class C, class T>
+__device__ __forceinline__ C load_c(T v) {
+  return cvt<C>(v);
+}
+template <>
+__device__ __forceinline__ float load_c<float, float>(float v) {
+  return v;
+}
+__device__ __forceinline__ double store_t(double v) { return v; }
+__device__ __forceinline__ float store_t(float v) { return v; }
+__device__ __forceinline__ double store_t(df v) { return df_to_double(v); }
+__device__ __forceinline__ bool nonzero(float v) { return v != 0.0f; }
+__device__ __forceinline__ bool nonzero(double v) { return v != 0.0; }
+__device__ __forceinline__ bool nonzero(df v) { return df_nonzero(v); }
+__device__ __forceinline__ float shfl_up(float v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+__device__ __forceinline__ double shfl_up(double v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+__device__ __forceinline__ float shfl_down(float v, int d) {
+  return __shfl_down_sync(0xffffffffu, v, d);
+}
+__device__ __forceinline__ double shfl_down(double v, int d) {
+  return __shfl_down_sync(0xffffffffu, v, d);
+}
+template <class C>
+__host__ __device__ __forceinline__ C czero() {
+  return cvt<C>(0.0);
+}
+
 template <class T>
 ModalT<T> to_modal(const ModalConsts& c) {
   ModalT<T> m;
-  m.L0 = T(c.L[0]);
-  m.L1 = T(c.L[1]);
-  m.M0 = T(c.M[0]);
-  m.M1 = T(c.M[1]);
-  m.M02 = T(2.0 * c.M[0]);
-  m.M12 = T(2.0 * c.M[1]);
-  m.LM2 = T(c.L[2] + 4.0 * c.M[2]);
+  m.L0 = cvt<T>(c.L[0]);
+  m.L1 = cvt<T>(c.L[1]);
+  m.M0 = cvt<T>(c.M[0]);
+  m.M1 = cvt<T>(c.M[1]);
+  m.M02 = cvt<T>(2.0 * c.M[0]);
+  m.M12 = cvt<T>(2.0 * c.M[1]);
+  m.LM2 = cvt<T>(c.L[2] + 4.0 * c.M[2]);
   return m;
 }
 
@@ -156,7 +194,7 @@ __device__ __forceinline__ void modal_apply(const ModalT<T>& mc, T f, T (&ux)[8]
   gx[7] = LM2 * ux[7];
   gy[7] = LM2 * uy[7];
   gz[7] = LM2 * uz[7];
-  gx[0] = gy[0] = gz[0] = T(0);
+  gx[0] = gy[0] = gz[0] = czero<T>();
   walsh_inv(gx);
   walsh_inv(gy);
   walsh_inv(gz);
@@ -224,6 +262,10 @@ template <>
 struct Pencil<float> {
   static constexpr int PY = 8, KZ = 16, MINB = 3;
 };
+template <>
+struct Pencil<df> {
+  static constexpr int PY = 8, KZ = 16, MINB = 2;
+};
 
 template <class T, bool PER = false>
 __device__ __forceinline__ void load_node(const GridDev& g, const T* __restrict__ x, int a, int b,
@@ -260,9 +302,9 @@ __device__ __forceinline__ void load_raw(const GridDev& g, const T* __restrict__
 // The same loads for the non-periodic grid with the column's x/y validity
 // (m[yb][xb]) and base offset hoisted out of the z march: layer c adds
 // 3*c*nnx*nny to the offset and tests only its own z range.
-template <class T>
+template <class T, class C>
 __device__ __forceinline__ void load_raw_np(const T* __restrict__ x, int64_t o, int snx, bool vc,
-                                            const bool (&m)[2][2], int lane, T (&r)[2][2][3]) {
+                                            const bool (&m)[2][2], int lane, C (&r)[2][2][3]) {
 #pragma unroll
   for (int yb = 0; yb < 2; ++yb)
 #pragma unroll
@@ -271,7 +313,7 @@ __device__ __forceinline__ void load_raw_np(const T* __restrict__ x, int64_t o, 
       const bool ok = vc && m[yb][xb];
       const T* p = x + (o + yb * snx + 3 * xb);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) r[yb][xb][k] = ok ? p[k] : T(0);
+      for (int k = 0; k < 3; ++k) r[yb][xb][k] = ok ? load_c<C>(p[k]) : czero<C>();
     }
 }
 
@@ -284,7 +326,7 @@ __device__ __forceinline__ void finish_layer(int lane, const T (&r)[2][2][3], T 
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       v[yb][0][k] = r[yb][0][k];
-      const T nb = __shfl_down_sync(0xffffffffu, r[yb][0][k], 1);
+      const T nb = shfl_down(r[yb][0][k], 1);
       v[yb][1][k] = lane == 31 ? r[yb][1][k] : nb;
     }
 }
@@ -292,15 +334,15 @@ __device__ __forceinline__ void finish_layer(int lane, const T (&r)[2][2][3], T 
 // PER: the periodic (torus) grid of a batch of systems (BatchDev); nodes and
 // elements wrap around, so every element exists and the halo lanes read the
 // opposite face.  The non-periodic instantiations compile the PER branches away.
-template <class T, int PY, int KZ, int MINB, int MODE, bool PER = false>
-__global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> mc,
+template <class T, int PY, int KZ, int MINB, int MODE, bool PER = false, class C = T>
+__global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<C> mc,
                                                      const T* __restrict__ ef,
                                                      const uint8_t* __restrict__ kept,
                                                      const T* __restrict__ x, const T* __restrict__ b,
                                                      const T* __restrict__ invdiag, T omega,
                                                      T* __restrict__ y, double* __restrict__ dot_part,
                                                      BatchDev bd = BatchDev{}) {
-  __shared__ T sy[2][PY][6][32];
+  __shared__ C sy[2][PY][6][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int ex = blockIdx.x * 31 - 1 + lane;
   const int ey = blockIdx.y * (PY - 1) - 1 + w;
@@ -327,30 +369,30 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
   const bool vy0 = ey >= 0 && ey < g.nny, vy1 = ey + 1 < g.nny;
   const bool msk[2][2] = {{vx0 && vy0, vx1 && vy0}, {vx0 && vy1, vx1 && vy1}};
   const int64_t oxy = 3 * (int64_t(ey) * g.nnx + ex);
-  T cur[2][2][3], nxt[2][2][3], raw[2][2][3];
-  if (PER) {
+  C cur[2][2][3], nxt[2][2][3], raw[2][2][3];
+  if constexpr (PER) {
     load_raw<T, PER>(g, x, ex, ey, k0 - 1, lane, raw);
   } else {
     load_raw_np(x, oxy + (k0 - 1) * plane3, snx, k0 - 1 >= 0 && k0 - 1 < g.nnz, msk, lane, raw);
   }
   finish_layer(lane, raw, cur);
-  if (PER)
+  if constexpr (PER)
     load_raw<T, PER>(g, x, ex, ey, k0, lane, raw);
   else
     load_raw_np(x, oxy + k0 * plane3, snx, k0 < g.nnz, msk, lane, raw);
-  T pend[3] = {T(0), T(0), T(0)};
-  T dsum = T(0);  // this thread's share of x.y: a few dozen nodes, then FP64 across the CTA
+  C pend[3] = {czero<C>(), czero<C>(), czero<C>()};
+  C dsum = czero<C>();  // this thread's share of x.y: a few dozen nodes, then FP64 across the CTA
 #pragma unroll 1
   for (int s = 0; s <= KZ; ++s) {
     const int ez = k0 - 1 + s;
     finish_layer(lane, raw, nxt);
     if (s < KZ) {
-      if (PER)
+      if constexpr (PER)
         load_raw<T, PER>(g, x, ex, ey, ez + 2, lane, raw);
       else
         load_raw_np(x, oxy + (ez + 2) * plane3, snx, ez + 2 < g.nnz, msk, lane, raw);
     }
-    T ux[8], uy[8], uz[8];
+    C ux[8], uy[8], uz[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const int xb = c & 1, yb = (c >> 1) & 1, zb = c >> 2;
@@ -358,27 +400,27 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
       uy[c] = zb ? nxt[yb][xb][1] : cur[yb][xb][1];
       uz[c] = zb ? nxt[yb][xb][2] : cur[yb][xb][2];
     }
-    T f;
-    if (PER)
-      f = ef[int64_t(wrap_index(ez, g.nz)) * g.ny * g.nx + exy];
+    C f;
+    if constexpr (PER)
+      f = load_c<C>(ef[int64_t(wrap_index(ez, g.nz)) * g.ny * g.nx + exy]);
     else
-      f = (exy_ok && ez >= 0 && ez < g.nz) ? ef[ez * eplane + exy] : T(0);
-    if (f != T(0)) {
+      f = (exy_ok && ez >= 0 && ez < g.nz) ? load_c<C>(ef[ez * eplane + exy]) : czero<C>();
+    if (nonzero(f)) {
       modal_apply(mc, f, ux, uy, uz);
     } else {
 #pragma unroll
-      for (int c = 0; c < 8; ++c) ux[c] = uy[c] = uz[c] = T(0);
+      for (int c = 0; c < 8; ++c) ux[c] = uy[c] = uz[c] = czero<C>();
     }
     // x: add the previous lane's +x corners to this lane's -x corners.
-    T L[2][2][3];  // [yb][zb][comp] at node x = ex
+    C L[2][2][3];  // [yb][zb][comp] at node x = ex
 #pragma unroll
     for (int yb = 0; yb < 2; ++yb)
 #pragma unroll
       for (int zb = 0; zb < 2; ++zb) {
         const int c0 = (yb << 1) | (zb << 2);
-        L[yb][zb][0] = ux[c0] + __shfl_up_sync(0xffffffffu, ux[c0 | 1], 1);
-        L[yb][zb][1] = uy[c0] + __shfl_up_sync(0xffffffffu, uy[c0 | 1], 1);
-        L[yb][zb][2] = uz[c0] + __shfl_up_sync(0xffffffffu, uz[c0 | 1], 1);
+        L[yb][zb][0] = ux[c0] + shfl_up(ux[c0 | 1], 1);
+        L[yb][zb][1] = uy[c0] + shfl_up(uy[c0 | 1], 1);
+        L[yb][zb][2] = uz[c0] + shfl_up(uz[c0 | 1], 1);
       }
     // y: hand the +y corners to the next warp through shared memory.
     const int buf = s & 1;
@@ -387,34 +429,34 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
 #pragma unroll
       for (int k = 0; k < 3; ++k) sy[buf][w][zb * 3 + k][lane] = L[1][zb][k];
     __syncthreads();
-    T N[2][3];
+    C N[2][3];
 #pragma unroll
     for (int zb = 0; zb < 2; ++zb)
 #pragma unroll
       for (int k = 0; k < 3; ++k)
-        N[zb][k] = L[0][zb][k] + (w >= 1 ? sy[buf][w - 1][zb * 3 + k][lane] : T(0));
+        N[zb][k] = L[0][zb][k] + (w >= 1 ? sy[buf][w - 1][zb * 3 + k][lane] : czero<C>());
     // z: node layer ez is complete (element layers ez-1 and ez).
     if (s >= 1 && own_xy && ez < g.nnz) {
       const int64_t d0 = oxy + ez * plane3;
-      T node_dot = T(0);  // x.y over the node's 3 DOFs, accumulated in FP64 below
+      C node_dot = czero<C>();  // x.y over the node's 3 DOFs, accumulated in FP64 below
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int64_t d = d0 + k;
         const bool kk = kept == nullptr || kept[d] != 0;
-        const T ax = pend[k] + N[0][k];
-        const T xv = cur[0][0][k];
+        const C ax = pend[k] + N[0][k];
         T out;
-        if (MODE == kApply) {
-          out = kk ? ax : T(0);
-          node_dot += xv * out;
-        } else if (MODE == kResidual) {
-          out = kk ? T(b[d] - ax) : T(0);
+        if constexpr (MODE == kApply) {
+          out = kk ? store_t(ax) : T(0);
+          node_dot = node_dot + cur[0][0][k] * load_c<C>(out);
+        } else if constexpr (MODE == kResidual) {
+          // Residual in the storage type: a double-float sum is rounded to FP64 once.
+          out = kk ? T(b[d] - store_t(ax)) : T(0);
         } else {
-          out = kk ? T(xv + omega * invdiag[d] * (b[d] - ax)) : T(0);
+          out = kk ? T(store_t(cur[0][0][k]) + omega * invdiag[d] * (b[d] - store_t(ax))) : T(0);
         }
         y[d] = out;
       }
-      if (MODE == kApply) dsum += node_dot;
+      if constexpr (MODE == kApply) dsum = dsum + node_dot;
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) pend[k] = N[1][k];
@@ -426,7 +468,7 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<T> 
         for (int k = 0; k < 3; ++k) cur[yb][xb][k] = nxt[yb][xb][k];
   }
   if (MODE == kApply && dot_part != nullptr) {
-    const double sum = block_sum(double(dsum));
+    const double sum = block_sum(double(store_t(dsum)));
     if (threadIdx.x == 0)
       dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sum;
   }
@@ -469,6 +511,19 @@ void launch_fine_op(int mode, const Grid& g, const ModalConsts& c, const T* ef,
     default:
       launch_mode<T, kSmooth>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
   }
+}
+
+// The FP64 residual y = b - A x evaluated in double-float arithmetic (tg_df.h):
+// FP64 inputs and output, about 48 significant bits inside, on the FP32 pipe.
+void launch_fine_residual_df(const Grid& g, const ModalConsts& c, const double* ef,
+                             const uint8_t* kept, const double* x, const double* b, double* y,
+                             cudaStream_t s) {
+  using P = Pencil<df>;
+  const GridDev gd{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz};
+  const dim3 grid((g.nnx + 30) / 31, (g.nny + P::PY - 2) / (P::PY - 1), (g.nnz + P::KZ - 1) / P::KZ);
+  k_fine_op<double, P::PY, P::KZ, P::MINB, kResidual, false, df><<<grid, 32 * P::PY, 0, s>>>(
+      gd, to_modal<df>(c), ef, kept, x, b, nullptr, 0.0, y, nullptr);
+  TG_LAUNCH_CHECK();
 }
 
 template void launch_fine_op<double>(int, const Grid&, const ModalConsts&, const double*,

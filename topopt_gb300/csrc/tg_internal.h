@@ -146,6 +146,11 @@ struct ModalConsts {
 // ---------------------------------------------------------------- operator
 enum ApplyMode { kApply = 0, kResidual = 1, kSmooth = 2 };
 
+// kResidual of the FP64 operator evaluated in double-float arithmetic (FP32
+// pairs, ~48 significant bits): the refinement residual of the mixed form.
+void launch_fine_residual_df(const Grid& g, const ModalConsts& c, const double* ef,
+                             const uint8_t* kept, const double* x, const double* b, double* y,
+                             cudaStream_t s);
 // Fine operator on the full grid, element factors `ef` (0 = no element):
 //   kApply:    y = M A x                 (M = kept mask; dot = sum x.y if dot_part)
 //   kResidual: y = M (b - A x)

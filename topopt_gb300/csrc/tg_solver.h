@@ -68,7 +68,8 @@ class Solver {
   void apply_unmasked(const double* E, const double* x, double* y);
   const double* rhs() const { return rhs_.p; }
   // Time `reps` fine-operator launches (FP64 or FP32) on the current factors.
-  double time_operator(bool fp32, int reps);
+  // form: 0 FP64, 1 FP32, 2 the double-float residual kernel.
+  double time_operator(int form, int reps);
   size_t device_bytes() const;
   int levels() const { return int(levels_.size()) + 1; }
 
@@ -98,6 +99,8 @@ class Solver {
   double omega_ = 0.6;
   int budget_ = 300;
   int sweeps_ = 1;  // damped-Jacobi sweeps per side of the coarse correction
+  bool df_residual_ = true;  // mixed: refinement residual in double-float arithmetic
+  void refinement_residual();  // r = b - A x (FP64 in, FP64 out) for the mixed loop
   bool mixed_ = false;
   // fine state
   const double* E_ = nullptr;
