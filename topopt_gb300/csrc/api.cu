@@ -259,7 +259,9 @@ int projected_candidates(int64_t nv) {
 }
 
 struct OcState {
-  DBuf<double> dcf, dvf, xp, sq, lo, hi, vpart, vsum;
+  // sq, lo, hi and dvd carry double-float pairs for the fast volume pass (the
+  // projected update reuses sq and lo as FP64 scratch).
+  DBuf<double> dcf, dvf, xp, sq, lo, hi, dvd, vpart, vsum;
   int fast_evals = 0, exact_evals = 0;
   double radius = 1.5;
   DBuf<uint64_t> part, total;
@@ -279,7 +281,7 @@ struct OcState {
     cand.alloc(size_t(kproj) * size_t(g.nv));
   }
   void init(const Grid& g, cudaStream_t) {
-    for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi}) d->alloc(size_t(g.nv));
+    for (DBuf<double>* d : {&dcf, &dvf, &xp, &sq, &lo, &hi, &dvd}) d->alloc(size_t(g.nv));
     vpart.alloc(size_t(kRedBlocks) * kOcMulti);
     vsum.alloc(kOcMulti);
     h_v = static_cast<double*>(pinned_scalars(kOcMulti * sizeof(double)));
@@ -294,7 +296,7 @@ struct OcState {
   }
   size_t bytes() const {
     return dcf.bytes() + dvf.bytes() + xp.bytes() + sq.bytes() + lo.bytes() + hi.bytes() +
-           vpart.bytes() + vsum.bytes() + part.bytes() + total.bytes() + inexact.bytes() +
+           dvd.bytes() + vpart.bytes() + vsum.bytes() + part.bytes() + total.bytes() + inexact.bytes() +
            cand.bytes();
   }
 };
@@ -355,12 +357,17 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
                       double volfrac, double move, double rho_min, double* xnew, cudaStream_t s) {
   fs.adj(g, act, dc, oc.dcf.p, s);
   const double target = volfrac * double(oc.n_solid);
-  launch_oc_prepare(x, oc.dcf.p, oc.dvf.p, act, g.nv, move, rho_min, oc.sq.p, oc.lo.p, oc.hi.p, s);
+  launch_oc_prepare(x, oc.dcf.p, oc.dvf.p, act, g.nv, move, rho_min, oc.sq.p, oc.lo.p, oc.hi.p,
+                    oc.dvd.p, s);
   const double u = std::ldexp(1.0, -53);
   const double n = double(std::max<int64_t>(oc.n_solid, 1));
   const double m = double(fs.st.n);
+  // + 8192 u: the fast pass runs in double-float arithmetic -- the split of its
+  // four FP64 inputs (2^-49 each), the product, clamp and accumulation (~2^-46
+  // relative per operation over a per-thread run of a few dozen terms) -- far
+  // below the n u of the reference's own sequential sum.
   const double eps =
-      (n + 2.0 * (m + 1.0) + 12.0 + n / (double(kRedBlocks) * 256.0) + 64.0) * u * 1.01;
+      (n + 2.0 * (m + 1.0) + 12.0 + n / (double(kRedBlocks) * 256.0) + 64.0 + 8192.0) * u * 1.01;
   // Fast volumes are computed ahead, kmax lambdas per pass over the fields: the
   // next doublings while bracketing, the next levels of the bisection tree
   // (breadth first) while bisecting.  Every branch is still decided one at a
@@ -383,7 +390,7 @@ void oc_update_device(OcState& oc, FilterState& fs, const Grid& g, const uint8_t
     OcCands cs;
     cs.k = int(std::min<size_t>(lams.size(), size_t(kmax)));
     for (int k = 0; k < cs.k; ++k) cs.c[k] = 1.0 / std::sqrt(lams[size_t(k)]);
-    launch_oc_volume_multi(oc.sq.p, oc.lo.p, oc.hi.p, oc.dvf.p, g.nv, cs, oc.vpart.p, oc.vsum.p,
+    launch_oc_volume_multi(oc.sq.p, oc.lo.p, oc.hi.p, oc.dvd.p, g.nv, cs, oc.vpart.p, oc.vsum.p,
                            s);
     TG_CUDA(cudaMemcpyAsync(oc.h_v, oc.vsum.p, sizeof(double) * cs.k, cudaMemcpyDeviceToHost, s));
     TG_CUDA(cudaStreamSynchronize(s));

@@ -21,6 +21,7 @@
 
 #include <cmath>
 
+#include "tg_df.h"
 #include "tg_internal.h"
 
 namespace tg {
@@ -353,53 +354,63 @@ __global__ void k_mask_pins(const uint8_t* __restrict__ eff, int64_t n, double* 
 // certified error bound (api.cu); x_new itself always comes from k_oc_candidate.
 __global__ void k_oc_prepare(const double* __restrict__ x, const double* __restrict__ dcf,
                              const double* __restrict__ dvf, const uint8_t* __restrict__ act,
-                             int64_t n, double move, double rho_min, double* __restrict__ sq,
-                             double* __restrict__ lo, double* __restrict__ hi) {
+                             int64_t n, double move, double rho_min, df* __restrict__ sq,
+                             df* __restrict__ lo, df* __restrict__ hi, df* __restrict__ dvd) {
   for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
        e += int64_t(gridDim.x) * kThreads) {
-    double s = 0.0, l = 0.0, h = 0.0;
+    double s = 0.0, l = 0.0, h = 0.0, d = 0.0;
     if (act[e]) {
       const double xe = x[e];
+      d = dvf[e];
       double be = 0.0;
-      if (dvf[e] > 0.0) be = -dcf[e] / dvf[e];
+      if (d > 0.0) be = -dcf[e] / d;
       if (be < 0.0) be = 0.0;
       s = xe * sqrt(be);
       const double xm = xe - move, xp = xe + move;
       l = (rho_min < xm) ? xm : rho_min;
       h = (xp < 1.0) ? xp : 1.0;
     }
-    sq[e] = s;
-    lo[e] = l;
-    hi[e] = h;
+    sq[e] = df_from(s);
+    lo[e] = df_from(l);
+    hi[e] = df_from(h);
+    dvd[e] = df_from(d);
   }
 }
 
+// Double-float comparison of normalised pairs (|lo| <= ulp(hi) / 2): exact.
+__device__ __forceinline__ bool df_less(df a, df b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+
 // The linear volume sum_e dv_e clamp(sq_e c, lo_e, hi_e) for up to kOcMulti
-// candidates c = 1/sqrt(lambda) in one pass over the fields (each candidate
-// summed in a fixed per-thread order and tree).
+// candidates c = 1/sqrt(lambda) in one pass over the fields, in double-float
+// arithmetic on the FP32 pipe (tg_df.h; ~2^-46 relative per operation, all
+// terms positive), each candidate summed in a fixed per-thread order, then the
+// FP64 trees.  These volumes only decide bisection branches under a certified
+// bound that includes this arithmetic's error.
 template <int K>
 __global__ void __launch_bounds__(kThreads) k_oc_volume_multi(
-    const double* __restrict__ sq, const double* __restrict__ lo, const double* __restrict__ hi,
-    const double* __restrict__ dvf, int64_t n, OcCands cs, double* __restrict__ part) {
-  double acc[K];
+    const df* __restrict__ sq, const df* __restrict__ lo, const df* __restrict__ hi,
+    const df* __restrict__ dvd, int64_t n, OcCandsDF cs, double* __restrict__ part) {
+  df acc[K];
 #pragma unroll
-  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (int k = 0; k < K; ++k) acc[k] = df(0.0f, 0.0f);
   for (int64_t e = blockIdx.x * int64_t(kThreads) + threadIdx.x; e < n;
        e += int64_t(gridDim.x) * kThreads) {
-    const double s = sq[e], l = lo[e], h = hi[e], d = dvf[e];
+    const df s = sq[e], l = lo[e], h = hi[e], d = dvd[e];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       if (k >= cs.k) break;
-      double xt = s * cs.c[k];
-      xt = xt < l ? l : xt;
-      xt = xt > h ? h : xt;
-      acc[k] += d * xt;
+      df xt = s * cs.c[k];
+      xt = df_less(xt, l) ? l : xt;
+      xt = df_less(h, xt) ? h : xt;
+      acc[k] = acc[k] + d * xt;
     }
   }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     if (k >= cs.k) break;  // cs.k is uniform over the block
-    const double v = block_sum256(acc[k]);
+    const double v = block_sum256(df_to_double(acc[k]));
     if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = v;
   }
 }
@@ -947,12 +958,20 @@ void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t
 int exact_sum_blocks() { return kRedBlocks; }
 
 void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi,
-                            const double* dvf, int64_t n, const OcCands& cs, double* part,
+                            const double* dvd, int64_t n, const OcCands& cs, double* part,
                             double* out, cudaStream_t s) {
+  // sq, lo, hi, dvd hold double-float pairs (written by launch_oc_prepare).
+  OcCandsDF cd;
+  cd.k = cs.k;
+  for (int k = 0; k < kOcMulti; ++k) cd.c[k] = df_from(k < cs.k ? cs.c[k] : 0.0);
+  const df* a = reinterpret_cast<const df*>(sq);
+  const df* l = reinterpret_cast<const df*>(lo);
+  const df* h = reinterpret_cast<const df*>(hi);
+  const df* d = reinterpret_cast<const df*>(dvd);
   if (cs.k <= 4)
-    k_oc_volume_multi<4><<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, cs, part);
+    k_oc_volume_multi<4><<<kRedBlocks, kThreads, 0, s>>>(a, l, h, d, n, cd, part);
   else
-    k_oc_volume_multi<kOcMulti><<<kRedBlocks, kThreads, 0, s>>>(sq, lo, hi, dvf, n, cs, part);
+    k_oc_volume_multi<kOcMulti><<<kRedBlocks, kThreads, 0, s>>>(a, l, h, d, n, cd, part);
   TG_LAUNCH_CHECK();
   k_sum_partials_multi<<<cs.k, kThreads, 0, s>>>(part, kRedBlocks, out);
   TG_LAUNCH_CHECK();
@@ -960,8 +979,10 @@ void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi
 
 void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, const uint8_t* act,
                        int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
-                       cudaStream_t s) {
-  k_oc_prepare<<<grid_blocks(n), kThreads, 0, s>>>(x, dcf, dvf, act, n, move, rho_min, sq, lo, hi);
+                       double* dvd, cudaStream_t s) {
+  k_oc_prepare<<<grid_blocks(n), kThreads, 0, s>>>(
+      x, dcf, dvf, act, n, move, rho_min, reinterpret_cast<df*>(sq), reinterpret_cast<df*>(lo),
+      reinterpret_cast<df*>(hi), reinterpret_cast<df*>(dvd));
   TG_LAUNCH_CHECK();
 }
 

@@ -10,6 +10,8 @@
 
 #include <cuda_runtime.h>
 
+#include "tg_df.h"
+
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -235,9 +237,16 @@ struct OcCands {
   int k;
   double c[kOcMulti];
 };
-// out[k] = sum_e dvf_e clamp(sq_e c_k, lo_e, hi_e); part holds k * kRedBlocks partials.
+// The same candidates as double-float pairs (tg_df.h) for the device.
+struct OcCandsDF {
+  int k;
+  df c[kOcMulti];
+};
+// out[k] = sum_e dv_e clamp(sq_e c_k, lo_e, hi_e) in double-float arithmetic;
+// sq, lo, hi, dvd are the double-float fields launch_oc_prepare writes (8 bytes
+// per voxel each, in double-sized buffers); part holds k * kRedBlocks partials.
 void launch_oc_volume_multi(const double* sq, const double* lo, const double* hi,
-                            const double* dvf, int64_t n, const OcCands& cs, double* part,
+                            const double* dvd, int64_t n, const OcCands& cs, double* part,
                             double* out, cudaStream_t s);
 void launch_oc_candidate(const double* x, const double* dcf, const double* dvf,
                          const uint8_t* act, int64_t n, double lambda, double move,
@@ -292,9 +301,10 @@ void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t
 // Exact (fixed-point, order independent) sum of a non-negative field over the
 // solid voxels; returns per-block 192-bit partials, then the final total.
 int exact_sum_blocks();
+// sq = x sqrt(B), lo, hi (the move window) and dvd = dvf, as double-float pairs.
 void launch_oc_prepare(const double* x, const double* dcf, const double* dvf, const uint8_t* act,
                        int64_t n, double move, double rho_min, double* sq, double* lo, double* hi,
-                       cudaStream_t s);
+                       double* dvd, cudaStream_t s);
 void launch_exact_sum(const double* v, const uint8_t* act, int64_t n, uint64_t* part,
                       uint64_t* total, int* inexact, cudaStream_t s);
 double fma_probe_tflops(bool fp64);
