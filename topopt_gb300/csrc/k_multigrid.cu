@@ -516,14 +516,21 @@ __global__ void k_chol_update(double* __restrict__ D, int nc, int k0) {
 // Explicit inverse of the coarsest operator from its Cholesky factor, for small
 // coarsest levels: thread j forms column j of L^-1 by forward substitution, then
 // Ainv = L^-T L^-1 (both FP64).  Each V-cycle then needs one dense matvec.
+// Column j of L^-1 by forward substitution, one warp per column: the inner
+// product of row i of L with the column's entries above i is split over the
+// lanes and reduced by shuffles, so a column costs nc short steps instead of a
+// serial O(nc^2) chain (the factor and the column stay in L2).
 __global__ void k_chol_invert_L(const double* __restrict__ L, int nc, double* __restrict__ Li) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nc) return;
-  for (int i = 0; i < j; ++i) Li[int64_t(i) * nc + j] = 0.0;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (j >= nc) return;  // warp-uniform
+  for (int i = lane; i < j; i += 32) Li[int64_t(i) * nc + j] = 0.0;
   for (int i = j; i < nc; ++i) {
-    double v = (i == j) ? 1.0 : 0.0;
-    for (int k = j; k < i; ++k) v -= L[int64_t(i) * nc + k] * Li[int64_t(k) * nc + j];
-    Li[int64_t(i) * nc + j] = v / L[int64_t(i) * nc + i];
+    double part = 0.0;
+    for (int k = j + lane; k < i; k += 32) part += L[int64_t(i) * nc + k] * Li[int64_t(k) * nc + j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) Li[int64_t(i) * nc + j] = ((i == j ? 1.0 : 0.0) - part) / L[int64_t(i) * nc + i];
+    __syncwarp();  // the new entry is read by every lane from the next row on
   }
 }
 
@@ -682,7 +689,7 @@ void mg_cholesky(double* D, int nc, int* fail, cudaStream_t s) {
 }
 
 void mg_chol_inverse(const double* L, int nc, double* Li, double* Ainv, cudaStream_t s) {
-  k_chol_invert_L<<<(nc + 127) / 128, 128, 0, s>>>(L, nc, Li);
+  k_chol_invert_L<<<(nc + 3) / 4, 128, 0, s>>>(L, nc, Li);  // a warp per column
   TG_LAUNCH_CHECK();
   const dim3 grid((nc + 15) / 16, (nc + 15) / 16);
   k_chol_inverse<<<grid, dim3(16, 16), 0, s>>>(Li, nc, Ainv);

@@ -258,9 +258,18 @@ template <>
 struct Pencil<double> {
   static constexpr int PY = 8, KZ = 16, MINB = 2;
 };
+#ifndef TG_PENCIL_F32_PY
+#define TG_PENCIL_F32_PY 8
+#endif
+#ifndef TG_PENCIL_F32_KZ
+#define TG_PENCIL_F32_KZ 16
+#endif
+#ifndef TG_PENCIL_F32_MINB
+#define TG_PENCIL_F32_MINB 3
+#endif
 template <>
 struct Pencil<float> {
-  static constexpr int PY = 8, KZ = 16, MINB = 3;
+  static constexpr int PY = TG_PENCIL_F32_PY, KZ = TG_PENCIL_F32_KZ, MINB = TG_PENCIL_F32_MINB;
 };
 template <>
 struct Pencil<df> {
