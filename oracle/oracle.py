@@ -383,6 +383,92 @@ class OracleLib:
                     max_von_mises=od[1], max_interlayer=od[2], margin_in_plane=od[3],
                     margin_interlayer=od[4], margin_worst=od[5], margin_effective=od[6]), vm
 
+    def active_domain_auto_band(self, radius):
+        """active_domain_auto_band (simp.cpp:440-447)."""
+        return int(self._sig("active_domain_auto_band", [C.c_double])(radius))
+
+    def active_domain_mask(self, pb: Problem, density, rho_min, band):
+        """active_domain_mask (simp.cpp:449-528) on pb's tags (pb.solid)."""
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        out = np.zeros(pb.nv, np.uint8)
+        f = self._sig("active_domain_mask", [C.c_int] * 3 + [C.c_void_p, _dp, C.c_double,
+                                                             C.c_int, C.c_void_p])
+        self._check(f(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), d, rho_min, band,
+                      out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def active_domain_escape_count(self, pb: Problem, density, prev, rho_min):
+        """active_domain_escape_count (simp.cpp:530-556); prev None = no band yet."""
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        pm = None if prev is None else np.ascontiguousarray(prev, dtype=np.uint8)
+        if self.kind == "port":
+            f = self._sig("active_domain_escape_count",
+                          [C.c_int] * 3 + [C.c_void_p, _dp, C.c_void_p, C.c_double],
+                          C.c_longlong)
+            return int(f(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), d, self._ptr(pm), rho_min))
+        out = C.c_longlong(0)
+        f = self._sig("active_domain_escape_count",
+                      [C.c_int] * 3 + [C.c_void_p, _dp, C.c_void_p, C.c_double,
+                                       C.POINTER(C.c_longlong)])
+        self._check(f(pb.nx, pb.ny, pb.nz, self._ptr(pb.solid), d, self._ptr(pm), rho_min,
+                      C.byref(out)))
+        return int(out.value)
+
+    def simp_optimize_active(self, pb: Problem, band, mask=None, seed=None, E0=1.0, nu=0.3,
+                             penal=3.0, rho_min=1e-3, volfrac=0.3, radius=1.5, move=0.2,
+                             max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0):
+        """simp_optimize (OC; plain, or masked with mask) with
+        SimpOptions::active_domain_band = band and an optional warm-start seed:
+        the history with each iteration's active fraction, and the run's
+        active-domain record (finalize_active_domain, simp.cpp:1981-1988)."""
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        sd = None if seed is None else np.ascontiguousarray(seed, dtype=np.float64)
+        hc, hch, hvf, haf = (np.zeros(max_it) for _ in range(4))
+        design, phys = np.zeros(pb.nv), np.zeros(pb.nv)
+        if self.kind == "reference":
+            sc, ints = np.zeros(4), np.zeros(8, np.int64)
+            reason = C.create_string_buffer(256)
+            f = self._sig("simp_optimize_active",
+                          [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p] +
+                          [C.c_double] * 4 + [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp] +
+                          [C.c_double] * 3 + [C.c_int, C.c_double, C.c_double, C.c_int,
+                                              C.c_int, C.c_void_p] + [_dp] * 7 +
+                          [C.c_void_p, C.c_char_p])
+            self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(m), E0, nu,
+                          penal, rho_min, *pb.bc_args(), volfrac, radius, move, max_it,
+                          change_tol, cg_tol, cg_max_it, band, self._ptr(sd), hc, hch, hvf, haf,
+                          design, phys, sc, ints.ctypes.data_as(C.c_void_p), reason))
+            n = int(ints[0])
+            return dict(compliance=sc[0], volume_fraction=sc[1], initial_compliance=sc[2],
+                        iterations=n, converged=bool(ints[1]), non_convergent=bool(ints[2]),
+                        infeasible=bool(ints[3]), hist_c=hc[:n], hist_change=hch[:n],
+                        hist_vf=hvf[:n], hist_af=haf[:n], design=design, phys=phys,
+                        band=int(ints[4]), latched=bool(ints[5]), latch_iteration=int(ints[6]),
+                        escape_count=int(ints[7]), fraction_mean=sc[3],
+                        reason=reason.value.decode())
+        opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, 0,
+                             None, None, None, 0.5, self._ptr(sd), 0, 0, 0.0, 0.0, 0, band,
+                             haf.ctypes.data_as(C.c_void_p))
+        res = _OrSimpResult()
+        hcg = np.zeros(max_it, np.int32)
+        if m is None:
+            self._check(self.lib.or_simp_optimize(
+                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                *pb.bc_args(), C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        else:
+            self._check(self.lib.or_simp_optimize_masked(
+                pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), m, E0, nu, penal, rho_min,
+                *pb.bc_args(), C.byref(opt), hc, hch, hvf, hcg, design, phys, C.byref(res)))
+        n = res.iterations
+        return dict(compliance=res.compliance, volume_fraction=res.volume_fraction,
+                    initial_compliance=res.initial_compliance, iterations=n,
+                    converged=bool(res.converged), non_convergent=bool(res.non_convergent),
+                    infeasible=bool(res.infeasible), hist_c=hc[:n], hist_change=hch[:n],
+                    hist_vf=hvf[:n], hist_af=haf[:n], hist_cg=hcg[:n], design=design, phys=phys,
+                    band=res.ad_band, latched=bool(res.ad_latched),
+                    latch_iteration=res.ad_latch_iteration, escape_count=res.ad_escape_count,
+                    fraction_mean=res.ad_fraction_mean, reason=res.ad_latch_reason.decode())
+
     def simp_optimize_mma(self, pb: Problem, mask=None, E0=1.0, nu=0.3, penal=3.0,
                           rho_min=1e-3, volfrac=0.3, radius=1.5, move=0.2, max_it=50,
                           change_tol=0.01, cg_tol=1e-8, cg_max_it=0, plateau_window=10,
@@ -665,7 +751,8 @@ class _OrSimpOptions(C.Structure):
                 ("stage_iterations", C.c_void_p), ("eta", C.c_double),
                 ("initial_design", C.c_void_p), ("updater", C.c_int),
                 ("mma_plateau_window", C.c_int), ("mma_plateau_tol", C.c_double),
-                ("mma_plateau_min_drop", C.c_double), ("mma_plateau_flat_windows", C.c_int)]
+                ("mma_plateau_min_drop", C.c_double), ("mma_plateau_flat_windows", C.c_int),
+                ("active_domain_band", C.c_int), ("hist_active_fraction", C.c_void_p)]
 
 
 class _OrAnalysis(C.Structure):
@@ -710,7 +797,10 @@ def _stage_arrays(stages):
 class _OrSimpResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("non_convergent", C.c_int),
                 ("infeasible", C.c_int), ("compliance", C.c_double),
-                ("volume_fraction", C.c_double), ("initial_compliance", C.c_double)]
+                ("volume_fraction", C.c_double), ("initial_compliance", C.c_double),
+                ("ad_band", C.c_int), ("ad_latched", C.c_int), ("ad_latch_iteration", C.c_int),
+                ("ad_escape_count", C.c_longlong), ("ad_fraction_mean", C.c_double),
+                ("ad_latch_reason", C.c_char * 256)]
 
 
 def cantilever(nx, ny, nz, total_load=-1.0, spacing=1.0, solid=None):
@@ -766,3 +856,58 @@ def gate_v2_metrics(nx, ny, nz, rho):
     mnd = float(np.mean(4.0 * r * (1.0 - r)))
     ysym = float(np.abs(r - r[:, ::-1, :]).max())
     return int(ncomp), mnd, ysym
+
+
+# Active-domain cases (SimpOptions::active_domain_band, simp.cpp:1745-1896): a
+# warm-start seed with a thin beam from the clamped face to the loaded edge, so
+# that most of the box sits at the density floor and the band excludes it.
+def beam_seed(nx, ny, nz, half_width=2, floor=1e-3):
+    """Seed density: 1 on a (2*half_width)^2 beam along x through the box centre
+    and on a two-voxel plate under the loaded edge (x = nx-2..nx-1, z around the
+    middle, every y), `floor` elsewhere."""
+    s = np.full((nz, ny, nx), floor)
+    zc, yc, w = nz // 2, ny // 2, half_width
+    s[zc - w:zc + w, yc - w:yc + w, :] = 1.0
+    s[zc - 1:zc + 1, :, nx - 2:] = 1.0
+    return s.ravel()
+
+
+# name: (nx, ny, nz, masked, seed (half_width, floor) or None, band, radius,
+#        volfrac, iterations) -- each run at move 0.2, change_tol 0, cg 1e-9.
+ACTIVE_DOMAIN_RUNS = {
+    "restricted": (32, 16, 16, False, (2, 1e-3), -1, 1.5, 0.05, 20),
+    "masked": (32, 16, 16, True, (2, 1e-3), -1, 1.5, 0.05, 10),
+    "escape": (24, 12, 12, False, (1, 1e-6), 1, 2.5, 0.1, 10),
+    "failed": (16, 6, 6, False, "plate", 1, 1.5, 0.2, 6),
+    "latch": (12, 4, 4, False, None, -1, 1.5, 0.3, 12),
+}
+
+
+def active_domain_case(name):
+    """(Problem, mask or None, seed or None, band, radius, volfrac, iterations) of
+    one ACTIVE_DOMAIN_RUNS entry.  The masked box has a Fixture slab at x = 0,
+    Load voxels under the loaded edge, a FrozenVoid keep-out block and a
+    FrozenSolid insert on the beam.  The "failed" seed puts material only near
+    the clamped face, so band 1 leaves the loaded edge void and the restricted
+    system fails the void-load gate."""
+    nx, ny, nz, masked, sd, band, radius, vf, its = ACTIVE_DOMAIN_RUNS[name]
+    mask = None
+    tags = None
+    if masked:
+        t = np.ones((nz, ny, nx), np.uint8)
+        t[:, :, 0] = 5
+        t[nz // 2 - 1:nz // 2 + 1, :, nx - 1] = 4
+        m = np.zeros((nz, ny, nx), np.uint8)
+        m[2:6, 2:6, 10:16] = 2
+        m[nz // 2 - 1:nz // 2 + 1, ny // 2 - 1:ny // 2 + 1, 20:24] = 1
+        tags, mask = t.ravel(), m.ravel()
+    pb = cantilever(nx, ny, nz, solid=tags)
+    if sd is None:
+        seed = None
+    elif sd == "plate":
+        seed = np.full((nz, ny, nx), 1e-3)
+        seed[:, :, :5] = 1.0
+        seed = seed.ravel()
+    else:
+        seed = beam_seed(nx, ny, nz, sd[0], sd[1])
+    return pb, mask, seed, band, radius, vf, its

@@ -771,4 +771,95 @@ int ref_simp_optimize_mma(int nx, int ny, int nz, double h, const uint8_t* tags,
     out_ints[3] = r.infeasible ? 1 : 0;
   });
 }
+
+// active_domain_auto_band / active_domain_mask / active_domain_escape_count.
+int ref_active_domain_auto_band(double radius) { return active_domain_auto_band(radius); }
+
+int ref_active_domain_mask(int nx, int ny, int nz, const uint8_t* tags, const double* density,
+                           double rho_min, int band, uint8_t* out) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, 1.0, tags);
+    const std::vector<double> d(density, density + g.voxel_count());
+    const std::vector<char> m = active_domain_mask(g, d, rho_min, band);
+    for (std::size_t e = 0; e < m.size(); ++e) out[e] = static_cast<uint8_t>(m[e]);
+  });
+}
+
+int ref_active_domain_escape_count(int nx, int ny, int nz, const uint8_t* tags,
+                                   const double* density, const uint8_t* prev, double rho_min,
+                                   long long* out) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, 1.0, tags);
+    const std::vector<double> d(density, density + g.voxel_count());
+    std::vector<char> pm;
+    if (prev) pm.assign(prev, prev + g.voxel_count());
+    *out = active_domain_escape_count(g, d, pm, rho_min);
+  });
+}
+
+// simp_optimize (OC, MultigridCG_Matfree, plain when mask is NULL) with
+// options.active_domain_band = band and an optional warm-start seed; the
+// per-iteration active fraction comes from the observe hook.
+// out_ints: iterations, converged, non_convergent, infeasible, band, latched,
+// latch_iteration, escape_count.  out_scalars: compliance, vf, init_c,
+// active_fraction_mean.  reason: 256 bytes.
+int ref_simp_optimize_active(int nx, int ny, int nz, double h, const uint8_t* tags,
+                             const uint8_t* mask, double E0, double nu, double penal,
+                             double rho_min, int nbc, const int* bc_node, const int* bc_comp,
+                             const double* bc_val, int nload, const int* ld_node,
+                             const int* ld_comp, const double* ld_val, double volfrac,
+                             double radius, double move, int max_it, double change_tol,
+                             double cg_tol, int cg_max_it, int band, const double* seed,
+                             double* hist_c, double* hist_change, double* hist_vf,
+                             double* hist_af, double* design, double* phys,
+                             double* out_scalars, long long* out_ints, char* reason) {
+  return guarded([&] {
+    const VoxelGrid g = make_grid_tags(nx, ny, nz, h, tags);
+    SimpParams p;
+    p.youngs_modulus = E0;
+    p.poisson = nu;
+    p.penalty = penal;
+    p.density_min = rho_min;
+    SimpOptions o;
+    o.volume_fraction = volfrac;
+    o.filter_radius = radius;
+    o.move = move;
+    o.max_iterations = max_it;
+    o.change_tol = change_tol;
+    o.cg_tolerance = cg_tol;
+    o.cg_max_iterations = cg_max_it;
+    o.solver = SolverKind::MultigridCG_Matfree;
+    o.active_domain_band = band;
+    if (seed) o.initial_design.assign(seed, seed + g.voxel_count());
+    std::vector<double> af;
+    o.observe = [&](const SimpIterationObservation& ob) { af.push_back(ob.active_fraction); };
+    const auto bcs = make_bcs(nbc, bc_node, bc_comp, bc_val);
+    const auto loads = make_loads(nload, ld_node, ld_comp, ld_val);
+    const SimpOptimizeResult r =
+        mask ? simp_optimize(g, p, bcs, loads, o, make_mask(g.voxel_count(), mask))
+             : simp_optimize(g, p, bcs, loads, o);
+    for (std::size_t i = 0; i < r.history.size(); ++i) {
+      hist_c[i] = r.history[i].compliance;
+      hist_change[i] = r.history[i].change;
+      hist_vf[i] = r.history[i].volume_fraction;
+    }
+    for (std::size_t i = 0; i < af.size(); ++i) hist_af[i] = af[i];
+    std::memcpy(design, r.design.data(), r.design.size() * sizeof(double));
+    std::memcpy(phys, r.physical_density.data(), r.physical_density.size() * sizeof(double));
+    out_scalars[0] = r.compliance;
+    out_scalars[1] = r.volume_fraction;
+    out_scalars[2] = r.initial_compliance;
+    out_scalars[3] = r.active_fraction_mean;
+    out_ints[0] = r.iterations;
+    out_ints[1] = r.converged ? 1 : 0;
+    out_ints[2] = r.non_convergent ? 1 : 0;
+    out_ints[3] = r.infeasible ? 1 : 0;
+    out_ints[4] = r.active_domain_band;
+    out_ints[5] = r.active_domain_latched ? 1 : 0;
+    out_ints[6] = r.active_domain_latch_iteration;
+    out_ints[7] = r.active_domain_escape_count;
+    std::memset(reason, 0, 256);
+    std::strncpy(reason, r.active_domain_latch_reason.c_str(), 255);
+  });
+}
 }  // extern "C"

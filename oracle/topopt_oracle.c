@@ -263,14 +263,14 @@ static int build_reduced(red_sys* m, int nbc, const int* bc_node, const int* bc_
         rmax = fmax(rmax, fabs(f[d]));
       }
     if (nf > 0 && ntouched == 0) {
-      st = fail(OR_ESINGULAR, "singular system (no stiffness - every free DOF is void)");
+      st = fail(OR_ESINGULAR, "singular system (no stiffness \xe2\x80\x94 every free DOF is void)");
       goto out;
     }
     const double load_tol = 1e-9 * rmax;
     for (size_t d = 0; d < ndof; ++d)
       if (!fixed[d] && !touched[d] && fabs(f[d]) > load_tol) {
-        st = fail(OR_ESINGULAR,
-                  "under-constrained system (load applied to a void DOF with no stiffness)");
+        st = fail(OR_ESINGULAR, "under-constrained system (load applied to a void DOF with no "
+                                "stiffness \xe2\x80\x94 no equilibrium possible)");
         goto out;
       }
   }
@@ -407,7 +407,9 @@ done:
   *iters_out = it;
   *err_out = err;
   free(r); free(p); free(z); free(t);
-  return converged ? OR_OK : fail(OR_ENONCONV, "CG did not reach the requested tolerance");
+  return converged ? OR_OK
+                   : fail(OR_ENONCONV,
+                          "CG did not reach the requested tolerance within max_iterations");
 }
 
 int or_solve_cg(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
@@ -1023,6 +1025,158 @@ static void mask_pins(const uint8_t* eff, size_t nv, double* xphys) {
  * (simp.cpp:2989-3640) otherwise: the effective mask, the Active-only filter,
  * the analysis grid without FrozenVoid voxels, pins after every filter pass and
  * the Active budget. */
+/* --------------------------------------------------------- active domain */
+/* active_domain_auto_band (simp.cpp:440-447): ceil(rmin) + 1, 1 for a degenerate
+ * radius. */
+int or_active_domain_auto_band(double filter_radius) {
+  if (!isfinite(filter_radius) || filter_radius <= 0.0) return 1;
+  const int k = (int)ceil(filter_radius) + 1;
+  return k < 1 ? 1 : k;
+}
+
+/* One axis of the Chebyshev dilation (simp.cpp:487-516): out is 1 where a set
+ * voxel of `in` lies on the same axis line within `band`.  Evaluated with a
+ * running count per line; the set is the reference's window scan. */
+static void ad_dilate(int nx, int ny, int nz, int axis, int band, const uint8_t* in,
+                      uint8_t* out, int* pre) {
+  const int n[3] = {nx, ny, nz};
+  const size_t st[3] = {1, (size_t)nx, (size_t)nx * ny};
+  const int a1 = (axis + 1) % 3, a2 = (axis + 2) % 3, len = n[axis];
+  const int b = band > len ? len : band;
+  for (int q = 0; q < n[a2]; ++q)
+    for (int p = 0; p < n[a1]; ++p) {
+      const size_t base = (size_t)p * st[a1] + (size_t)q * st[a2];
+      pre[0] = 0;
+      for (int t = 0; t < len; ++t) pre[t + 1] = pre[t] + (in[base + (size_t)t * st[axis]] != 0);
+      for (int t = 0; t < len; ++t) {
+        const int lo = t - b < 0 ? 0 : t - b, hi = t + b > len - 1 ? len - 1 : t + b;
+        out[base + (size_t)t * st[axis]] = (uint8_t)(pre[hi + 1] - pre[lo] > 0);
+      }
+    }
+}
+
+/* active_domain_mask (simp.cpp:449-528).  tags NULL: every voxel Interior. */
+int or_active_domain_mask(int nx, int ny, int nz, const uint8_t* tags, const double* density,
+                          double density_min, int band, uint8_t* out) {
+  const size_t nv = (size_t)nx * ny * nz;
+  if (band <= 0) {
+    for (size_t e = 0; e < nv; ++e) out[e] = (uint8_t)is_solid(tags, e);
+    return OR_OK;
+  }
+  const double thresh = 1.5 * density_min;
+  uint8_t* m = calloc(nv, 1);
+  uint8_t* t = calloc(nv, 1);
+  int nmax = nx > ny ? nx : ny;
+  if (nz > nmax) nmax = nz;
+  int* pre = malloc((size_t)(nmax + 1) * sizeof(int));
+  for (size_t e = 0; e < nv; ++e)
+    m[e] = (uint8_t)(is_solid(tags, e) &&
+                     (density[e] > thresh || (tags && (tags[e] == 4 || tags[e] == 5))));
+  ad_dilate(nx, ny, nz, 0, band, m, t, pre);
+  ad_dilate(nx, ny, nz, 1, band, t, m, pre);
+  ad_dilate(nx, ny, nz, 2, band, m, t, pre);
+  for (size_t e = 0; e < nv; ++e) out[e] = (uint8_t)(t[e] && is_solid(tags, e));
+  free(m); free(t); free(pre);
+  return OR_OK;
+}
+
+/* active_domain_escape_count (simp.cpp:530-556). */
+long long or_active_domain_escape_count(int nx, int ny, int nz, const uint8_t* tags,
+                                        const double* density, const uint8_t* prev_mask,
+                                        double density_min) {
+  if (prev_mask == NULL) return 0;
+  const size_t nv = (size_t)nx * ny * nz;
+  const double thresh = 1.5 * density_min;
+  long long n = 0;
+  for (size_t e = 0; e < nv; ++e)
+    if (is_solid(tags, e) && prev_mask[e] == 0 && density[e] > thresh) ++n;
+  return n;
+}
+
+/* The run's active-domain state (ActiveDomainRun, simp.cpp:1745-1766). */
+typedef struct {
+  int band, latched, latch_iteration, hot_streak, have_prev;
+  long long escape_count;
+  double fraction_sum;
+  long long fraction_count;
+  char reason[256];
+  uint8_t *prev, *mask, *rsolid;
+} ad_run;
+
+/* One trajectory solve under the active domain (active_domain_solve,
+ * simp.cpp:1809-1896): the escape latch, the restricted solve on solid AND mask,
+ * the fraction latch (0.85 for 5 iterations, simp.hpp:363-364), and on a failed
+ * restricted solve the latch plus a full-domain re-solve.  *af receives the
+ * active fraction (1 on the full domain). */
+static int ad_solve(ad_run* ad, int nx, int ny, int nz, double h, const uint8_t* atags,
+                    const uint8_t* asolid, double n_solid, int iteration, double E0, double nu,
+                    double penal, double rho_min, const double* xphys, int nbc,
+                    const int* bc_node, const int* bc_comp, const double* bc_val, int nload,
+                    const int* ld_node, const int* ld_comp, const double* ld_val, double tol,
+                    int max_it, double* u, double* dc, double* c, int* cgit, double* resid,
+                    double* af) {
+  const size_t nv = (size_t)nx * ny * nz;
+  *af = 1.0;
+  if (ad->band > 0 && !ad->latched) {
+    const long long esc = or_active_domain_escape_count(nx, ny, nz, atags, xphys,
+                                                        ad->have_prev ? ad->prev : NULL, rho_min);
+    if (esc > 0) {
+      ad->latched = 1;
+      ad->latch_iteration = iteration;
+      ad->escape_count = esc;
+      snprintf(ad->reason, sizeof ad->reason,
+               "escape detected: %lld element(s) took material outside the active band "
+               "(growth invariant failed); mask disabled, full domain restored",
+               esc);
+      ad->fraction_sum += 1.0;
+      ++ad->fraction_count;
+    } else {
+      or_active_domain_mask(nx, ny, nz, atags, xphys, rho_min, ad->band, ad->mask);
+      long long active = 0;
+      for (size_t e = 0; e < nv; ++e) {
+        active += ad->mask[e] ? 1 : 0;
+        ad->rsolid[e] = (uint8_t)(is_solid(asolid, e) && ad->mask[e]);
+      }
+      const double fraction = n_solid > 0.0 ? (double)active / n_solid : 1.0;
+      const int st = or_simp_compliance(nx, ny, nz, h, ad->rsolid, E0, nu, penal, rho_min, xphys,
+                                        nbc, bc_node, bc_comp, bc_val, nload, ld_node, ld_comp,
+                                        ld_val, tol, max_it, u, dc, c, cgit, resid);
+      if (st == OR_OK) {
+        *af = fraction;
+        ad->fraction_sum += fraction;
+        ++ad->fraction_count;
+        if (fraction >= 0.85) {
+          if (++ad->hot_streak >= 5) {
+            ad->latched = 1;
+            ad->latch_iteration = iteration;
+            snprintf(ad->reason, sizeof ad->reason,
+                     "active fraction >= %.2f for %d consecutive iterations (band covers the "
+                     "domain and buys nothing)",
+                     0.85, 5);
+          }
+        } else {
+          ad->hot_streak = 0;
+        }
+        memcpy(ad->prev, ad->mask, nv);
+        ad->have_prev = 1;
+        return OR_OK;
+      }
+      ad->latched = 1;
+      ad->latch_iteration = iteration;
+      snprintf(ad->reason, sizeof ad->reason,
+               "restricted solve failed: fea_solve_mgcg_matfree: %s", or_last_error());
+      ad->fraction_sum += 1.0;
+      ++ad->fraction_count;
+    }
+  } else if (ad->band > 0) {
+    ad->fraction_sum += 1.0;
+    ++ad->fraction_count;
+  }
+  return or_simp_compliance(nx, ny, nz, h, asolid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
+                            bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, tol, max_it, u, dc,
+                            c, cgit, resid);
+}
+
 static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
                        const uint8_t* mask, double E0, double nu, double penal, double rho_min,
                        int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
@@ -1117,6 +1271,27 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
   int st = OR_OK, stop = 0;
   or_mma_state mma = {NULL, NULL, NULL, NULL};
   int mma_iter = 0;
+  /* Active domain (resolve_active_domain_band, simp.cpp:1773-1782): < 0 is the
+   * auto band.  The mask sees the analysis grid's tags (the masked loop's
+   * FrozenVoid voxels are Empty there, simp.cpp:3251). */
+  ad_run ad;
+  memset(&ad, 0, sizeof ad);
+  ad.band = o->active_domain_band < 0 ? or_active_domain_auto_band(o->filter_radius)
+                                      : o->active_domain_band;
+  uint8_t* atags_buf = NULL;
+  const uint8_t* atags = solid;
+  double n_asolid = 0.0;
+  if (mask) {
+    atags_buf = malloc(nv);
+    for (size_t e = 0; e < nv; ++e) atags_buf[e] = analysis[e] ? (solid ? solid[e] : 1) : 0;
+    atags = atags_buf;
+  }
+  for (size_t e = 0; e < nv; ++e) n_asolid += is_solid(atags, e) ? 1.0 : 0.0;
+  if (ad.band > 0) {
+    ad.prev = malloc(nv);
+    ad.mask = malloc(nv);
+    ad.rsolid = malloc(nv);
+  }
   /* validate_updater_options (simp.cpp:83-88). */
   if (o->updater == 1 && o->nstages > 0) {
     st = fail(OR_EINVAL, "simp_optimize: MMA updater does not support a Heaviside projection "
@@ -1139,11 +1314,12 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
       or_filter_density(f, x, xphys);
       if (project) project_design(dset, nv, xphys, beta, o->eta);
       if (mask) mask_pins(eff, nv, xphys);
-      double c = 0.0, resid = 0.0;
+      double c = 0.0, resid = 0.0, af = 1.0;
       int cgit = 0;
-      st = or_simp_compliance(nx, ny, nz, h, asolid, E0, nu, penal, rho_min, xphys, nbc, bc_node,
-                              bc_comp, bc_val, nload, ld_node, ld_comp, ld_val, o->cg_tolerance,
-                              o->cg_max_iterations, u, dc, &c, &cgit, &resid);
+      st = ad_solve(&ad, nx, ny, nz, h, atags, asolid, n_asolid, res->iterations + 1, E0, nu,
+                    penal, rho_min, xphys, nbc, bc_node, bc_comp, bc_val, nload, ld_node, ld_comp,
+                    ld_val, o->cg_tolerance, o->cg_max_iterations, u, dc, &c, &cgit, &resid, &af);
+      if (o->hist_active_fraction) o->hist_active_fraction[res->iterations] = af;
       if (st == OR_ENONCONV) {
         res->non_convergent = 1;
         st = OR_OK;
@@ -1220,7 +1396,16 @@ static int simp_common(int nx, int ny, int nz, double h, const uint8_t* solid,
     }
   }
   res->volume_fraction = n_design > 0.0 ? vol_final / n_design : 0.0;
+  /* finalize_active_domain (simp.cpp:1981-1988). */
+  res->ad_band = ad.band;
+  res->ad_latched = ad.latched;
+  res->ad_latch_iteration = ad.latch_iteration;
+  res->ad_escape_count = ad.escape_count;
+  res->ad_fraction_mean =
+      ad.fraction_count > 0 ? ad.fraction_sum / (double)ad.fraction_count : 1.0;
+  memcpy(res->ad_latch_reason, ad.reason, sizeof ad.reason);
 out:
+  free(ad.prev); free(ad.mask); free(ad.rsolid); free(atags_buf);
   free(mma.low); free(mma.upp); free(mma.xold1); free(mma.xold2);
   free(x); free(xphys); free(xnew); free(dc); free(u);
   free(eff); free(active); free(analysis);

@@ -146,6 +146,11 @@ typedef struct {
   int mma_plateau_window;
   double mma_plateau_tol, mma_plateau_min_drop;
   int mma_plateau_flat_windows;
+  /* Active domain (SimpOptions::active_domain_band, simp.hpp:1185-1227): 0 off,
+   * > 0 the band, < 0 the auto band.  hist_active_fraction (output, may be NULL)
+   * receives each iteration's active fraction (1 on the full domain). */
+  int active_domain_band;
+  double* hist_active_fraction;
 } or_simp_options;
 
 /* The MMA state across one run (MmaJointState): asymptotes and the last two
@@ -164,6 +169,17 @@ int or_mma_update(int nx, int ny, int nz, const uint8_t* design, const or_filter
 int or_mma_objective_plateau(const double* c, int n, int window, double rel_tol, double min_drop,
                              int min_flat_windows);
 
+/* The active domain: active_domain_auto_band (simp.cpp:440-447),
+ * active_domain_mask (simp.cpp:449-528; tags NULL = every voxel Interior, Load 4
+ * and Fixture 5 are pinned active), active_domain_escape_count
+ * (simp.cpp:530-556; prev_mask NULL = 0). */
+int or_active_domain_auto_band(double filter_radius);
+int or_active_domain_mask(int nx, int ny, int nz, const uint8_t* tags, const double* density,
+                          double density_min, int band, uint8_t* out);
+long long or_active_domain_escape_count(int nx, int ny, int nz, const uint8_t* tags,
+                                        const double* density, const uint8_t* prev_mask,
+                                        double density_min);
+
 /* heaviside_project and its derivative (simp.cpp:352-365). */
 double or_heaviside_project(double rt, double beta, double eta);
 double or_heaviside_project_derivative(double rt, double beta, double eta);
@@ -175,6 +191,11 @@ int or_oc_update_projected(int nx, int ny, int nz, const uint8_t* solid, const o
 typedef struct {
   int iterations, converged, non_convergent, infeasible;
   double compliance, volume_fraction, initial_compliance;
+  /* finalize_active_domain (simp.cpp:1981-1988). */
+  int ad_band, ad_latched, ad_latch_iteration;
+  long long ad_escape_count;
+  double ad_fraction_mean;
+  char ad_latch_reason[256];
 } or_simp_result;
 int or_simp_optimize(int nx, int ny, int nz, double h, const uint8_t* solid,
                      double E0, double nu, double penal, double rho_min,

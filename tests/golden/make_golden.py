@@ -18,8 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
 
-from oracle.oracle import (CONTINUATION, GATE_V2, OracleLib, Problem, build_reference,  # noqa: E402
-                           cantilever, gate_v2_problem)
+from oracle.oracle import (ACTIVE_DOMAIN_RUNS, CONTINUATION, GATE_V2, OracleLib,  # noqa: E402
+                           Problem, active_domain_case, build_reference, cantilever,
+                           gate_v2_problem)
 
 REF_KE_JSON = "/root/reference/core/tests/fixtures/fea/hex_stiffness_reference.json"
 BENCH_JSON = "/root/reference/core/tests/fixtures/benchmarks.json"
@@ -257,6 +258,11 @@ def main():
     # On-disk formats, written by the reference's own writers.
     out.update(_formats(R, rng))
 
+    # The active domain: masks and escape counts on a tagged grid, the auto band,
+    # and armed runs covering each posture (restricted throughout, masked, the
+    # escape latch, a failed restricted solve, the fraction latch).
+    out.update(_active_domain(R, rng))
+
     old = os.path.join(HERE, "golden.npz")
     if os.path.exists(old):  # regenerating must not move any earlier vector
         with np.load(old) as z:
@@ -312,6 +318,36 @@ def _formats(R, rng):
                 fmt_fields_d=fd, fmt_fields_i=fi, fmt_fields_vm=vm, fmt_fields_disp=disp,
                 fmt_fields_bytes=bf, fmt_csv_od=od, fmt_csv_oi=oi, fmt_csv_ol=ol,
                 fmt_csv_bytes=bc)
+
+
+def _active_domain(R, rng):
+    out = {}
+    nx, ny, nz = 11, 7, 5
+    tags = rng.choice(np.array([0, 1, 1, 1, 2, 4, 5], np.uint8), nx * ny * nz)
+    pb = Problem(nx, ny, nz, 1.0, tags)
+    rho = np.where(rng.random(pb.nv) < 0.1, rng.random(pb.nv), 1e-3)
+    rho[rng.random(pb.nv) < 0.03] = 1.5e-3  # on the core threshold: not core
+    bands = np.array([0, 1, 2, 3, 64])
+    prev = (rng.random(pb.nv) < 0.5).astype(np.uint8)
+    radii = np.array([0.0, -1.0, 1.0, 1.2, 1.5, 2.5, 3.0, np.nan, np.inf])
+    out.update(ad_dims=np.array([nx, ny, nz]), ad_tags=tags, ad_rho=rho, ad_bands=bands,
+               ad_masks=np.stack([R.active_domain_mask(pb, rho, 1e-3, int(b)) for b in bands]),
+               ad_prev=prev, ad_escapes=np.array(R.active_domain_escape_count(pb, rho, prev, 1e-3)),
+               ad_radii=radii,
+               ad_auto=np.array([R.active_domain_auto_band(float(r)) for r in radii]))
+    for name in ACTIVE_DOMAIN_RUNS:
+        pbr, mask, seed, band, radius, vf, its = active_domain_case(name)
+        r = R.simp_optimize_active(pbr, band, mask=mask, seed=seed, radius=radius, volfrac=vf,
+                                   move=0.2, max_it=its, change_tol=0.0, cg_tol=1e-9)
+        k = "adr_" + name
+        out[k + "_hist_c"] = r["hist_c"]
+        out[k + "_hist_af"] = r["hist_af"]
+        out[k + "_phys"] = r["phys"]
+        out[k + "_d"] = np.array([r["compliance"], r["volume_fraction"], r["fraction_mean"]])
+        out[k + "_i"] = np.array([r["iterations"], r["band"], int(r["latched"]),
+                                  r["latch_iteration"], r["escape_count"]])
+        out[k + "_reason"] = np.frombuffer(r["reason"].encode(), np.uint8)
+    return out
 
 
 if __name__ == "__main__":

@@ -327,3 +327,51 @@ def test_mma_masked_run_golden(port, golden):
         assert np.array_equal(s[k], golden["mmam_" + k]), k
     assert s["compliance"] == float(golden["mmam_compliance"])
     assert s["volume_fraction"] == float(golden["mmam_volume_fraction"])
+
+
+def test_active_domain_mask_golden(port, golden):
+    """active_domain_mask (core + Load/Fixture pin, the x -> y -> z Chebyshev
+    dilation, AND solid) at bands 0, 1, 2, 3, 64, the escape count and the auto
+    band: identical to the reference's."""
+    nx, ny, nz = (int(v) for v in golden["ad_dims"])
+    pb = Problem(nx, ny, nz, 1.0, golden["ad_tags"])
+    rho = golden["ad_rho"]
+    for b, want in zip(golden["ad_bands"], golden["ad_masks"]):
+        assert np.array_equal(port.active_domain_mask(pb, rho, 1e-3, int(b)), want), b
+    assert port.active_domain_escape_count(pb, rho, golden["ad_prev"], 1e-3) == \
+        int(golden["ad_escapes"])
+    assert port.active_domain_escape_count(pb, rho, None, 1e-3) == 0
+    got = [port.active_domain_auto_band(float(r)) for r in golden["ad_radii"]]
+    assert got == golden["ad_auto"].tolist()
+
+
+def ad_reason(golden, name):
+    """The reference's latch reason.  The reference build here routes the
+    matrix-free multigrid solve to its exact Jacobi-PCG (oracle/ref_shim.cpp), so
+    a failed restricted solve names that function; the library itself names
+    fea_solve_mgcg_matfree, as the reference's own build does."""
+    r = bytes(golden[f"adr_{name}_reason"]).decode()
+    return r.replace("fea_solve_cg_matfree:", "fea_solve_mgcg_matfree:")
+
+
+@pytest.mark.parametrize("name", ["restricted", "masked", "escape", "failed", "latch"])
+def test_active_domain_runs_golden(port, golden, name):
+    """simp_optimize with active_domain_band (active_domain_solve,
+    simp.cpp:1809-1896): the restricted trajectory solves, the per-iteration
+    active fraction, each latch (escape, fraction, failed restricted solve) with
+    its iteration and reason, and the full-domain certification: identical."""
+    from oracle.oracle import active_domain_case
+    pb, mask, seed, band, radius, vf, its = active_domain_case(name)
+    s = port.simp_optimize_active(pb, band, mask=mask, seed=seed, radius=radius, volfrac=vf,
+                                  move=0.2, max_it=its, change_tol=0.0, cg_tol=1e-9)
+    k = "adr_" + name
+    assert [s["iterations"], s["band"], int(s["latched"]), s["latch_iteration"],
+            s["escape_count"]] == golden[k + "_i"].tolist()
+    assert np.array_equal(s["hist_af"], golden[k + "_hist_af"])
+    assert np.array_equal(s["hist_c"], golden[k + "_hist_c"])
+    assert np.array_equal(s["phys"], golden[k + "_phys"])
+    assert [s["compliance"], s["volume_fraction"], s["fraction_mean"]] == \
+        golden[k + "_d"].tolist()
+    assert s["reason"] == ad_reason(golden, name)
+    if name in ("restricted", "masked"):
+        assert not s["latched"] and s["hist_af"].max() < 0.85
