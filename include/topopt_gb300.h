@@ -167,6 +167,16 @@ typedef struct {
   int32_t mma_plateau_window;
   double mma_plateau_tol, mma_plateau_min_drop;
   int32_t mma_plateau_flat_windows;
+  /* Active domain (SimpOptions::active_domain_band, simp.hpp:1185-1227): 0 (the
+   * default) off; > 0 every trajectory solve runs on the material plus a band of
+   * this half-width in voxels (tg_active_domain_mask), out-of-band elements get
+   * no energy and no sensitivity; < 0 the band is tg_active_domain_auto_band
+   * (filter_radius).  The certification solve is always on the full domain.
+   * The mask is switched off for the rest of the run (one way) on the first
+   * escape, after 5 consecutive iterations at an active fraction >= 0.85, or
+   * when a restricted solve fails (that iteration is then re-solved on the full
+   * domain); tg_simp_result records which. */
+  int32_t active_domain_band;
 } tg_simp_options;
 
 enum { TG_UPDATER_OC = 0, TG_UPDATER_MMA = 1 };
@@ -186,11 +196,21 @@ typedef struct {
   int32_t mg_cycles_attempted; /* V-cycles this solve ran */
   int32_t oc_exact_evals;      /* bisection branches the fast volume bound could not decide */
   int32_t oc_host_fallbacks;   /* of those, decided by the host's sequential sum */
+  double active_fraction;      /* active elements / solid elements of this iteration's solve;
+                                  1 when it ran on the full domain */
 } tg_simp_iteration;
 
 typedef struct {
   int32_t iterations, converged, cancelled, infeasible, non_convergent;
   double compliance, initial_compliance, volume_fraction;
+  /* Active domain (SimpOptimizeResult, simp.hpp:1735-1761): the band the run
+   * used (0 = off), whether and at which 1-based iteration the mask was
+   * switched off and why, the escapes counted when the escape latch fired, and
+   * the mean of the per-iteration active fractions (1 when off). */
+  int32_t active_domain_band, active_domain_latched, active_domain_latch_iteration;
+  int64_t active_domain_escape_count;
+  double active_fraction_mean;
+  char active_domain_latch_reason[256];
 } tg_simp_result;
 
 /* Progress hook (TopOptBridge.hpp:262-263): called on the optimizing thread
@@ -255,6 +275,27 @@ int tg_filter(const tg_grid* grid, double radius, int32_t adjoint, const double*
 int tg_oc_update(const tg_grid* grid, double radius, const double* density,
                  const double* dcompliance, double volume_fraction, double move,
                  double density_min, double* x_new);
+
+/* ---- active domain (the restricted-analysis mask) ----
+ * active_domain_auto_band (simp.hpp:314; simp.cpp:440-447): ceil(filter_radius) + 1,
+ * 1 for a non-finite or non-positive radius.  Host only. */
+int32_t tg_active_domain_auto_band(double filter_radius);
+
+/* active_domain_mask (simp.hpp:298-300; simp.cpp:449-528), on the device:
+ * mask_out[e] = 1 iff voxel e is solid and within Chebyshev distance `band` of
+ * a core voxel (solid with density > 1.5 density_min, or tagged Load 4 / Fixture
+ * 5); band <= 0 returns every solid voxel.  Integer-exact: bit-identical to the
+ * reference for the same inputs.  active_count (may be NULL) receives the number
+ * of ones. */
+int tg_active_domain_mask(const tg_grid* grid, const double* density, double density_min,
+                          int32_t band, uint8_t* mask_out, int64_t* active_count);
+
+/* active_domain_escape_count (simp.hpp:336-339; simp.cpp:530-556), on the
+ * device: solid voxels outside prev_mask whose density exceeds 1.5 density_min;
+ * 0 when prev_mask is NULL (the first armed iteration). */
+int tg_active_domain_escape_count(const tg_grid* grid, const double* density,
+                                  const uint8_t* prev_mask, double density_min,
+                                  int64_t* escapes);
 
 /* ---- design masks (passive regions) ----
  * Mask bytes are MaskValue (core/include/topopt/voxel.hpp:42-46): 0 Active,

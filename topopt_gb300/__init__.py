@@ -26,6 +26,9 @@ from ._capi import (  # noqa: F401
     SolveOptions,
     SolverNonConvergence,
     device_fma_peaks,
+    active_domain_auto_band,
+    active_domain_escape_count,
+    active_domain_mask,
     effective_design_mask,
     fea_build_reduced,
     kernel_launches,

@@ -90,7 +90,8 @@ class _SimpOpt(C.Structure):
                 ("projection_stages", C.c_int32), ("projection_eta", C.c_double),
                 ("initial_design", C.c_void_p), ("updater", C.c_int32),
                 ("mma_plateau_window", C.c_int32), ("mma_plateau_tol", C.c_double),
-                ("mma_plateau_min_drop", C.c_double), ("mma_plateau_flat_windows", C.c_int32)]
+                ("mma_plateau_min_drop", C.c_double), ("mma_plateau_flat_windows", C.c_int32),
+                ("active_domain_band", C.c_int32)]
 
 
 class _Iter(C.Structure):
@@ -104,14 +105,19 @@ class _Iter(C.Structure):
                 ("fine_matvecs_lowp", C.c_int64), ("oc_volume_passes", C.c_int32),
                 ("beta", C.c_double), ("hier_built", C.c_int32),
                 ("mg_cycles_attempted", C.c_int32), ("oc_exact_evals", C.c_int32),
-                ("oc_host_fallbacks", C.c_int32)]
+                ("oc_host_fallbacks", C.c_int32), ("active_fraction", C.c_double)]
 
 
 class _Result(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("cancelled", C.c_int32),
                 ("infeasible", C.c_int32), ("non_convergent", C.c_int32),
                 ("compliance", C.c_double), ("initial_compliance", C.c_double),
-                ("volume_fraction", C.c_double)]
+                ("volume_fraction", C.c_double), ("active_domain_band", C.c_int32),
+                ("active_domain_latched", C.c_int32),
+                ("active_domain_latch_iteration", C.c_int32),
+                ("active_domain_escape_count", C.c_int64),
+                ("active_fraction_mean", C.c_double),
+                ("active_domain_latch_reason", C.c_char * 256)]
 
 
 _PROGRESS = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_double, C.c_double)
@@ -148,6 +154,9 @@ def lib():
         "tg_simp_optimize": ([vp, vp, vp, i32, vp, i32, vp, _PROGRESS, vp, vp, vp, vp, vp, vp],
                              C.c_int),
         "tg_effective_design_mask": ([vp, vp, vp], C.c_int),
+        "tg_active_domain_auto_band": ([dbl], C.c_int32),
+        "tg_active_domain_mask": ([vp, vp, dbl, i32, vp, vp], C.c_int),
+        "tg_active_domain_escape_count": ([vp, vp, vp, dbl, vp], C.c_int),
         "tg_filter_masked": ([vp, vp, dbl, i32, vp, vp], C.c_int),
         "tg_oc_update_masked": ([vp, vp, dbl, vp, vp, dbl, dbl, dbl, vp], C.c_int),
         "tg_simp_optimize_masked": ([vp, vp, vp, i32, vp, i32, vp, vp, _PROGRESS, vp, vp, vp, vp,
@@ -323,6 +332,9 @@ class SimpOptions:
     mma_plateau_tol: float = 1e-3
     mma_plateau_min_drop: float = 0.05
     mma_plateau_flat_windows: int = 3
+    # The active domain (simp.hpp:1185-1227): 0 off, > 0 the band half-width in
+    # voxels, < 0 the auto band ceil(filter_radius) + 1.
+    active_domain_band: int = 0
 
     def total_iterations(self) -> int:
         if self.projection:
@@ -345,6 +357,7 @@ class SimpOptions:
         o.mma_plateau_tol = self.mma_plateau_tol
         o.mma_plateau_min_drop = self.mma_plateau_min_drop
         o.mma_plateau_flat_windows = self.mma_plateau_flat_windows
+        o.active_domain_band = self.active_domain_band
         if self.initial_design is not None:
             seed = np.ascontiguousarray(self.initial_design, dtype=np.float64).ravel()
             o._seed = seed  # kept alive with the struct
@@ -496,6 +509,35 @@ def make_density_filter(pb: Problem, radius: float, mask=None) -> DensityFilter:
     if not (radius > 0.0):
         raise ValueError("make_density_filter: radius must be > 0")
     return DensityFilter(pb, radius, mask)
+
+
+def active_domain_auto_band(filter_radius):
+    """active_domain_auto_band (simp.hpp:314): ceil(filter_radius) + 1, at least 1."""
+    return int(lib().tg_active_domain_auto_band(float(filter_radius)))
+
+
+def active_domain_mask(pb: Problem, density, density_min, band):
+    """active_domain_mask (simp.hpp:298-300) on the device: (mask uint8[nv], ones)."""
+    d = _f64(density, pb.nv)
+    out = np.zeros(pb.nv, np.uint8)
+    n = C.c_int64(0)
+    _check(lib().tg_active_domain_mask(C.byref(pb._grid), _p(d), float(density_min), int(band),
+                                       _p(out), C.byref(n)))
+    return out, int(n.value)
+
+
+def active_domain_escape_count(pb: Problem, density, prev_mask, density_min):
+    """active_domain_escape_count (simp.hpp:336-339) on the device; prev_mask None
+    (the first armed iteration) counts 0."""
+    d = _f64(density, pb.nv)
+    pm = None if prev_mask is None else np.ascontiguousarray(prev_mask, dtype=np.uint8).ravel()
+    if pm is not None and pm.size != pb.nv:
+        raise ValueError("prev_mask size != voxel_count")
+    n = C.c_int64(0)
+    _check(lib().tg_active_domain_escape_count(C.byref(pb._grid), _p(d),
+                                               None if pm is None else _p(pm),
+                                               float(density_min), C.byref(n)))
+    return int(n.value)
 
 
 def effective_design_mask(pb: Problem, mask):
@@ -919,7 +961,13 @@ def simp_optimize(pb: Problem, params: SimpParams, options: SimpOptions, progres
                 initial_compliance=res.initial_compliance, volume_fraction=res.volume_fraction,
                 iterations=res.iterations, converged=bool(res.converged),
                 cancelled=bool(res.cancelled), infeasible=bool(res.infeasible),
-                non_convergent=bool(res.non_convergent), history=_rows(hist, res.iterations))
+                non_convergent=bool(res.non_convergent), history=_rows(hist, res.iterations),
+                active_domain=dict(band=res.active_domain_band,
+                                   latched=bool(res.active_domain_latched),
+                                   latch_iteration=res.active_domain_latch_iteration,
+                                   escape_count=res.active_domain_escape_count,
+                                   fraction_mean=res.active_fraction_mean,
+                                   reason=res.active_domain_latch_reason.decode()))
 
 
 class _ServerConfig(C.Structure):

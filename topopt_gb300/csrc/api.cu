@@ -701,8 +701,40 @@ struct tg_job {
   bool xphys_valid = false;
   std::vector<double> hist_c;
   std::vector<int> hist_cg;
+  // The active domain (ActiveDomainRun, simp.cpp:1745-1766): the resolved band,
+  // the one-way latch and its record, the running fraction mean, the band the
+  // previous armed solve ran under (device), the analysis grid's tags, BCs and
+  // loads (to build the restricted system), and the restricted system with its
+  // solver, rebuilt only when the mask changes.
+  struct ActiveDomain {
+    int band = 0;
+    bool latched = false, have_prev = false;
+    int latch_iteration = 0, hot_streak = 0;
+    int64_t escape_count = 0, n_solid = 0;
+    double fraction_sum = 0.0;
+    int64_t fraction_count = 0;
+    std::string reason;
+    tg_grid grid{};
+    std::vector<uint8_t> tags_h, cur_h, built_h;
+    std::vector<tg_dirichlet_bc> bcs;
+    std::vector<tg_nodal_load> loads;
+    DBuf<uint8_t> tags, prev, cur, tmp;
+    DBuf<unsigned long long> count;
+    FineProblem fp;
+    std::unique_ptr<Solver> solver;  // declared after fp: destroyed first
+    bool armed() const { return band > 0 && !latched; }
+    void record(double f) {
+      fraction_sum += f;
+      ++fraction_count;
+    }
+    size_t bytes() const {
+      return tags.bytes() + prev.bytes() + cur.bytes() + tmp.bytes() + count.bytes() +
+             fp.device_bytes() + (solver ? solver->device_bytes() : 0);
+    }
+  } ad;
 
   ~tg_job() {
+    ad.solver.reset();
     solver.reset();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -713,7 +745,7 @@ struct tg_job {
     size_t b = fp.device_bytes() + filt.bytes() + oc.bytes() + solid.bytes() + eff.bytes();
     for (const DBuf<double>* d : {&x, &xnew, &xphys, &E, &u, &dc, &part, &scal, &xtilde, &mma_buf})
       b += d->bytes();
-    return b + (solver ? solver->device_bytes() : 0);
+    return b + (solver ? solver->device_bytes() : 0) + ad.bytes();
   }
 };
 
@@ -796,6 +828,23 @@ void job_init(tg_job* j, const tg_grid* grid, const tg_simp_params* params,
   j->n_solid = 0;
   for (uint8_t v : j->solid_h) j->n_solid += v;
   upload(j->solid, j->solid_h.data(), j->solid_h.size(), s);
+  // resolve_active_domain_band (simp.cpp:1773-1782): < 0 is the auto band.
+  j->ad.band = o.active_domain_band < 0 ? tg_active_domain_auto_band(o.filter_radius)
+                                        : o.active_domain_band;
+  if (j->ad.band > 0) {
+    tg_job::ActiveDomain& ad = j->ad;
+    ad.grid = analysis;
+    if (analysis.tags) {
+      ad.tags_h.assign(analysis.tags, analysis.tags + g.nv);
+      ad.grid.tags = ad.tags_h.data();
+      upload(ad.tags, ad.tags_h.data(), ad.tags_h.size(), s);
+    }
+    ad.bcs.assign(bcs, bcs + nbc);
+    ad.loads.assign(loads, loads + nloads);
+    for (uint8_t v : j->fp.elem_h) ad.n_solid += v;  // solid voxels of the analysis grid
+    for (DBuf<uint8_t>* d : {&ad.prev, &ad.cur, &ad.tmp}) d->alloc(size_t(g.nv));
+    ad.count.alloc(1);
+  }
   for (DBuf<double>* d : {&j->x, &j->xnew, &j->xphys, &j->E, &j->dc}) d->alloc(size_t(g.nv));
   if (j->projecting()) j->xtilde.alloc(size_t(g.nv));
   if (j->mma) {
@@ -869,13 +918,17 @@ double read1(tg_job* j, const double* dptr) {
   return j->h_scal[0];
 }
 
-// Compliance + dc at the current physical density and displacement.
-double job_sensitivity(tg_job* j) {
+// Compliance + dc at the current physical density and displacement, over the
+// elements of the system that was solved (`elem`: the job's solid set, or the
+// restricted set of an active-domain solve, whose other elements get no energy
+// and no sensitivity, simp.cpp:752-763).
+double job_sensitivity(tg_job* j, const uint8_t* elem = nullptr) {
   const Grid& g = j->fp.g;
   const tg_simp_params& p = j->params;
   int nparts = 0;
-  launch_sensitivity(g, j->fp.mc, j->xphys.p, j->fp.elem.p, j->u.p, p.youngs_modulus, p.penalty,
-                     p.density_min, p.material_law, p.e_min, j->dc.p, j->part.p, &nparts, j->s);
+  launch_sensitivity(g, j->fp.mc, j->xphys.p, elem ? elem : j->fp.elem.p, j->u.p,
+                     p.youngs_modulus, p.penalty, p.density_min, p.material_law, p.e_min,
+                     j->dc.p, j->part.p, &nparts, j->s);
   launch_sum_partials(j->part.p, nparts, j->scal.p, j->s);
   return read1(j, j->scal.p);
 }
@@ -889,6 +942,109 @@ SolverStats job_solve(tg_job* j, double tol, int max_it) {
                  p.material_law, p.e_min, j->E.p, j->s);
   j->solver->set_modulus(j->E.p);
   return j->solver->solve(tol, max_it, nullptr, j->u.p);
+}
+
+// One trajectory solve under the active domain (active_domain_solve,
+// simp.cpp:1809-1896).  Armed: the escape check against the previous band
+// (first escape: latch, full domain), then the mask of the current physical
+// density, the restricted system (rebuilt when the mask changed) and its solve;
+// a restricted system that fails its void gates or does not converge latches
+// the mask off and the same field is re-solved on the full domain.  After a
+// restricted solve the fraction latch counts iterations at >= 0.85
+// (kActiveDomainLatchFraction / kActiveDomainLatchWindow, simp.hpp:363-364).
+// *af: the active fraction of the solve that ran (1 on the full domain);
+// *elem: its element set.
+SolverStats ad_job_solve(tg_job* j, double tol, int max_it, double* af, const uint8_t** elem) {
+  tg_job::ActiveDomain& ad = j->ad;
+  *af = 1.0;
+  *elem = j->fp.elem.p;
+  if (ad.armed()) {
+    AllocScope scope(j->s);
+    const Grid& g = j->fp.g;
+    const tg_simp_params& p = j->params;
+    const int iteration = j->iteration + 1;
+    const uint8_t* tags = ad.tags.p;  // null: every voxel solid, nothing pinned
+    int64_t esc = 0;
+    if (ad.have_prev) {
+      launch_active_domain_escape(tags, j->xphys.p, ad.prev.p, p.density_min, g.nv, ad.count.p,
+                                  j->s);
+      unsigned long long n = 0;
+      TG_CUDA(cudaMemcpyAsync(&n, ad.count.p, sizeof n, cudaMemcpyDeviceToHost, j->s));
+      TG_CUDA(cudaStreamSynchronize(j->s));
+      esc = int64_t(n);
+    }
+    if (esc > 0) {
+      ad.latched = true;
+      ad.latch_iteration = iteration;
+      ad.escape_count = esc;
+      char buf[192];
+      std::snprintf(buf, sizeof buf,
+                    "escape detected: %lld element(s) took material outside the active band "
+                    "(growth invariant failed); mask disabled, full domain restored",
+                    static_cast<long long>(esc));
+      ad.reason = buf;
+      ad.record(1.0);
+    } else {
+      launch_active_domain_mask(g.nx, g.ny, g.nz, tags, j->xphys.p, p.density_min, ad.band,
+                                ad.cur.p, ad.tmp.p, ad.count.p, j->s);
+      unsigned long long active = 0;
+      ad.cur_h.resize(size_t(g.nv));
+      TG_CUDA(cudaMemcpyAsync(ad.cur_h.data(), ad.cur.p, size_t(g.nv), cudaMemcpyDeviceToHost,
+                              j->s));
+      TG_CUDA(cudaMemcpyAsync(&active, ad.count.p, sizeof active, cudaMemcpyDeviceToHost, j->s));
+      TG_CUDA(cudaStreamSynchronize(j->s));
+      const double fraction = ad.n_solid > 0 ? double(active) / double(ad.n_solid) : 1.0;
+      try {
+        if (!ad.solver || ad.cur_h != ad.built_h) {
+          ad.solver.reset();
+          ad.built_h.clear();
+          ad.fp.build(ad.grid, p.poisson, ad.bcs.data(), int(ad.bcs.size()), ad.loads.data(),
+                      int(ad.loads.size()), ad.cur_h.data(), j->s);
+          ad.solver = std::make_unique<Solver>(ad.fp, j->opt.solve, j->s);
+          ad.built_h = ad.cur_h;
+        }
+        launch_modulus(j->xphys.p, ad.fp.elem.p, g.nv, p.youngs_modulus, p.penalty,
+                       p.density_min, p.material_law, p.e_min, j->E.p, j->s);
+        ad.solver->set_modulus(j->E.p);
+        const SolverStats st = ad.solver->solve(tol, max_it, nullptr, j->u.p);
+        if (!st.converged)
+          raise(TG_ENONCONV, "CG did not reach the requested tolerance within max_iterations");
+        *af = fraction;
+        *elem = ad.fp.elem.p;
+        ad.record(fraction);
+        if (fraction >= 0.85) {
+          if (++ad.hot_streak >= 5) {
+            ad.latched = true;
+            ad.latch_iteration = iteration;
+            char buf[192];
+            std::snprintf(buf, sizeof buf,
+                          "active fraction >= %.2f for %d consecutive iterations (band covers "
+                          "the domain and buys nothing)",
+                          0.85, 5);
+            ad.reason = buf;
+          }
+        } else {
+          ad.hot_streak = 0;
+        }
+        std::swap(ad.prev, ad.cur);
+        ad.have_prev = true;
+        return st;
+      } catch (const Error& e) {
+        // The reference catches every exception of the restricted solve; device
+        // faults are not the band's doing and stay fatal here.
+        if (e.code == TG_EDEVICE) throw;
+        ad.latched = true;
+        ad.latch_iteration = iteration;
+        ad.reason = std::string("restricted solve failed: fea_solve_mgcg_matfree: ") + e.what();
+        ad.record(1.0);
+        ad.solver.reset();
+        ad.built_h.clear();
+      }
+    }
+  } else if (ad.band > 0) {
+    ad.record(1.0);  // latched: still counted, as 1.0
+  }
+  return job_solve(j, tol, max_it);
 }
 
 // xPhys = filter(x), projected on the design voxels at the current stage's beta
@@ -920,7 +1076,9 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   if (!j->xphys_valid) job_filter_x(j);
   TG_CUDA(cudaEventRecord(j->evf, j->s));  // filter time from events, no host wait here
   const double t1 = now_ms();
-  SolverStats st = job_solve(j, o.cg_tolerance, o.cg_max_iterations);
+  double af = 1.0;
+  const uint8_t* elem = nullptr;
+  SolverStats st = ad_job_solve(j, o.cg_tolerance, o.cg_max_iterations, &af, &elem);
   const double t2 = now_ms();
   if (!st.converged) {
     Error e(TG_ENONCONV, "simp_optimize: the trajectory solve did not reach the requested tolerance");
@@ -928,7 +1086,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
     e.residual = st.residual;
     throw e;
   }
-  const double c = job_sensitivity(j);
+  const double c = job_sensitivity(j, elem);
   const double t3 = now_ms();
   const int fb0 = j->oc.evals, ps0 = j->oc.passes, ex0 = j->oc.exact_evals,
             hf0 = j->oc.fallbacks;
@@ -983,6 +1141,7 @@ int job_step(tg_job* j, tg_simp_iteration* row) {
   r.mg_cycles_attempted = st.mg_cycles;
   r.oc_exact_evals = j->oc.exact_evals - ex0;
   r.oc_host_fallbacks = j->oc.fallbacks - hf0;
+  r.active_fraction = af;
   j->hist_c.push_back(c);
   j->hist_cg.push_back(st.iterations);
   if (row) *row = r;
@@ -1580,6 +1739,58 @@ int tg_effective_design_mask(const tg_grid* grid, const uint8_t* mask, uint8_t* 
   });
 }
 
+int32_t tg_active_domain_auto_band(double filter_radius) {
+  if (!std::isfinite(filter_radius) || filter_radius <= 0.0) return 1;
+  const int k = static_cast<int>(std::ceil(filter_radius)) + 1;
+  return k < 1 ? 1 : k;
+}
+
+int tg_active_domain_mask(const tg_grid* grid, const double* density, double density_min,
+                          int32_t band, uint8_t* mask_out, int64_t* active_count) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!density || !mask_out) raise(TG_EINVAL, "density and mask_out must be non-null");
+    CallStream cs;
+    const int64_t nv = int64_t(grid->nx) * grid->ny * grid->nz;
+    DBuf<uint8_t> tags, out{static_cast<size_t>(nv)}, tmp{static_cast<size_t>(nv)};
+    DBuf<double> rho;
+    DBuf<unsigned long long> count(1);
+    if (grid->tags) upload(tags, grid->tags, size_t(nv), cs.s);
+    upload(rho, density, size_t(nv), cs.s);
+    launch_active_domain_mask(grid->nx, grid->ny, grid->nz, tags.p, rho.p, density_min, band,
+                              out.p, tmp.p, count.p, cs.s);
+    unsigned long long n = 0;
+    TG_CUDA(cudaMemcpyAsync(mask_out, out.p, size_t(nv), cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaMemcpyAsync(&n, count.p, sizeof n, cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+    if (active_count) *active_count = int64_t(n);
+  });
+}
+
+int tg_active_domain_escape_count(const tg_grid* grid, const double* density,
+                                  const uint8_t* prev_mask, double density_min,
+                                  int64_t* escapes) {
+  return guarded([&] {
+    validate_grid(grid);
+    if (!density || !escapes) raise(TG_EINVAL, "density and escapes must be non-null");
+    *escapes = 0;
+    if (!prev_mask) return;  // the first armed iteration: no band to overrun
+    CallStream cs;
+    const int64_t nv = int64_t(grid->nx) * grid->ny * grid->nz;
+    DBuf<uint8_t> tags, prev;
+    DBuf<double> rho;
+    DBuf<unsigned long long> count(1);
+    if (grid->tags) upload(tags, grid->tags, size_t(nv), cs.s);
+    upload(prev, prev_mask, size_t(nv), cs.s);
+    upload(rho, density, size_t(nv), cs.s);
+    launch_active_domain_escape(tags.p, rho.p, prev.p, density_min, nv, count.p, cs.s);
+    unsigned long long n = 0;
+    TG_CUDA(cudaMemcpyAsync(&n, count.p, sizeof n, cudaMemcpyDeviceToHost, cs.s));
+    TG_CUDA(cudaStreamSynchronize(cs.s));
+    *escapes = int64_t(n);
+  });
+}
+
 int tg_job_create(const tg_grid* grid, const tg_simp_params* params, const tg_dirichlet_bc* bcs,
                   int32_t nbc, const tg_nodal_load* loads, int32_t nloads,
                   const tg_simp_options* options, tg_job** job_out) {
@@ -1668,6 +1879,14 @@ int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* option
   if (options && options->projection_stages > 0)  // xtilde and the candidate fields
     b += nv * 8.0 * (1 + projected_candidates(int64_t(nv)));
   if (options && options->updater == TG_UPDATER_MMA) b += nv * 8.0 * 10;  // MMA fields
+  if (options && options->active_domain_band != 0) {
+    // The restricted system: its own reduced problem, solver vectors and
+    // hierarchy (at most the full system's), and three byte masks.
+    double r = ndof * (9 * 8 + 1 + 16) + nv * 4;
+    r += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 126 * 8 * 8.0 / 7.0;
+    if (mixed) r += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 126 * 4 * 8.0 / 7.0 + nv * 4;
+    b += r;
+  }
   return int64_t(b * 1.05) + (64 << 20);
 }
 
@@ -1782,6 +2001,17 @@ static int simp_optimize_impl(const tg_grid* grid, const tg_simp_params* params,
     bool exact = false;
     const double vol = exact_volume(j->oc, g, j->solid.p, j->xphys.p, &exact, j->s);
     res.volume_fraction = j->n_solid > 0 ? vol / double(j->n_solid) : 0.0;
+    // finalize_active_domain (simp.cpp:1981-1988), after the full-domain
+    // certification solve.
+    const tg_job::ActiveDomain& ad = j->ad;
+    res.active_domain_band = ad.band;
+    res.active_domain_latched = ad.latched ? 1 : 0;
+    res.active_domain_latch_iteration = ad.latch_iteration;
+    res.active_domain_escape_count = ad.escape_count;
+    res.active_fraction_mean =
+        ad.fraction_count > 0 ? ad.fraction_sum / double(ad.fraction_count) : 1.0;
+    std::snprintf(res.active_domain_latch_reason, sizeof res.active_domain_latch_reason, "%s",
+                  ad.reason.c_str());
     if (design_out)
       TG_CUDA(cudaMemcpyAsync(design_out, j->x.p, size_t(g.nv) * sizeof(double),
                               cudaMemcpyDeviceToHost, j->s));

@@ -314,7 +314,8 @@ void tg_iteration_record_from(const tg_simp_iteration* row, int32_t infeasible,
   r.hier_built = row->hier_built;
   r.mg_cycles_attempted = row->mg_cycles_attempted;
   r.infeasible = infeasible;
-  r.active_fraction = 1.0;
+  // A solve's active fraction is in (0, 1]; a zeroed row carries none (full domain).
+  r.active_fraction = row->active_fraction > 0.0 ? row->active_fraction : 1.0;
   r.total_ms = row->t_total_ms;
   r.filter_ms = row->t_filter_ms;
   r.solve_ms = row->t_solve_ms + row->t_sensitivity_ms;

@@ -154,14 +154,14 @@ void FineProblem::build(const tg_grid& grid, double poisson, const tg_dirichlet_
     }
   }
   if (n_free > 0 && n_touched_free == 0)
-    raise(TG_ESINGULAR, "singular system (no stiffness - every free DOF is void)");
+    raise(TG_ESINGULAR, "singular system (no stiffness \xe2\x80\x94 every free DOF is void)");
   const double load_tol = 1e-9 * rmax;
   if (!nonzero_bc)
     for (int64_t d = 0; d < g.ndof; ++d)
       if (!fixed[size_t(d)] && !touched[size_t(d / 3)] && std::fabs(f_h[size_t(d)]) > load_tol)
         raise(TG_ESINGULAR,
-              "under-constrained system (load applied to a void DOF with no stiffness - no "
-              "equilibrium possible)");
+              "under-constrained system (load applied to a void DOF with no stiffness \xe2\x80\x94 "
+              "no equilibrium possible)");
   elem.alloc(size_t(g.nv));
   kept.alloc(size_t(g.ndof));
   f.alloc(size_t(g.ndof));
@@ -504,8 +504,8 @@ void Solver::set_modulus(const double* E) {
       if (!fp_.fixed_h[size_t(d)] && !fp_.kept_h[size_t(d)] &&
           std::fabs(fp_.f_h[size_t(d)] - kup[size_t(d)]) > 1e-9 * rmax)
         raise(TG_ESINGULAR,
-              "under-constrained system (load applied to a void DOF with no stiffness - no "
-              "equilibrium possible)");
+              "under-constrained system (load applied to a void DOF with no stiffness \xe2\x80\x94 "
+              "no equilibrium possible)");
   }
   if (mixed_) {
     launch_copy_d2f(Ef_.p, E, g.nv, s_);

@@ -298,6 +298,15 @@ void launch_element_stress(const Grid& g, const uint8_t* solid, const double* rh
                            cudaStream_t s);
 // FrozenSolid (1) -> 1, FrozenVoid (2) -> 0 on the physical density.
 void launch_mask_pins(const uint8_t* eff, int64_t n, double* xphys, cudaStream_t s);
+// Active domain (k_active.cu): the mask into `out` (tmp: nv scratch bytes) and
+// its count of ones; the escape count of rho against prev.  Counts are reset
+// on the stream first.
+void launch_active_domain_mask(int nx, int ny, int nz, const uint8_t* tags, const double* rho,
+                               double density_min, int band, uint8_t* out, uint8_t* tmp,
+                               unsigned long long* count, cudaStream_t s);
+void launch_active_domain_escape(const uint8_t* tags, const double* rho, const uint8_t* prev,
+                                 double density_min, int64_t nv, unsigned long long* count,
+                                 cudaStream_t s);
 // Exact (fixed-point, order independent) sum of a non-negative field over the
 // solid voxels; returns per-block 192-bit partials, then the final total.
 int exact_sum_blocks();
