@@ -862,6 +862,7 @@ void Solver::refinement_residual() {
 }
 
 bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
+  mixed_partial_ = false;
   const Grid& g = fp_.g;
   const int64_t n = g.ndof;
   launch_dot(rhs_.p, rhs_.p, n, part_.p, scal_.p + 4, s_);
@@ -889,6 +890,7 @@ bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
   const double inner_tol = opt_.inner_tolerance > 0.0 ? opt_.inner_tolerance : 1e-5;
   const int max_ref = opt_.max_refinements > 0 ? opt_.max_refinements : 20;
   int total_inner = 0;
+  double rn0 = -1.0;
   for (int ref = 0; ref <= max_ref; ++ref) {
     launch_dot(r_.p, r_.p, n, part_.p, scal_.p + 5, s_);
     const double rr = read_scalar(5);
@@ -899,7 +901,13 @@ bool Solver::mixed_refine(double tol, int max_it, bool warm, SolverStats& st) {
       st.iterations = total_inner;
       return true;
     }
-    if (ref == max_ref || total_inner >= max_it) break;
+    if (rn0 < 0.0) rn0 = rn;
+    if (ref == max_ref || total_inner >= max_it) {
+      // Out of budget: x is finite and, when it reduced the residual, a better
+      // start for the FP64 retry than its initial guess.
+      mixed_partial_ = rn < rn0;
+      break;
+    }
     launch_scale_d2f(zf_.p, r_.p, scal_.p + 5, n, s_);
     int it = 0;
     // Default inner tolerance: 0.3x the reduction still needed, within
@@ -996,8 +1004,13 @@ SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u
     }
     if (mixed_ && !solved) st.mixed_fallback = true;
     if (!solved && (!mixed_ || build_numeric<double>())) {
-      if (warm) seed();
-      solved = mgpcg(tol, std::min(cap, budget_), warm, st);
+      // The FP64 retry of a mixed solve starts from the mixed attempt's last
+      // iterate when that attempt made progress (high-contrast designs can need
+      // more FP32 refinements than the budget allows while each one still
+      // gains); otherwise from the caller's guess or zero.
+      const bool resume = mixed_ && mixed_partial_;
+      if (warm && !resume) seed();
+      solved = mgpcg(tol, std::min(cap, budget_), warm || resume, st);
     }
     st.mg_cycles = st.iterations;
     if (solved) {

@@ -100,6 +100,7 @@ class Solver {
   int budget_ = 300;
   int sweeps_ = 1;  // damped-Jacobi sweeps per side of the coarse correction
   bool df_residual_ = true;  // mixed: refinement residual in double-float arithmetic
+  bool mixed_partial_ = false;  // the last mixed attempt ran out of budget with progress
   void refinement_residual();  // r = b - A x (FP64 in, FP64 out) for the mixed loop
   bool mixed_ = false;
   // fine state
