@@ -416,7 +416,7 @@ class OracleLib:
 
     def simp_optimize_active(self, pb: Problem, band, mask=None, seed=None, E0=1.0, nu=0.3,
                              penal=3.0, rho_min=1e-3, volfrac=0.3, radius=1.5, move=0.2,
-                             max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0):
+                             max_it=50, change_tol=0.01, cg_tol=1e-8, cg_max_it=0, updater=0):
         """simp_optimize (OC; plain, or masked with mask) with
         SimpOptions::active_domain_band = band and an optional warm-start seed:
         the history with each iteration's active fraction, and the run's
@@ -432,11 +432,12 @@ class OracleLib:
                           [C.c_int] * 3 + [C.c_double, C.c_void_p, C.c_void_p] +
                           [C.c_double] * 4 + [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp] +
                           [C.c_double] * 3 + [C.c_int, C.c_double, C.c_double, C.c_int,
-                                              C.c_int, C.c_void_p] + [_dp] * 7 +
+                                              C.c_int, C.c_int, C.c_void_p] + [_dp] * 7 +
                           [C.c_void_p, C.c_char_p])
             self._check(f(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), self._ptr(m), E0, nu,
                           penal, rho_min, *pb.bc_args(), volfrac, radius, move, max_it,
-                          change_tol, cg_tol, cg_max_it, band, self._ptr(sd), hc, hch, hvf, haf,
+                          change_tol, cg_tol, cg_max_it, band, updater, self._ptr(sd), hc, hch,
+                          hvf, haf,
                           design, phys, sc, ints.ctypes.data_as(C.c_void_p), reason))
             n = int(ints[0])
             return dict(compliance=sc[0], volume_fraction=sc[1], initial_compliance=sc[2],
@@ -446,8 +447,10 @@ class OracleLib:
                         band=int(ints[4]), latched=bool(ints[5]), latch_iteration=int(ints[6]),
                         escape_count=int(ints[7]), fraction_mean=sc[3],
                         reason=reason.value.decode())
+        # MMA's plateau stop at the SimpOptions defaults (simp.hpp:1241-1277).
         opt = _OrSimpOptions(volfrac, radius, move, change_tol, cg_tol, max_it, cg_max_it, 0,
-                             None, None, None, 0.5, self._ptr(sd), 0, 0, 0.0, 0.0, 0, band,
+                             None, None, None, 0.5, self._ptr(sd), updater,
+                             10 if updater == 1 else 0, 1e-3, 0.05, 3, band,
                              haf.ctypes.data_as(C.c_void_p))
         res = _OrSimpResult()
         hcg = np.zeros(max_it, np.int32)
@@ -873,24 +876,26 @@ def beam_seed(nx, ny, nz, half_width=2, floor=1e-3):
 
 
 # name: (nx, ny, nz, masked, seed (half_width, floor) or None, band, radius,
-#        volfrac, iterations) -- each run at move 0.2, change_tol 0, cg 1e-9.
+#        volfrac, iterations, updater 0 OC / 1 MMA) -- each run at move 0.2,
+#        change_tol 0, cg 1e-9.
 ACTIVE_DOMAIN_RUNS = {
-    "restricted": (32, 16, 16, False, (2, 1e-3), -1, 1.5, 0.05, 20),
-    "masked": (32, 16, 16, True, (2, 1e-3), -1, 1.5, 0.05, 10),
-    "escape": (24, 12, 12, False, (1, 1e-6), 1, 2.5, 0.1, 10),
-    "failed": (16, 6, 6, False, "plate", 1, 1.5, 0.2, 6),
-    "latch": (12, 4, 4, False, None, -1, 1.5, 0.3, 12),
+    "restricted": (32, 16, 16, False, (2, 1e-3), -1, 1.5, 0.05, 20, 0),
+    "masked": (32, 16, 16, True, (2, 1e-3), -1, 1.5, 0.05, 10, 0),
+    "escape": (24, 12, 12, False, (1, 1e-6), 1, 2.5, 0.1, 10, 0),
+    "failed": (16, 6, 6, False, "plate", 1, 1.5, 0.2, 6, 0),
+    "latch": (12, 4, 4, False, None, -1, 1.5, 0.3, 12, 0),
+    "mma": (32, 16, 16, False, (2, 1e-3), -1, 1.5, 0.05, 15, 1),
 }
 
 
 def active_domain_case(name):
-    """(Problem, mask or None, seed or None, band, radius, volfrac, iterations) of
-    one ACTIVE_DOMAIN_RUNS entry.  The masked box has a Fixture slab at x = 0,
+    """(Problem, mask or None, seed or None, band, radius, volfrac, iterations,
+    updater) of one ACTIVE_DOMAIN_RUNS entry.  The masked box has a Fixture slab at x = 0,
     Load voxels under the loaded edge, a FrozenVoid keep-out block and a
     FrozenSolid insert on the beam.  The "failed" seed puts material only near
     the clamped face, so band 1 leaves the loaded edge void and the restricted
     system fails the void-load gate."""
-    nx, ny, nz, masked, sd, band, radius, vf, its = ACTIVE_DOMAIN_RUNS[name]
+    nx, ny, nz, masked, sd, band, radius, vf, its, upd = ACTIVE_DOMAIN_RUNS[name]
     mask = None
     tags = None
     if masked:
@@ -910,4 +915,4 @@ def active_domain_case(name):
         seed = seed.ravel()
     else:
         seed = beam_seed(nx, ny, nz, sd[0], sd[1])
-    return pb, mask, seed, band, radius, vf, its
+    return pb, mask, seed, band, radius, vf, its, upd

@@ -797,8 +797,9 @@ int ref_active_domain_escape_count(int nx, int ny, int nz, const uint8_t* tags,
   });
 }
 
-// simp_optimize (OC, MultigridCG_Matfree, plain when mask is NULL) with
-// options.active_domain_band = band and an optional warm-start seed; the
+// simp_optimize (OC, or MMA with updater 1; MultigridCG_Matfree; plain when
+// mask is NULL) with options.active_domain_band = band and an optional
+// warm-start seed; the
 // per-iteration active fraction comes from the observe hook.
 // out_ints: iterations, converged, non_convergent, infeasible, band, latched,
 // latch_iteration, escape_count.  out_scalars: compliance, vf, init_c,
@@ -809,7 +810,8 @@ int ref_simp_optimize_active(int nx, int ny, int nz, double h, const uint8_t* ta
                              const double* bc_val, int nload, const int* ld_node,
                              const int* ld_comp, const double* ld_val, double volfrac,
                              double radius, double move, int max_it, double change_tol,
-                             double cg_tol, int cg_max_it, int band, const double* seed,
+                             double cg_tol, int cg_max_it, int band, int updater,
+                             const double* seed,
                              double* hist_c, double* hist_change, double* hist_vf,
                              double* hist_af, double* design, double* phys,
                              double* out_scalars, long long* out_ints, char* reason) {
@@ -830,6 +832,7 @@ int ref_simp_optimize_active(int nx, int ny, int nz, double h, const uint8_t* ta
     o.cg_max_iterations = cg_max_it;
     o.solver = SolverKind::MultigridCG_Matfree;
     o.active_domain_band = band;
+    if (updater == 1) o.updater = SimpUpdater::MMA;  // plateau stop at its defaults
     if (seed) o.initial_design.assign(seed, seed + g.voxel_count());
     std::vector<double> af;
     o.observe = [&](const SimpIterationObservation& ob) { af.push_back(ob.active_fraction); };

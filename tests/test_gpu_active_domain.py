@@ -65,12 +65,13 @@ def _reason(golden, name):
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("name", list(ACTIVE_DOMAIN_RUNS))
 def test_active_domain_runs_match_reference(tg, golden, name, prec):
-    """Restricted trajectory solves (plain and masked), the escape latch, a failed
-    restricted solve re-solved on the full domain, and the fraction latch."""
-    o, mask, seed, band, radius, vf, its = active_domain_case(name)
+    """Restricted trajectory solves (plain, masked, and under the MMA updater), the
+    escape latch, a failed restricted solve re-solved on the full domain, and the
+    fraction latch."""
+    o, mask, seed, band, radius, vf, its, upd = active_domain_case(name)
     s = tg.simp_optimize(_tg_problem(tg, o), tg.SimpParams(), tg.SimpOptions(
         volume_fraction=vf, filter_radius=radius, move=0.2, change_tol=0.0, max_iterations=its,
-        cg_tolerance=1e-9, initial_design=seed, active_domain_band=band,
+        cg_tolerance=1e-9, initial_design=seed, active_domain_band=band, updater=upd,
         solve=tg.SolveOptions(precision=prec)), mask=mask)
     k = "adr_" + name
     ad = s["active_domain"]
@@ -90,7 +91,7 @@ def test_active_domain_off_is_unchanged(tg):
     """band 0 (the default) runs exactly the unarmed loop: every fraction 1, no
     record; the same run with the band armed on a compact domain latches at the
     fifth iteration and then matches it step for step."""
-    o, _, _, _, radius, vf, its = active_domain_case("latch")
+    o, _, _, _, radius, vf, its, _ = active_domain_case("latch")
     base = dict(volume_fraction=vf, filter_radius=radius, move=0.2, change_tol=0.0,
                 max_iterations=its, cg_tolerance=1e-9)
     off = tg.simp_optimize(_tg_problem(tg, o), tg.SimpParams(), tg.SimpOptions(**base))

@@ -354,16 +354,17 @@ def ad_reason(golden, name):
     return r.replace("fea_solve_cg_matfree:", "fea_solve_mgcg_matfree:")
 
 
-@pytest.mark.parametrize("name", ["restricted", "masked", "escape", "failed", "latch"])
+@pytest.mark.parametrize("name", ["restricted", "masked", "escape", "failed", "latch", "mma"])
 def test_active_domain_runs_golden(port, golden, name):
     """simp_optimize with active_domain_band (active_domain_solve,
     simp.cpp:1809-1896): the restricted trajectory solves, the per-iteration
     active fraction, each latch (escape, fraction, failed restricted solve) with
     its iteration and reason, and the full-domain certification: identical."""
     from oracle.oracle import active_domain_case
-    pb, mask, seed, band, radius, vf, its = active_domain_case(name)
+    pb, mask, seed, band, radius, vf, its, upd = active_domain_case(name)
     s = port.simp_optimize_active(pb, band, mask=mask, seed=seed, radius=radius, volfrac=vf,
-                                  move=0.2, max_it=its, change_tol=0.0, cg_tol=1e-9)
+                                  move=0.2, max_it=its, change_tol=0.0, cg_tol=1e-9,
+                                  updater=upd)
     k = "adr_" + name
     assert [s["iterations"], s["band"], int(s["latched"]), s["latch_iteration"],
             s["escape_count"]] == golden[k + "_i"].tolist()
@@ -373,5 +374,5 @@ def test_active_domain_runs_golden(port, golden, name):
     assert [s["compliance"], s["volume_fraction"], s["fraction_mean"]] == \
         golden[k + "_d"].tolist()
     assert s["reason"] == ad_reason(golden, name)
-    if name in ("restricted", "masked"):
+    if name in ("restricted", "masked", "mma"):
         assert not s["latched"] and s["hist_af"].max() < 0.85
