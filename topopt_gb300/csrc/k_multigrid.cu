@@ -107,6 +107,28 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
     T acc[24];
 #pragma unroll
     for (int r = 0; r < 24; ++r) acc[r] = T(0);
+    // Level 1: the children's moduli (lane ch holds child ch's) and this lane's
+    // kept bit of every child (bit ch), all requested before the child loop.
+    T f_lane = T(0);
+    unsigned int kept_bits = 0;
+    if (LEVEL1) {
+      if (lane < 8) {
+        const int fi = 2 * I + cx(lane), fj = 2 * J + cy(lane), fk = 2 * K + cz(lane);
+        if (fi < fd.ex && fj < fd.ey && fk < fd.ez)
+          f_lane = ef[(int64_t(fk) * fd.ey + fj) * fd.ex + fi];
+      }
+      if (lane < 24) {
+        const int c = lane / 3, comp = lane % 3;
+#pragma unroll
+        for (int ch = 0; ch < 8; ++ch) {
+          const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
+          if (fi >= fd.ex || fj >= fd.ey || fk >= fd.ez) continue;
+          const int64_t node =
+              (int64_t(fk + cz(c)) * fd.nny + (fj + cy(c))) * fd.nnx + (fi + cx(c));
+          if (fact[3 * node + comp]) kept_bits |= 1u << ch;
+        }
+      }
+    }
     for (int ch = 0; ch < 8; ++ch) {
       const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
       if (fi >= fd.ex || fj >= fd.ey || fk >= fd.ez) continue;
@@ -114,16 +136,9 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
       T f = T(1);
       unsigned int m = 0xffffffu;
       if (LEVEL1) {
-        f = ef[fe];
+        f = __shfl_sync(0xffffffffu, f_lane, ch);
         if (f == T(0)) continue;
-        unsigned int mm = 0;
-        if (lane < 24) {
-          const int c = lane / 3, comp = lane % 3;
-          const int64_t node =
-              (int64_t(fk + cz(c)) * fd.nny + (fj + cy(c))) * fd.nnx + (fi + cx(c));
-          if (fact[3 * node + comp]) mm = 1u << lane;
-        }
-        m = __reduce_or_sync(0xffffffffu, mm);
+        m = __reduce_or_sync(0xffffffffu, ((kept_bits >> ch) & 1u) << lane);
         if (m == 0xffffffu && hm == 0) {
           if (lane < 24)
 #pragma unroll
