@@ -926,9 +926,12 @@ double job_sensitivity(tg_job* j, const uint8_t* elem = nullptr) {
   const Grid& g = j->fp.g;
   const tg_simp_params& p = j->params;
   int nparts = 0;
+  // The mixed form evaluates element energies in double-float (~1e-14), the
+  // plain form in FP64 as the reference does.
   launch_sensitivity(g, j->fp.mc, j->xphys.p, elem ? elem : j->fp.elem.p, j->u.p,
                      p.youngs_modulus, p.penalty, p.density_min, p.material_law, p.e_min,
-                     j->dc.p, j->part.p, &nparts, j->s);
+                     j->dc.p, j->part.p, &nparts, j->s,
+                     j->opt.solve.precision == TG_PREC_MIXED);
   launch_sum_partials(j->part.p, nparts, j->scal.p, j->s);
   return read1(j, j->scal.p);
 }

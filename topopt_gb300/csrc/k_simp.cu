@@ -109,17 +109,20 @@ __global__ void k_modulus(const double* __restrict__ rho, const uint8_t* __restr
 }
 
 // The same Walsh-modal element operator as k_operator.cu, unit modulus, FP64.
-struct Modal64 {
-  double L0, L1, M0, M1, M02, M12, LM2;
+template <class C>
+struct ModalC {
+  C L0, L1, M0, M1, M02, M12, LM2;
 };
+using Modal64 = ModalC<double>;
 
-__device__ __forceinline__ void walsh_fwd(double (&v)[8]) {
+template <class C>
+__device__ __forceinline__ void walsh_fwd(C (&v)[8]) {
 #pragma unroll
   for (int b = 1; b < 8; b <<= 1)
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       if (i & b) continue;
-      const double lo = v[i], hi = v[i | b];
+      const C lo = v[i], hi = v[i | b];
       v[i] = hi + lo;
       v[i | b] = hi - lo;
     }
@@ -129,27 +132,28 @@ __device__ __forceinline__ void walsh_fwd(double (&v)[8]) {
 // q = sum over monomial classes of (unnormalised) modes x stresses, which is
 // u . (K u) evaluated in the modal basis (Parseval of the Walsh transform: the
 // corner-space dot equals 1/8 of the mode-space dot).
-__device__ __forceinline__ double modal_energy(const Modal64& mc, double (&ux)[8],
-                                               double (&uy)[8], double (&uz)[8]) {
+template <class C>
+__device__ __forceinline__ C modal_energy(const ModalC<C>& mc, C (&ux)[8], C (&uy)[8],
+                                          C (&uz)[8]) {
   walsh_fwd(ux);
   walsh_fwd(uy);
   walsh_fwd(uz);
-  double gx[8], gy[8], gz[8];
+  C gx[8], gy[8], gz[8];
   {
-    const double Ltr = mc.L0 * (ux[1] + uy[2] + uz[4]);
+    const C Ltr = mc.L0 * (ux[1] + uy[2] + uz[4]);
     gx[1] = Ltr + mc.M02 * ux[1];
     gy[2] = Ltr + mc.M02 * uy[2];
     gz[4] = Ltr + mc.M02 * uz[4];
-    const double txy = mc.M0 * (uy[1] + ux[2]);
-    const double txz = mc.M0 * (uz[1] + ux[4]);
-    const double tyz = mc.M0 * (uz[2] + uy[4]);
+    const C txy = mc.M0 * (uy[1] + ux[2]);
+    const C txz = mc.M0 * (uz[1] + ux[4]);
+    const C tyz = mc.M0 * (uz[2] + uy[4]);
     gy[1] = txy; gz[1] = txz;
     gx[2] = txy; gz[2] = tyz;
     gx[4] = txz; gy[4] = tyz;
   }
   {
-    const double Ltr = mc.L1 * (uy[3] + uz[5]);
-    const double t = mc.M1 * (uz[3] + uy[5]);
+    const C Ltr = mc.L1 * (uy[3] + uz[5]);
+    const C t = mc.M1 * (uz[3] + uy[5]);
     gx[3] = mc.M1 * ux[3];
     gy[3] = Ltr + mc.M12 * uy[3];
     gz[3] = t;
@@ -158,37 +162,54 @@ __device__ __forceinline__ double modal_energy(const Modal64& mc, double (&ux)[8
     gz[5] = Ltr + mc.M12 * uz[5];
   }
   {
-    const double Ltr = mc.L1 * (ux[3] + uz[6]);
-    const double t = mc.M1 * (uz[3] + ux[6]);
-    gx[3] += Ltr + mc.M12 * ux[3];
-    gy[3] += mc.M1 * uy[3];
-    gz[3] += t;
+    const C Ltr = mc.L1 * (ux[3] + uz[6]);
+    const C t = mc.M1 * (uz[3] + ux[6]);
+    gx[3] = gx[3] + (Ltr + mc.M12 * ux[3]);
+    gy[3] = gy[3] + (mc.M1 * uy[3]);
+    gz[3] = gz[3] + (t);
     gx[6] = t;
     gy[6] = mc.M1 * uy[6];
     gz[6] = Ltr + mc.M12 * uz[6];
   }
   {
-    const double Ltr = mc.L1 * (ux[5] + uy[6]);
-    const double t = mc.M1 * (uy[5] + ux[6]);
-    gx[5] += Ltr + mc.M12 * ux[5];
-    gy[5] += t;
-    gz[5] += mc.M1 * uz[5];
-    gx[6] += t;
-    gy[6] += Ltr + mc.M12 * uy[6];
-    gz[6] += mc.M1 * uz[6];
+    const C Ltr = mc.L1 * (ux[5] + uy[6]);
+    const C t = mc.M1 * (uy[5] + ux[6]);
+    gx[5] = gx[5] + (Ltr + mc.M12 * ux[5]);
+    gy[5] = gy[5] + (t);
+    gz[5] = gz[5] + (mc.M1 * uz[5]);
+    gx[6] = gx[6] + (t);
+    gy[6] = gy[6] + (Ltr + mc.M12 * uy[6]);
+    gz[6] = gz[6] + (mc.M1 * uz[6]);
   }
   gx[7] = mc.LM2 * ux[7];
   gy[7] = mc.LM2 * uy[7];
   gz[7] = mc.LM2 * uz[7];
   // K u = H g (corner space), so u.(K u) = (H^T u).g = sum over modes of M.g,
   // where M = H^T u are exactly the unnormalised mode coefficients above.
-  double q = 0.0;
+  C q = ux[1] * gx[1] + uy[1] * gy[1] + uz[1] * gz[1];
 #pragma unroll
-  for (int i = 1; i < 8; ++i) q += ux[i] * gx[i] + uy[i] * gy[i] + uz[i] * gz[i];
+  for (int i = 2; i < 8; ++i) q = q + (ux[i] * gx[i] + uy[i] * gy[i] + uz[i] * gz[i]);
   return q;
 }
 
-__global__ void k_sensitivity(GridDev g, Modal64 mc, const double* __restrict__ rho,
+// Element energies in C: FP64 (the plain form: the reference's arithmetic), or
+// double-float (the mixed form: FP32 pairs, ~1e-14 relative, on the FP32 pipe
+// instead of GB300's narrow FP64 one); the material law and the sums stay FP64.
+template <class C>
+__device__ __forceinline__ C to_c(double v);
+template <>
+__device__ __forceinline__ double to_c<double>(double v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ df to_c<df>(double v) {
+  return df_from(v);
+}
+__device__ __forceinline__ double from_c(double v) { return v; }
+__device__ __forceinline__ double from_c(df v) { return df_to_double(v); }
+
+template <class C>
+__global__ void k_sensitivity(GridDev g, ModalC<C> mc, const double* __restrict__ rho,
                               const uint8_t* __restrict__ elem, const double* __restrict__ u,
                               double E0, double p, double rho_min, int law, double emin,
                               double* __restrict__ dc, double* __restrict__ c_part) {
@@ -200,16 +221,16 @@ __global__ void k_sensitivity(GridDev g, Modal64 mc, const double* __restrict__ 
     if (elem[e]) {
       int i, j, k;
       vox_ijk(g, e, i, j, k);
-      double ux[8], uy[8], uz[8];
+      C ux[8], uy[8], uz[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         const int64_t node =
             (int64_t(k + (c >> 2)) * g.nny + (j + ((c >> 1) & 1))) * g.nnx + i + (c & 1);
-        ux[c] = u[3 * node];
-        uy[c] = u[3 * node + 1];
-        uz[c] = u[3 * node + 2];
+        ux[c] = to_c<C>(u[3 * node]);
+        uy[c] = to_c<C>(u[3 * node + 1]);
+        uz[c] = to_c<C>(u[3 * node + 2]);
       }
-      const double q = modal_energy(mc, ux, uy, uz);
+      const double q = from_c(modal_energy(mc, ux, uy, uz));
       if (law == 0) {
         const double r = clamp_density(rho[e], rho_min);
         csum += powp(r, p) * E0 * q;
@@ -881,12 +902,19 @@ void launch_modulus(const double* rho, const uint8_t* elem, int64_t n, double E0
 void launch_sensitivity(const Grid& g, const ModalConsts& c, const double* rho,
                         const uint8_t* elem, const double* u, double E0, double p,
                         double rho_min, int law, double emin, double* dc, double* c_part,
-                        int* nparts, cudaStream_t s) {
+                        int* nparts, cudaStream_t s, bool double_float) {
   const Modal64 mc{c.L[0], c.L[1], c.M[0], c.M[1], 2 * c.M[0], 2 * c.M[1], c.L[2] + 4 * c.M[2]};
   const int nb = grid_blocks(g.nv);
   *nparts = nb;
-  k_sensitivity<<<nb, kThreads, 0, s>>>(dev(g), mc, rho, elem, u, E0, p, rho_min, law, emin, dc,
-                                        c_part);
+  if (double_float) {
+    const ModalC<df> m2{df_from(mc.L0), df_from(mc.L1), df_from(mc.M0), df_from(mc.M1),
+                        df_from(mc.M02), df_from(mc.M12), df_from(mc.LM2)};
+    k_sensitivity<df><<<nb, kThreads, 0, s>>>(dev(g), m2, rho, elem, u, E0, p, rho_min, law,
+                                              emin, dc, c_part);
+  } else {
+    k_sensitivity<double><<<nb, kThreads, 0, s>>>(dev(g), mc, rho, elem, u, E0, p, rho_min, law,
+                                                  emin, dc, c_part);
+  }
   TG_LAUNCH_CHECK();
 }
 

@@ -214,7 +214,8 @@ void launch_modulus(const double* rho, const uint8_t* elem, int64_t n, double E0
 void launch_sensitivity(const Grid& g, const ModalConsts& mc, const double* rho,
                         const uint8_t* elem, const double* u, double E0, double p,
                         double rho_min, int law, double emin, double* dc, double* c_part,
-                        int* nparts, cudaStream_t s);
+                        int* nparts, cudaStream_t s,
+                        bool double_float = false);
 
 struct FilterStencil {
   int R = 0, n = 0;
