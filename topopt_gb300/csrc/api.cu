@@ -727,6 +727,16 @@ struct tg_job {
       fraction_sum += f;
       ++fraction_count;
     }
+    // The latch is one way: the restricted system is not solved again, so its
+    // device memory goes back (stream-ordered) when the mask is switched off.
+    void release_restricted() {
+      solver.reset();
+      fp = FineProblem{};
+      built_h.clear();
+      built_h.shrink_to_fit();
+      cur_h.clear();
+      cur_h.shrink_to_fit();
+    }
     size_t bytes() const {
       return tags.bytes() + prev.bytes() + cur.bytes() + tmp.bytes() + count.bytes() +
              fp.device_bytes() + (solver ? solver->device_bytes() : 0);
@@ -980,6 +990,7 @@ SolverStats ad_job_solve(tg_job* j, double tol, int max_it, double* af, const ui
       ad.latched = true;
       ad.latch_iteration = iteration;
       ad.escape_count = esc;
+      ad.release_restricted();
       char buf[192];
       std::snprintf(buf, sizeof buf,
                     "escape detected: %lld element(s) took material outside the active band "
@@ -1019,6 +1030,8 @@ SolverStats ad_job_solve(tg_job* j, double tol, int max_it, double* af, const ui
           if (++ad.hot_streak >= 5) {
             ad.latched = true;
             ad.latch_iteration = iteration;
+            // This solve's u and element set are read by the sensitivity that
+            // follows; the restricted system is released at the next solve.
             char buf[192];
             std::snprintf(buf, sizeof buf,
                           "active fraction >= %.2f for %d consecutive iterations (band covers "
@@ -1040,12 +1053,12 @@ SolverStats ad_job_solve(tg_job* j, double tol, int max_it, double* af, const ui
         ad.latch_iteration = iteration;
         ad.reason = std::string("restricted solve failed: fea_solve_mgcg_matfree: ") + e.what();
         ad.record(1.0);
-        ad.solver.reset();
-        ad.built_h.clear();
+        ad.release_restricted();
       }
     }
   } else if (ad.band > 0) {
     ad.record(1.0);  // latched: still counted, as 1.0
+    if (ad.solver) ad.release_restricted();  // latched on the fraction last iteration
   }
   return job_solve(j, tol, max_it);
 }
