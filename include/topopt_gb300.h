@@ -111,9 +111,17 @@ typedef struct {
                               TG_RESIDUAL_DF (0, default) in double-float arithmetic (FP32
                               pairs, ~48 significant bits, on the FP32 pipe), TG_RESIDUAL_FP64
                               with the native FP64 operator */
+  int32_t coarse_smoother; /* mixed: the smoother of the FP32 V-cycle's levels >= 2:
+                              TG_SMOOTHER_AUTO (0) Chebyshev on grids of >= 200K elements,
+                              Jacobi below; TG_SMOOTHER_JACOBI (1) damped Jacobi (the
+                              reference's); TG_SMOOTHER_CHEBYSHEV (2) a degree-3 Chebyshev
+                              polynomial in D^-1 A on [lmax / 30, lmax], lmax by power
+                              iteration per hierarchy build.  The FP64 V-cycle always uses
+                              damped Jacobi. */
 } tg_solve_options;
 
 enum { TG_RESIDUAL_DF = 0, TG_RESIDUAL_FP64 = 1 };
+enum { TG_SMOOTHER_AUTO = 0, TG_SMOOTHER_JACOBI = 1, TG_SMOOTHER_CHEBYSHEV = 2 };
 
 /* CgInfo subset (core/include/topopt/fea.hpp:272-382). */
 typedef struct {

@@ -282,3 +282,33 @@ def test_mixed_solve_residual_forms_agree(tg, residual):
         precision=tg.PREC_MIXED, mixed_residual=residual))
     assert info.converged and info.residual <= 1e-10
     assert rel(um, u64) < 1e-8
+
+
+def test_mixed_coarse_smoothers_agree(tg):
+    """The FP32 V-cycle's coarse smoother (damped Jacobi or the Chebyshev
+    polynomial) changes the preconditioner, not the answer: both mixed runs track
+    the FP64 run's compliance history within 1e-6.  On a seeded high-contrast
+    design (a thin beam at 1, the box at the density floor, stiffness contrast
+    ~1e-8) Chebyshev needs no more inner iterations than Jacobi.  Bad values are
+    rejected."""
+    from oracle.oracle import beam_seed
+    nx, ny, nz = 96, 48, 48
+    o = cantilever(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                    list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+    base = dict(volume_fraction=0.05, filter_radius=1.5, change_tol=0.0, max_iterations=8,
+                cg_tolerance=1e-9, initial_design=beam_seed(nx, ny, nz, half_width=3))
+    ref = tg.simp_optimize(pb, tg.SimpParams(), tg.SimpOptions(**base))
+    hc64 = np.array([h["compliance"] for h in ref["history"]])
+    cg = {}
+    for sm in (tg.SMOOTHER_JACOBI, tg.SMOOTHER_CHEBYSHEV):
+        s = tg.simp_optimize(pb, tg.SimpParams(), tg.SimpOptions(
+            solve=tg.SolveOptions(precision=tg.PREC_MIXED, coarse_smoother=sm), **base))
+        hc = np.array([h["compliance"] for h in s["history"]])
+        assert rel(hc, hc64) < 1e-6
+        assert abs(s["compliance"] - ref["compliance"]) <= 1e-8 * ref["compliance"]
+        cg[sm] = sum(h["cg_iterations"] for h in s["history"])
+    assert cg[tg.SMOOTHER_CHEBYSHEV] <= cg[tg.SMOOTHER_JACOBI]
+    with pytest.raises(ValueError, match="coarse_smoother"):
+        tg.simp_optimize(pb, tg.SimpParams(), tg.SimpOptions(
+            solve=tg.SolveOptions(precision=tg.PREC_MIXED, coarse_smoother=7), **base))

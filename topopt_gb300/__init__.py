@@ -74,6 +74,9 @@ from ._capi import (  # noqa: F401
     UPDATER_MMA,
     RESIDUAL_DF,
     RESIDUAL_FP64,
+    SMOOTHER_AUTO,
+    SMOOTHER_CHEBYSHEV,
+    SMOOTHER_JACOBI,
     UPDATER_OC,
     SOLVER_MGCG,
     SOLVER_JACOBI_CG,

@@ -25,6 +25,7 @@ SOLVER_MGCG, SOLVER_JACOBI_CG = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 UPDATER_OC, UPDATER_MMA = 0, 1
 RESIDUAL_DF, RESIDUAL_FP64 = 0, 1
+SMOOTHER_AUTO, SMOOTHER_JACOBI, SMOOTHER_CHEBYSHEV = 0, 1, 2
 
 
 class LibraryMissing(RuntimeError):
@@ -64,7 +65,8 @@ class _SolveOpt(C.Structure):
                 ("mg_iter_budget", C.c_int32), ("omega", C.c_double),
                 ("inner_tolerance", C.c_double), ("max_refinements", C.c_int32),
                 ("coarsening", C.c_int32), ("graph_mode", C.c_int32),
-                ("smooth_sweeps", C.c_int32), ("mixed_residual", C.c_int32)]
+                ("smooth_sweeps", C.c_int32), ("mixed_residual", C.c_int32),
+                ("coarse_smoother", C.c_int32)]
 
 
 class _CgInfo(C.Structure):
@@ -287,12 +289,13 @@ class SolveOptions:
     graph_mode: int = 0  # GRAPH_ON / GRAPH_OFF
     smooth_sweeps: int = 0  # Jacobi sweeps per side of the coarse correction (0 = 1)
     mixed_residual: int = 0  # RESIDUAL_DF (double-float, default) / RESIDUAL_FP64
+    coarse_smoother: int = 0  # SMOOTHER_AUTO / SMOOTHER_JACOBI / SMOOTHER_CHEBYSHEV (mixed)
 
     def _c(self):
         return _SolveOpt(self.solver, self.precision, self.mg_levels, self.mg_iter_budget,
                          self.omega, self.inner_tolerance, self.max_refinements,
                          self.coarsening, self.graph_mode, self.smooth_sweeps,
-                         self.mixed_residual)
+                         self.mixed_residual, self.coarse_smoother)
 
 
 @dataclass

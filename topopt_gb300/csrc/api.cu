@@ -201,6 +201,8 @@ tg_solve_options default_solve(const tg_solve_options* o) {
     raise(TG_EINVAL, "solve options: smooth_sweeps must be in [0, 8]");
   if (d.mixed_residual != TG_RESIDUAL_DF && d.mixed_residual != TG_RESIDUAL_FP64)
     raise(TG_EINVAL, "solve options: unknown mixed_residual");
+  if (d.coarse_smoother < TG_SMOOTHER_AUTO || d.coarse_smoother > TG_SMOOTHER_CHEBYSHEV)
+    raise(TG_EINVAL, "solve options: unknown coarse_smoother");
   return d;
 }
 

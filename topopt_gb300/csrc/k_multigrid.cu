@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(192) k_stencil_op(MgDims d, const T* __restric
                                                     const T* __restrict__ x,
                                                     const T* __restrict__ b,
                                                     const T* __restrict__ invdiag, T omega,
-                                                    T* __restrict__ y) {
+                                                    T* __restrict__ y, ChebStep ch) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   const int64_t sy = d.nnx, sz = int64_t(d.nnx) * d.nny;
   // Block (32, 3, 2): x the node along x, y the component, z the node row along y.
@@ -316,14 +316,63 @@ __global__ void __launch_bounds__(192) k_stencil_op(MgDims d, const T* __restric
   T out;
   if (!act[dof]) {
     out = T(0);
+    if (MODE == kCheb) static_cast<T*>(ch.dir_)[dof] = T(0);
   } else if (MODE == kApply) {
     out = s;
   } else if (MODE == kResidual) {
     out = b[dof] - s;
+  } else if (MODE == kCheb) {
+    // Chebyshev step `ch.step` on [lmax / ratio, lmax] of D^-1 A (Saad,
+    // Iterative Methods, Alg. 12.1): d_k = rho_k rho_{k-1} d_{k-1} +
+    // (2 rho_k / delta) D^-1 (b - A x_k), d_0 = D^-1 (b - A x_0) / theta,
+    // x_{k+1} = x_k + d_k; rho_0 = delta / theta, rho_k = 1 / (2 theta / delta - rho_{k-1}).
+    const double lmax = ch.lam[0], lmin = lmax / ch.ratio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sig = theta / delta;
+    double rp = 1.0 / sig, rk = rp;
+    for (int i = 1; i <= ch.step; ++i) {
+      rp = rk;
+      rk = 1.0 / (2.0 * sig - rp);
+    }
+    const T res = invdiag[dof] * (b[dof] - s);
+    T* dir = static_cast<T*>(ch.dir_);
+    const T dn = ch.step == 0 ? T(1.0 / theta) * res
+                              : T(rk * rp) * dir[dof] + T(2.0 * rk / delta) * res;
+    dir[dof] = dn;
+    out = x[dof] + dn;
   } else {
     out = x[dof] + omega * invdiag[dof] * (b[dof] - s);
   }
   y[dof] = out;
+}
+
+// Power iteration for lambda_max(D^-1 A) of one stencil level: v on the
+// active DOFs from a fixed hash, then w = D^-1 A v, v = w / |w|; |w| -> lam.
+template <class T>
+__global__ void k_pi_init(const uint8_t* __restrict__ act, int64_t n, T* __restrict__ v) {
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads) {
+    uint32_t h = uint32_t(i) * 2654435761u;
+    h ^= h >> 16;
+    v[i] = act[i] ? T(0.5) + T(h & 0xffff) * T(1.0 / 65536.0) : T(0);
+  }
+}
+template <class T>
+__global__ void k_pi_dinv(T* __restrict__ w, const T* __restrict__ invdiag, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads)
+    w[i] *= invdiag[i];
+}
+template <class T>
+__global__ void k_pi_scale(T* __restrict__ v, const T* __restrict__ w,
+                           const double* __restrict__ nrm2, int64_t n) {
+  const double q = nrm2[0] > 0.0 ? 1.0 / sqrt(nrm2[0]) : 0.0;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads)
+    v[i] = T(q) * w[i];
+}
+__global__ void k_pi_lambda(const double* __restrict__ nrm2, double safety,
+                            double* __restrict__ lam) {
+  if (threadIdx.x == 0) lam[0] = safety * sqrt(nrm2[0] > 0.0 ? nrm2[0] : 1.0);
 }
 
 // x = omega * invdiag .* b (the first smoother sweep from a zero iterate).
@@ -647,16 +696,45 @@ void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s) {
 
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
-                   const T* b, const T* invdiag, T omega, T* y, cudaStream_t s) {
+                   const T* b, const T* invdiag, T omega, T* y, cudaStream_t s,
+                   ChebStep ch) {
   const dim3 nb((d.nnx + 31) / 32, (d.nny + 1) / 2, d.nnz), nt(32, 3, 2);
   if (mode == kApply)
-    k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
   else if (mode == kResidual)
-    k_stencil_op<T, kResidual><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kResidual><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
+  else if (mode == kCheb)
+    k_stencil_op<T, kCheb><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
   else
-    k_stencil_op<T, kSmooth><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y);
+    k_stencil_op<T, kSmooth><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
   TG_LAUNCH_CHECK();
 }
+
+template <class T>
+void mg_lambda_max(const MgDims& d, const T* A, const uint8_t* act, const T* invdiag, T* v,
+                   T* w, int iters, double safety, double* part, double* nrm2, double* lam,
+                   cudaStream_t s) {
+  const int64_t n = 3 * int64_t(d.nnx) * d.nny * d.nnz;
+  const int nbk = nblk(n);
+  k_pi_init<T><<<nbk, kThreads, 0, s>>>(act, n, v);
+  TG_LAUNCH_CHECK();
+  for (int it = 0; it < iters; ++it) {
+    mg_stencil_op<T>(kApply, d, A, act, v, nullptr, nullptr, T(0), w, s);
+    k_pi_dinv<T><<<nbk, kThreads, 0, s>>>(w, invdiag, n);
+    TG_LAUNCH_CHECK();
+    if constexpr (sizeof(T) == 4)
+      launch_dot_f(w, w, n, part, nrm2, s);
+    else
+      launch_dot(w, w, n, part, nrm2, s);
+    k_pi_scale<T><<<nbk, kThreads, 0, s>>>(v, w, nrm2, n);
+    TG_LAUNCH_CHECK();
+  }
+  k_pi_lambda<<<1, 32, 0, s>>>(nrm2, safety, lam);
+  TG_LAUNCH_CHECK();
+}
+template void mg_lambda_max<float>(const MgDims&, const float*, const uint8_t*, const float*,
+                                   float*, float*, int, double, double*, double*, double*,
+                                   cudaStream_t);
 
 template <class T>
 void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cudaStream_t s) {
@@ -727,7 +805,7 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
 
 #define TG_INST(T)                                                                            \
   template void mg_stencil_op<T>(int, const MgDims&, const T*, const uint8_t*, const T*,      \
-                                 const T*, const T*, T, T*, cudaStream_t);                    \
+                                 const T*, const T*, T, T*, cudaStream_t, ChebStep);          \
   template void mg_jacobi_first<T>(const T*, const T*, T, int64_t, T*, cudaStream_t);         \
   template void mg_restrict<T>(const MgDims&, const MgDims&, const T*, const uint8_t*, T*,    \
                                cudaStream_t);                                                 \

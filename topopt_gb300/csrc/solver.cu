@@ -187,6 +187,7 @@ struct Solver::Level {
   DBuf<double> Kel, A, invd, xa, xb, b;
   // FP32 operators and vectors (mixed form).
   DBuf<float> Kelf, Af, invdf, fxa, fxb, fb;
+  DBuf<float> chd;  // Chebyshev direction (mixed form, levels >= 2)
   double *x = nullptr, *r = nullptr;
   float *xf = nullptr, *rf = nullptr;
   template <class T>
@@ -206,6 +207,7 @@ struct Solver::Level {
   size_t bytes() const {
     return act.bytes() + Kel.bytes() + A.bytes() + invd.bytes() + xa.bytes() + xb.bytes() +
            b.bytes() + Kelf.bytes() + Af.bytes() + invdf.bytes() + fxa.bytes() + fxb.bytes() +
+           chd.bytes() +
            fb.bytes();
   }
 };
@@ -260,6 +262,12 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   sweeps_ = opt.smooth_sweeps > 0 ? opt.smooth_sweeps : 1;
   df_residual_ = opt.mixed_residual != TG_RESIDUAL_FP64;
   mixed_ = opt.precision == TG_PREC_MIXED;
+  // Coarse levels >= 2 of the FP32 V-cycle: Chebyshev by default on grids of
+  // >= 200K elements (below that the extra launches of the small levels cost
+  // more than the PCG iterations they save), damped Jacobi otherwise.
+  const bool cheb = opt.coarse_smoother == TG_SMOOTHER_CHEBYSHEV ||
+                    (opt.coarse_smoother == TG_SMOOTHER_AUTO && fp.g.nv >= 200000);
+  cheb_m_ = (mixed_ && cheb) ? 3 : 0;
   const size_t n = size_t(fp.g.ndof);
   for (DBuf<double>* b : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_}) b->alloc(n);
   part_n_ = std::max({kRedBlocks, fine_op_blocks(fp.g, true), fine_op_blocks(fp.g, false),
@@ -551,6 +559,18 @@ bool Solver::build_numeric() {
     mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, L.Am<T>(), L.Dinv<T>(), s_);
     pd = L.d;
   }
+  if (sizeof(T) == 4 && cheb_m_ > 0) {
+    // lambda_max(D^-1 A) of every smoothed level >= 2 for its Chebyshev smoother.
+    if (!lam_.p) lam_.alloc(levels_.size() + 1);
+    if (!pi_.p) pi_.alloc(1);
+    for (size_t li = 1; li + 1 < levels_.size(); ++li) {
+      Level& L = *levels_[li];
+      if (!L.chd.p) L.chd.alloc(size_t(L.ndof));
+      mg_lambda_max<float>(L.d, L.Am<float>(), L.act.p, L.Dinv<float>(), L.X<float>(),
+                           L.R<float>(), cheb_iters_, cheb_safety_, part_.p, pi_.p,
+                           lam_.p + li, s_);
+    }
+  }
   Level& C = *levels_.back();
   mg_dense_from_stencil<T>(C.d, C.Am<T>(), cidx_.p, nc_, chol_.p, s_);
   TG_CUDA(cudaMemsetAsync(chol_fail_.p, 0, sizeof(int), s_));
@@ -580,6 +600,27 @@ void Solver::vcycle_level(size_t l) {
     mg_stencil_op<T>(mode, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w, L.R<T>(),
                      s_);
   };
+  if (sizeof(T) == 4 && cheb_m_ > 0 && l >= 2) {
+    // Mixed form, levels >= 2: a degree-cheb_m_ Chebyshev polynomial in D^-1 A
+    // before (from a zero iterate) and after the coarse correction.
+    ChebStep ch{L.chd.p, lam_.p + (l - 1), cheb_ratio_, 0};
+    auto cheb = [&] {
+      for (int k = 0; k < cheb_m_; ++k) {
+        ch.step = k;
+        mg_stencil_op<T>(kCheb, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
+                         L.R<T>(), s_, ch);
+        std::swap(L.X<T>(), L.R<T>());
+      }
+    };
+    launch_fill<T>(L.X<T>(), T(0), L.ndof, s_);
+    cheb();
+    op(kResidual);
+    mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
+    vcycle_level<T>(l + 1);
+    mg_prolong_add<T>(L.d, N.d, N.X<T>(), L.act.p, L.X<T>(), s_);
+    cheb();
+    return;
+  }
   // sweeps_ damped-Jacobi sweeps on each side (the first from a zero iterate);
   // every sweep leaves the iterate in X.
   mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);

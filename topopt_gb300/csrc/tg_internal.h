@@ -146,7 +146,7 @@ struct ModalConsts {
 };
 
 // ---------------------------------------------------------------- operator
-enum ApplyMode { kApply = 0, kResidual = 1, kSmooth = 2 };
+enum ApplyMode { kApply = 0, kResidual = 1, kSmooth = 2, kCheb = 3 };
 
 // kResidual of the FP64 operator evaluated in double-float arithmetic (FP32
 // pairs, ~48 significant bits): the refinement residual of the mixed form.

@@ -33,9 +33,25 @@ template <class T>
 void mg_assemble_stencil(const MgDims& d, const T* Kel, const uint8_t* act, T* A, T* invdiag,
                          cudaStream_t s);
 void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s);
+// One Chebyshev smoothing step (kCheb): the direction vector it updates in
+// place (the level's precision), lambda_max of D^-1 A on the device, the
+// interval ratio lmax / lmin and the step index within the polynomial.
+struct ChebStep {
+  void* dir_ = nullptr;
+  const double* lam = nullptr;
+  double ratio = 0.0;
+  int step = 0;
+};
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
-                   const T* b, const T* invdiag, T omega, T* y, cudaStream_t s);
+                   const T* b, const T* invdiag, T omega, T* y, cudaStream_t s,
+                   ChebStep ch = ChebStep{});
+// lambda_max(D^-1 A) of a stencil level by `iters` power-iteration steps (v, w:
+// level-sized scratch), times `safety`, into lam[0] on the device.
+template <class T>
+void mg_lambda_max(const MgDims& d, const T* A, const uint8_t* act, const T* invdiag, T* v,
+                   T* w, int iters, double safety, double* part, double* nrm2, double* lam,
+                   cudaStream_t s);
 template <class T>
 void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cudaStream_t s);
 template <class T>

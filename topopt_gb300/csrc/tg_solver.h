@@ -101,6 +101,14 @@ class Solver {
   int sweeps_ = 1;  // damped-Jacobi sweeps per side of the coarse correction
   bool df_residual_ = true;  // mixed: refinement residual in double-float arithmetic
   bool mixed_partial_ = false;  // the last mixed attempt ran out of budget with progress
+  // Chebyshev smoothing of the FP32 V-cycle's levels >= 2: polynomial degree
+  // (0 = damped Jacobi), interval [lmax / ratio, lmax] of D^-1 A, lmax from a
+  // power iteration times a safety factor, per hierarchy build.
+  int cheb_m_ = 0;
+  double cheb_ratio_ = 30.0;
+  int cheb_iters_ = 10;
+  double cheb_safety_ = 1.1;
+  DBuf<double> lam_, pi_;  // lambda_max per level; the power iteration's norm
   void refinement_residual();  // r = b - A x (FP64 in, FP64 out) for the mixed loop
   bool mixed_ = false;
   // fine state
