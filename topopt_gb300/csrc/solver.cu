@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <thread>
 
 #include "tg_solver.h"
 
@@ -90,6 +91,26 @@ void hex8_ke(double E, double nu, double h, double* ke) {
 }
 
 // ------------------------------------------------------------- FineProblem
+// fn(lo, hi) over [0, n) split across host threads (serial below 64K items).
+// The loops it runs are integer and boolean work with per-thread results
+// combined exactly, so the outcome does not depend on the split.
+template <class F>
+static void host_parallel(int64_t n, F&& fn) {
+  const unsigned hc = std::thread::hardware_concurrency();
+  const int nt = int(std::max(1u, std::min(16u, hc)));
+  if (n < (int64_t(1) << 16) || nt == 1) {
+    fn(0, n, 0);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int64_t chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    const int64_t lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo < hi) th.emplace_back([&fn, lo, hi, t] { fn(lo, hi, t); });
+  }
+  for (std::thread& x : th) x.join();
+}
+
 void FineProblem::build(const tg_grid& grid, double poisson, const tg_dirichlet_bc* bcs, int nbc,
                         const tg_nodal_load* loads, int nloads, const uint8_t* active_mask,
                         cudaStream_t s) {
@@ -105,10 +126,12 @@ void FineProblem::build(const tg_grid& grid, double poisson, const tg_dirichlet_
   ke.assign(576, 0.0);
   hex8_ke(1.0, nu, g.h, ke.data());
   mc.kdiag = ke[0];
-  elem_h.assign(size_t(g.nv), 0);
-  for (int64_t e = 0; e < g.nv; ++e)
-    elem_h[size_t(e)] = uint8_t((grid.tags == nullptr || grid.tags[e] != 0) &&
-                                (active_mask == nullptr || active_mask[e] != 0));
+  elem_h.resize(size_t(g.nv));
+  host_parallel(g.nv, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t e = lo; e < hi; ++e)
+      elem_h[size_t(e)] = uint8_t((grid.tags == nullptr || grid.tags[e] != 0) &&
+                                  (active_mask == nullptr || active_mask[e] != 0));
+  });
   std::vector<uint8_t>& fixed = fixed_h;
   fixed.assign(size_t(g.ndof), 0);
   std::vector<uint8_t> touched(size_t(g.nnodes), 0);
@@ -129,39 +152,68 @@ void FineProblem::build(const tg_grid& grid, double poisson, const tg_dirichlet_
       raise(TG_EINVAL, "load index out of range");
     f_h[size_t(3 * int64_t(loads[l].node) + loads[l].component)] += loads[l].value;
   }
-  for (int k = 0; k < g.nz; ++k)
-    for (int j = 0; j < g.ny; ++j)
-      for (int i = 0; i < g.nx; ++i) {
-        if (!elem_h[size_t((int64_t(k) * g.ny + j) * g.nx + i)]) continue;
-        for (int c = 0; c < 8; ++c) {
-          const int64_t n = (int64_t(k + (c >> 2)) * g.nny + (j + ((c >> 1) & 1))) * g.nnx + i + (c & 1);
-          touched[size_t(n)] = 1;
+  // A node is touched when one of its (up to 8) elements exists.
+  host_parallel(g.nnodes, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t n = lo; n < hi; ++n) {
+      const int a = int(n % g.nnx), b = int((n / g.nnx) % g.nny), c = int(n / (int64_t(g.nnx) * g.nny));
+      uint8_t t = 0;
+      for (int q = 0; q < 8 && !t; ++q) {
+        const int i = a - (q & 1), j = b - ((q >> 1) & 1), k = c - (q >> 2);
+        if (i >= 0 && i < g.nx && j >= 0 && j < g.ny && k >= 0 && k < g.nz)
+          t = elem_h[size_t((int64_t(k) * g.ny + j) * g.nx + i)];
+      }
+      touched[size_t(n)] = t;
+    }
+  });
+  kept_h.resize(size_t(g.ndof));
+  struct Part {
+    int64_t n_free = 0, n_touched_free = 0;
+    double rmax = 0.0;
+    bool void_load = false;
+  };
+  Part part[16];
+  host_parallel(g.ndof, [&](int64_t lo, int64_t hi, int t) {
+    Part p;
+    for (int64_t d = lo; d < hi; ++d) {
+      uint8_t k = 0;
+      if (!fixed[size_t(d)]) {
+        ++p.n_free;
+        p.rmax = std::max(p.rmax, std::fabs(f_h[size_t(d)]));
+        if (touched[size_t(d / 3)]) {
+          ++p.n_touched_free;
+          k = 1;
         }
       }
-  kept_h.assign(size_t(g.ndof), 0);
+      kept_h[size_t(d)] = k;
+    }
+    part[t] = p;
+  });
   ng = 0;
   n_free = 0;
   int64_t n_touched_free = 0;
   double rmax = 0.0;
-  for (int64_t d = 0; d < g.ndof; ++d) {
-    if (fixed[size_t(d)]) continue;
-    ++n_free;
-    rmax = std::max(rmax, std::fabs(f_h[size_t(d)]));
-    if (touched[size_t(d / 3)]) {
-      ++n_touched_free;
-      kept_h[size_t(d)] = 1;
-      ++ng;
-    }
+  for (const Part& p : part) {
+    n_free += p.n_free;
+    n_touched_free += p.n_touched_free;
+    ng += p.n_touched_free;
+    rmax = std::max(rmax, p.rmax);
   }
   if (n_free > 0 && n_touched_free == 0)
     raise(TG_ESINGULAR, "singular system (no stiffness \xe2\x80\x94 every free DOF is void)");
   const double load_tol = 1e-9 * rmax;
-  if (!nonzero_bc)
-    for (int64_t d = 0; d < g.ndof; ++d)
-      if (!fixed[size_t(d)] && !touched[size_t(d / 3)] && std::fabs(f_h[size_t(d)]) > load_tol)
+  if (!nonzero_bc) {
+    host_parallel(g.ndof, [&](int64_t lo, int64_t hi, int t) {
+      bool v = false;
+      for (int64_t d = lo; d < hi && !v; ++d)
+        v = !fixed[size_t(d)] && !touched[size_t(d / 3)] && std::fabs(f_h[size_t(d)]) > load_tol;
+      part[t].void_load = v;
+    });
+    for (const Part& p : part)
+      if (p.void_load)
         raise(TG_ESINGULAR,
               "under-constrained system (load applied to a void DOF with no stiffness \xe2\x80\x94 "
               "no equilibrium possible)");
+  }
   elem.alloc(size_t(g.nv));
   kept.alloc(size_t(g.ndof));
   f.alloc(size_t(g.ndof));
