@@ -687,8 +687,10 @@ void tg_job_destroy(tg_job* job);
  * at most 1,048,576 voxels and a radius of at most 6 voxels (TG_EINVAL beyond);
  * every GPU that loads the library holds the array (~17 MB) until exit.  Calls
  * share it, so calls that overlap on the GPU race -- keep them on one stream.
- * The first call on each device sets up the array's address (make it before any
- * stream capture); no call allocates, frees or leaves state for the next. */
+ * Every call looks up the array's address in the current device's context, so
+ * it stays valid across cudaDeviceReset; the first call on a device may load
+ * the library's module there (make it before any stream capture).  No call
+ * allocates, frees or leaves state for the next. */
 int tg_filter_noalloc(int32_t nx, int32_t ny, int32_t nz, const uint8_t* d_tags, double radius,
                       int32_t adjoint, const double* d_x, double* d_out, void* stream);
 

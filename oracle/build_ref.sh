@@ -4,10 +4,10 @@
 # oracle/_ref/libtopopt_ref.so.  Test infrastructure: a checker and the timed CPU
 # baseline, never linked into the product.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default $TOPOPT_REFERENCE_ROOT, else /root/reference)
 # Skips with exit 0 when the reference tree is absent (e.g. on a GPU machine).
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${TOPOPT_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/core/src" ]; then

@@ -24,6 +24,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libtopopt_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libtopopt_ref.so")
 
+
+def reference_root() -> str:
+    """Root of the reference source tree: $TOPOPT_REFERENCE_ROOT, else the
+    conventional mount point.  The tree is needed only to build or read the
+    reference's own code and fixtures; nothing at run time depends on it."""
+    return os.environ.get("TOPOPT_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_path(*parts: str) -> str:
+    return os.path.join(reference_root(), *parts)
+
+
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _bp = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
@@ -50,7 +62,7 @@ def build_port(force: bool = False) -> str:
 def build_reference() -> str | None:
     """Compile the reference's own code (needs the reference tree); None if absent."""
     script = os.path.join(HERE, "build_ref.sh")
-    subprocess.check_call(["bash", script])
+    subprocess.check_call(["bash", script, reference_root()])
     return REF_SO if os.path.exists(REF_SO) else None
 
 

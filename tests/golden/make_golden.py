@@ -20,10 +20,10 @@ sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
 
 from oracle.oracle import (ACTIVE_DOMAIN_RUNS, CONTINUATION, GATE_V2, OracleLib,  # noqa: E402
                            Problem, active_domain_case, build_reference, cantilever,
-                           gate_v2_problem)
+                           gate_v2_problem, reference_path)
 
-REF_KE_JSON = "/root/reference/core/tests/fixtures/fea/hex_stiffness_reference.json"
-BENCH_JSON = "/root/reference/core/tests/fixtures/benchmarks.json"
+REF_KE_JSON = reference_path("core", "tests", "fixtures", "fea", "hex_stiffness_reference.json")
+BENCH_JSON = reference_path("core", "tests", "fixtures", "benchmarks.json")
 
 
 def main():

@@ -309,6 +309,16 @@ def test_mixed_coarse_smoothers_agree(tg):
         assert abs(s["compliance"] - ref["compliance"]) <= 1e-8 * ref["compliance"]
         cg[sm] = sum(h["cg_iterations"] for h in s["history"])
     assert cg[tg.SMOOTHER_CHEBYSHEV] <= cg[tg.SMOOTHER_JACOBI]
+    # lambda_max of the Chebyshev interval comes from a power iteration: on a
+    # smooth SIMP field neither smoother may make the FP32 preconditioner
+    # indefinite (an inner breakdown) or hand the solve to FP64.
+    E = smooth_modulus(pb)
+    u64, _ = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10)
+    for sm in (tg.SMOOTHER_JACOBI, tg.SMOOTHER_CHEBYSHEV):
+        um, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+            precision=tg.PREC_MIXED, coarse_smoother=sm))
+        assert info.converged and not info.mixed_fallback and info.inner_breakdowns == 0, info
+        assert rel(um, u64) < 1e-8
     with pytest.raises(ValueError, match="coarse_smoother"):
         tg.simp_optimize(pb, tg.SimpParams(), tg.SimpOptions(
             solve=tg.SolveOptions(precision=tg.PREC_MIXED, coarse_smoother=7), **base))

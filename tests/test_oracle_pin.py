@@ -7,9 +7,9 @@ import os
 import numpy as np
 import pytest
 
-from oracle.oracle import Problem, cantilever
+from oracle.oracle import Problem, cantilever, reference_path
 
-REF_KE_JSON = "/root/reference/core/tests/fixtures/fea/hex_stiffness_reference.json"
+REF_KE_JSON = reference_path("core", "tests", "fixtures", "fea", "hex_stiffness_reference.json")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_KE_JSON), reason="reference tree not mounted")
@@ -157,7 +157,7 @@ def test_cfg0_trajectory_prefix(port, golden):
     assert np.array_equal(s["hist_vf"], golden["cfg0_hist_vf"][:10])
 
 
-BENCH_JSON = "/root/reference/core/tests/fixtures/benchmarks.json"
+BENCH_JSON = reference_path("core", "tests", "fixtures", "benchmarks.json")
 
 
 def test_projection_golden(port, golden):

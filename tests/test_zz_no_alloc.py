@@ -16,20 +16,29 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+def _entry(tg):
+    f = tg.lib().tg_filter_noalloc
+    f.argtypes = [ctypes.c_int32] * 3 + [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    return f
+
+
+def _call(tg, pb, tags_dev, radius, adjoint, xd, od):
+    """One call on caller-owned device tensors; raises ValueError on a non-zero status."""
+    import torch
+    rc = _entry(tg)(pb.nx, pb.ny, pb.nz, None if tags_dev is None else tags_dev.data_ptr(),
+                    radius, adjoint, xd.data_ptr(), od.data_ptr(), None)
+    torch.cuda.synchronize()
+    if rc != 0:
+        raise ValueError(tg.lib().tg_last_error().decode())
+
+
 def _noalloc(tg, pb, tags_dev, radius, adjoint, x):
     import torch
     xd = torch.tensor(x, dtype=torch.float64, device="cuda")
     od = torch.full_like(xd, float("nan"))
-    L = tg.lib()
-    f = L.tg_filter_noalloc
-    f.argtypes = [ctypes.c_int32] * 3 + [ctypes.c_void_p, ctypes.c_double, ctypes.c_int32,
-                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-    f.restype = ctypes.c_int
-    rc = f(pb.nx, pb.ny, pb.nz, None if tags_dev is None else tags_dev.data_ptr(), radius, adjoint,
-           xd.data_ptr(), od.data_ptr(), None)
-    torch.cuda.synchronize()
-    if rc != 0:
-        raise ValueError(L.tg_last_error().decode())
+    _call(tg, pb, tags_dev, radius, adjoint, xd, od)
     return od.cpu().numpy()
 
 
@@ -57,3 +66,35 @@ def test_noalloc_filter_rejects_sizes_beyond_its_scratch(tg):
     pb = tg.Problem(128, 128, 65)  # 1,064,960 voxels > 1,048,576
     with pytest.raises(ValueError, match="1,048,576"):
         _noalloc(tg, pb, None, 1.5, 0, np.zeros(pb.nv))
+
+
+def test_noalloc_filter_allocates_nothing(tg):
+    """After one warm-up call, further calls leave the device's free memory
+    unchanged: the scratch is the library's fixed array, nothing else."""
+    import torch
+    rng = np.random.default_rng(3)
+    nx, ny, nz = 64, 48, 40
+    pb = tg.Problem(nx, ny, nz)
+    xd = torch.tensor(rng.random(pb.nv), dtype=torch.float64, device="cuda")
+    od = torch.empty_like(xd)
+    _call(tg, pb, None, 2.5, 0, xd, od)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for radius, adjoint in [(1.5, 0), (2.5, 1), (6.0, 0), (1.2, 1)]:
+        _call(tg, pb, None, radius, adjoint, xd, od)
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
+def test_noalloc_filter_adjoint_without_tags(tg):
+    rng = np.random.default_rng(5)
+    pb = tg.Problem(30, 20, 12)
+    x = rng.random(pb.nv)
+    want = tg.make_density_filter(pb, 2.5).filter_sensitivity(x)
+    assert np.array_equal(_noalloc(tg, pb, None, 2.5, 1, x), want)
+
+
+def test_noalloc_filter_rejects_radius_beyond_its_stencil(tg):
+    pb = tg.Problem(16, 8, 8)
+    with pytest.raises(ValueError, match="radius above 6"):
+        _noalloc(tg, pb, None, 6.5, 0, np.zeros(pb.nv))

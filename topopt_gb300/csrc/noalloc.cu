@@ -23,14 +23,16 @@
 //    entry it reads (mask, stencil, weight sums, scaled sensitivity) before
 //    reading it, so no clearing is needed and a call's result does not depend
 //    on the previous call's contents;
-//  * the first call on each device (with that device current) looks up the
-//    array's device address with cudaGetSymbolAddress and caches it; make that
-//    first call before any stream capture begins.
+//  * every call, with the target device current, looks up the array's device
+//    address with cudaGetSymbolAddress (host code cannot use the symbol itself:
+//    on the host it names a stand-in, not device memory).  The first call on
+//    a device may load the library's module there; make it before any stream
+//    capture begins.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstring>
-#include <mutex>
+#include <string>
 
 #include "tg_internal.h"
 
@@ -57,21 +59,20 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-NoAllocScratch* g_scratch_ptr[kMaxDevices] = {};
-std::mutex g_scratch_mu;
-
-// The array's device address for the current device (looked up once per device).
+// The array's device address in the current device's context.  Looked up on
+// every call (a symbol lookup; it allocates nothing), so the address always
+// belongs to the context that is current now -- also after cudaDeviceReset or a
+// primary context that was torn down and created again.
 NoAllocScratch* scratch_for_current_device() {
   int dev = 0;
   TG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) raise(TG_EINVAL, "tg_filter_noalloc: device ordinal too large");
-  std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    TG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
-  }
-  return g_scratch_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr)
+    raise(TG_EDEVICE, std::string("tg_filter_noalloc: cudaGetSymbolAddress of the scratch "
+                                  "array failed: ") + cudaGetErrorString(e));
+  return static_cast<NoAllocScratch*>(p);
 }
 
 // Same stencil as FilterStencil::make: offsets in (dk, dj, di) ascending order

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <system_error>
 #include <thread>
 
 #include "tg_solver.h"
@@ -103,10 +104,21 @@ static void host_parallel(int64_t n, F&& fn) {
     return;
   }
   std::vector<std::thread> th;
+  th.reserve(size_t(nt));
   const int64_t chunk = (n + nt - 1) / nt;
-  for (int t = 0; t < nt; ++t) {
+  int t = 0;
+  for (; t < nt; ++t) {
     const int64_t lo = t * chunk, hi = std::min(n, lo + chunk);
-    if (lo < hi) th.emplace_back([&fn, lo, hi, t] { fn(lo, hi, t); });
+    if (lo >= hi) continue;
+    try {
+      th.emplace_back([&fn, lo, hi, t] { fn(lo, hi, t); });
+    } catch (const std::system_error&) {
+      break;  // no thread to be had (many jobs building at once): the rest runs here
+    }
+  }
+  for (; t < nt; ++t) {
+    const int64_t lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo < hi) fn(lo, hi, t);
   }
   for (std::thread& x : th) x.join();
 }
