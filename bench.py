@@ -11,14 +11,18 @@ the x = nx end face, spread bilinearly to its four nodes.  Synthetic, seeded.
 A step is one design iteration on a resident job (filter, penalised solve,
 sensitivities, OC update with its bisection), timed with CUDA events on the job's
 stream; `value` is the mixed-precision form (FP32 V-cycle inside FP64 iterative
-refinement), the plain FP64 form is reported beside it.  `e2e` runs the public
-host API (tg_simp_optimize with host buffers: problem upload, the optimisation,
-the design read-back) for K iterations.  Inputs are larger than L2 (the fine
-vectors alone are 100 MB each), so no L2 flush is needed.
+refinement), the plain FP64 form is reported beside it.  `e2e` covers the same
+iteration window through the public job API with host buffers: every step writes
+the design from host memory, runs the iteration and reads the design and the
+physical density back.  Inputs are larger than L2 (the fine vectors alone are
+100 MB each), so no L2 flush is needed.
 
---impl reference times the CPU implementation of the same step on the host
-cores: the oracle's C restatement of the reference (the reference tree itself is
-not present on the GPU host), measured on a bounded sample and scaled.
+--impl reference times the reference's CPU path on the host cores: whole design
+iterations of the same problem by the oracle's C restatement of the reference's
+MG-PCG design iteration (oracle/oracle_mg.c; the reference tree itself is not
+present on the GPU host), iterations 1..--ref-iterations from the uniform start.
+The in-arm `cpu_baseline` runs the same code on the first iterations of the
+timed window (the GPU job's design and displacement where the window starts).
 
 Secondary workloads (--workload; one JSON line each, not the headline):
   batch  -- 64 seeded designs of the batched workload (nx in [32,128], ny, nz in
@@ -81,22 +85,8 @@ def committed_traffic(nx, ny, nz):
 
 
 def cantilever_random_load(nx, ny, nz, seed=0):
-    """Clamped x = 0 face; unit -z load at a seeded point of the x = nx face."""
-    rng = np.random.default_rng(seed)
-    yy, zz = rng.uniform(0.0, ny), rng.uniform(0.0, nz)
-    b0, c0 = min(int(yy), ny - 1), min(int(zz), nz - 1)
-    ty, tz = yy - b0, zz - c0
-
-    def node(a, b, c):
-        return (c * (ny + 1) + b) * (nx + 1) + a
-
-    bcs = [(node(0, b, c), k, 0.0) for c in range(nz + 1) for b in range(ny + 1) for k in range(3)]
-    loads = []
-    for db, wb in ((0, 1.0 - ty), (1, ty)):
-        for dc, wc in ((0, 1.0 - tz), (1, tz)):
-            if wb * wc > 0.0:
-                loads.append((node(nx, b0 + db, c0 + dc), 2, -1.0 * wb * wc))
-    return bcs, loads
+    from topopt_gb300.workloads import cantilever_seeded_load
+    return cantilever_seeded_load(nx, ny, nz, seed)
 
 
 class ClockSampler:
@@ -196,68 +186,52 @@ def sum_over_ranks(pg, v):
 
 
 # ------------------------------------------------------------------ CPU side
-def cpu_sample(nx, ny, nz, applies_per_iter, budget_s=25.0):
-    """Time the oracle's C restatement on a bounded sample of one design
-    iteration: one fine-operator apply, the sensitivity sweep and one OC update
-    (filter + bisection) on the full grid; scale the apply by the number of fine
-    applies one iteration needs (as counted by the FP64 GPU run).  Coarse-level
-    multigrid work is not charged to the CPU (in its favour)."""
+def cpu_iterations(nx, ny, nz, n, x0=None, u0=None):
+    """Whole design iterations of the benchmark problem on the host cores: the
+    oracle's CPU restatement of the reference's MG-PCG design iteration
+    (oracle/oracle_mg.c: filter, modulus, reduced system, Galerkin hierarchy,
+    MG-PCG warm-started from the previous displacement, sensitivities, OC),
+    from design x0 (the uniform start when None) and warm start u0."""
     from oracle.oracle import OracleLib, Problem
     port = OracleLib("port")
     bcs, loads = cantilever_random_load(nx, ny, nz)
-    pb = Problem(nx, ny, nz, 1.0, None, bcs, loads)
-    rng = np.random.default_rng(1)
-    rho = rng.random(pb.nv) * 0.9 + 0.05
-    E = rho ** 3
-    u = rng.standard_normal(pb.ndof)
-    t0 = time.perf_counter()
-    port.apply(pb, u, E)
-    t_apply = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    port.sensitivity(pb, rho, u)
-    t_sens = time.perf_counter() - t0
-    t_oc = 0.0
-    if t_apply + t_sens < budget_s:
-        dc = -rng.random(pb.nv)
-        t0 = time.perf_counter()
-        port.oc_update(pb, rho, dc, 0.3)
-        t_oc = time.perf_counter() - t0
-    t_iter = applies_per_iter * t_apply + t_sens + t_oc
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return dict(value=1.0 / t_iter, unit="design_iters/s", cores=port_threads(),
-                kind="port",
-                sample=(f"oracle C restatement on {nx}x{ny}x{nz}: 1 fine apply "
-                        f"({t_apply:.2f}s) x {applies_per_iter:.0f} applies/iteration + "
-                        f"sensitivities ({t_sens:.2f}s) + 1 OC update ({t_oc:.2f}s); "
-                        f"{threads} host threads available"),
-                t_apply_s=t_apply, t_sens_s=t_sens, t_oc_s=t_oc)
+    o = Problem(nx, ny, nz, 1.0, None, bcs, loads)
+    x = np.full(o.nv, 0.3) if x0 is None else x0
+    r = port.design_iterations_mg(o, x, n, u=u0, cg_tol=1e-8)
+    per = r["seconds"].sum(axis=1)
+    return dict(value=n / float(per.sum()), unit="design_iters/s", cores=port.threads(),
+                kind="port", seconds=r["seconds"], cg=[int(c) for c in r["cg"]],
+                compliance=[float(c) for c in r["compliance"]], per_iter_s=per)
 
 
-def port_threads():
-    from oracle.oracle import OracleLib
-    try:
-        return int(OracleLib("port").threads())
-    except Exception:
-        return 1
+def cpu_phase_note(r):
+    ph = r["seconds"].mean(axis=0)
+    return (f"per iteration {r['per_iter_s'].mean():.1f} s: filter {ph[0]:.2f}, reduced system + "
+            f"hierarchy {ph[1]:.2f}, MG-PCG {ph[2]:.2f} ({'/'.join(str(c) for c in r['cg'])} "
+            f"iterations), sensitivities {ph[3]:.2f}, OC {ph[4]:.2f} s")
 
 
 def run_reference(args, world, rank, pg):
+    """The reference's CPU path on the host cores: whole design iterations
+    1..n of the benchmark problem from the uniform start (the reference's own
+    first iterations), timed end to end per iteration."""
     if rank != 0:
         return
     nx, ny, nz = args.nx, args.ny, args.nz
-    applies = args.ref_applies
-    vals = []
-    for _ in range(max(1, args.steps if args.steps <= 3 else 1)):
-        s = cpu_sample(nx, ny, nz, applies)
-        vals.append(s["value"])
-    v = statistics.median(vals)
+    n = max(1, min(args.steps, args.ref_iterations))
+    r = cpu_iterations(nx, ny, nz, n)
+    v = r["value"]
+    sample = (f"oracle/oracle_mg.c (CPU restatement of the reference's MG-PCG design iteration), "
+              f"{nx}x{ny}x{nz} design iterations 1..{n} from the uniform start, whole "
+              f"iterations timed; " + cpu_phase_note(r))
     line = {"impl": "reference", "metric": "design_iters_per_s", "value": v,
-            "unit": "design_iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "unit": "design_iters/s", "n_gpus": world, "steps": n, "warmup": 0,
             "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": workload_config(args),
-            "cpu_baseline": {"value": v, "unit": "design_iters/s", "cores": s["cores"],
-                             "kind": s["kind"], "sample": s["sample"]},
+            "cpu_baseline": {"value": v, "unit": "design_iters/s", "cores": r["cores"],
+                             "kind": r["kind"], "sample": sample},
+            "cg_iterations": r["cg"], "compliance": r["compliance"],
             "e2e": {"value": v, "unit": "design_iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -298,6 +272,9 @@ def run_ours(args, world, rank, local, pg):
         job = tg.SimpJob(pb, params, opts(prec, args.warmup + args.steps + 1))
         for _ in range(args.warmup):
             job.step()
+        if form == "mixed":  # the state the timed window starts from (CPU baseline input)
+            window_x, _ = job.read()
+            window_u = job.read_displacement()
         barrier(pg)
         launches0 = tg.kernel_launches()
         rows = []
@@ -341,17 +318,28 @@ def run_ours(args, world, rank, local, pg):
                "solve_ms_fp64": r64["cg"].t_solve_ms, "solve_ms_mixed": r32["cg"].t_solve_ms,
                "cg_iters_fp64": r64["cg"].iterations, "cg_iters_mixed_inner": r32["cg"].iterations,
                "refinements_mixed": r32["cg"].refinements}
-    # End to end through the public host API.
+    # End to end through the public host API, the same iteration window as
+    # `value`: a second job takes the same warm-up steps untimed, then every
+    # timed step writes the design from host memory, runs the iteration and
+    # reads the design and physical density back (host buffers both ways).
     K = args.steps
-    o = opts(tg.PREC_MIXED, K)
-    barrier(pg)
-    t0 = time.perf_counter()
+    e2e_wall = None
     if not args.profile:
-        tg.simp_optimize(pb, params, o)
-    e2e_wall = max_over_ranks(pg, time.perf_counter() - t0)
+        job = tg.SimpJob(pb, params, opts(tg.PREC_MIXED, args.warmup + K + 1))
+        for _ in range(args.warmup):
+            job.step()
+        xh, _ = job.read()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(K):
+            job.write_design(xh)
+            job.step()
+            xh, _ = job.read()
+        e2e_wall = max_over_ranks(pg, time.perf_counter() - t0)
+        job.close()
     nv, ndof = pb.nv, pb.ndof
-    h2d = (len(bcs) + len(loads)) * 16 + 64
-    d2h = 2 * nv * 8
+    h2d = nv * 8  # the design, every step
+    d2h = 2 * nv * 8  # the design and the physical density, every step
     hbm, src = peaks()
     m = forms["mixed"]
     op_bytes32 = 2 * ndof * 4 + nv * 4
@@ -363,9 +351,11 @@ def run_ours(args, world, rank, local, pg):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded cantilever)", "config": workload_config(args),
         "clocks": m["clocks"], "gpu_launches": int(m["launches"]),
-        "e2e": {"value": sum_over_ranks(pg, K) / e2e_wall, "unit": "design_iters/s",
-                "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
-                "includes": "problem upload + job setup + K iterations + certification solve + read-back"},
+        "e2e": {"value": sum_over_ranks(pg, K) / e2e_wall if e2e_wall else None,
+                "unit": "design_iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "includes": f"design iterations {args.warmup + 1}..{args.warmup + K} (the "
+                            "window of value) through the job API: host design written, "
+                            "iteration, design and physical density read back, every step"},
         "roofline": {"bound": "hbm", "kernel": "fine operator apply, FP32 (mixed V-cycle)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "bytes_per_launch": op_bytes32,
@@ -382,26 +372,36 @@ def run_ours(args, world, rank, local, pg):
         "forms": forms, "mixed_vs_fp64": acc,
     }
     if rank == 0 and not args.no_cpu:
-        applies = forms.get("fp64", m)["fine_matvecs_fp64"] or 60
-        cb = cpu_sample(nx, ny, nz, applies)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        n = max(1, args.ref_iterations)
+        cb = cpu_iterations(nx, ny, nz, n, window_x, window_u)
+        line["cpu_baseline"] = {
+            "value": cb["value"], "unit": cb["unit"], "cores": cb["cores"], "kind": cb["kind"],
+            "sample": (f"oracle/oracle_mg.c (CPU restatement of the reference's MG-PCG design "
+                       f"iteration), design iterations {args.warmup + 1}..{args.warmup + n} of "
+                       f"the same run (the GPU job's design and displacement at the start of the "
+                       f"timed window), whole iterations timed; " + cpu_phase_note(cb))}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 def run_op_only(args):
-    """Three fine-operator applies at the workload size (for ncu captures)."""
+    """Fine-operator launches on a resident job of the benchmark workload (its
+    kept mask and element factors), for ncu captures: three FP32 or FP64
+    launches after one design iteration."""
     import topopt_gb300 as tg
     from topopt_gb300.build import build
     build()
-    pb = tg.Problem(args.nx, args.ny, args.nz)
-    rng = np.random.default_rng(0)
-    f = rng.random(pb.nv) * 0.999 + 0.001
-    u = rng.standard_normal(pb.ndof)
+    nx, ny, nz = args.nx, args.ny, args.nz
+    bcs, loads = cantilever_random_load(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, bcs, loads)
     prec = tg.PREC_MIXED if args.op_only == "fp32" else tg.PREC_FP64
-    for _ in range(3):
-        y = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f, precision=prec)
-    print(json.dumps({"op_only": args.op_only, "checksum": float(np.abs(y).sum())}))
+    job = tg.SimpJob(pb, tg.SimpParams(), tg.SimpOptions(
+        volume_fraction=0.3, filter_radius=1.5, move=0.2, change_tol=0.0, cg_tolerance=1e-8,
+        max_iterations=2, solve=tg.SolveOptions(precision=prec, mg_levels=args.mg_levels)))
+    job.step()
+    ms = job.time_operator(prec, 3)
+    job.close()
+    print(json.dumps({"op_only": args.op_only, "ms_per_launch": ms}))
 
 
 # ------------------------------------------------------ secondary workloads
@@ -597,9 +597,9 @@ def main():
     ap.add_argument("--ny", type=int, default=WORKLOAD["ny"])
     ap.add_argument("--nz", type=int, default=WORKLOAD["nz"])
     ap.add_argument("--mg-levels", type=int, default=7)
-    # Fine applies per design iteration charged to the CPU arm: the FP64 GPU form's
-    # measured count on this workload (3 per MG-PCG iteration, ~42 iterations).
-    ap.add_argument("--ref-applies", type=float, default=126.0)
+    # Whole CPU design iterations timed by the reference arm and the CPU baseline
+    # (each ~20-40 s at 16 host threads on the 256x128x128 cantilever).
+    ap.add_argument("--ref-iterations", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--op-only", choices=["fp32", "fp64"], default=None,

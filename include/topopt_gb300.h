@@ -668,6 +668,10 @@ int tg_job_set_stage(tg_job* job, int32_t stage);
 /* Copy the current design x and physical density (filter(x), projected at the
  * current stage's beta, pinned for masked jobs) to the host. */
 int tg_job_read(tg_job* job, double* design_out, double* phys_out);
+/* Copy the displacement of the job's last solve (ndof, the full field with the
+ * prescribed values on fixed DOFs; zeros before the first step) to the host:
+ * the warm start the next step's solve begins from (simp.cpp:1788-1797). */
+int tg_job_read_displacement(tg_job* job, double* u_out);
 /* Replace the design with a host field (voxels). */
 int tg_job_write_design(tg_job* job, const double* design);
 /* Bytes of device memory the job holds. */
@@ -702,6 +706,16 @@ int tg_filter_noalloc(int32_t nx, int32_t ny, int32_t nz, const uint8_t* d_tags,
 int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* avg_ms);
 /* Kernels this library has launched in the process so far. */
 int64_t tg_kernel_launches(void);
+/* Schedule of the FP32 fine operator (the mixed form's fine level).  kind 0:
+ * the pencil kernel; kind 1: the column-blocked kernel with tile shape `shape`
+ * (0 <= shape < 4: Y x W element rows per thread x warps per CTA of 4x4, 6x4,
+ * 3x4, 2x8) and `kz` >= 8 element layers per CTA.  The setting overrides the
+ * per-grid table for every later FP32 launch in the process; kind < 0 clears
+ * it.  Results of every schedule agree to FP32 rounding. */
+int tg_set_fp32_schedule(int32_t kind, int32_t shape, int32_t kz);
+/* The FP32 schedule the operator uses on an nx x ny x nz grid now. */
+int tg_fp32_schedule(int32_t nx, int32_t ny, int32_t nz, int32_t* kind, int32_t* shape,
+                     int32_t* kz);
 /* FMA microbenchmark: sustained FP64 and FP32 FMA throughput of the device in
  * TFLOP/s (2 flops per FMA), all SMs, register-resident operands. */
 int tg_device_fma_peaks(double* fp64_tflops, double* fp32_tflops);

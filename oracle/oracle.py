@@ -44,13 +44,13 @@ _bp = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 def build_port(force: bool = False) -> str:
     """Compile the C restatement (gcc, -ffp-contract=off, no -march; OpenMP when
     the compiler has it -- threading never changes a result)."""
-    src = os.path.join(HERE, "topopt_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("topopt_oracle.c", "oracle_mg.c")]
     hdr = os.path.join(HERE, "topopt_oracle.h")
     os.makedirs(os.path.dirname(PORT_SO), exist_ok=True)
-    newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+    newest = max([os.path.getmtime(f) for f in srcs] + [os.path.getmtime(hdr)])
     if force or not os.path.exists(PORT_SO) or newest > os.path.getmtime(PORT_SO):
         base = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-o",
-                PORT_SO + ".tmp", src, "-lm"]
+                PORT_SO + ".tmp"] + srcs + ["-lm"]
         try:
             subprocess.check_call(base[:2] + ["-fopenmp"] + base[2:], stderr=subprocess.DEVNULL)
         except subprocess.CalledProcessError:
@@ -261,6 +261,45 @@ class OracleLib:
                                          E, nu, *pb.bc_args(), tol, max_it, self._ptr(g), u,
                                          C.byref(it), C.byref(res)))
         return u, it.value, res.value
+
+    def mg_solve(self, pb: Problem, factor, nu=0.3, tol=1e-8, max_it=300, max_levels=0,
+                 guess=None):
+        """The MG-PCG restatement (oracle_mg.c): (u, iterations, residual, levels)."""
+        assert self.kind == "port"
+        f = np.ascontiguousarray(factor, dtype=np.float64)
+        g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float64)
+        u = np.zeros(pb.ndof)
+        it, res, lev = C.c_int(0), C.c_double(0), C.c_int(0)
+        fn = self._sig("mg_solve", [C.c_int] * 3 + [C.c_double, C.c_void_p, _dp, C.c_double,
+                                                    C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip,
+                                                    _dp, C.c_double, C.c_int, C.c_int, C.c_void_p,
+                                                    _dp, C.c_void_p, C.c_void_p, C.c_void_p])
+        self._check(fn(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), f, nu, *pb.bc_args(), tol,
+                       max_it, max_levels, self._ptr(g), u, C.byref(it), C.byref(res),
+                       C.byref(lev)))
+        return u, it.value, res.value, lev.value
+
+    def design_iterations_mg(self, pb: Problem, x, niter, u=None, E0=1.0, nu=0.3, penal=3.0,
+                             rho_min=1e-3, volfrac=0.3, radius=1.5, move=0.2, cg_tol=1e-8,
+                             cg_max_it=300):
+        """niter OC design iterations with the MG-PCG restatement from design x.
+        Returns dict(x, u, compliance[], cg[], seconds[niter][5]) where seconds
+        are [filter+modulus, reduced system+hierarchy, MG-PCG, sensitivities, OC]."""
+        assert self.kind == "port"
+        xs = np.array(x, dtype=np.float64, copy=True)
+        warm = u is not None
+        us = np.zeros(pb.ndof) if u is None else np.array(u, dtype=np.float64, copy=True)
+        hc = np.zeros(niter)
+        hcg = np.zeros(niter, np.int32)
+        ht = np.zeros((niter, 5))
+        fn = self._sig("design_iterations_mg",
+                       [C.c_int] * 3 + [C.c_double, C.c_void_p] + [C.c_double] * 4 +
+                       [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp] + [C.c_double] * 4 +
+                       [C.c_int] * 3 + [_dp, _dp, _dp, _ip, _dp])
+        self._check(fn(pb.nx, pb.ny, pb.nz, pb.h, self._ptr(pb.solid), E0, nu, penal, rho_min,
+                       *pb.bc_args(), volfrac, radius, move, cg_tol, cg_max_it, niter, int(warm),
+                       xs, us, hc, hcg, ht))
+        return dict(x=xs, u=us, compliance=hc, cg=hcg, seconds=ht)
 
     def simp_compliance(self, pb: Problem, density, E0=1.0, nu=0.3, penal=3.0, rho_min=1e-3,
                         tol=1e-8, max_it=0):

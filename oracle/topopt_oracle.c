@@ -177,6 +177,11 @@ static int check_factor(int nx, int ny, int nz, const uint8_t* solid, const doub
   return OR_OK;
 }
 
+void or_apply_ke(int nx, int ny, int nz, const uint8_t* solid, const double* factor,
+                 const double* ke, const double* u, double* y) {
+  apply_full(nx, ny, nz, solid, factor, ke, u, y);
+}
+
 int or_apply(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
              double E, double nu, const double* u, double* y) {
   double ke[576];

@@ -49,6 +49,11 @@ int or_hex8_stiffness(double E, double nu, double h, double* ke576);
 int or_apply(int nx, int ny, int nz, double h, const uint8_t* solid,
              const double* factor, double E, double nu, const double* u, double* y);
 
+/* The same apply with a caller-computed unit-modulus Ke (or_hex8_stiffness) and
+ * factors already checked (> 0 on solid voxels). */
+void or_apply_ke(int nx, int ny, int nz, const uint8_t* solid, const double* factor,
+                 const double* ke576, const double* u, double* y);
+
 /* Reduced, void-gated system (matfree.cpp:670-834).  Outputs (all ndof long):
  *   kept[d]   1 if DOF d survives (free and touched by a solid element)
  *   rhs[d]    f - K u_p on kept DOFs, 0 elsewhere
@@ -288,6 +293,30 @@ int or_ladder(int nx, int ny, int nz, double h, const uint8_t* tags, const uint8
 int or_homogenize(int nx, int ny, int nz, double h, double E, double nu, const uint8_t* solid,
                   int cases_mask, double cg_tol, int max_it, double* CH, int* iters_max,
                   int* converged);
+
+/* ---- oracle_mg.c: the geometric-multigrid PCG, a labelled restatement ----
+ * (multigrid.cpp:1211-1313 mf_mgpcg, :1344-1515 build_mf_hierarchy,
+ * :557-697 build_hierarchy, :780-817 v_cycle, :1119-1146 mf_v_cycle): Galerkin
+ * coarse operators as 27-point node stencils, damped Jacobi 0.6 with 1+1
+ * sweeps, a banded Cholesky at the coarsest level (the reference: Eigen
+ * SimplicialLDLT), coarsening until <= 6000 active DOFs (max_levels <= 0) or
+ * exactly max_levels levels.  u = x on kept DOFs, u_p elsewhere. */
+int or_mg_solve(int nx, int ny, int nz, double h, const uint8_t* solid, const double* factor,
+                double nu, int nbc, const int* bc_node, const int* bc_comp, const double* bc_val,
+                int nload, const int* ld_node, const int* ld_comp, const double* ld_val,
+                double tol, int max_it, int max_levels, const double* initial_guess, double* u,
+                int* iters, double* resid, int* levels);
+/* niter design iterations of simp_optimize's OC loop with that solver, from the
+ * design x (advanced in place); u: the displacement (a warm start on entry when
+ * warm != 0).  Per iteration: compliance, MG-PCG iterations and seconds in
+ * [filter + modulus, reduced system + hierarchy, MG-PCG, sensitivities, OC]. */
+int or_design_iterations_mg(int nx, int ny, int nz, double h, const uint8_t* solid, double E0,
+                            double nu, double penal, double rho_min, int nbc, const int* bc_node,
+                            const int* bc_comp, const double* bc_val, int nload,
+                            const int* ld_node, const int* ld_comp, const double* ld_val,
+                            double volfrac, double radius, double move, double cg_tol,
+                            int cg_max_it, int niter, int warm, double* x, double* u,
+                            double* hist_c, int* hist_cg, double* hist_t5);
 
 #ifdef __cplusplus
 }

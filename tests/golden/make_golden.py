@@ -5,7 +5,8 @@ oracle/build_ref.sh from the reference tree) on small seeded problems and saves
 inputs and outputs as golden.npz.  Only runs where the reference tree is
 available; the committed golden.npz is what the tests read everywhere else.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                       # everything
+    python tests/golden/make_golden.py --section cfg0_steps  # one section into the existing file
 """
 from __future__ import annotations
 
@@ -130,6 +131,7 @@ def main():
                cfg0_hist_vf=s0["hist_vf"], cfg0_design=s0["design"],
                cfg0_compliance=np.array(s0["compliance"]),
                cfg0_iterations=np.array(s0["iterations"]))
+    out.update(_cfg0_steps(R))
 
     # Heaviside projection: value and derivative at the fixture's spot values
     # and on a dense grid of rho_tilde, from the reference's own functions.
@@ -277,6 +279,42 @@ def main():
     print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
 
 
+def _cfg0_steps(R):
+    """Per-step inputs of the 60x20x20 configuration: the reference's physical
+    density after 10, 25 and 50 design iterations (its own OC trajectory,
+    filtered by its own filter) and its compliance, displacement and
+    sensitivities on exactly that density, solved to 1e-12."""
+    pb0 = cantilever(60, 20, 20)
+    out = {}
+    for k in (10, 25, 50):
+        sk = R.simp_optimize(pb0, volfrac=0.3, radius=1.5, move=0.2, max_it=k, change_tol=0.0,
+                             cg_tol=1e-10)
+        xp = R.filter(pb0, sk["design"], 1.5)
+        ck = R.simp_compliance(pb0, xp, tol=1e-12)
+        out.update({f"cfg0_it{k}_phys": xp, f"cfg0_it{k}_c": np.array(ck["compliance"]),
+                    f"cfg0_it{k}_u": ck["u"], f"cfg0_it{k}_dc": ck["dc"]})
+    return out
+
+
+def update_section(name):
+    """Recompute one section into the existing golden.npz (every other array is
+    kept as it is)."""
+    if build_reference() is None:
+        raise SystemExit("reference tree not available; nothing generated")
+    R = OracleLib("reference")
+    R.set_threads(int(os.environ.get("GOLDEN_THREADS", "1")))
+    path = os.path.join(HERE, "golden.npz")
+    with np.load(path) as z:
+        out = {k: z[k] for k in z.files}
+    new = {"cfg0_steps": _cfg0_steps}[name](R)
+    for k, v in new.items():
+        if k in out and not np.array_equal(out[k], v, equal_nan=True):
+            raise SystemExit(f"golden array {k} changed on regeneration")
+    out.update(new)
+    np.savez_compressed(path, **out)
+    print("updated", path, sorted(new))
+
+
 def _formats(R, rng):
     import ctypes as C
     import tempfile
@@ -356,4 +394,7 @@ def _active_domain(R, rng):
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 2 and sys.argv[1] == "--section":
+        update_section(sys.argv[2])
+    else:
+        main()

@@ -1,0 +1,72 @@
+"""Schedules of the FP32 fine operator: the pencil kernel and the column-blocked
+kernel in each tile shape and z-chunk length give Ke u to FP32 rounding (within
+2e-6 of the FP64 result, relative to its largest entry) on brick edges, partial
+tiles, voids and the 256x128x128 benchmark grid.  GPU only."""
+import numpy as np
+import pytest
+
+from oracle.oracle import cantilever
+
+pytestmark = pytest.mark.gpu
+
+SCHEDULES = [(0, 0, 32)] + [(1, s, kz) for s in range(4) for kz in (8, 13, 32)]
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.fixture
+def schedule(tg):
+    yield tg.set_fp32_schedule
+    tg.set_fp32_schedule(None)
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 1, 3), (33, 17, 9), (61, 20, 11), (40, 24, 9)])
+def test_fp32_schedules_match_oracle(tg, port, schedule, dims):
+    rng = np.random.default_rng(sum(dims) + 1)
+    nx, ny, nz = dims
+    solid = (rng.random(nx * ny * nz) > 0.1).astype(np.uint8)
+    o = cantilever(nx, ny, nz, solid=solid)
+    pb = tg.Problem(nx, ny, nz, 1.0, solid)
+    u = rng.standard_normal(o.ndof)
+    f = rng.random(o.nv) + 1e-3
+    ref = port.apply(o, u, f)
+    for kind, shape, kz in SCHEDULES:
+        schedule(kind, shape, kz)
+        y = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f, precision=tg.PREC_MIXED)
+        assert rel(y, ref) < 2e-6, (kind, shape, kz)
+
+
+def test_fp32_schedules_at_scale(tg, schedule):
+    """256x128x128: every schedule agrees with the FP64 operator to FP32
+    rounding; the default schedule is the column kernel."""
+    nx, ny, nz = 256, 128, 128
+    assert tg.fp32_schedule(nx, ny, nz)[0] == tg.SCHED_COLUMN
+    pb = tg.Problem(nx, ny, nz)
+    rng = np.random.default_rng(7)
+    f = rng.random(pb.nv) * 0.999 + 0.001
+    u = rng.standard_normal(pb.ndof)
+    y64 = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f)
+    for kind, shape, kz in [(0, 0, 32), (1, 0, 26), (1, 1, 26), (1, 2, 13), (1, 3, 32)]:
+        schedule(kind, shape, kz)
+        y = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f, precision=tg.PREC_MIXED)
+        assert rel(y, y64) < 2e-6, (kind, shape, kz)
+
+
+def test_mixed_solve_same_answer_every_schedule(tg, schedule):
+    """The mixed solve (FP32 operator in the V-cycle, the smoother and the inner
+    Krylov apply) reaches the FP64 solution under every schedule."""
+    from test_gpu_parity import smooth_modulus
+    nx, ny, nz = 48, 24, 24
+    o = cantilever(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                    list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+    E = smooth_modulus(pb)
+    u64, _ = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10)
+    for kind, shape, kz in [(0, 0, 32), (1, 0, 8), (1, 2, 13)]:
+        schedule(kind, shape, kz)
+        um, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
+            precision=tg.PREC_MIXED))
+        assert info.converged and not info.mixed_fallback, (kind, shape, kz, info)
+        assert rel(um, u64) < 1e-8

@@ -32,6 +32,11 @@ from ._capi import (  # noqa: F401
     effective_design_mask,
     fea_build_reduced,
     kernel_launches,
+    set_fp32_schedule,
+    fp32_schedule,
+    SCHED_PENCIL,
+    SCHED_COLUMN,
+    FP32_SHAPES,
     fea_matfree_apply,
     fea_solve_mgcg_matfree,
     hex8_stiffness,

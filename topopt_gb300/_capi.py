@@ -194,12 +194,15 @@ def lib():
         "tg_job_step": ([vp, vp], C.c_int),
         "tg_job_read": ([vp, vp, vp], C.c_int),
         "tg_job_write_design": ([vp, vp], C.c_int),
+        "tg_job_read_displacement": ([vp, vp], C.c_int),
         "tg_job_device_bytes": ([vp], C.c_int64),
         "tg_job_estimate_bytes": ([vp, vp], C.c_int64),
         "tg_job_destroy": ([vp], None),
         "tg_job_time_operator": ([vp, i32, i32, vp], C.c_int),
         "tg_kernel_launches": ([], C.c_int64),
         "tg_device_fma_peaks": ([vp, vp], C.c_int),
+        "tg_set_fp32_schedule": ([i32, i32, i32], C.c_int),
+        "tg_fp32_schedule": ([i32, i32, i32, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -926,6 +929,23 @@ def kernel_launches() -> int:
     return int(lib().tg_kernel_launches())
 
 
+SCHED_PENCIL, SCHED_COLUMN = 0, 1
+FP32_SHAPES = [(4, 4), (6, 4), (3, 4), (2, 8)]  # (element rows per thread, warps per CTA)
+
+
+def set_fp32_schedule(kind=None, shape=0, kz=32):
+    """Force the FP32 operator's schedule for every later launch (kind None
+    clears the override: the per-grid table decides again)."""
+    _check(lib().tg_set_fp32_schedule(-1 if kind is None else int(kind), int(shape), int(kz)))
+
+
+def fp32_schedule(nx, ny, nz):
+    """(kind, shape, kz) the FP32 operator uses on an nx x ny x nz grid now."""
+    k, s, z = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+    _check(lib().tg_fp32_schedule(nx, ny, nz, C.byref(k), C.byref(s), C.byref(z)))
+    return k.value, s.value, z.value
+
+
 def device_fma_peaks():
     """(fp64, fp32) sustained FMA TFLOP/s from the library's microbenchmark."""
     a, b = C.c_double(0.0), C.c_double(0.0)
@@ -1083,6 +1103,12 @@ class SimpJob:
         x, xp = np.zeros(self.pb.nv), np.zeros(self.pb.nv)
         _check(lib().tg_job_read(self._h, _p(x), _p(xp)))
         return x, xp
+
+    def read_displacement(self):
+        """The displacement of the last solve (the next step's warm start)."""
+        u = np.zeros(self.pb.ndof)
+        _check(lib().tg_job_read_displacement(self._h, _p(u)))
+        return u
 
     def write_design(self, x):
         x = _f64(x, self.pb.nv)

@@ -1872,6 +1872,14 @@ int tg_job_read(tg_job* job, double* design_out, double* phys_out) {
   });
 }
 
+int tg_job_read_displacement(tg_job* job, double* u_out) {
+  return guarded([&] {
+    if (!job || !u_out) raise(TG_EINVAL, "job and u_out must be non-null");
+    TG_CUDA(cudaMemcpyAsync(u_out, job->u.p, job->u.bytes(), cudaMemcpyDeviceToHost, job->s));
+    TG_CUDA(cudaStreamSynchronize(job->s));
+  });
+}
+
 int tg_job_write_design(tg_job* job, const double* design) {
   return guarded([&] {
     if (!job || !design) raise(TG_EINVAL, "job and design must be non-null");
@@ -1891,7 +1899,7 @@ int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* option
   // Fine: 9 FP64 DOF vectors + kept/f/up; ~12 voxel arrays.  Hierarchy: the
   // level-1 element matrices (576 doubles per 8 voxels) and stencils (126
   // doubles per node / 8), a geometric series over the coarser levels.
-  double b = ndof * (9 * 8 + 1 + 16) + nv * (12 * 8 + 2);
+  double b = ndof * (9 * 8 + 1 + 16) + ndof / 3.0 + nv * (12 * 8 + 2);
   b += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 126 * 8 * 8.0 / 7.0;
   if (mixed) b += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 126 * 4 * 8.0 / 7.0 + nv * 4;
   if (options && options->projection_stages > 0)  // xtilde and the candidate fields
@@ -1900,7 +1908,7 @@ int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* option
   if (options && options->active_domain_band != 0) {
     // The restricted system: its own reduced problem, solver vectors and
     // hierarchy (at most the full system's), and three byte masks.
-    double r = ndof * (9 * 8 + 1 + 16) + nv * 4;
+    double r = ndof * (9 * 8 + 1 + 16) + ndof / 3.0 + nv * 4;
     r += (nv / 8.0) * 576 * 8 * 8.0 / 7.0 + (ndof / 3.0 / 8.0) * 126 * 8 * 8.0 / 7.0;
     if (mixed) r += ndof * 8 * 4 + (ndof / 3.0 / 8.0) * 126 * 4 * 8.0 / 7.0 + nv * 4;
     b += r;
@@ -1928,6 +1936,32 @@ int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* a
 }
 
 int64_t tg_kernel_launches(void) { return tg::g_launches.load(); }
+
+int tg_set_fp32_schedule(int32_t kind, int32_t shape, int32_t kz) {
+  return guarded([&] {
+    if (kind < 0) {
+      set_fine_schedule_override(nullptr);
+      return;
+    }
+    FineSchedule s;
+    s.kind = kind;
+    s.shape = shape;
+    s.kz = kz;
+    if (!fine_schedule_valid(s)) raise(TG_EINVAL, "tg_set_fp32_schedule: no such schedule");
+    set_fine_schedule_override(&s);
+  });
+}
+
+int tg_fp32_schedule(int32_t nx, int32_t ny, int32_t nz, int32_t* kind, int32_t* shape,
+                     int32_t* kz) {
+  return guarded([&] {
+    if (nx < 1 || ny < 1 || nz < 1) raise(TG_EINVAL, "grid dimensions must be >= 1");
+    const FineSchedule s = fine_schedule_for(Grid::make(nx, ny, nz, 1.0));
+    if (kind) *kind = s.kind;
+    if (shape) *shape = s.shape;
+    if (kz) *kz = s.kz;
+  });
+}
 
 int tg_device_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
   return guarded([&] {

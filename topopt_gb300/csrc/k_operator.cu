@@ -483,15 +483,339 @@ __global__ void __launch_bounds__(32 * PY, MINB) k_fine_op(GridDev g, ModalT<C> 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Column-blocked FP32 operator (the mixed form's fine level).
+//
+// The pencil kernel above spends most of its issue slots on moving node values
+// between lanes and warps and recomputes 37% of its element slots as halo.  This
+// schedule keeps more of the combine in registers:
+//   * lanes run along x: lane l evaluates the element column ex = x0 - 1 + l and
+//     finishes node column ex (lanes 1..30; lane 0 and lane 31 are halo);
+//   * each thread marches a column of Y element rows in y: the y-combine of two
+//     consecutive element rows is a register add inside the thread, and an
+//     element's inputs share the node row with the element below it;
+//   * W warps stack in y; the node row between two warps is finished by the
+//     lower warp with the upper warp's contribution handed over through shared
+//     memory (one __syncthreads per element layer), so a CTA recomputes one
+//     element row of halo in y, not one per warp;
+//   * the CTA marches KZ element layers in z (KZ chosen per grid so the chunks
+//     divide the node layers evenly), completing node layers in registers.
+// Per node the summation order is fixed (y inside the thread, then x across
+// lanes, then the warp hand-over, then z), so the apply is deterministic.
+// Node values of layer ez+2 are loaded while layer ez is evaluated.
+template <int Y, int W>
+struct ColShape {
+  static constexpr int kRows = W * Y - 1;  // node rows a CTA finishes
+  static constexpr int kMinB = 12 / W > 0 ? 12 / W : 1;  // ~12 resident warps per SM
+};
+
+template <int Y, int W, int MODE>
+__global__ void __launch_bounds__(32 * W, (ColShape<Y, W>::kMinB))
+    k_fine_op_col(GridDev g, ModalT<float> mc, int KZ, const float* __restrict__ ef,
+                  const uint8_t* __restrict__ kept, const uint8_t* __restrict__ kn,
+                  const float* __restrict__ x, const float* __restrict__ b,
+                  const float* __restrict__ invdiag, float omega, float* __restrict__ y,
+                  double* __restrict__ dot_part) {
+  __shared__ float xs[2][W][6][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ex = blockIdx.x * 30 - 1 + lane;
+  const int ey0 = blockIdx.y * ColShape<Y, W>::kRows - 1 + w * Y;  // element rows ey0 .. ey0+Y-1
+  const int z0 = blockIdx.z * KZ;
+  const int64_t plane = int64_t(g.nnx) * g.nny, eplane = int64_t(g.nx) * g.ny;
+  const bool vx = ex >= 0 && ex < g.nnx;
+  const bool own_x = lane >= 1 && lane <= 30 && ex < g.nnx;
+  bool rv[Y + 1];
+#pragma unroll
+  for (int i = 0; i <= Y; ++i) rv[i] = vx && ey0 + i >= 0 && ey0 + i < g.nny;
+  bool ev[Y];
+#pragma unroll
+  for (int j = 0; j < Y; ++j) ev[j] = ex >= 0 && ex < g.nx && ey0 + j >= 0 && ey0 + j < g.ny;
+  // Node rows i = 1..Y of the column are this thread's (row Y only below the
+  // top warp); row 0 belongs to the warp below.
+  bool ro[Y + 1];
+#pragma unroll
+  for (int i = 0; i <= Y; ++i) ro[i] = own_x && i >= 1 && (i < Y || w < W - 1) && ey0 + i < g.nny;
+  const int64_t col = int64_t(ey0) * g.nnx + ex;  // node (ex, ey0) in a layer
+  const int64_t ecol = int64_t(ey0) * g.nx + ex;   // element (ex, ey0) in a layer
+
+  auto load_layer = [&](int c, float (&r)[Y + 1][3]) {
+    const bool vc = c >= 0 && c < g.nnz;
+    const float* p = x + 3 * (int64_t(c) * plane + col);
+#pragma unroll
+    for (int i = 0; i <= Y; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) r[i][k] = (vc && rv[i]) ? p[3 * i * g.nnx + k] : 0.0f;
+  };
+  // Element factors of layer c (0 outside the grid).
+  auto load_f = [&](int c, float (&f)[Y]) {
+    const bool vc = c >= 0 && c < g.nz;
+#pragma unroll
+    for (int j = 0; j < Y; ++j)
+      f[j] = (vc && ev[j]) ? ef[int64_t(c) * eplane + ecol + int64_t(j) * g.nx] : 0.0f;
+  };
+  // Kept bits of the owned node rows of layer c (bit k: DOF k kept; all kept
+  // without a mask).
+  auto load_kb = [&](int c, unsigned (&kb)[Y + 1]) {
+    const bool vc = c >= 0 && c < g.nnz;
+#pragma unroll
+    for (int i = 1; i <= Y; ++i)
+      kb[i] = kn == nullptr ? 7u
+                            : ((vc && ro[i]) ? unsigned(kn[int64_t(c) * plane + col + int64_t(i) * g.nnx])
+                                             : 0u);
+  };
+
+  float cur[Y + 1][3], nxt[Y + 1][3], raw[Y + 1][3];
+  load_layer(z0 - 1, cur);
+  load_layer(z0, nxt);
+  float fn[Y];
+  load_f(z0 - 1, fn);
+  unsigned kbn[Y + 1];
+  load_kb(z0 - 1, kbn);
+  float pend[Y + 1][3];
+#pragma unroll
+  for (int i = 0; i <= Y; ++i) pend[i][0] = pend[i][1] = pend[i][2] = 0.0f;
+  float dsum = 0.0f;
+
+  // The right-hand side and inverse diagonal of node row i, layer c (smoothing
+  // and residual modes), requested an element ahead of their use.
+  auto load_bd = [&](int i, int c, float (&bv)[3], float (&dv)[3]) {
+    const bool ok = c >= 0 && c < g.nnz && ro[i];
+    const int64_t d0 = 3 * (int64_t(c) * plane + col + int64_t(i) * g.nnx);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      bv[k] = (MODE != kApply && ok) ? b[d0 + k] : 0.0f;
+      dv[k] = (MODE == kSmooth && ok) ? invdiag[d0 + k] : 0.0f;
+    }
+  };
+  // Writes node row i of layer ez from its finished sum ax.
+  auto emit = [&](int i, int ez, unsigned kb, const float (&ax)[3], const float (&bv)[3],
+                  const float (&dv)[3]) {
+    const int64_t d0 = 3 * (int64_t(ez) * plane + col + int64_t(i) * g.nnx);
+    float nd = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int64_t d = d0 + k;
+      const bool kk = kn != nullptr ? ((kb >> k) & 1u) != 0u : (kept == nullptr || kept[d] != 0);
+      float out;
+      if constexpr (MODE == kApply) {
+        out = kk ? ax[k] : 0.0f;
+        nd = fmaf(cur[i][k], out, nd);
+      } else if constexpr (MODE == kResidual) {
+        out = kk ? bv[k] - ax[k] : 0.0f;
+      } else {
+        out = kk ? cur[i][k] + omega * dv[k] * (bv[k] - ax[k]) : 0.0f;
+      }
+      y[d] = out;
+    }
+    if constexpr (MODE == kApply) dsum += nd;
+  };
+
+#pragma unroll 1
+  for (int s = 0; s <= KZ; ++s) {
+    const int ez = z0 - 1 + s;
+    if (s < KZ) load_layer(ez + 2, raw);
+    float f[Y];
+    unsigned kb[Y + 1];
+#pragma unroll
+    for (int j = 0; j < Y; ++j) f[j] = fn[j];
+#pragma unroll
+    for (int i = 1; i <= Y; ++i) kb[i] = kbn[i];
+    if (s < KZ) {
+      load_f(ez + 1, fn);
+      load_kb(ez + 1, kbn);
+    }
+    const bool out_z = s >= 1 && ez < g.nnz;
+    float bv[3], dv[3];
+    load_bd(1, out_z ? ez : -1, bv, dv);
+    // x + 1 node values of the element's lower row (cur, nxt layers).
+    float c1[3], n1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      c1[k] = shfl_down(cur[0][k], 1);
+      n1[k] = shfl_down(nxt[0][k], 1);
+    }
+    float C[2][2][3];  // the previous element's +y corners [cx][cz][comp]
+#pragma unroll
+    for (int j = 0; j < Y; ++j) {
+      float c1u[3], n1u[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        c1u[k] = shfl_down(cur[j + 1][k], 1);
+        n1u[k] = shfl_down(nxt[j + 1][k], 1);
+      }
+      // corner c = xb | yb << 1 | zb << 2
+      float ux[8] = {cur[j][0], c1[0], cur[j + 1][0], c1u[0], nxt[j][0], n1[0], nxt[j + 1][0], n1u[0]};
+      float uy[8] = {cur[j][1], c1[1], cur[j + 1][1], c1u[1], nxt[j][1], n1[1], nxt[j + 1][1], n1u[1]};
+      float uz[8] = {cur[j][2], c1[2], cur[j + 1][2], c1u[2], nxt[j][2], n1[2], nxt[j + 1][2], n1u[2]};
+      if (f[j] != 0.0f) {
+        modal_apply(mc, f[j], ux, uy, uz);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) ux[c] = uy[c] = uz[c] = 0.0f;
+      }
+      // Node row j: the previous element's +y corners and this element's -y
+      // corners, then the x-combine with the lane below.
+      float T[2][2][3];
+#pragma unroll
+      for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz) {
+          const int c0 = cx | (cz << 2), c1i = cx | 2 | (cz << 2);
+          T[cx][cz][0] = j > 0 ? C[cx][cz][0] + ux[c0] : ux[c0];
+          T[cx][cz][1] = j > 0 ? C[cx][cz][1] + uy[c0] : uy[c0];
+          T[cx][cz][2] = j > 0 ? C[cx][cz][2] + uz[c0] : uz[c0];
+          C[cx][cz][0] = ux[c1i];
+          C[cx][cz][1] = uy[c1i];
+          C[cx][cz][2] = uz[c1i];
+        }
+      float N[2][3];
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) N[cz][k] = T[0][cz][k] + shfl_up(T[1][cz][k], 1);
+      if (j == 0) {
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) xs[s & 1][w][cz * 3 + k][lane] = N[cz][k];
+      } else {
+        float ax[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          ax[k] = pend[j][k] + N[0][k];
+          pend[j][k] = N[1][k];
+        }
+        if (out_z && ro[j]) emit(j, ez, kb[j], ax, bv, dv);
+        load_bd(j + 1, out_z ? ez : -1, bv, dv);
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        c1[k] = c1u[k];
+        n1[k] = n1u[k];
+      }
+    }
+    // Node row Y: this thread's top element's +y corners and the next warp's
+    // bottom element's -y corners (through shared memory).
+    float NY[2][3];
+#pragma unroll
+    for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) NY[cz][k] = C[0][cz][k] + shfl_up(C[1][cz][k], 1);
+    __syncthreads();
+    if (w < W - 1) {
+      float ax[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ax[k] = pend[Y][k] + (NY[0][k] + xs[s & 1][w + 1][k][lane]);
+        pend[Y][k] = NY[1][k] + xs[s & 1][w + 1][3 + k][lane];
+      }
+      if (out_z && ro[Y]) emit(Y, ez, kb[Y], ax, bv, dv);
+    }
+#pragma unroll
+    for (int i = 0; i <= Y; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        cur[i][k] = nxt[i][k];
+        nxt[i][k] = raw[i][k];
+      }
+  }
+  if (MODE == kApply && dot_part != nullptr) {
+    const double sum = block_sum(double(dsum));
+    if (threadIdx.x == 0)
+      dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
+// Tile shapes of the column kernel (Y element rows per thread, W warps per CTA)
+// and the z-chunk target; the shape is picked per grid (fine_op_col_shape).
+struct ColCfg {
+  int shape;  // index into kColShapes
+  int kz;     // element layers per CTA
+};
+struct ColShapeDesc {
+  int Y, W;
+};
+constexpr ColShapeDesc kColShapes[] = {{4, 4}, {6, 4}, {3, 4}, {2, 8}};
+constexpr int kNumColShapes = 4;
+
+static dim3 col_grid(const Grid& g, const ColCfg& c) {
+  const ColShapeDesc d = kColShapes[c.shape];
+  const int rows = d.W * d.Y - 1;
+  return dim3((g.nnx + 29) / 30, (g.nny + rows - 1) / rows, (g.nnz + c.kz - 1) / c.kz);
+}
+
 template <class T>
 static dim3 pencil_grid(const Grid& g) {
   using P = Pencil<T>;
   return dim3((g.nnx + 30) / 31, (g.nny + P::PY - 2) / (P::PY - 1), (g.nnz + P::KZ - 1) / P::KZ);
 }
 
+// Smallest z-chunk the column schedule uses: bounds the partial-sum count.
+constexpr int kColMinKz = 8;
+
 int fine_op_blocks(const Grid& g, bool fp64) {
   const dim3 d = fp64 ? pencil_grid<double>(g) : pencil_grid<float>(g);
-  return int(d.x * d.y * d.z);
+  int n = int(d.x * d.y * d.z);
+  if (!fp64)
+    for (int sh = 0; sh < kNumColShapes; ++sh) {
+      const dim3 c = col_grid(g, ColCfg{sh, kColMinKz});
+      n = std::max(n, int(c.x * c.y * c.z));
+    }
+  return n;
+}
+
+// z-chunk length: chunks of at most `target` element layers that divide the
+// node layers evenly (fewest chunks, then the shortest chunk that covers).
+static int even_kz(int nnz, int target) {
+  const int chunks = std::max(1, (nnz + target - 1) / target);
+  return std::max(kColMinKz, (nnz + chunks - 1) / chunks);
+}
+
+FineSchedule default_fine_schedule(const Grid& g) {
+  FineSchedule s;
+  s.kind = FineSchedule::kColumn;
+  s.shape = 0;
+  s.kz = even_kz(g.nnz, 32);
+  return s;
+}
+
+int fine_schedule_shapes() { return kNumColShapes; }
+
+bool fine_schedule_valid(const FineSchedule& s) {
+  if (s.kind == FineSchedule::kPencil) return true;
+  return s.kind == FineSchedule::kColumn && s.shape >= 0 && s.shape < kNumColShapes &&
+         s.kz >= kColMinKz && s.kz <= 4096;
+}
+
+template <int Y, int W, int MODE>
+static void launch_col(const Grid& g, const ColCfg& cc, const ModalConsts& c, const float* ef,
+                       const uint8_t* kept, const uint8_t* kn, const float* x, const float* b,
+                       const float* invdiag, float omega, float* y, double* dot_part,
+                       cudaStream_t s) {
+  const GridDev gd{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz};
+  k_fine_op_col<Y, W, MODE><<<col_grid(g, cc), 32 * W, 0, s>>>(
+      gd, to_modal<float>(c), cc.kz, ef, kept, kn, x, b, invdiag, omega, y, dot_part);
+  TG_LAUNCH_CHECK();
+}
+
+template <int MODE>
+static void launch_col_shape(const Grid& g, const ColCfg& cc, const ModalConsts& c,
+                             const float* ef, const uint8_t* kept, const uint8_t* kn,
+                             const float* x, const float* b, const float* invdiag, float omega,
+                             float* y, double* dot_part, cudaStream_t s) {
+  switch (cc.shape) {
+    case 0:
+      launch_col<4, 4, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case 1:
+      launch_col<6, 4, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case 2:
+      launch_col<3, 4, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    default:
+      launch_col<2, 8, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+  }
 }
 
 template <class T, int MODE>
@@ -508,8 +832,29 @@ static void launch_mode(const Grid& g, const ModalConsts& c, const T* ef, const 
 template <class T>
 void launch_fine_op(int mode, const Grid& g, const ModalConsts& c, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
-                    T* y, double* dot_part, int* nblocks_out, cudaStream_t s) {
-  if (nblocks_out) *nblocks_out = fine_op_blocks(g, sizeof(T) == 8);
+                    T* y, double* dot_part, int* nblocks_out, cudaStream_t s,
+                    const uint8_t* kn) {
+  if constexpr (std::is_same<T, float>::value) {
+    const FineSchedule fs = fine_schedule_for(g);
+    if (fs.kind == FineSchedule::kColumn) {
+      const ColCfg cc{fs.shape, fs.kz};
+      if (nblocks_out) {
+        const dim3 d = col_grid(g, cc);
+        *nblocks_out = int(d.x * d.y * d.z);
+      }
+      if (mode == kApply)
+        launch_col_shape<kApply>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      else if (mode == kResidual)
+        launch_col_shape<kResidual>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      else
+        launch_col_shape<kSmooth>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      return;
+    }
+  }
+  if (nblocks_out) {
+    const dim3 d = pencil_grid<T>(g);
+    *nblocks_out = int(d.x * d.y * d.z);
+  }
   switch (mode) {
     case kApply:
       launch_mode<T, kApply>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
@@ -538,10 +883,11 @@ void launch_fine_residual_df(const Grid& g, const ModalConsts& c, const double* 
 template void launch_fine_op<double>(int, const Grid&, const ModalConsts&, const double*,
                                      const uint8_t*, const double*, const double*,
                                      const double*, double, double*, double*, int*,
-                                     cudaStream_t);
+                                     cudaStream_t, const uint8_t*);
 template void launch_fine_op<float>(int, const Grid&, const ModalConsts&, const float*,
                                     const uint8_t*, const float*, const float*, const float*,
-                                    float, float*, double*, int*, cudaStream_t);
+                                    float, float*, double*, int*, cudaStream_t,
+                                    const uint8_t*);
 
 // Periodic batched apply: nsys systems on the nx*ny*nz torus; system bi uses
 // x/b/y at bi*ndof and the factors / kept mask / inverse diagonal of cell

@@ -226,19 +226,30 @@ void FineProblem::build(const tg_grid& grid, double poisson, const tg_dirichlet_
               "under-constrained system (load applied to a void DOF with no stiffness \xe2\x80\x94 "
               "no equilibrium possible)");
   }
+  // The kept mask once more as 3 bits per node (bit k: DOF 3n+k kept) for the
+  // FP32 column operator, which reads one byte per node instead of three.
+  kept_node_h.resize(size_t(g.nnodes));
+  host_parallel(g.nnodes, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t n = lo; n < hi; ++n)
+      kept_node_h[size_t(n)] = uint8_t(kept_h[size_t(3 * n)] | kept_h[size_t(3 * n + 1)] << 1 |
+                                       kept_h[size_t(3 * n + 2)] << 2);
+  });
   elem.alloc(size_t(g.nv));
   kept.alloc(size_t(g.ndof));
+  kept_node.alloc(size_t(g.nnodes));
   f.alloc(size_t(g.ndof));
   up.alloc(size_t(g.ndof));
   TG_CUDA(cudaMemcpyAsync(elem.p, elem_h.data(), elem.bytes(), cudaMemcpyHostToDevice, s));
   TG_CUDA(cudaMemcpyAsync(kept.p, kept_h.data(), kept.bytes(), cudaMemcpyHostToDevice, s));
+  TG_CUDA(cudaMemcpyAsync(kept_node.p, kept_node_h.data(), kept_node.bytes(),
+                          cudaMemcpyHostToDevice, s));
   TG_CUDA(cudaMemcpyAsync(f.p, f_h.data(), f.bytes(), cudaMemcpyHostToDevice, s));
   TG_CUDA(cudaMemcpyAsync(up.p, up_h.data(), up.bytes(), cudaMemcpyHostToDevice, s));
   TG_CUDA(cudaStreamSynchronize(s));
 }
 
 size_t FineProblem::device_bytes() const {
-  return elem.bytes() + kept.bytes() + f.bytes() + up.bytes();
+  return elem.bytes() + kept.bytes() + kept_node.bytes() + f.bytes() + up.bytes();
 }
 
 // ------------------------------------------------------------------ levels
@@ -535,7 +546,7 @@ double Solver::time_operator(int form, int reps) {
   for (int i = 0; i < reps; ++i) {
     if (fp32)
       launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
-                            apf_.p, nullptr, nullptr, s_);
+                            apf_.p, nullptr, nullptr, s_, fp_.kept_node.p);
     else if (form == 2)  // the double-float residual kernel
       launch_fine_residual_df(g, fp_.mc, E_, fp_.kept.p, p_.p, rhs_.p, ap_.p, s_);
     else
@@ -736,13 +747,13 @@ float* Solver::vcycle<float>(const float* b) {
   const float w = float(omega_);
   auto smooth = [&] {
     launch_fine_op<float>(kSmooth, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
-                          nullptr, s_);
+                          nullptr, s_, fp_.kept_node.p);
     std::swap(x, r);
   };
   mg_jacobi_first<float>(b, invdiagf_.p, w, g.ndof, x, s_);
   for (int k = 1; k < sweeps_; ++k) smooth();
   launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
-                        nullptr, s_);
+                        nullptr, s_, fp_.kept_node.p);
   mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_);
   vcycle_level<float>(1);
   mg_prolong_add<float>(fd, N.d, N.X<float>(), fp_.kept.p, x, s_);
@@ -864,7 +875,7 @@ bool Solver::build_inner_graph() {
                               s_));
       int nb = 0;
       launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
-                            apf_.p, part_.p, &nb, s_);
+                            apf_.p, part_.p, &nb, s_, fp_.kept_node.p);
       launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
       launch_cg_update_xr<float>(xf_.p, rf_.p, pf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n,
                                  part_.p, s_);
@@ -907,7 +918,7 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
   *iters = 0;
   for (int k = 1; k <= max_it; ++k) {
     launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
-                          apf_.p, part_.p, &nb, s_);
+                          apf_.p, part_.p, &nb, s_, fp_.kept_node.p);
     ++lowp_matvecs_;
     launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
     launch_cg_update_xr<float>(xf_.p, rf_.p, pf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);

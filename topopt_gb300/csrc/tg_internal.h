@@ -157,11 +157,30 @@ void launch_fine_residual_df(const Grid& g, const ModalConsts& c, const double* 
 //   kApply:    y = M A x                 (M = kept mask; dot = sum x.y if dot_part)
 //   kResidual: y = M (b - A x)
 //   kSmooth:   y = x + omega*invdiag*(b - A x)   (invdiag is 0 off the kept set)
+//   kept_node (optional): the kept mask as 3 bits per node, read by the FP32
+//   column schedule instead of kept (one byte per node instead of three).
 template <class T>
 void launch_fine_op(int mode, const Grid& g, const ModalConsts& mc, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
-                    T* y, double* dot_part, int* nblocks_out, cudaStream_t s);
-int fine_op_blocks(const Grid& g, bool fp64);
+                    T* y, double* dot_part, int* nblocks_out, cudaStream_t s,
+                    const uint8_t* kept_node = nullptr);
+int fine_op_blocks(const Grid& g, bool fp64);  // upper bound of the partials any schedule writes
+
+// How the FP32 fine operator is scheduled on a grid (k_operator.cu): the
+// pencil kernel (the FP64 form's schedule) or the column-blocked kernel with
+// one of fine_schedule_shapes() tile shapes and kz element layers per CTA.
+struct FineSchedule {
+  enum { kPencil = 0, kColumn = 1 };
+  int kind = kColumn, shape = 0, kz = 32;
+};
+FineSchedule default_fine_schedule(const Grid& g);
+int fine_schedule_shapes();
+bool fine_schedule_valid(const FineSchedule& s);
+// The schedule the FP32 operator uses on g: a process-wide override when one is
+// set, else the table entry for g's dimensions (tune.cu), else the default.
+FineSchedule fine_schedule_for(const Grid& g);
+void set_fine_schedule_override(const FineSchedule* s);  // null clears
+void set_fine_schedule(const Grid& g, const FineSchedule& s);
 // Batched apply on the periodic nx*ny*nz torus (nodes = elements per axis); see
 // k_operator.cu.
 template <class T>

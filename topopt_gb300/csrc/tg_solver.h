@@ -23,12 +23,13 @@ struct FineProblem {
   std::vector<double> ke;          // unit-modulus Ke, reference order
   std::vector<uint8_t> elem_h;     // element exists (solid and active) [nv]
   std::vector<uint8_t> kept_h;     // [ndof]
+  std::vector<uint8_t> kept_node_h;  // [nnodes] kept bits per node (bit k: DOF 3n+k)
   std::vector<double> f_h;         // load vector [ndof]
   std::vector<double> up_h;        // prescribed field [ndof]
   std::vector<uint8_t> fixed_h;    // Dirichlet mask [ndof]
   bool nonzero_bc = false;
   int64_t ng = 0, n_free = 0;
-  DBuf<uint8_t> elem, kept;
+  DBuf<uint8_t> elem, kept, kept_node;
   DBuf<double> f, up;
 
   // Throws Error(TG_EINVAL) on bad indices, Error(TG_ESINGULAR) on a void-only

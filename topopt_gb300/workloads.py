@@ -94,3 +94,25 @@ def stream(seed: int, rate: float, duration: float, precision: int = 1, iteratio
         sizes = stream_sizes(rng)
         pb, prm, opt = design(int(rng.integers(1 << 31)), precision, iterations, sizes)
         out.append((t, pb, prm, opt))
+
+
+def cantilever_seeded_load(nx, ny, nz, seed=0):
+    """The benchmark cantilever's boundary conditions: the x = 0 face clamped,
+    a unit -z load at a seeded uniform point (numpy default_rng(seed)) of the
+    x = nx end face, spread bilinearly to the four surrounding nodes.  Returns
+    (bcs, loads) as (node, component, value) triples."""
+    rng = np.random.default_rng(seed)
+    yy, zz = rng.uniform(0.0, ny), rng.uniform(0.0, nz)
+    b0, c0 = min(int(yy), ny - 1), min(int(zz), nz - 1)
+    ty, tz = yy - b0, zz - c0
+
+    def node(a, b, c):
+        return (c * (ny + 1) + b) * (nx + 1) + a
+
+    bcs = [(node(0, b, c), k, 0.0) for c in range(nz + 1) for b in range(ny + 1) for k in range(3)]
+    loads = []
+    for db, wb in ((0, 1.0 - ty), (1, ty)):
+        for dc, wc in ((0, 1.0 - tz), (1, tz)):
+            if wb * wc > 0.0:
+                loads.append((node(nx, b0 + db, c0 + dc), 2, -1.0 * wb * wc))
+    return bcs, loads
