@@ -79,6 +79,9 @@ typedef enum { TG_PREC_FP64 = 0, TG_PREC_MIXED = 1 } tg_precision;
 /* tg_matfree_apply only: the FP64 operator evaluated in double-float arithmetic
  * (the mixed form's refinement residual kernel). */
 enum { TG_APPLY_DF = 2 };
+/* tg_job_time_operator only: the level-1 operator of the mixed form's V-cycle,
+ * residual mode -- the assembled FP32 stencil or the tensor-core operator. */
+enum { TG_APPLY_L1_STENCIL = 3, TG_APPLY_L1_TC = 4 };
 
 /* Solver knobs.  Zero-initialised means: MG-PCG, FP64, the deepest hierarchy the
  * grid allows, the reference's iteration budget of 300 MG cycles before the
@@ -701,15 +704,27 @@ int tg_filter_noalloc(int32_t nx, int32_t ny, int32_t nz, const uint8_t* d_tags,
 /* ---- measurement (no reference counterpart) ---- */
 /* Average device time of one fine-operator launch (y = A x on the job's current
  * element factors), precision TG_PREC_FP64, TG_PREC_MIXED (FP32) or TG_APPLY_DF
- * (the double-float residual kernel), over `reps`
- * back-to-back launches timed with CUDA events on the job's stream. */
+ * (the double-float residual kernel), or of one level-1 operator launch of a
+ * mixed job (TG_APPLY_L1_STENCIL, TG_APPLY_L1_TC), over `reps` back-to-back
+ * launches timed with CUDA events on the job's stream. */
 int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* avg_ms);
+/* The level-1 operator of a mixed job's V-cycle on its current design, applied
+ * to a seeded vector by the assembled FP32 stencil and by the tensor-core
+ * operator: max |difference| / max |stencil result|. */
+int tg_job_check_level1(tg_job* job, double* rel_diff);
 /* Kernels this library has launched in the process so far. */
 int64_t tg_kernel_launches(void);
+/* Level 1 of the mixed form's V-cycle: on (default) the Galerkin operator is
+ * applied on the tensor cores from the fine moduli (tcgen05, TF32 splits to
+ * FP32 accuracy); off, as the assembled FP32 node stencil.  Applies to solvers
+ * created afterwards. */
+int tg_set_level1_tc(int32_t on);
 /* Schedule of the FP32 fine operator (the mixed form's fine level).  kind 0:
  * the pencil kernel; kind 1: the column-blocked kernel with tile shape `shape`
- * (0 <= shape < 4: Y x W element rows per thread x warps per CTA of 4x4, 6x4,
- * 3x4, 2x8) and `kz` >= 8 element layers per CTA.  The setting overrides the
+ * (0 <= shape < 8: Y x W element rows per thread x warps per CTA of 4x4, 6x4,
+ * 3x4, 2x8 for shapes 0-3, the same tiles with the x and y components in
+ * paired FP32 instructions for shapes 4-7) and `kz` >= 8 element layers per
+ * CTA.  The setting overrides the
  * per-grid table for every later FP32 launch in the process; kind < 0 clears
  * it.  Results of every schedule agree to FP32 rounding. */
 int tg_set_fp32_schedule(int32_t kind, int32_t shape, int32_t kz);

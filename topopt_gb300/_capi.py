@@ -202,6 +202,8 @@ def lib():
         "tg_kernel_launches": ([], C.c_int64),
         "tg_device_fma_peaks": ([vp, vp], C.c_int),
         "tg_set_fp32_schedule": ([i32, i32, i32], C.c_int),
+        "tg_set_level1_tc": ([i32], C.c_int),
+        "tg_job_check_level1": ([vp, vp], C.c_int),
         "tg_fp32_schedule": ([i32, i32, i32, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -930,7 +932,18 @@ def kernel_launches() -> int:
 
 
 SCHED_PENCIL, SCHED_COLUMN = 0, 1
-FP32_SHAPES = [(4, 4), (6, 4), (3, 4), (2, 8)]  # (element rows per thread, warps per CTA)
+# (element rows per thread, warps per CTA, x/y in paired FP32 instructions)
+FP32_SHAPES = [(4, 4, False), (6, 4, False), (3, 4, False), (2, 8, False),
+               (4, 4, True), (6, 4, True), (3, 4, True), (2, 8, True)]
+
+
+APPLY_L1_STENCIL, APPLY_L1_TC = 3, 4
+
+
+def set_level1_tc(on: bool):
+    """Level 1 of the mixed V-cycle on the tensor cores (True, default) or as the
+    assembled FP32 stencil (False), for solvers created afterwards."""
+    _check(lib().tg_set_level1_tc(int(bool(on))))
 
 
 def set_fp32_schedule(kind=None, shape=0, kz=32):
@@ -1103,6 +1116,13 @@ class SimpJob:
         x, xp = np.zeros(self.pb.nv), np.zeros(self.pb.nv)
         _check(lib().tg_job_read(self._h, _p(x), _p(xp)))
         return x, xp
+
+    def check_level1(self):
+        """Level-1 operator, tensor cores against the assembled FP32 stencil on a
+        seeded vector: max |difference| / max |stencil result|."""
+        d = C.c_double(0.0)
+        _check(lib().tg_job_check_level1(self._h, C.byref(d)))
+        return d.value
 
     def read_displacement(self):
         """The displacement of the last solve (the next step's warm start)."""

@@ -19,7 +19,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtopopt_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["k_operator.cu", "k_vector.cu", "k_simp.cu", "k_multigrid.cu", "solver.cu", "api.cu",
-           "formats.cu", "noalloc.cu", "homog.cu", "server.cu", "k_active.cu", "tune.cu"]
+           "formats.cu", "noalloc.cu", "homog.cu", "server.cu", "k_active.cu", "tune.cu",
+           "k_coarse_tc.cu"]
 
 
 def nvcc() -> str:

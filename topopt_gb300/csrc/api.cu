@@ -1928,14 +1928,33 @@ int tg_job_time_operator(tg_job* job, int32_t precision, int32_t reps, double* a
     launch_modulus(job->xphys.p, job->fp.elem.p, g.nv, p.youngs_modulus, p.penalty,
                    p.density_min, p.material_law, p.e_min, job->E.p, job->s);
     job->solver->set_modulus(job->E.p);
-    *avg_ms = job->solver->time_operator(precision == TG_PREC_MIXED ? 1
-                                         : precision == TG_APPLY_DF   ? 2
-                                                                      : 0,
+    *avg_ms = job->solver->time_operator(precision == TG_PREC_MIXED       ? 1
+                                         : precision == TG_APPLY_DF         ? 2
+                                         : precision == TG_APPLY_L1_STENCIL ? 3
+                                         : precision == TG_APPLY_L1_TC      ? 4
+                                                                            : 0,
                                          reps);
   });
 }
 
+int tg_job_check_level1(tg_job* job, double* rel_diff) {
+  return guarded([&] {
+    if (!job || !rel_diff) raise(TG_EINVAL, "job and rel_diff required");
+    AllocScope scope(job->s);
+    if (!job->xphys_valid) job_filter_x(job);
+    const tg_simp_params& p = job->params;
+    launch_modulus(job->xphys.p, job->fp.elem.p, job->fp.g.nv, p.youngs_modulus, p.penalty,
+                   p.density_min, p.material_law, p.e_min, job->E.p, job->s);
+    job->solver->set_modulus(job->E.p);
+    *rel_diff = job->solver->check_level1();
+  });
+}
+
 int64_t tg_kernel_launches(void) { return tg::g_launches.load(); }
+
+int tg_set_level1_tc(int32_t on) {
+  return guarded([&] { set_level1_tc(on != 0); });
+}
 
 int tg_set_fp32_schedule(int32_t kind, int32_t shape, int32_t kz) {
   return guarded([&] {

@@ -206,6 +206,102 @@ __device__ __forceinline__ void modal_apply(const ModalT<T>& mc, T f, T (&ux)[8]
   }
 }
 
+// ---- the same element operator with the x and y components packed ----
+// Blackwell's paired FP32 instructions (FADD2/FMUL2/FFMA2) operate on a float2
+// as one instruction.  The Walsh transforms treat x and y identically, so they
+// run on (x, y) pairs; the isotropic "stress" block mixes components and stays
+// scalar.  Same operations per component as modal_apply, same rounding.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);  // a - b, one rounding
+}
+__device__ __forceinline__ void walsh_fwd2(float2 (&v)[8]) {
+#pragma unroll
+  for (int b = 1; b < 8; b <<= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (i & b) continue;
+      const float2 lo = v[i], hi = v[i | b];
+      v[i] = add2(hi, lo);
+      v[i | b] = sub2(hi, lo);
+    }
+  }
+}
+__device__ __forceinline__ void walsh_inv2(float2 (&w)[8]) {
+#pragma unroll
+  for (int b = 1; b < 8; b <<= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (i & b) continue;
+      const float2 lo = w[i], hi = w[i | b];
+      w[i] = sub2(lo, hi);
+      w[i | b] = add2(lo, hi);
+    }
+  }
+}
+__device__ __forceinline__ void modal_apply_xy(const ModalT<float>& mc, float f, float2 (&uxy)[8],
+                                               float (&uz)[8]) {
+  walsh_fwd2(uxy);
+  walsh_fwd(uz);
+  const float L0 = mc.L0 * f, L1 = mc.L1 * f, M0 = mc.M0 * f, M1 = mc.M1 * f;
+  const float M02 = mc.M02 * f, M12 = mc.M12 * f, LM2 = mc.LM2 * f;
+  float2 g[8];
+  float gz[8];
+  {
+    const float Ltr = L0 * (uxy[1].x + uxy[2].y + uz[4]);
+    g[1].x = mad(M02, uxy[1].x, Ltr);
+    g[2].y = mad(M02, uxy[2].y, Ltr);
+    gz[4] = mad(M02, uz[4], Ltr);
+    const float txy = M0 * (uxy[1].y + uxy[2].x);
+    const float txz = M0 * (uz[1] + uxy[4].x);
+    const float tyz = M0 * (uz[2] + uxy[4].y);
+    g[1].y = txy; gz[1] = txz;
+    g[2].x = txy; gz[2] = tyz;
+    g[4].x = txz; g[4].y = tyz;
+  }
+  {
+    const float Ltr = L1 * (uxy[3].y + uz[5]);
+    const float t = M1 * (uz[3] + uxy[5].y);
+    g[3].x = M1 * uxy[3].x;
+    g[3].y = mad(M12, uxy[3].y, Ltr);
+    gz[3] = t;
+    g[5].x = M1 * uxy[5].x;
+    g[5].y = t;
+    gz[5] = mad(M12, uz[5], Ltr);
+  }
+  {
+    const float Ltr = L1 * (uxy[3].x + uz[6]);
+    const float t = M1 * (uz[3] + uxy[6].x);
+    g[3].x = g[3].x + mad(M12, uxy[3].x, Ltr);
+    g[3].y = mad(M1, uxy[3].y, g[3].y);
+    gz[3] = gz[3] + t;
+    g[6].x = t;
+    g[6].y = M1 * uxy[6].y;
+    gz[6] = mad(M12, uz[6], Ltr);
+  }
+  {
+    const float Ltr = L1 * (uxy[5].x + uxy[6].y);
+    const float t = M1 * (uxy[5].y + uxy[6].x);
+    g[5].x = g[5].x + mad(M12, uxy[5].x, Ltr);
+    g[5].y = g[5].y + t;
+    gz[5] = mad(M1, uz[5], gz[5]);
+    g[6].x = g[6].x + t;
+    g[6].y = g[6].y + mad(M12, uxy[6].y, Ltr);
+    gz[6] = mad(M1, uz[6], gz[6]);
+  }
+  g[7] = __fmul2_rn(make_float2(LM2, LM2), uxy[7]);
+  gz[7] = LM2 * uz[7];
+  g[0] = make_float2(0.0f, 0.0f);
+  gz[0] = 0.0f;
+  walsh_inv2(g);
+  walsh_inv(gz);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uxy[i] = g[i];
+    uz[i] = gz[i];
+  }
+}
+
 struct GridDev {
   int nx, ny, nz, nnx, nny, nnz;
 };
@@ -509,7 +605,7 @@ struct ColShape {
   static constexpr int kMinB = 12 / W > 0 ? 12 / W : 1;  // ~12 resident warps per SM
 };
 
-template <int Y, int W, int MODE>
+template <int Y, int W, int MODE, bool PK>
 __global__ void __launch_bounds__(32 * W, (ColShape<Y, W>::kMinB))
     k_fine_op_col(GridDev g, ModalT<float> mc, int KZ, const float* __restrict__ ef,
                   const uint8_t* __restrict__ kept, const uint8_t* __restrict__ kn,
@@ -648,7 +744,19 @@ __global__ void __launch_bounds__(32 * W, (ColShape<Y, W>::kMinB))
       float uy[8] = {cur[j][1], c1[1], cur[j + 1][1], c1u[1], nxt[j][1], n1[1], nxt[j + 1][1], n1u[1]};
       float uz[8] = {cur[j][2], c1[2], cur[j + 1][2], c1u[2], nxt[j][2], n1[2], nxt[j + 1][2], n1u[2]};
       if (f[j] != 0.0f) {
-        modal_apply(mc, f[j], ux, uy, uz);
+        if constexpr (PK) {
+          float2 uxy[8];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) uxy[c] = make_float2(ux[c], uy[c]);
+          modal_apply_xy(mc, f[j], uxy, uz);
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            ux[c] = uxy[c].x;
+            uy[c] = uxy[c].y;
+          }
+        } else {
+          modal_apply(mc, f[j], ux, uy, uz);
+        }
       } else {
 #pragma unroll
         for (int c = 0; c < 8; ++c) ux[c] = uy[c] = uz[c] = 0.0f;
@@ -736,10 +844,10 @@ struct ColShapeDesc {
   int Y, W;
 };
 constexpr ColShapeDesc kColShapes[] = {{4, 4}, {6, 4}, {3, 4}, {2, 8}};
-constexpr int kNumColShapes = 4;
+constexpr int kNumColShapes = 8;  // shapes 4..7: the same tiles with the packed (x, y) arithmetic
 
 static dim3 col_grid(const Grid& g, const ColCfg& c) {
-  const ColShapeDesc d = kColShapes[c.shape];
+  const ColShapeDesc d = kColShapes[c.shape % 4];
   const int rows = d.W * d.Y - 1;
   return dim3((g.nnx + 29) / 30, (g.nny + rows - 1) / rows, (g.nnz + c.kz - 1) / c.kz);
 }
@@ -787,13 +895,13 @@ bool fine_schedule_valid(const FineSchedule& s) {
          s.kz >= kColMinKz && s.kz <= 4096;
 }
 
-template <int Y, int W, int MODE>
+template <int Y, int W, int MODE, bool PK>
 static void launch_col(const Grid& g, const ColCfg& cc, const ModalConsts& c, const float* ef,
                        const uint8_t* kept, const uint8_t* kn, const float* x, const float* b,
                        const float* invdiag, float omega, float* y, double* dot_part,
                        cudaStream_t s) {
   const GridDev gd{g.nx, g.ny, g.nz, g.nnx, g.nny, g.nnz};
-  k_fine_op_col<Y, W, MODE><<<col_grid(g, cc), 32 * W, 0, s>>>(
+  k_fine_op_col<Y, W, MODE, PK><<<col_grid(g, cc), 32 * W, 0, s>>>(
       gd, to_modal<float>(c), cc.kz, ef, kept, kn, x, b, invdiag, omega, y, dot_part);
   TG_LAUNCH_CHECK();
 }
@@ -805,16 +913,28 @@ static void launch_col_shape(const Grid& g, const ColCfg& cc, const ModalConsts&
                              float* y, double* dot_part, cudaStream_t s) {
   switch (cc.shape) {
     case 0:
-      launch_col<4, 4, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      launch_col<4, 4, MODE, false>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
       break;
     case 1:
-      launch_col<6, 4, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      launch_col<6, 4, MODE, false>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
       break;
     case 2:
-      launch_col<3, 4, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      launch_col<3, 4, MODE, false>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case 3:
+      launch_col<2, 8, MODE, false>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case 4:
+      launch_col<4, 4, MODE, true>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case 5:
+      launch_col<6, 4, MODE, true>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case 6:
+      launch_col<3, 4, MODE, true>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
       break;
     default:
-      launch_col<2, 8, MODE>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
+      launch_col<2, 8, MODE, true>(g, cc, c, ef, kept, kn, x, b, invdiag, omega, y, dot_part, s);
   }
 }
 

@@ -511,8 +511,52 @@ void Solver::build_structure() {
   Gf_.alloc(8 * 576);
   TG_CUDA(cudaMemcpyAsync(kebf_.p, kbf.data(), kebf_.bytes(), cudaMemcpyHostToDevice, s_));
   TG_CUDA(cudaMemcpyAsync(Gf_.p, Gf.data(), Gf_.bytes(), cudaMemcpyHostToDevice, s_));
+  l1_tc_ = mixed_ && level1_tc_enabled();
+  if (l1_tc_) {
+    // Coarse elements of level 1 off the sum_c E_c G_c fast path.
+    const Level& L1 = *levels_[0];
+    const MgDims& d = L1.d;
+    std::vector<uint8_t> spec(size_t(L1.nel), 0);
+    host_parallel(L1.nel, [&](int64_t lo, int64_t hi, int) {
+      for (int64_t ce = lo; ce < hi; ++ce) {
+        const int I = int(ce % d.ex), J = int((ce / d.ex) % d.ey), K = int(ce / (int64_t(d.ex) * d.ey));
+        bool sp = d.align && ((2 * I + 1 == g.nx) || (2 * J + 1 == g.ny) || (2 * K + 1 == g.nz));
+        for (int c = 0; c < 8 && !sp; ++c) {
+          const int64_t cn = (int64_t(K + (c >> 2)) * d.nny + (J + ((c >> 1) & 1))) * d.nnx +
+                             (I + (c & 1));
+          for (int k = 0; k < 3; ++k)
+            if (!L1.act_h[size_t(3 * cn + k)]) sp = true;
+        }
+        for (int ch = 0; ch < 8 && !sp; ++ch) {
+          const int fi = 2 * I + (ch & 1), fj = 2 * J + ((ch >> 1) & 1), fk = 2 * K + (ch >> 2);
+          if (fi >= g.nx || fj >= g.ny || fk >= g.nz) continue;
+          if (!fp_.elem_h[size_t((int64_t(fk) * g.ny + fj) * g.nx + fi)]) continue;
+          for (int c = 0; c < 8 && !sp; ++c) {
+            const int64_t fn = (int64_t(fk + (c >> 2)) * g.nny + (fj + ((c >> 1) & 1))) * g.nnx +
+                               (fi + (c & 1));
+            for (int k = 0; k < 3; ++k)
+              if (!fp_.kept_h[size_t(3 * fn + k)]) sp = true;
+          }
+        }
+        spec[size_t(ce)] = uint8_t(sp);
+      }
+    });
+    spec1_.alloc(spec.size());
+    TG_CUDA(cudaMemcpyAsync(spec1_.p, spec.data(), spec1_.bytes(), cudaMemcpyHostToDevice, s_));
+    tc_err_.alloc(1);
+    TG_CUDA(cudaMemsetAsync(tc_err_.p, 0, sizeof(int), s_));
+  }
   TG_CUDA(cudaStreamSynchronize(s_));
   have_mg_ = true;
+}
+
+// Level 1 of the FP32 V-cycle on the tensor cores (mode kResidual or kSmooth):
+// L.R = b - A1 x or the smoothed iterate, as the stencil apply would write it.
+void Solver::level1_op(int mode, Level& L, float omega) {
+  const Grid& g = fp_.g;
+  mg_level1_tc(mode, dims_of(g.nx, g.ny, g.nz), L.d, Ef_.p, L.act.p, spec1_.p, L.Ke<float>(),
+               Gf_.p, L.X<float>(), L.B<float>(), L.Dinv<float>(), omega, L.R<float>(),
+               tc_err_.p, s_);
 }
 
 double Solver::read_scalar(int idx) {
@@ -533,10 +577,70 @@ void Solver::apply_unmasked(const double* E, const double* x, double* y) {
                          nullptr, s_);
 }
 
+double Solver::check_level1() {
+  if (!mixed_ || !l1_tc_ || !have_mg_ || !numeric_ok_)
+    raise(TG_EINVAL, "check_level1: needs a mixed job with the level-1 tensor-core path");
+  Level& L = *levels_[0];
+  const size_t n = size_t(L.ndof);
+  std::vector<float> xh(n), a(n), bq(n);
+  uint64_t h = 0x9E3779B97F4A7C15ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= h << 13;
+    h ^= h >> 7;
+    h ^= h << 17;
+    xh[i] = L.act_h[i] ? float(double(h >> 11) * (1.0 / 9007199254740992.0) - 0.5) : 0.0f;
+  }
+  TG_CUDA(cudaMemcpyAsync(L.X<float>(), xh.data(), n * sizeof(float), cudaMemcpyHostToDevice, s_));
+  mg_stencil_op<float>(kApply, L.d, L.Am<float>(), L.act.p, L.X<float>(), L.B<float>(),
+                       L.Dinv<float>(), 0.0f, L.R<float>(), s_);
+  TG_CUDA(cudaMemcpyAsync(a.data(), L.R<float>(), n * sizeof(float), cudaMemcpyDeviceToHost, s_));
+  TG_CUDA(cudaStreamSynchronize(s_));
+  level1_op(kApply, L, 0.0f);
+  TG_CUDA(cudaMemcpyAsync(bq.data(), L.R<float>(), n * sizeof(float), cudaMemcpyDeviceToHost, s_));
+  int tc_err = 0;
+  TG_CUDA(cudaMemcpyAsync(&tc_err, tc_err_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+  TG_CUDA(cudaStreamSynchronize(s_));
+  if (tc_err) raise(TG_EDEVICE, "level-1 tensor-core operator: MMA completion wait timed out");
+  double dmax = 0.0, amax = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    dmax = std::max(dmax, std::fabs(double(a[i]) - double(bq[i])));
+    amax = std::max(amax, std::fabs(double(a[i])));
+  }
+  return amax > 0.0 ? dmax / amax : dmax;
+}
+
 double Solver::time_operator(int form, int reps) {
   const Grid& g = fp_.g;
   const bool fp32 = form == 1;
-  if (fp32 && !mixed_) raise(TG_EINVAL, "time_operator: FP32 operator needs a mixed-precision job");
+  if ((fp32 || form >= 3) && !mixed_)
+    raise(TG_EINVAL, "time_operator: FP32 operators need a mixed-precision job");
+  if (form >= 3) {
+    // Level 1 of the FP32 V-cycle, residual mode: form 3 the assembled stencil,
+    // form 4 the tensor-core operator.
+    if (!have_mg_ || !numeric_ok_) raise(TG_EINVAL, "time_operator: no multigrid hierarchy");
+    if (form == 4 && !l1_tc_) raise(TG_EINVAL, "time_operator: level-1 tensor-core path is off");
+    Level& L = *levels_[0];
+    launch_fill<float>(L.X<float>(), 1.0f, L.ndof, s_);
+    launch_fill<float>(L.B<float>(), 0.5f, L.ndof, s_);
+    cudaEvent_t a, b;
+    TG_CUDA(cudaEventCreate(&a));
+    TG_CUDA(cudaEventCreate(&b));
+    TG_CUDA(cudaEventRecord(a, s_));
+    for (int i = 0; i < reps; ++i) {
+      if (form == 4)
+        level1_op(kResidual, L, float(omega_));
+      else
+        mg_stencil_op<float>(kResidual, L.d, L.Am<float>(), L.act.p, L.X<float>(), L.B<float>(),
+                             L.Dinv<float>(), float(omega_), L.R<float>(), s_);
+    }
+    TG_CUDA(cudaEventRecord(b, s_));
+    TG_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    TG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return double(ms) / reps;
+  }
   launch_fill<double>(p_.p, 1.0, g.ndof, s_);
   if (fp32) launch_copy_d2f(pf_.p, p_.p, g.ndof, s_);
   cudaEvent_t a, b;
@@ -672,6 +776,12 @@ void Solver::vcycle_level(size_t l) {
   Level& N = *levels_[l];
   const T w = T(omega_);
   auto op = [&](int mode) {
+    if constexpr (sizeof(T) == 4) {
+      if (l == 1 && l1_tc_) {
+        level1_op(mode, L, float(w));
+        return;
+      }
+    }
     mg_stencil_op<T>(mode, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w, L.R<T>(),
                      s_);
   };
@@ -1117,6 +1227,15 @@ SolverStats Solver::solve(double tol, int max_it, const double* guess, double* u
       // and an FP32 iteration costs about 1/6 of the FP64 retry's.
       if (warm) seed();
       solved = mixed_refine(tol, std::min(cap, 3 * budget_), warm, st);
+    }
+    if (mixed_ && l1_tc_) {
+      // A tensor-core completion wait that ran out is a device error, not a
+      // solver verdict.
+      int tc_err = 0;
+      TG_CUDA(cudaMemcpyAsync(&tc_err, tc_err_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+      TG_CUDA(cudaStreamSynchronize(s_));
+      if (tc_err)
+        raise(TG_EDEVICE, "level-1 tensor-core operator: MMA completion wait timed out");
     }
     if (mixed_ && !solved) st.mixed_fallback = true;
     if (!solved && (!mixed_ || build_numeric<double>())) {

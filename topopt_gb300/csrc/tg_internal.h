@@ -181,6 +181,10 @@ bool fine_schedule_valid(const FineSchedule& s);
 FineSchedule fine_schedule_for(const Grid& g);
 void set_fine_schedule_override(const FineSchedule* s);  // null clears
 void set_fine_schedule(const Grid& g, const FineSchedule& s);
+// Whether the mixed form's V-cycle applies its level-1 operator on the tensor
+// cores (k_coarse_tc.cu) instead of the assembled FP32 stencil; on by default.
+bool level1_tc_enabled();
+void set_level1_tc(bool on);
 // Batched apply on the periodic nx*ny*nz torus (nodes = elements per axis); see
 // k_operator.cu.
 template <class T>

@@ -71,6 +71,9 @@ class Solver {
   // Time `reps` fine-operator launches (FP64 or FP32) on the current factors.
   // form: 0 FP64, 1 FP32, 2 the double-float residual kernel.
   double time_operator(int form, int reps);
+  // Level 1 of the FP32 V-cycle applied to a seeded vector by the assembled
+  // stencil and by the tensor-core operator: max |difference| / max |stencil|.
+  double check_level1();
   size_t device_bytes() const;
   int levels() const { return int(levels_.size()) + 1; }
 
@@ -136,6 +139,14 @@ class Solver {
   std::unique_ptr<InnerGraph> ig_;
   bool ig_failed_ = false, use_graph_ = true;
   DBuf<int> istate_;           // [0] iterations done, [1] budget, [2] breakdown
+  // Level 1 of the FP32 V-cycle on the tensor cores: per coarse element, 1 when
+  // its matrix is not sum_c E_c G_c (a Dirichlet or untouched fine DOF in a
+  // solid child, an inactive coarse DOF or a half element) and the stored
+  // matrix is applied instead; the kernel's timeout flag.
+  bool l1_tc_ = false;
+  DBuf<uint8_t> spec1_;
+  DBuf<int> tc_err_;
+  void level1_op(int mode, Level& L, float omega);
   int* h_ist_ = nullptr;       // pinned mirror of istate_
 };
 

@@ -6,6 +6,7 @@
 // divides into tiles.  The table maps grid dimensions to the schedule in use.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -40,5 +41,11 @@ void set_fine_schedule(const Grid& g, const FineSchedule& s) {
   std::lock_guard<std::mutex> lk(g_sched_mu);
   g_sched[std::make_tuple(g.nx, g.ny, g.nz)] = s;
 }
+
+namespace {
+std::atomic<bool> g_level1_tc{true};
+}
+bool level1_tc_enabled() { return g_level1_tc.load(); }
+void set_level1_tc(bool on) { g_level1_tc.store(on); }
 
 }  // namespace tg
