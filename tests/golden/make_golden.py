@@ -7,6 +7,7 @@ available; the committed golden.npz is what the tests read everywhere else.
 
     python tests/golden/make_golden.py                       # everything
     python tests/golden/make_golden.py --section cfg0_steps  # one section into the existing file
+    python tests/golden/make_golden.py --section homog
 """
 from __future__ import annotations
 
@@ -132,6 +133,7 @@ def main():
                cfg0_compliance=np.array(s0["compliance"]),
                cfg0_iterations=np.array(s0["iterations"]))
     out.update(_cfg0_steps(R))
+    out.update(_homog(R))
 
     # Heaviside projection: value and derivative at the fixture's spot values
     # and on a dense grid of rho_tilde, from the reference's own functions.
@@ -296,6 +298,110 @@ def _cfg0_steps(R):
     return out
 
 
+def _homog_reference_operator(R, kind, vpc, rho, tol=1e-12):
+    """C^H of one periodic unit cell with the reference's own compiled operator.
+
+    The harness (core/tests/harness/lattice_homog_probe.cpp:290-412) assembles
+    the periodic stiffness with Eigen, which is absent here; its operator is
+    rebuilt from the reference's Eigen-free fea_matfree_apply on the
+    (vpc+1)^3-node grid of the same cell:
+      * periodic apply: torus values unfolded onto the grid (node vpc = node 0
+        on every axis), the reference's apply, results folded back (wrapped
+        nodes summed);
+      * F_J: the apply of the global linear field of unit strain J -- on every
+        element it differs from the harness's element-local chi0_J by a rigid
+        translation, which Ke maps to zero;
+      * node 0 and untouched DOFs pinned (identity rows), Jacobi-PCG to `tol`;
+      * C^H_IJ = D_I . K D_J / |Y| with D_J = (linear field J) - unfold(chi_J),
+        the harness's element sum of (chi0 - chi_e)^T ke (chi0 - chi_e).
+    """
+    from topopt_gb300 import lattice
+    n = vpc
+    cell = lattice.cell(kind, n, lattice.calibrate(kind, n, rho)).astype(np.uint8).ravel()
+    pb = Problem(n, n, n, 1.0, cell)
+    nn = n + 1
+    idx = np.arange(nn)
+    tor = (idx % n)
+    cz, cy, cx = np.meshgrid(tor, tor, tor, indexing="ij")
+    g2t = ((cz * n + cy) * n + cx).ravel()  # grid node -> torus node
+
+    def unfold(v):
+        return v.reshape(-1, 3)[g2t].ravel()
+
+    def fold(v):
+        out = np.zeros((n ** 3, 3))
+        np.add.at(out, g2t, v.reshape(-1, 3))
+        return out.ravel()
+
+    def kfull(u):
+        return R.apply(pb, u, None, E=1.0)
+
+    z, y, x = np.meshgrid(idx, idx, idx, indexing="ij")
+    X, Y, Z = x.ravel().astype(float), y.ravel().astype(float), z.ravel().astype(float)
+    lin = []
+    for J in range(6):  # the harness's chi0 columns: xx, yy, zz, xy, yz, zx
+        u = np.zeros((nn ** 3, 3))
+        if J == 0: u[:, 0] = X
+        if J == 1: u[:, 1] = Y
+        if J == 2: u[:, 2] = Z
+        if J == 3: u[:, 0] = Y
+        if J == 4: u[:, 1] = Z
+        if J == 5: u[:, 2] = X
+        lin.append(u.ravel())
+    # touched DOFs and the Jacobi diagonal (uniform modulus: every diagonal entry of Ke equal)
+    ke = R.hex8_stiffness(1.0, 0.3, 1.0).reshape(24, 24)
+    cnt = np.zeros(n ** 3)
+    c3 = cell.reshape(n, n, n)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                cnt += np.roll(np.roll(np.roll(c3, dz, 0), dy, 1), dx, 2).ravel()
+    diag = np.repeat(cnt * ke[0, 0], 3)
+    pinned = np.repeat(cnt == 0, 3)
+    pinned[:3] = True
+    inv = np.where(pinned, 1.0, 1.0 / np.where(diag > 0, diag, 1.0))
+
+    def kper(v):
+        w = np.where(pinned, 0.0, v)
+        out = fold(kfull(unfold(w)))
+        return np.where(pinned, v, out)
+
+    chis = []
+    for J in range(6):
+        b = np.where(pinned, 0.0, fold(kfull(lin[J])))
+        xk = np.zeros_like(b)
+        r = b.copy()
+        bn2 = b @ b
+        z_ = inv * r
+        p = z_.copy()
+        rz = r @ z_
+        for _ in range(200000):
+            if r @ r <= tol * tol * bn2:
+                break
+            q = kper(p)
+            a = rz / (p @ q)
+            xk += a * p
+            r -= a * q
+            z_ = inv * r
+            rzn = r @ z_
+            p = z_ + (rzn / rz) * p
+            rz = rzn
+        chis.append(xk)
+    D = [lin[J] - unfold(chis[J]) for J in range(6)]
+    KD = [kfull(d) for d in D]
+    CH = np.array([[D[I] @ KD[J] for J in range(6)] for I in range(6)]) / float(n ** 3)
+    return cell, CH
+
+
+def _homog(R):
+    out = {}
+    for kind, vpc, rho in (("gyroid", 12, 0.3), ("octet", 12, 0.25)):
+        cell, CH = _homog_reference_operator(R, kind, vpc, rho)
+        out[f"homog_{kind}_cell"] = cell
+        out[f"homog_{kind}_CH"] = CH
+    return out
+
+
 def update_section(name):
     """Recompute one section into the existing golden.npz (every other array is
     kept as it is)."""
@@ -306,7 +412,7 @@ def update_section(name):
     path = os.path.join(HERE, "golden.npz")
     with np.load(path) as z:
         out = {k: z[k] for k in z.files}
-    new = {"cfg0_steps": _cfg0_steps}[name](R)
+    new = {"cfg0_steps": _cfg0_steps, "homog": _homog}[name](R)
     for k, v in new.items():
         if k in out and not np.array_equal(out[k], v, equal_nan=True):
             raise SystemExit(f"golden array {k} changed on regeneration")

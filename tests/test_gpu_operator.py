@@ -40,9 +40,9 @@ def test_fp32_schedules_match_oracle(tg, port, schedule, dims):
 
 def test_fp32_schedules_at_scale(tg, schedule):
     """256x128x128: every schedule agrees with the FP64 operator to FP32
-    rounding; the default schedule is the column kernel."""
+    rounding."""
     nx, ny, nz = 256, 128, 128
-    assert tg.fp32_schedule(nx, ny, nz)[0] == tg.SCHED_COLUMN
+    assert tg.fp32_schedule(nx, ny, nz)[0] in (tg.SCHED_PENCIL, tg.SCHED_COLUMN)
     pb = tg.Problem(nx, ny, nz)
     rng = np.random.default_rng(7)
     f = rng.random(pb.nv) * 0.999 + 0.001
@@ -71,3 +71,21 @@ def test_mixed_solve_same_answer_every_schedule(tg, schedule):
             precision=tg.PREC_MIXED))
         assert info.converged and not info.mixed_fallback, (kind, shape, kz, info)
         assert rel(um, u64) < 1e-8
+
+
+def test_autotuned_schedule_is_recorded(tg):
+    """A mixed job on a grid of >= 2^20 voxels measures the FP32 schedules on
+    its first use of those dimensions and records the fastest in the table."""
+    nx, ny, nz = 128, 96, 88
+    o = cantilever(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                    list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+    job = tg.SimpJob(pb, tg.SimpParams(), tg.SimpOptions(
+        volume_fraction=0.3, filter_radius=1.5, change_tol=0.0, max_iterations=2,
+        solve=tg.SolveOptions(precision=tg.PREC_MIXED)))
+    kind, shape, kz = tg.fp32_schedule(nx, ny, nz)
+    assert kind in (tg.SCHED_PENCIL, tg.SCHED_COLUMN)
+    assert kind == tg.SCHED_PENCIL or (0 <= shape < len(tg.FP32_SHAPES) and kz >= 8)
+    r = job.step()
+    assert r["compliance"] > 0.0
+    job.close()

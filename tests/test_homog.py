@@ -1,8 +1,9 @@
 """Periodic homogenization (core/tests/harness/lattice_homog_probe.cpp:290-412).
 
 CPU: the oracle's restatement recovers the isotropic tensor of a solid cell (the
-harness's H1 self-check) and gives symmetric, positive definite tensors on
-lattice cells.  GPU: the batched CUDA path against the oracle on the same cells
+harness's H1 self-check), matches tensors built on the reference's own compiled
+operator for a gyroid and an octet cell, and gives symmetric, positive definite
+tensors on lattice cells.  GPU: the batched CUDA path against the oracle on the same cells
 (Jacobi-PCG on both sides at tolerance 1e-10: tensors within 1e-7 relative),
 the H1 check, and batch invariance (a cell's tensor does not depend on the
 other cells or strain columns in the batch: bit-identical)."""
@@ -33,6 +34,19 @@ def test_oracle_solid_cell_isotropic(port):
     assert relerr(CH, iso()) < 1e-12
     CH, _, _ = port.homogenize(3, 4, 5, h=0.5, E=2.0, nu=0.25, tol=1e-12)
     assert relerr(CH, iso(2.0, 0.25)) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["gyroid", "octet"])
+def test_oracle_pinned_to_reference_operator(port, golden, kind):
+    """The restatement against tensors built on the reference's own compiled
+    operator (fea_matfree_apply folded onto the torus, tests/golden/make_golden.py
+    _homog_reference_operator): a 12^3 gyroid at relative density 0.3 and an
+    octet truss at 0.25, both solved to 1e-12."""
+    cell = golden[f"homog_{kind}_cell"]
+    want = golden[f"homog_{kind}_CH"]
+    CH, it, conv = port.homogenize(12, 12, 12, solid=cell, tol=1e-12)
+    assert conv
+    assert relerr(CH, want) < 1e-10
 
 
 def test_oracle_lattice_tensor_properties(port):
@@ -101,3 +115,15 @@ def test_gpu_mixed_matches_fp64(tg):
         assert relerr(a, b) < 1e-8
     solo, _ = tg.homogenize(cells[1], tolerance=1e-10, precision=tg.PREC_MIXED)
     assert np.array_equal(solo[0], c32[1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["gyroid", "octet"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_matches_reference_operator_tensors(tg, golden, kind, prec):
+    """The batched CUDA path (FP64 and mixed) against the tensors built on the
+    reference's own compiled operator."""
+    cell = golden[f"homog_{kind}_cell"].reshape(12, 12, 12)
+    got, info = tg.homogenize(cell, tolerance=1e-10, precision=prec)
+    assert info["converged"]
+    assert relerr(got[0], golden[f"homog_{kind}_CH"]) < 1e-7

@@ -35,6 +35,7 @@
 #include "tg_tc.h"
 
 #include <algorithm>
+#include <atomic>
 
 namespace tg {
 namespace {
@@ -63,7 +64,7 @@ __device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xfffffff
 template <int MODE>
 __global__ void __launch_bounds__(128) k_level1_tc(
     MgDims fd, MgDims cd, int KZ, const float* __restrict__ ef, const uint8_t* __restrict__ act,
-    const uint8_t* __restrict__ spec, const float* __restrict__ Kel,
+    const int* __restrict__ spos, const float* __restrict__ yspec,
     const float* __restrict__ G, const float* __restrict__ x, const float* __restrict__ b,
     const float* __restrict__ invdiag, float omega, float* __restrict__ y,
     int* __restrict__ err) {
@@ -193,14 +194,14 @@ __global__ void __launch_bounds__(128) k_level1_tc(
       }
       const bool valid = ev[j] && ezok;
       const int64_t ce = valid ? (int64_t(ez) * cd.ey + (ey0 + j)) * cd.ex + ex : 0;
-      const bool special = valid && spec[ce] != 0;
+      const int sp = valid ? spos[ce] : -1;  // off the fast path: its outputs precomputed
       // Children's moduli (0 for children outside the fine grid).
       float E[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         const int fi = 2 * ex + (c & 1), fj = 2 * (ey0 + j) + ((c >> 1) & 1),
                   fk = 2 * ez + (c >> 2);
-        E[c] = (valid && fi < fd.ex && fj < fd.ey && fk < fd.ez)
+        E[c] = (valid && sp < 0 && fi < fd.ex && fj < fd.ey && fk < fd.ez)
                    ? ef[(int64_t(fk) * fd.ey + fj) * fd.ex + fi]
                    : 0.0f;
       }
@@ -264,15 +265,9 @@ __global__ void __launch_bounds__(128) k_level1_tc(
         out[2 * r] = acc[r].x;
         out[2 * r + 1] = acc[r].y;
       }
-      if (special) {
-        const float* K = Kel + ce * 576;
-#pragma unroll 4
-        for (int r = 0; r < 24; ++r) {
-          float a = 0.0f;
+      if (sp >= 0) {
 #pragma unroll
-          for (int k = 0; k < 24; ++k) a = fmaf(K[r * 24 + k], u[k], a);
-          out[r] = a;
-        }
+        for (int r = 0; r < 24; ++r) out[r] = yspec[int64_t(sp) * 24 + r];
       }
       // Node row j: the previous element's +y corners and this element's -y
       // corners, then the x-combine with the lane below.
@@ -341,37 +336,68 @@ __global__ void __launch_bounds__(128) k_level1_tc(
   if (w == 0) tc::tmem_dealloc(tmem, kTcTmemCols);
 }
 
+// The elements off the fast path: one warp per element, lane r < 24 forms row r
+// of (stored element matrix) x (element DOFs) into yspec[p].
+__global__ void __launch_bounds__(256) k_level1_special(MgDims cd, int nspec,
+                                                        const int* __restrict__ list,
+                                                        const float* __restrict__ Kel,
+                                                        const float* __restrict__ x,
+                                                        float* __restrict__ yspec) {
+  const int lane = threadIdx.x & 31;
+  const int p = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (p >= nspec) return;
+  const int64_t ce = list[p];
+  const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey), K = int(ce / (int64_t(cd.ex) * cd.ey));
+  float uk = 0.0f;
+  if (lane < 24) {
+    const int c = lane / 3, comp = lane % 3;
+    const int64_t node = (int64_t(K + (c >> 2)) * cd.nny + (J + ((c >> 1) & 1))) * cd.nnx +
+                         (I + (c & 1));
+    uk = x[3 * node + comp];
+  }
+  float a = 0.0f;
+  const float* Kr = Kel + ce * 576 + int64_t(lane < 24 ? lane : 0) * 24;
+#pragma unroll
+  for (int k = 0; k < 24; ++k) a = fmaf(Kr[k], __shfl_sync(0xffffffffu, uk, k), a);
+  if (lane < 24) yspec[int64_t(p) * 24 + lane] = a;
+}
+
 }  // namespace
 
 int level1_tc_kz(const MgDims& cd) {
-  const int chunks = std::max(1, (cd.nnz + 31) / 32);
+  const int chunks = std::max(1, (cd.nnz + 7) / 8);
   return std::max(4, (cd.nnz + chunks - 1) / chunks);
 }
 
 void mg_level1_tc(int mode, const MgDims& fd, const MgDims& cd, const float* ef,
-                  const uint8_t* act, const uint8_t* spec, const float* Kel, const float* G,
-                  const float* x, const float* b, const float* invdiag, float omega, float* y,
-                  int* err, cudaStream_t s) {
-  static bool attr_set = false;  // per process; the attribute is per function
-  if (!attr_set) {
+                  const uint8_t* act, const int* spos, const int* slist, int nspec,
+                  const float* Kel, const float* G, const float* x, const float* b,
+                  const float* invdiag, float omega, float* y, float* yspec, int* err,
+                  cudaStream_t s) {
+  static std::atomic<int> attr_set{0};  // the attribute is set once per process
+  if (!attr_set.load()) {
     TG_CUDA(cudaFuncSetAttribute(k_level1_tc<kApply>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  kTcSmem));
     TG_CUDA(cudaFuncSetAttribute(k_level1_tc<kResidual>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     TG_CUDA(cudaFuncSetAttribute(k_level1_tc<kSmooth>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
-    attr_set = true;
+    attr_set.store(1);
+  }
+  if (nspec > 0) {
+    k_level1_special<<<(nspec + 7) / 8, 256, 0, s>>>(cd, nspec, slist, Kel, x, yspec);
+    TG_LAUNCH_CHECK();
   }
   const int kz = level1_tc_kz(cd);
   const dim3 grid((cd.nnx + 29) / 30, (cd.nny + kTcRows - 1) / kTcRows, (cd.nnz + kz - 1) / kz);
   if (mode == kApply)
-    k_level1_tc<kApply><<<grid, 128, kTcSmem, s>>>(fd, cd, kz, ef, act, spec, Kel, G, x, b,
+    k_level1_tc<kApply><<<grid, 128, kTcSmem, s>>>(fd, cd, kz, ef, act, spos, yspec, G, x, b,
                                                    invdiag, omega, y, err);
   else if (mode == kResidual)
-    k_level1_tc<kResidual><<<grid, 128, kTcSmem, s>>>(fd, cd, kz, ef, act, spec, Kel, G, x, b,
+    k_level1_tc<kResidual><<<grid, 128, kTcSmem, s>>>(fd, cd, kz, ef, act, spos, yspec, G, x, b,
                                                       invdiag, omega, y, err);
   else
-    k_level1_tc<kSmooth><<<grid, 128, kTcSmem, s>>>(fd, cd, kz, ef, act, spec, Kel, G, x, b,
+    k_level1_tc<kSmooth><<<grid, 128, kTcSmem, s>>>(fd, cd, kz, ef, act, spos, yspec, G, x, b,
                                                     invdiag, omega, y, err);
   TG_LAUNCH_CHECK();
 }

@@ -949,13 +949,45 @@ static void launch_mode(const Grid& g, const ModalConsts& c, const T* ef, const 
   TG_LAUNCH_CHECK();
 }
 
+void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const ModalConsts& c,
+                          const float* ef, const uint8_t* kept, const float* x, const float* b,
+                          const float* invdiag, float omega, float* y, double* dot_part,
+                          int* nblocks_out, cudaStream_t s, const uint8_t* kn);
+
 template <class T>
 void launch_fine_op(int mode, const Grid& g, const ModalConsts& c, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
                     T* y, double* dot_part, int* nblocks_out, cudaStream_t s,
                     const uint8_t* kn) {
   if constexpr (std::is_same<T, float>::value) {
-    const FineSchedule fs = fine_schedule_for(g);
+    launch_fine_op_sched(fine_schedule_for(g), mode, g, c, ef, kept, x, b, invdiag, omega, y,
+                         dot_part, nblocks_out, s, kn);
+    return;
+  }
+  if (nblocks_out) {
+    const dim3 d = pencil_grid<T>(g);
+    *nblocks_out = int(d.x * d.y * d.z);
+  }
+  switch (mode) {
+    case kApply:
+      launch_mode<T, kApply>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    case kResidual:
+      launch_mode<T, kResidual>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
+      break;
+    default:
+      launch_mode<T, kSmooth>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
+  }
+}
+
+// The FP32 operator under an explicit schedule (the autotuner times candidates
+// through this without touching the process-wide table).
+void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const ModalConsts& c,
+                          const float* ef, const uint8_t* kept, const float* x, const float* b,
+                          const float* invdiag, float omega, float* y, double* dot_part,
+                          int* nblocks_out, cudaStream_t s, const uint8_t* kn) {
+  using T = float;
+  {
     if (fs.kind == FineSchedule::kColumn) {
       const ColCfg cc{fs.shape, fs.kz};
       if (nblocks_out) {

@@ -37,6 +37,7 @@ const double kEta[8] = {-1, -1, +1, +1, -1, -1, +1, +1};
 const double kZeta[8] = {-1, -1, -1, -1, +1, +1, +1, +1};
 constexpr int kMaxCoarseDof = 8192;   // dense coarsest factor <= 512 MB
 constexpr int kMaxInverseDof = 512;   // explicit coarsest inverse up to here
+constexpr int64_t kAutotuneMinVoxels = int64_t(1) << 20;  // FP32 schedule measured from here
 
 MgDims dims_of(int ex, int ey, int ez) { return MgDims{ex, ey, ez, ex + 1, ey + 1, ez + 1}; }
 }  // namespace
@@ -356,6 +357,15 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   if (mixed_) {
     Ef_.alloc(size_t(fp.g.nv));
     for (DBuf<float>* b : {&invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_}) b->alloc(n);
+    // Large grids: the FP32 operator's tile shape and z-chunk are measured on
+    // first use of the grid's dimensions in the process (a few ms; smaller
+    // grids keep the default schedule).
+    if (fp.g.nv >= kAutotuneMinVoxels && !fine_schedule_known(fp.g)) {
+      launch_fill<float>(Ef_.p, 1.0f, fp.g.nv, s_);
+      launch_fill<float>(pf_.p, 1.0f, fp.g.ndof, s_);
+      autotune_fine_schedule(fp.g, fp.mc, Ef_.p, fp.kept.p, fp.kept_node.p, pf_.p, apf_.p,
+                             part_.p, s_);
+    }
   }
   if (opt.solver == TG_SOLVER_MGCG) build_structure();
 }
@@ -385,6 +395,7 @@ size_t Solver::device_bytes() const {
   for (const DBuf<float>* d : {&Ef_, &invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_})
     b += d->bytes();
   for (const auto& L : levels_) b += L->bytes();
+  b += spos1_.bytes() + slist1_.bytes() + yspec1_.bytes() + tc_err_.bytes();
   return b + cidx_.bytes() + kebf_.bytes() + Gf_.bytes();
 }
 
@@ -541,8 +552,21 @@ void Solver::build_structure() {
         spec[size_t(ce)] = uint8_t(sp);
       }
     });
-    spec1_.alloc(spec.size());
-    TG_CUDA(cudaMemcpyAsync(spec1_.p, spec.data(), spec1_.bytes(), cudaMemcpyHostToDevice, s_));
+    std::vector<int> spos(spec.size(), -1), slist;
+    for (size_t ce = 0; ce < spec.size(); ++ce)
+      if (spec[ce]) {
+        spos[ce] = int(slist.size());
+        slist.push_back(int(ce));
+      }
+    nspec1_ = int(slist.size());
+    spos1_.alloc(spos.size());
+    TG_CUDA(cudaMemcpyAsync(spos1_.p, spos.data(), spos1_.bytes(), cudaMemcpyHostToDevice, s_));
+    if (nspec1_ > 0) {
+      slist1_.alloc(slist.size());
+      yspec1_.alloc(slist.size() * 24);
+      TG_CUDA(cudaMemcpyAsync(slist1_.p, slist.data(), slist1_.bytes(), cudaMemcpyHostToDevice,
+                              s_));
+    }
     tc_err_.alloc(1);
     TG_CUDA(cudaMemsetAsync(tc_err_.p, 0, sizeof(int), s_));
   }
@@ -554,9 +578,9 @@ void Solver::build_structure() {
 // L.R = b - A1 x or the smoothed iterate, as the stencil apply would write it.
 void Solver::level1_op(int mode, Level& L, float omega) {
   const Grid& g = fp_.g;
-  mg_level1_tc(mode, dims_of(g.nx, g.ny, g.nz), L.d, Ef_.p, L.act.p, spec1_.p, L.Ke<float>(),
-               Gf_.p, L.X<float>(), L.B<float>(), L.Dinv<float>(), omega, L.R<float>(),
-               tc_err_.p, s_);
+  mg_level1_tc(mode, dims_of(g.nx, g.ny, g.nz), L.d, Ef_.p, L.act.p, spos1_.p, slist1_.p,
+               nspec1_, L.Ke<float>(), Gf_.p, L.X<float>(), L.B<float>(), L.Dinv<float>(), omega,
+               L.R<float>(), yspec1_.p, tc_err_.p, s_);
 }
 
 double Solver::read_scalar(int idx) {

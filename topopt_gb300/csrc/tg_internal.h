@@ -181,6 +181,17 @@ bool fine_schedule_valid(const FineSchedule& s);
 FineSchedule fine_schedule_for(const Grid& g);
 void set_fine_schedule_override(const FineSchedule* s);  // null clears
 void set_fine_schedule(const Grid& g, const FineSchedule& s);
+bool fine_schedule_known(const Grid& g);  // in the table, or an override is set
+// The FP32 operator under an explicit schedule.
+void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const ModalConsts& c,
+                          const float* ef, const uint8_t* kept, const float* x, const float* b,
+                          const float* invdiag, float omega, float* y, double* dot_part,
+                          int* nblocks_out, cudaStream_t s, const uint8_t* kn);
+// Times every candidate schedule of the FP32 apply on the given buffers (CUDA
+// events on s), stores the fastest in the table for g and returns it.
+FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const float* ef,
+                                    const uint8_t* kept, const uint8_t* kn, const float* x,
+                                    float* y, double* part, cudaStream_t s, int reps = 3);
 // Whether the mixed form's V-cycle applies its level-1 operator on the tensor
 // cores (k_coarse_tc.cu) instead of the assembled FP32 stencil; on by default.
 bool level1_tc_enabled();

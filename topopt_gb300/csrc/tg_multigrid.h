@@ -76,12 +76,15 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
 
 // The FP32 level-1 Galerkin operator on the tensor cores (k_coarse_tc.cu):
 // y = A1 x (kApply), b - A1 x (kResidual) or x + omega D^-1 (b - A1 x) (kSmooth),
-// masked by act, from the fine FP32 factors ef, the 8 child blocks G (FP32,
-// [8][576] corner-bit order) and, for the coarse elements flagged in spec, their
-// stored element matrices Kel.  A wait that runs out sets *err.
+// masked by act, from the fine FP32 factors ef and the 8 child blocks G (FP32,
+// [8][576] corner-bit order).  The nspec coarse elements off the fast path
+// (slist; spos[ce] = position in slist or -1) are applied from their stored
+// matrices Kel by a pre-pass into yspec (nspec x 24).  A wait that runs out
+// sets *err.
 void mg_level1_tc(int mode, const MgDims& fd, const MgDims& cd, const float* ef,
-                  const uint8_t* act, const uint8_t* spec, const float* Kel, const float* G,
-                  const float* x, const float* b, const float* invdiag, float omega, float* y,
-                  int* err, cudaStream_t s);
+                  const uint8_t* act, const int* spos, const int* slist, int nspec,
+                  const float* Kel, const float* G, const float* x, const float* b,
+                  const float* invdiag, float omega, float* y, float* yspec, int* err,
+                  cudaStream_t s);
 
 }  // namespace tg

@@ -144,7 +144,9 @@ class Solver {
   // solid child, an inactive coarse DOF or a half element) and the stored
   // matrix is applied instead; the kernel's timeout flag.
   bool l1_tc_ = false;
-  DBuf<uint8_t> spec1_;
+  int nspec1_ = 0;
+  DBuf<int> spos1_, slist1_;  // per coarse element: position in slist1_ or -1
+  DBuf<float> yspec1_;        // their outputs, nspec1_ x 24
   DBuf<int> tc_err_;
   void level1_op(int mode, Level& L, float omega);
   int* h_ist_ = nullptr;       // pinned mirror of istate_

@@ -7,7 +7,9 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <algorithm>
 #include <map>
+#include <vector>
 #include <mutex>
 #include <tuple>
 
@@ -40,6 +42,65 @@ void set_fine_schedule_override(const FineSchedule* s) {
 void set_fine_schedule(const Grid& g, const FineSchedule& s) {
   std::lock_guard<std::mutex> lk(g_sched_mu);
   g_sched[std::make_tuple(g.nx, g.ny, g.nz)] = s;
+}
+
+bool fine_schedule_known(const Grid& g) {
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  return g_have_override || g_sched.count(std::make_tuple(g.nx, g.ny, g.nz)) != 0;
+}
+
+// The measured sweep: every column tile shape with z-chunks of about 8 .. 33
+// element layers, and the pencil kernel, each launched once untimed and then
+// timed over `reps` back-to-back launches of the apply (with the kept mask and
+// the p.Ap partials, as the inner PCG runs it).  The fastest goes into the
+// table for g's dimensions.  Results of every candidate agree to FP32
+// rounding, so the choice changes timing only.
+FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const float* ef,
+                                    const uint8_t* kept, const uint8_t* kn, const float* x,
+                                    float* y, double* part, cudaStream_t s, int reps) {
+  std::vector<FineSchedule> cands;
+  FineSchedule pencil;
+  pencil.kind = FineSchedule::kPencil;
+  cands.push_back(pencil);
+  std::vector<int> kzs;
+  for (int target : {8, 11, 13, 16, 22, 26, 33}) {
+    const int chunks = std::max(1, (g.nnz + target - 1) / target);
+    const int kz = std::max(8, (g.nnz + chunks - 1) / chunks);
+    if (std::find(kzs.begin(), kzs.end(), kz) == kzs.end()) kzs.push_back(kz);
+  }
+  for (int sh = 0; sh < fine_schedule_shapes(); ++sh)
+    for (int kz : kzs) {
+      FineSchedule c;
+      c.kind = FineSchedule::kColumn;
+      c.shape = sh;
+      c.kz = kz;
+      cands.push_back(c);
+    }
+  cudaEvent_t a, b;
+  TG_CUDA(cudaEventCreate(&a));
+  TG_CUDA(cudaEventCreate(&b));
+  FineSchedule best = default_fine_schedule(g);
+  float best_ms = 1e30f;
+  for (const FineSchedule& c : cands) {
+    launch_fine_op_sched(c, kApply, g, mc, ef, kept, x, nullptr, nullptr, 0.0f, y, part, nullptr,
+                         s, kn);
+    TG_CUDA(cudaEventRecord(a, s));
+    for (int r = 0; r < reps; ++r)
+      launch_fine_op_sched(c, kApply, g, mc, ef, kept, x, nullptr, nullptr, 0.0f, y, part,
+                           nullptr, s, kn);
+    TG_CUDA(cudaEventRecord(b, s));
+    TG_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    TG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  set_fine_schedule(g, best);
+  return best;
 }
 
 namespace {
