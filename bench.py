@@ -405,6 +405,44 @@ def run_op_only(args):
 
 
 # ------------------------------------------------------ secondary workloads
+def _oracle_problem(pb):
+    from oracle.oracle import Problem
+    return Problem(pb.nx, pb.ny, pb.nz, pb.spacing, pb.tags, pb.bcs, pb.loads)
+
+
+def _cpu_design_sample(designs, iters):
+    """Whole OC design iterations of a few designs on the host cores, one design
+    at a time: the oracle's CPU restatement of the reference's MG-PCG design
+    iteration.  Returns (iterations/s, cores, note)."""
+    from oracle.oracle import OracleLib
+    port = OracleLib("port")
+    n, t = 0, 0.0
+    for pb, prm, opt in designs:
+        o = _oracle_problem(pb)
+        x0 = np.full(o.nv, opt.volume_fraction)
+        r = port.design_iterations_mg(o, x0, iters, volfrac=opt.volume_fraction,
+                                      radius=opt.filter_radius, move=opt.move, cg_tol=1e-8)
+        n += iters
+        t += float(r["seconds"].sum())
+    return n / t, port.threads(), f"{len(designs)} designs x {iters} iterations, {t:.1f} s"
+
+
+def _fp32_roofline(tg, pb, prm, opt, label):
+    """The FP32 fine operator on one design (CUDA events on its job's stream)."""
+    hbm, src = peaks()
+    job = tg.SimpJob(pb, prm, tg.SimpOptions(
+        volume_fraction=opt.volume_fraction, filter_radius=opt.filter_radius, move=opt.move,
+        change_tol=0.0, max_iterations=2, solve=tg.SolveOptions(precision=tg.PREC_MIXED)))
+    job.step()
+    ms = job.time_operator(tg.PREC_MIXED, 20)
+    job.close()
+    byt = 2 * pb.ndof * 4 + pb.nv * 4
+    ach = byt / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": f"fine operator apply, FP32, {label}", "achieved": ach,
+            "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_source": src,
+            "bytes_per_launch": byt, "ms_per_launch": ms, "traffic": None}
+
+
 def _pctl(v, q):
     return float(np.percentile(np.asarray(v, dtype=float), q)) if len(v) else None
 
@@ -428,6 +466,7 @@ def run_batch(args):
     st = srv.stats()
     srv.close()
     iters = sum(r["iterations"] for r in res)
+    launches = None
     # Plain FP64, one design at a time, on a sample.
     sample = [workloads.design(s, precision=tg.PREC_FP64, iterations=K) for s in range(4)]
     t0 = time.perf_counter()
@@ -444,6 +483,22 @@ def run_batch(args):
             "wall_s": wall, "clocks": cs.summary(), "server": st,
             "fp64_one_at_a_time": {"design_iters_per_s": 4 * K / t64, "designs": 4},
             "speedup_vs_fp64_one_at_a_time": (iters / wall) / (4 * K / t64)}
+    # The whole batch already runs through the public API with host buffers.
+    h2d = sum(pb.nv + 16 * (pb.nbc + pb.nloads) for pb, _, _ in jobs)
+    d2h = sum(2 * pb.nv * 8 for pb, _, _ in jobs)
+    line["e2e"] = {"value": iters / wall, "unit": "design_iters/s",
+                   "h2d_bytes_per_step": h2d / max(1, iters), "d2h_bytes_per_step": d2h / max(1, iters),
+                   "includes": "submission of every design (host problem), all iterations, results "
+                               "(design and physical density) read back"}
+    big = max(jobs, key=lambda j: j[0].nv)
+    line["roofline"] = _fp32_roofline(tg, *big, f"largest design of the batch "
+                                                  f"({big[0].nx}x{big[0].ny}x{big[0].nz})")
+    if not args.no_cpu:
+        v, cores, note = _cpu_design_sample(jobs[:3], 2)
+        line["cpu_baseline"] = {"value": v, "unit": "design_iters/s", "cores": cores,
+                                "kind": "port",
+                                "sample": "oracle/oracle_mg.c (CPU restatement of the reference's "
+                                          "MG-PCG design iteration), one design at a time: " + note}
     print(json.dumps(line), flush=True)
 
 
@@ -472,6 +527,25 @@ def run_homog(args):
             "fp64": {"cells_per_s": ns / t64, "cells": ns, "info": info64},
             "ch_rel_err_mixed_vs_fp64": err,
             "mean_density": float(np.mean([m[2] for m in meta]))}
+    line["e2e"] = {"value": args.cells / wall, "unit": "cells/s",
+                   "h2d_bytes_per_step": 32 ** 3, "d2h_bytes_per_step": 36 * 8,
+                   "includes": "tg_homogenize on host cell arrays: upload, batched solves, tensors "
+                               "read back (per cell)"}
+    line["roofline"] = None
+    line["roofline_note"] = ("the batched periodic operator runs inside the lock-step solve only; "
+                             "its kernel is the pencil operator of the FP64 form (see the headline "
+                             "line for the fine operator's roofline)")
+    if not args.no_cpu:
+        from oracle.oracle import OracleLib
+        port = OracleLib("port")
+        nc = 2
+        t0 = time.perf_counter()
+        for c in cells[:nc]:
+            port.homogenize(32, 32, 32, solid=np.ascontiguousarray(c).ravel(), tol=1e-8)
+        tc = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nc / tc, "unit": "cells/s", "cores": 1, "kind": "port",
+                                "sample": f"oracle homogenize (FP64 Jacobi-PCG, the harness's "
+                                          f"method), {nc} cells of the batch, one core"}
     print(json.dumps(line), flush=True)
 
 
@@ -519,12 +593,26 @@ def run_serve(args):
                        "arrival_seconds": args.serve_seconds, "jobs": len(stream),
                        "hbm_budget_gb": 150, "max_active": args.max_active},
             "jobs_per_s": len(res) / wall, "wall_s": wall,
-            "gpu_occupancy": st["busy_ms"] / st["uptime_ms"] if st["uptime_ms"] else None,
+            "host_busy_frac": st["busy_ms"] / st["uptime_ms"] if st["uptime_ms"] else None,
             "queue_ms_p50": _pctl([r["t_queue_ms"] for r in res], 50),
             "queue_ms_p99": _pctl([r["t_queue_ms"] for r in res], 99),
             "server": st, "clocks": cs.summary(),
             "fp64_one_at_a_time": {"mean_service_s": svc64, "jobs_per_s": 1.0 / svc64,
                                    "sample_jobs": len(sample)}}
+    line["host_busy_note"] = ("fraction of the loop's uptime with at least one job admitted "
+                              "(host-side), not device occupancy")
+    line["e2e"] = {"value": _pctl(lat, 50), "unit": "ms",
+                   "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                   "includes": "arrival (host problem) to result read back, through tg_server"}
+    if not args.no_cpu:
+        small = sorted(stream, key=lambda a: a[1].nv)[:2]
+        v, cores, note = _cpu_design_sample([(p, q, o) for _, p, q, o in small], 2)
+        its = small[0][3].max_iterations
+        line["cpu_baseline"] = {"value": 1e3 * its / v, "unit": "ms (service time of a job, "
+                                "one at a time)", "cores": cores, "kind": "port",
+                                "sample": "oracle/oracle_mg.c design iterations on the two "
+                                          f"smallest jobs of the stream ({note}), scaled to "
+                                          f"{its} iterations per job"}
     print(json.dumps(line), flush=True)
 
 

@@ -139,22 +139,37 @@ __global__ void __launch_bounds__(128) k_level1_tc(
 #pragma unroll
   for (int i = 0; i <= Y; ++i) pend[i][0] = pend[i][1] = pend[i][2] = 0.0f;
 
-  auto emit = [&](int i, int ez, const float (&ax)[3]) {
+  // Activity, right-hand side and inverse diagonal of node row i, layer c,
+  // requested an element ahead of their use.
+  struct RowIn {
+    float bv[3], dv[3];
+    bool ak[3];
+  };
+  auto load_row = [&](int i, int c, RowIn& q) {
+    const bool ok = c >= 0 && c < cd.nnz && ro[i];
+    const int64_t d0 = 3 * (int64_t(c) * plane + col + int64_t(i) * cd.nnx);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      q.ak[k] = ok && act[d0 + k] != 0;
+      q.bv[k] = (MODE != kApply && ok) ? b[d0 + k] : 0.0f;
+      q.dv[k] = (MODE == kSmooth && ok) ? invdiag[d0 + k] : 0.0f;
+    }
+  };
+  auto emit = [&](int i, int ez, const float (&ax)[3], const RowIn& q) {
     const int64_t d0 = 3 * (int64_t(ez) * plane + col + int64_t(i) * cd.nnx);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const int64_t d = d0 + k;
       float out;
-      if (!act[d]) {
+      if (!q.ak[k]) {
         out = 0.0f;
       } else if constexpr (MODE == kApply) {
         out = ax[k];
       } else if constexpr (MODE == kResidual) {
-        out = b[d] - ax[k];
+        out = q.bv[k] - ax[k];
       } else {
-        out = cur[i][k] + omega * invdiag[d] * (b[d] - ax[k]);
+        out = cur[i][k] + omega * q.dv[k] * (q.bv[k] - ax[k]);
       }
-      y[d] = out;
+      y[d0 + k] = out;
     }
   };
 
@@ -164,6 +179,8 @@ __global__ void __launch_bounds__(128) k_level1_tc(
     if (s < KZ) load_layer(ez + 2, raw);
     const bool out_z = s >= 1 && ez < cd.nnz;
     const bool ezok = ez >= 0 && ez < cd.ez;
+    RowIn rin;
+    load_row(1, out_z ? ez : -1, rin);
     float c1[3], n1[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -201,7 +218,7 @@ __global__ void __launch_bounds__(128) k_level1_tc(
       for (int c = 0; c < 8; ++c) {
         const int fi = 2 * ex + (c & 1), fj = 2 * (ey0 + j) + ((c >> 1) & 1),
                   fk = 2 * ez + (c >> 2);
-        E[c] = (valid && sp < 0 && fi < fd.ex && fj < fd.ey && fk < fd.ez)
+        E[c] = (valid && fi < fd.ex && fj < fd.ey && fk < fd.ez)
                    ? ef[(int64_t(fk) * fd.ey + fj) * fd.ex + fi]
                    : 0.0f;
       }
@@ -300,7 +317,8 @@ __global__ void __launch_bounds__(128) k_level1_tc(
           ax[k] = pend[j][k] + N[0][k];
           pend[j][k] = N[1][k];
         }
-        if (out_z && ro[j]) emit(j, ez, ax);
+        if (out_z && ro[j]) emit(j, ez, ax, rin);
+        load_row(j + 1, out_z ? ez : -1, rin);
       }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -321,7 +339,7 @@ __global__ void __launch_bounds__(128) k_level1_tc(
         ax[k] = pend[Y][k] + (NY[0][k] + xs[s & 1][w + 1][k][lane]);
         pend[Y][k] = NY[1][k] + xs[s & 1][w + 1][3 + k][lane];
       }
-      if (out_z && ro[Y]) emit(Y, ez, ax);
+      if (out_z && ro[Y]) emit(Y, ez, ax, rin);
     }
 #pragma unroll
     for (int i = 0; i <= Y; ++i)
@@ -364,8 +382,9 @@ __global__ void __launch_bounds__(256) k_level1_special(MgDims cd, int nspec,
 
 }  // namespace
 
+// z-chunks of about 6 node layers: enough CTAs to fill the GPU at two per SM.
 int level1_tc_kz(const MgDims& cd) {
-  const int chunks = std::max(1, (cd.nnz + 7) / 8);
+  const int chunks = std::max(1, (cd.nnz + 5) / 6);
   return std::max(4, (cd.nnz + chunks - 1) / chunks);
 }
 
