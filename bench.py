@@ -270,6 +270,7 @@ def run_ours(args, world, rank, local, pg):
     for form in order:
         prec = tg.PREC_MIXED if form == "mixed" else tg.PREC_FP64
         job = tg.SimpJob(pb, params, opts(prec, args.warmup + args.steps + 1))
+        sched = tg.fp32_schedule(nx, ny, nz)
         for _ in range(args.warmup):
             job.step()
         if form == "mixed":  # the state the timed window starts from (CPU baseline input)
@@ -298,6 +299,11 @@ def run_ours(args, world, rank, local, pg):
             oc_volume_passes=statistics.median(r["oc_volume_passes"] for r in rows),
             compliance=[r["compliance"] for r in rows],
             device_gb=job.device_bytes / 1e9)
+        if form == "mixed":
+            forms[form]["fp32_schedule"] = {"kind": sched[0], "shape": sched[1], "kz": sched[2],
+                                            "source": "measured on the job's first use of the grid"}
+            forms[form]["op_level1_tc_ms"] = job.time_operator(tg.APPLY_L1_TC, 10)
+            forms[form]["op_level1_stencil_ms"] = job.time_operator(tg.APPLY_L1_STENCIL, 10)
         # Dominant-kernel timing (CUDA events, job stream).
         forms[form]["op_fp64_ms"] = job.time_operator(tg.PREC_FP64, 5)
         if form == "mixed":
@@ -385,23 +391,28 @@ def run_ours(args, world, rank, local, pg):
 
 
 def run_op_only(args):
-    """Fine-operator launches on a resident job of the benchmark workload (its
-    kept mask and element factors), for ncu captures: three FP32 or FP64
-    launches after one design iteration."""
+    """Operator launches on a resident job of the benchmark workload (its kept
+    mask and element factors), for ncu captures: three launches of the FP32 or
+    FP64 fine operator, or of the level-1 tensor-core operator ("l1tc").  The
+    FP32 schedule comes from --fp32-schedule (kind,shape,kz), so no autotuning
+    launches precede the captured ones."""
     import topopt_gb300 as tg
     from topopt_gb300.build import build
     build()
+    if args.fp32_schedule:
+        tg.set_fp32_schedule(*(int(v) for v in args.fp32_schedule.split(",")))
     nx, ny, nz = args.nx, args.ny, args.nz
     bcs, loads = cantilever_random_load(nx, ny, nz)
     pb = tg.Problem(nx, ny, nz, 1.0, None, bcs, loads)
-    prec = tg.PREC_MIXED if args.op_only == "fp32" else tg.PREC_FP64
+    prec = tg.PREC_FP64 if args.op_only == "fp64" else tg.PREC_MIXED
     job = tg.SimpJob(pb, tg.SimpParams(), tg.SimpOptions(
         volume_fraction=0.3, filter_radius=1.5, move=0.2, change_tol=0.0, cg_tolerance=1e-8,
         max_iterations=2, solve=tg.SolveOptions(precision=prec, mg_levels=args.mg_levels)))
-    job.step()
-    ms = job.time_operator(prec, 3)
+    form = {"fp32": tg.PREC_MIXED, "fp64": tg.PREC_FP64, "l1tc": tg.APPLY_L1_TC}[args.op_only]
+    ms = job.time_operator(form, 3)
     job.close()
-    print(json.dumps({"op_only": args.op_only, "ms_per_launch": ms}))
+    print(json.dumps({"op_only": args.op_only, "ms_per_launch": ms,
+                      "fp32_schedule": tg.fp32_schedule(nx, ny, nz)}))
 
 
 # ------------------------------------------------------ secondary workloads
@@ -690,8 +701,10 @@ def main():
     ap.add_argument("--ref-iterations", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--op-only", choices=["fp32", "fp64"], default=None,
-                    help="profiling aid: run only the fine operator (fea_matfree_apply) 3 times")
+    ap.add_argument("--op-only", choices=["fp32", "fp64", "l1tc"], default=None,
+                    help="profiling aid: three launches of one operator on a resident job")
+    ap.add_argument("--fp32-schedule", default=None,
+                    help="profiling aid: kind,shape,kz of the FP32 operator (tg_set_fp32_schedule)")
     ap.add_argument("--profile", action="store_true",
                     help="profiling aid: allow warmup < 3, skip e2e and the CPU baseline")
     ap.add_argument("--no-graph", action="store_true",
