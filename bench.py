@@ -73,7 +73,7 @@ def peaks():
 def committed_traffic(nx, ny, nz):
     """DRAM bytes per launch of the FP32 fine operator from the committed ncu
     capture of the same workload (profiles/), or None."""
-    path = os.path.join(ROOT, "profiles", f"fine_op_fp32_{nx}x{ny}x{nz}.txt")
+    path = os.path.join(ROOT, "profiles", f"fine_op_fp32_column_{nx}x{ny}x{nz}.txt")
     try:
         with open(path) as f:
             for line in f:
