@@ -34,6 +34,7 @@ from ._capi import (  # noqa: F401
     kernel_launches,
     set_fp32_schedule,
     set_level1_tc,
+    set_coarse_fused,
     APPLY_L1_STENCIL,
     APPLY_L1_TC,
     fp32_schedule,

@@ -203,6 +203,7 @@ def lib():
         "tg_device_fma_peaks": ([vp, vp], C.c_int),
         "tg_set_fp32_schedule": ([i32, i32, i32], C.c_int),
         "tg_set_level1_tc": ([i32], C.c_int),
+        "tg_set_coarse_fused": ([i32], C.c_int),
         "tg_job_check_level1": ([vp, vp], C.c_int),
         "tg_fp32_schedule": ([i32, i32, i32, vp, vp, vp], C.c_int),
     }
@@ -944,6 +945,13 @@ def set_level1_tc(on: bool):
     """Level 1 of the mixed V-cycle on the tensor cores (True, default) or as the
     assembled FP32 stencil (False), for solvers created afterwards."""
     _check(lib().tg_set_level1_tc(int(bool(on))))
+
+
+def set_coarse_fused(on: bool):
+    """The small levels of the mixed V-cycle (from the first of at most 4096
+    nodes to the coarsest) as one thread-block-cluster launch (True, default) or
+    a launch per step (False), for solvers created afterwards."""
+    _check(lib().tg_set_coarse_fused(int(bool(on))))
 
 
 def set_fp32_schedule(kind=None, shape=0, kz=32):

@@ -1956,6 +1956,10 @@ int tg_set_level1_tc(int32_t on) {
   return guarded([&] { set_level1_tc(on != 0); });
 }
 
+int tg_set_coarse_fused(int32_t on) {
+  return guarded([&] { set_coarse_fused(on != 0); });
+}
+
 int tg_set_fp32_schedule(int32_t kind, int32_t shape, int32_t kz) {
   return guarded([&] {
     if (kind < 0) {

@@ -30,6 +30,7 @@
 #include "tg_multigrid.h"
 
 #include <algorithm>
+#include <atomic>
 
 namespace tg {
 
@@ -278,22 +279,38 @@ __global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int6
 // stored forward block of a node whose neighbour lies outside the grid is zero,
 // and the backward term is selected away).  Per output the terms are summed in
 // a fixed order: the self block, then per j the forward and backward term.
-template <class T, int MODE>
-__global__ void __launch_bounds__(192) k_stencil_op(MgDims d, const T* __restrict__ A,
-                                                    const uint8_t* __restrict__ act,
-                                                    const T* __restrict__ x,
-                                                    const T* __restrict__ b,
-                                                    const T* __restrict__ invdiag, T omega,
-                                                    T* __restrict__ y, ChebStep ch) {
+// Loads of vectors another CTA may have written earlier in the same launch (the
+// fused coarse V-cycle) go through L2; elsewhere plain loads.
+template <class T, bool COH>
+__device__ __forceinline__ T vload(const T* p) {
+  if constexpr (COH)
+    return __ldcg(p);
+  else
+    return *p;
+}
+
+// Chebyshev direction update c0 * d_prev + c1 * res with one explicit rounding
+// pattern (the product c1 * res rounded, then one fused multiply-add), so every
+// kernel that takes the step produces the same bits.
+__device__ __forceinline__ float cheb_dir(float c0, float dprev, float c1, float res) {
+  return __fmaf_rn(c0, dprev, __fmul_rn(c1, res));
+}
+__device__ __forceinline__ double cheb_dir(double c0, double dprev, double c1, double res) {
+  return __fma_rn(c0, dprev, __dmul_rn(c1, res));
+}
+
+// Row r of node (a, bb, c) of a stored symmetric stencil times x, in the fixed
+// order: the self block, then per forward block j its forward and (transposed)
+// backward term.
+template <class T, bool COH>
+__device__ __forceinline__ T stencil_row(const MgDims& d, const T* __restrict__ A, const T* x,
+                                         int a, int bb, int c, int r) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   const int64_t sy = d.nnx, sz = int64_t(d.nnx) * d.nny;
-  // Block (32, 3, 2): x the node along x, y the component, z the node row along y.
-  const int a = blockIdx.x * 32 + threadIdx.x, r = threadIdx.y;
-  const int bb = blockIdx.y * 2 + threadIdx.z, c = blockIdx.z;
-  if (a >= d.nnx || bb >= d.nny) return;
   const int64_t n = c * sz + bb * sy + a;
   const T* An = A + n + int64_t(3 * r) * nn;  // row r of the self block
-  T s = An[0] * x[3 * n] + An[nn] * x[3 * n + 1] + An[2 * nn] * x[3 * n + 2];
+  T s = An[0] * vload<T, COH>(x + 3 * n) + An[nn] * vload<T, COH>(x + 3 * n + 1) +
+        An[2 * nn] * vload<T, COH>(x + 3 * n + 2);
 #pragma unroll
   for (int j = 1; j < 14; ++j) {
     const int di = 13 + j;
@@ -307,11 +324,36 @@ __global__ void __launch_bounds__(192) k_stencil_op(MgDims d, const T* __restric
     const int64_t p = bin ? n - off : n;
     const T* Af = An + int64_t(j * 9) * nn;
     const T* Ab = A + int64_t(j * 9 + r) * nn + p;
-    const T u = Af[0] * x[3 * m] + Af[nn] * x[3 * m + 1] + Af[2 * nn] * x[3 * m + 2];
-    const T v = Ab[0] * x[3 * p] + Ab[3 * nn] * x[3 * p + 1] + Ab[6 * nn] * x[3 * p + 2];
+    const T u = Af[0] * vload<T, COH>(x + 3 * m) + Af[nn] * vload<T, COH>(x + 3 * m + 1) +
+                Af[2 * nn] * vload<T, COH>(x + 3 * m + 2);
+    const T v = Ab[0] * vload<T, COH>(x + 3 * p) + Ab[3 * nn] * vload<T, COH>(x + 3 * p + 1) +
+                Ab[6 * nn] * vload<T, COH>(x + 3 * p + 2);
     s += fin ? u : T(0);
     s += bin ? v : T(0);
   }
+  return s;
+}
+
+constexpr int kStencilThreads = 192;
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(kStencilThreads) k_stencil_op(MgDims d, const T* __restrict__ A,
+                                                    const uint8_t* __restrict__ act,
+                                                    const T* __restrict__ x,
+                                                    const T* __restrict__ b,
+                                                    const T* __restrict__ invdiag, T omega,
+                                                    T* __restrict__ y, ChebStep ch) {
+  // 192 threads: two chunks of 32 consecutive nodes (in x-fastest order, across
+  // row ends) x 3 components, one component per warp, so a warp's stencil and
+  // vector reads are coalesced and no lane idles at the odd row lengths
+  // (2^k + 1 nodes) of the coarse levels.
+  const int64_t it = blockIdx.x * int64_t(kStencilThreads) + threadIdx.x;
+  const int64_t n = (it / 96) * 32 + (it & 31);
+  const int r = int((it / 32) % 3);
+  if (n >= int64_t(d.nnx) * d.nny * d.nnz) return;
+  const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny);
+  const int c = int(n / (int64_t(d.nnx) * d.nny));
+  const T s = stencil_row<T, false>(d, A, x, a, bb, c, r);
   const int64_t dof = 3 * n + r;
   T out;
   if (!act[dof]) {
@@ -322,21 +364,15 @@ __global__ void __launch_bounds__(192) k_stencil_op(MgDims d, const T* __restric
   } else if (MODE == kResidual) {
     out = b[dof] - s;
   } else if (MODE == kCheb) {
-    // Chebyshev step `ch.step` on [lmax / ratio, lmax] of D^-1 A (Saad,
-    // Iterative Methods, Alg. 12.1): d_k = rho_k rho_{k-1} d_{k-1} +
-    // (2 rho_k / delta) D^-1 (b - A x_k), d_0 = D^-1 (b - A x_0) / theta,
-    // x_{k+1} = x_k + d_k; rho_0 = delta / theta, rho_k = 1 / (2 theta / delta - rho_{k-1}).
-    const double lmax = ch.lam[0], lmin = lmax / ch.ratio;
-    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sig = theta / delta;
-    double rp = 1.0 / sig, rk = rp;
-    for (int i = 1; i <= ch.step; ++i) {
-      rp = rk;
-      rk = 1.0 / (2.0 * sig - rp);
-    }
+    // Chebyshev step `ch.step` (Saad, Iterative Methods, Alg. 12.1): d_k =
+    // rho_k rho_{k-1} d_{k-1} + (2 rho_k / delta) D^-1 (b - A x_k),
+    // d_0 = D^-1 (b - A x_0) / theta, x_{k+1} = x_k + d_k, with the step's
+    // coefficients from the level's table.
     const T res = invdiag[dof] * (b[dof] - s);
     T* dir = static_cast<T*>(ch.dir_);
-    const T dn = ch.step == 0 ? T(1.0 / theta) * res
-                              : T(rk * rp) * dir[dof] + T(2.0 * rk / delta) * res;
+    const float* cf = ch.coef;
+    const T dn = ch.step == 0 ? T(cf[0]) * res
+                              : cheb_dir(T(cf[2 * ch.step]), dir[dof], T(cf[2 * ch.step + 1]), res);
     dir[dof] = dn;
     out = x[dof] + dn;
   } else {
@@ -375,6 +411,29 @@ __global__ void k_pi_lambda(const double* __restrict__ nrm2, double safety,
   if (threadIdx.x == 0) lam[0] = safety * sqrt(nrm2[0] > 0.0 ? nrm2[0] : 1.0);
 }
 
+// Chebyshev coefficients on [lmax / ratio, lmax]: theta, delta the interval's
+// centre and half-width, rho_0 = delta / theta, rho_k = 1 / (2 theta / delta -
+// rho_{k-1}); thread k writes step k's pair.
+__global__ void k_cheb_table(const double* __restrict__ lam, double ratio, int m,
+                             float* __restrict__ coef) {
+  const int k = threadIdx.x;
+  if (k >= m) return;
+  const double lmax = lam[0], lmin = lmax / ratio;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sig = theta / delta;
+  double rp = 1.0 / sig, rk = rp;
+  for (int i = 1; i <= k; ++i) {
+    rp = rk;
+    rk = 1.0 / (2.0 * sig - rp);
+  }
+  if (k == 0) {
+    coef[0] = float(1.0 / theta);
+    coef[1] = 0.0f;
+  } else {
+    coef[2 * k] = float(rk * rp);
+    coef[2 * k + 1] = float(2.0 * rk / delta);
+  }
+}
+
 // x = omega * invdiag .* b (the first smoother sweep from a zero iterate).
 template <class T>
 __global__ void k_jacobi_first(const T* __restrict__ b, const T* __restrict__ invdiag, T omega,
@@ -400,13 +459,12 @@ __device__ __forceinline__ T axis_w(int i, int N, int d, int Ef, int align) {
 // 2N + delta, delta in {-1,0,1}^3, weight prod(1 or 1/2).  Inactive coarse DOFs
 // get 0; fine residuals are already 0 on inactive fine DOFs.  One thread per
 // coarse node on a 3D grid (x fastest), 32-bit index arithmetic.
-template <class T>
-__global__ void __launch_bounds__(256) k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
-                                                  const uint8_t* __restrict__ cact,
-                                                  T* __restrict__ bc) {
-  const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
-  if (a >= cd.nnx || b >= cd.nny) return;
-  T s0 = 0, s1 = 0, s2 = 0;
+// The restricted residual at coarse node (a, b, c): s[k] = sum of the (up to 27)
+// fine nodes' component k times their weights, in a fixed order.
+template <class T, bool COH>
+__device__ __forceinline__ void restrict_node(const MgDims& fd, const MgDims& cd, const T* rf,
+                                              int a, int b, int c, T (&s)[3]) {
+  s[0] = s[1] = s[2] = T(0);
 #pragma unroll
   for (int dz = -1; dz <= 1; ++dz) {
     const int k = 2 * c + dz;
@@ -423,29 +481,33 @@ __global__ void __launch_bounds__(256) k_restrict(MgDims fd, MgDims cd, const T*
         if (i < 0 || i >= fd.nnx) continue;
         const T w = axis_w<T>(i, a, dx, fd.ex, cd.align) * wy;
         const T* q = rf + 3 * ((int64_t(k) * fd.nny + j) * fd.nnx + i);
-        s0 += w * q[0];
-        s1 += w * q[1];
-        s2 += w * q[2];
+        s[0] += w * vload<T, COH>(q);
+        s[1] += w * vload<T, COH>(q + 1);
+        s[2] += w * vload<T, COH>(q + 2);
       }
     }
   }
-  const int64_t n = (int64_t(c) * cd.nny + b) * cd.nnx + a;
-  bc[3 * n] = cact[3 * n] ? s0 : T(0);
-  bc[3 * n + 1] = cact[3 * n + 1] ? s1 : T(0);
-  bc[3 * n + 2] = cact[3 * n + 2] ? s2 : T(0);
 }
 
-// Prolongation + correction: x_f += P e_c on active fine DOFs.  One thread per
-// fine node on a 3D grid.
 template <class T>
-__global__ void __launch_bounds__(256) k_prolong_add(MgDims fd, MgDims cd,
-                                                     const T* __restrict__ ec,
-                                                     const uint8_t* __restrict__ fact,
-                                                     T* __restrict__ xf) {
+__global__ void __launch_bounds__(256) k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
+                                                  const uint8_t* __restrict__ cact,
+                                                  T* __restrict__ bc) {
   const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
-  if (a >= fd.nnx || b >= fd.nny) return;
-  // Per axis: one coarse node (even fine node, or the aligned tail node) or two
-  // at weight 1/2.
+  if (a >= cd.nnx || b >= cd.nny) return;
+  T s[3];
+  restrict_node<T, false>(fd, cd, rf, a, b, c, s);
+  const int64_t n = (int64_t(c) * cd.nny + b) * cd.nnx + a;
+  bc[3 * n] = cact[3 * n] ? s[0] : T(0);
+  bc[3 * n + 1] = cact[3 * n + 1] ? s[1] : T(0);
+  bc[3 * n + 2] = cact[3 * n + 2] ? s[2] : T(0);
+}
+
+// The prolonged correction at fine node (a, b, c): per axis one coarse node
+// (an even fine node, or the aligned tail node) or two at weight 1/2.
+template <class T, bool COH>
+__device__ __forceinline__ void prolong_node(const MgDims& fd, const MgDims& cd, const T* ec,
+                                             int a, int b, int c, T (&s)[3]) {
   const bool ta = tail_node(a, fd.ex, cd.align), tb = tail_node(b, fd.ey, cd.align),
              tc = tail_node(c, fd.ez, cd.align);
   const int na = (a & 1) && !ta ? 2 : 1, nb = (b & 1) && !tb ? 2 : 1, ncz = (c & 1) && !tc ? 2 : 1;
@@ -453,7 +515,7 @@ __global__ void __launch_bounds__(256) k_prolong_add(MgDims fd, MgDims cd,
   const int ib0 = tb ? (b + 1) >> 1 : b >> 1, ib1 = (b + 1) >> 1;
   const int ic0 = tc ? (c + 1) >> 1 : c >> 1, ic1 = (c + 1) >> 1;
   const T w = (na == 2 ? T(0.5) : T(1)) * (nb == 2 ? T(0.5) : T(1)) * (ncz == 2 ? T(0.5) : T(1));
-  T s0 = 0, s1 = 0, s2 = 0;
+  s[0] = s[1] = s[2] = T(0);
 #pragma unroll
   for (int zz = 0; zz < 2; ++zz) {
     if (zz >= ncz) continue;
@@ -468,16 +530,29 @@ __global__ void __launch_bounds__(256) k_prolong_add(MgDims fd, MgDims cd,
         const int i = xx ? ia1 : ia0;
         if (i >= cd.nnx || j >= cd.nny || k >= cd.nnz) continue;
         const T* q = ec + 3 * ((int64_t(k) * cd.nny + j) * cd.nnx + i);
-        s0 += w * q[0];
-        s1 += w * q[1];
-        s2 += w * q[2];
+        s[0] += w * vload<T, COH>(q);
+        s[1] += w * vload<T, COH>(q + 1);
+        s[2] += w * vload<T, COH>(q + 2);
       }
     }
   }
+}
+
+// Prolongation + correction: x_f += P e_c on active fine DOFs.  One thread per
+// fine node on a 3D grid.
+template <class T>
+__global__ void __launch_bounds__(256) k_prolong_add(MgDims fd, MgDims cd,
+                                                     const T* __restrict__ ec,
+                                                     const uint8_t* __restrict__ fact,
+                                                     T* __restrict__ xf) {
+  const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
+  if (a >= fd.nnx || b >= fd.nny) return;
+  T s[3];
+  prolong_node<T, false>(fd, cd, ec, a, b, c, s);
   const int64_t n = (int64_t(c) * fd.nny + b) * fd.nnx + a;
-  if (fact[3 * n]) xf[3 * n] += s0;
-  if (fact[3 * n + 1]) xf[3 * n + 1] += s1;
-  if (fact[3 * n + 2]) xf[3 * n + 2] += s2;
+  if (fact[3 * n]) xf[3 * n] += s[0];
+  if (fact[3 * n + 1]) xf[3 * n + 1] += s[1];
+  if (fact[3 * n + 2]) xf[3 * n + 2] += s[2];
 }
 
 // ---------------------------------------------------------- coarsest solve
@@ -698,7 +773,9 @@ template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s,
                    ChebStep ch) {
-  const dim3 nb((d.nnx + 31) / 32, (d.nny + 1) / 2, d.nnz), nt(32, 3, 2);
+  const int64_t items = (int64_t(d.nnx) * d.nny * d.nnz + 31) / 32 * 96;
+  const unsigned nb = unsigned((items + kStencilThreads - 1) / kStencilThreads);
+  const unsigned nt = kStencilThreads;
   if (mode == kApply)
     k_stencil_op<T, kApply><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
   else if (mode == kResidual)
@@ -707,6 +784,12 @@ void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, co
     k_stencil_op<T, kCheb><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
   else
     k_stencil_op<T, kSmooth><<<nb, nt, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
+  TG_LAUNCH_CHECK();
+}
+
+void mg_cheb_table(const double* lam, double ratio, int m, float* coef, cudaStream_t s) {
+  if (m < 1 || 2 * m > kChebCoefStride) raise(TG_EINVAL, "Chebyshev degree out of range");
+  k_cheb_table<<<1, 32, 0, s>>>(lam, ratio, m, coef);
   TG_LAUNCH_CHECK();
 }
 
@@ -826,5 +909,245 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
 TG_INST(double)
 TG_INST(float)
 #undef TG_INST
+
+
+
+// ------------------------------------------------- fused coarse V-cycle
+// The small levels of the FP32 V-cycle -- from the first level with at most
+// kFusedMaxNodes nodes down to the coarsest -- in one launch of one thread-block
+// cluster.  Launch by launch, each step on these levels is a kernel of a few
+// thousand DOFs whose cost is its launch latency (about 7 us per step inside the
+// inner PCG's graph; levels 3..6 of the 256x128x128 cantilever took ~270 us per
+// V-cycle).  Here every step of the same V-cycle is a phase of one kernel -- a
+// cluster-stride loop with the arithmetic and summation order of the separate
+// kernels (stencil_row, restrict_node, prolong_node, the coarsest inverse) --
+// and phases are separated by the cluster's hardware barrier (release/acquire
+// at cluster scope, no spin loop).  The restriction into a level and that
+// level's first smoothing step (from a zero iterate, so it needs no operator)
+// share a phase.  Vectors written in earlier phases are read through L2
+// (another SM of the cluster may have written them).  The iterate ping-pongs
+// between each level's two buffers exactly as the launch-by-launch V-cycle does.
+namespace {
+
+// Every thread of the cluster arrives; writes before the barrier (global and
+// shared memory) are visible to every thread of the cluster after it.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Work items of a per-DOF phase: chunks of 32 nodes x 3 components, one
+// component per warp, so a warp's stencil reads are coalesced.
+__device__ __forceinline__ void dof_item(int64_t it, const MgDims& d, int& a, int& b, int& c,
+                                         int& r, int64_t& n) {
+  const int64_t chunk = it / 96;
+  r = int((it / 32) % 3);
+  n = chunk * 32 + (it & 31);
+  a = int(n % d.nnx);
+  b = int((n / d.nnx) % d.nny);
+  c = int(n / (int64_t(d.nnx) * d.nny));
+}
+
+__global__ void __launch_bounds__(kFusedThreads, 1) k_coarse_vcycle(FusedCoarse fc) {
+  const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int64_t nthreads = int64_t(gridDim.x) * blockDim.x;
+  const int top = fc.nlev - 1;  // the coarsest
+  int cur[kFusedMaxLevels] = {};  // 0: the iterate is in xp, 1: in xq
+  auto X = [&](int i) { return cur[i] ? fc.L[i].xq : fc.L[i].xp; };
+  auto O = [&](int i) { return cur[i] ? fc.L[i].xp : fc.L[i].xq; };
+  auto nitems = [&](int i) { return ((int64_t(fc.L[i].d.nnx) * fc.L[i].d.nny * fc.L[i].d.nnz + 31) / 32) * 96; };
+
+  // One smoothing step of level i from its current iterate (or from zero) into
+  // the other buffer: Chebyshev step k, or damped Jacobi (whose first sweep from
+  // zero writes the iterate's own buffer, as the separate launches do).
+  auto smooth = [&](int i, int k, bool from_zero) {
+    const FusedLevel& L = fc.L[i];
+    const float* xin = X(i);
+    const bool in_place = from_zero && fc.cheb_m == 0;
+    float* xout = in_place ? X(i) : O(i);
+    const int64_t ni = nitems(i), nn = int64_t(L.d.nnx) * L.d.nny * L.d.nnz;
+    for (int64_t it = tid; it < ni; it += nthreads) {
+      int a, b, c, r;
+      int64_t n;
+      dof_item(it, L.d, a, b, c, r, n);
+      if (n >= nn) continue;
+      const int64_t dof = 3 * n + r;
+      const float s = from_zero ? 0.0f : stencil_row<float, true>(L.d, L.A, xin, a, b, c, r);
+      const float xv = from_zero ? 0.0f : __ldcg(xin + dof);
+      float out;
+      if (!L.act[dof]) {
+        out = 0.0f;
+        if (fc.cheb_m > 0) L.chd[dof] = 0.0f;
+      } else if (fc.cheb_m > 0) {
+        const float res = L.dinv[dof] * (__ldcg(L.b + dof) - s);
+        const float dn = k == 0 ? L.coef[0] * res
+                                : cheb_dir(L.coef[2 * k], __ldcg(L.chd + dof), L.coef[2 * k + 1],
+                                           res);
+        L.chd[dof] = dn;
+        out = xv + dn;
+      } else {
+        out = xv + fc.omega * L.dinv[dof] * (__ldcg(L.b + dof) - s);
+      }
+      xout[dof] = out;
+    }
+    if (!in_place) cur[i] ^= 1;
+  };
+  // r = b - A x of level i into its other buffer (the iterate stays).
+  auto residual = [&](int i) {
+    const FusedLevel& L = fc.L[i];
+    const float* xin = X(i);
+    float* rout = O(i);
+    const int64_t ni = nitems(i), nn = int64_t(L.d.nnx) * L.d.nny * L.d.nnz;
+    for (int64_t it = tid; it < ni; it += nthreads) {
+      int a, b, c, r;
+      int64_t n;
+      dof_item(it, L.d, a, b, c, r, n);
+      if (n >= nn) continue;
+      const int64_t dof = 3 * n + r;
+      const float s = stencil_row<float, true>(L.d, L.A, xin, a, b, c, r);
+      rout[dof] = L.act[dof] ? __ldcg(L.b + dof) - s : 0.0f;
+    }
+  };
+  // Level i's residual restricted into level i + 1's right-hand side, and --
+  // for a smoothed level -- its first smoothing step from zero, per DOF.
+  auto restrict_to = [&](int i) {
+    const FusedLevel& F = fc.L[i];
+    const FusedLevel& C = fc.L[i + 1];
+    const float* rf = O(i);
+    const bool smoothed = i + 1 < top;
+    const int64_t nn = int64_t(C.d.nnx) * C.d.nny * C.d.nnz;
+    float* xfirst = C.xq;  // Chebyshev step 0 writes the other buffer (x = 0 in xp)
+    if (smoothed && fc.cheb_m == 0) xfirst = C.xp;  // Jacobi's first sweep writes the iterate
+    for (int64_t n = tid; n < nn; n += nthreads) {
+      const int a = int(n % C.d.nnx), b = int((n / C.d.nnx) % C.d.nny),
+                c = int(n / (int64_t(C.d.nnx) * C.d.nny));
+      float s[3];
+      restrict_node<float, true>(F.d, C.d, rf, a, b, c, s);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int64_t dof = 3 * n + k;
+        const float bv = C.act[dof] ? s[k] : 0.0f;
+        C.b[dof] = bv;
+        if (!smoothed) continue;
+        if (fc.cheb_m > 0) {
+          const float dn = C.act[dof] ? C.coef[0] * (C.dinv[dof] * (bv - 0.0f)) : 0.0f;
+          C.chd[dof] = dn;
+          xfirst[dof] = C.act[dof] ? 0.0f + dn : 0.0f;
+        } else {
+          xfirst[dof] = fc.omega * C.dinv[dof] * bv;
+        }
+      }
+    }
+    if (smoothed && fc.cheb_m > 0) cur[i + 1] = 1;
+  };
+  auto prolong_from = [&](int i) {  // level i's iterate += P (level i + 1's iterate)
+    const FusedLevel& F = fc.L[i];
+    const FusedLevel& C = fc.L[i + 1];
+    const float* ec = X(i + 1);
+    float* xf = X(i);
+    const int64_t nn = int64_t(F.d.nnx) * F.d.nny * F.d.nnz;
+    for (int64_t n = tid; n < nn; n += nthreads) {
+      const int a = int(n % F.d.nnx), b = int((n / F.d.nnx) % F.d.nny),
+                c = int(n / (int64_t(F.d.nnx) * F.d.nny));
+      float s[3];
+      prolong_node<float, true>(F.d, C.d, ec, a, b, c, s);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (F.act[3 * n + k]) xf[3 * n + k] = __ldcg(xf + 3 * n + k) + s[k];
+    }
+  };
+  auto coarsest = [&]() {  // x = A^-1 b over the compact numbering, a warp per row
+    const FusedLevel& L = fc.L[top];
+    const int64_t ndof = 3 * int64_t(L.d.nnx) * L.d.nny * L.d.nnz;
+    for (int64_t dd = tid; dd < ndof; dd += nthreads)
+      if (fc.cidx[dd] < 0) L.xp[dd] = 0.0f;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = tid >> 5, nwarps = nthreads >> 5;
+    for (int64_t row = warp; row < fc.nc; row += nwarps) {
+      double s = 0.0;
+      for (int k = lane; k < fc.nc; k += 32)
+        s += fc.Ainv[row * fc.nc + k] * double(__ldcg(L.b + fc.cdof[k]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) L.xp[fc.cdof[row]] = float(s);
+    }
+    cur[top] = 0;
+  };
+
+  // Down: level 0's first step from zero (its right-hand side came from level 1).
+  smooth(0, 0, true);
+  cluster_sync_all();
+  for (int i = 0; i < top; ++i) {
+    const int steps = fc.cheb_m > 0 ? fc.cheb_m : fc.sweeps;
+    for (int k = 1; k < steps; ++k) {
+      smooth(i, k, false);
+      cluster_sync_all();
+    }
+    residual(i);
+    cluster_sync_all();
+    restrict_to(i);
+    cluster_sync_all();
+  }
+  coarsest();
+  for (int i = top - 1; i >= 0; --i) {
+    cluster_sync_all();
+    prolong_from(i);
+    const int steps = fc.cheb_m > 0 ? fc.cheb_m : fc.sweeps;
+    for (int k = 0; k < steps; ++k) {
+      cluster_sync_all();
+      smooth(i, k, false);
+    }
+  }
+}
+
+}  // namespace
+
+// Cluster size of the fused launch: the largest of 16 (non-portable), 8, 4, 2
+// CTAs that the device can co-schedule with this kernel's resources.
+int fused_coarse_blocks() {
+  static std::atomic<int> cached{0};
+  const int c = cached.load();
+  if (c > 0) return c;
+  TG_CUDA(cudaFuncSetAttribute(k_coarse_vcycle, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  int best = 1;
+  for (int cs : {16, 8, 4, 2}) {
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = unsigned(cs);
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(unsigned(cs));
+    cfg.blockDim = dim3(kFusedThreads);
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_coarse_vcycle, &cfg) == cudaSuccess && n >= 1) {
+      best = cs;
+      break;
+    }
+    cudaGetLastError();  // an unsupported size is not an error of the solve
+  }
+  cached.store(best);
+  return best;
+}
+
+void mg_coarse_vcycle_fused(const FusedCoarse& fc, cudaStream_t s) {
+  const int cs = fused_coarse_blocks();
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = unsigned(cs);
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(unsigned(cs));
+  cfg.blockDim = dim3(kFusedThreads);
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  TG_CUDA(cudaLaunchKernelEx(&cfg, k_coarse_vcycle, fc));
+  note_launch();
+}
 
 }  // namespace tg

@@ -395,7 +395,7 @@ size_t Solver::device_bytes() const {
   for (const DBuf<float>* d : {&Ef_, &invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_})
     b += d->bytes();
   for (const auto& L : levels_) b += L->bytes();
-  b += spos1_.bytes() + slist1_.bytes() + yspec1_.bytes() + tc_err_.bytes();
+  b += spos1_.bytes() + slist1_.bytes() + yspec1_.bytes() + tc_err_.bytes() + chc_.bytes();
   return b + cidx_.bytes() + kebf_.bytes() + Gf_.bytes();
 }
 
@@ -569,6 +569,19 @@ void Solver::build_structure() {
     }
     tc_err_.alloc(1);
     TG_CUDA(cudaMemsetAsync(tc_err_.p, 0, sizeof(int), s_));
+  }
+  // The small levels (from the first one of at most kFusedMaxNodes nodes, below
+  // level 1) in one cluster launch, when at least one of them is smoothed and
+  // the coarsest has the explicit inverse.
+  fused_level_ = 0;
+  if (mixed_ && coarse_fused_enabled() && chol_inv_.p != nullptr) {
+    for (size_t l = 2; l < levels_.size(); ++l) {
+      const MgDims& d = levels_[l - 1]->d;
+      if (int64_t(d.nnx) * d.nny * d.nnz <= kFusedMaxNodes) {
+        if (levels_.size() - (l - 1) <= size_t(kFusedMaxLevels)) fused_level_ = l;
+        break;
+      }
+    }
   }
   TG_CUDA(cudaStreamSynchronize(s_));
   have_mg_ = true;
@@ -765,6 +778,7 @@ bool Solver::build_numeric() {
   if (sizeof(T) == 4 && cheb_m_ > 0) {
     // lambda_max(D^-1 A) of every smoothed level >= 2 for its Chebyshev smoother.
     if (!lam_.p) lam_.alloc(levels_.size() + 1);
+    if (!chc_.p) chc_.alloc(kChebCoefStride * (levels_.size() + 1));
     if (!pi_.p) pi_.alloc(1);
     for (size_t li = 1; li + 1 < levels_.size(); ++li) {
       Level& L = *levels_[li];
@@ -772,6 +786,7 @@ bool Solver::build_numeric() {
       mg_lambda_max<float>(L.d, L.Am<float>(), L.act.p, L.Dinv<float>(), L.X<float>(),
                            L.R<float>(), cheb_iters_, cheb_safety_, part_.p, pi_.p,
                            lam_.p + li, s_);
+      mg_cheb_table(lam_.p + li, cheb_ratio_, cheb_m_, chc_.p + kChebCoefStride * li, s_);
     }
   }
   Level& C = *levels_.back();
@@ -788,14 +803,17 @@ bool Solver::build_numeric() {
 
 // ------------------------------------------------------------------ V-cycle
 template <class T>
-void Solver::vcycle_level(size_t l) {
+T* Solver::vcycle_level(size_t l) {
   Level& L = *levels_[l - 1];
   if (l == levels_.size()) {
     if (chol_inv_.p)
       mg_coarse_inv_apply<T>(chol_inv_.p, nc_, cidx_.p, cdof_.p, L.ndof, L.B<T>(), L.X<T>(), s_);
     else
       mg_chol_solve<T>(chol_.p, nc_, cidx_.p, L.ndof, L.B<T>(), L.X<T>(), chol_work_.p, s_);
-    return;
+    return L.X<T>();
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (l == fused_level_) return reinterpret_cast<T*>(fused_coarse_vcycle());
   }
   Level& N = *levels_[l];
   const T w = T(omega_);
@@ -812,7 +830,7 @@ void Solver::vcycle_level(size_t l) {
   if (sizeof(T) == 4 && cheb_m_ > 0 && l >= 2) {
     // Mixed form, levels >= 2: a degree-cheb_m_ Chebyshev polynomial in D^-1 A
     // before (from a zero iterate) and after the coarse correction.
-    ChebStep ch{L.chd.p, lam_.p + (l - 1), cheb_ratio_, 0};
+    ChebStep ch{L.chd.p, chc_.p + kChebCoefStride * (l - 1), 0};
     auto cheb = [&] {
       for (int k = 0; k < cheb_m_; ++k) {
         ch.step = k;
@@ -825,10 +843,10 @@ void Solver::vcycle_level(size_t l) {
     cheb();
     op(kResidual);
     mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
-    vcycle_level<T>(l + 1);
-    mg_prolong_add<T>(L.d, N.d, N.X<T>(), L.act.p, L.X<T>(), s_);
+    T* ec = vcycle_level<T>(l + 1);
+    mg_prolong_add<T>(L.d, N.d, ec, L.act.p, L.X<T>(), s_);
     cheb();
-    return;
+    return L.X<T>();
   }
   // sweeps_ damped-Jacobi sweeps on each side (the first from a zero iterate);
   // every sweep leaves the iterate in X.
@@ -839,12 +857,46 @@ void Solver::vcycle_level(size_t l) {
   }
   op(kResidual);
   mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
-  vcycle_level<T>(l + 1);
-  mg_prolong_add<T>(L.d, N.d, N.X<T>(), L.act.p, L.X<T>(), s_);
+  T* ec = vcycle_level<T>(l + 1);
+  mg_prolong_add<T>(L.d, N.d, ec, L.act.p, L.X<T>(), s_);
   for (int k = 0; k < sweeps_; ++k) {
     op(kSmooth);
     std::swap(L.X<T>(), L.R<T>());
   }
+  return L.X<T>();
+}
+
+// Levels fused_level_ .. coarsest of the FP32 V-cycle as one cluster launch;
+// returns the buffer that holds level fused_level_'s result (the launch-by-launch
+// V-cycle leaves it in the same one).
+float* Solver::fused_coarse_vcycle() {
+  FusedCoarse fc;
+  const size_t first = fused_level_ - 1;  // levels_ index of the first fused level
+  fc.nlev = int(levels_.size() - first);
+  for (int i = 0; i < fc.nlev; ++i) {
+    Level& L = *levels_[first + size_t(i)];
+    FusedLevel& F = fc.L[i];
+    F.d = L.d;
+    F.A = L.Am<float>();
+    F.act = L.act.p;
+    F.dinv = L.Dinv<float>();
+    F.xp = L.X<float>();
+    F.xq = L.R<float>();
+    F.b = L.B<float>();
+    F.chd = L.chd.p;
+    F.coef = chc_.p ? chc_.p + kChebCoefStride * (first + size_t(i)) : nullptr;
+  }
+  fc.cheb_m = cheb_m_;
+  fc.sweeps = sweeps_;
+  fc.omega = float(omega_);
+  fc.Ainv = chol_inv_.p;
+  fc.nc = nc_;
+  fc.cidx = cidx_.p;
+  fc.cdof = cdof_.p;
+  mg_coarse_vcycle_fused(fc, s_);
+  // Chebyshev: 2 cheb_m toggles per level (even); Jacobi: the first sweep in
+  // place, then 2 sweeps - 1 toggles (odd).
+  return cheb_m_ > 0 ? fc.L[0].xp : fc.L[0].xq;
 }
 
 template <>
@@ -864,8 +916,8 @@ double* Solver::vcycle<double>(const double* b) {
   launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
                          nullptr, nullptr, s_);
   mg_restrict<double>(fd, N.d, r, N.act.p, N.B<double>(), s_);
-  vcycle_level<double>(1);
-  mg_prolong_add<double>(fd, N.d, N.X<double>(), fp_.kept.p, x, s_);
+  double* ec = vcycle_level<double>(1);
+  mg_prolong_add<double>(fd, N.d, ec, fp_.kept.p, x, s_);
   for (int k = 0; k < sweeps_; ++k) smooth();
   fine_matvecs_ += 2 * sweeps_;
   return x;
@@ -889,8 +941,8 @@ float* Solver::vcycle<float>(const float* b) {
   launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
                         nullptr, s_, fp_.kept_node.p);
   mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_);
-  vcycle_level<float>(1);
-  mg_prolong_add<float>(fd, N.d, N.X<float>(), fp_.kept.p, x, s_);
+  float* ec = vcycle_level<float>(1);
+  mg_prolong_add<float>(fd, N.d, ec, fp_.kept.p, x, s_);
   for (int k = 0; k < sweeps_; ++k) smooth();
   lowp_matvecs_ += 2 * sweeps_;
   return x;

@@ -196,6 +196,11 @@ FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const 
 // cores (k_coarse_tc.cu) instead of the assembled FP32 stencil; on by default.
 bool level1_tc_enabled();
 void set_level1_tc(bool on);
+// Whether the mixed form's V-cycle runs its small levels (from the first one of
+// at most kFusedMaxNodes nodes to the coarsest) as one cluster launch
+// (k_multigrid.cu) instead of a launch per step; on by default.
+bool coarse_fused_enabled();
+void set_coarse_fused(bool on);
 // Batched apply on the periodic nx*ny*nz torus (nodes = elements per axis); see
 // k_operator.cu.
 template <class T>

@@ -36,12 +36,21 @@ void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s);
 // One Chebyshev smoothing step (kCheb): the direction vector it updates in
 // place (the level's precision), lambda_max of D^-1 A on the device, the
 // interval ratio lmax / lmin and the step index within the polynomial.
+// One Chebyshev smoothing step: the direction buffer and the level's
+// coefficient table (mg_cheb_table).
 struct ChebStep {
   void* dir_ = nullptr;
-  const double* lam = nullptr;
-  double ratio = 0.0;
+  const float* coef = nullptr;
   int step = 0;
 };
+// Chebyshev coefficients of steps 0 .. m-1 on [lam/ratio, lam] (lam = *lam on
+// the device) into coef[0 .. 2m): coef[0] = 1/theta, coef[2k], coef[2k+1] =
+// rho_k rho_{k-1}, 2 rho_k / delta for k >= 1, each rounded to FP32 once.
+// Computed once per hierarchy build: the smoothing kernels read them instead of
+// evaluating the FP64 recurrence in every thread (GB300's FP64 rate is 1/64 of
+// its FP32 rate).
+constexpr int kChebCoefStride = 8;
+void mg_cheb_table(const double* lam, double ratio, int m, float* coef, cudaStream_t s);
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s,
@@ -73,6 +82,44 @@ void mg_coarse_inv_apply(const double* Ainv, int nc, const int* cidx, const int*
 template <class T>
 void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const T* b, T* x,
                    double* work, cudaStream_t s);
+
+// The small levels of the FP32 V-cycle in one launch of one thread-block cluster
+// (k_multigrid.cu).  L[0] is the first fused level (its right-hand side b set by
+// the finer level's restriction), L[nlev-1] the coarsest (solved with the dense
+// inverse Ainv over the compact numbering cidx/cdof).  Each smoothed level has
+// two iterate buffers: xp (the iterate on entry, as the launch-by-launch
+// V-cycle's X) and xq; smoothing is Chebyshev of degree cheb_m (> 0, direction
+// chd, coefficient table coef on the device) or damped Jacobi with `sweeps` sweeps per
+// side.  The fused part starts at the first level with at most kFusedMaxNodes
+// nodes: a cluster of kFusedThreads-thread CTAs covers a few DOFs per thread.
+constexpr int kFusedMaxLevels = 12;
+constexpr int64_t kFusedMaxNodes = 4096;
+constexpr int kFusedThreads = 512;
+struct FusedLevel {
+  MgDims d;
+  const float* A = nullptr;
+  const uint8_t* act = nullptr;
+  const float* dinv = nullptr;
+  float* xp = nullptr;
+  float* xq = nullptr;
+  float* b = nullptr;
+  float* chd = nullptr;
+  const float* coef = nullptr;  // Chebyshev coefficients (mg_cheb_table)
+};
+struct FusedCoarse {
+  int nlev = 0;
+  FusedLevel L[kFusedMaxLevels];
+  int cheb_m = 0, sweeps = 1;
+  float omega = 0.6f;
+  const double* Ainv = nullptr;
+  int nc = 0;
+  const int* cidx = nullptr;
+  const int* cdof = nullptr;
+};
+// CTAs in the fused launch's cluster (16 where the device co-schedules that
+// many, else 8, 4, 2, 1).
+int fused_coarse_blocks();
+void mg_coarse_vcycle_fused(const FusedCoarse& fc, cudaStream_t s);
 
 // The FP32 level-1 Galerkin operator on the tensor cores (k_coarse_tc.cu):
 // y = A1 x (kApply), b - A1 x (kResidual) or x + omega D^-1 (b - A1 x) (kSmooth),

@@ -90,7 +90,8 @@ class Solver {
   template <class T>
   T* vcycle(const T* b);
   template <class T>
-  void vcycle_level(size_t l);
+  T* vcycle_level(size_t l);  // returns the buffer holding the level's result
+  float* fused_coarse_vcycle();
   template <class T>
   bool inner_pcg(int max_it, double rel_tol, SolverStats& st, int* iters);
   bool build_inner_graph();
@@ -113,6 +114,7 @@ class Solver {
   int cheb_iters_ = 10;
   double cheb_safety_ = 1.1;
   DBuf<double> lam_, pi_;  // lambda_max per level; the power iteration's norm
+  DBuf<float> chc_;        // Chebyshev coefficients per level (kChebCoefStride each)
   void refinement_residual();  // r = b - A x (FP64 in, FP64 out) for the mixed loop
   bool mixed_ = false;
   // fine state
@@ -147,7 +149,9 @@ class Solver {
   int nspec1_ = 0;
   DBuf<int> spos1_, slist1_;  // per coarse element: position in slist1_ or -1
   DBuf<float> yspec1_;        // their outputs, nspec1_ x 24
-  DBuf<int> tc_err_;
+  DBuf<int> tc_err_;  // a tensor-core completion wait that ran out
+  // The small levels of the FP32 V-cycle in one cluster launch.
+  size_t fused_level_ = 0;  // first level of the fused cluster launch (0: none)
   void level1_op(int mode, Level& L, float omega);
   int* h_ist_ = nullptr;       // pinned mirror of istate_
 };

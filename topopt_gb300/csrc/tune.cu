@@ -108,5 +108,10 @@ std::atomic<bool> g_level1_tc{true};
 }
 bool level1_tc_enabled() { return g_level1_tc.load(); }
 void set_level1_tc(bool on) { g_level1_tc.store(on); }
+namespace {
+std::atomic<bool> g_coarse_fused{true};
+}
+bool coarse_fused_enabled() { return g_coarse_fused.load(); }
+void set_coarse_fused(bool on) { g_coarse_fused.store(on); }
 
 }  // namespace tg
