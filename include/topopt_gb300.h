@@ -720,10 +720,10 @@ int64_t tg_kernel_launches(void);
  * created afterwards. */
 int tg_set_level1_tc(int32_t on);
 /* The mixed form's V-cycle on its small levels (below level 1, from the first
- * level of at most 4096 nodes to the coarsest): on (default) they run as one
- * launch of one thread-block cluster with the cluster barrier between steps;
- * off, as a launch per step.  Same arithmetic either way.  Applies to solvers
- * created afterwards. */
+ * level of at most 4096 nodes to the coarsest): on, they run as one launch of
+ * one thread-block cluster with the cluster barrier between steps; off
+ * (default), as a launch per step, which measured faster on GB300.  Same
+ * arithmetic either way.  Applies to solvers created afterwards. */
 int tg_set_coarse_fused(int32_t on);
 /* Schedule of the FP32 fine operator (the mixed form's fine level).  kind 0:
  * the pencil kernel; kind 1: the column-blocked kernel with tile shape `shape`

@@ -33,7 +33,7 @@ def test_fused_coarse_vcycle_bit_identical(tg, dims):
             assert info.converged and not info.mixed_fallback, (on, info)
             out[on] = (u, info.iterations, tg.kernel_launches() - k0)
     finally:
-        tg.set_coarse_fused(True)
+        tg.set_coarse_fused(False)
     assert out[True][1] == out[False][1]
     assert out[True][2] < out[False][2], (out[True][2], out[False][2])
     assert np.array_equal(out[True][0], out[False][0])
@@ -50,5 +50,5 @@ def test_fused_coarse_vcycle_design_run(tg):
                 cg_tolerance=1e-8, solve=tg.SolveOptions(precision=tg.PREC_MIXED)))
             hist[on] = [h["compliance"] for h in s["history"]]
     finally:
-        tg.set_coarse_fused(True)
+        tg.set_coarse_fused(False)
     assert hist[True] == hist[False]

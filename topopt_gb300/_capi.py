@@ -949,8 +949,8 @@ def set_level1_tc(on: bool):
 
 def set_coarse_fused(on: bool):
     """The small levels of the mixed V-cycle (from the first of at most 4096
-    nodes to the coarsest) as one thread-block-cluster launch (True, default) or
-    a launch per step (False), for solvers created afterwards."""
+    nodes to the coarsest) as one thread-block-cluster launch (True) or a launch
+    per step (False, default), for solvers created afterwards."""
     _check(lib().tg_set_coarse_fused(int(bool(on))))
 
 

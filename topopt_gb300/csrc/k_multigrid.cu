@@ -42,6 +42,24 @@ int nblk(int64_t n, int t = kThreads) {
   return int(b < 152 * 64 ? (b > 0 ? b : 1) : 152 * 64);
 }
 
+// Coordinates (a, b, c) of linear node index n of a level: 32-bit unsigned
+// division whenever the index fits (every coarse level; a 64-bit division is a
+// long dependent instruction sequence that small, latency-bound kernels pay on
+// every item).
+__device__ __forceinline__ void node_abc(const MgDims& d, int64_t n, int& a, int& b, int& c) {
+  if (n <= int64_t(0xffffffffu)) {
+    const unsigned un = unsigned(n), nx = unsigned(d.nnx), ny = unsigned(d.nny);
+    const unsigned q = un / nx, r = q / ny;
+    a = int(un - q * nx);
+    b = int(q - r * ny);
+    c = int(r);
+  } else {
+    a = int(n % d.nnx);
+    b = int((n / d.nnx) % d.nny);
+    c = int(n / (int64_t(d.nnx) * d.nny));
+  }
+}
+
 // Local corner index -> offsets; corners in Walsh bit order (x | y<<1 | z<<2).
 __device__ __forceinline__ int cx(int c) { return c & 1; }
 __device__ __forceinline__ int cy(int c) { return (c >> 1) & 1; }
@@ -212,7 +230,8 @@ __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
        n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % d.nnx), b = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
+    int a, b, c;
+    node_abc(d, n, a, b, c);
     bool ra[3];
     for (int k = 0; k < 3; ++k) ra[k] = act[3 * n + k] != 0;
     for (int dz = -1; dz <= 1; ++dz)
@@ -299,20 +318,37 @@ __device__ __forceinline__ double cheb_dir(double c0, double dprev, double c1, d
   return __fma_rn(c0, dprev, __dmul_rn(c1, res));
 }
 
-// Row r of node (a, bb, c) of a stored symmetric stencil times x, in the fixed
-// order: the self block, then per forward block j its forward and (transposed)
-// backward term.
+// u = a0 x0 + a1 x1 + a2 x2 with one rounding pattern (a product, then two
+// fused multiply-adds) in every kernel that evaluates a stencil term.
+__device__ __forceinline__ float dot3(float a0, float x0, float a1, float x1, float a2, float x2) {
+  return __fmaf_rn(a2, x2, __fmaf_rn(a1, x1, __fmul_rn(a0, x0)));
+}
+__device__ __forceinline__ double dot3(double a0, double x0, double a1, double x1, double a2,
+                                       double x2) {
+  return __fma_rn(a2, x2, __fma_rn(a1, x1, __dmul_rn(a0, x0)));
+}
+
+// Part `part` (0..3) of row r of node (a, bb, c) of a stored symmetric stencil
+// times x.  The row is the self block (term 0) plus, for j = 1..13, forward
+// block j (neighbour n + off_j) and the transposed forward block of neighbour
+// n - off_j; part q sums the terms j = q, q + 4, ... in increasing j (part 0
+// starts from the self term), and the row is ((p0 + p1) + p2) + p3.  Four
+// parts let four threads share a row on the small levels, where a row's ~160
+// loads in one thread are a chain of dependent memory round trips.
 template <class T, bool COH>
-__device__ __forceinline__ T stencil_row(const MgDims& d, const T* __restrict__ A, const T* x,
-                                         int a, int bb, int c, int r) {
+__device__ __forceinline__ T stencil_part(const MgDims& d, const T* __restrict__ A, const T* x,
+                                          int a, int bb, int c, int r, int part) {
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   const int64_t sy = d.nnx, sz = int64_t(d.nnx) * d.nny;
   const int64_t n = c * sz + bb * sy + a;
   const T* An = A + n + int64_t(3 * r) * nn;  // row r of the self block
-  T s = An[0] * vload<T, COH>(x + 3 * n) + An[nn] * vload<T, COH>(x + 3 * n + 1) +
-        An[2 * nn] * vload<T, COH>(x + 3 * n + 2);
+  T s = T(0);
+  if (part == 0)
+    s = dot3(An[0], vload<T, COH>(x + 3 * n), An[nn], vload<T, COH>(x + 3 * n + 1), An[2 * nn],
+             vload<T, COH>(x + 3 * n + 2));
 #pragma unroll
   for (int j = 1; j < 14; ++j) {
+    if ((j & 3) != part) continue;
     const int di = 13 + j;
     const int dx = di % 3 - 1, dy = (di / 3) % 3 - 1, dz = di / 9 - 1;
     const int64_t off = dz * sz + dy * sy + dx;
@@ -324,14 +360,49 @@ __device__ __forceinline__ T stencil_row(const MgDims& d, const T* __restrict__ 
     const int64_t p = bin ? n - off : n;
     const T* Af = An + int64_t(j * 9) * nn;
     const T* Ab = A + int64_t(j * 9 + r) * nn + p;
-    const T u = Af[0] * vload<T, COH>(x + 3 * m) + Af[nn] * vload<T, COH>(x + 3 * m + 1) +
-                Af[2 * nn] * vload<T, COH>(x + 3 * m + 2);
-    const T v = Ab[0] * vload<T, COH>(x + 3 * p) + Ab[3 * nn] * vload<T, COH>(x + 3 * p + 1) +
-                Ab[6 * nn] * vload<T, COH>(x + 3 * p + 2);
+    const T u = dot3(Af[0], vload<T, COH>(x + 3 * m), Af[nn], vload<T, COH>(x + 3 * m + 1),
+                     Af[2 * nn], vload<T, COH>(x + 3 * m + 2));
+    const T v = dot3(Ab[0], vload<T, COH>(x + 3 * p), Ab[3 * nn], vload<T, COH>(x + 3 * p + 1),
+                     Ab[6 * nn], vload<T, COH>(x + 3 * p + 2));
     s += fin ? u : T(0);
     s += bin ? v : T(0);
   }
   return s;
+}
+
+// Row r of node (a, bb, c) of the stencil times x: the four parts in order.
+template <class T, bool COH>
+__device__ __forceinline__ T stencil_row(const MgDims& d, const T* __restrict__ A, const T* x,
+                                         int a, int bb, int c, int r) {
+  T p[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) p[q] = stencil_part<T, COH>(d, A, x, a, bb, c, r, q);
+  return ((p[0] + p[1]) + p[2]) + p[3];
+}
+
+// The per-DOF update of the stencil kernels from the row sum s, in one
+// rounding pattern: kApply s, kResidual b - s, kSmooth x + (omega dinv)(b - s),
+// kCheb the Chebyshev step (direction dprev of the previous step, coefficients
+// of the level's table); inactive DOFs 0 (and a zero direction).
+template <class T, int MODE>
+__device__ __forceinline__ T stencil_update(bool active, T s, T xv, T bv, T dv, T omega,
+                                            const float* cf, int step, T dprev, T& dnew) {
+  dnew = T(0);
+  if (!active) return T(0);
+  if (MODE == kApply) return s;
+  if (MODE == kResidual) return bv - s;
+  if (MODE == kCheb) {
+    // Chebyshev step (Saad, Iterative Methods, Alg. 12.1): d_k = rho_k rho_{k-1}
+    // d_{k-1} + (2 rho_k / delta) D^-1 (b - A x_k), d_0 = D^-1 (b - A x_0) / theta,
+    // x_{k+1} = x_k + d_k.
+    const T res = dv * (bv - s);
+    dnew = step == 0 ? T(cf[0]) * res : cheb_dir(T(cf[2 * step]), dprev, T(cf[2 * step + 1]), res);
+    return xv + dnew;
+  }
+  if constexpr (sizeof(T) == 4)
+    return __fmaf_rn(__fmul_rn(omega, dv), __fsub_rn(bv, s), xv);
+  else
+    return __fma_rn(__dmul_rn(omega, dv), __dsub_rn(bv, s), xv);
 }
 
 constexpr int kStencilThreads = 192;
@@ -351,33 +422,63 @@ __global__ void __launch_bounds__(kStencilThreads) k_stencil_op(MgDims d, const 
   const int64_t n = (it / 96) * 32 + (it & 31);
   const int r = int((it / 32) % 3);
   if (n >= int64_t(d.nnx) * d.nny * d.nnz) return;
-  const int a = int(n % d.nnx), bb = int((n / d.nnx) % d.nny);
-  const int c = int(n / (int64_t(d.nnx) * d.nny));
+  int a, bb, c;
+  node_abc(d, n, a, bb, c);
   const T s = stencil_row<T, false>(d, A, x, a, bb, c, r);
   const int64_t dof = 3 * n + r;
-  T out;
-  if (!act[dof]) {
-    out = T(0);
-    if (MODE == kCheb) static_cast<T*>(ch.dir_)[dof] = T(0);
-  } else if (MODE == kApply) {
-    out = s;
-  } else if (MODE == kResidual) {
-    out = b[dof] - s;
-  } else if (MODE == kCheb) {
-    // Chebyshev step `ch.step` (Saad, Iterative Methods, Alg. 12.1): d_k =
-    // rho_k rho_{k-1} d_{k-1} + (2 rho_k / delta) D^-1 (b - A x_k),
-    // d_0 = D^-1 (b - A x_0) / theta, x_{k+1} = x_k + d_k, with the step's
-    // coefficients from the level's table.
-    const T res = invdiag[dof] * (b[dof] - s);
-    T* dir = static_cast<T*>(ch.dir_);
-    const float* cf = ch.coef;
-    const T dn = ch.step == 0 ? T(cf[0]) * res
-                              : cheb_dir(T(cf[2 * ch.step]), dir[dof], T(cf[2 * ch.step + 1]), res);
-    dir[dof] = dn;
-    out = x[dof] + dn;
-  } else {
-    out = x[dof] + omega * invdiag[dof] * (b[dof] - s);
+  T* dir = static_cast<T*>(ch.dir_);
+  const bool ac = act[dof] != 0;
+  T dnew;
+  const T out = stencil_update<T, MODE>(
+      ac, s, (MODE == kSmooth || MODE == kCheb) ? x[dof] : T(0), MODE != kApply ? b[dof] : T(0),
+      (MODE == kSmooth || MODE == kCheb) ? invdiag[dof] : T(0), omega, ch.coef, ch.step,
+      (MODE == kCheb && ch.step > 0 && ac) ? dir[dof] : T(0), dnew);
+  if (MODE == kCheb) dir[dof] = dnew;
+  y[dof] = out;
+}
+
+// The FP32 stencil kernels on small levels: four threads per (node, row), one
+// part of the row each (stencil_part), combined in shared memory in the order
+// stencil_row uses, so both kernels give the same bits.  384 threads: 32
+// consecutive nodes x 3 rows x 4 parts.  The update's vector reads are issued
+// before the row's, so they overlap.
+constexpr int kSplitThreads = 384;
+constexpr int64_t kSplitMaxNodes = 16384;
+
+template <int MODE>
+__global__ void __launch_bounds__(kSplitThreads) k_stencil_split(
+    MgDims d, const float* __restrict__ A, const uint8_t* __restrict__ act,
+    const float* __restrict__ x, const float* __restrict__ b, const float* __restrict__ invdiag,
+    float omega, float* __restrict__ y, ChebStep ch) {
+  __shared__ float parts[3][3][32];
+  const int t = threadIdx.x, q = t / 96, r = (t / 32) % 3, lane = t & 31;
+  const int64_t n = int64_t(blockIdx.x) * 32 + lane;
+  const bool valid = n < int64_t(d.nnx) * d.nny * d.nnz;
+  const int64_t dof = 3 * n + r;
+  float* dir = static_cast<float*>(ch.dir_);
+  bool ac = false;
+  float xv = 0.0f, bv = 0.0f, dv = 0.0f, dprev = 0.0f;
+  if (q == 0 && valid) {
+    ac = act[dof] != 0;
+    if (MODE == kSmooth || MODE == kCheb) xv = x[dof];
+    if (MODE != kApply) bv = b[dof];
+    if (MODE == kSmooth || MODE == kCheb) dv = invdiag[dof];
+    if (MODE == kCheb && ch.step > 0) dprev = dir[dof];
   }
+  float p = 0.0f;
+  if (valid) {
+    int a, bb, c;
+    node_abc(d, n, a, bb, c);
+    p = stencil_part<float, false>(d, A, x, a, bb, c, r, q);
+  }
+  if (q > 0) parts[q - 1][r][lane] = p;
+  __syncthreads();
+  if (q != 0 || !valid) return;
+  const float s = ((p + parts[0][r][lane]) + parts[1][r][lane]) + parts[2][r][lane];
+  float dnew;
+  const float out = stencil_update<float, MODE>(ac, s, xv, bv, dv, omega, ch.coef, ch.step,
+                                                ac ? dprev : 0.0f, dnew);
+  if (MODE == kCheb) dir[dof] = dnew;
   y[dof] = out;
 }
 
@@ -566,7 +667,8 @@ __global__ void k_dense_from_stencil(MgDims d, const T* __restrict__ A,
   const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
   for (int64_t n = blockIdx.x * int64_t(kThreads) + threadIdx.x; n < nn;
        n += int64_t(gridDim.x) * kThreads) {
-    const int a = int(n % d.nnx), b = int((n / d.nnx) % d.nny), c = int(n / (int64_t(d.nnx) * d.nny));
+    int a, b, c;
+    node_abc(d, n, a, b, c);
     for (int j = 0; j < 14; ++j) {
       const int di = 13 + j;
       const int i = a + di % 3 - 1, jj = b + (di / 3) % 3 - 1, k = c + di / 9 - 1;
@@ -773,7 +875,25 @@ template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
                    const T* b, const T* invdiag, T omega, T* y, cudaStream_t s,
                    ChebStep ch) {
-  const int64_t items = (int64_t(d.nnx) * d.nny * d.nnz + 31) / 32 * 96;
+  const int64_t nn = int64_t(d.nnx) * d.nny * d.nnz;
+  if constexpr (sizeof(T) == 4) {
+    if (nn <= kSplitMaxNodes) {
+      const unsigned ns = unsigned((nn + 31) / 32);
+      if (mode == kApply)
+        k_stencil_split<kApply><<<ns, kSplitThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
+      else if (mode == kResidual)
+        k_stencil_split<kResidual><<<ns, kSplitThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y,
+                                                                ch);
+      else if (mode == kCheb)
+        k_stencil_split<kCheb><<<ns, kSplitThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y, ch);
+      else
+        k_stencil_split<kSmooth><<<ns, kSplitThreads, 0, s>>>(d, A, act, x, b, invdiag, omega, y,
+                                                              ch);
+      TG_LAUNCH_CHECK();
+      return;
+    }
+  }
+  const int64_t items = (nn + 31) / 32 * 96;
   const unsigned nb = unsigned((items + kStencilThreads - 1) / kStencilThreads);
   const unsigned nt = kStencilThreads;
   if (mode == kApply)
@@ -944,9 +1064,7 @@ __device__ __forceinline__ void dof_item(int64_t it, const MgDims& d, int& a, in
   const int64_t chunk = it / 96;
   r = int((it / 32) % 3);
   n = chunk * 32 + (it & 31);
-  a = int(n % d.nnx);
-  b = int((n / d.nnx) % d.nny);
-  c = int(n / (int64_t(d.nnx) * d.nny));
+  node_abc(d, n, a, b, c);
 }
 
 __global__ void __launch_bounds__(kFusedThreads, 1) k_coarse_vcycle(FusedCoarse fc) {
@@ -975,19 +1093,15 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_coarse_vcycle(FusedCoarse 
       const int64_t dof = 3 * n + r;
       const float s = from_zero ? 0.0f : stencil_row<float, true>(L.d, L.A, xin, a, b, c, r);
       const float xv = from_zero ? 0.0f : __ldcg(xin + dof);
-      float out;
-      if (!L.act[dof]) {
-        out = 0.0f;
-        if (fc.cheb_m > 0) L.chd[dof] = 0.0f;
-      } else if (fc.cheb_m > 0) {
-        const float res = L.dinv[dof] * (__ldcg(L.b + dof) - s);
-        const float dn = k == 0 ? L.coef[0] * res
-                                : cheb_dir(L.coef[2 * k], __ldcg(L.chd + dof), L.coef[2 * k + 1],
-                                           res);
-        L.chd[dof] = dn;
-        out = xv + dn;
+      const bool ac = L.act[dof] != 0;
+      float out, dnew;
+      if (fc.cheb_m > 0) {
+        out = stencil_update<float, kCheb>(ac, s, xv, __ldcg(L.b + dof), L.dinv[dof], 0.0f, L.coef,
+                                           k, (k > 0 && ac) ? __ldcg(L.chd + dof) : 0.0f, dnew);
+        L.chd[dof] = dnew;
       } else {
-        out = xv + fc.omega * L.dinv[dof] * (__ldcg(L.b + dof) - s);
+        out = stencil_update<float, kSmooth>(ac, s, xv, __ldcg(L.b + dof), L.dinv[dof], fc.omega,
+                                             nullptr, 0, 0.0f, dnew);
       }
       xout[dof] = out;
     }
@@ -1020,8 +1134,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_coarse_vcycle(FusedCoarse 
     float* xfirst = C.xq;  // Chebyshev step 0 writes the other buffer (x = 0 in xp)
     if (smoothed && fc.cheb_m == 0) xfirst = C.xp;  // Jacobi's first sweep writes the iterate
     for (int64_t n = tid; n < nn; n += nthreads) {
-      const int a = int(n % C.d.nnx), b = int((n / C.d.nnx) % C.d.nny),
-                c = int(n / (int64_t(C.d.nnx) * C.d.nny));
+      int a, b, c;
+      node_abc(C.d, n, a, b, c);
       float s[3];
       restrict_node<float, true>(F.d, C.d, rf, a, b, c, s);
 #pragma unroll
@@ -1048,8 +1162,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_coarse_vcycle(FusedCoarse 
     float* xf = X(i);
     const int64_t nn = int64_t(F.d.nnx) * F.d.nny * F.d.nnz;
     for (int64_t n = tid; n < nn; n += nthreads) {
-      const int a = int(n % F.d.nnx), b = int((n / F.d.nnx) % F.d.nny),
-                c = int(n / (int64_t(F.d.nnx) * F.d.nny));
+      int a, b, c;
+      node_abc(F.d, n, a, b, c);
       float s[3];
       prolong_node<float, true>(F.d, C.d, ec, a, b, c, s);
 #pragma unroll

@@ -613,6 +613,7 @@ __global__ void __launch_bounds__(32 * W, (ColShape<Y, W>::kMinB))
                   const float* __restrict__ invdiag, float omega, float* __restrict__ y,
                   double* __restrict__ dot_part) {
   __shared__ float xs[2][W][6][32];
+  // Smoothing with dot_part set: partial b . y as well (the PCG's r . z).
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int ex = blockIdx.x * 30 - 1 + lane;
   const int ey0 = blockIdx.y * ColShape<Y, W>::kRows - 1 + w * Y;  // element rows ey0 .. ey0+Y-1
@@ -700,10 +701,11 @@ __global__ void __launch_bounds__(32 * W, (ColShape<Y, W>::kMinB))
         out = kk ? bv[k] - ax[k] : 0.0f;
       } else {
         out = kk ? cur[i][k] + omega * dv[k] * (bv[k] - ax[k]) : 0.0f;
+        nd = fmaf(bv[k], out, nd);
       }
       y[d] = out;
     }
-    if constexpr (MODE == kApply) dsum += nd;
+    if constexpr (MODE != kResidual) dsum += nd;
   };
 
 #pragma unroll 1
@@ -827,7 +829,7 @@ __global__ void __launch_bounds__(32 * W, (ColShape<Y, W>::kMinB))
         nxt[i][k] = raw[i][k];
       }
   }
-  if (MODE == kApply && dot_part != nullptr) {
+  if (MODE != kResidual && dot_part != nullptr) {
     const double sum = block_sum(double(dsum));
     if (threadIdx.x == 0)
       dot_part[(int64_t(blockIdx.z) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sum;
@@ -949,11 +951,6 @@ static void launch_mode(const Grid& g, const ModalConsts& c, const T* ef, const 
   TG_LAUNCH_CHECK();
 }
 
-void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const ModalConsts& c,
-                          const float* ef, const uint8_t* kept, const float* x, const float* b,
-                          const float* invdiag, float omega, float* y, double* dot_part,
-                          int* nblocks_out, cudaStream_t s, const uint8_t* kn);
-
 template <class T>
 void launch_fine_op(int mode, const Grid& g, const ModalConsts& c, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
@@ -1003,19 +1000,21 @@ void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const
       return;
     }
   }
+  // The pencil kernel has no fused b . y: its partials come from a dot kernel.
   if (nblocks_out) {
     const dim3 d = pencil_grid<T>(g);
-    *nblocks_out = int(d.x * d.y * d.z);
+    *nblocks_out = mode == kSmooth && dot_part != nullptr ? kRedBlocks : int(d.x * d.y * d.z);
   }
   switch (mode) {
     case kApply:
       launch_mode<T, kApply>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
       break;
     case kResidual:
-      launch_mode<T, kResidual>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
+      launch_mode<T, kResidual>(g, c, ef, kept, x, b, invdiag, omega, y, nullptr, s);
       break;
     default:
-      launch_mode<T, kSmooth>(g, c, ef, kept, x, b, invdiag, omega, y, dot_part, s);
+      launch_mode<T, kSmooth>(g, c, ef, kept, x, b, invdiag, omega, y, nullptr, s);
+      if (dot_part != nullptr) launch_dot_partials_f(b, y, g.ndof, dot_part, s);
   }
 }
 

@@ -300,6 +300,12 @@ void launch_dot_f(const float* a, const float* b, int64_t n, double* part, doubl
   TG_LAUNCH_CHECK();
 }
 
+void launch_dot_partials_f(const float* a, const float* b, int64_t n, double* part,
+                           cudaStream_t s) {
+  k_dot<float><<<kRedBlocks, kThreads, 0, s>>>(a, b, n, part);
+  TG_LAUNCH_CHECK();
+}
+
 void launch_sum_partials(const double* part, int n, double* out, cudaStream_t s) {
   k_sum_partials<<<1, kThreads, 0, s>>>(part, n, out);
   TG_LAUNCH_CHECK();

@@ -900,7 +900,8 @@ float* Solver::fused_coarse_vcycle() {
 }
 
 template <>
-double* Solver::vcycle<double>(const double* b) {
+double* Solver::vcycle<double>(const double* b, double* bz) {
+  if (bz != nullptr) raise(TG_EINVAL, "vcycle<double>: no fused b.z");
   const Grid& g = fp_.g;
   Level& N = *levels_[0];
   const MgDims fd = dims_of(g.nx, g.ny, g.nz);
@@ -924,26 +925,31 @@ double* Solver::vcycle<double>(const double* b) {
 }
 
 template <>
-float* Solver::vcycle<float>(const float* b) {
+// With bz set, b . z of the returned z is summed into *bz (device): the last
+// smoothing sweep accumulates it while it writes z.
+float* Solver::vcycle<float>(const float* b, double* bz) {
   const Grid& g = fp_.g;
   Level& N = *levels_[0];
   const MgDims fd = dims_of(g.nx, g.ny, g.nz);
   float* x = t1f_.p;
   float* r = t0f_.p;
   const float w = float(omega_);
-  auto smooth = [&] {
-    launch_fine_op<float>(kSmooth, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
-                          nullptr, s_, fp_.kept_node.p);
+  auto smooth = [&](bool last) {
+    int nb = 0;
+    double* part = last && bz != nullptr ? part_.p : nullptr;
+    launch_fine_op<float>(kSmooth, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, part,
+                          &nb, s_, fp_.kept_node.p);
+    if (part != nullptr) launch_sum_partials(part_.p, nb, bz, s_);
     std::swap(x, r);
   };
   mg_jacobi_first<float>(b, invdiagf_.p, w, g.ndof, x, s_);
-  for (int k = 1; k < sweeps_; ++k) smooth();
+  for (int k = 1; k < sweeps_; ++k) smooth(false);
   launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
                         nullptr, s_, fp_.kept_node.p);
   mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_);
   float* ec = vcycle_level<float>(1);
   mg_prolong_add<float>(fd, N.d, ec, fp_.kept.p, x, s_);
-  for (int k = 0; k < sweeps_; ++k) smooth();
+  for (int k = 0; k < sweeps_; ++k) smooth(k == sweeps_ - 1);
   lowp_matvecs_ += 2 * sweeps_;
   return x;
 }
@@ -1054,8 +1060,7 @@ bool Solver::build_inner_graph() {
     const int64_t m0 = lowp_matvecs_;
     bool cap_ok = true;
     try {
-      float* z = vcycle<float>(rf_.p);
-      launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 9, s_);
+      float* z = vcycle<float>(rf_.p, scal_.p + 9);
       launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
       TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice,
                               s_));
@@ -1095,9 +1100,8 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
   launch_fill<float>(xf_.p, 0.0f, n, s_);
   TG_CUDA(cudaMemcpyAsync(rf_.p, zf_.p, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, s_));
   launch_dot_f(rf_.p, rf_.p, n, part_.p, scal_.p + 10, s_);
-  float* z = vcycle<float>(rf_.p);
+  float* z = vcycle<float>(rf_.p, scal_.p + 6);
   TG_CUDA(cudaMemcpyAsync(pf_.p, z, size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, s_));
-  launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 6, s_);
   const double b2 = read_scalar(10);
   const double thr = rel_tol * std::sqrt(b2);
   int nb = 0;
@@ -1137,8 +1141,7 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
       if (broke) ++st.inner_breakdowns;
       return true;
     }
-    z = vcycle<float>(rf_.p);
-    launch_dot_f(rf_.p, z, n, part_.p, scal_.p + 9, s_);
+    z = vcycle<float>(rf_.p, scal_.p + 9);
     launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
     TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice, s_));
   }

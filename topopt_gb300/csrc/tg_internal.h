@@ -159,6 +159,7 @@ void launch_fine_residual_df(const Grid& g, const ModalConsts& c, const double* 
 //   kSmooth:   y = x + omega*invdiag*(b - A x)   (invdiag is 0 off the kept set)
 //   kept_node (optional): the kept mask as 3 bits per node, read by the FP32
 //   column schedule instead of kept (one byte per node instead of three).
+//   kSmooth with dot_part (FP32 only): partials of b . y as well.
 template <class T>
 void launch_fine_op(int mode, const Grid& g, const ModalConsts& mc, const T* ef,
                     const uint8_t* kept, const T* x, const T* b, const T* invdiag, T omega,
@@ -198,7 +199,7 @@ bool level1_tc_enabled();
 void set_level1_tc(bool on);
 // Whether the mixed form's V-cycle runs its small levels (from the first one of
 // at most kFusedMaxNodes nodes to the coarsest) as one cluster launch
-// (k_multigrid.cu) instead of a launch per step; on by default.
+// (k_multigrid.cu) instead of a launch per step; off by default.
 bool coarse_fused_enabled();
 void set_coarse_fused(bool on);
 // Batched apply on the periodic nx*ny*nz torus (nodes = elements per axis); see
@@ -223,6 +224,9 @@ void launch_dot(const double* a, const double* b, int64_t n, double* part, doubl
 void launch_dot_f(const float* a, const float* b, int64_t n, double* part, double* out,
                   cudaStream_t s);
 void launch_sum_partials(const double* part, int n, double* out, cudaStream_t s);
+// Partials of a . b (FP32 vectors) over kRedBlocks blocks, not yet summed.
+void launch_dot_partials_f(const float* a, const float* b, int64_t n, double* part,
+                           cudaStream_t s);
 // PCG pieces with scalars living in device memory (no host round trip).
 template <class T>
 void launch_cg_update_xr(T* x, T* r, const T* p, const T* ap, const double* rz,

@@ -88,7 +88,7 @@ class Solver {
   bool jacobi_pcg(double tol, int max_it, bool warm, SolverStats& st);
   bool mixed_refine(double tol, int max_it, bool warm, SolverStats& st);
   template <class T>
-  T* vcycle(const T* b);
+  T* vcycle(const T* b, double* bz = nullptr);
   template <class T>
   T* vcycle_level(size_t l);  // returns the buffer holding the level's result
   float* fused_coarse_vcycle();
