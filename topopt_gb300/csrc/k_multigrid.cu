@@ -648,12 +648,16 @@ __global__ void __launch_bounds__(256) k_prolong_add(MgDims fd, MgDims cd,
                                                      T* __restrict__ xf) {
   const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
   if (a >= fd.nnx || b >= fd.nny) return;
+  const int64_t n = (int64_t(c) * fd.nny + b) * fd.nnx + a;
+  // The iterate and the mask are read unconditionally, in parallel with the
+  // coarse values: a read under the mask's branch would wait for the mask first.
+  const T x0 = xf[3 * n], x1 = xf[3 * n + 1], x2 = xf[3 * n + 2];
+  const bool f0 = fact[3 * n] != 0, f1 = fact[3 * n + 1] != 0, f2 = fact[3 * n + 2] != 0;
   T s[3];
   prolong_node<T, false>(fd, cd, ec, a, b, c, s);
-  const int64_t n = (int64_t(c) * fd.nny + b) * fd.nnx + a;
-  if (fact[3 * n]) xf[3 * n] += s[0];
-  if (fact[3 * n + 1]) xf[3 * n + 1] += s[1];
-  if (fact[3 * n + 2]) xf[3 * n + 2] += s[2];
+  if (f0) xf[3 * n] = x0 + s[0];
+  if (f1) xf[3 * n + 1] = x1 + s[1];
+  if (f2) xf[3 * n + 2] = x2 + s[2];
 }
 
 // ---------------------------------------------------------- coarsest solve
