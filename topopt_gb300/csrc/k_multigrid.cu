@@ -593,15 +593,27 @@ __device__ __forceinline__ void restrict_node(const MgDims& fd, const MgDims& cd
 template <class T>
 __global__ void __launch_bounds__(256) k_restrict(MgDims fd, MgDims cd, const T* __restrict__ rf,
                                                   const uint8_t* __restrict__ cact,
-                                                  T* __restrict__ bc) {
+                                                  T* __restrict__ bc, FirstStep<T> first) {
   const int a = blockIdx.x * 32 + threadIdx.x, b = blockIdx.y * 8 + threadIdx.y, c = blockIdx.z;
   if (a >= cd.nnx || b >= cd.nny) return;
   T s[3];
   restrict_node<T, false>(fd, cd, rf, a, b, c, s);
   const int64_t n = (int64_t(c) * cd.nny + b) * cd.nnx + a;
-  bc[3 * n] = cact[3 * n] ? s[0] : T(0);
-  bc[3 * n + 1] = cact[3 * n + 1] ? s[1] : T(0);
-  bc[3 * n + 2] = cact[3 * n + 2] ? s[2] : T(0);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int64_t dof = 3 * n + k;
+    const bool ac = cact[dof] != 0;
+    const T bv = ac ? s[k] : T(0);
+    bc[dof] = bv;
+    if (first.kind == 1) {
+      first.x[dof] = first.omega * first.dinv[dof] * bv;
+    } else if (first.kind == 2) {
+      T dnew;
+      first.x[dof] = stencil_update<T, kCheb>(ac, T(0), T(0), bv, first.dinv[dof], T(0),
+                                              first.coef, 0, T(0), dnew);
+      first.chd[dof] = dnew;
+    }
+  }
 }
 
 // The prolonged correction at fine node (a, b, c): per axis one coarse node
@@ -951,9 +963,9 @@ void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cud
 
 template <class T>
 void mg_restrict(const MgDims& fd, const MgDims& cd, const T* rf, const uint8_t* cact, T* bc,
-                 cudaStream_t s) {
+                 cudaStream_t s, FirstStep<T> first) {
   const dim3 grid((cd.nnx + 31) / 32, (cd.nny + 7) / 8, cd.nnz);
-  k_restrict<T><<<grid, dim3(32, 8), 0, s>>>(fd, cd, rf, cact, bc);
+  k_restrict<T><<<grid, dim3(32, 8), 0, s>>>(fd, cd, rf, cact, bc, first);
   TG_LAUNCH_CHECK();
 }
 
@@ -1015,7 +1027,7 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
                                  const T*, const T*, T, T*, cudaStream_t, ChebStep);          \
   template void mg_jacobi_first<T>(const T*, const T*, T, int64_t, T*, cudaStream_t);         \
   template void mg_restrict<T>(const MgDims&, const MgDims&, const T*, const uint8_t*, T*,    \
-                               cudaStream_t);                                                 \
+                               cudaStream_t, FirstStep<T>);                                   \
   template void mg_prolong_add<T>(const MgDims&, const MgDims&, const T*, const uint8_t*, T*, \
                                   cudaStream_t);                                              \
   template void mg_chol_solve<T>(const double*, int, const int*, int64_t, const T*, T*,       \

@@ -803,7 +803,31 @@ bool Solver::build_numeric() {
 
 // ------------------------------------------------------------------ V-cycle
 template <class T>
-T* Solver::vcycle_level(size_t l) {
+FirstStep<T> Solver::first_step(size_t l) {
+  FirstStep<T> f;
+  if (l >= levels_.size()) return f;  // the coarsest: solved, not smoothed
+  if constexpr (sizeof(T) == 4) {
+    if (l == fused_level_) return f;  // the fused launch takes its own first step
+  }
+  Level& L = *levels_[l - 1];
+  f.dinv = L.Dinv<T>();
+  if (sizeof(T) == 4 && cheb_m_ > 0 && l >= 2) {
+    f.kind = 2;
+    f.coef = chc_.p + kChebCoefStride * (l - 1);
+    f.x = L.R<T>();  // step 0 writes the other buffer, as the stencil step does
+    f.chd = static_cast<T*>(static_cast<void*>(L.chd.p));
+  } else {
+    f.kind = 1;
+    f.omega = T(omega_);
+    f.x = L.X<T>();
+  }
+  return f;
+}
+
+// first_done: the restriction into this level already took its first smoothing
+// step from zero (first_step).
+template <class T>
+T* Solver::vcycle_level(size_t l, bool first_done) {
   Level& L = *levels_[l - 1];
   if (l == levels_.size()) {
     if (chol_inv_.p)
@@ -831,33 +855,40 @@ T* Solver::vcycle_level(size_t l) {
     // Mixed form, levels >= 2: a degree-cheb_m_ Chebyshev polynomial in D^-1 A
     // before (from a zero iterate) and after the coarse correction.
     ChebStep ch{L.chd.p, chc_.p + kChebCoefStride * (l - 1), 0};
-    auto cheb = [&] {
-      for (int k = 0; k < cheb_m_; ++k) {
+    auto cheb = [&](int k0) {
+      for (int k = k0; k < cheb_m_; ++k) {
         ch.step = k;
         mg_stencil_op<T>(kCheb, L.d, L.Am<T>(), L.act.p, L.X<T>(), L.B<T>(), L.Dinv<T>(), w,
                          L.R<T>(), s_, ch);
         std::swap(L.X<T>(), L.R<T>());
       }
     };
-    launch_fill<T>(L.X<T>(), T(0), L.ndof, s_);
-    cheb();
+    if (first_done) {
+      std::swap(L.X<T>(), L.R<T>());
+      cheb(1);
+    } else {
+      launch_fill<T>(L.X<T>(), T(0), L.ndof, s_);
+      cheb(0);
+    }
     op(kResidual);
-    mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
-    T* ec = vcycle_level<T>(l + 1);
+    const FirstStep<T> fs = first_step<T>(l + 1);
+    mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_, fs);
+    T* ec = vcycle_level<T>(l + 1, fs.kind != 0);
     mg_prolong_add<T>(L.d, N.d, ec, L.act.p, L.X<T>(), s_);
-    cheb();
+    cheb(0);
     return L.X<T>();
   }
   // sweeps_ damped-Jacobi sweeps on each side (the first from a zero iterate);
   // every sweep leaves the iterate in X.
-  mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);
+  if (!first_done) mg_jacobi_first<T>(L.B<T>(), L.Dinv<T>(), w, L.ndof, L.X<T>(), s_);
   for (int k = 1; k < sweeps_; ++k) {
     op(kSmooth);
     std::swap(L.X<T>(), L.R<T>());
   }
   op(kResidual);
-  mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_);
-  T* ec = vcycle_level<T>(l + 1);
+  const FirstStep<T> fs = first_step<T>(l + 1);
+  mg_restrict<T>(L.d, N.d, L.R<T>(), N.act.p, N.B<T>(), s_, fs);
+  T* ec = vcycle_level<T>(l + 1, fs.kind != 0);
   mg_prolong_add<T>(L.d, N.d, ec, L.act.p, L.X<T>(), s_);
   for (int k = 0; k < sweeps_; ++k) {
     op(kSmooth);
@@ -916,8 +947,9 @@ double* Solver::vcycle<double>(const double* b, double* bz) {
   for (int k = 1; k < sweeps_; ++k) smooth();
   launch_fine_op<double>(kResidual, g, fp_.mc, E_, fp_.kept.p, x, b, invdiag_.p, omega_, r,
                          nullptr, nullptr, s_);
-  mg_restrict<double>(fd, N.d, r, N.act.p, N.B<double>(), s_);
-  double* ec = vcycle_level<double>(1);
+  const FirstStep<double> fs = first_step<double>(1);
+  mg_restrict<double>(fd, N.d, r, N.act.p, N.B<double>(), s_, fs);
+  double* ec = vcycle_level<double>(1, fs.kind != 0);
   mg_prolong_add<double>(fd, N.d, ec, fp_.kept.p, x, s_);
   for (int k = 0; k < sweeps_; ++k) smooth();
   fine_matvecs_ += 2 * sweeps_;
@@ -946,8 +978,9 @@ float* Solver::vcycle<float>(const float* b, double* bz) {
   for (int k = 1; k < sweeps_; ++k) smooth(false);
   launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
                         nullptr, s_, fp_.kept_node.p);
-  mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_);
-  float* ec = vcycle_level<float>(1);
+  const FirstStep<float> fs = first_step<float>(1);
+  mg_restrict<float>(fd, N.d, r, N.act.p, N.B<float>(), s_, fs);
+  float* ec = vcycle_level<float>(1, fs.kind != 0);
   mg_prolong_add<float>(fd, N.d, ec, fp_.kept.p, x, s_);
   for (int k = 0; k < sweeps_; ++k) smooth(k == sweeps_ - 1);
   lowp_matvecs_ += 2 * sweeps_;

@@ -63,9 +63,22 @@ void mg_lambda_max(const MgDims& d, const T* A, const uint8_t* act, const T* inv
                    cudaStream_t s);
 template <class T>
 void mg_jacobi_first(const T* b, const T* invdiag, T omega, int64_t n, T* x, cudaStream_t s);
+// The coarse level's first smoothing step from a zero iterate, taken by the
+// restriction that forms its right-hand side (it needs no operator): kind 1
+// damped Jacobi, x = omega dinv b (as mg_jacobi_first); kind 2 Chebyshev step 0,
+// chd = coef[0] dinv b and x = 0 + chd (as the kCheb stencil step on x = 0).
+template <class T>
+struct FirstStep {
+  int kind = 0;  // 0: none
+  const T* dinv = nullptr;
+  T omega = T(0);
+  const float* coef = nullptr;
+  T* x = nullptr;
+  T* chd = nullptr;
+};
 template <class T>
 void mg_restrict(const MgDims& fd, const MgDims& cd, const T* rf, const uint8_t* cact, T* bc,
-                 cudaStream_t s);
+                 cudaStream_t s, FirstStep<T> first = FirstStep<T>{});
 template <class T>
 void mg_prolong_add(const MgDims& fd, const MgDims& cd, const T* ec, const uint8_t* fact, T* xf,
                     cudaStream_t s);

@@ -90,7 +90,9 @@ class Solver {
   template <class T>
   T* vcycle(const T* b, double* bz = nullptr);
   template <class T>
-  T* vcycle_level(size_t l);  // returns the buffer holding the level's result
+  T* vcycle_level(size_t l, bool first_done = false);  // returns the level's result buffer
+  template <class T>
+  FirstStep<T> first_step(size_t l);  // level l's first sweep, for the restriction into it
   float* fused_coarse_vcycle();
   template <class T>
   bool inner_pcg(int max_it, double rel_tol, SolverStats& st, int* iters);
