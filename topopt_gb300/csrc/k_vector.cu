@@ -132,6 +132,59 @@ __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// The two halves of k_cg_update_xr for the FP32 inner PCG, with its alpha and
+// its arithmetic: r -= alpha Ap with partial r.r, and x += alpha p, which the
+// solver runs later, beside the next V-cycle's coarse levels (nothing in the
+// loop reads x).
+__device__ __forceinline__ float cg_alpha_f(const double* rz, const double* pap) {
+  const double pp = *pap;
+  return float((pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0);
+}
+__global__ void k_cg_update_r_f(float* __restrict__ r, const float* __restrict__ ap,
+                                const double* __restrict__ rz, const double* __restrict__ pap,
+                                int64_t n, double* __restrict__ part) {
+  const float af = cg_alpha_f(rz, pap);
+  const int64_t n4 = n >> 2;
+  float4* r4 = reinterpret_cast<float4*>(r);
+  const float4* a4 = reinterpret_cast<const float4*>(ap);
+  float tf = 0.0f;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n4;
+       i += int64_t(gridDim.x) * kThreads) {
+    float4 rv = r4[i];
+    const float4 qv = a4[i];
+    rv.x -= af * qv.x; rv.y -= af * qv.y; rv.z -= af * qv.z; rv.w -= af * qv.w;
+    r4[i] = rv;
+    tf += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+  }
+  float t = tf;
+  for (int64_t i = (n4 << 2) + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads) {
+    const float ri = r[i] - af * ap[i];
+    r[i] = ri;
+    t += ri * ri;
+  }
+  const double s = block_sum256(double(t));
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void k_cg_update_x_f(float* __restrict__ x, const float* __restrict__ p,
+                                const double* __restrict__ rz, const double* __restrict__ pap,
+                                int64_t n) {
+  const float af = cg_alpha_f(rz, pap);
+  const int64_t n4 = n >> 2;
+  float4* x4 = reinterpret_cast<float4*>(x);
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n4;
+       i += int64_t(gridDim.x) * kThreads) {
+    float4 xv = x4[i];
+    const float4 pv = p4[i];
+    xv.x += af * pv.x; xv.y += af * pv.y; xv.z += af * pv.z; xv.w += af * pv.w;
+    x4[i] = xv;
+  }
+  for (int64_t i = (n4 << 2) + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * kThreads)
+    x[i] += af * p[i];
+}
+
 // z = invdiag .* r (Jacobi preconditioner); partial r.z.
 __global__ void k_scale_mask(double* __restrict__ z, const double* __restrict__ r,
                              const double* __restrict__ invdiag, int64_t n,
@@ -323,6 +376,17 @@ template void launch_cg_update_xr<double>(double*, double*, const double*, const
 template void launch_cg_update_xr<float>(float*, float*, const float*, const float*,
                                          const double*, const double*, int64_t, double*,
                                          cudaStream_t);
+
+void launch_cg_update_r_f(float* r, const float* ap, const double* rz, const double* pap,
+                          int64_t n, double* rr_part, cudaStream_t s) {
+  k_cg_update_r_f<<<kRedBlocks, kThreads, 0, s>>>(r, ap, rz, pap, n, rr_part);
+  TG_LAUNCH_CHECK();
+}
+void launch_cg_update_x_f(float* x, const float* p, const double* rz, const double* pap,
+                          int64_t n, cudaStream_t s) {
+  k_cg_update_x_f<<<kRedBlocks, kThreads, 0, s>>>(x, p, rz, pap, n);
+  TG_LAUNCH_CHECK();
+}
 
 void launch_scale_mask(double* z, const double* r, const double* invdiag, int64_t n,
                        double* rz_part, cudaStream_t s) {

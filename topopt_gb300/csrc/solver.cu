@@ -382,6 +382,12 @@ struct Solver::InnerGraph {
 
 Solver::~Solver() {
   ig_.reset();
+  if (s2_) {
+    cudaStreamSynchronize(s2_);
+    cudaEventDestroy(ev_fork_);
+    cudaEventDestroy(ev_join_);
+    cudaStreamDestroy(s2_);
+  }
   pinned_release(h_scal_);
   pinned_release(h_ist_);
 }
@@ -573,6 +579,8 @@ void Solver::build_structure() {
   // The small levels (from the first one of at most kFusedMaxNodes nodes, below
   // level 1) in one cluster launch, when at least one of them is smoothed and
   // the coarsest has the explicit inverse.
+  side_level_ = levels_.size() >= 2 ? 2 : 0;
+  if (mixed_ && side_level_ > 0) ensure_side();
   fused_level_ = 0;
   if (mixed_ && coarse_fused_enabled() && chol_inv_.p != nullptr) {
     for (size_t l = 2; l < levels_.size(); ++l) {
@@ -824,11 +832,60 @@ FirstStep<T> Solver::first_step(size_t l) {
   return f;
 }
 
+// The side stream (lowest priority) and its two events; created before any
+// capture begins, never inside one.
+void Solver::ensure_side() {
+  if (s2_) return;
+  int lo = 0, hi = 0;
+  TG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  TG_CUDA(cudaStreamCreateWithPriority(&s2_, cudaStreamNonBlocking, lo));
+  TG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+  TG_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+}
+
+bool Solver::fork_x() {
+  if (!pending_x_ || !s2_) return false;
+  TG_CUDA(cudaEventRecord(ev_fork_, s_));
+  TG_CUDA(cudaStreamWaitEvent(s2_, ev_fork_, 0));
+  launch_cg_update_x_f(xf_.p, pf_.p, scal_.p + 6, scal_.p + 7, fp_.g.ndof, s2_);
+  TG_CUDA(cudaEventRecord(ev_join_, s2_));
+  pending_x_ = false;
+  side_joined_ = false;
+  return true;
+}
+
+// Called from a destructor while an error may be propagating: no throw; a
+// failed wait leaves the error for the next checked call.
+void Solver::join_x() noexcept {
+  if (side_joined_) return;
+  cudaStreamWaitEvent(s_, ev_join_, 0);
+  side_joined_ = true;
+}
+
+void Solver::flush_x() {
+  if (!pending_x_) return;
+  launch_cg_update_x_f(xf_.p, pf_.p, scal_.p + 6, scal_.p + 7, fp_.g.ndof, s_);
+  pending_x_ = false;
+}
+
 // first_done: the restriction into this level already took its first smoothing
 // step from zero (first_step).
 template <class T>
 T* Solver::vcycle_level(size_t l, bool first_done) {
   Level& L = *levels_[l - 1];
+  // The pending x += alpha p of the FP32 PCG runs on the side stream while this
+  // level and the ones below it work (latency-bound launches that leave HBM
+  // idle); it joins the solver's stream when this level returns.
+  struct SideJoin {
+    Solver* s;
+    bool on;
+    ~SideJoin() {
+      if (on) s->join_x();
+    }
+  } side{this, false};
+  if constexpr (sizeof(T) == 4) {
+    if (l == side_level_ && pending_x_) side.on = fork_x();
+  }
   if (l == levels_.size()) {
     if (chol_inv_.p)
       mg_coarse_inv_apply<T>(chol_inv_.p, nc_, cidx_.p, cdof_.p, L.ndof, L.B<T>(), L.X<T>(), s_);
@@ -1093,7 +1150,9 @@ bool Solver::build_inner_graph() {
     const int64_t m0 = lowp_matvecs_;
     bool cap_ok = true;
     try {
+      pending_x_ = true;  // every body execution starts with the last one's x update
       float* z = vcycle<float>(rf_.p, scal_.p + 9);
+      flush_x();
       launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
       TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice,
                               s_));
@@ -1101,14 +1160,15 @@ bool Solver::build_inner_graph() {
       launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
                             apf_.p, part_.p, &nb, s_, fp_.kept_node.p);
       launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
-      launch_cg_update_xr<float>(xf_.p, rf_.p, pf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n,
-                                 part_.p, s_);
+      launch_cg_update_r_f(rf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);
       launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
       k_inner_cond<<<1, 1, 0, s_>>>(h, scal_.p, istate_.p);
       TG_LAUNCH_CHECK();
     } catch (const Error&) {
       cap_ok = false;
     }
+    pending_x_ = false;
+    side_joined_ = true;
     cudaGraph_t out = nullptr;
     const bool end_ok = cudaStreamEndCapture(s_, &out) == cudaSuccess;
     ig->body_launches = kernel_launch_count() - l0;
@@ -1144,16 +1204,23 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
                           apf_.p, part_.p, &nb, s_, fp_.kept_node.p);
     ++lowp_matvecs_;
     launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
-    launch_cg_update_xr<float>(xf_.p, rf_.p, pf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);
+    // r now; x += alpha p when p is next overwritten or at exit (flush_x), or on
+    // the side stream beside the next V-cycle's coarse levels (fork_x).
+    launch_cg_update_r_f(rf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);
+    pending_x_ = true;
     launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
     double sc[2];
     read_scalars(7, 2, sc);
-    if (!(sc[0] > 0.0) || !std::isfinite(sc[0])) {  // breakdown: x, r were left untouched
+    if (!(sc[0] > 0.0) || !std::isfinite(sc[0])) {  // breakdown: alpha = 0, x and r untouched
+      flush_x();
       ++st.inner_breakdowns;
       return k > 1;
     }
     *iters = k;
-    if (std::sqrt(sc[1]) <= thr) return true;
+    if (std::sqrt(sc[1]) <= thr) {
+      flush_x();
+      return true;
+    }
     if (k == 1 && max_it > 1 && use_graph_ && build_inner_graph()) {
       // Iterations 2.. on the device: one graph launch, one read-back.
       h_scal_[11] = thr;
@@ -1164,6 +1231,8 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
                               s_));
       TG_CUDA(cudaMemcpyAsync(istate_.p, h_ist_, 3 * sizeof(int), cudaMemcpyHostToDevice, s_));
       TG_CUDA(cudaGraphLaunch(ig_->exec, s_));
+      pending_x_ = true;  // the last body execution's x update
+      flush_x();
       TG_CUDA(cudaMemcpyAsync(h_ist_, istate_.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s_));
       TG_CUDA(cudaStreamSynchronize(s_));
       const int done = h_ist_[0], broke = h_ist_[2];
@@ -1175,9 +1244,11 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
       return true;
     }
     z = vcycle<float>(rf_.p, scal_.p + 9);
+    flush_x();
     launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
     TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice, s_));
   }
+  flush_x();
   (void)st;
   return true;
 }

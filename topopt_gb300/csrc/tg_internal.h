@@ -231,6 +231,12 @@ void launch_dot_partials_f(const float* a, const float* b, int64_t n, double* pa
 template <class T>
 void launch_cg_update_xr(T* x, T* r, const T* p, const T* ap, const double* rz,
                          const double* pap, int64_t n, double* rr_part, cudaStream_t s);
+// The FP32 PCG update split in two (same alpha, same arithmetic as
+// launch_cg_update_xr<float>): r -= alpha Ap with partials of r.r, and x += alpha p.
+void launch_cg_update_r_f(float* r, const float* ap, const double* rz, const double* pap,
+                          int64_t n, double* rr_part, cudaStream_t s);
+void launch_cg_update_x_f(float* x, const float* p, const double* rz, const double* pap,
+                          int64_t n, cudaStream_t s);
 void launch_scale_mask(double* z, const double* r, const double* invdiag, int64_t n,
                        double* rz_part, cudaStream_t s);
 template <class T>

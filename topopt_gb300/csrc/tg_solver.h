@@ -154,6 +154,17 @@ class Solver {
   DBuf<int> tc_err_;  // a tensor-core completion wait that ran out
   // The small levels of the FP32 V-cycle in one cluster launch.
   size_t fused_level_ = 0;  // first level of the fused cluster launch (0: none)
+  // The FP32 PCG's deferred x += alpha p (alpha from scal_[6], scal_[7]; p in
+  // pf_): pending until flush_x() runs it on s_ or fork_x() on the side stream
+  // s2_ as the V-cycle enters side_level_; join_x() makes s_ wait for it.
+  bool pending_x_ = false, side_joined_ = true;
+  size_t side_level_ = 0;
+  cudaStream_t s2_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+  void ensure_side();
+  bool fork_x();
+  void join_x() noexcept;
+  void flush_x();
   void level1_op(int mode, Level& L, float omega);
   int* h_ist_ = nullptr;       // pinned mirror of istate_
 };
