@@ -222,7 +222,8 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
 
 // Node stencil from the element matrices around each node: the self block and
 // the forward blocks only.  Entry index q = (j*3 + c1)*3 + c2 with
-// j = d - 13, d = (dz+1)*9 + (dy+1)*3 + (dx+1) >= 13.
+// j = d - 13, d = (dz+1)*9 + (dy+1)*3 + (dx+1) >= 13.  With A null only the
+// inverse diagonal is formed (the self block), from the same sums.
 template <class T>
 __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
                                    const uint8_t* __restrict__ act, T* __restrict__ A,
@@ -239,6 +240,7 @@ __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
         for (int dx = -1; dx <= 1; ++dx) {
           const int di = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
           if (di < 13) continue;  // backward blocks: the neighbour's forward block, transposed
+          if (A == nullptr && di != 13) continue;
           const int j = di - 13;
           T blk[9];
 #pragma unroll
@@ -266,11 +268,12 @@ __global__ void k_assemble_stencil(MgDims d, const T* __restrict__ Kel,
               }
             }
           }
+          if (A != nullptr)
 #pragma unroll
-          for (int c1 = 0; c1 < 3; ++c1)
+            for (int c1 = 0; c1 < 3; ++c1)
 #pragma unroll
-            for (int c2 = 0; c2 < 3; ++c2)
-              A[int64_t(j * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : T(0);
+              for (int c2 = 0; c2 < 3; ++c2)
+                A[int64_t(j * 9 + c1 * 3 + c2) * nn + n] = ra[c1] ? blk[c1 * 3 + c2] : T(0);
           if (j == 0)
             for (int k = 0; k < 3; ++k) {
               const T dg = blk[k * 3 + k];
@@ -297,7 +300,7 @@ __global__ void k_to_float(const double* __restrict__ s, T* __restrict__ d, int6
 // of those loads are outstanding.  Out-of-grid neighbours are predicated (the
 // stored forward block of a node whose neighbour lies outside the grid is zero,
 // and the backward term is selected away).  Per output the terms are summed in
-// a fixed order: the self block, then per j the forward and backward term.
+// the fixed order of stencil_row.
 // Loads of vectors another CTA may have written earlier in the same launch (the
 // fused coarse V-cycle) go through L2; elsewhere plain loads.
 template <class T, bool COH>

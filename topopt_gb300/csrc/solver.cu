@@ -622,9 +622,19 @@ void Solver::apply_unmasked(const double* E, const double* x, double* y) {
                          nullptr, s_);
 }
 
+// The assembled FP32 level-1 stencil, formed from the level's element matrices
+// if the last hierarchy build kept only its diagonal.
+void Solver::level1_stencil() {
+  if (l1_stencil_ok_) return;
+  Level& L = *levels_[0];
+  mg_assemble_stencil<float>(L.d, L.Ke<float>(), L.act.p, L.Am<float>(), L.Dinv<float>(), s_);
+  l1_stencil_ok_ = true;
+}
+
 double Solver::check_level1() {
   if (!mixed_ || !l1_tc_ || !have_mg_ || !numeric_ok_)
     raise(TG_EINVAL, "check_level1: needs a mixed job with the level-1 tensor-core path");
+  level1_stencil();
   Level& L = *levels_[0];
   const size_t n = size_t(L.ndof);
   std::vector<float> xh(n), a(n), bq(n);
@@ -664,6 +674,7 @@ double Solver::time_operator(int form, int reps) {
     // form 4 the tensor-core operator.
     if (!have_mg_ || !numeric_ok_) raise(TG_EINVAL, "time_operator: no multigrid hierarchy");
     if (form == 4 && !l1_tc_) raise(TG_EINVAL, "time_operator: level-1 tensor-core path is off");
+    if (form == 3) level1_stencil();
     Level& L = *levels_[0];
     launch_fill<float>(L.X<float>(), 1.0f, L.ndof, s_);
     launch_fill<float>(L.B<float>(), 0.5f, L.ndof, s_);
@@ -780,7 +791,12 @@ bool Solver::build_numeric() {
                             pick<T>(G_, Gf_), L.Ke<T>(), s_);
     else
       mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
-    mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, L.Am<T>(), L.Dinv<T>(), s_);
+    // Level 1 on the tensor cores needs only its inverse diagonal; the assembled
+    // stencil (275 MB on cfg1) is formed on demand (level1_stencil()).
+    const bool diag_only = sizeof(T) == 4 && l == 0 && l1_tc_;
+    mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, diag_only ? nullptr : L.Am<T>(), L.Dinv<T>(),
+                           s_);
+    if (sizeof(T) == 4 && l == 0) l1_stencil_ok_ = !diag_only;
     pd = L.d;
   }
   if (sizeof(T) == 4 && cheb_m_ > 0) {

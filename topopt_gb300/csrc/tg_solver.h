@@ -154,6 +154,8 @@ class Solver {
   DBuf<int> tc_err_;  // a tensor-core completion wait that ran out
   // The small levels of the FP32 V-cycle in one cluster launch.
   size_t fused_level_ = 0;  // first level of the fused cluster launch (0: none)
+  bool l1_stencil_ok_ = true;  // the FP32 level-1 stencil is assembled (not only its diagonal)
+  void level1_stencil();
   // The FP32 PCG's deferred x += alpha p (alpha from scal_[6], scal_[7]; p in
   // pf_): pending until flush_x() runs it on s_ or fork_x() on the side stream
   // s2_ as the V-cycle enters side_level_; join_x() makes s_ wait for it.
