@@ -11,6 +11,7 @@ reference's exception classes: ``ValueError`` for std::invalid_argument,
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 import time
 import os
 from dataclasses import dataclass, field
@@ -199,6 +200,8 @@ def lib():
         "tg_job_estimate_bytes": ([vp, vp], C.c_int64),
         "tg_job_destroy": ([vp], None),
         "tg_job_time_operator": ([vp, i32, i32, vp], C.c_int),
+        "tg_host_alloc": ([C.c_int64], C.c_void_p),
+        "tg_host_free": ([C.c_void_p], C.c_int),
         "tg_kernel_launches": ([], C.c_int64),
         "tg_device_fma_peaks": ([vp, vp], C.c_int),
         "tg_set_fp32_schedule": ([i32, i32, i32], C.c_int),
@@ -928,6 +931,20 @@ def homogenize(cells, spacing=1.0, youngs_modulus=1.0, poisson=0.3, cases=0x3F, 
     return ch, d
 
 
+def host_array(n: int, dtype=np.float64) -> np.ndarray:
+    """A numpy array of ``n`` elements in page-locked host memory (tg_host_alloc),
+    freed when the array is garbage-collected: host buffers the job API copies
+    to and from by direct DMA."""
+    nbytes = int(n) * np.dtype(dtype).itemsize
+    ptr = lib().tg_host_alloc(max(nbytes, 1))
+    if not ptr:
+        raise MemoryError("tg_host_alloc failed")
+    buf = (C.c_char * max(nbytes, 1)).from_address(ptr)
+    arr = np.frombuffer(buf, dtype=dtype, count=int(n))
+    weakref.finalize(buf, lib().tg_host_free, C.c_void_p(ptr))
+    return arr
+
+
 def kernel_launches() -> int:
     return int(lib().tg_kernel_launches())
 
@@ -1120,8 +1137,14 @@ class SimpJob:
         """Run the next steps at stage ``stage`` of the options' projection plan."""
         _check(lib().tg_job_set_stage(self._h, int(stage)))
 
-    def read(self):
-        x, xp = np.zeros(self.pb.nv), np.zeros(self.pb.nv)
+    def read(self, x=None, xp=None):
+        """The design and physical density, into ``x`` / ``xp`` when given
+        (float64 arrays of nv, e.g. host_array buffers) or new arrays."""
+        x = np.zeros(self.pb.nv) if x is None else x
+        xp = np.zeros(self.pb.nv) if xp is None else xp
+        for a in (x, xp):
+            if a.dtype != np.float64 or a.size != self.pb.nv or not a.flags.c_contiguous:
+                raise ValueError("read buffers must be contiguous float64 arrays of nv")
         _check(lib().tg_job_read(self._h, _p(x), _p(xp)))
         return x, xp
 

@@ -1889,6 +1889,22 @@ int tg_job_write_design(tg_job* job, const double* design) {
   });
 }
 
+void* tg_host_alloc(int64_t bytes) {
+  if (bytes <= 0) return nullptr;
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, size_t(bytes), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+int tg_host_free(void* ptr) {
+  return guarded([&] {
+    if (ptr) TG_CUDA(cudaFreeHost(ptr));
+  });
+}
+
 int64_t tg_job_device_bytes(const tg_job* job) { return job ? int64_t(job->bytes()) : 0; }
 
 int64_t tg_job_estimate_bytes(const tg_grid* grid, const tg_simp_options* options) {

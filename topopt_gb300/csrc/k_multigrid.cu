@@ -93,6 +93,8 @@ __device__ __forceinline__ void kron_map(const T (&mw)[3][4], T (&v)[24]) {
 // G_c = W_c^T Ke W_c times f when all 24 are active); deeper levels -- the stored,
 // already masked, child element matrix.  Rows/cols of inactive coarse DOFs are
 // zeroed at the end.
+// With skip set, level 1's elements with skip[ce] < 0 are left to
+// k_galerkin1_fast.
 template <class T, bool LEVEL1>
 __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T* __restrict__ ef,
                                                   const uint8_t* __restrict__ fact,
@@ -100,7 +102,8 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
                                                   const T* __restrict__ Ke,
                                                   const T* __restrict__ G,
                                                   const T* __restrict__ Kf,
-                                                  T* __restrict__ Kc) {
+                                                  T* __restrict__ Kc,
+                                                  const int* __restrict__ skip) {
   constexpr int NW = 4;
   constexpr int LD = 25;  // padded row stride: row and column walks are bank-conflict free
   // Level 1 in FP32: the 8 child blocks G_c live in shared memory (18 KB per CTA).
@@ -118,6 +121,7 @@ __global__ void __launch_bounds__(128) k_galerkin(MgDims fd, MgDims cd, const T*
   }
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
   for (int64_t ce = blockIdx.x * int64_t(NW) + warp; ce < nce; ce += int64_t(gridDim.x) * NW) {
+    if (skip != nullptr && skip[ce] < 0) continue;  // warp-uniform
     const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
               K = int(ce / (int64_t(cd.ex) * cd.ey));
     const int hm = cd.align ? ((2 * I + 1 == fd.ex) | ((2 * J + 1 == fd.ey) << 1) |
@@ -860,11 +864,73 @@ __global__ void k_chol_solve(const double* __restrict__ L, int nc, const int* __
 }
 }  // namespace
 
+// Level 1's Galerkin matrices of the coarse elements on the fast path
+// (spos[ce] < 0: no aligned half element, every coarse DOF active, every fine
+// DOF of every existing child kept), where the matrix is sum_c f_c G_c.  The
+// sum runs over the children inside the grid with a nonzero modulus, in child
+// order, one fused multiply-add per term -- k_galerkin's arithmetic, so the
+// entries are bit-identical -- with one thread per entry: the 576 entries of
+// an element are 576 consecutive floats written by consecutive threads, and the
+// kernel runs at the speed of writing the 2.3 KB per element.
+constexpr int kGalFastElems = 8;  // elements per block step
+__global__ void __launch_bounds__(256) k_galerkin1_fast(MgDims fd, MgDims cd,
+                                                        const float* __restrict__ ef,
+                                                        const int* __restrict__ spos,
+                                                        const float* __restrict__ G,
+                                                        float* __restrict__ Kc) {
+  __shared__ float sG[8 * 576];
+  __shared__ float sf[kGalFastElems][8];
+  __shared__ int sfast[kGalFastElems];
+  for (int e = threadIdx.x; e < 8 * 576; e += blockDim.x) sG[e] = G[e];
+  const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
+  for (int64_t base = int64_t(blockIdx.x) * kGalFastElems; base < nce;
+       base += int64_t(gridDim.x) * kGalFastElems) {
+    __syncthreads();  // sG loaded; the previous step's sf / sfast consumed
+    if (threadIdx.x < kGalFastElems * 8) {
+      const int el = threadIdx.x >> 3, ch = threadIdx.x & 7;
+      const int64_t ce = base + el;
+      float f = 0.0f;
+      if (ce < nce) {
+        const int I = int(ce % cd.ex), J = int((ce / cd.ex) % cd.ey),
+                  K = int(ce / (int64_t(cd.ex) * cd.ey));
+        const int fi = 2 * I + cx(ch), fj = 2 * J + cy(ch), fk = 2 * K + cz(ch);
+        if (fi < fd.ex && fj < fd.ey && fk < fd.ez) f = ef[(int64_t(fk) * fd.ey + fj) * fd.ex + fi];
+      }
+      sf[el][ch] = f;
+      if (ch == 0) sfast[el] = ce < nce && spos[ce] < 0;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < kGalFastElems * 576; q += blockDim.x) {
+      const int el = q / 576, rc = q - el * 576;
+      if (!sfast[el]) continue;
+      float acc = 0.0f;
+#pragma unroll
+      for (int ch = 0; ch < 8; ++ch) {
+        const float f = sf[el][ch];
+        if (f != 0.0f) acc = __fmaf_rn(f, sG[ch * 576 + rc], acc);
+      }
+      Kc[(base + el) * 576 + rc] = acc;
+    }
+  }
+}
+
 template <class T>
 void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const T* ef, const uint8_t* fact,
-                        const uint8_t* cact, const T* Ke, const T* G, T* Kc, cudaStream_t s) {
+                        const uint8_t* cact, const T* Ke, const T* G, T* Kc, cudaStream_t s,
+                        const int* spos) {
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
-  k_galerkin<T, true><<<nblk(nce, 4), 128, 0, s>>>(fd, cd, ef, fact, cact, Ke, G, nullptr, Kc);
+  const int* skip = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    if (spos != nullptr) {
+      const int64_t steps = (nce + kGalFastElems - 1) / kGalFastElems;
+      const int nb = int(std::min<int64_t>(steps, 152 * 16));
+      k_galerkin1_fast<<<nb, 256, 0, s>>>(fd, cd, ef, spos, G, Kc);
+      TG_LAUNCH_CHECK();
+      skip = spos;
+    }
+  }
+  k_galerkin<T, true><<<nblk(nce, 4), 128, 0, s>>>(fd, cd, ef, fact, cact, Ke, G, nullptr, Kc,
+                                                   skip);
   TG_LAUNCH_CHECK();
 }
 
@@ -873,7 +939,7 @@ void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const T* Kf, const u
                         T* Kc, cudaStream_t s) {
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
   k_galerkin<T, false><<<nblk(nce, 4), 128, 0, s>>>(fd, cd, nullptr, nullptr, cact, nullptr,
-                                                    nullptr, Kf, Kc);
+                                                    nullptr, Kf, Kc, nullptr);
   TG_LAUNCH_CHECK();
 }
 
@@ -1038,7 +1104,8 @@ void mg_chol_solve(const double* L, int nc, const int* cidx, int64_t ndof, const
   template void mg_coarse_inv_apply<T>(const double*, int, const int*, const int*, int64_t,    \
                                        const T*, T*, cudaStream_t);                           \
   template void mg_galerkin_level1<T>(const MgDims&, const MgDims&, const T*, const uint8_t*,  \
-                                      const uint8_t*, const T*, const T*, T*, cudaStream_t);  \
+                                      const uint8_t*, const T*, const T*, T*, cudaStream_t,   \
+                                      const int*);                                            \
   template void mg_galerkin_coarse<T>(const MgDims&, const MgDims&, const T*, const uint8_t*,  \
                                       T*, cudaStream_t);                                      \
   template void mg_assemble_stencil<T>(const MgDims&, const T*, const uint8_t*, T*, T*,       \

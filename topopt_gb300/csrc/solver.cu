@@ -788,7 +788,8 @@ bool Solver::build_numeric() {
     L.ensure<T>();
     if (l == 0)
       mg_galerkin_level1<T>(fd, L.d, ef, fp_.kept.p, L.act.p, pick<T>(keb_, kebf_),
-                            pick<T>(G_, Gf_), L.Ke<T>(), s_);
+                            pick<T>(G_, Gf_), L.Ke<T>(), s_,
+                            sizeof(T) == 4 && l1_tc_ ? spos1_.p : nullptr);
     else
       mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
     // Level 1 on the tensor cores needs only its inverse diagonal; the assembled

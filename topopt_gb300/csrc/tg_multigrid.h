@@ -23,9 +23,13 @@ struct MgDims {
   int align = 0;
 };
 
+// spos (FP32, optional): per coarse element, < 0 on the fast path (sum_c f_c G_c;
+// the level-1 tensor-core operator's special-element positions), where a
+// bandwidth-bound kernel forms the matrix.
 template <class T>
 void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const T* ef, const uint8_t* fact,
-                        const uint8_t* cact, const T* Ke, const T* G, T* Kc, cudaStream_t s);
+                        const uint8_t* cact, const T* Ke, const T* G, T* Kc, cudaStream_t s,
+                        const int* spos = nullptr);
 template <class T>
 void mg_galerkin_coarse(const MgDims& fd, const MgDims& cd, const T* Kf, const uint8_t* cact,
                         T* Kc, cudaStream_t s);
