@@ -140,13 +140,19 @@ __device__ __forceinline__ float cg_alpha_f(const double* rz, const double* pap)
   const double pp = *pap;
   return float((pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0);
 }
+// With x0 set, also x0 = omega invdiag .* r (the next V-cycle's first smoothing
+// sweep from zero, as k_jacobi_first computes it).
 __global__ void k_cg_update_r_f(float* __restrict__ r, const float* __restrict__ ap,
                                 const double* __restrict__ rz, const double* __restrict__ pap,
-                                int64_t n, double* __restrict__ part) {
+                                int64_t n, double* __restrict__ part,
+                                const float* __restrict__ invdiag, float omega,
+                                float* __restrict__ x0) {
   const float af = cg_alpha_f(rz, pap);
   const int64_t n4 = n >> 2;
   float4* r4 = reinterpret_cast<float4*>(r);
   const float4* a4 = reinterpret_cast<const float4*>(ap);
+  const float4* d4 = reinterpret_cast<const float4*>(invdiag);
+  float4* x4 = reinterpret_cast<float4*>(x0);
   float tf = 0.0f;
   for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n4;
        i += int64_t(gridDim.x) * kThreads) {
@@ -155,6 +161,11 @@ __global__ void k_cg_update_r_f(float* __restrict__ r, const float* __restrict__
     rv.x -= af * qv.x; rv.y -= af * qv.y; rv.z -= af * qv.z; rv.w -= af * qv.w;
     r4[i] = rv;
     tf += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+    if (x0 != nullptr) {
+      const float4 dv = d4[i];
+      x4[i] = make_float4(omega * dv.x * rv.x, omega * dv.y * rv.y, omega * dv.z * rv.z,
+                          omega * dv.w * rv.w);
+    }
   }
   float t = tf;
   for (int64_t i = (n4 << 2) + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
@@ -162,6 +173,7 @@ __global__ void k_cg_update_r_f(float* __restrict__ r, const float* __restrict__
     const float ri = r[i] - af * ap[i];
     r[i] = ri;
     t += ri * ri;
+    if (x0 != nullptr) x0[i] = omega * invdiag[i] * ri;
   }
   const double s = block_sum256(double(t));
   if (threadIdx.x == 0) part[blockIdx.x] = s;
@@ -378,8 +390,10 @@ template void launch_cg_update_xr<float>(float*, float*, const float*, const flo
                                          cudaStream_t);
 
 void launch_cg_update_r_f(float* r, const float* ap, const double* rz, const double* pap,
-                          int64_t n, double* rr_part, cudaStream_t s) {
-  k_cg_update_r_f<<<kRedBlocks, kThreads, 0, s>>>(r, ap, rz, pap, n, rr_part);
+                          int64_t n, double* rr_part, cudaStream_t s, const float* invdiag,
+                          float omega, float* x0) {
+  k_cg_update_r_f<<<kRedBlocks, kThreads, 0, s>>>(r, ap, rz, pap, n, rr_part, invdiag, omega,
+                                                  x0);
   TG_LAUNCH_CHECK();
 }
 void launch_cg_update_x_f(float* x, const float* p, const double* rz, const double* pap,

@@ -1005,8 +1005,8 @@ float* Solver::fused_coarse_vcycle() {
 }
 
 template <>
-double* Solver::vcycle<double>(const double* b, double* bz) {
-  if (bz != nullptr) raise(TG_EINVAL, "vcycle<double>: no fused b.z");
+double* Solver::vcycle<double>(const double* b, double* bz, bool x0_ready) {
+  if (bz != nullptr || x0_ready) raise(TG_EINVAL, "vcycle<double>: no fused b.z or first sweep");
   const Grid& g = fp_.g;
   Level& N = *levels_[0];
   const MgDims fd = dims_of(g.nx, g.ny, g.nz);
@@ -1032,8 +1032,10 @@ double* Solver::vcycle<double>(const double* b, double* bz) {
 
 template <>
 // With bz set, b . z of the returned z is summed into *bz (device): the last
-// smoothing sweep accumulates it while it writes z.
-float* Solver::vcycle<float>(const float* b, double* bz) {
+// smoothing sweep accumulates it while it writes z.  With x0_ready the first
+// sweep from zero, omega D^-1 b, is already in t1f_ (the PCG's r update wrote
+// it).
+float* Solver::vcycle<float>(const float* b, double* bz, bool x0_ready) {
   const Grid& g = fp_.g;
   Level& N = *levels_[0];
   const MgDims fd = dims_of(g.nx, g.ny, g.nz);
@@ -1048,7 +1050,7 @@ float* Solver::vcycle<float>(const float* b, double* bz) {
     if (part != nullptr) launch_sum_partials(part_.p, nb, bz, s_);
     std::swap(x, r);
   };
-  mg_jacobi_first<float>(b, invdiagf_.p, w, g.ndof, x, s_);
+  if (!x0_ready) mg_jacobi_first<float>(b, invdiagf_.p, w, g.ndof, x, s_);
   for (int k = 1; k < sweeps_; ++k) smooth(false);
   launch_fine_op<float>(kResidual, g, fp_.mc, Ef_.p, fp_.kept.p, x, b, invdiagf_.p, w, r, nullptr,
                         nullptr, s_, fp_.kept_node.p);
@@ -1168,7 +1170,7 @@ bool Solver::build_inner_graph() {
     bool cap_ok = true;
     try {
       pending_x_ = true;  // every body execution starts with the last one's x update
-      float* z = vcycle<float>(rf_.p, scal_.p + 9);
+      float* z = vcycle<float>(rf_.p, scal_.p + 9, true);
       flush_x();
       launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
       TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice,
@@ -1177,7 +1179,8 @@ bool Solver::build_inner_graph() {
       launch_fine_op<float>(kApply, g, fp_.mc, Ef_.p, fp_.kept.p, pf_.p, nullptr, nullptr, 0.0f,
                             apf_.p, part_.p, &nb, s_, fp_.kept_node.p);
       launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
-      launch_cg_update_r_f(rf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);
+      launch_cg_update_r_f(rf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_, invdiagf_.p,
+                           float(omega_), t1f_.p);
       launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
       k_inner_cond<<<1, 1, 0, s_>>>(h, scal_.p, istate_.p);
       TG_LAUNCH_CHECK();
@@ -1223,7 +1226,8 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
     launch_sum_partials(part_.p, nb, scal_.p + 7, s_);
     // r now; x += alpha p when p is next overwritten or at exit (flush_x), or on
     // the side stream beside the next V-cycle's coarse levels (fork_x).
-    launch_cg_update_r_f(rf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_);
+    launch_cg_update_r_f(rf_.p, apf_.p, scal_.p + 6, scal_.p + 7, n, part_.p, s_, invdiagf_.p,
+                         float(omega_), t1f_.p);
     pending_x_ = true;
     launch_sum_partials(part_.p, kRedBlocks, scal_.p + 8, s_);
     double sc[2];
@@ -1260,7 +1264,7 @@ bool Solver::inner_pcg<float>(int max_it, double rel_tol, SolverStats& st, int* 
       if (broke) ++st.inner_breakdowns;
       return true;
     }
-    z = vcycle<float>(rf_.p, scal_.p + 9);
+    z = vcycle<float>(rf_.p, scal_.p + 9, true);
     flush_x();
     launch_cg_update_p<float>(pf_.p, z, scal_.p + 9, scal_.p + 6, n, s_);
     TG_CUDA(cudaMemcpyAsync(scal_.p + 6, scal_.p + 9, sizeof(double), cudaMemcpyDeviceToDevice, s_));

@@ -233,8 +233,11 @@ void launch_cg_update_xr(T* x, T* r, const T* p, const T* ap, const double* rz,
                          const double* pap, int64_t n, double* rr_part, cudaStream_t s);
 // The FP32 PCG update split in two (same alpha, same arithmetic as
 // launch_cg_update_xr<float>): r -= alpha Ap with partials of r.r, and x += alpha p.
+// With x0 set, launch_cg_update_r_f also writes x0 = omega invdiag .* r.
 void launch_cg_update_r_f(float* r, const float* ap, const double* rz, const double* pap,
-                          int64_t n, double* rr_part, cudaStream_t s);
+                          int64_t n, double* rr_part, cudaStream_t s,
+                          const float* invdiag = nullptr, float omega = 0.0f,
+                          float* x0 = nullptr);
 void launch_cg_update_x_f(float* x, const float* p, const double* rz, const double* pap,
                           int64_t n, cudaStream_t s);
 void launch_scale_mask(double* z, const double* r, const double* invdiag, int64_t n,

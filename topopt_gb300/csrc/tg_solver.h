@@ -88,7 +88,7 @@ class Solver {
   bool jacobi_pcg(double tol, int max_it, bool warm, SolverStats& st);
   bool mixed_refine(double tol, int max_it, bool warm, SolverStats& st);
   template <class T>
-  T* vcycle(const T* b, double* bz = nullptr);
+  T* vcycle(const T* b, double* bz = nullptr, bool x0_ready = false);
   template <class T>
   T* vcycle_level(size_t l, bool first_done = false);  // returns the level's result buffer
   template <class T>
