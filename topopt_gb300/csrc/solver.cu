@@ -382,6 +382,12 @@ struct Solver::InnerGraph {
 
 Solver::~Solver() {
   ig_.reset();
+  for (size_t i = 0; i < pi_streams_.size(); ++i) {
+    cudaStreamSynchronize(pi_streams_[i]);
+    cudaStreamDestroy(pi_streams_[i]);
+    cudaEventDestroy(pi_events_[i]);
+  }
+  if (pi_fork_) cudaEventDestroy(pi_fork_);
   if (s2_) {
     cudaStreamSynchronize(s2_);
     cudaEventDestroy(ev_fork_);
@@ -401,7 +407,8 @@ size_t Solver::device_bytes() const {
   for (const DBuf<float>* d : {&Ef_, &invdiagf_, &xf_, &rf_, &zf_, &pf_, &apf_, &t0f_, &t1f_})
     b += d->bytes();
   for (const auto& L : levels_) b += L->bytes();
-  b += spos1_.bytes() + slist1_.bytes() + yspec1_.bytes() + tc_err_.bytes() + chc_.bytes();
+  b += spos1_.bytes() + slist1_.bytes() + yspec1_.bytes() + tc_err_.bytes() + chc_.bytes() +
+       pipart_.bytes();
   return b + cidx_.bytes() + kebf_.bytes() + Gf_.bytes();
 }
 
@@ -802,16 +809,28 @@ bool Solver::build_numeric() {
   }
   if (sizeof(T) == 4 && cheb_m_ > 0) {
     // lambda_max(D^-1 A) of every smoothed level >= 2 for its Chebyshev smoother.
-    if (!lam_.p) lam_.alloc(levels_.size() + 1);
-    if (!chc_.p) chc_.alloc(kChebCoefStride * (levels_.size() + 1));
-    if (!pi_.p) pi_.alloc(1);
-    for (size_t li = 1; li + 1 < levels_.size(); ++li) {
+    // The levels' power iterations are independent chains of small launches
+    // (10 steps of 5 each); they run side by side, one stream per level, each
+    // with its own partials, and rejoin the solver's stream.
+    const size_t nlev = levels_.size();
+    if (!lam_.p) lam_.alloc(nlev + 1);
+    if (!chc_.p) chc_.alloc(kChebCoefStride * (nlev + 1));
+    constexpr size_t kPiStride = size_t(kRedBlocks) + 8;  // partials, then the norm
+    if (!pipart_.p) pipart_.alloc((nlev + 1) * kPiStride);
+    ensure_pi_streams(nlev);
+    TG_CUDA(cudaEventRecord(pi_fork_, s_));
+    for (size_t li = 1; li + 1 < nlev; ++li) {
       Level& L = *levels_[li];
       if (!L.chd.p) L.chd.alloc(size_t(L.ndof));
+      cudaStream_t ls = pi_streams_[li];
+      double* part = pipart_.p + li * kPiStride;
+      TG_CUDA(cudaStreamWaitEvent(ls, pi_fork_, 0));
       mg_lambda_max<float>(L.d, L.Am<float>(), L.act.p, L.Dinv<float>(), L.X<float>(),
-                           L.R<float>(), cheb_iters_, cheb_safety_, part_.p, pi_.p,
-                           lam_.p + li, s_);
-      mg_cheb_table(lam_.p + li, cheb_ratio_, cheb_m_, chc_.p + kChebCoefStride * li, s_);
+                           L.R<float>(), cheb_iters_, cheb_safety_, part, part + kRedBlocks,
+                           lam_.p + li, ls);
+      mg_cheb_table(lam_.p + li, cheb_ratio_, cheb_m_, chc_.p + kChebCoefStride * li, ls);
+      TG_CUDA(cudaEventRecord(pi_events_[li], ls));
+      TG_CUDA(cudaStreamWaitEvent(s_, pi_events_[li], 0));
     }
   }
   Level& C = *levels_.back();
@@ -847,6 +866,20 @@ FirstStep<T> Solver::first_step(size_t l) {
     f.x = L.X<T>();
   }
   return f;
+}
+
+// One stream and event per level for the power iterations of the hierarchy
+// build (never inside a capture), and the event they fork from.
+void Solver::ensure_pi_streams(size_t nlev) {
+  if (!pi_fork_) TG_CUDA(cudaEventCreateWithFlags(&pi_fork_, cudaEventDisableTiming));
+  while (pi_streams_.size() < nlev) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    TG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    TG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    pi_streams_.push_back(st);
+    pi_events_.push_back(ev);
+  }
 }
 
 // The side stream (lowest priority) and its two events; created before any

@@ -115,7 +115,12 @@ class Solver {
   double cheb_ratio_ = 30.0;
   int cheb_iters_ = 10;
   double cheb_safety_ = 1.1;
-  DBuf<double> lam_, pi_;  // lambda_max per level; the power iteration's norm
+  DBuf<double> lam_;     // lambda_max per level
+  DBuf<double> pipart_;  // per level: the power iteration's partials and norm
+  std::vector<cudaStream_t> pi_streams_;  // per level, the power iterations' streams
+  std::vector<cudaEvent_t> pi_events_;
+  cudaEvent_t pi_fork_ = nullptr;
+  void ensure_pi_streams(size_t nlev);
   DBuf<float> chc_;        // Chebyshev coefficients per level (kChebCoefStride each)
   void refinement_residual();  // r = b - A x (FP64 in, FP64 out) for the mixed loop
   bool mixed_ = false;
