@@ -957,7 +957,7 @@ void launch_fine_op(int mode, const Grid& g, const ModalConsts& c, const T* ef,
                     T* y, double* dot_part, int* nblocks_out, cudaStream_t s,
                     const uint8_t* kn) {
   if constexpr (std::is_same<T, float>::value) {
-    launch_fine_op_sched(fine_schedule_for(g), mode, g, c, ef, kept, x, b, invdiag, omega, y,
+    launch_fine_op_sched(fine_schedule_for(g, mode), mode, g, c, ef, kept, x, b, invdiag, omega, y,
                          dot_part, nblocks_out, s, kn);
     return;
   }

@@ -363,8 +363,10 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
     if (fp.g.nv >= kAutotuneMinVoxels && !fine_schedule_known(fp.g)) {
       launch_fill<float>(Ef_.p, 1.0f, fp.g.nv, s_);
       launch_fill<float>(pf_.p, 1.0f, fp.g.ndof, s_);
+      launch_fill<float>(t0f_.p, 0.5f, fp.g.ndof, s_);
+      launch_fill<float>(t1f_.p, 0.25f, fp.g.ndof, s_);
       autotune_fine_schedule(fp.g, fp.mc, Ef_.p, fp.kept.p, fp.kept_node.p, pf_.p, apf_.p,
-                             part_.p, s_);
+                             part_.p, s_, t0f_.p, t1f_.p);
     }
   }
   if (opt.solver == TG_SOLVER_MGCG) build_structure();

@@ -179,20 +179,24 @@ int fine_schedule_shapes();
 bool fine_schedule_valid(const FineSchedule& s);
 // The schedule the FP32 operator uses on g: a process-wide override when one is
 // set, else the table entry for g's dimensions (tune.cu), else the default.
-FineSchedule fine_schedule_for(const Grid& g);
+FineSchedule fine_schedule_for(const Grid& g, int mode = kApply);
 void set_fine_schedule_override(const FineSchedule* s);  // null clears
-void set_fine_schedule(const Grid& g, const FineSchedule& s);
+void set_fine_schedule(const Grid& g, const FineSchedule& s, int mode);
 bool fine_schedule_known(const Grid& g);  // in the table, or an override is set
 // The FP32 operator under an explicit schedule.
 void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const ModalConsts& c,
                           const float* ef, const uint8_t* kept, const float* x, const float* b,
                           const float* invdiag, float omega, float* y, double* dot_part,
                           int* nblocks_out, cudaStream_t s, const uint8_t* kn);
-// Times every candidate schedule of the FP32 apply on the given buffers (CUDA
-// events on s), stores the fastest in the table for g and returns it.
+// Times every candidate schedule of the FP32 operator on the given buffers
+// (CUDA events on s) for the apply and, with b and invdiag, the residual and
+// smoothing modes; stores the fastest per mode in the table for g and returns
+// the apply's.
 FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const float* ef,
                                     const uint8_t* kept, const uint8_t* kn, const float* x,
-                                    float* y, double* part, cudaStream_t s, int reps = 3);
+                                    float* y, double* part, cudaStream_t s,
+                                    const float* b = nullptr, const float* invdiag = nullptr,
+                                    int reps = 3);
 // Whether the mixed form's V-cycle applies its level-1 operator on the tensor
 // cores (k_coarse_tc.cu) instead of the assembled FP32 stencil; on by default.
 bool level1_tc_enabled();

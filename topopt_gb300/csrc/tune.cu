@@ -19,16 +19,18 @@ namespace tg {
 namespace {
 
 std::mutex g_sched_mu;
-std::map<std::tuple<int, int, int>, FineSchedule> g_sched;
+// (nx, ny, nz, mode): the apply, residual and smoothing modes read different
+// vectors and are tuned separately.
+std::map<std::tuple<int, int, int, int>, FineSchedule> g_sched;
 bool g_have_override = false;
 FineSchedule g_override;
 
 }  // namespace
 
-FineSchedule fine_schedule_for(const Grid& g) {
+FineSchedule fine_schedule_for(const Grid& g, int mode) {
   std::lock_guard<std::mutex> lk(g_sched_mu);
   if (g_have_override) return g_override;
-  auto it = g_sched.find(std::make_tuple(g.nx, g.ny, g.nz));
+  auto it = g_sched.find(std::make_tuple(g.nx, g.ny, g.nz, mode));
   if (it != g_sched.end()) return it->second;
   return default_fine_schedule(g);
 }
@@ -39,25 +41,28 @@ void set_fine_schedule_override(const FineSchedule* s) {
   if (s) g_override = *s;
 }
 
-void set_fine_schedule(const Grid& g, const FineSchedule& s) {
+void set_fine_schedule(const Grid& g, const FineSchedule& s, int mode) {
   std::lock_guard<std::mutex> lk(g_sched_mu);
-  g_sched[std::make_tuple(g.nx, g.ny, g.nz)] = s;
+  g_sched[std::make_tuple(g.nx, g.ny, g.nz, mode)] = s;
 }
 
 bool fine_schedule_known(const Grid& g) {
   std::lock_guard<std::mutex> lk(g_sched_mu);
-  return g_have_override || g_sched.count(std::make_tuple(g.nx, g.ny, g.nz)) != 0;
+  return g_have_override || g_sched.count(std::make_tuple(g.nx, g.ny, g.nz, int(kApply))) != 0;
 }
 
 // The measured sweep: every column tile shape with z-chunks of about 8 .. 33
 // element layers, and the pencil kernel, each launched once untimed and then
-// timed over `reps` back-to-back launches of the apply (with the kept mask and
-// the p.Ap partials, as the inner PCG runs it).  The fastest goes into the
-// table for g's dimensions.  Results of every candidate agree to FP32
-// rounding, so the choice changes timing only.
+// timed over `reps` back-to-back launches, for each of the three modes as the
+// mixed solve runs them: the apply with the kept mask and the p.Ap partials,
+// the residual, and the smoothing sweep with its b.y partials (b, invdiag:
+// any finite vectors).  The fastest per mode goes into the table for g's
+// dimensions.  Results of every candidate agree to FP32 rounding, so the
+// choice changes timing only.  Returns the apply's choice.
 FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const float* ef,
                                     const uint8_t* kept, const uint8_t* kn, const float* x,
-                                    float* y, double* part, cudaStream_t s, int reps) {
+                                    float* y, double* part, cudaStream_t s, const float* b,
+                                    const float* invdiag, int reps) {
   std::vector<FineSchedule> cands;
   FineSchedule pencil;
   pencil.kind = FineSchedule::kPencil;
@@ -76,31 +81,37 @@ FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const 
       c.kz = kz;
       cands.push_back(c);
     }
-  cudaEvent_t a, b;
-  TG_CUDA(cudaEventCreate(&a));
-  TG_CUDA(cudaEventCreate(&b));
-  FineSchedule best = default_fine_schedule(g);
-  float best_ms = 1e30f;
-  for (const FineSchedule& c : cands) {
-    launch_fine_op_sched(c, kApply, g, mc, ef, kept, x, nullptr, nullptr, 0.0f, y, part, nullptr,
-                         s, kn);
-    TG_CUDA(cudaEventRecord(a, s));
-    for (int r = 0; r < reps; ++r)
-      launch_fine_op_sched(c, kApply, g, mc, ef, kept, x, nullptr, nullptr, 0.0f, y, part,
-                           nullptr, s, kn);
-    TG_CUDA(cudaEventRecord(b, s));
-    TG_CUDA(cudaEventSynchronize(b));
-    float ms = 0.0f;
-    TG_CUDA(cudaEventElapsedTime(&ms, a, b));
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = c;
+  cudaEvent_t ea, eb;
+  TG_CUDA(cudaEventCreate(&ea));
+  TG_CUDA(cudaEventCreate(&eb));
+  FineSchedule best_apply = default_fine_schedule(g);
+  for (int mode : {int(kApply), int(kResidual), int(kSmooth)}) {
+    if (mode != kApply && (b == nullptr || invdiag == nullptr)) continue;
+    const float* bb = mode == kApply ? nullptr : b;
+    const float* dd = mode == kSmooth ? invdiag : nullptr;
+    double* pp = mode == kResidual ? nullptr : part;
+    FineSchedule best = default_fine_schedule(g);
+    float best_ms = 1e30f;
+    for (const FineSchedule& c : cands) {
+      launch_fine_op_sched(c, mode, g, mc, ef, kept, x, bb, dd, 0.6f, y, pp, nullptr, s, kn);
+      TG_CUDA(cudaEventRecord(ea, s));
+      for (int r = 0; r < reps; ++r)
+        launch_fine_op_sched(c, mode, g, mc, ef, kept, x, bb, dd, 0.6f, y, pp, nullptr, s, kn);
+      TG_CUDA(cudaEventRecord(eb, s));
+      TG_CUDA(cudaEventSynchronize(eb));
+      float ms = 0.0f;
+      TG_CUDA(cudaEventElapsedTime(&ms, ea, eb));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
     }
+    set_fine_schedule(g, best, mode);
+    if (mode == kApply) best_apply = best;
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  set_fine_schedule(g, best);
-  return best;
+  cudaEventDestroy(ea);
+  cudaEventDestroy(eb);
+  return best_apply;
 }
 
 namespace {
