@@ -735,11 +735,12 @@ int tg_set_coarse_fused(int32_t on);
  * (0 <= shape < 8: Y x W element rows per thread x warps per CTA of 4x4, 6x4,
  * 3x4, 2x8 for shapes 0-3, the same tiles with the x and y components in
  * paired FP32 instructions for shapes 4-7) and `kz` >= 8 element layers per
- * CTA.  The setting overrides the
- * per-grid table for every later FP32 launch in the process; kind < 0 clears
- * it.  Results of every schedule agree to FP32 rounding. */
+ * CTA.  The setting overrides the per-grid, per-mode table (apply, residual,
+ * smoothing; measured on the first large mixed job of a grid) for every later
+ * FP32 launch in the process; kind < 0 clears it.  Results of every schedule
+ * agree to FP32 rounding. */
 int tg_set_fp32_schedule(int32_t kind, int32_t shape, int32_t kz);
-/* The FP32 schedule the operator uses on an nx x ny x nz grid now. */
+/* The FP32 schedule the operator's apply mode uses on an nx x ny x nz grid now. */
 int tg_fp32_schedule(int32_t nx, int32_t ny, int32_t nz, int32_t* kind, int32_t* shape,
                      int32_t* kz);
 /* FMA microbenchmark: sustained FP64 and FP32 FMA throughput of the device in
