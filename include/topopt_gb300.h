@@ -117,7 +117,7 @@ typedef struct {
   int32_t coarse_smoother; /* mixed: the smoother of the FP32 V-cycle's levels >= 2:
                               TG_SMOOTHER_AUTO (0) Chebyshev on grids of >= 200K elements,
                               Jacobi below; TG_SMOOTHER_JACOBI (1) damped Jacobi (the
-                              reference's); TG_SMOOTHER_CHEBYSHEV (2) a degree-3 Chebyshev
+                              reference's); TG_SMOOTHER_CHEBYSHEV (2) a degree-4 Chebyshev
                               polynomial in D^-1 A on [lmax / 30, lmax], lmax by power
                               iteration per hierarchy build.  The FP64 V-cycle always uses
                               damped Jacobi. */

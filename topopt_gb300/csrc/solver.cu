@@ -343,7 +343,7 @@ Solver::Solver(const FineProblem& fp, const tg_solve_options& opt, cudaStream_t 
   // more than the PCG iterations they save), damped Jacobi otherwise.
   const bool cheb = opt.coarse_smoother == TG_SMOOTHER_CHEBYSHEV ||
                     (opt.coarse_smoother == TG_SMOOTHER_AUTO && fp.g.nv >= 200000);
-  cheb_m_ = (mixed_ && cheb) ? 3 : 0;
+  cheb_m_ = (mixed_ && cheb) ? 4 : 0;
   const size_t n = size_t(fp.g.ndof);
   for (DBuf<double>* b : {&invdiag_, &rhs_, &x_, &r_, &z_, &p_, &ap_, &t0_, &t1_}) b->alloc(n);
   part_n_ = std::max({kRedBlocks, fine_op_blocks(fp.g, true), fine_op_blocks(fp.g, false),

@@ -53,7 +53,7 @@ struct ChebStep {
 // Computed once per hierarchy build: the smoothing kernels read them instead of
 // evaluating the FP64 recurrence in every thread (GB300's FP64 rate is 1/64 of
 // its FP32 rate).
-constexpr int kChebCoefStride = 8;
+constexpr int kChebCoefStride = 16;  // up to 8 steps
 void mg_cheb_table(const double* lam, double ratio, int m, float* coef, cudaStream_t s);
 template <class T>
 void mg_stencil_op(int mode, const MgDims& d, const T* A, const uint8_t* act, const T* x,
