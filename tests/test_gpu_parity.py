@@ -1,7 +1,7 @@
 """Parity of the CUDA path (through the C ABI) with the oracle and the golden
 vectors of the reference's own code.  GPU only.
 
-Tolerances (the benchmark spec): compliance within 1e-9 relative and displacement within
+Tolerances: compliance within 1e-9 relative and displacement within
 1e-8 relative max-norm for FP64 solves (both sides solved tighter than that);
 integer and index work (kept-DOF mask) bit-exact; the density filter and the OC
 update bit-exact (they round exactly like the reference).  The operator is a
