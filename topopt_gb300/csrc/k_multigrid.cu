@@ -869,24 +869,27 @@ __global__ void k_chol_solve(const double* __restrict__ L, int nc, const int* __
 // DOF of every existing child kept), where the matrix is sum_c f_c G_c.  The
 // sum runs over the children inside the grid with a nonzero modulus, in child
 // order, one fused multiply-add per term -- k_galerkin's arithmetic, so the
-// entries are bit-identical -- with one thread per entry: the 576 entries of
-// an element are 576 consecutive floats written by consecutive threads, and the
-// kernel runs at the speed of writing the 2.3 KB per element.
-constexpr int kGalFastElems = 8;  // elements per block step
-__global__ void __launch_bounds__(256) k_galerkin1_fast(MgDims fd, MgDims cd,
+// entries are bit-identical.  A block of 576 threads, one per matrix entry,
+// holds its entry of the 8 G_c in registers and walks a batch of elements: the
+// 576 entries of an element are 576 consecutive floats written by consecutive
+// threads.
+constexpr int kGalFastBatch = 32;  // elements per block step
+__global__ void __launch_bounds__(576) k_galerkin1_fast(MgDims fd, MgDims cd,
                                                         const float* __restrict__ ef,
                                                         const int* __restrict__ spos,
                                                         const float* __restrict__ G,
                                                         float* __restrict__ Kc) {
-  __shared__ float sG[8 * 576];
-  __shared__ float sf[kGalFastElems][8];
-  __shared__ int sfast[kGalFastElems];
-  for (int e = threadIdx.x; e < 8 * 576; e += blockDim.x) sG[e] = G[e];
+  __shared__ float sf[kGalFastBatch][8];
+  __shared__ int sfast[kGalFastBatch];
+  const int rc = threadIdx.x;  // this thread's matrix entry, 0 .. 575
+  float g[8];                  // its 8 child blocks' entries, for every element
+#pragma unroll
+  for (int ch = 0; ch < 8; ++ch) g[ch] = G[ch * 576 + rc];
   const int64_t nce = int64_t(cd.ex) * cd.ey * cd.ez;
-  for (int64_t base = int64_t(blockIdx.x) * kGalFastElems; base < nce;
-       base += int64_t(gridDim.x) * kGalFastElems) {
-    __syncthreads();  // sG loaded; the previous step's sf / sfast consumed
-    if (threadIdx.x < kGalFastElems * 8) {
+  for (int64_t base = int64_t(blockIdx.x) * kGalFastBatch; base < nce;
+       base += int64_t(gridDim.x) * kGalFastBatch) {
+    __syncthreads();  // the previous step's sf / sfast consumed
+    if (threadIdx.x < kGalFastBatch * 8) {
       const int el = threadIdx.x >> 3, ch = threadIdx.x & 7;
       const int64_t ce = base + el;
       float f = 0.0f;
@@ -900,14 +903,13 @@ __global__ void __launch_bounds__(256) k_galerkin1_fast(MgDims fd, MgDims cd,
       if (ch == 0) sfast[el] = ce < nce && spos[ce] < 0;
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < kGalFastElems * 576; q += blockDim.x) {
-      const int el = q / 576, rc = q - el * 576;
-      if (!sfast[el]) continue;
+    for (int el = 0; el < kGalFastBatch; ++el) {
+      if (!sfast[el]) continue;  // uniform over the block
       float acc = 0.0f;
 #pragma unroll
       for (int ch = 0; ch < 8; ++ch) {
         const float f = sf[el][ch];
-        if (f != 0.0f) acc = __fmaf_rn(f, sG[ch * 576 + rc], acc);
+        if (f != 0.0f) acc = __fmaf_rn(f, g[ch], acc);
       }
       Kc[(base + el) * 576 + rc] = acc;
     }
@@ -922,9 +924,9 @@ void mg_galerkin_level1(const MgDims& fd, const MgDims& cd, const T* ef, const u
   const int* skip = nullptr;
   if constexpr (sizeof(T) == 4) {
     if (spos != nullptr) {
-      const int64_t steps = (nce + kGalFastElems - 1) / kGalFastElems;
-      const int nb = int(std::min<int64_t>(steps, 152 * 16));
-      k_galerkin1_fast<<<nb, 256, 0, s>>>(fd, cd, ef, spos, G, Kc);
+      const int64_t steps = (nce + kGalFastBatch - 1) / kGalFastBatch;
+      const int nb = int(std::min<int64_t>(steps, 152 * 6));
+      k_galerkin1_fast<<<nb, 576, 0, s>>>(fd, cd, ef, spos, G, Kc);
       TG_LAUNCH_CHECK();
       skip = spos;
     }
