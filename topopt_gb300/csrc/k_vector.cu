@@ -87,6 +87,7 @@ __global__ void k_max_partials(const double* __restrict__ part, int n, double* _
 }
 
 // x += alpha p; r -= alpha Ap with alpha = rz / pAp; partial r.r (FP64 sums).
+// The FP64 PCG's update; the FP32 inner PCG runs it as two kernels below.
 template <class T>
 __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                                const T* __restrict__ ap, const double* __restrict__ rz,
@@ -95,33 +96,9 @@ __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __
   // A non-positive or non-finite pAp is a breakdown the host reports; leave the
   // iterate untouched so the last good x survives.
   const double pp = *pap;
-  const double alpha = (pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0;
-  const T a = T(alpha);
+  const T a = T((pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0);
   T t = T(0);
-  int64_t i0 = 0;
-  if (std::is_same<T, float>::value) {
-    // FP32: 16-byte vector accesses (the buffers are cudaMalloc-aligned).
-    const int64_t n4 = n >> 2;
-    float4* x4 = reinterpret_cast<float4*>(x);
-    float4* r4 = reinterpret_cast<float4*>(r);
-    const float4* p4 = reinterpret_cast<const float4*>(p);
-    const float4* a4 = reinterpret_cast<const float4*>(ap);
-    const float af = float(alpha);
-    float tf = 0.0f;
-    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n4;
-         i += int64_t(gridDim.x) * kThreads) {
-      float4 xv = x4[i], rv = r4[i];
-      const float4 pv = p4[i], qv = a4[i];
-      xv.x += af * pv.x; xv.y += af * pv.y; xv.z += af * pv.z; xv.w += af * pv.w;
-      rv.x -= af * qv.x; rv.y -= af * qv.y; rv.z -= af * qv.z; rv.w -= af * qv.w;
-      x4[i] = xv;
-      r4[i] = rv;
-      tf += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
-    }
-    t = T(tf);
-    i0 = n4 << 2;
-  }
-  for (int64_t i = i0 + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * kThreads) {
     x[i] += a * p[i];
     const T ri = r[i] - a * ap[i];
@@ -132,10 +109,10 @@ __global__ void k_cg_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// The two halves of k_cg_update_xr for the FP32 inner PCG, with its alpha and
-// its arithmetic: r -= alpha Ap with partial r.r, and x += alpha p, which the
-// solver runs later, beside the next V-cycle's coarse levels (nothing in the
-// loop reads x).
+// The FP32 inner PCG's update in two kernels (alpha as k_cg_update_xr forms it,
+// 16-byte vector accesses): r -= alpha Ap with partial r.r, and x += alpha p,
+// which the solver runs later, beside the next V-cycle's coarse levels
+// (nothing in the loop reads x).
 __device__ __forceinline__ float cg_alpha_f(const double* rz, const double* pap) {
   const double pp = *pap;
   return float((pp > 0.0 && isfinite(pp)) ? *rz / pp : 0.0);
@@ -385,9 +362,6 @@ void launch_cg_update_xr(T* x, T* r, const T* p, const T* ap, const double* rz,
 template void launch_cg_update_xr<double>(double*, double*, const double*, const double*,
                                           const double*, const double*, int64_t, double*,
                                           cudaStream_t);
-template void launch_cg_update_xr<float>(float*, float*, const float*, const float*,
-                                         const double*, const double*, int64_t, double*,
-                                         cudaStream_t);
 
 void launch_cg_update_r_f(float* r, const float* ap, const double* rz, const double* pap,
                           int64_t n, double* rr_part, cudaStream_t s, const float* invdiag,

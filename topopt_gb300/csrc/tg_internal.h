@@ -235,8 +235,9 @@ void launch_dot_partials_f(const float* a, const float* b, int64_t n, double* pa
 template <class T>
 void launch_cg_update_xr(T* x, T* r, const T* p, const T* ap, const double* rz,
                          const double* pap, int64_t n, double* rr_part, cudaStream_t s);
-// The FP32 PCG update split in two (same alpha, same arithmetic as
-// launch_cg_update_xr<float>): r -= alpha Ap with partials of r.r, and x += alpha p.
+// The FP32 PCG update in two kernels (alpha = rz / pAp as launch_cg_update_xr
+// forms it, 0 on a breakdown): r -= alpha Ap with partials of r.r, and
+// x += alpha p.
 // With x0 set, launch_cg_update_r_f also writes x0 = omega invdiag .* r.
 void launch_cg_update_r_f(float* r, const float* ap, const double* rz, const double* pap,
                           int64_t n, double* rr_part, cudaStream_t s,
