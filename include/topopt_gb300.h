@@ -724,6 +724,12 @@ int64_t tg_kernel_launches(void);
  * FP32 accuracy); off, as the assembled FP32 node stencil.  Applies to solvers
  * created afterwards. */
 int tg_set_level1_tc(int32_t on);
+/* Level 1's Galerkin matrices in the mixed form with level 1 on the tensor
+ * cores: on (default) the fast-path elements' matrices (sum_c E_c G_c) come
+ * from a bandwidth-bound kernel, the others from the general one; off, all from
+ * the general one.  The matrices are bit-identical either way.  Applies to
+ * hierarchy builds from then on. */
+int tg_set_level1_galerkin_fast(int32_t on);
 /* The mixed form's V-cycle on its small levels (below level 1, from the first
  * level of at most 4096 nodes to the coarsest): on, they run as one launch of
  * one thread-block cluster with the cluster barrier between steps; off

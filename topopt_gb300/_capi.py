@@ -206,6 +206,7 @@ def lib():
         "tg_device_fma_peaks": ([vp, vp], C.c_int),
         "tg_set_fp32_schedule": ([i32, i32, i32], C.c_int),
         "tg_set_level1_tc": ([i32], C.c_int),
+        "tg_set_level1_galerkin_fast": ([i32], C.c_int),
         "tg_set_coarse_fused": ([i32], C.c_int),
         "tg_job_check_level1": ([vp, vp], C.c_int),
         "tg_fp32_schedule": ([i32, i32, i32, vp, vp, vp], C.c_int),
@@ -962,6 +963,12 @@ def set_level1_tc(on: bool):
     """Level 1 of the mixed V-cycle on the tensor cores (True, default) or as the
     assembled FP32 stencil (False), for solvers created afterwards."""
     _check(lib().tg_set_level1_tc(int(bool(on))))
+
+
+def set_level1_galerkin_fast(on: bool):
+    """Level 1's fast-path Galerkin matrices from the bandwidth-bound kernel
+    (True, default) or all from the general kernel (False); bit-identical."""
+    _check(lib().tg_set_level1_galerkin_fast(int(bool(on))))
 
 
 def set_coarse_fused(on: bool):

@@ -1972,6 +1972,10 @@ int tg_set_level1_tc(int32_t on) {
   return guarded([&] { set_level1_tc(on != 0); });
 }
 
+int tg_set_level1_galerkin_fast(int32_t on) {
+  return guarded([&] { set_level1_galerkin_fast(on != 0); });
+}
+
 int tg_set_coarse_fused(int32_t on) {
   return guarded([&] { set_coarse_fused(on != 0); });
 }

@@ -798,7 +798,9 @@ bool Solver::build_numeric() {
     if (l == 0)
       mg_galerkin_level1<T>(fd, L.d, ef, fp_.kept.p, L.act.p, pick<T>(keb_, kebf_),
                             pick<T>(G_, Gf_), L.Ke<T>(), s_,
-                            sizeof(T) == 4 && l1_tc_ ? spos1_.p : nullptr);
+                            sizeof(T) == 4 && l1_tc_ && level1_galerkin_fast_enabled()
+                                ? spos1_.p
+                                : nullptr);
     else
       mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
     // Level 1 on the tensor cores needs only its inverse diagonal; the assembled

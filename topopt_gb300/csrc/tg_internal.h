@@ -201,6 +201,10 @@ FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const 
 // cores (k_coarse_tc.cu) instead of the assembled FP32 stencil; on by default.
 bool level1_tc_enabled();
 void set_level1_tc(bool on);
+// Whether the hierarchy build forms level 1's fast-path Galerkin matrices with
+// the bandwidth-bound kernel (bit-identical to the general one); on by default.
+bool level1_galerkin_fast_enabled();
+void set_level1_galerkin_fast(bool on);
 // Whether the mixed form's V-cycle runs its small levels (from the first one of
 // at most kFusedMaxNodes nodes to the coarsest) as one cluster launch
 // (k_multigrid.cu) instead of a launch per step; off by default.

@@ -119,6 +119,11 @@ std::atomic<bool> g_level1_tc{true};
 }
 bool level1_tc_enabled() { return g_level1_tc.load(); }
 void set_level1_tc(bool on) { g_level1_tc.store(on); }
+namespace {
+std::atomic<bool> g_level1_galerkin_fast{true};
+}
+bool level1_galerkin_fast_enabled() { return g_level1_galerkin_fast.load(); }
+void set_level1_galerkin_fast(bool on) { g_level1_galerkin_fast.store(on); }
 // Off by default: on the 256x128x128 cantilever the cluster launch took 155 us
 // per V-cycle for levels 4..6 against 139 us as separate launches (a fused phase
 // costs ~9 us: one cluster of 16 SMs, L2 round trips on every phase).
