@@ -6,7 +6,7 @@ inputs and outputs as golden.npz.  Only runs where the reference tree is
 available; the committed golden.npz is what the tests read everywhere else.
 
     python tests/golden/make_golden.py                       # everything
-    python tests/golden/make_golden.py --section cfg0_steps  # one section into the existing file
+    python tests/golden/make_golden.py --section cant60_steps  # one section into the existing file
     python tests/golden/make_golden.py --section homog
 """
 from __future__ import annotations
@@ -128,11 +128,11 @@ def main():
     pb0 = cantilever(60, 20, 20)
     s0 = R.simp_optimize(pb0, volfrac=0.3, radius=1.5, move=0.2, max_it=50, change_tol=0.0,
                          cg_tol=1e-10)
-    out.update(cfg0_hist_c=s0["hist_c"], cfg0_hist_change=s0["hist_change"],
-               cfg0_hist_vf=s0["hist_vf"], cfg0_design=s0["design"],
-               cfg0_compliance=np.array(s0["compliance"]),
-               cfg0_iterations=np.array(s0["iterations"]))
-    out.update(_cfg0_steps(R))
+    out.update(cant60_hist_c=s0["hist_c"], cant60_hist_change=s0["hist_change"],
+               cant60_hist_vf=s0["hist_vf"], cant60_design=s0["design"],
+               cant60_compliance=np.array(s0["compliance"]),
+               cant60_iterations=np.array(s0["iterations"]))
+    out.update(_cant60_steps(R))
     out.update(_homog(R))
 
     # Heaviside projection: value and derivative at the fixture's spot values
@@ -281,7 +281,7 @@ def main():
     print("wrote", os.path.join(HERE, "golden.npz"), len(out), "arrays")
 
 
-def _cfg0_steps(R):
+def _cant60_steps(R):
     """Per-step inputs of the 60x20x20 configuration: the reference's physical
     density after 10, 25 and 50 design iterations (its own OC trajectory,
     filtered by its own filter) and its compliance, displacement and
@@ -293,8 +293,8 @@ def _cfg0_steps(R):
                              cg_tol=1e-10)
         xp = R.filter(pb0, sk["design"], 1.5)
         ck = R.simp_compliance(pb0, xp, tol=1e-12)
-        out.update({f"cfg0_it{k}_phys": xp, f"cfg0_it{k}_c": np.array(ck["compliance"]),
-                    f"cfg0_it{k}_u": ck["u"], f"cfg0_it{k}_dc": ck["dc"]})
+        out.update({f"cant60_it{k}_phys": xp, f"cant60_it{k}_c": np.array(ck["compliance"]),
+                    f"cant60_it{k}_u": ck["u"], f"cant60_it{k}_dc": ck["dc"]})
     return out
 
 
@@ -412,7 +412,7 @@ def update_section(name):
     path = os.path.join(HERE, "golden.npz")
     with np.load(path) as z:
         out = {k: z[k] for k in z.files}
-    new = {"cfg0_steps": _cfg0_steps, "homog": _homog}[name](R)
+    new = {"cant60_steps": _cant60_steps, "homog": _homog}[name](R)
     for k, v in new.items():
         if k in out and not np.array_equal(out[k], v, equal_nan=True):
             raise SystemExit(f"golden array {k} changed on regeneration")

@@ -232,7 +232,7 @@ def test_graph_inner_loop_matches_host_loop(tg, dims):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-def test_cfg0_fifty_iterations(tg, golden, prec):
+def test_cant60_fifty_iterations(tg, golden, prec):
     """The reference's CPU-runnable configuration end to end: 60x20x20
     cantilever, volume fraction 0.3, rmin 1.5, move 0.2, 50 design iterations,
     solves at 1e-10 -- against the reference's own 50-iteration run."""
@@ -244,10 +244,10 @@ def test_cfg0_fifty_iterations(tg, golden, prec):
         cg_tolerance=1e-10, solve=tg.SolveOptions(precision=prec)))
     hc = np.array([h["compliance"] for h in s["history"]])
     assert s["iterations"] == 50
-    assert abs(hc[0] - golden["cfg0_hist_c"][0]) <= 1e-9 * hc[0]
-    assert rel(hc, golden["cfg0_hist_c"]) < 1e-6
-    assert rel(s["design"], golden["cfg0_design"]) < 1e-4
-    assert abs(s["compliance"] - float(golden["cfg0_compliance"])) <= 1e-6 * s["compliance"]
+    assert abs(hc[0] - golden["cant60_hist_c"][0]) <= 1e-9 * hc[0]
+    assert rel(hc, golden["cant60_hist_c"]) < 1e-6
+    assert rel(s["design"], golden["cant60_design"]) < 1e-4
+    assert abs(s["compliance"] - float(golden["cant60_compliance"])) <= 1e-6 * s["compliance"]
 
 
 def test_double_float_operator_matches_fp64(tg, golden):

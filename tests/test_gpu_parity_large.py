@@ -43,7 +43,7 @@ MAX_IT = 600
 
 
 @pytest.fixture(scope="module")
-def cfg1(tg):
+def cant256(tg):
     from topopt_gb300.workloads import cantilever_seeded_load
     bcs, loads = cantilever_seeded_load(NX, NY, NZ)
     pb = tg.Problem(NX, NY, NZ, 1.0, None, bcs, loads)
@@ -52,8 +52,8 @@ def cfg1(tg):
     return pb, o, rho
 
 
-def test_cfg1_operator(tg, port, cfg1):
-    pb, o, rho = cfg1
+def test_cant256_operator(tg, port, cant256):
+    pb, o, rho = cant256
     E = rho ** 3
     u = np.random.default_rng(1).standard_normal(pb.ndof)
     ref = port.apply(o, u, E)
@@ -61,16 +61,16 @@ def test_cfg1_operator(tg, port, cfg1):
     assert rel(tg.fea_matfree_apply(pb, u, youngs_per_voxel=E, precision=tg.PREC_MIXED), ref) < 2e-6
 
 
-def test_cfg1_filter_bit_exact(tg, port, cfg1):
-    pb, o, rho = cfg1
+def test_cant256_filter_bit_exact(tg, port, cant256):
+    pb, o, rho = cant256
     f = tg.make_density_filter(pb, 1.5)
     assert np.array_equal(f.filter_density(rho), port.filter(o, rho, 1.5))
     s = -np.random.default_rng(2).random(pb.nv)
     assert np.array_equal(f.filter_sensitivity(s), port.filter(o, s, 1.5, adjoint=True))
 
 
-def test_cfg1_sensitivity_and_oc(tg, port, cfg1):
-    pb, o, rho = cfg1
+def test_cant256_sensitivity_and_oc(tg, port, cant256):
+    pb, o, rho = cant256
     r = tg.simp_compliance(pb, tg.SimpParams(), rho, tolerance=1e-8, max_iterations=MAX_IT)
     c_o, dc_o = port.sensitivity(o, rho, r["u"])
     assert abs(r["compliance"] - c_o) <= 1e-10 * abs(c_o)  # element sums in another order
@@ -80,8 +80,8 @@ def test_cfg1_sensitivity_and_oc(tg, port, cfg1):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-def test_cfg1_solution_true_residual(tg, port, cfg1, prec):
-    pb, o, rho = cfg1
+def test_cant256_solution_true_residual(tg, port, cant256, prec):
+    pb, o, rho = cant256
     E = rho ** 3
     u, info = tg.fea_solve_mgcg_matfree(pb, E, tolerance=5e-9, max_iterations=MAX_IT,
                                         options=tg.SolveOptions(precision=prec))
@@ -94,14 +94,14 @@ def test_cfg1_solution_true_residual(tg, port, cfg1, prec):
 
 @pytest.mark.parametrize("it", [10, 25, 50])
 @pytest.mark.parametrize("prec", [0, 1])
-def test_cfg0_per_step(tg, golden, it, prec):
+def test_cant60_per_step(tg, golden, it, prec):
     o = cantilever(60, 20, 20)
     pb = tg.Problem(60, 20, 20, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
                     list(zip(o.ld_node, o.ld_comp, o.ld_val)))
-    xp = golden[f"cfg0_it{it}_phys"]
+    xp = golden[f"cant60_it{it}_phys"]
     r = tg.simp_compliance(pb, tg.SimpParams(), xp, tolerance=1e-12, max_iterations=MAX_IT,
                            options=tg.SolveOptions(precision=prec))
-    c_ref = float(golden[f"cfg0_it{it}_c"])
+    c_ref = float(golden[f"cant60_it{it}_c"])
     assert abs(r["compliance"] - c_ref) <= 1e-9 * c_ref
-    assert rel(r["u"], golden[f"cfg0_it{it}_u"]) < 1e-8
-    assert rel(r["dcompliance"], golden[f"cfg0_it{it}_dc"]) < 1e-8
+    assert rel(r["u"], golden[f"cant60_it{it}_u"]) < 1e-8
+    assert rel(r["dcompliance"], golden[f"cant60_it{it}_dc"]) < 1e-8

@@ -145,16 +145,16 @@ def test_void_gate_errors(port):
     assert e.value.code == 2 and "void DOF" in str(e.value)
 
 
-def test_cfg0_trajectory_prefix(port, golden):
+def test_cant60_trajectory_prefix(port, golden):
     """The reference's CPU configuration (60x20x20 cantilever, 50 iterations in
     the golden run): the first 10 iterations of the oracle's loop match the
     reference's bit for bit."""
     pb = cantilever(60, 20, 20)
     s = port.simp_optimize(pb, volfrac=0.3, radius=1.5, move=0.2, max_it=10, change_tol=0.0,
                            cg_tol=1e-10)
-    assert np.array_equal(s["hist_c"], golden["cfg0_hist_c"][:10])
-    assert np.array_equal(s["hist_change"], golden["cfg0_hist_change"][:10])
-    assert np.array_equal(s["hist_vf"], golden["cfg0_hist_vf"][:10])
+    assert np.array_equal(s["hist_c"], golden["cant60_hist_c"][:10])
+    assert np.array_equal(s["hist_change"], golden["cant60_hist_change"][:10])
+    assert np.array_equal(s["hist_vf"], golden["cant60_hist_vf"][:10])
 
 
 BENCH_JSON = reference_path("core", "tests", "fixtures", "benchmarks.json")

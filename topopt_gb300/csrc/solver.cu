@@ -804,7 +804,7 @@ bool Solver::build_numeric() {
     else
       mg_galerkin_coarse<T>(pd, L.d, levels_[l - 1]->Ke<T>(), L.act.p, L.Ke<T>(), s_);
     // Level 1 on the tensor cores needs only its inverse diagonal; the assembled
-    // stencil (275 MB on cfg1) is formed on demand (level1_stencil()).
+    // stencil (275 MB on the 256x128x128 cantilever) is formed on demand (level1_stencil()).
     const bool diag_only = sizeof(T) == 4 && l == 0 && l1_tc_;
     mg_assemble_stencil<T>(L.d, L.Ke<T>(), L.act.p, diag_only ? nullptr : L.Am<T>(), L.Dinv<T>(),
                            s_);
