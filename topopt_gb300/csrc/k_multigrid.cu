@@ -1123,10 +1123,11 @@ TG_INST(float)
 // ------------------------------------------------- fused coarse V-cycle
 // The small levels of the FP32 V-cycle -- from the first level with at most
 // kFusedMaxNodes nodes down to the coarsest -- in one launch of one thread-block
-// cluster.  Launch by launch, each step on these levels is a kernel of a few
-// thousand DOFs whose cost is its launch latency (about 7 us per step inside the
-// inner PCG's graph; levels 3..6 of the 256x128x128 cantilever took ~270 us per
-// V-cycle).  Here every step of the same V-cycle is a phase of one kernel -- a
+// cluster (off by default: a launch per step, 3-4 us each with the four-thread
+// stencil kernel, measured faster than a phase of this kernel, ~9 us on 16
+// SMs).  Launch by launch, each step on these levels is a kernel of a few
+// thousand DOFs whose cost is its latency.  Here every step of the same
+// V-cycle is a phase of one kernel -- a
 // cluster-stride loop with the arithmetic and summation order of the separate
 // kernels (stencil_row, restrict_node, prolong_node, the coarsest inverse) --
 // and phases are separated by the cluster's hardware barrier (release/acquire
