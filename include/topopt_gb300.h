@@ -679,7 +679,8 @@ int tg_job_read_displacement(tg_job* job, double* u_out);
 int tg_job_write_design(tg_job* job, const double* design);
 /* Page-locked host memory for the host buffers of the calls above: their copies
  * from and to such a buffer run as direct DMA instead of through a staging
- * copy.  NULL when the allocation fails; free with tg_host_free. */
+ * copy.  NULL when the allocation fails; free with tg_host_free (NULL is a
+ * no-op). */
 void* tg_host_alloc(int64_t bytes);
 int tg_host_free(void* ptr);
 /* Bytes of device memory the job holds. */

@@ -44,6 +44,21 @@ def test_errors_without_device_are_reported_not_fallen_back(tg):
     assert np.array_equal(ke, OracleLib("port").hex8_stiffness(1.0, 0.3, 1.0))
 
 
+def test_page_locked_host_buffers_fail_loudly(tg):
+    """tg_host_alloc returns NULL for a non-positive size and, without a device,
+    for any size; host_array then raises instead of handing out pageable memory.
+    With a device the buffer is a usable float64 array."""
+    lib = tg.lib()
+    assert not lib.tg_host_alloc(0)
+    assert lib.tg_host_free(None) == 0
+    try:
+        a = tg.host_array(16)
+    except MemoryError:
+        return
+    a[:] = 1.0
+    assert a.dtype.name == "float64" and a.sum() == 16.0
+
+
 def test_python_face_mirrors_reference_names(tg):
     for n in ("hex8_stiffness", "fea_matfree_apply", "fea_solve_mgcg_matfree", "simp_compliance",
               "make_density_filter", "oc_update", "simp_optimize", "SimpJob",

@@ -1900,9 +1900,8 @@ void* tg_host_alloc(int64_t bytes) {
 }
 
 int tg_host_free(void* ptr) {
-  return guarded([&] {
-    if (ptr) TG_CUDA(cudaFreeHost(ptr));
-  });
+  if (ptr == nullptr) return TG_OK;  // like free(NULL): no device needed
+  return guarded([&] { TG_CUDA(cudaFreeHost(ptr)); });
 }
 
 int64_t tg_job_device_bytes(const tg_job* job) { return job ? int64_t(job->bytes()) : 0; }
