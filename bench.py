@@ -186,14 +186,31 @@ def sum_over_ranks(pg, v):
 
 
 # ------------------------------------------------------------------ CPU side
+def host_cores():
+    """Host cores this process may run on."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_port():
+    """The oracle's C restatement with its parallel loops on every host core
+    (torchrun exports OMP_NUM_THREADS=1 to its ranks; the CPU legs override it)."""
+    from oracle.oracle import OracleLib
+    port = OracleLib("port")
+    port.set_threads(host_cores())
+    return port
+
+
 def cpu_iterations(nx, ny, nz, n, x0=None, u0=None):
     """Whole design iterations of the benchmark problem on the host cores: the
     oracle's CPU restatement of the reference's MG-PCG design iteration
     (oracle/oracle_mg.c: filter, modulus, reduced system, Galerkin hierarchy,
     MG-PCG warm-started from the previous displacement, sensitivities, OC),
     from design x0 (the uniform start when None) and warm start u0."""
-    from oracle.oracle import OracleLib, Problem
-    port = OracleLib("port")
+    from oracle.oracle import Problem
+    port = oracle_port()
     bcs, loads = cantilever_random_load(nx, ny, nz)
     o = Problem(nx, ny, nz, 1.0, None, bcs, loads)
     x = np.full(o.nv, 0.3) if x0 is None else x0
@@ -428,8 +445,7 @@ def _cpu_design_sample(designs, iters):
     """Whole OC design iterations of a few designs on the host cores, one design
     at a time: the oracle's CPU restatement of the reference's MG-PCG design
     iteration.  Returns (iterations/s, cores, note)."""
-    from oracle.oracle import OracleLib
-    port = OracleLib("port")
+    port = oracle_port()
     n, t = 0, 0.0
     for pb, prm, opt in designs:
         o = _oracle_problem(pb)
@@ -550,16 +566,16 @@ def run_homog(args):
                              "its kernel is the pencil operator of the FP64 form (see the headline "
                              "line for the fine operator's roofline)")
     if not args.no_cpu:
-        from oracle.oracle import OracleLib
-        port = OracleLib("port")
+        port = oracle_port()
         nc = 2
         t0 = time.perf_counter()
         for c in cells[:nc]:
             port.homogenize(32, 32, 32, solid=np.ascontiguousarray(c).ravel(), tol=1e-8)
         tc = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": nc / tc, "unit": "cells/s", "cores": 1, "kind": "port",
+        line["cpu_baseline"] = {"value": nc / tc, "unit": "cells/s", "cores": port.threads(),
+                                "kind": "port",
                                 "sample": f"oracle homogenize (FP64 Jacobi-PCG, the harness's "
-                                          f"method), {nc} cells of the batch, one core"}
+                                          f"method), {nc} cells of the batch, one cell at a time"}
     print(json.dumps(line), flush=True)
 
 
@@ -633,9 +649,9 @@ def run_serve(args):
 def run_gatev2(args):
     """The Gate V2 benchmark problems end to end (300 projected OC iterations,
     beta 1 -> 32) in both forms, their gates, and the oracle's time for the same
-    run on one host core."""
+    run on the host cores."""
     import topopt_gb300 as tg
-    from oracle.oracle import CONTINUATION, GATE_V2, OracleLib, gate_v2_metrics, gate_v2_problem
+    from oracle.oracle import CONTINUATION, GATE_V2, gate_v2_metrics, gate_v2_problem
     from topopt_gb300.build import build
     build()
     out = {}
@@ -665,10 +681,11 @@ def run_gatev2(args):
                                                      for h in s["history"])),
                          "cg_iterations": int(sum(h["cg_iterations"] for h in s["history"]))}
         if not args.no_cpu:
+            port = oracle_port()
             t0 = time.perf_counter()
-            r = OracleLib("port").simp_optimize(o, volfrac=0.3, radius=2.5, change_tol=0.0,
-                                                cg_tol=1e-9, stages=CONTINUATION)
-            row["cpu_port"] = {"wall_s": time.perf_counter() - t0, "cores": 1,
+            r = port.simp_optimize(o, volfrac=0.3, radius=2.5, change_tol=0.0,
+                                   cg_tol=1e-9, stages=CONTINUATION)
+            row["cpu_port"] = {"wall_s": time.perf_counter() - t0, "cores": port.threads(),
                                "final_compliance": r["compliance"]}
         out[name] = row
     tot = sum(r["mixed"]["wall_s"] for r in out.values())
@@ -680,7 +697,8 @@ def run_gatev2(args):
             "runs": out}
     if not args.no_cpu:
         cpu = sum(r["cpu_port"]["wall_s"] for r in out.values())
-        line["cpu_baseline"] = {"value": len(out) / cpu, "unit": "runs/s", "cores": 1,
+        cores = max(r["cpu_port"]["cores"] for r in out.values())
+        line["cpu_baseline"] = {"value": len(out) / cpu, "unit": "runs/s", "cores": cores,
                                 "kind": "port", "sample": "both problems, full 300 iterations"}
     print(json.dumps(line), flush=True)
 

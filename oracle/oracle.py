@@ -228,6 +228,9 @@ class OracleLib:
     def set_threads(self, n):
         if self.kind == "reference":
             self.lib.ref_set_threads(int(n))
+        else:
+            self.lib.or_set_threads.argtypes = [C.c_int]
+            self.lib.or_set_threads(int(n))
 
     # ------------------------------------------------------------------- API
     def hex8_stiffness(self, E=1.0, nu=0.3, h=1.0):

@@ -32,6 +32,13 @@ int or_threads(void) {
   return 1;
 #endif
 }
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
 static int fail(int code, const char* msg) {
   snprintf(g_err, sizeof g_err, "%s", msg);
   return code;

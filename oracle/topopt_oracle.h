@@ -36,6 +36,10 @@ enum { OR_OK = 0, OR_EINVAL = 1, OR_ESINGULAR = 2, OR_ENONCONV = 3 };
 
 /* Host threads the oracle's parallel loops use (1 when built without OpenMP). */
 int or_threads(void);
+/* Sets the thread count of later parallel loops (n > 0; a no-op without
+ * OpenMP).  Launchers such as torchrun export OMP_NUM_THREADS=1; a timed CPU
+ * run sets the count it means to use. */
+void or_set_threads(int n);
 
 /* Last error message of the calling thread ("" when none). */
 const char* or_last_error(void);
