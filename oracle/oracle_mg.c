@@ -498,10 +498,22 @@ static void mf_v_cycle(mg_solver* S, const double* b, double* x) {
   for (size_t d = 0; d < n; ++d) x[d] += om * S->invdiag[d] * (b[d] - S->fr[d]);
 }
 
+/* Dot product in a fixed order: 64 contiguous blocks, each summed serially,
+ * then the block sums in block order.  The value does not depend on the thread
+ * count (an OpenMP reduction combines per-thread sums in no fixed order). */
 static double dotk(const mg_solver* S, const double* a, const double* b) {
+  enum { kBlocks = 64 };
+  double part[kBlocks];
+  const long long n = (long long)S->ndof;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < kBlocks; ++k) {
+    const long long lo = n * k / kBlocks, hi = n * (k + 1) / kBlocks;
+    double s = 0.0;
+    for (long long d = lo; d < hi; ++d) s += a[d] * b[d];
+    part[k] = s;
+  }
   double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-  for (long long d = 0; d < (long long)S->ndof; ++d) s += a[d] * b[d];
+  for (int k = 0; k < kBlocks; ++k) s += part[k];
   return s;
 }
 

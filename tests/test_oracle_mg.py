@@ -62,3 +62,24 @@ def test_design_iterations_follow_the_oracle_trajectory(port):
     assert np.abs(r["compliance"] - ref["hist_c"]).max() <= 1e-8 * ref["hist_c"][0]
     assert np.abs(r["x"] - ref["design"]).max() <= 1e-6
     assert (r["cg"] > 0).all() and r["seconds"].shape == (3, 5)
+
+
+def test_mg_independent_of_thread_count(port):
+    """The restatement gives the same bits on 1 and 3 threads: its element apply
+    runs colour by colour, every other parallel loop writes one output each,
+    and its dot products sum fixed blocks in a fixed order."""
+    o = cantilever(24, 12, 10)
+    f = smooth_modulus(24, 12, 10)
+    old = port.threads()
+    try:
+        out = []
+        for t in (1, 3):
+            port.set_threads(t)
+            u, it, res, lev = port.mg_solve(o, f, tol=1e-10)
+            r = port.design_iterations_mg(o, np.full(o.nv, 0.3), 2, cg_tol=1e-8)
+            out.append((u, it, res, r["x"], r["compliance"], r["cg"]))
+    finally:
+        port.set_threads(old)
+    (u1, i1, r1, x1, c1, g1), (u3, i3, r3, x3, c3, g3) = out
+    assert i1 == i3 and r1 == r3 and np.array_equal(u1, u3)
+    assert np.array_equal(x1, x3) and np.array_equal(c1, c3) and np.array_equal(g1, g3)
