@@ -38,10 +38,8 @@ void mg_assemble_stencil(const MgDims& d, const T* Kel, const uint8_t* act, T* A
                          cudaStream_t s);
 void mg_to_float(const double* src, float* dst, int64_t n, cudaStream_t s);
 // One Chebyshev smoothing step (kCheb): the direction vector it updates in
-// place (the level's precision), lambda_max of D^-1 A on the device, the
-// interval ratio lmax / lmin and the step index within the polynomial.
-// One Chebyshev smoothing step: the direction buffer and the level's
-// coefficient table (mg_cheb_table).
+// place (the level's precision), the level's coefficient table (mg_cheb_table)
+// and the step index within the polynomial.
 struct ChebStep {
   void* dir_ = nullptr;
   const float* coef = nullptr;
