@@ -640,12 +640,15 @@ int tg_server_submit(tg_server* server, const tg_grid* grid, const tg_simp_param
                      const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
                      int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
                      int64_t* ticket_out);
-/* Blocks until the job is done; returns its status and releases the ticket.
- * design_out / phys_out (voxels) may be NULL. */
+/* Blocks until the job is done; returns its status and releases the ticket
+ * (a later wait on it returns TG_EINVAL).  design_out / phys_out (voxels) may
+ * be NULL. */
 int tg_server_wait(tg_server* server, int64_t ticket, tg_server_result* out,
                    double* design_out, double* phys_out);
 int tg_server_stats(tg_server* server, tg_server_counters* out);
-/* Drops queued jobs, waits for the admitted ones, frees the server. */
+/* Drops queued jobs (their waiters return TG_EINVAL), waits for the admitted
+ * ones, frees the server.  No other call on the server may be in flight or
+ * follow. */
 void tg_server_destroy(tg_server* server);
 
 /* ---- resident jobs: state stays on the device between design iterations ---- */

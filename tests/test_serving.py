@@ -20,6 +20,32 @@ def test_workload_generators():
         assert 24 ** 3 * 0.5 <= p.nv <= 192 * 96 * 96 * 1.5
 
 
+def test_server_host_logic(tg):
+    """Admission, rejection, tickets and shutdown are host logic and run without
+    a device.  Without one, the admitted job ends with the device error (there
+    is no CPU fallback); with one, it completes."""
+    pb, prm, opt = workloads.design(5, iterations=1, sizes=(16, 8, 8))
+    est = tg.job_estimate_bytes(pb, opt)
+    srv = tg.Server(hbm_budget_bytes=est, max_active=2)
+    with pytest.raises(MemoryError, match="budget"):
+        srv.submit(*workloads.design(6, iterations=1, sizes=(32, 16, 16)))
+    t = srv.submit(pb, prm, opt)
+    try:
+        assert srv.wait(t, fields=False)["iterations"] == 1
+    except tg.DeviceError:
+        pass
+    lib = tg.lib()
+    assert lib.tg_server_wait(srv._h, t, None, None, None) == 1  # released: TG_EINVAL
+    assert b"unknown ticket" in lib.tg_last_error()
+    st = srv.stats()
+    assert (st["submitted"], st["rejected"], st["admitted"], st["completed"]) == (2, 1, 1, 1)
+    assert st["active"] == 0 and st["queued"] == 0 and st["bytes_in_use"] == 0
+    assert st["peak_bytes"] == est
+    srv.close()
+    with pytest.raises(ValueError, match="max_active"):
+        tg.Server(hbm_budget_bytes=est, max_active=0)
+
+
 @pytest.mark.gpu
 def test_same_alone_and_in_the_mix(tg):
     jobs = [workloads.design(s, precision=p, iterations=6, sizes=sz)

@@ -136,35 +136,11 @@ struct tg_server {
   }
 };
 
-extern "C" {
-
-int tg_server_create(const tg_server_config* cfg, tg_server** out) {
-  if (!cfg || !out) {
-    tg::set_last_error("tg_server_create: cfg and out must be non-null");
-    return TG_EINVAL;
-  }
-  if (cfg->hbm_budget_bytes <= 0 || cfg->max_active < 1) {
-    tg::set_last_error("tg_server_create: hbm_budget_bytes must be > 0 and max_active >= 1");
-    return TG_EINVAL;
-  }
-  auto s = std::make_unique<tg_server>();
-  s->cfg = *cfg;
-  tg_server* sp = s.get();
-  for (int i = 0; i < cfg->max_active; ++i) s->workers.emplace_back([sp] { sp->worker(); });
-  *out = s.release();
-  return TG_OK;
-}
-
-int tg_server_submit(tg_server* s, const tg_grid* grid, const tg_simp_params* params,
-                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
-                     int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
-                     int64_t* ticket_out) {
-  if (!s || !grid || !params || !options || !ticket_out || nbc < 0 || nloads < 0 ||
-      (nbc > 0 && !bcs) || (nloads > 0 && !loads) || grid->nx < 1 || grid->ny < 1 ||
-      grid->nz < 1) {
-    tg::set_last_error("tg_server_submit: invalid arguments");
-    return TG_EINVAL;
-  }
+// tg_server_submit after its argument checks: copies the problem and queues it.
+static int submit_request(tg_server* s, const tg_grid* grid, const tg_simp_params* params,
+                          const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                          int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                          int64_t* ticket_out) {
   auto r = std::make_shared<Request>();
   r->grid = *grid;
   const int64_t nv = int64_t(grid->nx) * grid->ny * grid->nz;
@@ -203,6 +179,59 @@ int tg_server_submit(tg_server* s, const tg_grid* grid, const tg_simp_params* pa
   return TG_OK;
 }
 
+extern "C" {
+
+int tg_server_create(const tg_server_config* cfg, tg_server** out) {
+  if (!cfg || !out) {
+    tg::set_last_error("tg_server_create: cfg and out must be non-null");
+    return TG_EINVAL;
+  }
+  if (cfg->hbm_budget_bytes <= 0 || cfg->max_active < 1) {
+    tg::set_last_error("tg_server_create: hbm_budget_bytes must be > 0 and max_active >= 1");
+    return TG_EINVAL;
+  }
+  std::unique_ptr<tg_server> s;
+  try {
+    s = std::make_unique<tg_server>();
+    s->cfg = *cfg;
+    tg_server* sp = s.get();
+    for (int i = 0; i < cfg->max_active; ++i) s->workers.emplace_back([sp] { sp->worker(); });
+  } catch (const std::exception& e) {
+    // The server or a worker thread could not be created: stop and join the
+    // workers already running, so that no joinable thread is destroyed.
+    if (s) {
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+      }
+      s->cv_work.notify_all();
+      for (std::thread& t : s->workers) t.join();
+    }
+    tg::set_last_error(std::string("tg_server_create: ") + e.what());
+    return TG_ENOMEM;
+  }
+  *out = s.release();
+  return TG_OK;
+}
+
+int tg_server_submit(tg_server* s, const tg_grid* grid, const tg_simp_params* params,
+                     const tg_dirichlet_bc* bcs, int32_t nbc, const tg_nodal_load* loads,
+                     int32_t nloads, const tg_simp_options* options, const uint8_t* mask,
+                     int64_t* ticket_out) {
+  if (!s || !grid || !params || !options || !ticket_out || nbc < 0 || nloads < 0 ||
+      (nbc > 0 && !bcs) || (nloads > 0 && !loads) || grid->nx < 1 || grid->ny < 1 ||
+      grid->nz < 1) {
+    tg::set_last_error("tg_server_submit: invalid arguments");
+    return TG_EINVAL;
+  }
+  try {
+    return submit_request(s, grid, params, bcs, nbc, loads, nloads, options, mask, ticket_out);
+  } catch (const std::exception& e) {  // the copies of the problem could not be made
+    tg::set_last_error(std::string("tg_server_submit: ") + e.what());
+    return TG_ENOMEM;
+  }
+}
+
 int tg_server_wait(tg_server* s, int64_t ticket, tg_server_result* out, double* design_out,
                    double* phys_out) {
   if (!s) {
@@ -219,7 +248,7 @@ int tg_server_wait(tg_server* s, int64_t ticket, tg_server_result* out, double* 
     }
     r = it->second;
     s->cv_done.wait(lk, [&] { return r->done; });
-    s->tickets.erase(it);
+    s->tickets.erase(ticket);  // by key: another waiter on the same ticket may have erased it
   }
   if (out) {
     std::memset(out, 0, sizeof *out);
