@@ -50,6 +50,16 @@ def test_design_file_bytes_match_reference(tg, golden, tmp_path):
     (tmp_path / "v2.bin").write_bytes(bytes(raw))
     with pytest.raises(ValueError, match="version"):
         tg.read_design_file(tmp_path / "v2.bin")
+    # A header whose voxel count the file cannot hold is refused before any
+    # allocation; so is a file cut short inside a variant.
+    raw = bytearray(p.read_bytes())
+    raw[4:16] = np.array([1 << 20] * 3, "<i4").tobytes()
+    (tmp_path / "huge.bin").write_bytes(bytes(raw))
+    with pytest.raises(ValueError, match="truncated"):
+        tg.read_design_file(tmp_path / "huge.bin")
+    (tmp_path / "cut.bin").write_bytes(p.read_bytes()[:-100])
+    with pytest.raises(ValueError, match="truncated"):
+        tg.read_design_file(tmp_path / "cut.bin")
 
 
 def test_fields_file_bytes_match_reference(tg, golden, tmp_path):

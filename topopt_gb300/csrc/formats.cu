@@ -218,7 +218,13 @@ int tg_read_design_file(const char* path, tg_grid_frame* frame, int32_t* count,
     r.skip(4);
     if (g.nx <= 0 || g.ny <= 0 || g.nz <= 0 || nblocks < 0)
       throw tg::Error(TG_EINVAL, "design.bin: nonsensical header");
-    const int64_t nv = int64_t(g.nx) * g.ny * g.nz;
+    // Every variant stores one density per voxel: a header whose voxel count
+    // does not fit in the file is refused before anything is allocated.
+    const double nvd = double(g.nx) * double(g.ny) * double(g.nz);
+    if (nblocks > 0 && nvd * 8.0 > double(bytes.size()))
+      throw tg::Error(TG_EINVAL, "design.bin: truncated container (the header's voxel count " +
+                                     std::to_string(nvd) + " exceeds the file)");
+    const int64_t nv = nblocks > 0 ? int64_t(nvd) : 0;
     std::vector<double> dens(static_cast<size_t>(nv));
     for (int32_t i = 0; i < nblocks; ++i) {
       tg_design_variant v{};
