@@ -89,3 +89,37 @@ def test_autotuned_schedule_is_recorded(tg):
     r = job.step()
     assert r["compliance"] > 0.0
     job.close()
+
+
+def test_concurrent_jobs_share_one_measured_schedule(tg):
+    """Two mixed jobs of one new grid created at the same time: one measures the
+    FP32 schedules while the other waits, both then run the published schedule,
+    and their results are identical."""
+    import threading
+    nx, ny, nz = 128, 96, 96
+    o = cantilever(nx, ny, nz)
+    pb = tg.Problem(nx, ny, nz, 1.0, None, list(zip(o.bc_node, o.bc_comp, o.bc_val)),
+                    list(zip(o.ld_node, o.ld_comp, o.ld_val)))
+    opts = tg.SimpOptions(volume_fraction=0.3, filter_radius=1.5, change_tol=0.0,
+                          max_iterations=2, solve=tg.SolveOptions(precision=tg.PREC_MIXED))
+    out, errs = [None, None], []
+
+    def run(i):
+        try:
+            job = tg.SimpJob(pb, tg.SimpParams(), opts)
+            r = job.step()
+            x, _ = job.read()
+            job.close()
+            out[i] = (r["compliance"], x)
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errs, errs
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+    assert tg.fp32_schedule(nx, ny, nz)[0] in (tg.SCHED_PENCIL, tg.SCHED_COLUMN)

@@ -181,7 +181,6 @@ bool fine_schedule_valid(const FineSchedule& s);
 // set, else the table entry for g's dimensions (tune.cu), else the default.
 FineSchedule fine_schedule_for(const Grid& g, int mode = kApply);
 void set_fine_schedule_override(const FineSchedule* s);  // null clears
-void set_fine_schedule(const Grid& g, const FineSchedule& s, int mode);
 bool fine_schedule_known(const Grid& g);  // in the table, or an override is set
 // The FP32 operator under an explicit schedule.
 void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const ModalConsts& c,
@@ -190,7 +189,8 @@ void launch_fine_op_sched(const FineSchedule& fs, int mode, const Grid& g, const
                           int* nblocks_out, cudaStream_t s, const uint8_t* kn);
 // Times every candidate schedule of the FP32 operator on the given buffers
 // (CUDA events on s) for the apply and, with b and invdiag, the residual and
-// smoothing modes; stores the fastest per mode in the table for g and returns
+// smoothing modes; publishes the fastest per mode in the table for g (one sweep
+// at a time; a grid already in the table is not measured again) and returns
 // the apply's.
 FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const float* ef,
                                     const uint8_t* kept, const uint8_t* kn, const float* x,

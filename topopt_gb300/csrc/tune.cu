@@ -22,6 +22,22 @@ std::mutex g_sched_mu;
 // (nx, ny, nz, mode): the apply, residual and smoothing modes read different
 // vectors and are tuned separately.
 std::map<std::tuple<int, int, int, int>, FineSchedule> g_sched;
+// One measured sweep at a time.  A grid's entries are published together once
+// its sweep ends and are never replaced by a later sweep, so concurrent jobs of
+// the same grid (which wait here while it is measured) all run one schedule.
+std::mutex g_tune_mu;
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EventPair() {
+    TG_CUDA(cudaEventCreate(&a));
+    TG_CUDA(cudaEventCreate(&b));
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
 bool g_have_override = false;
 FineSchedule g_override;
 
@@ -41,11 +57,6 @@ void set_fine_schedule_override(const FineSchedule* s) {
   if (s) g_override = *s;
 }
 
-void set_fine_schedule(const Grid& g, const FineSchedule& s, int mode) {
-  std::lock_guard<std::mutex> lk(g_sched_mu);
-  g_sched[std::make_tuple(g.nx, g.ny, g.nz, mode)] = s;
-}
-
 bool fine_schedule_known(const Grid& g) {
   std::lock_guard<std::mutex> lk(g_sched_mu);
   return g_have_override || g_sched.count(std::make_tuple(g.nx, g.ny, g.nz, int(kApply))) != 0;
@@ -57,12 +68,15 @@ bool fine_schedule_known(const Grid& g) {
 // mixed solve runs them: the apply with the kept mask and the p.Ap partials,
 // the residual, and the smoothing sweep with its b.y partials (b, invdiag:
 // any finite vectors).  The fastest per mode goes into the table for g's
-// dimensions.  Results of every candidate agree to FP32 rounding, so the
-// choice changes timing only.  Returns the apply's choice.
+// dimensions, unless another sweep of the same grid published first.  Results
+// of every candidate agree to FP32 rounding, so the choice changes timing only.
+// Returns the apply's schedule in the table.
 FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const float* ef,
                                     const uint8_t* kept, const uint8_t* kn, const float* x,
                                     float* y, double* part, cudaStream_t s, const float* b,
                                     const float* invdiag, int reps) {
+  std::lock_guard<std::mutex> tune_lock(g_tune_mu);
+  if (fine_schedule_known(g)) return fine_schedule_for(g, kApply);
   std::vector<FineSchedule> cands;
   FineSchedule pencil;
   pencil.kind = FineSchedule::kPencil;
@@ -81,10 +95,9 @@ FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const 
       c.kz = kz;
       cands.push_back(c);
     }
-  cudaEvent_t ea, eb;
-  TG_CUDA(cudaEventCreate(&ea));
-  TG_CUDA(cudaEventCreate(&eb));
-  FineSchedule best_apply = default_fine_schedule(g);
+  EventPair ev;
+  const cudaEvent_t ea = ev.a, eb = ev.b;
+  std::vector<std::pair<int, FineSchedule>> chosen;
   for (int mode : {int(kApply), int(kResidual), int(kSmooth)}) {
     if (mode != kApply && (b == nullptr || invdiag == nullptr)) continue;
     const float* bb = mode == kApply ? nullptr : b;
@@ -106,12 +119,14 @@ FineSchedule autotune_fine_schedule(const Grid& g, const ModalConsts& mc, const 
         best = c;
       }
     }
-    set_fine_schedule(g, best, mode);
-    if (mode == kApply) best_apply = best;
+    chosen.emplace_back(mode, best);
   }
-  cudaEventDestroy(ea);
-  cudaEventDestroy(eb);
-  return best_apply;
+  {
+    std::lock_guard<std::mutex> lk(g_sched_mu);
+    for (const auto& [mode, sch] : chosen)
+      g_sched.emplace(std::make_tuple(g.nx, g.ny, g.nz, mode), sch);
+  }
+  return fine_schedule_for(g, kApply);
 }
 
 namespace {
