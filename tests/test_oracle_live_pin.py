@@ -1,8 +1,8 @@
 """The oracle's C restatement against the reference's own compiled code, run
 live on seeded problems beyond the golden vectors: odd grids, void pockets,
 prescribed non-zero displacements, point loads at random end-face nodes, graded
-moduli, three filter radii, and short plain and masked optimisation runs.
-Every comparison is bit for bit.
+moduli, three filter radii, and short plain, masked, MMA and Heaviside-projected
+optimisation runs.  Every comparison is bit for bit.
 
 CPU only.  Skipped where the reference build (oracle/_ref, compiled from the
 reference tree by oracle/build_ref.sh) is absent; the golden vectors carry the
@@ -109,4 +109,26 @@ def test_short_runs(port, ref, seed):
     b = ref.simp_optimize_masked(pt, mask, volfrac=0.35, radius=1.5, move=0.2, max_it=5,
                                  change_tol=0.0, cg_tol=1e-10)
     for k in ("hist_c", "hist_change", "hist_vf", "design", "phys"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("seed", SEEDS[3:])
+def test_short_mma_and_projected_runs(port, ref, seed):
+    """Eight MMA design iterations and a two-stage Heaviside-projected run
+    (beta 1 then 2): identical trajectories."""
+    pb, rng = random_problem(seed)
+    a = port.simp_optimize_mma(pb, volfrac=0.35, radius=1.5, move=0.2, max_it=8, change_tol=0.0,
+                               cg_tol=1e-10)
+    b = ref.simp_optimize_mma(pb, volfrac=0.35, radius=1.5, move=0.2, max_it=8, change_tol=0.0,
+                              cg_tol=1e-10)
+    assert a["iterations"] == b["iterations"]
+    for k in ("hist_c", "hist_change", "hist_vf", "design", "phys"):
+        assert np.array_equal(a[k], b[k]), k
+    stages = [(1.0, 0.2, 3), (2.0, 0.2, 3)]
+    a = port.simp_optimize(pb, volfrac=0.35, radius=2.0, change_tol=0.0, cg_tol=1e-10,
+                           stages=stages)
+    b = ref.simp_optimize(pb, volfrac=0.35, radius=2.0, change_tol=0.0, cg_tol=1e-10,
+                          stages=stages)
+    assert a["iterations"] == b["iterations"] == 6
+    for k in ("hist_c", "hist_vf", "design", "phys"):
         assert np.array_equal(a[k], b[k]), k
