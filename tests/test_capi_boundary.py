@@ -134,3 +134,17 @@ def test_load_path_host_matches_oracle(tg, port):
         seen.add(want)
     assert seen == {True, False}
     assert tg.load_path_connected(tg.Problem(nx, ny, nz), np.zeros(tags.size))  # vacuous
+
+
+def test_integration_lists_every_entry_point():
+    """INTEGRATION.md's table names every entry point the header declares,
+    each against the reference interface it replaces (or "no counterpart")."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    listed = set()
+    for cell in re.findall(r"`(tg_[\w/]+)`", doc):
+        head, *rest = cell.split("/")
+        listed.add(head)
+        stem = head.rsplit("_", 1)[0]  # tg_job_create/step -> tg_job_step
+        listed.update(f"{stem}_{r}" for r in rest)
+    missing = [n for n in declared_functions() if n not in listed]
+    assert not missing, missing
